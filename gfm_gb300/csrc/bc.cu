@@ -1,0 +1,491 @@
+// bc.cu -- boundary extrapolation, staggered interpolation, exit mass
+// balance, pressure re-reference, emission-only radiation, layout conversion
+// and the deterministic finish of FP64 reductions.
+#include "state.cuh"
+
+namespace gfm {
+
+#define A(arr, I, J, K) (arr)[pidx(g, (I), (J), (K))]
+
+constexpr int kBlk = 256;
+inline int gridn(long long n) {
+    long long b = (n + kBlk - 1) / kBlk;
+    if (b < 1) b = 1;
+    if (b > kRedBlocks) b = kRedBlocks;
+    return (int)b;
+}
+
+template <typename R> __device__ __forceinline__ R rmax2(R a, R b) { return a > b ? a : b; }
+template <typename R> __device__ __forceinline__ R rmin2(R a, R b) { return a < b ? a : b; }
+
+template <typename R>
+__device__ __forceinline__ R area_cc(const GeoT<R>& g, int I, int J, int K, int ix) {
+    if (IBC(g, I, J, K) == 1) return R(0);
+    if (ix == 1) return g.DR[J] * g.RS[J] * g.DZ[K];
+    if (ix == 2) return g.DX[I] * g.DZ[K];
+    return g.DX[I] * g.DR[J] * g.RS[J];
+}
+
+// dnst_calc at one position of the split arrays (calls CONC, Prop.f90:187-198)
+template <typename R>
+__device__ void dnst_at(const Ctx<R>& c, long long o) {
+    R y[9];
+    for (int l = 0; l < 9; ++l) y[l] = l == 7 ? R(0) : c.GF[l][o];
+    R rho = dnst_calc<R>(y, 1, c.P[o], c.T[o], R(c.p.wt0));
+    c.GF[kYF][o] = y[kYF]; c.GF[kYO2][o] = y[kYO2]; c.GF[kYCO2][o] = y[kYCO2];
+    c.GF[kYN2][o] = y[kYN2]; c.GF[kYH2O][o] = y[kYH2O];
+    c.DNST[o] = rho;
+}
+
+// ---------------------------------------------------------------------------
+// EXTR(1) (Extr.f90:31-250) from host-built records
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_extr_io(Ctx<R> c) {
+    __shared__ double sh[32];
+    const GeoT<R>& g = c.g;
+    double gfin0 = 0.0, qex = 0.0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_io; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_io[t];
+        const long long o = pidx(g, e.I, e.J, e.K), o1 = pidx(g, e.I1, e.J1, e.K1), o2 = pidx(g, e.I2, e.J2, e.K2);
+        const R F1 = R(e.F1), F2 = R(e.F2);
+        c.GF[kEps][o] = c.GF[kEps][o1];
+        c.P[o] = c.P[o1] * F1 + c.P[o2] * F2;
+        if (e.kind == 2) {
+            // THER at the inlet keeps TMU and is overwritten in GAMA: only its eps clip survives
+            c.GF[kEps][o] = rmax2(c.GF[kEps][o], R(1.0e-12));
+            c.GAMA[o] = c.GAMA[o1];
+            R area = area_cc(g, e.I, e.J, e.K, e.IX);
+            R g0 = c.THETA[o] * c.DNST[o] * c.UG[e.IX - 1][o] * area;
+            gfin0 += fabs((double)g0);
+            continue;
+        }
+        c.TMU[o] = c.TMU[o1];
+        c.GAMA[o] = c.GAMA[o1];
+        for (int L = 1; L <= 7; ++L) {
+            if (L == kEps + 1) continue;
+            R g0 = c.GF[L - 1][o1] * F1 + c.GF[L - 1][o2] * F2;
+            if (L == kK + 1) c.GF[L - 1][o] = rmax2(g0, R(1.0e-6));
+            else if (L == kH + 1) c.GF[L - 1][o] = g0;
+            else c.GF[L - 1][o] = rmax2(g0, R(0));
+        }
+        {
+            double y[9];
+            for (int l = 0; l < 9; ++l) y[l] = l == 7 ? 0.0 : (double)c.GF[l][o];
+            c.T[o] = R(enth_to_t(*c.nist, y, 1, y[kH], (double)c.T[o], c.p.t0, c.p.h_0));
+        }
+        dnst_at(c, o);
+        R area = area_cc(g, e.I, e.J, e.K, e.IX);
+        double g0 = fabs((double)c.UG[e.IX - 1][o]) * c.p.ug0 * (double)area;
+        g0 = g0 * (double)c.THETA[o] * (double)c.DNST[o] * c.p.dnst0;
+        qex += (double)c.GF[kH][o] * c.p.h_0 * g0;
+        if (e.kind == 3) {
+            // SBC4 copy onto the exit face (Sbc.f90:506-522)
+            const long long o3 = pidx(g, e.I3, e.J3, e.K3);
+            c.P[o3] = c.P[o]; c.T[o3] = c.T[o];
+            for (int l = 0; l < 9; ++l) if (l != 7) c.GF[l][o3] = c.GF[l][o];
+            c.DNST[o3] = c.DNST[o]; c.THETA[o3] = c.THETA[o]; c.TMU[o3] = c.TMU[o]; c.GAMA[o3] = c.GAMA[o];
+        }
+    }
+    double a = block_sum(gfin0, sh), b = block_sum(qex, sh);
+    if (threadIdx.x == 0) { c.partials[8 * kRedBlocks + blockIdx.x] = a; c.partials[9 * kRedBlocks + blockIdx.x] = b; }
+}
+
+template <typename R>
+__device__ void extr_wall_one(const Ctx<R>& c, const ExtrRec& e) {
+    const GeoT<R>& g = c.g;
+    const long long o = pidx(g, e.I, e.J, e.K), o1 = pidx(g, e.I1, e.J1, e.K1), o2 = pidx(g, e.I2, e.J2, e.K2);
+    c.P[o] = c.P[o1] * R(e.F1) + c.P[o2] * R(e.F2);
+    c.TMU[o] = c.TMU[o2];
+    c.GAMA[o] = c.GAMA[o2];
+    for (int L = 1; L <= 7; ++L) c.GF[L - 1][o] = c.GF[L - 1][o1];
+    c.T[o] = c.T[o1];   // walls adiabatic until a first full radiation call
+    dnst_at(c, o);
+}
+
+// wall cells whose six axis neighbours are walls read the cell above them
+// (EXT1 falls through, Extr.f90:626-660): one thread per (I,J) column, K
+// ascending, as the Fortran loop visits them
+template <typename R>
+__global__ void k_extr_ft(Ctx<R> c) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_ft_cols; t += gridDim.x * blockDim.x)
+        for (int q = c.ft_col_start[t]; q < c.ft_col_start[t + 1]; ++q) extr_wall_one(c, c.extr_ft[q]);
+}
+template <typename R>
+__global__ void k_extr_wall(Ctx<R> c) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_wall; t += gridDim.x * blockDim.x)
+        extr_wall_one(c, c.extr_wall[t]);
+}
+
+// ---------------------------------------------------------------------------
+// EXTRV (Extr.f90:358-567): exit faces of direction IU.  Slots: 10 GFEX,
+// 11 T*|G0|, 12 T*area, 13 area.
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ __forceinline__ R bound_v(R f, const Prm& p) {
+    f = rmin2(f, R(p.u_mx));
+    f = rmax2(f, R(p.u_mn));
+    if (fabs(f) < R(1.0e-12)) f = R(0);
+    return f;
+}
+template <typename R>
+__global__ void k_extrv(Ctx<R> c, int mex, int first, int count) {
+    __shared__ double sh[32];
+    const GeoT<R>& g = c.g;
+    double gfex = 0, tm = 0, ta = 0, ar = 0;
+    const R factor = R(c.scal[S_FACTOR]);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < count; t += gridDim.x * blockDim.x) {
+        const ExtrvRec& e = c.extrv[first + t];
+        const int IU = e.IU;
+        R* u = c.UG[IU - 1];
+        const long long o = pidx(g, e.I, e.J, e.K);
+        if (e.mode == 1) { u[o] = A(u, e.Is, e.Js, e.Ks); continue; }
+        if (e.mode == 2) continue;
+        const int M = e.m;
+        int I1 = e.I, J1 = e.J, K1 = e.K, I0 = e.I, J0 = e.J, K0 = e.K;
+        if (IU == 1) { I1 = e.I + 2 * M; I0 = e.I - M; }
+        else if (IU == 2) { J1 = e.J + 2 * M; J0 = e.J - M; }
+        else { K1 = e.K + 2 * M; K0 = e.K - M; }
+        const long long o1 = pidx(g, I1, J1, K1);
+        if (u[o1] * R(M) > R(0)) u[o1] = R(0);
+        R area = area_cc(g, e.I, e.J, e.K, IU);
+        R g0 = c.THETA[o1] * c.DNST[o1] * u[o1] * area;
+        if (mex == 0) {
+            gfex += fabs((double)g0);
+            tm += (double)c.T[o] * fabs((double)g0);
+            ta += (double)c.T[o] * (double)area;
+            ar += (double)area;
+            continue;
+        }
+        ar += (double)area;
+        u[o1] = u[o1] * factor;
+        if (IU == 3) continue;   // GOTO 160 (Extr.f90:529)
+        g0 = g0 * factor;
+        R v = bound_v(g0 / (c.THETA[o] * c.DNST[o] * area), c.p);
+        u[o] = v;
+        A(u, I0, J0, K0) = v;
+    }
+    double a = block_sum(gfex, sh), b = block_sum(tm, sh), d = block_sum(ta, sh), e2 = block_sum(ar, sh);
+    if (threadIdx.x == 0) {
+        c.partials[10 * kRedBlocks + blockIdx.x] = a;
+        c.partials[11 * kRedBlocks + blockIdx.x] = b;
+        c.partials[12 * kRedBlocks + blockIdx.x] = d;
+        c.partials[13 * kRedBlocks + blockIdx.x] = e2;
+    }
+}
+
+// GFEX/Tmean_ex finish of EXTRV(0), GFIN of FLX1D and the exit FACTOR
+// (Extr.f90:553-565, Flx1d.f90:75-77, Gslv3v.f90:213-231).  One thread.
+__global__ void k_factor(double* scal, double gmfr, double t0, double f_mx, double f_mn, int itr_gas) {
+    if (threadIdx.x != 0) return;
+    double gfex = scal[S_GFEX] * gmfr;
+    scal[S_GFEX] = gfex;
+    if (gfex < 1.0e-16) scal[S_TMEAN_EX] = scal[S_TAREA_MEAN] * t0 / scal[S_AREA_EX];
+    else scal[S_TMEAN_EX] = scal[S_TMEAN_EX] * t0 * gmfr / gfex;
+    scal[S_GFIN] = scal[S_GFIN0] * gmfr;
+    if (itr_gas > 10) {
+        if (gfex < 1.0e-20) { scal[S_FACTOR] = 1.0; scal[S_FADJ] = 0.0; }
+        else {
+            double f = scal[S_GFIN] / gfex;
+            if (f > f_mx) { f = f_mx; scal[S_FADJ] = 0.0; }
+            else if (f < f_mn) { f = f_mn; scal[S_FADJ] = 0.0; }
+            scal[S_FACTOR] = f;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// INTPV (Intp.f90:84-139, 230-272): stage a/b/c of component IU
+// ---------------------------------------------------------------------------
+template <typename R>
+__device__ R intp1(const GeoT<R>& g, int I, int J, int K, int ix) {
+    if (ix == 3) return (g.DZ[K] <= R(0) || K > g.LP) ? R(0) : (g.Z[K] - g.Z[K - 1]) / g.DZ[K];
+    if (ix == 2) return (g.DR[J] <= R(0) || J > g.NP) ? R(0) : (g.Rr[J] - g.Rr[J - 1]) / g.DR[J];
+    return (g.DX[I] <= R(0) || I > g.MP) ? R(0) : (g.X[I] - g.X[I - 1]) / g.DX[I];
+}
+
+template <typename R>
+__global__ void k_intpv(Ctx<R> c, int IU, int stage, int m0, int m1, int mstep, int n0, int n1, int nstep, int l0, int l1,
+                        int lstep, int IX) {
+    const GeoT<R>& g = c.g;
+    const int nm = (m1 - m0) / mstep + 1, nn = (n1 - n0) / nstep + 1, nl = (l1 - l0) / lstep + 1;
+    if (m1 < m0 || n1 < n0 || l1 < l0) return;
+    const long long tot = (long long)nm * nn * nl;
+    R* u = c.UG[IU - 1];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        // fastest-varying index is the one mapping to I
+        int a = (int)(t % nm), b = (int)((t / nm) % nn), d = (int)(t / ((long long)nm * nn));
+        int M, N, L;
+        if (IU == 1) { M = m0 + mstep * a; N = n0 + nstep * b; L = l0 + lstep * d; }
+        else if (IU == 2) { L = l0 + lstep * (t % nl); long long r = t / nl; M = m0 + mstep * (int)(r % nm); N = n0 + nstep * (int)(r / nm); }
+        else { N = n0 + nstep * (int)(t % nn); long long r = t / nn; L = l0 + lstep * (int)(r % nl); M = m0 + mstep * (int)(r / nl); }
+        int I, J, K;
+        if (IU == 1) { I = M; J = N; K = L; } else if (IU == 2) { J = M; K = N; I = L; } else { K = M; I = N; J = L; }
+        int b0 = IBC(g, I, J, K);
+        if (b0 >= 1 && b0 != 4) continue;
+        R f1 = intp1(g, I, J, K, IX), f2 = R(1) - f1;
+        R v;
+        if (IX == 1) {
+            v = A(u, I + 1, J, K) * f1 + A(u, I - 1, J, K) * f2;
+        } else if (IX == 2) {
+            if (IBC(g, I, J + 1, K) == 2 && b0 == 0) { f1 = R(0); f2 = R(1); }
+            else if (IBC(g, I, J - 1, K) == 2 && b0 == 0) { f1 = R(1); f2 = R(0); }
+            v = A(u, I, J + 1, K) * f1 + A(u, I, J - 1, K) * f2;
+        } else {
+            if (IBC(g, I, J, K + 1) == 2 && b0 == 0) { f1 = R(0); f2 = R(1); }
+            else if (IBC(g, I, J, K - 1) == 2 && b0 == 0) { f1 = R(1); f2 = R(0); }
+            v = A(u, I, J, K + 1) * f1 + A(u, I, J, K - 1) * f2;
+        }
+        A(u, I, J, K) = bound_v(v, c.p);
+        (void)stage;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// INTP (Intp.f90:32-72, 145-206) with the carried-F1 code of each position
+// (0 skip, 1 coordinate weight, 2 weight forced to 1, 3 weight forced to 0)
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_intp(Ctx<R> c, int stage) {
+    const GeoT<R>& g = c.g;
+    // stage 1: I even, K odd, J even; stage 2: I even, J odd, K all; stage 3: I odd, J all, K all
+    int i0, i1, j0, j1, js, k0, k1, ks;
+    if (stage == 1) { i0 = 2; i1 = g.MP; j0 = 2; j1 = g.NP; js = 2; k0 = 3; k1 = g.LPM1; ks = 2; }
+    else if (stage == 2) { i0 = 2; i1 = g.MP; j0 = 3; j1 = g.NPM1; js = 2; k0 = 2; k1 = g.LP; ks = 1; }
+    else { i0 = 3; i1 = g.MPM1; j0 = 2; j1 = g.NP; js = 1; k0 = 2; k1 = g.LP; ks = 1; }
+    const int ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / js + 1, nk = (k1 - k0) / ks + 1;
+    const long long tot = (long long)ni * nj * nk;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        int I = i0 + 2 * (int)(t % ni);
+        long long r = t / ni;
+        int J = j0 + js * (int)(r % nj), K = k0 + ks * (int)(r / nj);
+        const long long o = pidx(g, I, J, K);
+        int mode = c.intp_mode[o];
+        if (mode == 0) continue;
+        int I1, J1, K1, I2, J2, K2, ix;
+        if (stage == 1) { I1 = I; J1 = J; K1 = K + 1; I2 = I; J2 = J; K2 = K - 1; ix = 3; }
+        else if (stage == 2) { I1 = I; J1 = J + 1; K1 = K; I2 = I; J2 = J - 1; K2 = K; ix = 2; }
+        else { I1 = I + 1; J1 = J; K1 = K; I2 = I - 1; J2 = J; K2 = K; ix = 1; }
+        R f1 = mode == 1 ? intp1(g, I, J, K, ix) : (mode == 2 ? R(1) : R(0));
+        R f2 = R(1) - f1;
+        const long long a = pidx(g, I1, J1, K1), b = pidx(g, I2, J2, K2);
+        c.P[o] = f1 * c.P[a] + f2 * c.P[b];
+        c.T[o] = f1 * c.T[a] + f2 * c.T[b];
+        R y[9];
+        for (int l = 0; l < 9; ++l) y[l] = l == 7 ? R(0) : c.GF[l][o];
+        for (int L = 1; L <= 7; ++L) y[L - 1] = f1 * c.GF[L - 1][a] + f2 * c.GF[L - 1][b];
+        conc(y, 1);
+        c.TMU[o] = f1 * c.TMU[a] + f2 * c.TMU[b];
+        c.GAMA[o] = f1 * c.GAMA[a] + f2 * c.GAMA[b];
+        c.THETA[o] = f1 * c.THETA[a] + f2 * c.THETA[b];
+        R rho = dnst_calc<R>(y, 1, c.P[o], c.T[o], R(c.p.wt0));
+        for (int l = 0; l < 9; ++l) if (l != 7) c.GF[l][o] = y[l];
+        c.DNST[o] = rho;
+    }
+}
+
+// P at the reference inlet and the re-reference shift G0 (Gflow.f90:182-242)
+template <typename R>
+__global__ void k_pref(Ctx<R> c, int I1, int J1, int K1, int I2, int J2, int K2, double F1, double F2) {
+    const GeoT<R>& g = c.g;
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    A(c.P, c.i_ref, c.j_ref, c.k_ref) = A(c.P, I1, J1, K1) * R(F1) + A(c.P, I2, J2, K2) * R(F2);
+    c.scal[S_G0] = (double)(A(c.P, I1, J1, K1) - R(c.p_ref));
+}
+
+// ---------------------------------------------------------------------------
+// Emission-only radiation (rad_qe_only, Rad_emis.f90:411-466; RAD0 with gray
+// bands, Rad0.f90:112-157; DEBX Rad_fun.f90:122-140).  QE on every centre
+// (zero where the cell does not emit), then T=(T*T0)/T0 as the reference's
+// whole-array round trip does.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_rad_emission(Ctx<R> c) {
+    const GeoT<R>& g = c.g;
+    const int hx = g.HX, hy = g.HY, hz = g.HZ;
+    const long long tot = (long long)hx * hy * hz;
+    const double sgn = c.p.sig * c.p.ri * c.p.ri;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+        int ia = (int)(t % hx);
+        long long r = t / hx;
+        int ja = (int)(r % hy), ka = (int)(r / hy);
+        int I = 2 * ia, J = 2 * ja, K = 2 * ka;
+        if (I < 2 || J < 2 || K < 2) continue;
+        const long long o = pidx(g, I, J, K);
+        double qe = 0.0;
+        double T_rad = (double)c.T[o] * c.p.t0;
+        if (g.ib[o] <= 0 && T_rad >= 300.0) {
+            double dx = g.DX[I], dr = g.DR[J], dz = g.DZ[K];
+            double vol = dx * dr * (double)g.RS[J] * dz;
+            double sa = ((dx * dr) + (dr * dz) + (dx * dz)) * 2.0;
+            double opl = sa > 1.0e-16 ? 6.0 * vol / sa : 0.0;
+            if (sa > 1.0e-16 && opl > 1.0e-10) {
+                double deb[16], eb0 = 0.0;
+                for (int l = 1; l <= c.nwl - 1; ++l) {
+                    double x1 = (c.p.hck / c.p.ri / c.wl[l - 1]) / T_rad;
+                    double eb1 = rif3(x1);
+                    deb[l - 1] = eb1 - eb0;
+                    if (deb[l - 1] <= 1.0e-3) deb[l - 1] = 0.0; else eb0 = eb1;
+                }
+                deb[c.nwl - 1] = 1.0 - eb0;
+                double t2 = T_rad * T_rad;
+                double s = 0.0;
+                for (int l = 0; l < c.nwl; ++l) s = s + deb[l] * emf(c.akl0[l], opl);
+                qe = sa * sgn * (t2 * t2) * s;
+            }
+        }
+        c.QE[o] = R(qe);
+    }
+}
+template <typename R>
+__global__ void k_t_roundtrip(R* T, long long n, double t0) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        T[t] = R(((double)T[t] * t0) / t0);
+}
+
+// ---------------------------------------------------------------------------
+// layout conversion
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_to_split(GeoT<R> g, const double* __restrict__ src, R* __restrict__ dst) {
+    const long long n = (long long)g.MP * g.NP * g.LP;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int I = (int)(t % g.MP) + 1;
+        long long r = t / g.MP;
+        int J = (int)(r % g.NP) + 1, K = (int)(r / g.NP) + 1;
+        dst[pidx(g, I, J, K)] = R(src[t]);
+    }
+}
+template <typename R>
+__global__ void k_from_split(GeoT<R> g, const R* __restrict__ src, double* __restrict__ dst) {
+    const long long n = (long long)g.MP * g.NP * g.LP;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int I = (int)(t % g.MP) + 1;
+        long long r = t / g.MP;
+        int J = (int)(r % g.NP) + 1, K = (int)(r / g.NP) + 1;
+        dst[t] = (double)src[pidx(g, I, J, K)];
+    }
+}
+template <typename R>
+__global__ void k_cells_to_split(GeoT<R> g, const double* __restrict__ src, R* __restrict__ dst, int mz, int nz, int lz) {
+    const long long n = (long long)mz * nz * lz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int id = (int)(t % mz) + 1;
+        long long r = t / mz;
+        int jd = (int)(r % nz) + 1, kd = (int)(r / nz) + 1;
+        dst[pidx(g, 2 * id, 2 * jd, 2 * kd)] = R(src[t]);
+    }
+}
+template <typename R>
+__global__ void k_cells_from_split(GeoT<R> g, const R* __restrict__ src, double* __restrict__ dst, int mz, int nz, int lz) {
+    const long long n = (long long)mz * nz * lz;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int id = (int)(t % mz) + 1;
+        long long r = t / mz;
+        int jd = (int)(r % nz) + 1, kd = (int)(r / nz) + 1;
+        dst[t] = (double)src[pidx(g, 2 * id, 2 * jd, 2 * kd)];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// deterministic finish of block partials (FinishSpec in state.cuh)
+// ---------------------------------------------------------------------------
+__global__ void k_finish(const double* __restrict__ partials, double* scal, FinishSpec f, double ncells) {
+    __shared__ double sh[32];
+    for (int q = 0; q < f.n; ++q) {
+        const double* p = partials + (long long)f.slot[q] * kRedBlocks;
+        double v = f.op[q] == 1 ? -1.0e308 : 0.0;
+        for (int b = threadIdx.x; b < kRedBlocks; b += blockDim.x) v = f.op[q] == 1 ? (p[b] > v ? p[b] : v) : v + p[b];
+        double tot = f.op[q] == 1 ? block_max(v, sh) : block_sum(v, sh);
+        if (threadIdx.x == 0) {
+            double out = tot;
+            if (f.op[q] == 2) { out = tot / ncells; out = out > 1.0e-16 ? out : 1.0e-16; }
+            else if (f.op[q] == 3) out = tot / ncells;
+            scal[f.dst[q]] = out;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s) {
+    k_extr_io<R><<<gridn(c.n_extr_io), kBlk, 0, s>>>(c);
+    if (c.n_ft_cols > 0) k_extr_ft<R><<<gridn(c.n_ft_cols), kBlk, 0, s>>>(c);
+    if (c.n_extr_wall > 0) k_extr_wall<R><<<gridn(c.n_extr_wall), kBlk, 0, s>>>(c);
+}
+template <typename R> void launch_extrv(const Ctx<R>& c, int mex, cudaStream_t s) {
+    int first = 0;
+    for (int d = 0; d < 3; ++d) {
+        // one block per direction pass: the partial sums of the three passes go
+        // to blocks 0..2 of slots 10-13
+        Ctx<R> cc = c;
+        cc.partials = c.partials + d;   // shift so block 0 of pass d lands in column d
+        k_extrv<R><<<1, kBlk, 0, s>>>(cc, mex, first, c.n_extrv[d]);
+        first += c.n_extrv[d];
+    }
+}
+template <typename R> void launch_intpv(const Ctx<R>& c, cudaStream_t s) {
+    const GeoT<R>& g = c.g;
+    for (int IU = 1; IU <= 3; ++IU) {
+        int M3, N3, L3;
+        if (IU == 1) { M3 = g.MP; N3 = g.NP; L3 = g.LP; } else if (IU == 2) { M3 = g.NP; N3 = g.LP; L3 = g.MP; } else { M3 = g.LP; N3 = g.MP; L3 = g.NP; }
+        int ixa = IU == 1 ? 2 : (IU == 2 ? 3 : 1), ixb = IU == 1 ? 3 : (IU == 2 ? 1 : 2);
+        long long na = (long long)((M3 - 4) / 2 + 1) * ((N3 - 4) / 2 + 1) * (L3 / 2);
+        if (N3 > 3) k_intpv<R><<<gridn(na), kBlk, 0, s>>>(c, IU, 0, 3, M3 - 1, 2, 3, N3 - 1, 2, 2, L3, 2, ixa);
+        long long nb = (long long)((M3 - 4) / 2 + 1) * (N3 - 1) * ((L3 - 4) / 2 + 1);
+        if (L3 > 3) k_intpv<R><<<gridn(nb), kBlk, 0, s>>>(c, IU, 1, 3, M3 - 1, 2, 2, N3, 1, 3, L3 - 1, 2, ixb);
+        long long nc = (long long)((M3 - 4) / 2 + 1) * (N3 - 1) * (L3 - 1);
+        k_intpv<R><<<gridn(nc), kBlk, 0, s>>>(c, IU, 2, 4, M3, 2, 2, N3, 1, 2, L3, 1, IU);
+    }
+}
+template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s) {
+    long long n = (long long)c.g.MP * c.g.NP * c.g.LP / 4;
+    for (int st = 1; st <= 3; ++st) k_intp<R><<<gridn(n), kBlk, 0, s>>>(c, st);
+}
+template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s) {
+    long long n = (long long)c.g.HX * c.g.HY * c.g.HZ;
+    k_rad_emission<R><<<gridn(n), kBlk, 0, s>>>(c);
+    k_t_roundtrip<R><<<gridn(8 * c.g.CB), kBlk, 0, s>>>(c.T, 8 * c.g.CB, c.p.t0);
+}
+template <typename R> void launch_factor(const Ctx<R>& c, cudaStream_t s) {
+    k_factor<<<1, 32, 0, s>>>(c.scal, c.p.gmfr, c.p.t0, c.p.f_mx, c.p.f_mn, c.itr_gas);
+}
+void launch_finish(const double* partials, double* scal, const FinishSpec& f, double ncells, cudaStream_t s) {
+    k_finish<<<1, 256, 0, s>>>(partials, scal, f, ncells);
+}
+template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int K1, int I2, int J2, int K2, double F1, double F2,
+                                           cudaStream_t s) {
+    k_pref<R><<<1, 32, 0, s>>>(c, I1, J1, K1, I2, J2, K2, F1, F2);
+}
+template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s) {
+    k_to_split<R><<<gridn((long long)g.MP * g.NP * g.LP), kBlk, 0, s>>>(g, src, dst);
+}
+template <typename R> void launch_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s) {
+    k_from_split<R><<<gridn((long long)g.MP * g.NP * g.LP), kBlk, 0, s>>>(g, src, dst);
+}
+template <typename R> void launch_cells_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s) {
+    k_cells_to_split<R><<<gridn((long long)(g.MP / 2) * (g.NP / 2) * (g.LP / 2)), kBlk, 0, s>>>(g, src, dst, g.MP / 2, g.NP / 2, g.LP / 2);
+}
+template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s) {
+    k_cells_from_split<R><<<gridn((long long)(g.MP / 2) * (g.NP / 2) * (g.LP / 2)), kBlk, 0, s>>>(g, src, dst, g.MP / 2, g.NP / 2, g.LP / 2);
+}
+
+#define INST(R)                                                                                                     \
+    template void launch_extr<R>(const Ctx<R>&, cudaStream_t);                                                     \
+    template void launch_extrv<R>(const Ctx<R>&, int, cudaStream_t);                                               \
+    template void launch_intpv<R>(const Ctx<R>&, cudaStream_t);                                                    \
+    template void launch_intp<R>(const Ctx<R>&, cudaStream_t);                                                     \
+    template void launch_rad_emission<R>(const Ctx<R>&, cudaStream_t);                                             \
+    template void launch_factor<R>(const Ctx<R>&, cudaStream_t);                                                   \
+    template void launch_pref_idx<R>(const Ctx<R>&, int, int, int, int, int, int, double, double, cudaStream_t);  \
+    template void launch_to_split<R>(const GeoT<R>&, const double*, R*, cudaStream_t);                             \
+    template void launch_from_split<R>(const GeoT<R>&, const R*, double*, cudaStream_t);                           \
+    template void launch_cells_to_split<R>(const GeoT<R>&, const double*, R*, cudaStream_t);                       \
+    template void launch_cells_from_split<R>(const GeoT<R>&, const R*, double*, cudaStream_t);
+INST(double)
+INST(float)
+#undef INST
+
+}  // namespace gfm

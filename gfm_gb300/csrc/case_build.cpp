@@ -1,0 +1,443 @@
+// case_build.cpp -- host construction of a synthetic furnace case in the
+// reference's data layout: the work the Fortran host does before the first
+// GFLOW (GRID3, SETUP, SBC, gen_initial_guess; combustion/Code/A0main.f90:158-190).
+//
+// The synthetic furnace stands in for the reference's gd####c.dat / sbc####c.dat
+// input files: a rectangular box, walls on all six sides, inlets on the x=0
+// wall, one flue opening on the x=lx wall.
+#include "../../include/gfm_gb300.h"
+#include "physics.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace {
+
+using gfm::Nist;
+
+struct CaseStore {
+    int mp = 0, np = 0, lp = 0;
+    std::vector<double> x, dx, r, dr, rs, z, dz;
+    std::vector<int16_t> ibcell;
+    std::vector<int16_t> b_typ, b_i, b_j, b_k, b_orient, b_direct;
+    std::vector<double> b_t;
+    std::vector<double> rtim, delrt, hrt, delr, timed, hrd;
+    std::vector<double> wl, akl0;
+    std::vector<double> p, t, dnst, theta, tmu, gama, crate, hrate, bs_hprev, ug, gf, qa, qe;
+    long at(int i, int j, int k) const { return (i - 1) + (long)mp * ((j - 1) + (long)np * (k - 1)); }
+    long n() const { return (long)mp * np * lp; }
+};
+
+// splitmix64: deterministic per-cell noise for the perturbed initial state
+uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+double unit_noise(uint64_t seed, uint64_t idx, uint64_t comp) {
+    uint64_t h = splitmix64(seed ^ splitmix64(idx * 16 + comp));
+    return ((double)(h >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;  // [-1,1)
+}
+
+// GRID3 coordinate line (Grid3.f90:79-109): X(1..i1)=x0, then linear to
+// X(n-1)=x1 by repeated addition of DEL, X(n)=X(n-1), DX(I)=X(I+1)-X(I-1).
+void coord_line(int n, double len, std::vector<double>& x, std::vector<double>& dx) {
+    x.assign(n, 0.0);
+    dx.assign(n, 0.0);
+    const int i1 = 3, i2 = n - 1;
+    for (int i = 1; i <= i1; ++i) x[i - 1] = 0.0;
+    double del = (len - x[i1 - 1]) / (i2 - i1);
+    for (int i = i1 + 1; i <= i2; ++i) x[i - 1] = x[i - 2] + del;
+    for (int i = 1; i <= n - 1; ++i) x[i - 1] = x[i - 1] / 1.0;   // /R0, R0=1
+    x[n - 1] = x[n - 2];
+    dx[0] = 0.0;
+    for (int i = 2; i <= n - 1; ++i) dx[i - 1] = x[i] - x[i - 2];
+    dx[n - 1] = 0.0;
+}
+
+// snap an opening [a,b] on a uniform line of `ncell` cells of width h to a
+// run of whole cells; returns 1-based first cell and count
+void snap(double a, double b, double h, int ncell, int& first, int& count) {
+    count = (int)std::lround((b - a) / h);
+    if (count < 1) count = 1;
+    if (count > ncell) count = ncell;
+    double c = 0.5 * (a + b) / h;
+    first = (int)std::lround(c - 0.5 * count) + 1;
+    if (first < 1) first = 1;
+    if (first + count - 1 > ncell) first = ncell - count + 1;
+}
+
+bool read_kinetics(const char* path, int nr0, CaseStore& s, double h_0) {
+    FILE* fp = std::fopen(path, "r");
+    if (!fp) return false;
+    char line[512];
+    auto next = [&](double* a, double* b, double* c) -> bool {
+        while (std::fgets(line, sizeof line, fp)) {
+            if (std::sscanf(line, "%lf %lf %lf", a, b, c) == 3) return true;
+            return false;   // header line
+        }
+        return false;
+    };
+    s.rtim.resize(nr0); s.delrt.resize(nr0); s.hrt.resize(nr0);
+    s.delr.resize(nr0); s.timed.resize(nr0); s.hrd.resize(nr0);
+    const double chrd = 0.166;
+    if (!std::fgets(line, sizeof line, fp)) { std::fclose(fp); return false; }   // header
+    for (int i = 0; i < nr0; ++i) {
+        if (!next(&s.rtim[i], &s.delrt[i], &s.hrt[i])) { std::fclose(fp); return false; }
+        s.rtim[i] = s.rtim[i] * 0.7;                       // Setup.f90:874
+        s.hrt[i] = chrd * s.hrt[i] / h_0 / gfm::kWf;       // Setup.f90:876
+    }
+    if (!std::fgets(line, sizeof line, fp)) { std::fclose(fp); return false; }   // header
+    for (int i = 0; i < nr0; ++i) {
+        if (!next(&s.delr[i], &s.timed[i], &s.hrd[i])) { std::fclose(fp); return false; }
+        s.timed[i] = s.timed[i] * 0.7;                     // Setup.f90:884
+        s.hrd[i] = chrd * s.hrd[i] / h_0 / gfm::kWf;       // Setup.f90:886
+    }
+    std::fclose(fp);
+    return true;
+}
+
+}  // namespace
+
+extern "C" int gfm_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* out) {
+    if (!sp || !out || !kinetic_path) return GFM_E_ARG;
+    std::memset(out, 0, sizeof *out);
+    if (sp->nx < 4 || sp->ny < 4 || sp->nz < 4 || sp->nx > 4096 || sp->ny > 4096 || sp->nz > 4096)
+        return GFM_E_ARG;
+    if (sp->n_inlets < 1 || sp->n_inlets > 8 || sp->nwl < 1 || sp->nwl > 16) return GFM_E_ARG;
+    if (!(sp->lx > 0 && sp->ly > 0 && sp->lz > 0)) return GFM_E_ARG;
+
+    CaseStore* S = new (std::nothrow) CaseStore;
+    if (!S) return GFM_E_NOMEM;
+    CaseStore& s = *S;
+    const int mp = 2 * sp->nx + 4, np = 2 * sp->ny + 4, lp = 2 * sp->nz + 4;
+    s.mp = mp; s.np = np; s.lp = lp;
+    const long N = s.n();
+
+    // ---- GRID3 coordinates (Grid3.f90:76-226) -------------------------------
+    coord_line(mp, sp->lx, s.x, s.dx);
+    coord_line(np, sp->ly, s.r, s.dr);
+    coord_line(lp, sp->lz, s.z, s.dz);
+    s.rs.assign(np, 1.0);                        // cartesian: RS=1 (Grid3.f90:166)
+
+    // ---- cell map: walls, inlets on x=0, exit on x=lx -----------------------
+    s.ibcell.assign(N, 0);
+    auto IB = [&](int i, int j, int k) -> int16_t& { return s.ibcell[s.at(i, j, k)]; };
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 2; i <= mp; i += 2)
+                if (i == 2 || i == mp || j == 2 || j == np || k == 2 || k == lp) IB(i, j, k) = 1;
+    const double hy = sp->ly / sp->ny, hz = sp->lz / sp->nz;
+    struct InletCells { int j1, j2, k1, k2; double u; };
+    std::vector<InletCells> inl(sp->n_inlets);
+    for (int n = 0; n < sp->n_inlets; ++n) {
+        const gfm_inlet_spec& in = sp->inlets[n];
+        int fy, cy, fz, cz;
+        snap(in.y0, in.y1, hy, sp->ny, fy, cy);
+        snap(in.z0, in.z1, hz, sp->nz, fz, cz);
+        inl[n].j1 = 2 * fy + 2; inl[n].j2 = 2 * (fy + cy - 1) + 2;
+        inl[n].k1 = 2 * fz + 2; inl[n].k2 = 2 * (fz + cz - 1) + 2;
+        double a_nom = (in.y1 - in.y0) * (in.z1 - in.z0);
+        double a_snap = cy * hy * cz * hz;
+        double jit = 1.0;
+        if (sp->inlet_jitter > 0) jit = 1.0 + sp->inlet_jitter * unit_noise(sp->seed, 1000003ull + n, 7);
+        inl[n].u = in.u_ms * a_nom / a_snap * jit;
+        for (int k = inl[n].k1; k <= inl[n].k2; k += 2)
+            for (int j = inl[n].j1; j <= inl[n].j2; j += 2) IB(2, j, k) = 2;
+    }
+    {
+        int fy, cy, fz, cz;
+        snap(sp->exit_y0, sp->exit_y1, hy, sp->ny, fy, cy);
+        snap(sp->exit_z0, sp->exit_z1, hz, sp->nz, fz, cz);
+        for (int k = 2 * fz + 2; k <= 2 * (fz + cz - 1) + 2; k += 2)
+            for (int j = 2 * fy + 2; j <= 2 * (fy + cy - 1) + 2; j += 2) IB(mp, j, k) = 3;
+    }
+    // NCELLS and the 27-neighbour face/edge propagation (Grid3.f90:259-275),
+    // loop order I, J, K as in the Fortran
+    int ncells = 0;
+    for (int i = 2; i <= mp; i += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int k = 2; k <= lp; k += 2) {
+                int ibc1 = IB(i, j, k);
+                if (ibc1 <= 0) { ++ncells; continue; }
+                for (int i1 = i - 1; i1 <= i + 1; ++i1)
+                    for (int j1 = j - 1; j1 <= j + 1; ++j1)
+                        for (int k1 = k - 1; k1 <= k + 1; ++k1) {
+                            if (i1 > mp || j1 > np || k1 > lp) continue;
+                            if (IB(i1, j1, k1) != 1) IB(i1, j1, k1) = (int16_t)ibc1;
+                        }
+            }
+
+    // ---- SETUP constants (Setup.f90:27-217, 542-731) -------------------------
+    gfm_params& P = out->params;
+    std::memset(&P, 0, sizeof P);
+    const double t0 = gfm::kT0;
+    const double h_0 = 1.0057e+3 * (5.0e+2 - 298.15);                       // Var_mod.f90:184
+    const double wt0 = 1.0 / (0.5 / 16.0426 + 0.0 / 44.0098 + 0.0 / 18.0152 + 0.49 / 31.9988 + 0.01 / 28.0134);
+    const double pg0 = sp->pg0 > 0 ? sp->pg0 : 1.01325e5;
+    // GMFR = total inlet mass flow from the inlet states (the GUI writes it)
+    double gmfr = 0.0;
+    for (int n = 0; n < sp->n_inlets; ++n) {
+        const gfm_inlet_spec& in = sp->inlets[n];
+        double w_in = 1.0 / (in.yf / gfm::kWf + in.yco2 / gfm::kWco2 + in.yh2o / gfm::kWh2o +
+                             in.yo2 / gfm::kWo2 + in.yn2 / gfm::kWn2);
+        double rho = pg0 * w_in / (gfm::kRu * in.t_k);
+        int cy = (inl[n].j2 - inl[n].j1) / 2 + 1, cz = (inl[n].k2 - inl[n].k1) / 2 + 1;
+        gmfr += rho * std::fabs(inl[n].u) * (cy * hy) * (cz * hz);
+    }
+    const double r0 = 1.0, area0 = 1.0;
+    const double dnst0 = pg0 * wt0 / gfm::kRu / t0;
+    const double ug0 = gmfr / dnst0 / area0;
+    const double gmu_ref = 2.6e-5 * std::pow(gfm::kTl00 / 2.98e+2, 0.0);
+    const double tk0 = gfm::kCtea * (ug0 * ug0);
+    const double epsi0 = gfm::kCtda * (tk0 * tk0);
+    const double reyg = 2.0 * dnst0 * ug0 * r0 / gmu_ref;
+    P.t0 = t0; P.h_0 = h_0; P.dnst0 = dnst0; P.ug0 = ug0; P.gmfr = gmfr; P.pg0 = pg0; P.r0 = r0;
+    P.reyg = reyg; P.reyg2 = reyg / 2.0;
+    P.epsr = tk0 / (ug0 * ug0);
+    P.taur = epsi0 * r0 / (tk0 * ug0);
+    P.eun = pg0 / (dnst0 * (ug0 * ug0));
+    P.qr0 = h_0 * dnst0 * ug0 / r0;
+    P.q0 = (sp->q0_jkg > 0 ? sp->q0_jkg : 2.42e6) / h_0;
+    P.tk0 = tk0;
+    P.gra[0] = 0.0 / ug0 / ug0 * r0; P.gra[1] = 0.0 / ug0 / ug0 * r0; P.gra[2] = -9.80621 / ug0 / ug0 * r0;
+    P.amu = 0.0;
+    P.trdg = 298.15 / 5.0e+2;
+    P.wt0 = wt0;
+    P.stoich = 2.0 * 31.9988 / 16.0426;
+    P.cmu = gfm::kCmu; P.ct1 = gfm::kCt1; P.ct2 = gfm::kCt2;
+    P.p_mx = 0.2; P.p_mn = -0.6;
+    P.t_mx = 3.0e+3 / t0; P.t_mn = 2.0e+2 / 5.0e+2;
+    P.u_mx = 1.0e+3 / ug0; P.u_mn = -P.u_mx;
+    P.f_mx = 1.5; P.f_mn = 0.8;
+    for (int i = 0; i < 21; ++i) { P.rf[i] = 0.7; P.rfl[i] = 0.6; }
+    P.rf[0] = P.rf[1] = P.rf[2] = sp->rf_uvw;
+    P.rf[17] = 0.6; P.rf[20] = 0.6;
+    P.rfl[0] = sp->rfl_species; P.rfl[1] = sp->rfl_species; P.rfl[2] = sp->rfl_h;
+    P.rfl[3] = sp->rfl_k; P.rfl[4] = sp->rfl_eps; P.rfl[5] = sp->rfl_species; P.rfl[6] = sp->rfl_species;
+    const double sig0[12] = {0.7, 0.7, 0.7, 1.0, 1.0, 0.7, 0.7, 0.7, 0.7, 0.7, 0.7, 0.7};
+    for (int i = 0; i < 12; ++i) P.sigma[i] = sig0[i];
+    P.sigma[3] = sp->sigma_k; P.sigma[4] = sp->sigma_eps;
+    for (int i = 0; i < 20; ++i) P.ntimesg[i] = 2;
+    for (int i = 0; i < 12; ++i) P.ntimesg[i] = sp->ntimesg[i];
+    P.rf_hsource = sp->rf_hsource;
+    P.react = sp->react; P.turb = 1;
+    P.wall_sink = sp->wall_sink; P.h_g = sp->h_g;
+    P.rad_emission = sp->rad_emission; P.rad_qe_frequency = 10;
+    P.sig = gfm::kSig; P.ri = 1.0; P.hck = gfm::kHck;
+    P.bgcon = sp->bgcon; P.maxgi = sp->maxgi;
+    P.adi_mode = sp->adi_mode; P.precision = sp->precision;
+
+    // ---- fields at allocation (Setup.f90:747-779) -----------------------------
+    s.p.assign(N, 0.0); s.t.assign(N, 1.0); s.dnst.assign(N, 1.0); s.theta.assign(N, 1.0);
+    s.tmu.assign(N, 0.0); s.gama.assign(N, 0.0); s.crate.assign(N, 0.0); s.hrate.assign(N, 0.0);
+    s.bs_hprev.assign(N, 0.0);
+    s.ug.assign(3 * N, 0.0); s.gf.assign(9 * N, 0.0);
+    const long ncell_arr = (long)(mp / 2) * (np / 2) * (lp / 2);
+    s.qa.assign(ncell_arr, 0.0); s.qe.assign(ncell_arr, 0.0);
+    const Nist& NI = gfm::nist_host();
+    auto GF = [&](int i, int j, int k, int l) -> double& { return s.gf[s.at(i, j, k) + (long)l * N]; };
+    auto UG = [&](int i, int j, int k, int l) -> double& { return s.ug[s.at(i, j, k) + (long)l * N]; };
+    auto ther = [&](long a) {   // THER (Prop.f90:130-154)
+        double* y = &s.gf[a];
+        if (y[gfm::kEps * N] < 1.0e-12) y[gfm::kEps * N] = 1.0e-12;
+        double g0 = P.cmu * P.reyg * P.epsr / (2.0 * P.taur) * (y[gfm::kK * N] * y[gfm::kK * N]) / y[gfm::kEps * N] * s.dnst[a];
+        s.tmu[a] = g0;
+        s.gama[a] = 2.0 / P.reyg * (s.tmu[a] + std::pow(s.t[a] / P.trdg, P.amu));
+    };
+    auto tke = [&](long a) {    // TKE (Prop.f90:162-176)
+        double g = s.ug[a] * s.ug[a] + s.ug[a + N] * s.ug[a + N] + s.ug[a + 2 * N] * s.ug[a + 2 * N];
+        s.gf[a + gfm::kK * N] = g > 1.0e-6 ? g : 1.0e-6;
+        s.gf[a + gfm::kEps * N] = s.gf[a + gfm::kK * N] * s.gf[a + gfm::kK * N];
+    };
+    auto dnst = [&](long a) { s.dnst[a] = gfm::dnst_calc<double>(&s.gf[a], N, s.p[a], s.t[a], wt0); };
+    auto t2h = [&](long a) { s.gf[a + gfm::kH * N] = gfm::t_to_enth(NI, &s.gf[a], N, s.t[a], t0, h_0); };
+
+    // ---- SBC: inlet states and inlet faces (Sbc.f90:57-269, 365-386) ---------
+    const int i_ref = 2, j_ref = inl[0].j1, k_ref = inl[0].k1;
+    out->grid.p_ref = 0.0 / pg0;
+    double fr_f = 0, fr_ox = 0, fr_n2 = 0, q_h_in = 0;
+    std::vector<char> done(N, 0);   // plays the role of the temporary IBCELL=20 mark
+    for (int n = 0; n < sp->n_inlets; ++n) {
+        const gfm_inlet_spec& in = sp->inlets[n];
+        const double T_0 = in.t_k / t0, U_0 = inl[n].u / ug0;
+        const int i1 = 2, j1 = inl[n].j1, j2 = inl[n].j2, k1 = inl[n].k1, k2 = inl[n].k2;
+        for (int i = i1; i <= i1; i += 2)
+            for (int j = j1; j <= j2; j += 2)
+                for (int k = k1; k <= k2; k += 2) {
+                    long a = s.at(i, j, k);
+                    if (IB(i, j, k) != 2 || done[a]) continue;
+                    done[a] = 1;
+                    s.p[a] = out->grid.p_ref;
+                    s.t[a] = T_0;
+                    GF(i, j, k, gfm::kYF) = in.yf; GF(i, j, k, gfm::kYCO2) = in.yco2;
+                    GF(i, j, k, gfm::kYH2O) = in.yh2o; GF(i, j, k, gfm::kYO2) = in.yo2;
+                    GF(i, j, k, gfm::kYN2) = in.yn2;
+                    dnst(a);
+                    UG(i, j, k, 0) = U_0; UG(i, j, k, 1) = 0.0; UG(i, j, k, 2) = 0.0;
+                    tke(a);
+                    ther(a);
+                    t2h(a);
+                    double g0 = s.theta[a] * s.dnst[a] * dnst0;
+                    double area = s.dr[j - 1] * s.rs[j - 1] * s.dz[k - 1] * area0;   // AREA_C(I,J,K,1), open-face area
+                    g0 = g0 * std::fabs(U_0) * ug0 * area;
+                    fr_f += g0 * GF(i, j, k, gfm::kYF);
+                    fr_ox += g0 * GF(i, j, k, gfm::kYO2);
+                    fr_n2 += g0 * GF(i, j, k, gfm::kYN2);
+                    q_h_in += GF(i, j, k, gfm::kH) * h_0 * g0;
+                }
+        // SBC1: interpolate inlet-plane faces (IU=1 branch, Sbc.f90:179-200)
+        auto sbc1 = [&](int ia, int ja, int ka, int ib, int jb, int kb, int i, int j, int k, double f1) {
+            double f2 = 1.0 - f1;
+            long A = s.at(ia, ja, ka), B = s.at(ib, jb, kb), C = s.at(i, j, k);
+            s.p[C] = f1 * s.p[A] + f2 * s.p[B];
+            s.t[C] = f1 * s.t[A] + f2 * s.t[B];
+            for (int l = 0; l < 9; ++l) {
+                if (l < 3) s.ug[C + l * N] = f1 * s.ug[A + l * N] + f2 * s.ug[B + l * N];
+                s.gf[C + l * N] = f1 * s.gf[A + l * N] + f2 * s.gf[B + l * N];
+            }
+            dnst(C);
+            s.theta[C] = f1 * s.theta[A] + f2 * s.theta[B];
+            s.tmu[C] = f1 * s.tmu[A] + f2 * s.tmu[B];
+            s.gama[C] = f1 * s.gama[A] + f2 * s.gama[B];
+        };
+        const int i = i1;
+        if (k2 > k1)
+            for (int k = k1 + 1; k <= k2 - 1; k += 2)
+                for (int j = j1; j <= j2; j += 2) {
+                    double f1 = (s.z[k - 1] - s.z[k - 2]) / s.dz[k - 1];
+                    sbc1(i, j, k + 1, i, j, k - 1, i, j, k, f1);
+                }
+        if (j2 > j1)
+            for (int j = j1 + 1; j <= j2 - 1; j += 2)
+                for (int k = k1; k <= k2; ++k) {
+                    double f1 = (s.r[j - 1] - s.r[j - 2]) / s.dr[j - 1];
+                    sbc1(i, j + 1, k, i, j - 1, k, i, j, k, f1);
+                }
+        // SBC3 (Sbc.f90:201-207, 491-522): copy onto the inlet face planes
+        auto sbc3 = [&](int ia, int ja, int ka, int ib, int jb, int kb) {
+            long A = s.at(ia, ja, ka), B = s.at(ib, jb, kb);
+            for (int l = 0; l < 3; ++l) s.ug[B + l * N] = s.ug[A + l * N];
+            s.p[B] = s.p[A]; s.t[B] = s.t[A];
+            for (int l = 0; l < 9; ++l) s.gf[B + l * N] = s.gf[A + l * N];
+            s.dnst[B] = s.dnst[A]; s.theta[B] = s.theta[A]; s.tmu[B] = s.tmu[A]; s.gama[B] = s.gama[A];
+        };
+        for (int j = j1; j <= j2; ++j)
+            for (int k = k1; k <= k2; ++k) {
+                if (i < mp && IB(i + 1, j, k) == 2) sbc3(i, j, k, i + 1, j, k);
+                if (i > 2 && IB(i - 1, j, k) == 2) sbc3(i, j, k, i - 1, j, k);
+            }
+    }
+    const double gfin = fr_f + fr_ox + fr_n2;
+    const double gfin0 = gfin / gmfr;
+    // est_out_mass_frac (Sbc.f90:566-576)
+    const double yn2_out = fr_n2 / gfin;
+    const double yh2o_out = (2 * fr_f * gfm::kWh2o / gfm::kWf) / gfin;
+    const double yco2_out = (fr_f * gfm::kWco2 / gfm::kWf) / gfin;
+    const double yo2_out = (fr_ox - 2 * fr_f * gfm::kWo2 / gfm::kWf) / gfin;
+
+    // ---- gen_initial_guess with a seeded perturbation (Initsv.f90:97-162) ----
+    const double T_init = sp->t_init_k / t0;
+    const double amp = sp->noise_amp;
+    for (int i = 2; i <= mp; i += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int k = 2; k <= lp; k += 2) {
+                int ibc = IB(i, j, k);
+                if (ibc == 2) continue;
+                long a = s.at(i, j, k);
+                double nz[5] = {0, 0, 0, 0, 0};
+                if (ibc == 0 && amp != 0.0)
+                    for (int c = 0; c < 5; ++c) nz[c] = amp * unit_noise(sp->seed, (uint64_t)a, (uint64_t)c);
+                GF(i, j, k, gfm::kYF) = 0;
+                GF(i, j, k, gfm::kYO2) = yo2_out * (1.0 + nz[1]);
+                GF(i, j, k, gfm::kYCO2) = yco2_out * (1.0 + nz[2]);
+                GF(i, j, k, gfm::kYH2O) = yh2o_out * (1.0 + nz[3]);
+                GF(i, j, k, gfm::kYN2) = yn2_out * (1.0 + nz[4]);
+                if (ibc == 1) {
+                    s.t[a] = T_init;
+                    t2h(a);
+                    continue;
+                }
+                UG(i, j, k, 0) = 0; UG(i, j, k, 1) = 0; UG(i, j, k, 2) = 0;
+                s.theta[a] = 1.0;
+                s.t[a] = T_init * (1.0 + nz[0]);
+                t2h(a);
+                tke(a);
+                dnst(a);
+                ther(a);
+            }
+
+    // ---- wall patches of the fixed-temperature sink (Qwall.f90:395-513) -------
+    auto add_patch = [&](int typ, int ori, int dir, int i, int j, int k) {
+        s.b_typ.push_back((int16_t)typ); s.b_orient.push_back((int16_t)ori); s.b_direct.push_back((int16_t)dir);
+        s.b_i.push_back((int16_t)i); s.b_j.push_back((int16_t)j); s.b_k.push_back((int16_t)k);
+        s.b_t.push_back(sp->t_wall_k);
+    };
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 3; i <= mp - 1; i += 2) {
+                int m = IB(i, j, k);
+                if (m < 1) continue;
+                if (IB(i - 1, j, k) > 0 && IB(i + 1, j, k) > 0) continue;
+                add_patch(m, 1, IB(i + 1, j, k) == 0 ? 0 : 1, i, j, k);
+            }
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 3; j <= np - 1; j += 2)
+            for (int i = 2; i <= mp; i += 2) {
+                int m = IB(i, j, k);
+                if (m < 1) continue;
+                if (IB(i, j - 1, k) > 0 && IB(i, j + 1, k) > 0) continue;
+                add_patch(m, 2, IB(i, j + 1, k) == 0 ? 0 : 1, i, j, k);
+            }
+    for (int k = 3; k <= lp - 1; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 2; i <= mp; i += 2) {
+                int m = IB(i, j, k);
+                if (m < 1) continue;
+                if (IB(i, j, k - 1) > 0 && IB(i, j, k + 1) > 0) continue;
+                add_patch(m, 3, IB(i, j, k + 1) == 0 ? 0 : 1, i, j, k);
+            }
+
+    // ---- kinetics table and radiation bands -----------------------------------
+    const int nr0 = 100;
+    if (!read_kinetics(kinetic_path, nr0, s, h_0)) { delete S; return GFM_E_ARG; }
+    s.wl.resize(sp->nwl); s.akl0.resize(sp->nwl);
+    for (int l = 0; l < sp->nwl; ++l) { s.wl[l] = sp->wl_um[l] * 1.0e-6; s.akl0[l] = sp->kappa[l]; }
+
+    // ---- fill the public structs -----------------------------------------------
+    gfm_grid& G = out->grid;
+    G.mp = mp; G.np = np; G.lp = lp;
+    G.x = s.x.data(); G.dx = s.dx.data(); G.r = s.r.data(); G.dr = s.dr.data(); G.rs = s.rs.data();
+    G.z = s.z.data(); G.dz = s.dz.data();
+    G.ibcell = s.ibcell.data();
+    G.ncells = ncells;
+    G.i_ref = i_ref; G.j_ref = j_ref; G.k_ref = k_ref;
+    G.b_cnt = (int)s.b_typ.size();
+    G.b_typ = s.b_typ.data(); G.b_i = s.b_i.data(); G.b_j = s.b_j.data(); G.b_k = s.b_k.data();
+    G.b_orient = s.b_orient.data(); G.b_direct = s.b_direct.data(); G.b_t = s.b_t.data();
+    G.nr0 = nr0;
+    G.rtim = s.rtim.data(); G.delrt = s.delrt.data(); G.hrt = s.hrt.data();
+    G.delr = s.delr.data(); G.timed = s.timed.data(); G.hrd = s.hrd.data();
+    G.nwl = sp->nwl; G.wl = s.wl.data(); G.akl0 = s.akl0.data();
+
+    gfm_fields& F = out->fields;
+    F.p = s.p.data(); F.t = s.t.data(); F.dnst = s.dnst.data(); F.theta = s.theta.data();
+    F.tmu = s.tmu.data(); F.gama = s.gama.data(); F.crate = s.crate.data(); F.hrate = s.hrate.data();
+    F.bs_hprev = s.bs_hprev.data(); F.ug = s.ug.data(); F.gf = s.gf.data();
+    F.qa = s.qa.data(); F.qe = s.qe.data();
+    F.itr_gas = 0; F.do_rad_qe_only_cnt = 0; F.i1st_rad_qe_done = 0;
+    F.factor = 1.0; F.fadj = 0.0; F.gfin0 = gfin0; F.q_h_in = q_h_in;
+    out->priv = S;
+    return GFM_OK;
+}
+
+extern "C" void gfm_case_free(gfm_case* c) {
+    if (!c) return;
+    delete static_cast<CaseStore*>(c->priv);
+    std::memset(c, 0, sizeof *c);
+}

@@ -1,0 +1,103 @@
+// device.cuh -- device-side layout, context and helpers of the GB300 solver.
+//
+// Layout.  The reference stores every field on its doubled staggered grid
+// A(MP,NP,LP): cell centres at (even,even,even), x-faces at (odd,even,even),
+// edges and corners at the other parity classes (Grid3.f90:8-300).  A kernel
+// working on one class would touch every other element of a Fortran row.  On
+// the device each field is split by parity class: class c = (I&1)|(J&1)<<1|
+// (K&1)<<2 is a dense (PX,HY,HZ) block, element (I,J,K) at
+//     c*CB + ((K>>1)*HY + (J>>1))*PX + (I>>1).
+// The map is a bijection with the doubled grid, so every reference loop over
+// one class becomes a unit-stride, coalesced sweep, and neighbour (I+-1) is the
+// same (J,K) row of the neighbouring class.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gfm_gb300.h"
+#include "physics.h"
+
+namespace gfm {
+
+// Grid geometry on the device (coordinate arrays 1-based: index 0 unused),
+// coordinates stored in the arithmetic type R of the kernels using them.
+template <typename R>
+struct GeoT {
+    int MP, NP, LP;
+    int HX, HY, HZ, PX;        // half extents (MP/2+1 ...) and padded row pitch
+    long long CB;              // elements per parity class
+    int MPM1, MPM2, NPM1, NPM2, LPM1, LPM2;
+    int NJY1, NJY2, LKZ1, LKZ2;
+    int NJY1V[4], NJY2V[4], LKZ1V[4], LKZ2V[4];
+    int NCELLS;
+    const R *X, *DX, *Rr, *DR, *RS, *Z, *DZ;
+    const int8_t* ib;          // IBCELL, parity split
+};
+using Geo = GeoT<double>;
+
+template <typename R>
+__host__ __device__ __forceinline__ long long pidx(const GeoT<R>& g, int I, int J, int K) {
+    int c = (I & 1) | ((J & 1) << 1) | ((K & 1) << 2);
+    return (long long)c * g.CB + ((long long)(K >> 1) * g.HY + (J >> 1)) * g.PX + (I >> 1);
+}
+template <typename R>
+__device__ __forceinline__ int IBC(const GeoT<R>& g, int I, int J, int K) { return g.ib[pidx(g, I, J, K)]; }
+
+// Scalar constants of the run (gfm_params plus derived complements).
+struct Prm {
+    double t0, h_0, dnst0, ug0, gmfr, pg0, r0;
+    double reyg, reyg2, epsr, taur, eun, qr0, q0, tk0;
+    double gra[3];
+    double amu, trdg, wt0, stoich;
+    double cmu, ct1, ct2;
+    double p_mx, p_mn, t_mx, t_mn, u_mx, u_mn, f_mx, f_mn;
+    double rf[21], rfc[21], rfl[21], rflc[21];
+    double sigma[12];
+    double rf_hsource, h_g;
+    double sig, ri, hck;
+    int react, wall_sink;
+};
+
+// Deterministic FP64 reductions: every block writes one partial per slot into
+// `partials`, a single-block kernel sums them in a fixed order.
+constexpr int kRedSlots = 64;      // independent sums per iteration
+constexpr int kRedBlocks = 1024;   // max blocks contributing per pass
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        double w = __shfl_down_sync(0xffffffffu, v, o);
+        v = (w > v) ? w : v;
+    }
+    return v;
+}
+// Block-wide sum of v; result valid in thread 0.  Requires blockDim.x % 32 == 0.
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+    v = warp_sum(v);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (w == 0) v = warp_sum(v);
+    __syncthreads();
+    return v;
+}
+__device__ __forceinline__ double block_max(double v, double* sh) {
+    v = warp_max(v);
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    int nw = blockDim.x >> 5;
+    v = (threadIdx.x < nw) ? sh[threadIdx.x] : -1.0e308;
+    if (w == 0) v = warp_max(v);
+    __syncthreads();
+    return v;
+}
+
+}  // namespace gfm

@@ -1,0 +1,929 @@
+// solver.cu -- host orchestration of the GB300 solver behind the C ABI
+// (include/gfm_gb300.h): geometry and boundary tables built once on the host,
+// device state, upload/download in the reference layout, and the GFLOW
+// sequence (Gflow.f90:6-408) issued on one CUDA stream per handle.
+#include <cuda_runtime.h>
+
+#include <array>
+#include <cmath>
+#include <initializer_list>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/gfm_gb300.h"
+#include "state.cuh"
+
+using namespace gfm;
+
+namespace {
+
+// reduction slots (partials rows)
+enum Slot {
+    SL_RESM = 0, SL_RESMAX = 1, SL_QCONV = 4, SL_QREACT = 5, SL_TA = 6, SL_TB = 7, SL_GFIN0 = 8, SL_QEX = 9,
+    SL_GFEX = 10, SL_TM = 11, SL_TAREA = 12, SL_AREA = 13,
+    SL_P_PRE = 16, SL_P_POST = 17, SL_PC_POST = 18, SL_U_PRE = 19, SL_U_POST = 22, SL_GF_PRE = 25, SL_GF_POST = 32
+};
+
+struct HostGrid {
+    int MP, NP, LP;
+    std::vector<int16_t> ib;   // doubled layout
+    std::vector<double> X, DX, R, DR, RS, Z, DZ;   // 1-based
+    int at(int i, int j, int k) const { return ib[(i - 1) + (long)MP * ((j - 1) + (long)NP * (k - 1))]; }
+};
+
+}  // namespace
+
+struct gfm_handle {
+    int prec = GFM_PREC_FP64;
+    int adi_mode = GFM_ADI_MARCH;
+    gfm_params params{};
+    HostGrid hg;
+    long long N = 0, CB = 0, NS = 0;
+    int ncells = 0;
+    GeoT<double> gd{};
+    GeoT<float> gfl{};
+    Ctx<double> cd{};
+    Ctx<float> cf{};
+    AdiScratch<double> scr_d[8]{};
+    AdiScratch<float> scr_f[8]{};
+    std::vector<void*> allocs;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_adi0 = nullptr, ev_adi1 = nullptr;
+    int* d_wall = nullptr;
+    int n_wall = 0;
+    double* d_stage = nullptr;      // doubled-layout staging buffer (N doubles)
+    double* h_scal = nullptr;       // pinned copy of the device scalars
+    int pref_i1 = 0, pref_j1 = 0, pref_k1 = 0, pref_i2 = 0, pref_j2 = 0, pref_k2 = 0;
+    double pref_f1 = 1, pref_f2 = 0;
+    int itr_gas = 0, cnt_qe = 0, rad_active = 0;
+    double q_h_in = 0;
+    double adi_ms = 0, asm_ms = 0, other_ms = 0;
+    long long launches = 0;
+    std::string err;
+};
+
+namespace {
+
+#define CK(x)                                                                          \
+    do {                                                                               \
+        cudaError_t e_ = (x);                                                          \
+        if (e_ != cudaSuccess) {                                                       \
+            h->err = std::string(#x) + ": " + cudaGetErrorString(e_);                  \
+            return GFM_E_CUDA;                                                         \
+        }                                                                              \
+    } while (0)
+
+template <typename T>
+int dalloc(gfm_handle* h, T** p, long long n) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, (size_t)n * sizeof(T));
+    if (e != cudaSuccess) {
+        h->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return GFM_E_NOMEM;
+    }
+    cudaMemset(q, 0, (size_t)n * sizeof(T));
+    h->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return GFM_OK;
+}
+
+template <typename T>
+int dupload(gfm_handle* h, T** p, const std::vector<T>& v) {
+    long long n = v.empty() ? 1 : (long long)v.size();
+    int rc = dalloc(h, p, n);
+    if (rc) return rc;
+    if (!v.empty()) CK(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return GFM_OK;
+}
+
+// ---- host replicas of the reference index helpers (Extr.f90:311-661) --------
+void extr1(const HostGrid& g, double& F1, double& F2, int I, int J, int K, int I1, int J1, int K1, int I2, int J2, int K2, int IX) {
+    F2 = 0.0;
+    int ibc0 = g.at(I, J, K) % 10;
+    if (IX == 3) {
+        double d = g.Z[K2] - g.Z[K1];
+        if (d != 0.0) { int K0 = ibc0 == 2 ? (K + K1) / 2 : K; F2 = (g.Z[K0] - g.Z[K1]) / d; }
+    } else if (IX == 2) {
+        double d = g.R[J2] - g.R[J1];
+        if (d != 0.0) { int J0 = ibc0 == 2 ? (J + J1) / 2 : J; F2 = (g.R[J0] - g.R[J1]) / d; }
+    } else if (IX == 1) {
+        double d = g.X[I2] - g.X[I1];
+        if (d != 0.0) { int I0 = ibc0 == 2 ? (I + I1) / 2 : I; F2 = (g.X[I0] - g.X[I1]) / d; }
+    }
+    F1 = 1.0 - F2;
+}
+bool ext01(const HostGrid& g, bool wall, int I, int J, int K, int& I1, int& J1, int& K1, int& I2, int& J2, int& K2, int& IX) {
+    auto cl = [](int v, int hi) { return v < 2 ? 2 : (v > hi ? hi : v); };
+    for (IX = 1; IX <= 3; ++IX) {
+        int nx = IX == 1, ny = IX == 2, nz = IX == 3;
+        for (int M = -2; M <= 2; M += 4) {
+            I1 = cl(I + M * nx, g.MP); J1 = cl(J + M * ny, g.NP); K1 = cl(K + M * nz, g.LP);
+            bool hit = wall ? (g.at(I1, J1, K1) % 10 != 1) : (g.at(I1, J1, K1) <= 0);
+            if (hit) {
+                I2 = cl(I1 + M * nx, g.MP); J2 = cl(J1 + M * ny, g.NP); K2 = cl(K1 + M * nz, g.LP);
+                if (g.at(I2, J2, K2) % 10 == 1) { I2 = I1; J2 = J1; K2 = K1; }
+                return true;
+            }
+        }
+    }
+    IX = 4;
+    I2 = I1; J2 = J1; K2 = K1;
+    return false;
+}
+
+int build_tables(gfm_handle* h, const gfm_grid* gr, std::vector<int>& wall_list, std::vector<ExtrRec>& io,
+                 std::vector<ExtrRec>& walls, std::vector<ExtrRec>& ft, std::vector<int>& ft_start,
+                 std::vector<ExtrvRec>& ev, int nev[3], std::vector<Patch>& patches, std::vector<int>& cp_start,
+                 std::vector<int>& cp_list, std::vector<int8_t>& intp_mode_split) {
+    const HostGrid& g = h->hg;
+    const int MP = g.MP, NP = g.NP, LP = g.LP;
+    // ---- wall positions of the wall-function pass (Gflow.f90:67-130)
+    for (int K = 2; K <= LP; ++K)
+        for (int J = 2; J <= NP; ++J)
+            for (int I = 2; I <= MP; ++I) {
+                if (g.at(I, J, K) != 1) continue;
+                const int dirs[6][4] = {{1, 0, 0, 1}, {0, 1, 0, 1}, {0, 0, 1, 1}, {0, 0, 1, -1}, {0, 1, 0, -1}, {1, 0, 0, -1}};
+                for (int q = 0; q < 6; ++q) {
+                    int s = dirs[q][3];
+                    int In = I + s * dirs[q][0], Jn = J + s * dirs[q][1], Kn = K + s * dirs[q][2];
+                    if (In < 2 || In > MP || Jn < 2 || Jn > NP || Kn < 2 || Kn > LP) continue;
+                    if (g.at(In, Jn, Kn) >= 1) continue;
+                    int If = In + 2 * s * dirs[q][0], Jf = Jn + 2 * s * dirs[q][1], Kf = Kn + 2 * s * dirs[q][2];
+                    if (If < 1 || If > MP || Jf < 1 || Jf > NP || Kf < 1 || Kf > LP || g.at(If, Jf, Kf) == 1) {
+                        h->err = "geometry: wall-function extrapolation point is a wall (channel narrower than 2 cells)";
+                        return GFM_E_UNSUPPORTED;
+                    }
+                }
+                wall_list.push_back(I); wall_list.push_back(J); wall_list.push_back(K);
+            }
+    // ---- EXTR records (Extr.f90:31-250)
+    for (int I = 2; I <= MP; I += 2)
+        for (int J = 2; J <= NP; J += 2)
+            for (int K = 2; K <= LP; K += 2) {
+                int b = g.at(I, J, K) % 10;
+                if (b != 2 && b != 3) continue;
+                ExtrRec e{};
+                e.I = I; e.J = J; e.K = K; e.kind = b;
+                if (!ext01(g, false, I, J, K, e.I1, e.J1, e.K1, e.I2, e.J2, e.K2, e.IX)) {
+                    h->err = "geometry: inlet/exit cell without an open neighbour";
+                    return GFM_E_UNSUPPORTED;
+                }
+                if (g.at(e.I2, e.J2, e.K2) > 0) {
+                    h->err = "geometry: inlet/exit extrapolation reads another boundary cell";
+                    return GFM_E_UNSUPPORTED;
+                }
+                extr1(g, e.F1, e.F2, I, J, K, e.I1, e.J1, e.K1, e.I2, e.J2, e.K2, e.IX);
+                e.I3 = (I + e.I1) / 2; e.J3 = (J + e.J1) / 2; e.K3 = (K + e.K1) / 2;
+                io.push_back(e);
+            }
+    std::vector<std::vector<ExtrRec>> cols;
+    std::vector<long> col_key;
+    for (int I = 2; I <= MP; I += 2)
+        for (int J = 2; J <= NP; J += 2) {
+            std::vector<ExtrRec> col;
+            for (int K = 2; K <= LP; K += 2) {
+                if (g.at(I, J, K) % 10 != 1) continue;
+                ExtrRec e{};
+                e.I = I; e.J = J; e.K = K; e.kind = 1;
+                bool found = ext01(g, true, I, J, K, e.I1, e.J1, e.K1, e.I2, e.J2, e.K2, e.IX);
+                extr1(g, e.F1, e.F2, I, J, K, e.I1, e.J1, e.K1, e.I2, e.J2, e.K2, e.IX);
+                if (found) walls.push_back(e); else col.push_back(e);
+            }
+            if (!col.empty()) cols.push_back(col);
+        }
+    ft_start.push_back(0);
+    for (auto& col : cols) {
+        for (auto& e : col) ft.push_back(e);
+        ft_start.push_back((int)ft.size());
+    }
+    // ---- EXTRV records (Extr.f90:358-567), per direction in loop order
+    std::vector<char> wmark((size_t)MP * NP * LP * 3, 0);
+    auto lin = [&](int i, int j, int k) { return (size_t)(i - 1) + (size_t)MP * ((j - 1) + (size_t)NP * (k - 1)); };
+    for (int IU = 1; IU <= 3; ++IU) {
+        int cnt = 0;
+        std::vector<size_t> writes, reads;
+        auto visit = [&](int I, int J, int K) {
+            if (g.at(I, J, K) % 10 != 3) return;
+            ExtrvRec e{};
+            e.I = I; e.J = J; e.K = K; e.IU = IU; e.mode = 2;
+            for (int M = -1; M <= 1; M += 2) {
+                int In = I + (IU == 1) * M, Jn = J + (IU == 2) * M, Kn = K + (IU == 3) * M;
+                if (g.at(In, Jn, Kn) >= 1) continue;
+                e.mode = 0; e.m = M;
+                break;
+            }
+            if (e.mode == 0) {
+                int I1 = I + (IU == 1) * 2 * e.m, J1 = J + (IU == 2) * 2 * e.m, K1 = K + (IU == 3) * 2 * e.m;
+                int I0 = I - (IU == 1) * e.m, J0 = J - (IU == 2) * e.m, K0 = K - (IU == 3) * e.m;
+                writes.push_back(lin(I1, J1, K1));
+                if (IU != 3) { writes.push_back(lin(I, J, K)); writes.push_back(lin(I0, J0, K0)); }
+            } else {
+                // fallback copies in the reference's priority order
+                int Is = 0, Js = 0, Ks = 0;
+                bool ok = false;
+                if (IU == 1) {
+                    if (J > 2 && g.at(I, J - 2, K) <= 0) { Is = I; Js = J - 2; Ks = K; ok = true; }
+                    else if (J < NP && g.at(I, J + 2, K) <= 0) { Is = I; Js = J + 2; Ks = K; ok = true; }
+                    else if (K > 2 && g.at(I, J, K - 2) <= 0) { Is = I; Js = J; Ks = K - 2; ok = true; }
+                    else if (K < LP && g.at(I, J, K + 2) <= 0) { Is = I; Js = J; Ks = K + 2; ok = true; }
+                } else if (IU == 2) {
+                    if (K > 2 && g.at(I, J, K - 2) <= 0) { Is = I; Js = J; Ks = K - 2; ok = true; }
+                    else if (K < LP && g.at(I, J, K + 2) <= 0) { Is = I; Js = J; Ks = K + 2; ok = true; }
+                    else if (I > 2 && g.at(I - 2, J, K) <= 0) { Is = I - 2; Js = J; Ks = K; ok = true; }
+                    else if (I < MP && g.at(I + 2, J, K) <= 0) { Is = I + 2; Js = J; Ks = K; ok = true; }
+                } else {
+                    if (I > 2 && g.at(I - 2, J, K) <= 0) { Is = I - 2; Js = J; Ks = K; ok = true; }
+                    else if (I < MP && g.at(I + 2, J, K) <= 0) { Is = I + 2; Js = J; Ks = K; ok = true; }
+                    else if (J > 2 && g.at(I, J - 2, K) <= 0) { Is = I; Js = J - 2; Ks = K; ok = true; }
+                    else if (J < NP && g.at(I, J + 2, K) <= 0) { Is = I; Js = J + 2; Ks = K; ok = true; }
+                }
+                if (ok) {
+                    e.mode = 1; e.Is = Is; e.Js = Js; e.Ks = Ks;
+                    writes.push_back(lin(I, J, K));
+                    reads.push_back(lin(Is, Js, Ks));
+                }
+            }
+            ev.push_back(e);
+            ++cnt;
+        };
+        if (IU == 1) { for (int I = 3; I <= MP - 1; I += 2) for (int J = 2; J <= NP; J += 2) for (int K = 2; K <= LP; K += 2) visit(I, J, K); }
+        else if (IU == 2) { for (int J = 3; J <= NP - 1; J += 2) for (int K = 2; K <= LP; K += 2) for (int I = 2; I <= MP; I += 2) visit(I, J, K); }
+        else { for (int K = 3; K <= LP - 1; K += 2) for (int I = 2; I <= MP; I += 2) for (int J = 2; J <= NP; J += 2) visit(I, J, K); }
+        for (size_t w : writes) {
+            if (wmark[w * 3 + IU - 1]) { h->err = "geometry: exit faces write one velocity twice"; return GFM_E_UNSUPPORTED; }
+            wmark[w * 3 + IU - 1] = 1;
+        }
+        for (size_t r : reads)
+            if (wmark[r * 3 + IU - 1]) { h->err = "geometry: exit face copy reads a rescaled velocity"; return GFM_E_UNSUPPORTED; }
+        nev[IU - 1] = cnt;
+    }
+    // ---- wall patches and the per-cell patch lists (Qwall.f90:395-513)
+    cp_start.assign((size_t)h->CB + 1, 0);
+    std::vector<std::vector<int>> per_cell;
+    std::vector<long long> cell_of;
+    std::vector<int> counts((size_t)h->CB, 0);
+    for (int n = 0; n < gr->b_cnt; ++n) {
+        int typ = gr->b_typ[n];
+        if (typ != 1 && typ != 4) continue;
+        int bi = gr->b_i[n], bj = gr->b_j[n], bk = gr->b_k[n];
+        Patch q{};
+        q.inc = bi; q.jnc = bj; q.knc = bk;
+        if (gr->b_orient[n] == 1) {
+            if (gr->b_direct[n] == 0) { q.inc = bi + 1; q.ds_q = g.X[bi + 1] - g.X[bi]; } else { q.inc = bi - 1; q.ds_q = g.X[bi] - g.X[bi - 1]; }
+            q.ds_src = g.DX[q.inc];
+            q.area = g.DR[bj] * g.DZ[bk];
+        } else if (gr->b_orient[n] == 2) {
+            if (gr->b_direct[n] == 0) { q.jnc = bj + 1; q.ds_q = g.R[bj + 1] - g.R[bj]; } else { q.jnc = bj - 1; q.ds_q = g.R[bj] - g.R[bj - 1]; }
+            q.ds_src = g.DR[q.jnc];
+            q.area = g.DX[bi] * g.DZ[bk];
+        } else {
+            if (gr->b_direct[n] == 0) { q.knc = bk + 1; q.ds_q = g.Z[bk + 1] - g.Z[bk]; } else { q.knc = bk - 1; q.ds_q = g.Z[bk] - g.Z[bk - 1]; }
+            q.ds_src = g.DZ[q.knc];
+            q.area = g.DX[bi] * g.DR[bj];
+        }
+        q.bT = gr->b_t[n];
+        if ((q.inc & 1) || (q.jnc & 1) || (q.knc & 1)) { h->err = "geometry: wall patch not next to a cell centre"; return GFM_E_UNSUPPORTED; }
+        long long o = pidx(h->gd, q.inc, q.jnc, q.knc);
+        counts[(size_t)o]++;
+        patches.push_back(q);
+    }
+    for (long long o = 0; o < h->CB; ++o) cp_start[(size_t)o + 1] = cp_start[(size_t)o] + counts[(size_t)o];
+    cp_list.assign(patches.size(), 0);
+    std::vector<int> fill(cp_start.begin(), cp_start.end() - 1);
+    for (size_t n = 0; n < patches.size(); ++n) {
+        long long o = pidx(h->gd, patches[n].inc, patches[n].jnc, patches[n].knc);
+        cp_list[(size_t)fill[(size_t)o]++] = (int)n;
+    }
+    // ---- INTP carried-F1 codes (Intp.f90:32-72, 145-175)
+    intp_mode_split.assign((size_t)h->NS, 0);
+    auto setm = [&](int I, int J, int K, int m) { intp_mode_split[(size_t)pidx(h->gd, I, J, K)] = (int8_t)m; };
+    auto step = [&](int& cf, int I, int J, int K, int I1, int J1, int K1, int I2, int J2, int K2) {
+        int b = g.at(I, J, K);
+        if (b == 1 || b == 3) return;
+        if (b == 2) {
+            if (g.at(I1, J1, K1) == 2 && g.at(I2, J2, K2) == 0) cf = 2;
+            else if (g.at(I1, J1, K1) == 0 && g.at(I2, J2, K2) == 2) cf = 3;
+        }
+        setm(I, J, K, cf);
+    };
+    for (int I = 2; I <= MP; I += 2) {
+        for (int K = 3; K <= LP - 1; K += 2) {
+            int cf = 1;
+            for (int J = 2; J <= NP; J += 2) step(cf, I, J, K, I, J, K + 1, I, J, K - 1);
+        }
+        for (int J = 3; J <= NP - 1; J += 2) {
+            int cf = 1;
+            for (int K = 2; K <= LP; ++K) step(cf, I, J, K, I, J + 1, K, I, J - 1, K);
+        }
+    }
+    for (int I = 3; I <= MP - 1; I += 2) {
+        int cf = 1;
+        for (int K = 2; K <= LP; ++K)
+            for (int J = 2; J <= NP; ++J) step(cf, I, J, K, I + 1, J, K, I - 1, J, K);
+    }
+    // ---- pressure re-reference indices (Gflow.f90:182-242)
+    {
+        int I = gr->i_ref, J = gr->j_ref, K = gr->k_ref, I1 = I, J1 = J, K1 = K, I2 = I, J2 = J, K2 = K, NX = 0;
+        int MPM2 = MP - 2, NPM2 = NP - 2, LPM2 = LP - 2;
+        if (I < MPM2 && g.at(I + 2, J, K) == 0) { NX = 1; I1 = I + 2; I2 = g.at(I + 4, J, K) == 0 ? I + 4 : I1; }
+        else if (I > 2 && g.at(I - 2, J, K) == 0) { NX = 1; I1 = I - 2; I2 = g.at(I - 4, J, K) == 0 ? I - 4 : I1; }
+        else if (J < NPM2 && g.at(I, J + 2, K) == 0) { NX = 2; J1 = J + 2; J2 = (J < NPM2 && g.at(I, J + 4, K) <= 0) ? J + 4 : J1; }
+        else if (J > 2 && g.at(I, J - 2, K) <= 0) { NX = 2; J1 = J - 2; J2 = (J > 4 && g.at(I, J - 4, K) <= 0) ? J - 4 : J1; }
+        else if (K < LPM2 && g.at(I, J, K + 2) <= 0) { NX = 3; K1 = K + 2; K2 = (K < LPM2 && g.at(I, J, K + 4) <= 0) ? K + 4 : K1; }
+        else if (K > 2 && g.at(I, J, K - 2) <= 0) { NX = 3; K1 = K - 2; K2 = (K > 4 && g.at(I, J, K - 4) <= 0) ? K - 4 : K1; }
+        extr1(g, h->pref_f1, h->pref_f2, I, J, K, I1, J1, K1, I2, J2, K2, NX);
+        h->pref_i1 = I1; h->pref_j1 = J1; h->pref_k1 = K1; h->pref_i2 = I2; h->pref_j2 = J2; h->pref_k2 = K2;
+    }
+    return GFM_OK;
+}
+
+template <typename R>
+int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gfm_grid* gr) {
+    const HostGrid& hg = h->hg;
+    // geometry in R
+    auto up1 = [&](const std::vector<double>& v, const R** out) -> int {
+        std::vector<R> t(v.begin(), v.end());
+        R* p = nullptr;
+        int rc = dupload(h, &p, t);
+        *out = p;
+        return rc;
+    };
+    const int8_t* ib_shared = h->gd.ib;
+    g = GeoT<R>{};
+    g.MP = hg.MP; g.NP = hg.NP; g.LP = hg.LP;
+    g.HX = hg.MP / 2 + 1; g.HY = hg.NP / 2 + 1; g.HZ = hg.LP / 2 + 1;
+    g.PX = ((g.HX + 15) / 16) * 16;
+    g.CB = (long long)g.PX * g.HY * g.HZ;
+    g.MPM1 = hg.MP - 1; g.MPM2 = hg.MP - 2; g.NPM1 = hg.NP - 1; g.NPM2 = hg.NP - 2; g.LPM1 = hg.LP - 1; g.LPM2 = hg.LP - 2;
+    g.NJY1 = 4; g.NJY2 = g.NPM2; g.LKZ1 = 4; g.LKZ2 = g.LPM2;
+    g.NJY1V[1] = 4; g.NJY2V[1] = g.NPM2; g.NJY1V[2] = 5; g.NJY2V[2] = hg.NP - 3; g.NJY1V[3] = 4; g.NJY2V[3] = g.NPM2;
+    g.LKZ1V[1] = 4; g.LKZ2V[1] = g.LPM2; g.LKZ1V[2] = 4; g.LKZ2V[2] = g.LPM2; g.LKZ1V[3] = 5; g.LKZ2V[3] = hg.LP - 3;
+    g.NCELLS = h->ncells;
+    int rc;
+    if ((rc = up1(hg.X, &g.X)) || (rc = up1(hg.DX, &g.DX)) || (rc = up1(hg.R, &g.Rr)) || (rc = up1(hg.DR, &g.DR)) ||
+        (rc = up1(hg.RS, &g.RS)) || (rc = up1(hg.Z, &g.Z)) || (rc = up1(hg.DZ, &g.DZ)))
+        return rc;
+    g.ib = ib_shared;   // shared int8 map
+    c.g = g;
+    const long long NS = h->NS, CB = h->CB;
+    R** full[] = {&c.P, &c.T, &c.DNST, &c.THETA, &c.TMU, &c.GAMA, &c.CRATE, &c.HRATE, &c.GTE, &c.BSH, &c.FZ,
+                  &c.APm, &c.BSm, &c.SFPm, &c.UG[0], &c.UG[1], &c.UG[2]};
+    for (R** p : full) if ((rc = dalloc(h, p, NS))) return rc;
+    for (int l = 0; l < 9; ++l) {
+        if (l == 7) { c.GF[l] = nullptr; continue; }
+        if ((rc = dalloc(h, &c.GF[l], NS))) return rc;
+    }
+    for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASm[q], NS))) return rc;
+    R** cent[] = {&c.APc, &c.BSp, &c.BSq, &c.QA, &c.QE};
+    for (R** p : cent) if ((rc = dalloc(h, p, CB))) return rc;
+    for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASc[q], CB))) return rc;
+    for (int l = 0; l < 7; ++l) {
+        if ((rc = dalloc(h, &c.APs[l], CB)) || (rc = dalloc(h, &c.BSs[l], CB)) || (rc = dalloc(h, &c.FZs[l], CB)) ||
+            (rc = dalloc(h, &c.SFPs[l], CB)))
+            return rc;
+    }
+    for (int s = 0; s < 3; ++s)
+        for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASs[s][q], CB))) return rc;
+    for (int e = 0; e < 8; ++e)
+        if ((rc = dalloc(h, &scr[e].xt2, NS)) || (rc = dalloc(h, &scr[e].xt3, NS)) || (rc = dalloc(h, &scr[e].pty, NS)) ||
+            (rc = dalloc(h, &scr[e].ptz, NS)))
+            return rc;
+    if ((rc = dalloc(h, &c.qconv, gr->b_cnt > 0 ? gr->b_cnt : 1))) return rc;
+    return GFM_OK;
+}
+
+template <typename R>
+void fill_ctx_common(gfm_handle* h, Ctx<R>& c, const Ctx<double>& src) {
+    c.p = src.p;
+    c.rtim = src.rtim; c.delrt = src.delrt; c.delr = src.delr; c.timed = src.timed; c.nr0 = src.nr0;
+    c.extr_io = src.extr_io; c.extr_wall = src.extr_wall; c.extr_ft = src.extr_ft;
+    c.n_extr_io = src.n_extr_io; c.n_extr_wall = src.n_extr_wall; c.n_extr_ft = src.n_extr_ft;
+    c.ft_col_start = src.ft_col_start; c.n_ft_cols = src.n_ft_cols;
+    c.extrv = src.extrv;
+    for (int d = 0; d < 3; ++d) c.n_extrv[d] = src.n_extrv[d];
+    c.patch = src.patch; c.cell_patch_start = src.cell_patch_start; c.cell_patch_list = src.cell_patch_list;
+    c.n_patch = src.n_patch; c.n_patch_cells = src.n_patch_cells;
+    c.intp_mode = src.intp_mode; c.scal = src.scal; c.partials = src.partials;
+    c.nwl = src.nwl;
+    for (int l = 0; l < 16; ++l) { c.wl[l] = src.wl[l]; c.akl0[l] = src.akl0[l]; }
+    c.i_ref = src.i_ref; c.j_ref = src.j_ref; c.k_ref = src.k_ref; c.p_ref = src.p_ref;
+    for (int l = 0; l < 7; ++l) c.as_set[l] = src.as_set[l];
+    c.nist = src.nist;
+    (void)h;
+}
+
+// ---- one GFLOW ------------------------------------------------------------------
+template <typename R>
+Sys<R> sys_of(R* xt, const R* ap, R* const* as, const R* bs, int ib, int ie, int jb, int je, int kb, int ke, int nim) {
+    Sys<R> s;
+    s.xt = xt; s.ap = ap;
+    for (int q = 0; q < 6; ++q) s.as[q] = as[q];
+    s.bs = bs;
+    s.ib = ib; s.ie = ie; s.jb = jb; s.je = je; s.kb = kb; s.ke = ke; s.nim = nim;
+    return s;
+}
+
+template <typename R>
+void finish(gfm_handle* h, Ctx<R>& c, std::initializer_list<std::array<int, 3>> items) {
+    FinishSpec f{};
+    for (auto& it : items) { f.slot[f.n] = it[0]; f.dst[f.n] = it[1]; f.op[f.n] = it[2]; ++f.n; }
+    launch_finish(c.partials, c.scal, f, (double)h->ncells, h->stream);
+}
+
+template <typename R>
+int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
+    cudaStream_t st = h->stream;
+    const GeoT<R>& g = c.g;
+    const gfm_params& P = h->params;
+    c.itr_gas = h->itr_gas;
+    c.rad_active = h->rad_active;
+    cudaMemsetAsync(c.partials, 0, sizeof(double) * kRedSlots * kRedBlocks, st);
+    // wall functions (Gflow.f90:16-130)
+    launch_wallfn(c, h->d_wall, h->n_wall, st);
+    // GSLV3V: momentum coefficients and pseudo-velocities
+    launch_copy_faces_to_fz(c, st);
+    launch_mom_assemble(c, st);
+    // pressure equation
+    launch_p_assemble(c, st);
+    Sys<R> sp = sys_of<R>(c.P, c.APc, c.ASc, c.BSp, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[3]);
+    launch_residual(c, sp, SL_P_PRE, st);
+    cudaEventRecord(h->ev_adi0, st);
+    launch_adlbl3_scr(g, &sp, scr, 1, h->adi_mode, st);
+    launch_residual(c, sp, SL_P_POST, st);
+    launch_bound_p(c, st);
+    // momentum solves u, v, w (independent systems, one batch)
+    launch_mom_prep(c, st);
+    Sys<R> sm[3];
+    for (int iu = 1; iu <= 3; ++iu) {
+        int nx1 = iu == 1;
+        sm[iu - 1] = sys_of<R>(c.FZ, c.APm, c.ASm, c.BSm, 4 + nx1, g.MPM2 - nx1, g.NJY1V[iu], g.NJY2V[iu], g.LKZ1V[iu],
+                               g.LKZ2V[iu], P.ntimesg[iu - 1]);
+        launch_residual(c, sm[iu - 1], SL_U_PRE + iu - 1, st);
+    }
+    launch_adlbl3_scr(g, sm, scr, 3, h->adi_mode, st);
+    for (int iu = 0; iu < 3; ++iu) launch_residual(c, sm[iu], SL_U_POST + iu, st);
+    launch_mom_finish(c, st);
+    // pressure correction
+    launch_pcorr_source(c, st);
+    R* asc[6];
+    for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
+    Sys<R> spc = sys_of<R>(c.FZ, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[4]);
+    launch_adlbl3_scr(g, &spc, scr, 1, h->adi_mode, st);
+    launch_residual(c, spc, SL_PC_POST, st);
+    launch_velcorr(c, st);
+    // exit balance (EXTRV, FLX1D, FACTOR), INTPV
+    launch_extrv(c, 0, st);
+    finish(h, c, {{SL_GFEX, S_GFEX, 0}, {SL_TM, S_TMEAN_EX, 0}, {SL_TAREA, S_TAREA_MEAN, 0}, {SL_AREA, S_AREA_EX, 0}});
+    launch_factor(c, st);
+    launch_extrv(c, 1, st);
+    launch_intpv(c, st);
+    // pressure re-reference
+    launch_pref_idx(c, h->pref_i1, h->pref_j1, h->pref_k1, h->pref_i2, h->pref_j2, h->pref_k2, h->pref_f1, h->pref_f2, st);
+    // GSLV3G: scalar equations
+    if (P.wall_sink) launch_qconv(c, st);
+    launch_scalar_sources_first(c, st);
+    const int order[6] = {1, 2, 3, 4, 6, 7};
+    bool made[3] = {false, false, false};
+    Sys<R> ss[6];
+    for (int q = 0; q < 6; ++q) {
+        int L = order[q];
+        int set = c.as_set[L - 1];
+        launch_scalar_assemble(c, L, !made[set], st);
+        made[set] = true;
+        const int nelg = L == 1 ? 6 : L == 6 ? 7 : L == 3 ? 8 : L == 4 ? 9 : L == 5 ? 10 : L == 7 ? 11 : 12;
+        ss[q] = sys_of<R>(c.FZs[L - 1], c.APs[L - 1], c.ASs[set], c.BSs[L - 1], 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2,
+                          P.ntimesg[nelg - 1]);
+        launch_residual(c, ss[q], SL_GF_PRE + L - 1, st);
+    }
+    launch_adlbl3_scr(g, ss, scr, 6, h->adi_mode, st);
+    for (int q = 0; q < 6; ++q) {
+        int L = order[q];
+        launch_residual(c, ss[q], SL_GF_POST + L - 1, st);
+        launch_scalar_finish(c, L, st);
+    }
+    {
+        const int L = 5;
+        int set = c.as_set[L - 1];
+        launch_scalar_assemble(c, L, !made[set], st);
+        Sys<R> se = sys_of<R>(c.FZs[L - 1], c.APs[L - 1], c.ASs[set], c.BSs[L - 1], 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2,
+                              P.ntimesg[9]);
+        launch_residual(c, se, SL_GF_PRE + L - 1, st);
+        launch_adlbl3_scr(g, &se, scr, 1, h->adi_mode, st);
+        launch_residual(c, se, SL_GF_POST + L - 1, st);
+        launch_scalar_finish(c, L, st);
+    }
+    cudaEventRecord(h->ev_adi1, st);
+    // properties, mean temperature, boundary values, interpolation
+    launch_props(c, st);
+    launch_tave(c, st);
+    launch_extr(c, st);
+    launch_intp(c, st);
+    finish(h, c, {{SL_RESM, S_RES_MASS, 3}, {SL_RESMAX, S_RES_MASS_MAX, 1}, {SL_QCONV, S_QCONV, 0},
+                  {SL_QREACT, S_Q_REACT, 0}, {SL_TA, S_TAVE, 0}, {SL_TB, S_TAVE_DEN, 0},
+                  {SL_GFIN0, S_GFIN0, 0}, {SL_QEX, S_Q_EXHAUST, 0}});
+    FinishSpec f{};
+    auto add = [&](int slot, int dst, int op) { f.slot[f.n] = slot; f.dst[f.n] = dst; f.op[f.n] = op; ++f.n; };
+    add(SL_P_PRE, S_P_RESID_PRE, 2); add(SL_P_POST, S_P_RESID, 2); add(SL_PC_POST, S_PCORR_RESID, 2);
+    for (int i = 0; i < 3; ++i) { add(SL_U_PRE + i, S_U_RESID_PRE + i, 2); add(SL_U_POST + i, S_U_RESID + i, 2); }
+    for (int l = 0; l < 7; ++l) { add(SL_GF_PRE + l, S_GF_RESID_PRE + l, 2); add(SL_GF_POST + l, S_GF_RESID + l, 2); }
+    launch_finish(c.partials, c.scal, f, (double)h->ncells, st);
+    return GFM_OK;
+}
+
+template <typename R>
+int initsv_dev(gfm_handle* h, Ctx<R>& c) {
+    cudaStream_t st = h->stream;
+    cudaMemsetAsync(c.partials, 0, sizeof(double) * kRedSlots * kRedBlocks, st);
+    launch_intpv(c, st);
+    launch_extr(c, st);
+    launch_intp(c, st);
+    finish(h, c, {{SL_GFIN0, S_GFIN0, 0}, {SL_QEX, S_Q_EXHAUST, 0}});
+    return GFM_OK;
+}
+
+template <typename R>
+int upload_fields(gfm_handle* h, Ctx<R>& c, const gfm_fields* f) {
+    const long long N = h->N;
+    const GeoT<R>& g = c.g;
+    cudaStream_t st = h->stream;
+    auto put = [&](const double* src, R* dst) -> int {
+        if (!src) return GFM_OK;
+        CK(cudaMemcpyAsync(h->d_stage, src, N * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_to_split(g, h->d_stage, dst, st);
+        return GFM_OK;
+    };
+    int rc;
+    if ((rc = put(f->p, c.P)) || (rc = put(f->t, c.T)) || (rc = put(f->dnst, c.DNST)) || (rc = put(f->theta, c.THETA)) ||
+        (rc = put(f->tmu, c.TMU)) || (rc = put(f->gama, c.GAMA)) || (rc = put(f->crate, c.CRATE)) ||
+        (rc = put(f->hrate, c.HRATE)) || (rc = put(f->bs_hprev, c.BSH)))
+        return rc;
+    for (int l = 0; l < 3; ++l) if ((rc = put(f->ug ? f->ug + l * N : nullptr, c.UG[l]))) return rc;
+    for (int l = 0; l < 9; ++l) {
+        if (l == 7) continue;
+        if ((rc = put(f->gf ? f->gf + l * N : nullptr, c.GF[l]))) return rc;
+    }
+    long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    if (f->qa) { CK(cudaMemcpyAsync(h->d_stage, f->qa, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QA, st); }
+    if (f->qe) { CK(cudaMemcpyAsync(h->d_stage, f->qe, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QE, st); }
+    CK(cudaStreamSynchronize(st));
+    return GFM_OK;
+}
+
+template <typename R>
+int download_fields(gfm_handle* h, Ctx<R>& c, gfm_fields* f) {
+    const long long N = h->N;
+    const GeoT<R>& g = c.g;
+    cudaStream_t st = h->stream;
+    auto get = [&](const R* src, double* dst) -> int {
+        if (!dst) return GFM_OK;
+        launch_from_split(g, src, h->d_stage, st);
+        CK(cudaMemcpyAsync(dst, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return GFM_OK;
+    };
+    int rc;
+    if ((rc = get(c.P, f->p)) || (rc = get(c.T, f->t)) || (rc = get(c.DNST, f->dnst)) || (rc = get(c.THETA, f->theta)) ||
+        (rc = get(c.TMU, f->tmu)) || (rc = get(c.GAMA, f->gama)) || (rc = get(c.CRATE, f->crate)) ||
+        (rc = get(c.HRATE, f->hrate)) || (rc = get(c.BSH, f->bs_hprev)))
+        return rc;
+    for (int l = 0; l < 3; ++l) if ((rc = get(c.UG[l], f->ug ? f->ug + l * N : nullptr))) return rc;
+    for (int l = 0; l < 9; ++l) {
+        if (l == 7) { if (f->gf) std::memset(f->gf + 7 * N, 0, N * sizeof(double)); continue; }
+        if ((rc = get(c.GF[l], f->gf ? f->gf + l * N : nullptr))) return rc;
+    }
+    long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    if (f->qa) { launch_cells_from_split(g, c.QA, h->d_stage, st); CK(cudaMemcpyAsync(f->qa, h->d_stage, ncell * sizeof(double), cudaMemcpyDeviceToHost, st)); }
+    if (f->qe) { launch_cells_from_split(g, c.QE, h->d_stage, st); CK(cudaMemcpyAsync(f->qe, h->d_stage, ncell * sizeof(double), cudaMemcpyDeviceToHost, st)); }
+    CK(cudaStreamSynchronize(st));
+    f->itr_gas = h->itr_gas;
+    f->do_rad_qe_only_cnt = h->cnt_qe;
+    f->i1st_rad_qe_done = h->rad_active;
+    f->factor = h->h_scal[S_FACTOR];
+    f->fadj = h->h_scal[S_FADJ];
+    f->gfin0 = h->h_scal[S_GFIN0];
+    f->q_h_in = h->q_h_in;
+    return GFM_OK;
+}
+
+void fill_stats(gfm_handle* h, gfm_iter_stats* s, int converged) {
+    if (!s) return;
+    const double* v = h->h_scal;
+    std::memset(s, 0, sizeof *s);
+    s->itr_gas = h->itr_gas;
+    s->converged = converged;
+    s->res_mass = v[S_RES_MASS]; s->res_mass_max = v[S_RES_MASS_MAX];
+    s->p_resid_pre = v[S_P_RESID_PRE]; s->p_resid = v[S_P_RESID]; s->pcorr_resid = v[S_PCORR_RESID];
+    for (int i = 0; i < 3; ++i) { s->u_resid_pre[i] = v[S_U_RESID_PRE + i]; s->u_resid[i] = v[S_U_RESID + i]; }
+    for (int i = 0; i < 7; ++i) { s->gf_resid_pre[i] = v[S_GF_RESID_PRE + i]; s->gf_resid[i] = v[S_GF_RESID + i]; }
+    s->factor = v[S_FACTOR]; s->gfin = v[S_GFIN]; s->gfex = v[S_GFEX];
+    s->q_react = v[S_Q_REACT]; s->q_exhaust = v[S_Q_EXHAUST]; s->q_conv_total = v[S_QCONV];
+    double q_in_tot = v[S_Q_REACT] + h->q_h_in, q_out_tot = v[S_Q_EXHAUST];
+    s->q_global_bal = std::fabs((q_in_tot - q_out_tot) / q_in_tot);
+    double tb = v[S_TAVE_DEN];
+    s->tave = tb != 0.0 ? v[S_TAVE] * h->params.t0 / tb : 0.0;
+    s->tmean_ex = v[S_TMEAN_EX];
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" int gfm_gpu_device_count(void) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n < 1) return GFM_E_NODEVICE;
+    return n;
+}
+
+namespace {
+thread_local std::string g_create_err;
+int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out);
+}
+
+extern "C" int gfm_gpu_create(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
+    if (!out) return GFM_E_ARG;
+    *out = nullptr;
+    gfm_handle* h = nullptr;
+    int rc = create_impl(gr, prm, &h);
+    if (rc != GFM_OK) {
+        g_create_err = h ? h->err : std::string("invalid arguments or no CUDA device");
+        if (h) gfm_gpu_destroy(h);
+        return rc;
+    }
+    *out = h;
+    return GFM_OK;
+}
+
+namespace {
+int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
+    if (!gr || !prm || !out) return GFM_E_ARG;
+    *out = nullptr;
+    if (gr->mp < 8 || gr->np < 8 || gr->lp < 8 || (gr->mp & 1) || (gr->np & 1) || (gr->lp & 1)) return GFM_E_ARG;
+    if (gr->nwl < 1 || gr->nwl > 16 || gr->nr0 < 2) return GFM_E_ARG;
+    if (prm->precision != GFM_PREC_FP64 && prm->precision != GFM_PREC_MIXED) return GFM_E_ARG;
+    if (prm->adi_mode != GFM_ADI_MARCH && prm->adi_mode != GFM_ADI_REDBLACK) return GFM_E_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return GFM_E_NODEVICE;
+    gfm_handle* h = new (std::nothrow) gfm_handle();
+    if (!h) return GFM_E_NOMEM;
+    *out = h;
+    h->prec = prm->precision;
+    h->adi_mode = prm->adi_mode;
+    h->params = *prm;
+    HostGrid& hg = h->hg;
+    hg.MP = gr->mp; hg.NP = gr->np; hg.LP = gr->lp;
+    h->N = (long long)hg.MP * hg.NP * hg.LP;
+    hg.ib.assign(gr->ibcell, gr->ibcell + h->N);
+    for (long long i = 0; i < h->N; ++i)
+        if (hg.ib[i] < 0 || hg.ib[i] > 20) { h->err = "IBCELL: half-blocked cells are not supported"; return GFM_E_UNSUPPORTED; }
+    auto one_based = [](const double* s, int n) { std::vector<double> v(n + 3, 0.0); for (int i = 0; i < n; ++i) v[i + 1] = s[i]; return v; };
+    hg.X = one_based(gr->x, hg.MP); hg.DX = one_based(gr->dx, hg.MP);
+    hg.R = one_based(gr->r, hg.NP); hg.DR = one_based(gr->dr, hg.NP); hg.RS = one_based(gr->rs, hg.NP);
+    hg.Z = one_based(gr->z, hg.LP); hg.DZ = one_based(gr->dz, hg.LP);
+    h->ncells = gr->ncells;
+    cudaError_t ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { h->err = cudaGetErrorString(ce); return GFM_E_CUDA; }
+    cudaEventCreate(&h->ev_adi0);
+    cudaEventCreate(&h->ev_adi1);
+    // double geometry first: its int8 map is shared by the float copy
+    GeoT<double>& g = h->gd;
+    g.MP = hg.MP; g.NP = hg.NP; g.LP = hg.LP;
+    g.HX = hg.MP / 2 + 1; g.HY = hg.NP / 2 + 1; g.HZ = hg.LP / 2 + 1;
+    g.PX = ((g.HX + 15) / 16) * 16;
+    g.CB = (long long)g.PX * g.HY * g.HZ;
+    h->CB = g.CB;
+    h->NS = 8 * g.CB;
+    {
+        std::vector<int8_t> ibs((size_t)h->NS, 1);
+        for (int K = 1; K <= hg.LP; ++K)
+            for (int J = 1; J <= hg.NP; ++J)
+                for (int I = 1; I <= hg.MP; ++I) ibs[(size_t)pidx(g, I, J, K)] = (int8_t)hg.at(I, J, K);
+        int8_t* d = nullptr;
+        int rc = dupload(h, &d, ibs);
+        if (rc) return rc;
+        g.ib = d;
+    }
+    std::vector<int> wall_list, ft_start, cp_start, cp_list;
+    std::vector<ExtrRec> io, walls, ft;
+    std::vector<ExtrvRec> ev;
+    std::vector<Patch> patches;
+    std::vector<int8_t> intp_mode;
+    int nev[3] = {0, 0, 0};
+    int rc = build_tables(h, gr, wall_list, io, walls, ft, ft_start, ev, nev, patches, cp_start, cp_list, intp_mode);
+    if (rc) return rc;
+    Ctx<double>& c = h->cd;
+    // tables shared by both precisions (kept in the double context)
+    std::vector<double> rt(gr->rtim, gr->rtim + gr->nr0), dr(gr->delrt, gr->delrt + gr->nr0),
+        dl(gr->delr, gr->delr + gr->nr0), tm(gr->timed, gr->timed + gr->nr0);
+    double *p1, *p2, *p3, *p4;
+    if ((rc = dupload(h, &p1, rt)) || (rc = dupload(h, &p2, dr)) || (rc = dupload(h, &p3, dl)) || (rc = dupload(h, &p4, tm))) return rc;
+    c.rtim = p1; c.delrt = p2; c.delr = p3; c.timed = p4; c.nr0 = gr->nr0;
+    ExtrRec *e1, *e2, *e3;
+    ExtrvRec* e4;
+    Patch* pp;
+    int *i1, *i2, *i3;
+    int8_t* im;
+    if ((rc = dupload(h, &e1, io)) || (rc = dupload(h, &e2, walls)) || (rc = dupload(h, &e3, ft)) || (rc = dupload(h, &e4, ev)) ||
+        (rc = dupload(h, &pp, patches)) || (rc = dupload(h, &i1, ft_start)) || (rc = dupload(h, &i2, cp_start)) ||
+        (rc = dupload(h, &i3, cp_list)) || (rc = dupload(h, &im, intp_mode)) || (rc = dupload(h, &h->d_wall, wall_list)))
+        return rc;
+    h->n_wall = (int)wall_list.size() / 3;
+    c.extr_io = e1; c.extr_wall = e2; c.extr_ft = e3; c.n_extr_io = (int)io.size(); c.n_extr_wall = (int)walls.size();
+    c.n_extr_ft = (int)ft.size(); c.ft_col_start = i1; c.n_ft_cols = (int)ft_start.size() - 1;
+    c.extrv = e4;
+    for (int d = 0; d < 3; ++d) c.n_extrv[d] = nev[d];
+    c.patch = pp; c.cell_patch_start = i2; c.cell_patch_list = i3; c.n_patch = (int)patches.size();
+    c.intp_mode = im;
+    if ((rc = dalloc(h, &c.scal, S_NUM + 128)) || (rc = dalloc(h, &c.partials, (long long)kRedSlots * kRedBlocks)) ||
+        (rc = dalloc(h, &h->d_stage, h->N)))
+        return rc;
+    {
+        Nist* dn = nullptr;
+        std::vector<Nist> v(1, nist_host());
+        if ((rc = dupload(h, &dn, v))) return rc;
+        c.nist = dn;
+    }
+    if (cudaMallocHost(&h->h_scal, sizeof(double) * (S_NUM + 128)) != cudaSuccess) return GFM_E_NOMEM;
+    std::memset(h->h_scal, 0, sizeof(double) * (S_NUM + 128));
+    // constants
+    Prm& p = c.p;
+    p.t0 = prm->t0; p.h_0 = prm->h_0; p.dnst0 = prm->dnst0; p.ug0 = prm->ug0; p.gmfr = prm->gmfr; p.pg0 = prm->pg0; p.r0 = prm->r0;
+    p.reyg = prm->reyg; p.reyg2 = prm->reyg2; p.epsr = prm->epsr; p.taur = prm->taur; p.eun = prm->eun; p.qr0 = prm->qr0;
+    p.q0 = prm->q0; p.tk0 = prm->tk0;
+    for (int i = 0; i < 3; ++i) p.gra[i] = prm->gra[i];
+    p.amu = prm->amu; p.trdg = prm->trdg; p.wt0 = prm->wt0; p.stoich = prm->stoich;
+    p.cmu = prm->cmu; p.ct1 = prm->ct1; p.ct2 = prm->ct2;
+    p.p_mx = prm->p_mx; p.p_mn = prm->p_mn; p.t_mx = prm->t_mx; p.t_mn = prm->t_mn; p.u_mx = prm->u_mx; p.u_mn = prm->u_mn;
+    p.f_mx = prm->f_mx; p.f_mn = prm->f_mn;
+    for (int i = 0; i < 21; ++i) { p.rf[i] = prm->rf[i]; p.rfc[i] = 1.0 - prm->rf[i]; p.rfl[i] = prm->rfl[i]; p.rflc[i] = 1.0 - prm->rfl[i]; }
+    for (int i = 0; i < 12; ++i) p.sigma[i] = prm->sigma[i];
+    p.rf_hsource = prm->rf_hsource; p.h_g = prm->h_g;
+    p.sig = prm->sig; p.ri = prm->ri; p.hck = prm->hck;
+    p.react = prm->react; p.wall_sink = prm->wall_sink;
+    c.nwl = gr->nwl;
+    for (int l = 0; l < gr->nwl; ++l) { c.wl[l] = gr->wl[l]; c.akl0[l] = gr->akl0[l]; }
+    c.i_ref = gr->i_ref; c.j_ref = gr->j_ref; c.k_ref = gr->k_ref; c.p_ref = gr->p_ref;
+    // coefficient sets by sigma: equations with equal sigma share one set
+    {
+        double sv[3];
+        int ns = 0;
+        for (int L = 1; L <= 7; ++L) {
+            int s = -1;
+            for (int q = 0; q < ns; ++q) if (sv[q] == prm->sigma[L - 1]) s = q;
+            if (s < 0) { if (ns == 3) { h->err = "more than three distinct sigma values"; return GFM_E_UNSUPPORTED; } sv[ns] = prm->sigma[L - 1]; s = ns++; }
+            c.as_set[L - 1] = s;
+        }
+    }
+    if (h->prec == GFM_PREC_FP64) {
+        if ((rc = setup_ctx<double>(h, c, h->gd, h->scr_d, gr))) return rc;
+    } else {
+        fill_ctx_common(h, h->cf, c);
+        h->gfl.ib = g.ib;
+        if ((rc = setup_ctx<float>(h, h->cf, h->gfl, h->scr_f, gr))) return rc;
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    return GFM_OK;
+}
+}  // namespace
+
+extern "C" int gfm_gpu_upload(gfm_handle* h, const gfm_fields* f) {
+    if (!h || !f) return GFM_E_ARG;
+    h->itr_gas = f->itr_gas;
+    h->cnt_qe = f->do_rad_qe_only_cnt;
+    h->rad_active = f->i1st_rad_qe_done;
+    h->q_h_in = f->q_h_in;
+    h->h_scal[S_FACTOR] = f->factor;
+    h->h_scal[S_FADJ] = f->fadj;
+    h->h_scal[S_GFIN0] = f->gfin0;
+    double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
+    cudaError_t e = cudaMemcpy(scal, h->h_scal, sizeof(double) * (S_NUM + 128), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    return h->prec == GFM_PREC_FP64 ? upload_fields(h, h->cd, f) : upload_fields(h, h->cf, f);
+}
+
+extern "C" int gfm_gpu_initsv(gfm_handle* h) {
+    if (!h) return GFM_E_ARG;
+    int rc = h->prec == GFM_PREC_FP64 ? initsv_dev(h, h->cd) : initsv_dev(h, h->cf);
+    if (rc) return rc;
+    double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
+    cudaError_t e = cudaMemcpyAsync(h->h_scal, scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    return GFM_OK;
+}
+
+extern "C" int gfm_gpu_gflow(gfm_handle* h, int n_iter, gfm_iter_stats* out, int* n_done) {
+    if (!h || n_iter < 0) return GFM_E_ARG;
+    int done = 0, conv = 0;
+    for (int it = 0; it < n_iter; ++it) {
+        h->itr_gas += 1;
+        int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
+        if (rc) return rc;
+        double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
+        cudaError_t e = cudaMemcpyAsync(h->h_scal, scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->ev_adi0, h->ev_adi1) == cudaSuccess) h->adi_ms += ms;
+        ++done;
+        if (!std::isfinite(h->h_scal[S_RES_MASS])) { h->err = "res_mass is not finite"; if (n_done) *n_done = done; fill_stats(h, out, 0); return GFM_E_NAN; }
+        if (h->h_scal[S_RES_MASS] < h->params.bgcon) { conv = 1; break; }
+        if (h->params.rad_emission) {
+            h->cnt_qe += 1;
+            if (h->cnt_qe >= h->params.rad_qe_frequency && h->itr_gas > 50) {
+                if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
+                else launch_rad_emission(h->cf, h->stream);
+                h->rad_active = 1;
+                h->cnt_qe = 0;
+            }
+        }
+    }
+    fill_stats(h, out, conv);
+    if (n_done) *n_done = done;
+    return GFM_OK;
+}
+
+extern "C" int gfm_gpu_download(gfm_handle* h, gfm_fields* f) {
+    if (!h || !f) return GFM_E_ARG;
+    return h->prec == GFM_PREC_FP64 ? download_fields(h, h->cd, f) : download_fields(h, h->cf, f);
+}
+
+extern "C" int gfm_gpu_rad_emission(gfm_handle* h) {
+    if (!h) return GFM_E_ARG;
+    if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
+    else launch_rad_emission(h->cf, h->stream);
+    h->rad_active = 1;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    return GFM_OK;
+}
+
+namespace {
+template <typename R>
+int adlbl3_user(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, double* xt, const double* ap, const double* const as[6],
+                const double* bs, int ib, int ie, int jb, int je, int kb, int ke, int nim) {
+    const GeoT<R>& g = c.g;
+    cudaStream_t st = h->stream;
+    const long long N = h->N;
+    // the user system lives in the momentum coefficient arrays and FZ
+    auto put = [&](const double* src, R* dst) -> int {
+        CK(cudaMemcpyAsync(h->d_stage, src, N * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_to_split(g, h->d_stage, dst, st);
+        return GFM_OK;
+    };
+    int rc;
+    if ((rc = put(xt, c.FZ)) || (rc = put(ap, c.APm)) || (rc = put(bs, c.BSm))) return rc;
+    for (int q = 0; q < 6; ++q) if ((rc = put(as[q], c.ASm[q]))) return rc;
+    Sys<R> s = sys_of<R>(c.FZ, c.APm, c.ASm, c.BSm, ib, ie, jb, je, kb, ke, nim);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st);
+    launch_from_split(g, c.FZ, h->d_stage, st);
+    CK(cudaMemcpyAsync(xt, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GFM_OK;
+}
+}  // namespace
+
+extern "C" int gfm_gpu_adlbl3(gfm_handle* h, double* xt, const double* ap, const double* const as[6], const double* bs,
+                              int ib, int ie, int jb, int je, int kb, int ke, int nim) {
+    if (!h || !xt || !ap || !as || !bs || nim < 0) return GFM_E_ARG;
+    for (int q = 0; q < 6; ++q) if (!as[q]) return GFM_E_ARG;
+    const HostGrid& g = h->hg;
+    if (((ib ^ ie) & 1) || ((jb ^ je) & 1) || ((kb ^ ke) & 1) || ib < 3 || jb < 3 || kb < 3 || ie > g.MP - 2 || je > g.NP - 2 ||
+        ke > g.LP - 2 || ie < ib || je < jb || ke < kb)
+        return GFM_E_ARG;
+    return h->prec == GFM_PREC_FP64 ? adlbl3_user(h, h->cd, h->scr_d, xt, ap, as, bs, ib, ie, jb, je, kb, ke, nim)
+                                    : adlbl3_user(h, h->cf, h->scr_f, xt, ap, as, bs, ib, ie, jb, je, kb, ke, nim);
+}
+
+extern "C" int gfm_gpu_kernel_times(gfm_handle* h, double* adi_ms, double* assemble_ms, double* other_ms, long long* launches) {
+    if (!h) return GFM_E_ARG;
+    if (adi_ms) *adi_ms = h->adi_ms;
+    if (assemble_ms) *assemble_ms = h->asm_ms;
+    if (other_ms) *other_ms = h->other_ms;
+    if (launches) *launches = h->launches;
+    return GFM_OK;
+}
+extern "C" int gfm_gpu_reset_kernel_times(gfm_handle* h) {
+    if (!h) return GFM_E_ARG;
+    h->adi_ms = h->asm_ms = h->other_ms = 0;
+    h->launches = 0;
+    return GFM_OK;
+}
+extern "C" const char* gfm_gpu_last_error(gfm_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+extern "C" void gfm_gpu_destroy(gfm_handle* h);
+extern "C" void gfm_gpu_destroy(gfm_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (void* p : h->allocs) cudaFree(p);
+    if (h->h_scal) cudaFreeHost(h->h_scal);
+    if (h->ev_adi0) cudaEventDestroy(h->ev_adi0);
+    if (h->ev_adi1) cudaEventDestroy(h->ev_adi1);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}

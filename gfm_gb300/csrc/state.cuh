@@ -1,0 +1,136 @@
+// state.cuh -- device state of one solver handle and the launcher interface
+// between the host orchestration (solver.cu) and the kernel translation units.
+#pragma once
+#include "device.cuh"
+
+namespace gfm {
+
+// Boundary-cell record for EXTR (Extr.f90:31-250): indices and weights are
+// fixed by IBCELL and the grid, so they are computed once on the host.
+struct ExtrRec {
+    int I, J, K, I1, J1, K1, I2, J2, K2, IX;
+    int kind;            // 2 inlet, 3 exit, 1 wall
+    int I3, J3, K3;      // exit: face receiving the SBC4 copy
+    double F1, F2;
+};
+// Exit-face record for EXTRV (Extr.f90:358-567)
+struct ExtrvRec {
+    int I, J, K, IU;
+    int mode;            // 0: flux branch with neighbour offset m; 1: copy from (Is,Js,Ks)
+    int m;               // -1 / +1
+    int Is, Js, Ks;
+};
+// Wall patch of the fixed-temperature sink (Qwall.f90:395-513)
+struct Patch {
+    int inc, jnc, knc;   // open cell centre next to the patch
+    double ds_q;         // distance used in calc_q_conv_wall
+    double ds_src;       // cell width used in the source (Source.f90:488-502)
+    double area, bT;
+};
+
+// Device scalars (double), indices into Ctx::scal
+enum Scal {
+    S_RES_MASS = 0, S_RES_MASS_MAX, S_GFEX, S_GFIN0, S_GFIN, S_FACTOR, S_FADJ, S_G0, S_TMEAN_EX,
+    S_Q_REACT, S_Q_EXHAUST, S_QCONV, S_TAVE, S_P_RESID_PRE, S_P_RESID, S_PCORR_RESID,
+    S_U_RESID_PRE, S_U_RESID = S_U_RESID_PRE + 3, S_GF_RESID_PRE = S_U_RESID + 3, S_GF_RESID = S_GF_RESID_PRE + 10,
+    S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_NUM
+};
+
+template <typename R>
+struct Ctx {
+    GeoT<R> g;
+    Prm p;
+    R *P, *T, *DNST, *THETA, *TMU, *GAMA, *CRATE, *HRATE, *GTE, *BSH;
+    R *UG[3];
+    R *GF[9];
+    R *FZ;
+    R *APm, *ASm[6], *BSm, *SFPm;          // momentum, face classes
+    R *APc, *ASc[6], *BSp, *BSq;           // pressure / p', centre class
+    R *APs[7], *BSs[7], *FZs[7], *SFPs[7]; // scalar equations L=1..7 at index L-1
+    R *ASs[3][6];                          // coefficient sets shared by equal sigma
+    int as_set[7];
+    R *QA, *QE;                            // radiation rates (W) at cell centres
+    const double *rtim, *delrt, *delr, *timed;
+    int nr0;
+    const ExtrRec *extr_io, *extr_wall, *extr_ft;
+    int n_extr_io, n_extr_wall, n_extr_ft;
+    const int* ft_col_start;               // fall-through wall cells grouped by (I,J) column
+    int n_ft_cols;
+    const ExtrvRec* extrv;
+    int n_extrv[3];                        // records per direction, stored back to back
+    const Patch* patch;
+    const int* cell_patch_start;           // CSR: patches adjacent to each listed open cell
+    const int* cell_patch_list;
+    const int* patch_cells;                // open cell centres with patches (packed I|J<<12|K<<24 not used: ijk triplets)
+    int n_patch, n_patch_cells;
+    R* qconv;                              // q_conv per patch (W/m2)
+    const int8_t* intp_mode;               // INTP carried-F1 code per position
+    double* scal;                          // S_NUM device scalars
+    double* partials;                      // kRedSlots x kRedBlocks
+    int nwl;
+    double wl[16], akl0[16];
+    int i_ref, j_ref, k_ref;
+    double p_ref;
+    int itr_gas;                           // host copy for launches that branch on it
+    int rad_active;                        // i1st_rad_qe_done > 0: QA-QE enters the h source
+    const Nist* nist;                      // device copy of the Shomate table
+};
+
+// Equation system for the line solver: class given by (ib,jb,kb) parities.
+template <typename R>
+struct Sys {
+    R* xt;
+    const R* ap;
+    const R* as[6];
+    const R* bs;
+    int ib, ie, jb, je, kb, ke, nim;
+};
+
+// Per-equation scratch of the line solver (class-sized device buffers)
+template <typename R>
+struct AdiScratch {
+    R *xt2, *xt3, *pty, *ptz;
+};
+
+// ---- launchers (defined in the kernel translation units) --------------------
+template <typename R> void launch_wallfn(const Ctx<R>& c, const int* wall_list, int n_wall, cudaStream_t s);
+template <typename R> void launch_copy_faces_to_fz(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_mom_assemble(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_p_assemble(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_bound_p(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_mom_prep(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_mom_finish(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_pcorr_source(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_velcorr(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_extrv(const Ctx<R>& c, int mex, cudaStream_t s);
+template <typename R> void launch_factor(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_intpv(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_qconv(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_scalar_sources_first(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_scalar_assemble(const Ctx<R>& c, int L, bool new_as, cudaStream_t s);
+template <typename R> void launch_scalar_finish(const Ctx<R>& c, int L, cudaStream_t s);
+template <typename R> void launch_props(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_tave(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
+template <typename R> void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
+                                             int mode, cudaStream_t s);
+// deterministic finish of block partials: op 0 sum, 1 max, 2 residual
+// (sum/NCELLS floored at 1e-16, NaN -> 1e-16), 3 sum/NCELLS
+struct FinishSpec {
+    int n;
+    int slot[40], dst[40], op[40];
+};
+void launch_finish(const double* partials, double* scal, const FinishSpec& f, double ncells, cudaStream_t s);
+template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int K1, int I2, int J2, int K2, double F1,
+                                           double F2, cudaStream_t s);
+
+// layout conversion doubled <-> parity split (host-layout arrays on device)
+template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);
+template <typename R> void launch_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s);
+template <typename R> void launch_cells_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);
+template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s);
+
+}  // namespace gfm

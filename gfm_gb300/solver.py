@@ -1,0 +1,206 @@
+"""Host-side mirror of the reference's solver interface over the C ABI.
+
+``Case`` plays the role of the Fortran start-up (GRID3/SETUP/SBC/INITSV): it
+builds the grid, the constants and the fresh-start fields in the reference's
+doubled layout.  ``GpuSolver`` replaces ``CALL GFLOW`` (Sphase.f90:51) with
+``gflow(n)``, keeps the reference's field layout at the boundary, and raises
+``GfmError`` for every non-zero status, as the reference's ``stop_run`` ends
+the run (A0main.f90:415-424).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .configs import FurnaceCase
+
+
+class GfmError(RuntimeError):
+    def __init__(self, rc: int, msg: str):
+        super().__init__(f"gfm status {rc}: {msg}")
+        self.rc = rc
+
+
+FIELD_NAMES = ("p", "t", "dnst", "theta", "tmu", "gama", "crate", "hrate", "bs_hprev")
+
+
+@dataclass
+class Fields:
+    """Host fields in the reference layout: arrays of shape (LP,NP,MP) C-order
+    = Fortran (MP,NP,LP); ug (3,LP,NP,MP); gf (9,LP,NP,MP); qa/qe (LZ,NZ,MZ)."""
+    arrays: dict
+    itr_gas: int = 0
+    do_rad_qe_only_cnt: int = 0
+    i1st_rad_qe_done: int = 0
+    factor: float = 1.0
+    fadj: float = 0.0
+    gfin0: float = 0.0
+    q_h_in: float = 0.0
+
+    @staticmethod
+    def empty(mp: int, np_: int, lp: int) -> "Fields":
+        shp = (lp, np_, mp)
+        arr = {n: np.zeros(shp) for n in FIELD_NAMES}
+        arr["ug"] = np.zeros((3,) + shp)
+        arr["gf"] = np.zeros((9,) + shp)
+        arr["qa"] = np.zeros((lp // 2, np_ // 2, mp // 2))
+        arr["qe"] = np.zeros((lp // 2, np_ // 2, mp // 2))
+        return Fields(arr)
+
+    def to_c(self) -> abi.GfmFields:
+        f = abi.GfmFields()
+        for n in FIELD_NAMES + ("ug", "gf", "qa", "qe"):
+            a = self.arrays[n]
+            assert a.dtype == np.float64 and a.flags["C_CONTIGUOUS"]
+            setattr(f, n, abi.dptr(a))
+        f.itr_gas, f.do_rad_qe_only_cnt, f.i1st_rad_qe_done = self.itr_gas, self.do_rad_qe_only_cnt, self.i1st_rad_qe_done
+        f.factor, f.fadj, f.gfin0, f.q_h_in = self.factor, self.fadj, self.gfin0, self.q_h_in
+        return f
+
+    def update_scalars(self, f: abi.GfmFields) -> None:
+        self.itr_gas, self.do_rad_qe_only_cnt, self.i1st_rad_qe_done = f.itr_gas, f.do_rad_qe_only_cnt, f.i1st_rad_qe_done
+        self.factor, self.fadj, self.gfin0, self.q_h_in = f.factor, f.fadj, f.gfin0, f.q_h_in
+
+    def copy(self) -> "Fields":
+        return Fields({k: v.copy() for k, v in self.arrays.items()}, self.itr_gas, self.do_rad_qe_only_cnt,
+                      self.i1st_rad_qe_done, self.factor, self.fadj, self.gfin0, self.q_h_in)
+
+
+class Case:
+    """A built synthetic furnace (host arrays owned by the native library)."""
+
+    def __init__(self, cfg: FurnaceCase, lib: C.CDLL | None = None):
+        self.cfg = cfg
+        self.lib = lib or abi.load_library()
+        self.spec = cfg.to_spec()
+        self.c = abi.GfmCase()
+        rc = self.lib.gfm_case_build(C.byref(self.spec), str(abi.KINETIC_PATH).encode(), C.byref(self.c))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, "gfm_case_build failed")
+        g = self.c.grid
+        self.mp, self.np, self.lp = g.mp, g.np, g.lp
+        self.ncells = g.ncells
+
+    @property
+    def grid(self) -> abi.GfmGrid:
+        return self.c.grid
+
+    @property
+    def params(self) -> abi.GfmParams:
+        return self.c.params
+
+    def ibcell(self) -> np.ndarray:
+        n = self.mp * self.np * self.lp
+        return np.ctypeslib.as_array(self.c.grid.ibcell, shape=(n,)).reshape(self.lp, self.np, self.mp).copy()
+
+    def initial_fields(self) -> Fields:
+        """Copy of the fresh-start fields (before INITSV's interpolation)."""
+        n = self.mp * self.np * self.lp
+        nc = (self.mp // 2) * (self.np // 2) * (self.lp // 2)
+        f = self.c.fields
+        shp = (self.lp, self.np, self.mp)
+        arr = {}
+        for name in FIELD_NAMES:
+            arr[name] = np.ctypeslib.as_array(getattr(f, name), shape=(n,)).reshape(shp).copy()
+        arr["ug"] = np.ctypeslib.as_array(f.ug, shape=(3 * n,)).reshape((3,) + shp).copy()
+        arr["gf"] = np.ctypeslib.as_array(f.gf, shape=(9 * n,)).reshape((9,) + shp).copy()
+        csh = (self.lp // 2, self.np // 2, self.mp // 2)
+        arr["qa"] = np.ctypeslib.as_array(f.qa, shape=(nc,)).reshape(csh).copy()
+        arr["qe"] = np.ctypeslib.as_array(f.qe, shape=(nc,)).reshape(csh).copy()
+        return Fields(arr, f.itr_gas, f.do_rad_qe_only_cnt, f.i1st_rad_qe_done, f.factor, f.fadj, f.gfin0, f.q_h_in)
+
+    def close(self) -> None:
+        if self.c.priv:
+            self.lib.gfm_case_free(C.byref(self.c))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuSolver:
+    """GB300 SIMPLER solver for one case; fields stay resident on the device."""
+
+    def __init__(self, case: Case, adi_mode: int | None = None, precision: int | None = None):
+        self.case = case
+        self.lib = case.lib
+        n = self.lib.gfm_gpu_device_count()
+        if n < 1:
+            raise GfmError(n, "no CUDA device: the GB300 solver has no CPU path")
+        prm = abi.GfmParams.from_buffer_copy(case.params)
+        if adi_mode is not None:
+            prm.adi_mode = adi_mode
+        if precision is not None:
+            prm.precision = precision
+        self.params = prm
+        h = C.c_void_p()
+        rc = self.lib.gfm_gpu_create(C.byref(case.grid), C.byref(prm), C.byref(h))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, self.lib.gfm_gpu_last_error(None).decode())
+        self.h = h
+
+    def _check(self, rc: int) -> None:
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, self.lib.gfm_gpu_last_error(self.h).decode())
+
+    def upload(self, fields: Fields) -> None:
+        f = fields.to_c()
+        self._check(self.lib.gfm_gpu_upload(self.h, C.byref(f)))
+
+    def initsv(self) -> None:
+        self._check(self.lib.gfm_gpu_initsv(self.h))
+
+    def start(self) -> None:
+        """Upload the case's fresh-start fields and run INITSV's interpolation."""
+        self.upload(self.case.initial_fields())
+        self.initsv()
+
+    def gflow(self, n_iter: int = 1) -> tuple[dict, int]:
+        st = abi.GfmIterStats()
+        nd = C.c_int(0)
+        self._check(self.lib.gfm_gpu_gflow(self.h, n_iter, C.byref(st), C.byref(nd)))
+        return st.as_dict(), nd.value
+
+    def download(self) -> Fields:
+        out = Fields.empty(self.case.mp, self.case.np, self.case.lp)
+        f = out.to_c()
+        self._check(self.lib.gfm_gpu_download(self.h, C.byref(f)))
+        out.update_scalars(f)
+        return out
+
+    def rad_emission(self) -> None:
+        self._check(self.lib.gfm_gpu_rad_emission(self.h))
+
+    def adlbl3(self, xt, ap, as6, bs, ib, ie, jb, je, kb, ke, nim) -> np.ndarray:
+        x = np.ascontiguousarray(xt, dtype=np.float64).copy()
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in as6]
+        ptrs = (abi._dp * 6)(*[abi.dptr(a) for a in arrs])
+        self._check(self.lib.gfm_gpu_adlbl3(self.h, abi.dptr(x), abi.dptr(np.ascontiguousarray(ap, dtype=np.float64)),
+                                            ptrs, abi.dptr(np.ascontiguousarray(bs, dtype=np.float64)),
+                                            ib, ie, jb, je, kb, ke, nim))
+        return x
+
+    def kernel_times(self) -> dict:
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_longlong()
+        self._check(self.lib.gfm_gpu_kernel_times(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(n)))
+        return {"adi_ms": a.value, "assemble_ms": b.value, "other_ms": c.value, "launches": n.value}
+
+    def reset_kernel_times(self) -> None:
+        self._check(self.lib.gfm_gpu_reset_kernel_times(self.h))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gfm_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

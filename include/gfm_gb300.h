@@ -1,0 +1,221 @@
+/*
+ * gfm_gb300.h -- C ABI of the GB300-native GFM combustion-space solver.
+ *
+ * The reference solver (GFM v4, Fortran 90) runs its steady SIMPLER outer
+ * iteration as argument-less subroutines over module state (module GBL_VAR,
+ * combustion/Code/Var_mod.f90).  This header replaces three seams of it:
+ *
+ *   CALL GFLOW                       combustion/Code/Sphase.f90:51
+ *   CALL ADLBL3(XT,IB,IE,JB,JE,KB,KE) combustion/Code/Adlbl3.f90:10
+ *   CALL rad_qe_only                 combustion/Code/Sphase.f90:226
+ *
+ * plus the start-up work a Fortran host would otherwise do before the first
+ * GFLOW (SETUP/SBC/INITSV, combustion/Code/A0main.f90:158-190) for the
+ * synthetic furnace cases.
+ *
+ * Layout at the boundary is the reference's own: every field is a Fortran
+ * column-major array over the doubled staggered grid A(MP,NP,LP) (I fastest,
+ * 1-based in Fortran, element (I,J,K) at offset (I-1)+MP*((J-1)+NP*(K-1)) here),
+ * UG(MP,NP,LP,3) and GF(MP,NP,LP,9) append the component as the slowest index,
+ * IBCELL is integer(2).  Cell arrays QA/QE are (MZ,NZ,LZ) with MZ=MP/2.
+ *
+ * Conventions: every entry point returns an int status (0 = ok, <0 = error,
+ * see GFM_E_*), never aborts and never exits.  One handle per host thread;
+ * calls on one handle are serialised on the handle's own CUDA stream.
+ */
+#ifndef GFM_GB300_H
+#define GFM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define GFM_OK              0
+#define GFM_E_ARG         (-1)   /* bad argument / dimension                */
+#define GFM_E_CUDA        (-2)   /* CUDA runtime error                      */
+#define GFM_E_NAN         (-3)   /* non-finite value detected               */
+#define GFM_E_UNSUPPORTED (-4)   /* input outside the supported case set    */
+#define GFM_E_NOMEM       (-5)   /* allocation failed                       */
+#define GFM_E_TIMEOUT     (-6)   /* bounded device wait ran out             */
+#define GFM_E_NODEVICE    (-7)   /* no CUDA device / extension not usable   */
+
+/* ADI line-solver ordering (gfm_params.adi_mode) */
+#define GFM_ADI_MARCH      0     /* reference order: x-plane Gauss-Seidel march,
+                                    forward then backward (Adlbl3.f90:39-51)   */
+#define GFM_ADI_REDBLACK   1     /* red-black x-plane ordering, all planes of
+                                    one colour at once                          */
+
+/* arithmetic of the bulk stencil / line-solve work (gfm_params.precision) */
+#define GFM_PREC_FP64      0     /* plain FP64, the reference's arithmetic      */
+#define GFM_PREC_MIXED     1     /* FP32 stencil assembly and line solves, FP64
+                                    reductions and FP64 refinement on p'        */
+
+/* ---- grid: geometry, cell map, boundary patches, tables ------------------ */
+typedef struct gfm_grid {
+    int mp, np, lp;              /* doubled extents MP,NP,LP (Grid3.f90:36)   */
+    const double *x, *dx;        /* X(MP), DX(MP)  (Grid3.f90:79-109)         */
+    const double *r, *dr, *rs;   /* R(NP), DR(NP), RS(NP) (Grid3.f90:117-171) */
+    const double *z, *dz;        /* Z(LP), DZ(LP)  (Grid3.f90:177-226)        */
+    const int16_t *ibcell;       /* IBCELL(MP,NP,LP) after the 27-neighbour
+                                    propagation (Grid3.f90:259-275)           */
+    int ncells;                  /* NCELLS (Grid3.f90:259-268)                */
+    int i_ref, j_ref, k_ref;     /* pressure reference cell (Sbc.f90:57)      */
+    double p_ref;                /* P_REF/PG0                                 */
+    /* wall patches of the fixed-temperature wall sink (Qwall.f90:395-513) */
+    int b_cnt;
+    const int16_t *b_typ, *b_i, *b_j, *b_k, *b_orient, *b_direct;
+    const double *b_t;           /* patch temperature b_T (K)                 */
+    /* integral-reaction kinetics table (Setup.f90:858-888) */
+    int nr0;
+    const double *rtim, *delrt, *hrt, *delr, *timed, *hrd;
+    /* gray radiation bands: edges WL (m) and absorption coefficients (1/m) */
+    int nwl;
+    const double *wl, *akl0;
+} gfm_grid;
+
+/* ---- scalar constants of module GBL_VAR after SETUP ---------------------- */
+typedef struct gfm_params {
+    double t0, h_0, dnst0, ug0, gmfr, pg0, r0;           /* Setup.f90:542-543 */
+    double reyg, reyg2, epsr, taur, eun, qr0, q0, tk0;   /* Setup.f90:662-721 */
+    double gra[3];               /* GRA/UG0**2*R0 (Setup.f90:544)             */
+    double amu, trdg, wt0, stoich;
+    double cmu, ct1, ct2;        /* k-eps constants (Var_mod.f90:203-208)     */
+    double p_mx, p_mn, t_mx, t_mn, u_mx, u_mn, f_mx, f_mn;  /* bounds         */
+    double rf[21], rfl[21];      /* relaxation factors (Setup.f90:443-472)    */
+    double sigma[12];            /* Prandtl/Schmidt numbers (Var_mod.f90:211) */
+    int    ntimesg[20];          /* ADI sweeps per NELG (Setup.f90:495-509)   */
+    double rf_hsource;           /* enthalpy-source relaxation (Setup.f90:486) */
+    int    react, turb;
+    /* configuration-level switches (applied identically by every path) */
+    int    wall_sink;            /* fixed-T wall convective sink every iteration */
+    double h_g;                  /* internal wall heat-transfer floor (W/m2/K) */
+    int    rad_emission;         /* emission-only radiation source (rad_qe_only) */
+    int    rad_qe_frequency;     /* iterations between emission updates (10)   */
+    double sig, ri, hck;         /* Stefan-Boltzmann, refraction index, hc/k   */
+    double bgcon;                /* convergence on res_mass (Sphase.f90:193)  */
+    int    maxgi;
+    int    adi_mode;             /* GFM_ADI_*                                  */
+    int    precision;            /* GFM_PREC_*                                 */
+} gfm_params;
+
+/* ---- fields in the reference layout -------------------------------------- */
+typedef struct gfm_fields {
+    double *p, *t, *dnst, *theta, *tmu, *gama;   /* (MP,NP,LP)                 */
+    double *crate, *hrate, *bs_hprev;            /* (MP,NP,LP)                 */
+    double *ug;                  /* UG(MP,NP,LP,3)                             */
+    double *gf;                  /* GF(MP,NP,LP,9): 1 fuel 2 O2 3 h 4 k 5 eps
+                                    6 CO2 7 N2 9 H2O (Var_mod.f90:116-123)     */
+    double *qa, *qe;             /* QA, QE (MZ,NZ,LZ), W per cell              */
+    /* iteration state carried between GFLOW calls */
+    int    itr_gas, do_rad_qe_only_cnt, i1st_rad_qe_done;
+    double factor, fadj, gfin0, q_h_in;
+} gfm_fields;
+
+/* ---- per-iteration statistics (the reference's .plt log quantities) ------ */
+typedef struct gfm_iter_stats {
+    int    itr_gas;
+    int    converged;            /* res_mass < BGCON (Sphase.f90:193)          */
+    double res_mass, res_mass_max;          /* Source.f90:41-101              */
+    double p_resid_pre, p_resid, pcorr_resid;
+    double u_resid_pre[3], u_resid[3];
+    double gf_resid_pre[10], gf_resid[10];  /* index L-1, L=1..7              */
+    double factor, gfin, gfex;
+    double q_react, q_exhaust, q_conv_total, q_global_bal;
+    double tave, tmean_ex;
+} gfm_iter_stats;
+
+/* ---- synthetic furnace specification (stands in for gd/sbc files) -------- */
+typedef struct gfm_inlet_spec {
+    double y0, y1, z0, z1;       /* opening on the x=0 wall (m)               */
+    double t_k;                  /* inlet temperature (K)                      */
+    double yf, yo2, yn2, yco2, yh2o;
+    double u_ms;                 /* nominal velocity (m/s), rescaled to keep
+                                    the mass flow after snapping to cells      */
+} gfm_inlet_spec;
+
+typedef struct gfm_case_spec {
+    int    nx, ny, nz;           /* interior cells                             */
+    double lx, ly, lz;           /* box (m)                                    */
+    int    n_inlets;
+    gfm_inlet_spec inlets[8];    /* inlets[0] holds the pressure reference     */
+    double exit_y0, exit_y1, exit_z0, exit_z1;   /* flue on the x=lx wall      */
+    double t_init_k;             /* initial gas temperature (K)                */
+    double noise_amp;            /* uniform +-noise on initial T and species   */
+    uint64_t seed;
+    double inlet_jitter;         /* uniform +-jitter on inlet velocities       */
+    double t_wall_k;             /* fixed wall temperature (K)                 */
+    double rf_uvw, rfl_h, rfl_k, rfl_eps, rfl_species, rf_hsource;
+    int    ntimesg[12];          /* sweeps for NELG 1..12                      */
+    double sigma_k, sigma_eps;
+    int    nwl;
+    double kappa[16];            /* gray band absorption coefficients (1/m)    */
+    double wl_um[16];            /* band upper edges (um), as WL in &RADIN     */
+    double pg0, q0_jkg, h_g;
+    int    react, wall_sink, rad_emission, maxgi;
+    double bgcon;
+    int    adi_mode, precision;
+} gfm_case_spec;
+
+/* A built case: host-owned arrays allocated by gfm_case_build. */
+typedef struct gfm_case {
+    gfm_grid   grid;
+    gfm_params params;
+    gfm_fields fields;
+    void      *priv;             /* owns the storage behind the pointers       */
+} gfm_case;
+
+/* Opaque GPU solver handle. */
+typedef struct gfm_handle gfm_handle;
+
+/* ---- host side: synthetic case construction ------------------------------ */
+/* Builds grid, constants and the fresh-start state the reference reaches after
+ * GRID3 + SETUP + SBC + gen_initial_guess (Grid3.f90:8-300, Setup.f90:223-731,
+ * Sbc.f90:19-388, Initsv.f90:97-162).  The interpolation part of INITSV
+ * (INTPV, EXTR(1), INTP; Initsv.f90:63-84) is left to gfm_gpu_initsv. */
+int  gfm_case_build(const gfm_case_spec *spec, const char *kinetic_path,
+                    gfm_case *out);
+void gfm_case_free(gfm_case *c);
+
+/* ---- GPU solver ---------------------------------------------------------- */
+/* Query: number of CUDA devices usable (>=1) or a negative status. */
+int  gfm_gpu_device_count(void);
+/* Allocates device mirrors for the grid and the constants; uploads the static
+ * geometry and the boundary index tables. */
+int  gfm_gpu_create(const gfm_grid *grid, const gfm_params *params,
+                    gfm_handle **out);
+/* Host fields (reference layout) -> device. */
+int  gfm_gpu_upload(gfm_handle *h, const gfm_fields *f);
+/* INTPV, EXTR(1), INTP on the device: the tail of INITSV (Initsv.f90:63-84). */
+int  gfm_gpu_initsv(gfm_handle *h);
+/* n_iter passes of SPHASE's loop body: itr_gas+=1, GFLOW, convergence test,
+ * emission-only radiation cadence (Sphase.f90:37-235).  Stops early when
+ * res_mass < BGCON.  `out` (may be NULL) receives the last iteration's stats;
+ * `n_done` (may be NULL) the number of iterations run. */
+int  gfm_gpu_gflow(gfm_handle *h, int n_iter, gfm_iter_stats *out, int *n_done);
+/* Device -> host fields (reference layout). */
+int  gfm_gpu_download(gfm_handle *h, gfm_fields *f);
+/* One ADLBL3 call on a user system (Adlbl3.f90:10-97): xt, ap, as (6 arrays
+ * AS(..,L,M) in the order (1,1),(1,2),(2,1),(2,2),(3,1),(3,2)), bs in the
+ * reference layout; solves in place on the class of (ib,jb,kb) with the sweep
+ * count nim.  Uses the handle's grid (IBCELL) and adi_mode/precision. */
+int  gfm_gpu_adlbl3(gfm_handle *h, double *xt, const double *ap,
+                    const double *const as[6], const double *bs,
+                    int ib, int ie, int jb, int je, int kb, int ke, int nim);
+/* Emission-only radiation QE on the device from the current T, P
+ * (rad_qe_only, Rad_emis.f90:411-466 with RAD0 Rad0.f90:112-157). */
+int  gfm_gpu_rad_emission(gfm_handle *h);
+/* Device time of the dominant kernels accumulated since the last reset. */
+int  gfm_gpu_kernel_times(gfm_handle *h, double *adi_ms, double *assemble_ms,
+                          double *other_ms, long long *launches);
+int  gfm_gpu_reset_kernel_times(gfm_handle *h);
+/* Last error text of this handle (never NULL). */
+const char *gfm_gpu_last_error(gfm_handle *h);
+void gfm_gpu_destroy(gfm_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GFM_GB300_H */

@@ -1,0 +1,1753 @@
+// gfm_oracle.cpp -- TEST INFRASTRUCTURE ONLY: single-threaded FP64 C++
+// restatement of the reference's steady SIMPLER iteration (GFLOW and callees,
+// combustion/Code/*.f90), used as the parity checker and CPU baseline.
+//
+// Every routine keeps the Fortran loop order, array layout (doubled staggered
+// grid, column-major, 1-based indices) and expression order.  Build with
+// -ffp-contract=off so x86 and Arm hosts give the same bits.
+#include "gfm_oracle.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+typedef std::vector<double> vec;
+
+const double ZERO = 0.0, ONE = 1.0, TWO = 2.0;
+const double small20 = 1.0e-20, small16 = 1.0e-16, BIG = 1.0e+20;
+const double WF = 16.0426, WO2 = 31.9988, WCO2 = 44.0098, WH2O = 18.0152, WN2 = 28.0134;
+const int IYF = 1, IYO2 = 2, IH = 3, IK = 4, IEPS = 5, IYCO2 = 6, IYN2 = 7, IYH2O = 9;
+const int LSTAR = 1, LEND = 7;
+const double SMX0 = 1.0e-14;
+const double CP0 = 1.0057e+3;
+const double CPF1 = 2.156e+3 / 1.0057e+3, CPO21 = 0.9136e+3 / 1.0057e+3, CPCO21 = 2.0e+3 / 1.0057e+3,
+             CPH2O1 = 2.0e+3 / 1.0057e+3, CPN21 = 0.526e+3 / 1.0057e+3;   // Var_mod.f90:156-160
+
+// NIST Shomate sets (Setup.f90:103-141), [species][lo/hi], species CH4,O2,CO2,N2,H2O
+const double A_N[5][2] = {{-0.703029, 85.81217}, {29.659, 29.659}, {24.99735, 58.16639}, {26.092, 26.092}, {30.092, 41.96426}};
+const double B_N[5][2] = {{108.4773, 11.26467}, {6.137261, 6.137261}, {55.18696, 2.720074}, {8.218801, 8.218801}, {6.832514, 8.622053}};
+const double C_N[5][2] = {{-42.52157, -2.114146}, {-1.186521, -1.186521}, {-33.69137, -0.492289}, {-1.976141, -1.976141}, {6.793435, -1.49978}};
+const double D_N[5][2] = {{5.862788, 0.13819}, {0.09578, 0.09578}, {7.948387, 0.038844}, {0.159274, 0.159274}, {-2.53448, 0.098119}};
+const double E_N[5][2] = {{0.678565, -26.42221}, {-0.219663, -0.219663}, {-0.136638, -6.447293}, {0.044434, 0.044434}, {0.082139, -11.15764}};
+const double F_N[5][2] = {{-76.84376, -153.5327}, {-9.861391, -9.861391}, {-403.6075, -425.9186}, {-7.98923, -7.98923}, {-250.881, -272.1797}};
+const double H_N[5][2] = {{-74.8731, -74.8731}, {0.0, 0.0}, {-393.5224, -393.5224}, {0.0, 0.0}, {-241.8264, -241.8264}};
+const double CUTT[5] = {1300.0, 6000.0, 1200.0, 6000.0, 1700.0};
+const int GFCI[5] = {IYF, IYO2, IYCO2, IYN2, IYH2O};   // gf_chem_index
+const double T0C = 5.0e+2;
+const double H0C = 1.0057e+3 * (5.0e+2 - 298.15);
+
+inline double fmax2(double a, double b) { return a > b ? a : b; }   // Fortran MAX(a,b): NaN in a -> b
+inline double fmin2(double a, double b) { return a < b ? a : b; }
+
+// ---------------------------------------------------------------------------
+// Prop.f90 routines on a 9-component GF vector accessed with stride s
+// ---------------------------------------------------------------------------
+struct Y9 {
+    double* p; long s;
+    double& operator()(int l) const { return p[(long)(l - 1) * s]; }
+};
+
+void conc(Y9 y) {   // CONC, Prop.f90:28-59
+    double g0 = y(IYF) + y(IYO2) + y(IYCO2) + y(IYN2);
+    if (g0 > ONE) {
+        g0 = g0 + y(IYH2O);
+        y(IYF) = y(IYF) / g0;
+        y(IYO2) = y(IYO2) / g0;
+        y(IYCO2) = y(IYCO2) / g0;
+        y(IYN2) = y(IYN2) / g0;
+        y(IYH2O) = y(IYH2O) / g0;
+    } else {
+        y(IYH2O) = ONE - g0;
+    }
+}
+
+double wmix(Y9 y) {
+    return ONE / (y(IYF) / WF + y(IYCO2) / WCO2 + y(IYH2O) / WH2O + y(IYO2) / WO2 + y(IYN2) / WN2);
+}
+
+struct Mix { double a, b, c, d, e, f, h; int lohi[5]; };
+
+void mix_coeffs(Y9 y, double real_T, Mix& m) {   // Prop.f90:396-418 (incl. f_mix=d_mix+... quirk)
+    m.a = m.b = m.c = m.d = m.e = m.f = m.h = 0;
+    for (int n = 0; n < 5; ++n) {
+        int st = real_T < CUTT[n] ? 0 : 1;
+        double g = y(GFCI[n]);
+        m.a = m.a + g * A_N[n][st];
+        m.b = m.b + g * B_N[n][st];
+        m.c = m.c + g * C_N[n][st];
+        m.d = m.d + g * D_N[n][st];
+        m.e = m.e + g * E_N[n][st];
+        m.f = m.d + g * F_N[n][st];
+        m.h = m.e + g * H_N[n][st];
+        m.lohi[n] = st + 1;
+    }
+}
+
+double enth_to_T(Y9 y, double t_now) {   // enth_to_T, Prop.f90:369-505
+    double w_mix = wmix(y);
+    double h_s = y(IH) * H0C;
+    double h_molar = h_s * w_mix / 1.0e6;
+    double real_T = t_now * T0C;
+    Mix m;
+    mix_coeffs(y, real_T, m);
+    double T_old = real_T / 1000.0, T_new = T_old;
+    for (int n = 1; n <= 10; ++n) {
+        double gp = m.a + T_old * (m.b + T_old * (m.c + T_old * m.d)) + m.e / (T_old * T_old);
+        if (gp == ZERO) break;
+        double g0 = T_old * (m.a + T_old * ((m.b / 2.0) + T_old * ((m.c / 3.0) + T_old * (m.d / 4.0)))) -
+                    (m.e / T_old) + m.f - m.h;
+        double changeT = (g0 - h_molar) / gp;
+        T_new = T_old - changeT;
+        if (std::fabs(changeT) < 1.0e-11) break;
+        T_old = T_new;
+        for (int nn = 1; nn <= 5; ++nn) {
+            if (nn == 2 || nn == 4) continue;
+            int q = nn - 1;
+            double g = y(GFCI[q]);
+            if (T_new * 1000.0 < CUTT[q] && m.lohi[q] != 1) {
+                m.a = m.a - g * A_N[q][1]; m.b = m.b - g * B_N[q][1]; m.c = m.c - g * C_N[q][1];
+                m.d = m.d - g * D_N[q][1]; m.e = m.e - g * E_N[q][1];
+                m.f = m.d - g * F_N[q][1]; m.h = m.e - g * H_N[q][1];
+                m.lohi[q] = 1;
+                m.a = m.a + g * A_N[q][0]; m.b = m.b + g * B_N[q][0]; m.c = m.c + g * C_N[q][0];
+                m.d = m.d + g * D_N[q][0]; m.e = m.e + g * E_N[q][0];
+                m.f = m.d + g * F_N[q][0]; m.h = m.e + g * H_N[q][0];
+            }
+            if (T_new * 1000.0 >= CUTT[q] && m.lohi[q] != 2) {
+                m.a = m.a - g * A_N[q][0]; m.b = m.b - g * B_N[q][0]; m.c = m.c - g * C_N[q][0];
+                m.d = m.d - g * D_N[q][0]; m.e = m.e - g * E_N[q][0];
+                m.f = m.d - g * F_N[q][0]; m.h = m.e - g * H_N[q][0];
+                m.lohi[q] = 2;
+                m.a = m.a + g * A_N[q][1]; m.b = m.b + g * B_N[q][1]; m.c = m.c + g * C_N[q][1];
+                m.d = m.d + g * D_N[q][1]; m.e = m.e + g * E_N[q][1];
+                m.f = m.d + g * F_N[q][1]; m.h = m.e + g * H_N[q][1];
+            }
+        }
+    }
+    return T_new * 1000.0 / T0C;
+}
+
+double T_to_enth(Y9 y, double t_now) {   // T_to_enth, Prop.f90:525-565
+    double w_mix = wmix(y);
+    double real_T = t_now * T0C;
+    Mix m;
+    mix_coeffs(y, real_T, m);
+    double tn = real_T / 1000.0;
+    double ef = tn * (m.a + tn * ((m.b / 2.0) + tn * ((m.c / 3.0) + tn * (m.d / 4.0)))) - (m.e / tn) + m.f - m.h;
+    return ef * 1.0e6 / (w_mix * H0C);
+}
+
+double DA(double D, double F) {   // Prop.f90:97-117
+    const double sixth = 1.0 / 6.0;
+    if (D <= 1.0e-25) return 0.0;
+    double FA = std::fabs(F);
+    double PE = FA / D;
+    if (PE <= 1.0e-2) return D / (1.0 + PE * (0.5 + PE * (sixth + PE / 24.0)));
+    if (PE <= 2.0e+1) return FA / (std::exp(PE) - 1.0);
+    return 0.0;
+}
+
+double TGAMF(double B) {   // Gflow.f90:417-426
+    if (B < 11.5) return 1.0;
+    double G0 = B / (std::log(9 * B) * 2.5);
+    return fmax2(G0, 1.0);
+}
+
+double EMF(double XKL, double XL0) {   // Rad_fun.f90:97-115
+    const double X1 = 1.0e-3;
+    const double G1 = (ONE - std::exp(-X1)) / X1;
+    double X0 = XKL * XL0;
+    return X0 <= X1 ? X0 * G1 : ONE - std::exp(-X0);
+}
+
+double RIF3(double X) {   // RIF(3,0,X), Rad_fun.f90:45-91
+    const double PI = 3.141592653589793;
+    if (X > 1.0e16) return 0.0;
+    if (X == 0.0) return 1.0;
+    const double Y[4] = {1.0, 3.0, 6.0, 6.0};   // PER(3,I), I=0..3
+    double rif = 0.0;
+    for (int N = 1; N <= 1000; ++N) {
+        double G0 = 0.0;
+        for (int I = 0; I <= 3; ++I) {
+            double xp = 1.0;
+            for (int q = 0; q < 3 - I; ++q) xp = xp * X;
+            double an = 1.0;
+            for (int q = 0; q < I + 1; ++q) an = an * (double)N;
+            G0 = G0 + Y[I] * xp / an;
+        }
+        G0 = G0 * std::exp(-((double)N) * X);
+        rif = rif + G0;
+        if (std::fabs(G0) <= 1.0e-16) break;
+    }
+    rif = rif * 1.5e+1 / (PI * PI * PI * PI);
+    return rif > 1.0 ? 1.0 : rif;
+}
+
+double ZY1(const double* X, const double* Y, double X1, int N) {   // Source.f90:814-831
+    if (X1 < X[0]) return Y[0] * X1 / X[0];
+    for (int I = 2; I <= N; ++I)
+        if (X1 < X[I - 1]) {
+            double RATIO = (X1 - X[I - 2]) / (X[I - 1] - X[I - 2]);
+            return Y[I - 2] + (Y[I - 1] - Y[I - 2]) * RATIO;
+        }
+    return Y[N - 1];
+}
+
+// ---------------------------------------------------------------------------
+// The oracle state: module GBL_VAR
+// ---------------------------------------------------------------------------
+struct Oracle {
+    int MP, NP, LP, MPM1, MPM2, NPM1, NPM2, LPM1, LPM2, MZ, NZ, LZ;
+    long N;
+    int NJY1, NJY2, LKZ1, LKZ2, NJY1V[4], NJY2V[4], LKZ1V[4], LKZ2V[4];
+    int NCELLS, I_REF, J_REF, K_REF;
+    double P_REF;
+    vec X, DX, R, DR, RS, Z, DZ;   // 1-based (index 0 unused)
+    std::vector<int16_t> IBC;
+    vec P, T, DNST, THETA, TMU, GAMA, CRATE, HRATE, GTE, FZ, BS, SFP, AP, bs_hprev, UG, GF, AS, QA, QE;
+    gfm_params pr;
+    double RFC[21], RFLC[21];
+    // wall patches, kinetics, bands
+    std::vector<int> b_typ, b_i, b_j, b_k, b_orient, b_direct;
+    vec b_T, q_conv;
+    int NR0;
+    vec RTIM, DELRT, HRT, DELR, TIMED, HRD;
+    int NWL;
+    vec WL, AKL0;
+    // state scalars
+    int itr_gas, do_rad_qe_only_cnt, i1st_rad_qe_done, NELG;
+    double FACTOR, FADJ, GFIN0, GFIN, GFEX, SGM, q_h_in;
+    double res_mass, res_mass_max, p_resid_pre, p_resid, pcorr_resid, u_resid_pre[3], u_resid[3];
+    double gf_resid_pre[10], gf_resid[10], h_resid_pre;
+    double q_react, q_exhaust, qconv_total, q_rad_vol_tot, Tmean_ex, Tave;
+
+    long ix(int i, int j, int k) const {
+#ifdef GFO_CHECK
+        if (i < 1 || i > MP || j < 1 || j > NP || k < 1 || k > LP) {
+            std::fprintf(stderr, "gfm_oracle: index (%d,%d,%d) outside (%d,%d,%d)\n", i, j, k, MP, NP, LP);
+            std::abort();
+        }
+#endif
+        return (long)(i - 1) + (long)MP * ((long)(j - 1) + (long)NP * (long)(k - 1));
+    }
+    int ibcell(int i, int j, int k) const { return IBC[ix(i, j, k)]; }
+    double& a3(vec& v, int i, int j, int k) { return v[ix(i, j, k)]; }
+    double& ug(int i, int j, int k, int l) { return UG[ix(i, j, k) + (long)(l - 1) * N]; }
+    double& gf(int i, int j, int k, int l) { return GF[ix(i, j, k) + (long)(l - 1) * N]; }
+    double& as(int i, int j, int k, int l, int m) { return AS[ix(i, j, k) + (long)((l - 1) * 2 + (m - 1)) * N]; }
+    Y9 y9(int i, int j, int k) { return Y9{&GF[ix(i, j, k)], N}; }
+    long cix(int id2, int jd2, int kd2) const { return (long)(id2 - 1) + (long)MZ * ((long)(jd2 - 1) + (long)NZ * (long)(kd2 - 1)); }
+
+    // ---- Grid3.f90 metric functions -----------------------------------------
+    double DXAV(int I, int J, int K) {
+        if (ibcell(I - 2, J, K) >= 1) return X[I + 1] - X[I - 2];
+        if (ibcell(I + 2, J, K) >= 1) return X[I + 2] - X[I - 1];
+        return DX[I];
+    }
+    double DRAV(int I, int J, int K) {
+        if (ibcell(I, J - 2, K) >= 1) { double DRC = R[J + 1] - R[J - 2]; return (RS[J + 1] + RS[J - 2]) * 0.5 / RS[J] * DRC; }
+        if (ibcell(I, J + 2, K) >= 1) { double DRC = R[J + 2] - R[J - 1]; return (RS[J + 2] + RS[J - 1]) * 0.5 / RS[J] * DRC; }
+        return DR[J];
+    }
+    double DZAV(int I, int J, int K) {
+        if (ibcell(I, J, K - 2) >= 1) return Z[K + 1] - Z[K - 2];
+        if (ibcell(I, J, K + 2) >= 1) return Z[K + 2] - Z[K - 1];
+        return DZ[K];
+    }
+    double VOL_C0(int I, int J, int K) { return DX[I] * DR[J] * RS[J] * DZ[K]; }   // BV_F=1
+    double VOL_C(int I, int J, int K) {
+        double VOL;
+        if ((I / 2) * 2 != I) {
+            double VM = VOL_C0(I - 1, J, K); if (ibcell(I - 2, J, K) <= 0) VM = VM * 0.5;
+            double VP = VOL_C0(I + 1, J, K); if (ibcell(I + 2, J, K) <= 0) VP = VP * 0.5;
+            VOL = VP + VM;
+        } else if ((J / 2) * 2 != J) {
+            double VM = VOL_C0(I, J - 1, K); if (ibcell(I, J - 2, K) <= 0) VM = VM * 0.5;
+            double VP = VOL_C0(I, J + 1, K); if (ibcell(I, J + 2, K) <= 0) VP = VP * 0.5;
+            VOL = VP + VM;
+        } else if ((K / 2) * 2 != K) {
+            double VM = VOL_C0(I, J, K - 1); if (ibcell(I, J, K - 2) <= 0) VM = VM * 0.5;
+            double VP = VOL_C0(I, J, K + 1); if (ibcell(I, J, K + 2) <= 0) VP = VP * 0.5;
+            VOL = VP + VM;
+        } else {
+            VOL = VOL_C0(I, J, K);
+        }
+        return VOL;
+    }
+    double AREA_C(int I, int J, int K, int IXD) {   // BA_F=1
+        if (ibcell(I, J, K) == 1) return ZERO;
+        if (IXD == 1) return DR[J] * RS[J] * DZ[K];
+        if (IXD == 2) return DX[I] * DZ[K];
+        return DX[I] * DR[J] * RS[J];
+    }
+
+    // ---- Prop.f90 per-position wrappers --------------------------------------
+    void CONC(int i, int j, int k) { conc(y9(i, j, k)); }
+    void dnst_calc(int i, int j, int k) {
+        conc(y9(i, j, k));
+        double wt = wmix(y9(i, j, k));
+        double temp = (ONE + a3(P, i, j, k)) / a3(T, i, j, k) * wt / pr.wt0;
+        a3(DNST, i, j, k) = fmax2(temp, small20);
+    }
+    void THER(int i, int j, int k) {
+        gf(i, j, k, IEPS) = fmax2(gf(i, j, k, IEPS), 1.0e-12);
+        double G0 = pr.cmu * pr.reyg * pr.epsr / (TWO * pr.taur) * (gf(i, j, k, IK) * gf(i, j, k, IK)) /
+                    gf(i, j, k, IEPS) * a3(DNST, i, j, k);
+        a3(TMU, i, j, k) = G0;
+        a3(GAMA, i, j, k) = TWO / pr.reyg * (a3(TMU, i, j, k) + std::pow(a3(T, i, j, k) / pr.trdg, pr.amu));
+    }
+    void enth_to_T_at(int i, int j, int k) { a3(T, i, j, k) = enth_to_T(y9(i, j, k), a3(T, i, j, k)); }
+    void T_to_enth_at(int i, int j, int k) { gf(i, j, k, IH) = T_to_enth(y9(i, j, k), a3(T, i, j, k)); }
+    void BOUND(double& F, int IL, int IPP) {   // Prop.f90:243-296
+        if (IPP == 1) {
+            if (IL == 0) { F = fmin2(F, pr.p_mx); F = fmax2(F, pr.p_mn); }
+            else if (IL == 4) { F = fmin2(F, pr.t_mx); F = fmax2(F, pr.t_mn); }
+            else if (IL == 5) { F = fmax2(F, 1.0e-6); }
+            else { F = fmin2(F, pr.u_mx); F = fmax2(F, pr.u_mn); if (std::fabs(F) < 1.0e-12) F = ZERO; }
+        } else if (IPP == 2) {
+            if (IL == IK) F = fmax2(F, 1.0e-6);
+            else if (IL == IEPS) F = fmax2(F, 1.0e-12);
+            else if (IL == IH) return;
+            else if (IL == 20) F = fmax2(F, 1.0e-1);
+            else if (IL == 8) F = fmax2(F, 1.0e-14);
+            else { F = fmin2(F, ONE); F = fmax2(F, ZERO); }
+        }
+    }
+
+    // ---- Gslv3x.f90 -----------------------------------------------------------
+    void ECELL(int I, int J, int K, int IU, double FFL[4][3]) {
+        if (IU == 1) {
+            int I1 = I - 1, I2 = I - 2;
+            for (int M = 1; M <= 2; ++M) {
+                if (ibcell(I2, J, K) >= 1) FFL[1][M] = DX[I1]; else FFL[1][M] = std::fabs(X[I] - X[I1]);
+                FFL[2][M] = FFL[1][M] * DZ[K];
+                FFL[3][M] = FFL[1][M] * RS[J] * DR[J];
+                I1 = I + 1; I2 = I + 2;
+            }
+        } else if (IU == 2) {
+            int J1 = J - 1, J2 = J - 2;
+            for (int M = 1; M <= 2; ++M) {
+                if (ibcell(I, J2, K) >= 1) FFL[2][M] = RS[J1] * DR[J1]; else FFL[2][M] = RS[J1] * std::fabs(R[J] - R[J1]);
+                FFL[1][M] = FFL[2][M] * DZ[K];
+                FFL[3][M] = FFL[2][M] * DX[I];
+                J1 = J + 1; J2 = J + 2;
+            }
+        } else {
+            int K1 = K - 1, K2 = K - 2;
+            for (int M = 1; M <= 2; ++M) {
+                if (ibcell(I, J, K2) >= 1) FFL[3][M] = DZ[K1]; else FFL[3][M] = std::fabs(Z[K] - Z[K1]);
+                FFL[1][M] = FFL[3][M] * RS[J] * DR[J];
+                FFL[2][M] = FFL[3][M] * DX[I];
+                K1 = K + 1; K2 = K + 2;
+            }
+        }
+    }
+    double FDDL(int I, int J, int K, int IU) {
+        double DDL;
+        int b = ibcell(I, J, K);
+        if (IU == 1) {
+            if (b <= 0) DDL = DX[I];
+            else if (ibcell(I + 1, J, K) == 0) DDL = X[I + 1] - X[I];
+            else if (ibcell(I - 1, J, K) == 0) DDL = X[I] - X[I - 1];
+            else DDL = BIG;
+        } else if (IU == 2) {
+            if (b <= 0) DDL = DR[J] * RS[J];
+            else if (ibcell(I, J + 1, K) == 0) DDL = (R[J + 1] - R[J]) * RS[J];
+            else if (ibcell(I, J - 1, K) == 0) DDL = (R[J] - R[J - 1]) * RS[J];
+            else DDL = BIG;
+        } else {
+            if (b <= 0) DDL = DZ[K];
+            else if (ibcell(I, J, K + 1) == 0) DDL = Z[K + 1] - Z[K];
+            else if (ibcell(I, J, K - 1) == 0) DDL = Z[K] - Z[K - 1];
+            else DDL = BIG;
+        }
+        return DDL;
+    }
+    double VOL1(int I, int J, int K, int IXD, double FFL[4][3]) {
+        double AREA = AREA_C(I, J, K, IXD);
+        double VOL = (FFL[IXD][1] + FFL[IXD][2]) * AREA;
+        if (IXD == 1) {
+            if (ibcell(I - 1, J, K) <= -1) VOL = VOL - DX[I - 1] * AREA / TWO;
+            if (ibcell(I + 1, J, K) <= -1) VOL = VOL - DX[I + 1] * AREA / TWO;
+        } else if (IXD == 2) {
+            if (ibcell(I, J - 1, K) <= -1) VOL = VOL - RS[J - 1] * DR[J - 1] * AREA / TWO;
+            if (ibcell(I, J + 1, K) <= -1) VOL = VOL - RS[J + 1] * DR[J + 1] * AREA / TWO;
+        } else {
+            if (ibcell(I, J, K - 1) <= -1) VOL = VOL - DZ[K - 1] * AREA / TWO;
+            if (ibcell(I, J, K + 1) <= -1) VOL = VOL - DZ[K + 1] * AREA / TWO;
+        }
+        return VOL;
+    }
+    double FLW(int I, int J, int K, int IXD, int M) {
+        double AREA = AREA_C(I, J, K, IXD);
+        double F = a3(THETA, I, J, K) * a3(DNST, I, J, K) * ug(I, J, K, IXD) * AREA;
+        return M == 1 ? fmax2(ZERO, F) : fmax2(ZERO, -F);
+    }
+    double FLWD(int I, int J, int K, int IXD, int M) {
+        double AREA = AREA_C(I, J, K, IXD);
+        double DDL = IXD == 1 ? DX[I] : (IXD == 2 ? DR[J] : DZ[K]);
+        double F = a3(THETA, I, J, K) * a3(DNST, I, J, K) * ug(I, J, K, IXD) * AREA;
+        double DIFF = a3(THETA, I, J, K) * a3(GAMA, I, J, K) / SGM * AREA / DDL;
+        return M == 1 ? DA(DIFF, F) + fmax2(ZERO, F) : DA(DIFF, F) + fmax2(ZERO, -F);
+    }
+    static void VINDX(int IU, int M, int I, int J, int K, int& I1, int& J1, int& K1, int& I2, int& J2, int& K2) {
+        int NX[4] = {0, 0, 0, 0};
+        NX[IU] = M;
+        I1 = I + NX[1]; I2 = I1 + NX[1];
+        J1 = J + NX[2]; J2 = J1 + NX[2];
+        K1 = K + NX[3]; K2 = K1 + NX[3];
+    }
+    void GSLV3X1(int I, int J, int K, int IU, double& G0) {
+        G0 = ZERO;
+        for (int M = -1; M <= 1; M += 2) {
+            int M1 = (M + 3) / 2, I1, J1, K1, I2, J2, K2;
+            VINDX(IU, M, I, J, K, I1, J1, K1, I2, J2, K2);
+            int IBC1 = ibcell(I2, J2, K2);
+            if (IBC1 == 3) as(I, J, K, IU, M1) = ZERO;
+            else if (IBC1 == 2) as(I, J, K, IU, M1) = FLW(I2, J2, K2, IU, M1);
+            else as(I, J, K, IU, M1) = FLWD(I1, J1, K1, IU, M1);
+            a3(AP, I, J, K) = a3(AP, I, J, K) + as(I, J, K, IU, M1);
+            G0 = G0 + as(I, J, K, IU, M1) * a3(FZ, I2, J2, K2);
+        }
+    }
+    void GSLVX1(int IU1) {
+        int NX[4] = {0, 0, 0, 0};
+        NX[IU1] = 1;
+        int MI1 = 4 + NX[1], MI3 = MPM2 - NX[1], NJ1 = NJY1V[IU1], NJ3 = NJY2V[IU1], LK1 = LKZ1V[IU1], LK3 = LKZ2V[IU1];
+        SOURCE(MI1, MI3, NJ1, NJ3, LK1, LK3);
+        double FFL[4][3];
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    a3(AP, I, J, K) = ZERO;
+                    double G0 = ZERO;
+                    GSLV3X1(I, J, K, IU1, G0);
+                    ECELL(I, J, K, IU1, FFL);
+                    for (int IU = 1; IU <= 3; ++IU) {
+                        if (IU == IU1) continue;
+                        for (int M = -1; M <= 1; M += 2) {
+                            int M1 = (M + 3) / 2, I1, J1, K1, I2, J2, K2;
+                            VINDX(IU, M, I, J, K, I1, J1, K1, I2, J2, K2);
+                            if (ibcell(I1, J1, K1) == 3) { as(I, J, K, IU, M1) = ZERO; continue; }
+                            double F = ZERO, DIFF = ZERO;
+                            int II1 = 0, JJ1 = 0, KK1 = 0;
+                            for (int Nn = -1; Nn <= 1; Nn += 2) {
+                                int N1 = (Nn + 3) / 2;
+                                II1 = I1 + NX[1] * Nn; JJ1 = J1 + NX[2] * Nn; KK1 = K1 + NX[3] * Nn;
+                                int IBC1 = ibcell(II1, JJ1, KK1);
+                                if (IBC1 == 3) continue;
+                                double AREA = FFL[IU][N1];
+                                F = F + a3(THETA, II1, JJ1, KK1) * a3(DNST, II1, JJ1, KK1) * a3(FZ, II1, JJ1, KK1) * AREA;
+                                if (IBC1 == 2) continue;
+                                double DDL = FDDL(II1, JJ1, KK1, IU);
+                                DIFF = DIFF + a3(THETA, II1, JJ1, KK1) * a3(GAMA, II1, JJ1, KK1) / SGM * AREA / DDL;
+                            }
+                            double FLD = M1 == 1 ? DA(DIFF, F) + fmax2(ZERO, F) : DA(DIFF, F) + fmax2(ZERO, -F);
+                            if (ibcell(II1, JJ1, KK1) == 2 && ibcell(I2, J2, K2) == 1) {
+                                double BS0 = FLD * (ug(II1, J2, K2, IU1) - ug(I, J, K, IU1));
+                                a3(BS, I, J, K) = a3(BS, I, J, K) + BS0;
+                                as(I, J, K, IU, M1) = ZERO;
+                                continue;
+                            }
+                            as(I, J, K, IU, M1) = FLD;
+                            a3(AP, I, J, K) = a3(AP, I, J, K) + FLD;
+                            G0 = G0 + FLD * a3(FZ, I2, J2, K2);
+                        }
+                    }
+                    const double EVPM = ZERO, CONM = ZERO;
+                    double VOL = VOL1(I, J, K, IU1, FFL);
+                    a3(BS, I, J, K) = a3(BS, I, J, K) * VOL;
+                    a3(AP, I, J, K) = a3(AP, I, J, K) + (EVPM - CONM - a3(SFP, I, J, K)) * VOL;
+                    if (std::fabs(a3(AP, I, J, K)) > small20) ug(I, J, K, IU1) = (G0 + a3(BS, I, J, K)) / a3(AP, I, J, K);
+                }
+    }
+
+    // ---- Source.f90 ------------------------------------------------------------
+    void SRC1(int I, int J, int K, int IU1) {
+        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = ZERO; a3(SFP, I, J, K) = ZERO; return; }
+        double VIS[4][3], DXN[4], DX1[4], DX0[4];
+        DXN[1] = DX[I]; DXN[2] = DR[J] * RS[J]; DXN[3] = DZ[K];
+        for (int M = -1; M <= 1; M += 2) {
+            int I1, J1, K1, I2, J2, K2;
+            VINDX(IU1, M, I, J, K, I1, J1, K1, I2, J2, K2);
+            if (IU1 == 1) { DX0[1] = DX[I]; DX1[1] = DX[I1]; }
+            else if (IU1 == 2) { DX0[2] = DR[J] * RS[J]; DX1[2] = DR[J1] * RS[J1]; }
+            else { DX0[3] = DZ[K]; DX1[3] = DZ[K1]; }
+            double THGM;
+            if (ibcell(I2, J2, K2) == 2) {
+                THGM = a3(THETA, I2, J2, K2) * a3(GAMA, I2, J2, K2);
+                if (IU1 == 1) DXN[1] = DXN[1] + std::fabs(X[I2] - X[I1]);
+                if (IU1 == 2) DXN[2] = DXN[2] + std::fabs(R[J2] - R[J1]) * RS[J];
+                if (IU1 == 3) DXN[3] = DXN[3] + std::fabs(Z[K2] - Z[K1]);
+            } else {
+                THGM = a3(THETA, I1, J1, K1) * a3(GAMA, I1, J1, K1);
+            }
+            if (M == -1) VIS[IU1][1] = THGM * (a3(FZ, I, J, K) - a3(FZ, I2, J2, K2)) / DX1[IU1];
+            else VIS[IU1][2] = THGM * (a3(FZ, I2, J2, K2) - a3(FZ, I, J, K)) / DX1[IU1];
+        }
+        double VMS = (VIS[IU1][2] - VIS[IU1][1]) / DXN[IU1];
+        for (int IU = 1; IU <= 3; ++IU) {
+            if (IU == IU1) continue;
+            int I1 = I, J1 = J, K1 = K;
+            for (int M = -1; M <= 1; M += 2) {
+                if (IU == 1) I1 = I + M; else if (IU == 2) J1 = J + M; else K1 = K + M;
+                double DU0;
+                if (IU1 == 1) DU0 = a3(FZ, I + 1, J1, K1) - a3(FZ, I - 1, J1, K1);
+                else if (IU1 == 2) DU0 = a3(FZ, I1, J + 1, K1) - a3(FZ, I1, J - 1, K1);
+                else DU0 = a3(FZ, I1, J1, K + 1) - a3(FZ, I1, J1, K - 1);
+                int M1 = (M + 3) / 2;
+                VIS[IU][M1] = a3(THETA, I1, J1, K1) * a3(GAMA, I1, J1, K1) * DU0 / DX0[IU1];
+                if (IU == 2) VIS[IU][M1] = VIS[IU][M1] * RS[J1];
+            }
+            VMS = VMS + (VIS[IU][2] - VIS[IU][1]) / DXN[IU];
+        }
+        const double GDZ = ZERO, GDZU = ZERO, DUAV = ZERO;   // single phase: KEY=1, no droplets
+        a3(BS, I, J, K) = VMS + GDZU + DUAV;
+        a3(BS, I, J, K) = a3(BS, I, J, K) + a3(THETA, I, J, K) * a3(DNST, I, J, K) * pr.gra[IU1 - 1];
+        a3(SFP, I, J, K) = -GDZ;
+    }
+
+    void calc_q_conv_wall() {   // Qwall.f90:1370-1475 (T in K: T*T0)
+        const double pi = 3.141592653589793;
+        const double kappa_cmu = 0.4 * std::pow(9.0e-2, 0.25), E_cmu = 9.0 * std::pow(9.0e-2, 0.25);
+        const double c_htw = 0.4 * ((pi / 4) / std::sin(pi / 4)) * std::sqrt(26.0) * (0.7 - ONE) / std::pow(0.7, 0.25);
+        qconv_total = ZERO;
+        for (size_t n = 0; n < b_typ.size(); ++n) {
+            if (b_typ[n] == 2 || b_typ[n] == 3) { q_conv[n] = ZERO; continue; }
+            int inc = b_i[n], jnc = b_j[n], knc = b_k[n];
+            double ds;
+            if (b_orient[n] == 1) {
+                if (b_direct[n] == 0) { inc = inc + 1; ds = X[b_i[n] + 1] - X[b_i[n]]; }
+                else { inc = inc - 1; ds = X[b_i[n]] - X[b_i[n] - 1]; }
+            } else if (b_orient[n] == 2) {
+                if (b_direct[n] == 0) { jnc = jnc + 1; ds = R[b_j[n] + 1] - R[b_j[n]]; }
+                else { jnc = jnc - 1; ds = R[b_j[n]] - R[b_j[n] - 1]; }
+            } else {
+                if (b_direct[n] == 0) { knc = knc + 1; ds = Z[b_k[n] + 1] - Z[b_k[n]]; }
+                else { knc = knc - 1; ds = Z[b_k[n]] - Z[b_k[n] - 1]; }
+            }
+            double cpmix = CP0 * (CPF1 * gf(inc, jnc, knc, IYF) + CPCO21 * gf(inc, jnc, knc, IYCO2) +
+                                  CPH2O1 * gf(inc, jnc, knc, IYH2O) + CPO21 * gf(inc, jnc, knc, IYO2) +
+                                  CPN21 * gf(inc, jnc, knc, IYN2));
+            double Tgas = a3(T, inc, jnc, knc) * pr.t0;
+            double gmu_T = ((2.0e-15 * Tgas + -1.1e-11) * Tgas + 4.5e-8) * Tgas + 7.0e-6;
+            double h_t;
+            if (pr.tk0 * gf(inc, jnc, knc, IK) < 0.1) {
+                h_t = ZERO;
+            } else {
+                double sqrt_tke = std::sqrt(pr.tk0 * gf(inc, jnc, knc, IK));
+                double dtmp = (std::log(E_cmu * ds * pr.dnst0 * a3(DNST, inc, jnc, knc) * sqrt_tke / gmu_T) + (c_htw / sqrt_tke));
+                if (dtmp < 0.01) h_t = ZERO;
+                else h_t = fmin2(50.0, cpmix * kappa_cmu * pr.dnst0 * a3(DNST, inc, jnc, knc) * sqrt_tke / dtmp);
+            }
+            double delta_T = Tgas - b_T[n];
+            q_conv[n] = fmax2(pr.h_g, h_t) * delta_T;
+            double patch_area = b_orient[n] == 1 ? DR[b_j[n]] * DZ[b_k[n]]
+                                : (b_orient[n] == 2 ? DX[b_i[n]] * DZ[b_k[n]] : DX[b_i[n]] * DR[b_j[n]]);
+            qconv_total = qconv_total + (q_conv[n] * patch_area);
+        }
+    }
+
+    void SOURCE(int MI1, int MI3, int NJ1, int NJ3, int LK1, int LK3) {
+        switch (NELG) {
+        case 1: case 2: case 3: {
+            int IU1 = NELG;
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) SRC1(I, J, K, IU1);
+            break;
+        }
+        case 4: case 5: {
+            if (NELG == 5) { res_mass = ZERO; res_mass_max = ZERO; }
+            for (int i = MI1; i <= MI3; i += 2)
+                for (int j = NJ1; j <= NJ3; j += 2)
+                    for (int k = LK1; k <= LK3; k += 2) {
+                        if (ibcell(i, j, k) >= 1) continue;
+                        double area_x = AREA_C(i, j, k, 1);
+                        double frx1 = (a3(THETA, i - 1, j, k) * a3(DNST, i - 1, j, k) * ug(i - 1, j, k, 1)) * area_x;
+                        double frx2 = (a3(THETA, i + 1, j, k) * a3(DNST, i + 1, j, k) * ug(i + 1, j, k, 1)) * area_x;
+                        double rx = frx1 - frx2;
+                        double area_y = AREA_C(i, j, k, 2);
+                        double fry1 = (a3(THETA, i, j - 1, k) * a3(DNST, i, j - 1, k) * ug(i, j - 1, k, 2)) * area_y;
+                        double fry2 = (a3(THETA, i, j + 1, k) * a3(DNST, i, j + 1, k) * ug(i, j + 1, k, 2)) * area_y;
+                        double ry = fry1 - fry2;
+                        double area_z = AREA_C(i, j, k, 3);
+                        double frz1 = (a3(THETA, i, j, k - 1) * a3(DNST, i, j, k - 1) * ug(i, j, k - 1, 3)) * area_z;
+                        double frz2 = (a3(THETA, i, j, k + 1) * a3(DNST, i, j, k + 1) * ug(i, j, k + 1, 3)) * area_z;
+                        double rz = frz1 - frz2;
+                        const double evms = ZERO;
+                        a3(BS, i, j, k) = (rx + ry + rz + evms) / pr.eun;
+                        a3(SFP, i, j, k) = ZERO;
+                        if (NELG == 5) {
+                            double r_mass;
+                            if (ibcell(i - 1, j, k) == 3 || ibcell(i + 1, j, k) == 3 || ibcell(i, j - 1, k) == 3 ||
+                                ibcell(i, j + 1, k) == 3 || ibcell(i, j, k - 1) == 3 || ibcell(i, j, k + 1) == 3) {
+                                continue;
+                            } else {
+                                double fmax = fmax2(fmax2(fmax2(fmax2(fmax2(fmax2(std::fabs(frx1), std::fabs(frx2)), std::fabs(fry1)),
+                                                                   std::fabs(fry2)), std::fabs(frz1)), std::fabs(frz2)), evms);
+                                if (fmax == ZERO) r_mass = ZERO;
+                                else r_mass = std::fabs(a3(BS, i, j, k)) * pr.eun / fmax;
+                            }
+                            if (res_mass_max < r_mass) res_mass_max = r_mass;
+                            res_mass = res_mass + r_mass;
+                        }
+                    }
+            if (NELG == 5) res_mass = res_mass / NCELLS;
+            break;
+        }
+        case 6: {
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) {
+                            a3(BS, I, J, K) = a3(FZ, I, J, K); a3(SFP, I, J, K) = ZERO;
+                            a3(CRATE, I, J, K) = ZERO; a3(HRATE, I, J, K) = ZERO;
+                            continue;
+                        }
+                        const double SC = ZERO;
+                        double D11 = std::fabs(ug(I + 1, J, K, 1) / DX[I]);
+                        double D12 = std::fabs(ug(I - 1, J, K, 1) / DX[I]);
+                        double D21 = 0, D22 = 0, D31 = 0, D32 = 0;
+                        if (NJ3 > 6) { D21 = std::fabs(ug(I, J + 1, K, 2) / DR[J]); D22 = std::fabs(ug(I, J - 1, K, 2) / DR[J]); }
+                        if (LK3 > 6) { D31 = std::fabs(ug(I, J, K + 1, 3) / DZ[K]); D32 = std::fabs(ug(I, J, K - 1, 3) / DZ[K]); }
+                        double DTIME = fmax2(fmax2(fmax2(fmax2(fmax2(fmax2(D11, D12), D21), D22), D31), D32), SMX0);
+                        DTIME = ONE / DTIME;
+                        double DRTIME = DTIME * pr.r0 / pr.ug0;
+                        double AYF = fmin2(gf(I, J, K, IYF), gf(I, J, K, IYO2) / pr.stoich);
+                        if (AYF < 1.0e-5) {
+                            a3(CRATE, I, J, K) = ZERO; a3(HRATE, I, J, K) = ZERO; a3(SFP, I, J, K) = ZERO; a3(BS, I, J, K) = ZERO;
+                            continue;
+                        }
+                        double ZP1 = gf(I, J, K, IYCO2) / WCO2, DELR1;
+                        if (ZP1 <= small20) DELR1 = ZERO;
+                        else { double ZF = gf(I, J, K, IYF) / WF; DELR1 = ZP1 / (ZF + ZP1); }
+                        double TIME1 = ZY1(DELR.data(), TIMED.data(), DELR1, NR0);
+                        double TIME2 = TIME1 + DRTIME;
+                        double DELR2 = ZY1(RTIM.data(), DELRT.data(), TIME2, NR0);
+                        double AYF0 = AYF / (ONE - DELR1) * a3(DNST, I, J, K) * a3(THETA, I, J, K);
+                        double SR = AYF0 * (DELR2 - DELR1) / DTIME;
+                        if (SR <= ZERO) {
+                            a3(CRATE, I, J, K) = ZERO; a3(HRATE, I, J, K) = ZERO; a3(SFP, I, J, K) = ZERO; a3(BS, I, J, K) = SC;
+                            continue;
+                        }
+                        a3(CRATE, I, J, K) = SR;
+                        a3(SFP, I, J, K) = -a3(CRATE, I, J, K) / (gf(I, J, K, IYF) + small20);
+                        a3(BS, I, J, K) = SC;
+                        a3(HRATE, I, J, K) = a3(CRATE, I, J, K) * pr.q0;
+                    }
+            break;
+        }
+        case 7: {
+            double G0 = WCO2 / WF;
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        a3(SFP, I, J, K) = ZERO;
+                        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); continue; }
+                        if (!pr.react) { a3(BS, I, J, K) = ZERO; continue; }
+                        a3(BS, I, J, K) = a3(CRATE, I, J, K) * G0;
+                    }
+            break;
+        }
+        case 8: case 9: {
+            if (NELG == 8) {
+                q_rad_vol_tot = ZERO; q_react = ZERO;
+                for (int I = MI1; I <= MI3; I += 2)
+                    for (int J = NJ1; J <= NJ3; J += 2)
+                        for (int K = LK1; K <= LK3; K += 2) {
+                            if (ibcell(I, J, K) >= 1) continue;
+                            double DUDX, DVDX, DWDX, DUDR, DVDR, DWDR, DUDZ, DVDZ, DWDZ;
+                            if (ibcell(I + 1, J, K) == 3 || ibcell(I - 1, J, K) == 3) { DUDX = DVDX = DWDX = ZERO; }
+                            else {
+                                DUDX = (ug(I + 1, J, K, 1) - ug(I - 1, J, K, 1)) / DX[I];
+                                DVDX = (ug(I + 1, J, K, 2) - ug(I - 1, J, K, 2)) / DX[I];
+                                DWDX = (ug(I + 1, J, K, 3) - ug(I - 1, J, K, 3)) / DX[I];
+                            }
+                            if (NJ3 < 6 || ibcell(I, J + 1, K) == 3 || ibcell(I, J - 1, K) == 3) { DUDR = DVDR = DWDR = ZERO; }
+                            else {
+                                DUDR = (ug(I, J + 1, K, 1) - ug(I, J - 1, K, 1)) / DR[J];
+                                DVDR = (ug(I, J + 1, K, 2) - ug(I, J - 1, K, 2)) / DR[J];
+                                DWDR = (ug(I, J + 1, K, 3) - ug(I, J - 1, K, 3)) / DR[J];
+                            }
+                            if (LK3 < 6 || ibcell(I, J, K + 1) == 3 || ibcell(I, J, K - 1) == 3) { DUDZ = DVDZ = DWDZ = ZERO; }
+                            else {
+                                DUDZ = (ug(I, J, K + 1, 1) - ug(I, J, K - 1, 1)) / DZ[K];
+                                DVDZ = (ug(I, J, K + 1, 2) - ug(I, J, K - 1, 2)) / DZ[K];
+                                DWDZ = (ug(I, J, K + 1, 3) - ug(I, J, K - 1, 3)) / DZ[K];
+                            }
+                            const double VR = ZERO;
+                            double s1 = DUDR + DVDX, s2 = DWDR + DVDZ, s3 = DUDZ + DWDX, s4 = DUDX + DVDR + DWDZ;
+                            a3(GTE, I, J, K) = TWO * (DUDX * DUDX + DVDR * DVDR + VR * VR + DWDZ * DWDZ) + s1 * s1 + s2 * s2 +
+                                               s3 * s3 - s4 * s4 / 1.5;
+                        }
+                for (int I = MI1; I <= MI3; I += 2) {
+                    int ID2 = I / 2;
+                    for (int J = NJ1; J <= NJ3; J += 2) {
+                        int JD2 = J / 2;
+                        for (int K = LK1; K <= LK3; K += 2) {
+                            if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); a3(SFP, I, J, K) = ZERO; continue; }
+                            int KD2 = K / 2;
+                            const double GDZ = ZERO, GDZH = ZERO;
+                            double CPMIX1 = CPF1 * gf(I, J, K, IYF) + CPCO21 * gf(I, J, K, IYCO2) + CPH2O1 * gf(I, J, K, IYH2O) +
+                                            CPO21 * gf(I, J, K, IYO2) + CPN21 * gf(I, J, K, IYN2);
+                            a3(BS, I, J, K) = GDZH + a3(HRATE, I, J, K);
+                            a3(SFP, I, J, K) = -GDZ / CPMIX1;
+                            double vol = VOL_C(I, J, K) * 1.0;   // *vol0
+                            q_react = q_react + a3(HRATE, I, J, K) * pr.qr0 * vol;
+                            if (i1st_rad_qe_done > 0) {
+                                double q_rad = QA[cix(ID2, JD2, KD2)] - QE[cix(ID2, JD2, KD2)];
+                                a3(BS, I, J, K) = a3(BS, I, J, K) + q_rad / (vol * pr.qr0);
+                                q_rad_vol_tot = q_rad_vol_tot - q_rad;
+                            }
+                        }
+                    }
+                }
+                if (pr.wall_sink) {
+                    // q_conv was evaluated at the start of GSLV3G (see GSLV3G)
+                    for (size_t n = 0; n < b_typ.size(); ++n) {
+                        if (b_typ[n] == 1 || b_typ[n] == 4) {
+                            int inc = b_i[n], jnc = b_j[n], knc = b_k[n];
+                            double ds;
+                            if (b_orient[n] == 1) { inc = b_direct[n] == 0 ? inc + 1 : inc - 1; ds = DX[inc]; }
+                            else if (b_orient[n] == 2) { jnc = b_direct[n] == 0 ? jnc + 1 : jnc - 1; ds = DR[jnc]; }
+                            else { knc = b_direct[n] == 0 ? knc + 1 : knc - 1; ds = DZ[knc]; }
+                            a3(BS, inc, jnc, knc) = a3(BS, inc, jnc, knc) - q_conv[n] / (ds * pr.r0 * pr.qr0);
+                        }
+                    }
+                }
+                if (itr_gas > 1) {
+                    for (int i = MI1; i <= MI3; i += 2)
+                        for (int j = NJ1; j <= NJ3; j += 2)
+                            for (int k = LK1; k <= LK3; k += 2) {
+                                if (ibcell(i, j, k) >= 1) continue;
+                                a3(BS, i, j, k) = pr.rf_hsource * a3(BS, i, j, k) + (ONE - pr.rf_hsource) * a3(bs_hprev, i, j, k);
+                            }
+                }
+                bs_hprev = BS;
+                break;
+            }
+            // NELG == 9: turbulent kinetic energy (LSTAR<=3: GTE from the enthalpy call)
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); a3(SFP, I, J, K) = ZERO; continue; }
+                        const double SUM = ZERO;
+                        a3(BS, I, J, K) = TWO / (pr.reyg * pr.epsr) * a3(THETA, I, J, K) * a3(TMU, I, J, K) * a3(GTE, I, J, K) - SUM;
+                        a3(SFP, I, J, K) = -(pr.taur * a3(THETA, I, J, K) * a3(DNST, I, J, K) * gf(I, J, K, IEPS) /
+                                             (gf(I, J, K, IK) + small20));
+                    }
+            break;
+        }
+        case 10: {
+            double CBL0 = 2.5 * std::sqrt(pr.epsr) / pr.taur * std::pow(pr.cmu, 0.75);
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        a3(SFP, I, J, K) = ZERO;
+                        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); continue; }
+                        double CBL = CBL0 * std::pow(gf(I, J, K, IK), 1.5);
+                        a3(BS, I, J, K) = ZERO;
+                        if (MP > 8 && ibcell(I + 1, J, K) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (X[I + 1] - X[I]); a3(SFP, I, J, K) = -BIG; }
+                        if (MP > 8 && ibcell(I - 1, J, K) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (X[I] - X[I - 1]); a3(SFP, I, J, K) = -BIG; }
+                        if (NP > 8 && ibcell(I, J + 1, K) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (R[J + 1] - R[J]); a3(SFP, I, J, K) = -BIG; }
+                        if (NP > 8 && ibcell(I, J - 1, K) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (R[J] - R[J - 1]); a3(SFP, I, J, K) = -BIG; }
+                        if (LP > 8 && ibcell(I, J, K + 1) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (Z[K + 1] - Z[K]); a3(SFP, I, J, K) = -BIG; }
+                        if (LP > 8 && ibcell(I, J, K - 1) == 1) { a3(BS, I, J, K) = a3(BS, I, J, K) + BIG * CBL / (Z[K] - Z[K - 1]); a3(SFP, I, J, K) = -BIG; }
+                        if (a3(SFP, I, J, K) <= -BIG) continue;
+                        double BT = a3(THETA, I, J, K);
+                        a3(BS, I, J, K) = pr.ct1 * pr.cmu * BT / pr.taur * a3(DNST, I, J, K) * a3(GTE, I, J, K) * gf(I, J, K, IK);
+                        a3(SFP, I, J, K) = -(pr.ct2 * pr.taur * BT * a3(DNST, I, J, K) * gf(I, J, K, IEPS) / (gf(I, J, K, IK) + small20));
+                    }
+            break;
+        }
+        case 11: {
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); a3(SFP, I, J, K) = ZERO; continue; }
+                        a3(BS, I, J, K) = ZERO; a3(SFP, I, J, K) = ZERO;
+                    }
+            break;
+        }
+        case 12: {
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        a3(SFP, I, J, K) = ZERO;
+                        if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(FZ, I, J, K); continue; }
+                        if (!pr.react) { a3(BS, I, J, K) = ZERO; continue; }
+                        a3(BS, I, J, K) = -a3(CRATE, I, J, K) * pr.stoich;
+                    }
+            break;
+        }
+        default: break;
+        }
+    }
+
+    // ---- Adlbl3.f90 ----------------------------------------------------------------
+    // XT2/XT3 are (NP,LP) planes, 1-based
+    vec XT2, XT3;
+    int JBML, JEPL, IPL, IML;
+    double& p2(vec& v, int j, int k) { return v[(long)(j - 1) + (long)NP * (k - 1)]; }
+
+    void ADLZY(vec& XT, int LD, int I, int JB, int JE, int K) {
+        if (JE == 2) return;
+        int KPL = K + LD, KML = K - LD;
+        std::vector<double> PT(NP + 2, 0.0), QT(NP + 2, 0.0);
+        PT[JBML] = ZERO;
+        QT[JBML] = XT[ix(I, JBML, K)];
+        for (int J = JB; J <= JE; J += LD) {
+            int JML = J - LD;
+            double ALP = a3(AP, I, J, K) - PT[JML] * as(I, J, K, 2, 1);
+            double BSY = a3(BS, I, J, K);
+            if (std::fabs(ALP) <= small20 || ibcell(I * 2 / LD, J * 2 / LD, K * 2 / LD) >= 1) {
+                PT[J] = ZERO;
+                QT[J] = XT[ix(I, J, K)];
+            } else {
+                PT[J] = as(I, J, K, 2, 2) / ALP;
+                BSY = BSY + as(I, J, K, 1, 2) * XT[ix(IPL, J, K)] + as(I, J, K, 1, 1) * XT[ix(IML, J, K)];
+                if (LP >= 6) BSY = BSY + as(I, J, K, 3, 2) * XT[ix(I, J, KPL)] + as(I, J, K, 3, 1) * XT[ix(I, J, KML)];
+                QT[J] = (BSY + as(I, J, K, 2, 1) * QT[JML]) / ALP;
+            }
+        }
+        for (int J = JE; J >= JB; J -= LD) p2(XT2, J, K) = p2(XT2, J + LD, K) * PT[J] + QT[J];
+    }
+    void ADLYZ(vec& XT, int LD, int I, int J, int KB, int KE) {
+        if (LP == 2) return;
+        int JPL = J + LD, JML = J - LD, KBML = KB - LD;
+        std::vector<double> PT(LP + 2, 0.0), QT(LP + 2, 0.0);
+        PT[KBML] = ZERO;
+        QT[KBML] = XT[ix(I, J, KBML)];
+        for (int K = KB; K <= KE; K += LD) {
+            int KML = K - LD;
+            double ALP = a3(AP, I, J, K) - PT[KML] * as(I, J, K, 3, 1);
+            double BSY = a3(BS, I, J, K);
+            if (std::fabs(ALP) <= small20 || ibcell(I * 2 / LD, J * 2 / LD, K * 2 / LD) >= 1) {
+                PT[K] = ZERO;
+                QT[K] = XT[ix(I, J, K)];
+            } else {
+                PT[K] = as(I, J, K, 3, 2) / ALP;
+                BSY = BSY + as(I, J, K, 1, 2) * XT[ix(IPL, J, K)] + as(I, J, K, 1, 1) * XT[ix(IML, J, K)];
+                if (NP >= 6) BSY = BSY + as(I, J, K, 2, 2) * XT[ix(I, JPL, K)] + as(I, J, K, 2, 1) * XT[ix(I, JML, K)];
+                QT[K] = (BSY + as(I, J, K, 3, 1) * QT[KML]) / ALP;
+            }
+        }
+        for (int K = KE; K >= KB; K -= LD) p2(XT3, J, K) = p2(XT3, J, K + LD) * PT[K] + QT[K];
+    }
+    void ADLZ(vec& XT, int LD, int I, int JB, int JE, int KB, int KE) {
+        int KEPL = (LP == 2) ? KE : KE + LD;
+        for (int K = KB; K <= KEPL; K += LD)
+            for (int J = JB; J <= JEPL; J += LD) { p2(XT2, J, K) = XT[ix(I, J, K)]; p2(XT3, J, K) = XT[ix(I, J, K)]; }
+        for (int L = 1; L <= 2; ++L) {
+            for (int K = KB; K <= KE; K += LD) ADLZY(XT, LD, I, JB, JE, K);
+            if (KB >= KE) {
+                for (int K = KB; K <= KE; K += LD)
+                    for (int J = JB; J <= JE; J += LD) XT[ix(I, J, K)] = p2(XT2, J, K);
+                return;
+            }
+            for (int J = JB; J <= JE; J += LD) ADLYZ(XT, LD, I, J, KB, KE);
+            for (int K = KB; K <= KE; K += LD)
+                for (int J = JB; J <= JE; J += LD) XT[ix(I, J, K)] = (p2(XT2, J, K) + p2(XT3, J, K)) / TWO;
+        }
+    }
+    void ADLBL3(vec& XT, int IB, int IE, int JB, int JE, int KB, int KE, int NIM) {
+        const int LD = 2;
+        if (JE == 2) { JBML = JB; JEPL = JE; } else { JBML = JB - LD; JEPL = JE + LD; }
+        XT2.assign((long)NP * LP, 0.0);
+        XT3.assign((long)NP * LP, 0.0);
+        for (int Ns = 1; Ns <= NIM; ++Ns) {
+            for (int I = IB; I <= IE; I += LD) { IPL = I + LD; IML = I - LD; ADLZ(XT, LD, I, JB, JE, KB, KE); }
+            for (int I = IE; I >= IB; I -= LD) { IPL = I + LD; IML = I - LD; ADLZ(XT, LD, I, JB, JE, KB, KE); }
+        }
+        // end-of-call RESG residual (Adlbl3.f90:60-94) only feeds the final print (Sprint.f90:33): not kept
+    }
+
+    double calc_residual(vec& xt, int ib, int ie, int jb, int je, int kb, int ke) {   // Adlbl3.f90:239-271
+        double resid = ZERO;
+        for (int k = kb; k <= ke; k += 2)
+            for (int j = jb; j <= je; j += 2)
+                for (int i = ib; i <= ie; i += 2) {
+                    if (ibcell(i, j, k) > 0) continue;
+                    double t1 = as(i, j, k, 1, 1) * xt[ix(i - 2, j, k)], t2 = as(i, j, k, 1, 2) * xt[ix(i + 2, j, k)];
+                    double t3 = as(i, j, k, 2, 1) * xt[ix(i, j - 2, k)], t4 = as(i, j, k, 2, 2) * xt[ix(i, j + 2, k)];
+                    double t5 = as(i, j, k, 3, 1) * xt[ix(i, j, k - 2)], t6 = as(i, j, k, 3, 2) * xt[ix(i, j, k + 2)];
+                    double t7 = a3(AP, i, j, k) * xt[ix(i, j, k)], t8 = a3(BS, i, j, k);
+                    double eq_max = fmax2(fmax2(fmax2(fmax2(fmax2(fmax2(fmax2(std::fabs(t1), std::fabs(t2)), std::fabs(t3)),
+                                                                  std::fabs(t4)), std::fabs(t5)), std::fabs(t6)), std::fabs(t7)),
+                                          std::fabs(t8));
+                    resid = resid + std::fabs(t1 + t2 + t3 + t4 + t5 + t6 + t8 - t7) / eq_max;
+                }
+        resid = resid / NCELLS;
+        return resid > 1.0e-16 ? resid : 1.0e-16;   // MAX(resid,1d-16): a NaN sum gives 1d-16
+    }
+
+    // ---- Gslv3v.f90 --------------------------------------------------------------
+    void GSLV3V_momasm() {
+        SGM = ONE;
+        std::fill(AP.begin(), AP.end(), ONE);
+        std::fill(AS.begin(), AS.end(), ZERO);
+        for (int IU1 = 1; IU1 <= 3; ++IU1) {
+            int NX[4] = {0, 0, 0, 0}; NX[IU1] = 1;
+            for (int I = 2 + NX[1]; I <= MP - NX[1]; I += 2)
+                for (int J = 2 + NX[2]; J <= NP - NX[2]; J += 2)
+                    for (int K = 2 + NX[3]; K <= LP - NX[3]; K += 2) a3(FZ, I, J, K) = ug(I, J, K, IU1);
+        }
+        for (int IU1 = 1; IU1 <= 3; ++IU1) { NELG = IU1; GSLVX1(IU1); }
+    }
+    void GSLV3V_psolve() {
+        NELG = 4;
+        int MI1 = 4, MI3 = MPM2, NJ1 = NJY1, NJ3 = NJY2, LK1 = LKZ1, LK3 = LKZ2;
+        SOURCE(MI1, MI3, NJ1, NJ3, LK1, LK3);
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) { a3(BS, I, J, K) = a3(P, I, J, K); continue; }
+                    a3(AP, I, J, K) = -a3(SFP, I, J, K);
+                    int I1 = I - 1;
+                    for (int M = 1; M <= 2; ++M) {
+                        if (M == 2) I1 = I + 1;
+                        int IBC1 = ibcell(I1, J, K);
+                        if (IBC1 <= 0 && std::fabs(a3(AP, I1, J, K)) > small20) {
+                            double AREA = AREA_C(I, J, K, 1);
+                            double th = a3(THETA, I1, J, K);
+                            as(I, J, K, 1, M) = th * th * a3(DNST, I1, J, K) * (AREA * AREA) / a3(AP, I1, J, K) * DXAV(I1, J, K) / DX[I1];
+                        }
+                        a3(AP, I, J, K) = a3(AP, I, J, K) + as(I, J, K, 1, M);
+                    }
+                    int J1 = J - 1;
+                    for (int M = 1; M <= 2; ++M) {
+                        if (M == 2) J1 = J + 1;
+                        int IBC1 = ibcell(I, J1, K);
+                        if (IBC1 <= 0 && std::fabs(a3(AP, I, J1, K)) > small20) {
+                            double AREA = AREA_C(I, J, K, 2);
+                            double th = a3(THETA, I, J1, K);
+                            as(I, J, K, 2, M) = th * th * a3(DNST, I, J1, K) * (AREA * AREA) / a3(AP, I, J1, K) * DRAV(I, J1, K) / DR[J1];
+                        }
+                        a3(AP, I, J, K) = a3(AP, I, J, K) + as(I, J, K, 2, M);
+                    }
+                    int K1 = K - 1;
+                    for (int M = 1; M <= 2; ++M) {
+                        if (M == 2) K1 = K + 1;
+                        int IBC1 = ibcell(I, J, K1);
+                        if (IBC1 <= 0 && std::fabs(a3(AP, I, J, K1)) > small20) {
+                            double AREA = AREA_C(I, J, K, 3);
+                            double th = a3(THETA, I, J, K1);
+                            as(I, J, K, 3, M) = th * th * a3(DNST, I, J, K1) * (AREA * AREA) / a3(AP, I, J, K1) * DZAV(I, J, K1) / DZ[K1];
+                        }
+                        a3(AP, I, J, K) = a3(AP, I, J, K) + as(I, J, K, 3, M);
+                    }
+                }
+        p_resid_pre = calc_residual(P, MI1, MI3, NJ1, NJ3, LK1, LK3);
+        ADLBL3(P, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesg[NELG - 1]);
+        p_resid = calc_residual(P, MI1, MI3, NJ1, NJ3, LK1, LK3);
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    BOUND(a3(P, I, J, K), 0, 1);
+                }
+    }
+    void GSLV3V_momsolve() {
+        for (int IU1 = 1; IU1 <= 3; ++IU1) {
+            NELG = IU1;
+            int NX[4] = {0, 0, 0, 0}; NX[IU1] = 1;
+            int MI1 = 4 + NX[1], MI3 = MPM2 - NX[1], NJ1 = NJY1V[IU1], NJ3 = NJY2V[IU1], LK1 = LKZ1V[IU1], LK3 = LKZ2V[IU1];
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        a3(AP, I, J, K) = a3(AP, I, J, K) / pr.rf[NELG - 1];
+                        double VOL = VOL_C(I, J, K), DPDX;
+                        if (IU1 == 1) DPDX = (a3(P, I - 1, J, K) - a3(P, I + 1, J, K)) / DX[I];
+                        else if (IU1 == 2) DPDX = (a3(P, I, J - 1, K) - a3(P, I, J + 1, K)) / DR[J] / RS[J];
+                        else DPDX = (a3(P, I, J, K - 1) - a3(P, I, J, K + 1)) / DZ[K];
+                        a3(BS, I, J, K) = a3(BS, I, J, K) + pr.eun * a3(THETA, I, J, K) * VOL * DPDX +
+                                          RFC[NELG - 1] * a3(AP, I, J, K) * a3(FZ, I, J, K);
+                    }
+            u_resid_pre[IU1 - 1] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            ADLBL3(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesg[NELG - 1]);
+            u_resid[IU1 - 1] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        BOUND(a3(FZ, I, J, K), IU1, 1);
+                        ug(I, J, K, IU1) = a3(FZ, I, J, K);
+                    }
+        }
+    }
+    void GSLV3V_pcorr() {
+        NELG = 5;
+        int MI1 = 4, MI3 = MPM2, NJ1 = NJY1, NJ3 = NJY2, LK1 = LKZ1, LK3 = LKZ2;
+        SOURCE(MI1, MI3, NJ1, NJ3, LK1, LK3);
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) a3(FZ, I, J, K) = ZERO;
+        ADLBL3(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesg[NELG - 1]);
+        pcorr_resid = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+    }
+    void GSLV3V_velcorr() {
+        for (int IU1 = 1; IU1 <= 3; ++IU1) {
+            int NX[4] = {0, 0, 0, 0}; NX[IU1] = 1;
+            int MI1 = 4 + NX[1], MI3 = MPM2 - NX[1], NJ1 = NJY1V[IU1], NJ3 = NJY2V[IU1], LK1 = LKZ1V[IU1], LK3 = LKZ2V[IU1];
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1 || std::fabs(a3(AP, I, J, K)) < small20) continue;
+                        double VOL = VOL_C(I, J, K), DPDX;
+                        if (IU1 == 1) DPDX = (a3(FZ, I - 1, J, K) - a3(FZ, I + 1, J, K)) / DX[I];
+                        else if (IU1 == 2) DPDX = (a3(FZ, I, J - 1, K) - a3(FZ, I, J + 1, K)) / DR[J] / RS[J];
+                        else DPDX = (a3(FZ, I, J, K - 1) - a3(FZ, I, J, K + 1)) / DZ[K];
+                        double G0 = pr.eun * a3(THETA, I, J, K) * DPDX * VOL / (a3(AP, I, J, K) * pr.rf[IU1 - 1]);
+                        ug(I, J, K, IU1) = ug(I, J, K, IU1) + G0;
+                        BOUND(ug(I, J, K, IU1), IU1, 1);
+                    }
+        }
+    }
+    void GSLV3V_exits() {
+        EXTRV(0);
+        GFIN = GFIN0 * pr.gmfr;   // FLX1D, NPHAS=1 (Flx1d.f90:75-77)
+        if (itr_gas > 10) {
+            if (GFEX < small20) { FACTOR = ONE; FADJ = ZERO; }
+            else {
+                FACTOR = GFIN / GFEX;
+                if (FACTOR > pr.f_mx) { FACTOR = pr.f_mx; FADJ = ZERO; }
+                else if (FACTOR < pr.f_mn) { FACTOR = pr.f_mn; FADJ = ZERO; }
+            }
+        }
+        EXTRV(1);
+        INTPV();
+    }
+
+    // ---- Extr.f90 ----------------------------------------------------------------
+    void EXTR1(double& F1, double& F2, int I, int J, int K, int I1, int J1, int K1, int I2, int J2, int K2, int IXD) {
+        F2 = ZERO;
+        int IBC0 = ibcell(I, J, K) % 10;
+        if (IXD == 3) {
+            double DZK = Z[K2] - Z[K1];
+            if (DZK != ZERO) { int K0 = IBC0 == 2 ? (K + K1) / 2 : K; F2 = (Z[K0] - Z[K1]) / DZK; }
+        } else if (IXD == 2) {
+            double DRJ = R[J2] - R[J1];
+            if (DRJ != ZERO) { int J0 = IBC0 == 2 ? (J + J1) / 2 : J; F2 = (R[J0] - R[J1]) / DRJ; }
+        } else if (IXD == 1) {
+            double DXI = X[I2] - X[I1];
+            if (DXI != ZERO) { int I0 = IBC0 == 2 ? (I + I1) / 2 : I; F2 = (X[I0] - X[I1]) / DXI; }
+        }
+        F1 = ONE - F2;
+    }
+    // EXT0 / EXT1 (Extr.f90:575-661).  Returns false when no neighbour was
+    // found (the reference then keeps the loop's last indices and IX=4).
+    bool EXT01(bool wall, int I, int J, int K, int& I1, int& J1, int& K1, int& I2, int& J2, int& K2, int& IXD) {
+        for (IXD = 1; IXD <= 3; ++IXD) {
+            int NX[4] = {0, 0, 0, 0}; NX[IXD] = 1;
+            for (int M = -2; M <= 2; M += 4) {
+                I1 = std::max(2, std::min(MP, I + M * NX[1]));
+                J1 = std::max(2, std::min(NP, J + M * NX[2]));
+                K1 = std::max(2, std::min(LP, K + M * NX[3]));
+                bool hit = wall ? (ibcell(I1, J1, K1) % 10 != 1) : (ibcell(I1, J1, K1) <= 0);
+                if (hit) {
+                    I2 = std::max(2, std::min(MP, I1 + M * NX[1]));
+                    J2 = std::max(2, std::min(NP, J1 + M * NX[2]));
+                    K2 = std::max(2, std::min(LP, K1 + M * NX[3]));
+                    if (ibcell(I2, J2, K2) % 10 == 1) { I2 = I1; J2 = J1; K2 = K1; }
+                    return true;
+                }
+            }
+        }
+        // fall-through: last tried indices are (I,J,min(LP,K+2)); I2 keeps a
+        // stale value in the reference and enters only with weight F2=0
+        IXD = 4;
+        I2 = I1; J2 = J1; K2 = K1;
+        return false;
+    }
+    void SBC4(int I1, int J1, int K1, int I, int J, int K) {
+        a3(P, I, J, K) = a3(P, I1, J1, K1);
+        a3(T, I, J, K) = a3(T, I1, J1, K1);
+        for (int L = 1; L <= 9; ++L) gf(I, J, K, L) = gf(I1, J1, K1, L);
+        a3(DNST, I, J, K) = a3(DNST, I1, J1, K1);
+        a3(THETA, I, J, K) = a3(THETA, I1, J1, K1);
+        a3(TMU, I, J, K) = a3(TMU, I1, J1, K1);
+        a3(GAMA, I, J, K) = a3(GAMA, I1, J1, K1);
+    }
+    void EXTR() {   // EXTR(1): gas-phase variables
+        GFIN0 = ZERO;
+        q_exhaust = ZERO;
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    int IBC0 = ibcell(I, J, K) % 10;
+                    if (IBC0 != 2 && IBC0 != 3) continue;
+                    int I1, J1, K1, I2, J2, K2, IXD;
+                    EXT01(false, I, J, K, I1, J1, K1, I2, J2, K2, IXD);
+                    double F1, F2;
+                    EXTR1(F1, F2, I, J, K, I1, J1, K1, I2, J2, K2, IXD);
+                    gf(I, J, K, IEPS) = gf(I1, J1, K1, IEPS);
+                    a3(P, I, J, K) = a3(P, I1, J1, K1) * F1 + a3(P, I2, J2, K2) * F2;
+                    if (IBC0 == 2) {
+                        double G0 = a3(TMU, I, J, K);
+                        THER(I, J, K);
+                        a3(TMU, I, J, K) = G0;
+                        a3(GAMA, I, J, K) = a3(GAMA, I1, J1, K1);
+                        double AREA = AREA_C(I, J, K, IXD);
+                        G0 = a3(THETA, I, J, K) * a3(DNST, I, J, K) * ug(I, J, K, IXD) * AREA;
+                        GFIN0 = GFIN0 + std::fabs(G0);
+                        continue;
+                    }
+                    a3(TMU, I, J, K) = a3(TMU, I1, J1, K1);
+                    a3(GAMA, I, J, K) = a3(GAMA, I1, J1, K1);
+                    for (int L = LSTAR; L <= LEND; ++L) {
+                        if (L == IEPS) continue;
+                        double G0 = gf(I1, J1, K1, L) * F1 + gf(I2, J2, K2, L) * F2;
+                        if (L == IK) gf(I, J, K, IK) = fmax2(G0, 1.0e-6);
+                        else if (L == IH) gf(I, J, K, L) = G0;
+                        else gf(I, J, K, L) = fmax2(G0, ZERO);
+                    }
+                    enth_to_T_at(I, J, K);
+                    dnst_calc(I, J, K);
+                    double AREA = AREA_C(I, J, K, IXD) * 1.0;
+                    double G0 = std::fabs(ug(I, J, K, IXD)) * pr.ug0 * AREA;
+                    G0 = G0 * a3(THETA, I, J, K) * a3(DNST, I, J, K) * pr.dnst0;
+                    q_exhaust = q_exhaust + gf(I, J, K, IH) * pr.h_0 * G0;
+                    if (IBC0 == 3) SBC4(I, J, K, (I + I1) / 2, (J + J1) / 2, (K + K1) / 2);
+                }
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    int IBC0 = ibcell(I, J, K) % 10;
+                    if (IBC0 != 1) continue;
+                    int I1, J1, K1, I2, J2, K2, IXD;
+                    EXT01(true, I, J, K, I1, J1, K1, I2, J2, K2, IXD);
+                    double F1, F2;
+                    EXTR1(F1, F2, I, J, K, I1, J1, K1, I2, J2, K2, IXD);
+                    a3(P, I, J, K) = a3(P, I1, J1, K1) * F1 + a3(P, I2, J2, K2) * F2;
+                    a3(TMU, I, J, K) = a3(TMU, I2, J2, K2);
+                    a3(GAMA, I, J, K) = a3(GAMA, I2, J2, K2);
+                    for (int L = LSTAR; L <= LEND; ++L)
+                        if (L != IH) gf(I, J, K, L) = gf(I1, J1, K1, L);
+                    // walls adiabatic until the first full radiation call (i1st_rad_done=0)
+                    gf(I, J, K, IH) = gf(I1, J1, K1, IH);
+                    a3(T, I, J, K) = a3(T, I1, J1, K1);
+                    dnst_calc(I, J, K);
+                }
+    }
+    void EXTRV(int MEX) {   // Extr.f90:358-567
+        double Tarea_mean = 0, area_ex = 0;
+        if (MEX == 0) { GFEX = ZERO; Tmean_ex = ZERO; }
+        int IU = 1;
+        for (int I = 3; I <= MPM1; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    if (ibcell(I, J, K) % 10 != 3) continue;
+                    bool done = false;
+                    for (int M = -1; M <= 1 && !done; M += 2) {
+                        if (ibcell(I + M, J, K) >= 1) continue;
+                        int I0 = I - M, I1 = I + 2 * M;
+                        if (ug(I1, J, K, IU) * M > ZERO) ug(I1, J, K, IU) = ZERO;
+                        double AREA = AREA_C(I, J, K, IU);
+                        area_ex = area_ex + AREA;
+                        double G0 = a3(THETA, I1, J, K) * a3(DNST, I1, J, K) * ug(I1, J, K, IU) * AREA;
+                        if (MEX == 0) {
+                            GFEX = GFEX + std::fabs(G0);
+                            Tmean_ex = Tmean_ex + a3(T, I, J, K) * std::fabs(G0);
+                            Tarea_mean = Tarea_mean + a3(T, I, J, K) * AREA;
+                            done = true; break;
+                        }
+                        ug(I1, J, K, IU) = ug(I1, J, K, IU) * FACTOR;
+                        G0 = G0 * FACTOR;
+                        ug(I, J, K, IU) = G0 / (a3(THETA, I, J, K) * a3(DNST, I, J, K) * AREA);
+                        BOUND(ug(I, J, K, IU), IU, 1);
+                        ug(I0, J, K, IU) = ug(I, J, K, IU);
+                        done = true; break;
+                    }
+                    if (done) continue;
+                    if (J > 2 && ibcell(I, J - 2, K) <= 0) ug(I, J, K, IU) = ug(I, J - 2, K, IU);
+                    else if (J < NP && ibcell(I, J + 2, K) <= 0) ug(I, J, K, IU) = ug(I, J + 2, K, IU);
+                    else if (K > 2 && ibcell(I, J, K - 2) <= 0) ug(I, J, K, IU) = ug(I, J, K - 2, IU);
+                    else if (K < LP && ibcell(I, J, K + 2) <= 0) ug(I, J, K, IU) = ug(I, J, K + 2, IU);
+                }
+        IU = 2;
+        for (int J = 3; J <= NPM1; J += 2)
+            for (int K = 2; K <= LP; K += 2)
+                for (int I = 2; I <= MP; I += 2) {
+                    if (ibcell(I, J, K) % 10 != 3) continue;
+                    bool done = false;
+                    for (int M = -1; M <= 1 && !done; M += 2) {
+                        if (ibcell(I, J + M, K) >= 1) continue;
+                        int J0 = J - M, J1 = J + 2 * M;
+                        if (ug(I, J1, K, IU) * M > ZERO) ug(I, J1, K, IU) = ZERO;
+                        double AREA = AREA_C(I, J, K, IU);
+                        area_ex = area_ex + AREA;
+                        double G0 = a3(THETA, I, J1, K) * a3(DNST, I, J1, K) * ug(I, J1, K, IU) * AREA;
+                        if (MEX == 0) {
+                            GFEX = GFEX + std::fabs(G0);
+                            Tmean_ex = Tmean_ex + a3(T, I, J, K) * std::fabs(G0);
+                            Tarea_mean = Tarea_mean + a3(T, I, J, K) * AREA;
+                            done = true; break;
+                        }
+                        ug(I, J1, K, IU) = ug(I, J1, K, IU) * FACTOR;
+                        G0 = G0 * FACTOR;
+                        ug(I, J, K, IU) = G0 / (a3(THETA, I, J, K) * a3(DNST, I, J, K) * AREA);
+                        BOUND(ug(I, J, K, IU), IU, 1);
+                        ug(I, J0, K, IU) = ug(I, J, K, IU);
+                        done = true; break;
+                    }
+                    if (done) continue;
+                    if (K > 2 && ibcell(I, J, K - 2) <= 0) ug(I, J, K, IU) = ug(I, J, K - 2, IU);
+                    else if (K < LP && ibcell(I, J, K + 2) <= 0) ug(I, J, K, IU) = ug(I, J, K + 2, IU);
+                    else if (I > 2 && ibcell(I - 2, J, K) <= 0) ug(I, J, K, IU) = ug(I - 2, J, K, IU);
+                    else if (I < MP && ibcell(I + 2, J, K) <= 0) ug(I, J, K, IU) = ug(I + 2, J, K, IU);
+                }
+        IU = 3;
+        for (int K = 3; K <= LPM1; K += 2)
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2) {
+                    if (ibcell(I, J, K) % 10 != 3) continue;
+                    bool done = false;
+                    for (int M = -1; M <= 1 && !done; M += 2) {
+                        if (ibcell(I, J, K + M) >= 1) continue;
+                        int K1 = K + 2 * M;
+                        if (ug(I, J, K1, IU) * M > ZERO) ug(I, J, K1, IU) = ZERO;
+                        double AREA = AREA_C(I, J, K, IU);
+                        area_ex = area_ex + AREA;
+                        double G0 = a3(THETA, I, J, K1) * a3(DNST, I, J, K1) * ug(I, J, K1, IU) * AREA;
+                        if (MEX == 0) {
+                            GFEX = GFEX + std::fabs(G0);
+                            Tmean_ex = Tmean_ex + a3(T, I, J, K) * std::fabs(G0);
+                            Tarea_mean = Tarea_mean + a3(T, I, J, K) * AREA;
+                            done = true; break;
+                        }
+                        ug(I, J, K1, IU) = ug(I, J, K1, IU) * FACTOR;
+                        done = true; break;   // GOTO 160 (Extr.f90:529)
+                    }
+                    if (done) continue;
+                    if (I > 2 && ibcell(I - 2, J, K) <= 0) ug(I, J, K, IU) = ug(I - 2, J, K, IU);
+                    else if (I < MP && ibcell(I + 2, J, K) <= 0) ug(I, J, K, IU) = ug(I + 2, J, K, IU);
+                    else if (J > 2 && ibcell(I, J - 2, K) <= 0) ug(I, J, K, IU) = ug(I, J - 2, K, IU);
+                    else if (J < NP && ibcell(I, J + 2, K) <= 0) ug(I, J, K, IU) = ug(I, J + 2, K, IU);
+                }
+        if (MEX == 0) {
+            GFEX = GFEX * pr.gmfr;
+            if (GFEX < small16) Tmean_ex = Tarea_mean * pr.t0 / area_ex;
+            else Tmean_ex = Tmean_ex * pr.t0 * pr.gmfr / GFEX;
+        }
+    }
+
+    // ---- Intp.f90 ------------------------------------------------------------------
+    double INTP1(int I, int J, int K, int IXD) {
+        double F1;
+        if (IXD == 3) F1 = (DZ[K] <= ZERO || K > LP) ? ZERO : (Z[K] - Z[K - 1]) / DZ[K];
+        else if (IXD == 2) F1 = (DR[J] <= ZERO || J > NP) ? ZERO : (R[J] - R[J - 1]) / DR[J];
+        else F1 = (DX[I] <= ZERO || I > MP) ? ZERO : (X[I] - X[I - 1]) / DX[I];
+        return F1;
+    }
+    // F1 is the caller's variable (Fortran pass by reference): INTP0 may
+    // overwrite it and the caller keeps the new value for later positions.
+    void INTP0(double& F1, int I, int J, int K, int I1, int J1, int K1, int I2, int J2, int K2) {
+        if (ibcell(I, J, K) == 3) return;
+        if (ibcell(I, J, K) == 2) {
+            if (ibcell(I1, J1, K1) == 2 && ibcell(I2, J2, K2) == 0) F1 = ONE;
+            else if (ibcell(I1, J1, K1) == 0 && ibcell(I2, J2, K2) == 2) F1 = ZERO;
+        }
+        double F2 = ONE - F1;
+        a3(P, I, J, K) = F1 * a3(P, I1, J1, K1) + F2 * a3(P, I2, J2, K2);
+        a3(T, I, J, K) = F1 * a3(T, I1, J1, K1) + F2 * a3(T, I2, J2, K2);
+        for (int L = LSTAR; L <= LEND; ++L) gf(I, J, K, L) = F1 * gf(I1, J1, K1, L) + F2 * gf(I2, J2, K2, L);
+        CONC(I, J, K);
+        a3(TMU, I, J, K) = F1 * a3(TMU, I1, J1, K1) + F2 * a3(TMU, I2, J2, K2);
+        a3(GAMA, I, J, K) = F1 * a3(GAMA, I1, J1, K1) + F2 * a3(GAMA, I2, J2, K2);
+        a3(THETA, I, J, K) = F1 * a3(THETA, I1, J1, K1) + F2 * a3(THETA, I2, J2, K2);
+        dnst_calc(I, J, K);
+    }
+    void INTP() {
+        for (int I = 2; I <= MP; I += 2) {
+            for (int K = 3; K <= LPM1; K += 2) {
+                double F1 = INTP1(I, 0, K, 3);
+                for (int J = 2; J <= NP; J += 2) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0(F1, I, J, K, I, J, K + 1, I, J, K - 1);
+                }
+            }
+            for (int J = 3; J <= NPM1; J += 2) {
+                double F1 = INTP1(I, J, 0, 2);
+                for (int K = 2; K <= LP; ++K) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0(F1, I, J, K, I, J + 1, K, I, J - 1, K);
+                }
+            }
+        }
+        for (int I = 3; I <= MPM1; I += 2) {
+            double F1 = INTP1(I, 0, 0, 1);
+            for (int K = 2; K <= LP; ++K)
+                for (int J = 2; J <= NP; ++J) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0(F1, I, J, K, I + 1, J, K, I - 1, J, K);
+                }
+        }
+    }
+    void INTPV1(int M, int Nn, int L, int IU, int IXD) {
+        int I, J, K;
+        if (IU == 1) { I = M; J = Nn; K = L; } else if (IU == 2) { J = M; K = Nn; I = L; } else { K = M; I = Nn; J = L; }
+        int b = ibcell(I, J, K);
+        if (b >= 1 && b != 4) return;
+        double F1 = INTP1(I, J, K, IXD), F2 = ONE - F1;
+        if (IXD == 1) {
+            ug(I, J, K, IU) = ug(I + 1, J, K, IU) * F1 + ug(I - 1, J, K, IU) * F2;
+        } else if (IXD == 2) {
+            if (ibcell(I, J + 1, K) == 2 && b == 0) { F1 = 0; F2 = 1; }
+            else if (ibcell(I, J - 1, K) == 2 && b == 0) { F1 = 1; F2 = 0; }
+            ug(I, J, K, IU) = ug(I, J + 1, K, IU) * F1 + ug(I, J - 1, K, IU) * F2;
+        } else {
+            if (ibcell(I, J, K + 1) == 2 && b == 0) { F1 = 0; F2 = 1; }
+            else if (ibcell(I, J, K - 1) == 2 && b == 0) { F1 = 1; F2 = 0; }
+            ug(I, J, K, IU) = ug(I, J, K + 1, IU) * F1 + ug(I, J, K - 1, IU) * F2;
+        }
+        BOUND(ug(I, J, K, IU), IU, 1);
+    }
+    void INTPV() {
+        for (int IU = 1; IU <= 3; ++IU) {
+            int M3, N3, L3;
+            if (IU == 1) { M3 = MP; N3 = NP; L3 = LP; } else if (IU == 2) { M3 = NP; N3 = LP; L3 = MP; } else { M3 = LP; N3 = MP; L3 = NP; }
+            for (int M = 3; M <= M3 - 1; M += 2) {
+                if (N3 > 3) {
+                    for (int L = 2; L <= L3; L += 2)
+                        for (int Nn = 3; Nn <= N3 - 1; Nn += 2) INTPV1(M, Nn, L, IU, IU == 1 ? 2 : (IU == 2 ? 3 : 1));
+                }
+                if (L3 <= 3) continue;
+                for (int L = 3; L <= L3 - 1; L += 2)
+                    for (int Nn = 2; Nn <= N3; ++Nn) INTPV1(M, Nn, L, IU, IU == 1 ? 3 : (IU == 2 ? 1 : 2));
+            }
+            for (int M = 4; M <= M3; M += 2)
+                for (int Nn = 2; Nn <= N3; ++Nn)
+                    for (int L = 2; L <= L3; ++L) INTPV1(M, Nn, L, IU, IU);
+        }
+    }
+
+    // ---- Gflow.f90 -----------------------------------------------------------------
+    void wall_functions() {   // Gflow.f90:16-130
+        for (int I = 2; I <= MP; ++I)
+            for (int J = 2; J <= NP; ++J)
+                for (int K = 2; K <= LP; ++K) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    if (ibcell(I - 1, J, K) == 1) {
+                        double G1 = (X[I] - X[I - 1]) * (X[I] - X[I - 1]), G2 = (X[I + 2] - X[I - 1]) * (X[I + 2] - X[I - 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I - 1, J, K) = a3(THETA, I, J, K) * X01 + a3(THETA, I + 2, J, K) * X02;
+                    }
+                    if (ibcell(I + 1, J, K) == 1) {
+                        double G1 = (X[I] - X[I + 1]) * (X[I] - X[I + 1]), G2 = (X[I - 2] - X[I + 1]) * (X[I - 2] - X[I + 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I + 1, J, K) = a3(THETA, I, J, K) * X01 + a3(THETA, I - 2, J, K) * X02;
+                    }
+                    if (ibcell(I, J - 1, K) == 1) {
+                        double G1 = (R[J] - R[J - 1]) * (R[J] - R[J - 1]), G2 = (R[J + 2] - R[J - 1]) * (R[J + 2] - R[J - 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I, J - 1, K) = a3(THETA, I, J, K) * X01 + a3(THETA, I, J + 2, K) * X02;
+                    }
+                    if (ibcell(I, J + 1, K) == 1) {
+                        double G1 = (R[J] - R[J + 1]) * (R[J] - R[J + 1]), G2 = (R[J - 2] - R[J + 1]) * (R[J - 2] - R[J + 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I, J + 1, K) = a3(THETA, I, J, K) * X01 + a3(THETA, I, J - 2, K) * X02;
+                    }
+                    if (ibcell(I, J, K - 1) == 1) {
+                        double G1 = (Z[K] - Z[K - 1]) * (Z[K] - Z[K - 1]), G2 = (Z[K + 2] - Z[K - 1]) * (Z[K + 2] - Z[K - 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I, J, K - 1) = a3(THETA, I, J, K) * X01 + a3(THETA, I, J, K + 2) * X02;
+                    }
+                    if (ibcell(I, J, K + 1) == 1) {
+                        double G1 = (Z[K] - Z[K + 1]) * (Z[K] - Z[K + 1]), G2 = (Z[K - 2] - Z[K + 1]) * (Z[K - 2] - Z[K + 1]);
+                        double X01 = G2 / (G2 - G1), X02 = G1 / (G1 - G2);
+                        a3(THETA, I, J, K + 1) = a3(THETA, I, J, K) * X01 + a3(THETA, I, J, K - 2) * X02;
+                    }
+                }
+        for (int I = 2; I <= MP; ++I)
+            for (int J = 2; J <= NP; ++J)
+                for (int K = 2; K <= LP; ++K)
+                    if (ibcell(I, J, K) == 1) a3(GAMA, I, J, K) = ZERO;
+        double RT20 = pr.reyg2 * std::sqrt(pr.epsr) * std::pow(pr.cmu, 0.25);
+        for (int I = 2; I <= MP; ++I)
+            for (int J = 2; J <= NP; ++J)
+                for (int K = 2; K <= LP; ++K) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    double C = std::pow(a3(T, I, J, K) / pr.trdg, pr.amu);
+                    double BLVM = RT20 * a3(DNST, I, J, K) * std::sqrt(gf(I, J, K, IK)) / C;
+                    double VGAM = C / pr.reyg2;
+                    auto upd = [&](int i1, int j1, int k1, int i2, int j2, int k2, double dist) {
+                        double BLV = BLVM * dist;
+                        double GAMA0 = VGAM * TGAMF(BLV);
+                        a3(GAMA, i1, j1, k1) = fmax2(GAMA0, a3(GAMA, i1, j1, k1));
+                        a3(TMU, i1, j1, k1) = pr.reyg2 * a3(GAMA, i1, j1, k1);
+                        a3(TMU, i2, j2, k2) = a3(TMU, i1, j1, k1);
+                    };
+                    if (ibcell(I - 1, J, K) == 1) upd(I - 1, J, K, I - 2, J, K, X[I] - X[I - 1]);
+                    if (ibcell(I + 1, J, K) == 1) upd(I + 1, J, K, I + 2, J, K, X[I + 1] - X[I]);
+                    if (ibcell(I, J - 1, K) == 1) upd(I, J - 1, K, I, J - 2, K, R[J] - R[J - 1]);
+                    if (ibcell(I, J + 1, K) == 1) upd(I, J + 1, K, I, J + 2, K, R[J + 1] - R[J]);
+                    if (ibcell(I, J, K - 1) == 1) upd(I, J, K - 1, I, J, K - 2, Z[K] - Z[K - 1]);
+                    if (ibcell(I, J, K + 1) == 1) upd(I, J, K + 1, I, J, K + 2, Z[K + 1] - Z[K]);
+                }
+    }
+    double pref_g0() {   // Gflow.f90:182-242
+        int I = I_REF, J = J_REF, K = K_REF, I1 = I, J1 = J, K1 = K, I2 = I, J2 = J, K2 = K, NXd = 0;
+        if (I < MPM2 && ibcell(I + 2, J, K) == 0) { NXd = 1; I1 = I + 2; I2 = ibcell(I + 4, J, K) == 0 ? I + 4 : I1; }
+        else if (I > 2 && ibcell(I - 2, J, K) == 0) { NXd = 1; I1 = I - 2; I2 = ibcell(I - 4, J, K) == 0 ? I - 4 : I1; }
+        else if (J < NPM2 && ibcell(I, J + 2, K) == 0) { NXd = 2; J1 = J + 2; J2 = (J < NPM2 && ibcell(I, J + 4, K) <= 0) ? J + 4 : J1; }
+        else if (J > 2 && ibcell(I, J - 2, K) <= 0) { NXd = 2; J1 = J - 2; J2 = (J > 4 && ibcell(I, J - 4, K) <= 0) ? J - 4 : J1; }
+        else if (K < LPM2 && ibcell(I, J, K + 2) <= 0) { NXd = 3; K1 = K + 2; K2 = (K < LPM2 && ibcell(I, J, K + 4) <= 0) ? K + 4 : K1; }
+        else if (K > 2 && ibcell(I, J, K - 2) <= 0) { NXd = 3; K1 = K - 2; K2 = (K > 4 && ibcell(I, J, K - 4) <= 0) ? K - 4 : K1; }
+        double F1, F2;
+        EXTR1(F1, F2, I, J, K, I1, J1, K1, I2, J2, K2, NXd);
+        a3(P, I, J, K) = a3(P, I1, J1, K1) * F1 + a3(P, I2, J2, K2) * F2;
+        return a3(P, I1, J1, K1) - P_REF;
+    }
+    void GSLV3G() {   // Gslv3g.f90:6-115
+        int MI1 = 4, MI3 = MPM2, NJ1 = NJY1, NJ3 = NJY2, LK1 = LKZ1, LK3 = LKZ2;
+        // Fixed-temperature wall sink (configuration deviation): the reference
+        // evaluates q_conv inside its full radiation call; here it is evaluated
+        // once per iteration from the state at the start of the scalar loop.
+        if (pr.wall_sink) calc_q_conv_wall();
+        for (int L = LSTAR; L <= LEND; ++L) {
+            if (L == IYF) NELG = 6;
+            else if (L == IYCO2) NELG = 7;
+            else if (L == IH) NELG = 8;
+            else if (L == IK) NELG = 9;
+            else if (L == IEPS) NELG = 10;
+            else if (L == IYN2) NELG = 11;
+            else if (L == IYO2) NELG = 12;
+            else continue;
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) a3(FZ, I, J, K) = gf(I, J, K, L);
+            SOURCE(MI1, MI3, NJ1, NJ3, LK1, LK3);
+            if (L == LSTAR || SGM != pr.sigma[L - 1]) { SGM = pr.sigma[L - 1]; GSLV3G0(MI1, MI3, NJ1, NJ3, LK1, LK3, 0); }
+            else GSLV3G0(MI1, MI3, NJ1, NJ3, LK1, LK3, 1);
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        if (std::fabs(a3(AP, I, J, K)) <= small20) { a3(AP, I, J, K) = ONE; a3(BS, I, J, K) = a3(FZ, I, J, K); continue; }
+                        double VOL = VOL_C(I, J, K);
+                        a3(BS, I, J, K) = a3(BS, I, J, K) * VOL;
+                        a3(AP, I, J, K) = a3(AP, I, J, K) - (a3(SFP, I, J, K) * VOL);
+                        a3(AP, I, J, K) = a3(AP, I, J, K) / pr.rfl[L - 1];
+                        a3(BS, I, J, K) = a3(BS, I, J, K) + RFLC[L - 1] * a3(FZ, I, J, K) * a3(AP, I, J, K);
+                    }
+            if (NELG == 8) h_resid_pre = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            gf_resid_pre[L - 1] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            ADLBL3(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesg[NELG - 1]);
+            gf_resid[L - 1] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        BOUND(a3(FZ, I, J, K), L, 2);
+                        gf(I, J, K, L) = a3(FZ, I, J, K);
+                    }
+        }
+    }
+    void GSLV3G0(int MI1, int MI3, int NJ1, int NJ3, int LK1, int LK3, int IGS) {
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    a3(AP, I, J, K) = ZERO;
+                    for (int IU = 1; IU <= 3; ++IU)
+                        for (int M = -1; M <= 1; M += 2) {
+                            int M1 = (M + 3) / 2;
+                            if (IGS != 1) {
+                                int I1, J1, K1, I2, J2, K2;
+                                VINDX(IU, M, I, J, K, I1, J1, K1, I2, J2, K2);
+                                int IBC0 = ibcell(I2, J2, K2);
+                                if (IBC0 <= 0) as(I, J, K, IU, M1) = FLWD(I1, J1, K1, IU, M1);
+                                else if (IBC0 == 2) as(I, J, K, IU, M1) = FLW(I2, J2, K2, IU, M1);
+                                else as(I, J, K, IU, M1) = ZERO;
+                            }
+                            a3(AP, I, J, K) = a3(AP, I, J, K) + as(I, J, K, IU, M1);
+                        }
+                }
+    }
+    void props(double G0) {   // Gflow.f90:302-382
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    CONC(I, J, K);
+                    enth_to_T_at(I, J, K);
+                    if (a3(T, I, J, K) > pr.t_mx) { a3(T, I, J, K) = pr.t_mx; T_to_enth_at(I, J, K); }
+                    else if (a3(T, I, J, K) < pr.t_mn) { a3(T, I, J, K) = pr.t_mn; T_to_enth_at(I, J, K); }
+                    a3(P, I, J, K) = a3(P, I, J, K) - G0;
+                    BOUND(a3(P, I, J, K), 0, 1);
+                    dnst_calc(I, J, K);
+                    THER(I, J, K);
+                }
+    }
+    void T_ave_calc() {   // Utility.f90:1485-1510
+        double tave = 0, rho_vol_tot = 0;
+        for (int k = 4; k <= LP - 2; k += 2)
+            for (int j = 4; j <= NP - 2; j += 2)
+                for (int i = 4; i <= MP - 2; i += 2) {
+                    if (ibcell(i, j, k) != 0) continue;
+                    double vol = VOL_C(i, j, k);
+                    tave = tave + a3(T, i, j, k) * a3(DNST, i, j, k) * vol;
+                    rho_vol_tot = rho_vol_tot + a3(DNST, i, j, k) * vol;
+                }
+        Tave = tave * pr.t0 / rho_vol_tot;
+    }
+    void rad_qe_only() {   // Rad_emis.f90:411-466 with RAD0 (Rad0.f90:112-157), gray bands
+        std::vector<double> qe2(QE.size(), 0.0);
+        for (auto& t : T) t = t * pr.t0;
+        double SGN = pr.sig * pr.ri * pr.ri;
+        std::vector<double> DEB0(NWL), DEB(NWL);
+        for (int l = 0; l < NWL; ++l) DEB0[l] = pr.hck / pr.ri / WL[l];
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    double T_RAD = a3(T, I, J, K);
+                    if (!(ibcell(I, J, K) <= 0 && T_RAD >= 300.0)) continue;
+                    double VOL = VOL_C(I, J, K);
+                    double SA = ((DX[I] * DR[J]) + (DR[J] * DZ[K]) + (DX[I] * DZ[K])) * TWO;
+                    if (SA <= small16) continue;
+                    double OPL = 6.0 * VOL / SA;
+                    if (OPL <= 1.0e-10) continue;
+                    // DEBX (Rad_fun.f90:122-140)
+                    double EB0 = 0;
+                    for (int L = 1; L <= NWL - 1; ++L) {
+                        double X1 = DEB0[L - 1] / T_RAD;
+                        double EB1 = RIF3(X1);
+                        DEB[L - 1] = EB1 - EB0;
+                        if (DEB[L - 1] <= 1.0e-3) DEB[L - 1] = ZERO; else EB0 = EB1;
+                    }
+                    DEB[NWL - 1] = ONE - EB0;
+                    double t2 = T_RAD * T_RAD;
+                    double area_sgn_t4 = SA * SGN * (t2 * t2);
+                    double sum = ZERO;
+                    for (int l = 0; l < NWL; ++l) sum = sum + DEB[l] * EMF(AKL0[l], OPL);
+                    qe2[cix(I / 2, J / 2, K / 2)] = area_sgn_t4 * sum;
+                }
+        i1st_rad_qe_done = 1;
+        for (auto& t : T) t = t / pr.t0;
+        QE = qe2;
+    }
+
+    void gflow(int stop_after) {
+        wall_functions();
+        if (stop_after == GFO_STEP_WALLFN) return;
+        eq_reset();
+        GSLV3V_momasm();
+        if (stop_after == GFO_STEP_MOMASM) return;
+        GSLV3V_psolve();
+        if (stop_after == GFO_STEP_PSOLVE) return;
+        GSLV3V_momsolve();
+        if (stop_after == GFO_STEP_MOMSOLVE) return;
+        GSLV3V_pcorr();
+        if (stop_after == GFO_STEP_PCORR) return;
+        GSLV3V_velcorr();
+        if (stop_after == GFO_STEP_VELCORR) return;
+        GSLV3V_exits();
+        if (stop_after == GFO_STEP_GSLV3V) return;
+        double G0 = pref_g0();
+        GSLV3G();
+        if (stop_after == GFO_STEP_SCALARS) return;
+        props(G0);
+        T_ave_calc();
+        if (stop_after == GFO_STEP_PROPS) return;
+        EXTR();
+        INTP();
+    }
+    void eq_reset() {}
+
+    void fill_stats(gfm_iter_stats* s, int converged) {
+        if (!s) return;
+        std::memset(s, 0, sizeof *s);
+        s->itr_gas = itr_gas; s->converged = converged;
+        s->res_mass = res_mass; s->res_mass_max = res_mass_max;
+        s->p_resid_pre = p_resid_pre; s->p_resid = p_resid; s->pcorr_resid = pcorr_resid;
+        for (int i = 0; i < 3; ++i) { s->u_resid_pre[i] = u_resid_pre[i]; s->u_resid[i] = u_resid[i]; }
+        for (int i = 0; i < 10; ++i) { s->gf_resid_pre[i] = gf_resid_pre[i]; s->gf_resid[i] = gf_resid[i]; }
+        s->factor = FACTOR; s->gfin = GFIN; s->gfex = GFEX;
+        s->q_react = q_react; s->q_exhaust = q_exhaust; s->q_conv_total = qconv_total;
+        double q_in_tot = q_react + q_h_in, q_out_tot = q_exhaust;
+        s->q_global_bal = std::fabs((q_in_tot - q_out_tot) / q_in_tot);
+        s->tave = Tave; s->tmean_ex = Tmean_ex;
+    }
+};
+
+void copy_in(vec& dst, const double* src, long n) { dst.assign(src, src + n); }
+vec one_based(const double* src, int n) {
+    vec v(n + 3, 0.0);
+    for (int i = 0; i < n; ++i) v[i + 1] = src[i];
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* gfo_create(const gfm_grid* g, const gfm_params* p, const gfm_fields* f) {
+    if (!g || !p || !f) return nullptr;
+    Oracle* o = new Oracle();
+    o->MP = g->mp; o->NP = g->np; o->LP = g->lp;
+    o->MPM1 = o->MP - 1; o->MPM2 = o->MP - 2; o->NPM1 = o->NP - 1; o->NPM2 = o->NP - 2; o->LPM1 = o->LP - 1; o->LPM2 = o->LP - 2;
+    o->MZ = o->MP / 2; o->NZ = o->NP / 2; o->LZ = o->LP / 2;
+    o->N = (long)o->MP * o->NP * o->LP;
+    // NP,LP >= 6 branch of GRID3 (Grid3.f90:142-156, 202-216)
+    o->NJY1 = 4; o->NJY2 = o->NPM2; o->LKZ1 = 4; o->LKZ2 = o->LPM2;
+    o->NJY1V[1] = 4; o->NJY2V[1] = o->NPM2; o->NJY1V[2] = 5; o->NJY2V[2] = o->NP - 3; o->NJY1V[3] = 4; o->NJY2V[3] = o->NPM2;
+    o->LKZ1V[1] = 4; o->LKZ2V[1] = o->LPM2; o->LKZ1V[2] = 4; o->LKZ2V[2] = o->LPM2; o->LKZ1V[3] = 5; o->LKZ2V[3] = o->LP - 3;
+    o->NCELLS = g->ncells; o->I_REF = g->i_ref; o->J_REF = g->j_ref; o->K_REF = g->k_ref; o->P_REF = g->p_ref;
+    o->X = one_based(g->x, o->MP); o->DX = one_based(g->dx, o->MP);
+    o->R = one_based(g->r, o->NP); o->DR = one_based(g->dr, o->NP); o->RS = one_based(g->rs, o->NP);
+    o->Z = one_based(g->z, o->LP); o->DZ = one_based(g->dz, o->LP);
+    o->IBC.assign(g->ibcell, g->ibcell + o->N);
+    for (int i = 0; i < g->b_cnt; ++i) {
+        o->b_typ.push_back(g->b_typ[i]); o->b_i.push_back(g->b_i[i]); o->b_j.push_back(g->b_j[i]); o->b_k.push_back(g->b_k[i]);
+        o->b_orient.push_back(g->b_orient[i]); o->b_direct.push_back(g->b_direct[i]); o->b_T.push_back(g->b_t[i]);
+    }
+    o->q_conv.assign(g->b_cnt, 0.0);
+    o->NR0 = g->nr0;
+    copy_in(o->RTIM, g->rtim, g->nr0); copy_in(o->DELRT, g->delrt, g->nr0); copy_in(o->HRT, g->hrt, g->nr0);
+    copy_in(o->DELR, g->delr, g->nr0); copy_in(o->TIMED, g->timed, g->nr0); copy_in(o->HRD, g->hrd, g->nr0);
+    o->NWL = g->nwl; copy_in(o->WL, g->wl, g->nwl); copy_in(o->AKL0, g->akl0, g->nwl);
+    o->pr = *p;
+    for (int i = 0; i < 21; ++i) { o->RFC[i] = ONE - p->rf[i]; o->RFLC[i] = ONE - p->rfl[i]; }
+    const long N = o->N;
+    copy_in(o->P, f->p, N); copy_in(o->T, f->t, N); copy_in(o->DNST, f->dnst, N); copy_in(o->THETA, f->theta, N);
+    copy_in(o->TMU, f->tmu, N); copy_in(o->GAMA, f->gama, N); copy_in(o->CRATE, f->crate, N); copy_in(o->HRATE, f->hrate, N);
+    copy_in(o->bs_hprev, f->bs_hprev, N);
+    copy_in(o->UG, f->ug, 3 * N); copy_in(o->GF, f->gf, 9 * N);
+    long NCA = (long)o->MZ * o->NZ * o->LZ;
+    copy_in(o->QA, f->qa, NCA); copy_in(o->QE, f->qe, NCA);
+    o->GTE.assign(N, 0.0); o->FZ.assign(N, 0.0); o->BS.assign(N, 0.0); o->SFP.assign(N, 0.0); o->AP.assign(N, 0.0);
+    o->AS.assign(6 * N, 0.0);
+    o->itr_gas = f->itr_gas; o->do_rad_qe_only_cnt = f->do_rad_qe_only_cnt; o->i1st_rad_qe_done = f->i1st_rad_qe_done;
+    o->FACTOR = f->factor; o->FADJ = f->fadj; o->GFIN0 = f->gfin0; o->q_h_in = f->q_h_in;
+    o->GFIN = 0; o->GFEX = 0; o->SGM = ONE; o->NELG = 0;
+    o->res_mass = o->res_mass_max = 0;
+    o->p_resid_pre = o->p_resid = o->pcorr_resid = 0;
+    for (int i = 0; i < 3; ++i) o->u_resid_pre[i] = o->u_resid[i] = 0;
+    for (int i = 0; i < 10; ++i) o->gf_resid_pre[i] = o->gf_resid[i] = 0;
+    o->q_react = o->q_exhaust = o->qconv_total = o->q_rad_vol_tot = o->Tmean_ex = o->Tave = 0;
+    o->h_resid_pre = 0;
+    return o;
+}
+
+void gfo_destroy(void* o) { delete static_cast<Oracle*>(o); }
+
+int gfo_initsv(void* vo) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o) return GFM_E_ARG;
+    o->INTPV();
+    o->EXTR();
+    o->INTP();
+    return GFM_OK;
+}
+
+int gfo_gflow_steps(void* vo, int stop_after) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o) return GFM_E_ARG;
+    o->itr_gas = o->itr_gas + 1;
+    o->gflow(stop_after);
+    return GFM_OK;
+}
+
+int gfo_gflow(void* vo, int n_iter, gfm_iter_stats* out, int* n_done) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || n_iter < 0) return GFM_E_ARG;
+    int done = 0, conv = 0;
+    for (int it = 0; it < n_iter; ++it) {
+        o->itr_gas = o->itr_gas + 1;
+        o->gflow(GFO_STEP_ALL);
+        ++done;
+        if (o->res_mass < o->pr.bgcon) { conv = 1; break; }
+        if (o->pr.rad_emission) {   // Sphase.f90:204-231 (emission only)
+            o->do_rad_qe_only_cnt = o->do_rad_qe_only_cnt + 1;
+            if (o->do_rad_qe_only_cnt >= o->pr.rad_qe_frequency && o->itr_gas > 50) {
+                o->rad_qe_only();
+                o->do_rad_qe_only_cnt = 0;
+            }
+        }
+    }
+    o->fill_stats(out, conv);
+    if (n_done) *n_done = done;
+    return GFM_OK;
+}
+
+int gfo_download(void* vo, gfm_fields* f) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || !f) return GFM_E_ARG;
+    const long N = o->N;
+    auto cp = [](double* dst, const vec& src) { if (dst) std::memcpy(dst, src.data(), src.size() * sizeof(double)); };
+    cp(f->p, o->P); cp(f->t, o->T); cp(f->dnst, o->DNST); cp(f->theta, o->THETA); cp(f->tmu, o->TMU);
+    cp(f->gama, o->GAMA); cp(f->crate, o->CRATE); cp(f->hrate, o->HRATE); cp(f->bs_hprev, o->bs_hprev);
+    cp(f->ug, o->UG); cp(f->gf, o->GF); cp(f->qa, o->QA); cp(f->qe, o->QE);
+    (void)N;
+    f->itr_gas = o->itr_gas; f->do_rad_qe_only_cnt = o->do_rad_qe_only_cnt; f->i1st_rad_qe_done = o->i1st_rad_qe_done;
+    f->factor = o->FACTOR; f->fadj = o->FADJ; f->gfin0 = o->GFIN0; f->q_h_in = o->q_h_in;
+    return GFM_OK;
+}
+
+long gfo_get_array(void* vo, const char* name, double* out, long cap) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || !name || !out) return GFM_E_ARG;
+    const vec* src = nullptr;
+    long off = 0, n = o->N;
+    std::string s(name);
+    if (s == "ap") src = &o->AP; else if (s == "bs") src = &o->BS; else if (s == "sfp") src = &o->SFP;
+    else if (s == "fz") src = &o->FZ; else if (s == "gte") src = &o->GTE; else if (s == "bs_hprev") src = &o->bs_hprev;
+    else if (s.size() == 4 && s[0] == 'a' && s[1] == 's') {
+        int l = s[2] - '0', m = s[3] - '0';
+        if (l < 1 || l > 3 || m < 1 || m > 2) return GFM_E_ARG;
+        src = &o->AS; off = (long)((l - 1) * 2 + (m - 1)) * o->N;
+    } else return GFM_E_ARG;
+    if (cap < n) return GFM_E_ARG;
+    std::memcpy(out, src->data() + off, n * sizeof(double));
+    return n;
+}
+
+static void load_system(Oracle* o, const double* ap, const double* const as[6], const double* bs) {
+    o->AP.assign(ap, ap + o->N);
+    o->BS.assign(bs, bs + o->N);
+    for (int q = 0; q < 6; ++q) std::memcpy(o->AS.data() + (long)q * o->N, as[q], o->N * sizeof(double));
+}
+
+int gfo_adlbl3(void* vo, double* xt, const double* ap, const double* const as[6], const double* bs,
+               int ib, int ie, int jb, int je, int kb, int ke, int nim) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || !xt || !ap || !as || !bs) return GFM_E_ARG;
+    load_system(o, ap, as, bs);
+    vec X(xt, xt + o->N);
+    o->ADLBL3(X, ib, ie, jb, je, kb, ke, nim);
+    std::memcpy(xt, X.data(), o->N * sizeof(double));
+    return GFM_OK;
+}
+
+double gfo_calc_residual(void* vo, const double* xt, const double* ap, const double* const as[6], const double* bs,
+                         int ib, int ie, int jb, int je, int kb, int ke) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    load_system(o, ap, as, bs);
+    vec X(xt, xt + o->N);
+    return o->calc_residual(X, ib, ie, jb, je, kb, ke);
+}
+
+double gfo_da(double d, double f) { return DA(d, f); }
+double gfo_tgamf(double b) { return TGAMF(b); }
+double gfo_emf(double xkl, double xl0) { return EMF(xkl, xl0); }
+double gfo_rif3(double x) { return RIF3(x); }
+double gfo_zy1(const double* x, const double* y, double x1, int n) { return ZY1(x, y, x1, n); }
+double gfo_t_to_enth(const double* y, double t_norm) {
+    double c[9]; std::memcpy(c, y, sizeof c);
+    return T_to_enth(Y9{c, 1}, t_norm);
+}
+double gfo_enth_to_t(const double* y, double h_norm, double t_guess_norm) {
+    double c[9]; std::memcpy(c, y, sizeof c);
+    c[IH - 1] = h_norm;
+    return enth_to_T(Y9{c, 1}, t_guess_norm);
+}
+void gfo_conc(double* y) { conc(Y9{y, 1}); }
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+"""ctypes wrapper of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, as the checker; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import pathlib
+import sys
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent.parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+from gfm_gb300 import abi  # noqa: E402
+from gfm_gb300.solver import Case, Fields  # noqa: E402
+
+from . import build as _build  # noqa: E402
+
+STEP_WALLFN, STEP_MOMASM, STEP_PSOLVE, STEP_MOMSOLVE, STEP_PCORR, STEP_VELCORR, STEP_GSLV3V, STEP_SCALARS, STEP_PROPS, STEP_ALL = range(1, 11)
+
+_lib = None
+
+
+def load(check_bounds: bool = False) -> C.CDLL:
+    global _lib
+    if _lib is not None and not check_bounds:
+        return _lib
+    lib = C.CDLL(str(_build.build(check_bounds=check_bounds)))
+    dp = C.POINTER(C.c_double)
+    lib.gfo_create.restype = C.c_void_p
+    lib.gfo_create.argtypes = [C.POINTER(abi.GfmGrid), C.POINTER(abi.GfmParams), C.POINTER(abi.GfmFields)]
+    lib.gfo_destroy.argtypes = [C.c_void_p]
+    lib.gfo_initsv.argtypes = [C.c_void_p]
+    lib.gfo_gflow.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.GfmIterStats), C.POINTER(C.c_int)]
+    lib.gfo_gflow_steps.argtypes = [C.c_void_p, C.c_int]
+    lib.gfo_download.argtypes = [C.c_void_p, C.POINTER(abi.GfmFields)]
+    lib.gfo_get_array.restype = C.c_long
+    lib.gfo_get_array.argtypes = [C.c_void_p, C.c_char_p, dp, C.c_long]
+    lib.gfo_adlbl3.argtypes = [C.c_void_p, dp, dp, C.POINTER(dp), dp] + [C.c_int] * 7
+    lib.gfo_calc_residual.restype = C.c_double
+    lib.gfo_calc_residual.argtypes = [C.c_void_p, dp, dp, C.POINTER(dp), dp] + [C.c_int] * 6
+    for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1"):
+        getattr(lib, n).restype = C.c_double
+    lib.gfo_da.argtypes = [C.c_double, C.c_double]
+    lib.gfo_tgamf.argtypes = [C.c_double]
+    lib.gfo_emf.argtypes = [C.c_double, C.c_double]
+    lib.gfo_rif3.argtypes = [C.c_double]
+    lib.gfo_zy1.argtypes = [dp, dp, C.c_double, C.c_int]
+    lib.gfo_t_to_enth.argtypes = [dp, C.c_double]
+    lib.gfo_enth_to_t.argtypes = [dp, C.c_double, C.c_double]
+    lib.gfo_conc.argtypes = [dp]
+    if not check_bounds:
+        _lib = lib
+    return lib
+
+
+class Oracle:
+    """FP64 restatement of GFLOW/SPHASE on one case's host state."""
+
+    def __init__(self, case: Case, fields: Fields | None = None, check_bounds: bool = False):
+        self.lib = load(check_bounds)
+        self.case = case
+        fld = fields if fields is not None else case.initial_fields()
+        f = fld.to_c()   # pointers into fld's arrays: fld must outlive the call
+        self.o = self.lib.gfo_create(C.byref(case.grid), C.byref(case.params), C.byref(f))
+        del fld
+        if not self.o:
+            raise RuntimeError("gfo_create failed")
+
+    def initsv(self) -> None:
+        self.lib.gfo_initsv(self.o)
+
+    def gflow(self, n: int = 1) -> tuple[dict, int]:
+        st = abi.GfmIterStats()
+        nd = C.c_int(0)
+        self.lib.gfo_gflow(self.o, n, C.byref(st), C.byref(nd))
+        return st.as_dict(), nd.value
+
+    def gflow_steps(self, stop_after: int) -> None:
+        self.lib.gfo_gflow_steps(self.o, stop_after)
+
+    def download(self) -> Fields:
+        out = Fields.empty(self.case.mp, self.case.np, self.case.lp)
+        f = out.to_c()
+        self.lib.gfo_download(self.o, C.byref(f))
+        out.update_scalars(f)
+        return out
+
+    def array(self, name: str) -> np.ndarray:
+        n = self.case.mp * self.case.np * self.case.lp
+        out = np.zeros(n)
+        got = self.lib.gfo_get_array(self.o, name.encode(), abi.dptr(out), n)
+        if got != n:
+            raise KeyError(name)
+        return out.reshape(self.case.lp, self.case.np, self.case.mp)
+
+    def close(self) -> None:
+        if self.o:
+            self.lib.gfo_destroy(self.o)
+            self.o = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
