@@ -1,0 +1,352 @@
+"""Benchmark: steady SIMPLER outer iterations of the GFM combustion-space
+solver on the 192x96x64 synthetic furnace (1,179,648 cells).
+
+A step is one outer iteration (GFLOW: momentum, pressure, pressure correction,
+seven scalar equations, properties, boundary values) over the whole furnace.
+`value` is cells x iterations per second with the state resident in HBM (CUDA
+events on the solver's stream around the timed iterations); `e2e` is the same
+metric through the public C ABI with host buffers: upload of the state from
+pinned host memory, one gfm_gpu_gflow call per step returning its statistics,
+and the download of the fields at the end, all inside the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--prec mixed|fp64] [--adi redblack|march]
+
+Multi-GPU runs are independent replicas (the iteration does not shard): every
+rank solves its own furnace, `value` sums the replicas over the slowest rank's
+time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import subprocess
+import sys
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-iters/s, steady SIMPLER outer iteration, 192x96x64 furnace"
+UNIT = "cell-iter/s"
+WORKLOAD = "furnace_192x96x64: GFLOW steady SIMPLER outer iteration, 1,179,648 cells"
+BYTES_PER_CELL_VISIT = 10   # 8 coefficients + read x + write x per plane visit (algorithmic)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, local):
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_bench_{gpu}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit()) if rows else None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def load_traffic(prec: str):
+    """Per-launch DRAM traffic of the line-solver kernel from a committed ncu summary."""
+    p = ROOT / "profiles" / f"ncu_adi_{prec}_192x96x64.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+        except Exception:
+            return None
+    return None
+
+
+def cpu_baseline_oracle(steps: int = 1):
+    """The CPU oracle (FP64 restatement of the reference, 1 core) on the same case."""
+    from gfm_gb300 import Case, configs
+    from oracle.pyoracle import Oracle
+    case = Case(configs.large_furnace())
+    o = Oracle(case)
+    o.initsv()
+    t0 = time.perf_counter()
+    o.gflow(steps)
+    dt = time.perf_counter() - t0
+    return case.ncells * steps / dt, dt
+
+
+def _replica_worker(args):
+    steps, warmup = args
+    from gfm_gb300 import Case, configs
+    from oracle.pyoracle import Oracle
+    case = Case(configs.large_furnace())
+    o = Oracle(case)
+    o.initsv()
+    if warmup:
+        o.gflow(warmup)
+    t0 = time.perf_counter()
+    o.gflow(steps)
+    return time.perf_counter() - t0, case.ncells
+
+
+def run_reference(args):
+    """Reference arm: the CPU oracle (FP64, the reference's serial algorithm)
+    on the machine's host cores, one independent furnace per core."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    import multiprocessing as mp
+    ncpu = os.cpu_count() or 1
+    mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
+    cores = max(1, min(ncpu, int(mem // (6 * 2 ** 30))))
+    steps = max(1, min(args.steps, 2))
+    warm = 0
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_replica_worker, [(steps, warm)] * cores)
+    wall = time.perf_counter() - t0
+    worst = max(r[0] for r in res)
+    ncells = res[0][1]
+    value = cores * ncells * steps / worst
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
+        "warmup": warm, "ms_per_step": 1e3 * worst / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": ncells, "replicas": cores},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} independent replicas x {steps} outer iteration(s) of the FP64 oracle "
+                                   f"(C++ restatement of the Fortran GFLOW), wall {wall:.1f}s"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def pinned_fields(case):
+    """Fresh-start fields in pinned host memory when torch+CUDA are present."""
+    f = case.initial_fields()
+    try:
+        import torch
+        if torch.cuda.is_available():
+            for k, v in list(f.arrays.items()):
+                # the numpy view keeps the pinned tensor alive
+                a = torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy()
+                a[...] = v
+                f.arrays[k] = a
+            f._pinned = True
+    except Exception:
+        f._pinned = False
+    return f
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    dist = init_dist(world, local)
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    from gfm_gb300 import Case, GpuSolver, abi, configs
+    prec = abi.GFM_PREC_MIXED if args.prec == "mixed" else abi.GFM_PREC_FP64
+    adi = abi.GFM_ADI_REDBLACK if args.adi == "redblack" else abi.GFM_ADI_MARCH
+    if world > 1:
+        import torch
+        torch.cuda.set_device(local)
+    case = Case(configs.large_furnace())
+    solver = GpuSolver(case, adi_mode=adi, precision=prec)
+    solver.start()
+    solver.gflow(max(args.warmup, 0))
+    prof = solver.iteration_profile()
+    solver.reset_kernel_times()
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        st, nd = solver.gflow(args.steps)
+        t1 = time.perf_counter()
+    barrier(dist)
+    kt = solver.kernel_times()
+    dev_s = kt["gflow_ms"] / 1e3
+    dev_s = max_over_ranks(dist, dev_s)
+    ncells = case.ncells
+    value = world * ncells * nd / dev_s
+    w = 4 if args.prec == "mixed" else 8
+    # dominant kernel: the line solver (ADLBL3 plane updates)
+    adi_launches = prof["adi_kernels_per_iter"] * nd
+    adi_ms = kt["adi_ms"]
+    achieved = (prof["adi_cell_visits_per_iter"] * nd * BYTES_PER_CELL_VISIT * w / 1e9) / (adi_ms / 1e3) if adi_ms > 0 else None
+    peak, peak_kind = measured_peaks()
+    traffic = load_traffic(args.prec)
+
+    # e2e through the public API with host buffers (pinned when available)
+    fields = pinned_fields(case)
+    solver2 = GpuSolver(case, adi_mode=adi, precision=prec)
+    solver2.upload(fields)
+    solver2.initsv()
+    solver2.gflow(max(args.warmup, 0))
+    host_state = solver2.download()
+    out = pinned_fields(case)
+    import ctypes as C
+    barrier(dist)
+    e0 = time.perf_counter()
+    solver2.upload(host_state)
+    for _ in range(args.steps):
+        solver2.gflow(1)
+    f = out.to_c()
+    solver2._check(solver2.lib.gfm_gpu_download(solver2.h, C.byref(f)))
+    e1 = time.perf_counter()
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, e1 - e0)
+    n = case.mp * case.np * case.lp
+    nfield = 9 + 3 + 8
+    state_bytes = 8 * (nfield * n + 2 * (case.mp // 2) * (case.np // 2) * (case.lp // 2))
+    stats_bytes = C.sizeof(abi.GfmIterStats) + 8 * 200
+    h2d = state_bytes / args.steps + 16
+    d2h = state_bytes / args.steps + stats_bytes
+    e2e_value = world * ncells * args.steps / e2e_s
+    solver2.close()
+
+    plain = None
+    if args.prec == "mixed" and not args.no_plain:
+        s64 = GpuSolver(case, adi_mode=adi, precision=abi.GFM_PREC_FP64)
+        s64.start()
+        s64.gflow(max(args.warmup, 0))
+        s64.reset_kernel_times()
+        _, n64 = s64.gflow(args.steps)
+        t64 = s64.kernel_times()["gflow_ms"] / 1e3
+        plain = {"value": ncells * n64 / t64, "ms_per_step": 1e3 * t64 / n64, "dtype": "fp64"}
+        s64.close()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v, dt = cpu_baseline_oracle(1)
+            cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                   "sample": f"1 outer iteration of the FP64 oracle (C++ restatement of GFLOW) on the same "
+                             f"192x96x64 furnace after INITSV, {dt:.1f}s on one host core"}
+        except Exception as e:   # the baseline is reported, never required
+            cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / nd, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32" if args.prec == "mixed" else "fp64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": ncells, "precision": args.prec, "adi_order": args.adi,
+                       "l2": "inputs larger than L2 (device state ~%.1f GB)" % (state_bytes * (0.5 if w == 4 else 1) * 3 / 1e9),
+                       "parallelism": f"replicas x{world}", "res_mass_last": st["res_mass"]},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "pinned": bool(getattr(fields, "_pinned", False)),
+                    "path": "gfm_gpu_upload + K x gfm_gpu_gflow(1) + gfm_gpu_download"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_kind": peak_kind, "kernel": "ADLBL3 line solver (plane updates)",
+                         "algorithmic_bytes": f"{BYTES_PER_CELL_VISIT} x {w} B per cell per plane visit",
+                         "adi_launches": adi_launches, "adi_ms": adi_ms},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(prof["kernels_per_iter"] * nd),
+            "plain_fp64": plain,
+            "wall_s": t1 - t0,
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--prec", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--adi", choices=["redblack", "march"], default="redblack")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

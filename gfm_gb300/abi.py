@@ -161,6 +161,7 @@ SIGNATURES = [
     ("gfm_gpu_rad_emission", C.c_int, [C.c_void_p]),
     ("gfm_gpu_kernel_times", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     ("gfm_gpu_reset_kernel_times", C.c_int, [C.c_void_p]),
+    ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     ("gfm_gpu_last_error", C.c_char_p, [C.c_void_p]),
     ("gfm_gpu_destroy", None, [C.c_void_p]),
 ]

@@ -50,7 +50,8 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
     for s in CUDA_SOURCES:
         src, obj = CSRC / s, BUILD / (s + ".o")
         if force or _needs(obj, src):
-            jobs.append([cc, "-std=c++17", *ARCH, "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
+            extra = os.environ.get("GFM_NVCC_EXTRA", "").split()
+            jobs.append([cc, "-std=c++17", *ARCH, "-O3", "-lineinfo", *extra, "-Xcompiler", "-fPIC",
                          "-c", str(src), "-o", str(obj)])
     for s in CXX_SOURCES:
         src, obj = CSRC / s, BUILD / (s + ".o")

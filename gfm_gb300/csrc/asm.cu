@@ -623,7 +623,7 @@ __global__ void k_qconv(Ctx<R> c) {
 // radiation term, the wall sink gathered per cell in patch order and the
 // source relaxation with bs_hprev (Source.f90:269-522).
 template <typename R, int L>
-__global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as, int itr_gas) {
+__global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
     __shared__ double sh[32];
     const GeoT<R>& g = c.g;
     const R zero = R(0);
@@ -636,6 +636,8 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as, int itr_gas) {
     const R* fz = c.GF[L - 1];
     long long n = rg.count();
     double qreact = 0.0;
+    const int itr_gas = (int)c.scal[S_ITR_GAS];
+    const bool rad_active = c.scal[S_RAD_ACTIVE] > 0.0;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         int I, J, K;
         rg.at(t, I, J, K);
@@ -704,7 +706,7 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as, int itr_gas) {
         }
         if (NELG == 8 && !blocked) {
             // radiation rate (Source.f90:437-447)
-            if (c.rad_active) {
+            if (rad_active) {
                 R vol = vol_c(g, I, J, K);
                 R q_rad = c.QA[o] - c.QE[o];
                 bs = bs + q_rad / (vol * R(c.p.qr0));
@@ -933,13 +935,13 @@ template <typename R> void launch_scalar_assemble(const Ctx<R>& c, int L, bool n
     int nb = grid_for(r.count());
     int na = new_as ? 1 : 0;
     switch (L) {
-        case 1: k_scalar_assemble<R, 1><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 2: k_scalar_assemble<R, 2><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 3: k_scalar_assemble<R, 3><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 4: k_scalar_assemble<R, 4><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 5: k_scalar_assemble<R, 5><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 6: k_scalar_assemble<R, 6><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
-        case 7: k_scalar_assemble<R, 7><<<nb, kBlock, 0, s>>>(c, r, na, c.itr_gas); break;
+        case 1: k_scalar_assemble<R, 1><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 2: k_scalar_assemble<R, 2><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 3: k_scalar_assemble<R, 3><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 4: k_scalar_assemble<R, 4><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 5: k_scalar_assemble<R, 5><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 6: k_scalar_assemble<R, 6><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 7: k_scalar_assemble<R, 7><<<nb, kBlock, 0, s>>>(c, r, na); break;
     }
     // FZ(L) <- GF(L) for the solve: class 0 block
     k_copy_centres<R><<<grid_for(c.g.CB), kBlock, 0, s>>>(c.GF[L - 1], c.FZs[L - 1], c.g.CB);

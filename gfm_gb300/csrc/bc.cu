@@ -176,8 +176,9 @@ __global__ void k_extrv(Ctx<R> c, int mex, int first, int count) {
 
 // GFEX/Tmean_ex finish of EXTRV(0), GFIN of FLX1D and the exit FACTOR
 // (Extr.f90:553-565, Flx1d.f90:75-77, Gslv3v.f90:213-231).  One thread.
-__global__ void k_factor(double* scal, double gmfr, double t0, double f_mx, double f_mn, int itr_gas) {
+__global__ void k_factor(double* scal, double gmfr, double t0, double f_mx, double f_mn) {
     if (threadIdx.x != 0) return;
+    const int itr_gas = (int)scal[S_ITR_GAS];
     double gfex = scal[S_GFEX] * gmfr;
     scal[S_GFEX] = gfex;
     if (gfex < 1.0e-16) scal[S_TMEAN_EX] = scal[S_TAREA_MEAN] * t0 / scal[S_AREA_EX];
@@ -450,7 +451,7 @@ template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s) 
     k_t_roundtrip<R><<<gridn(8 * c.g.CB), kBlk, 0, s>>>(c.T, 8 * c.g.CB, c.p.t0);
 }
 template <typename R> void launch_factor(const Ctx<R>& c, cudaStream_t s) {
-    k_factor<<<1, 32, 0, s>>>(c.scal, c.p.gmfr, c.p.t0, c.p.f_mx, c.p.f_mn, c.itr_gas);
+    k_factor<<<1, 32, 0, s>>>(c.scal, c.p.gmfr, c.p.t0, c.p.f_mx, c.p.f_mn);
 }
 void launch_finish(const double* partials, double* scal, const FinishSpec& f, double ncells, cudaStream_t s) {
     k_finish<<<1, 256, 0, s>>>(partials, scal, f, ncells);

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <initializer_list>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -63,6 +64,17 @@ struct gfm_handle {
     double adi_ms = 0, asm_ms = 0, other_ms = 0;
     long long launches = 0;
     std::string err;
+    // one GFLOW captured as a CUDA graph and replayed every iteration
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    bool use_graph = true;
+    double* h_flags = nullptr;          // pinned: itr_gas, rad_active for the next replay
+    cudaEvent_t ev[16]{};
+    cudaEvent_t ev_g0 = nullptr, ev_g1 = nullptr;   // around a whole gfm_gpu_gflow call
+    int n_ev = 0;                       // events recorded per iteration (pairs around line solves)
+    long long kernels_per_iter = 0;     // kernel nodes of the captured iteration
+    long long adi_kernels_per_iter = 0;
+    double adi_cells_visits = 0;        // cells x plane visits per iteration (all line solves)
 };
 
 namespace {
@@ -433,13 +445,33 @@ void finish(gfm_handle* h, Ctx<R>& c, std::initializer_list<std::array<int, 3>> 
     launch_finish(c.partials, c.scal, f, (double)h->ncells, h->stream);
 }
 
+// one line-solver batch bracketed by CUDA events (device time of the dominant kernel)
+template <typename R>
+void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>* scr, int nsys, cudaStream_t st) {
+    // external records: inside a captured graph these become real event nodes
+    if (h->n_ev + 2 <= 16) cudaEventRecordWithFlags(h->ev[h->n_ev], st, cudaEventRecordExternal);
+    launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st);
+    if (h->n_ev + 2 <= 16) { cudaEventRecordWithFlags(h->ev[h->n_ev + 1], st, cudaEventRecordExternal); h->n_ev += 2; }
+    int nim = 0;
+    for (int e = 0; e < nsys; ++e) {
+        nim = sys[e].nim > nim ? sys[e].nim : nim;
+        double cells = (double)((sys[e].ie - sys[e].ib) / 2 + 1) * ((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);
+        h->adi_cells_visits += cells * 2.0 * sys[e].nim;   // each sweep visits every plane twice
+    }
+    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 4LL * nim;
+}
+
 template <typename R>
 int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     cudaStream_t st = h->stream;
     const GeoT<R>& g = c.g;
     const gfm_params& P = h->params;
-    c.itr_gas = h->itr_gas;
-    c.rad_active = h->rad_active;
+    h->n_ev = 0;
+    h->adi_kernels_per_iter = 0;
+    h->adi_cells_visits = 0;
+    // iteration flags read by the kernels (device scalars, so one captured graph serves every iteration)
+    cudaMemcpyAsync(c.scal + S_ITR_GAS, h->h_flags, sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c.scal + S_RAD_ACTIVE, h->h_flags + 1, sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(c.partials, 0, sizeof(double) * kRedSlots * kRedBlocks, st);
     // wall functions (Gflow.f90:16-130)
     launch_wallfn(c, h->d_wall, h->n_wall, st);
@@ -450,8 +482,7 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     launch_p_assemble(c, st);
     Sys<R> sp = sys_of<R>(c.P, c.APc, c.ASc, c.BSp, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[3]);
     launch_residual(c, sp, SL_P_PRE, st);
-    cudaEventRecord(h->ev_adi0, st);
-    launch_adlbl3_scr(g, &sp, scr, 1, h->adi_mode, st);
+    adi_call(h, g, &sp, scr, 1, st);
     launch_residual(c, sp, SL_P_POST, st);
     launch_bound_p(c, st);
     // momentum solves u, v, w (independent systems, one batch)
@@ -463,7 +494,7 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
                                g.LKZ2V[iu], P.ntimesg[iu - 1]);
         launch_residual(c, sm[iu - 1], SL_U_PRE + iu - 1, st);
     }
-    launch_adlbl3_scr(g, sm, scr, 3, h->adi_mode, st);
+    adi_call(h, g, sm, scr, 3, st);
     for (int iu = 0; iu < 3; ++iu) launch_residual(c, sm[iu], SL_U_POST + iu, st);
     launch_mom_finish(c, st);
     // pressure correction
@@ -471,7 +502,7 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     R* asc[6];
     for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
     Sys<R> spc = sys_of<R>(c.FZ, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[4]);
-    launch_adlbl3_scr(g, &spc, scr, 1, h->adi_mode, st);
+    adi_call(h, g, &spc, scr, 1, st);
     launch_residual(c, spc, SL_PC_POST, st);
     launch_velcorr(c, st);
     // exit balance (EXTRV, FLX1D, FACTOR), INTPV
@@ -498,7 +529,7 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
                           P.ntimesg[nelg - 1]);
         launch_residual(c, ss[q], SL_GF_PRE + L - 1, st);
     }
-    launch_adlbl3_scr(g, ss, scr, 6, h->adi_mode, st);
+    adi_call(h, g, ss, scr, 6, st);
     for (int q = 0; q < 6; ++q) {
         int L = order[q];
         launch_residual(c, ss[q], SL_GF_POST + L - 1, st);
@@ -511,11 +542,10 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
         Sys<R> se = sys_of<R>(c.FZs[L - 1], c.APs[L - 1], c.ASs[set], c.BSs[L - 1], 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2,
                               P.ntimesg[9]);
         launch_residual(c, se, SL_GF_PRE + L - 1, st);
-        launch_adlbl3_scr(g, &se, scr, 1, h->adi_mode, st);
+        adi_call(h, g, &se, scr, 1, st);
         launch_residual(c, se, SL_GF_POST + L - 1, st);
         launch_scalar_finish(c, L, st);
     }
-    cudaEventRecord(h->ev_adi1, st);
     // properties, mean temperature, boundary values, interpolation
     launch_props(c, st);
     launch_tave(c, st);
@@ -748,6 +778,14 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
         c.nist = dn;
     }
     if (cudaMallocHost(&h->h_scal, sizeof(double) * (S_NUM + 128)) != cudaSuccess) return GFM_E_NOMEM;
+    if (cudaMallocHost(&h->h_flags, sizeof(double) * 4) != cudaSuccess) return GFM_E_NOMEM;
+    for (int q = 0; q < 16; ++q) cudaEventCreate(&h->ev[q]);
+    cudaEventCreate(&h->ev_g0);
+    cudaEventCreate(&h->ev_g1);
+    {
+        const char* ng = std::getenv("GFM_NO_GRAPH");
+        h->use_graph = !(ng && ng[0] == '1');
+    }
     std::memset(h->h_scal, 0, sizeof(double) * (S_NUM + 128));
     // constants
     Prm& p = c.p;
@@ -817,19 +855,61 @@ extern "C" int gfm_gpu_initsv(gfm_handle* h) {
     return GFM_OK;
 }
 
+namespace {
+int capture_iteration(gfm_handle* h) {
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+    if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) { h->err = std::string("capture: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
+    int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
+    e = cudaStreamEndCapture(h->stream, &h->graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) { h->err = std::string("capture end: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
+    size_t n = 0;
+    cudaGraphGetNodes(h->graph, nullptr, &n);
+    std::vector<cudaGraphNode_t> nodes(n);
+    cudaGraphGetNodes(h->graph, nodes.data(), &n);
+    long long k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        cudaGraphNodeGetType(nd, &t);
+        if (t == cudaGraphNodeTypeKernel) ++k;
+    }
+    h->kernels_per_iter = k;
+    e = cudaGraphInstantiate(&h->graph_exec, h->graph, 0);
+    if (e != cudaSuccess) { h->err = std::string("instantiate: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
+    return GFM_OK;
+}
+}  // namespace
+
 extern "C" int gfm_gpu_gflow(gfm_handle* h, int n_iter, gfm_iter_stats* out, int* n_done) {
     if (!h || n_iter < 0) return GFM_E_ARG;
     int done = 0, conv = 0;
+    if (h->use_graph && !h->graph_exec) {
+        int rc = capture_iteration(h);
+        if (rc) return rc;
+    }
+    cudaEventRecord(h->ev_g0, h->stream);
     for (int it = 0; it < n_iter; ++it) {
         h->itr_gas += 1;
-        int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
-        if (rc) return rc;
+        h->h_flags[0] = (double)h->itr_gas;
+        h->h_flags[1] = (double)h->rad_active;
+        if (h->use_graph) {
+            cudaError_t e = cudaGraphLaunch(h->graph_exec, h->stream);
+            if (e != cudaSuccess) { h->err = std::string("graph launch: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
+            h->launches += h->kernels_per_iter;
+        } else {
+            int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
+            if (rc) return rc;
+        }
         double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
         cudaError_t e = cudaMemcpyAsync(h->h_scal, scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, h->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, h->ev_adi0, h->ev_adi1) == cudaSuccess) h->adi_ms += ms;
+        for (int q = 0; q + 1 < h->n_ev; q += 2) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, h->ev[q], h->ev[q + 1]) == cudaSuccess) h->adi_ms += ms;
+        }
         ++done;
         if (!std::isfinite(h->h_scal[S_RES_MASS])) { h->err = "res_mass is not finite"; if (n_done) *n_done = done; fill_stats(h, out, 0); return GFM_E_NAN; }
         if (h->h_scal[S_RES_MASS] < h->params.bgcon) { conv = 1; break; }
@@ -842,6 +922,11 @@ extern "C" int gfm_gpu_gflow(gfm_handle* h, int n_iter, gfm_iter_stats* out, int
                 h->cnt_qe = 0;
             }
         }
+    }
+    cudaEventRecord(h->ev_g1, h->stream);
+    if (cudaEventSynchronize(h->ev_g1) == cudaSuccess) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->ev_g0, h->ev_g1) == cudaSuccess) h->asm_ms += ms;
     }
     fill_stats(h, out, conv);
     if (n_done) *n_done = done;
@@ -914,6 +999,14 @@ extern "C" int gfm_gpu_reset_kernel_times(gfm_handle* h) {
     h->launches = 0;
     return GFM_OK;
 }
+extern "C" int gfm_gpu_iteration_profile(gfm_handle* h, long long* kernels_per_iter, long long* adi_kernels_per_iter,
+                                         double* adi_cell_visits_per_iter) {
+    if (!h) return GFM_E_ARG;
+    if (kernels_per_iter) *kernels_per_iter = h->kernels_per_iter;
+    if (adi_kernels_per_iter) *adi_kernels_per_iter = h->adi_kernels_per_iter;
+    if (adi_cell_visits_per_iter) *adi_cell_visits_per_iter = h->adi_cells_visits;
+    return GFM_OK;
+}
 extern "C" const char* gfm_gpu_last_error(gfm_handle* h) { return h ? h->err.c_str() : g_create_err.c_str(); }
 
 extern "C" void gfm_gpu_destroy(gfm_handle* h);
@@ -922,6 +1015,12 @@ extern "C" void gfm_gpu_destroy(gfm_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     for (void* p : h->allocs) cudaFree(p);
     if (h->h_scal) cudaFreeHost(h->h_scal);
+    if (h->h_flags) cudaFreeHost(h->h_flags);
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    for (int q = 0; q < 16; ++q) if (h->ev[q]) cudaEventDestroy(h->ev[q]);
+    if (h->ev_g0) cudaEventDestroy(h->ev_g0);
+    if (h->ev_g1) cudaEventDestroy(h->ev_g1);
     if (h->ev_adi0) cudaEventDestroy(h->ev_adi0);
     if (h->ev_adi1) cudaEventDestroy(h->ev_adi1);
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -33,7 +33,7 @@ enum Scal {
     S_RES_MASS = 0, S_RES_MASS_MAX, S_GFEX, S_GFIN0, S_GFIN, S_FACTOR, S_FADJ, S_G0, S_TMEAN_EX,
     S_Q_REACT, S_Q_EXHAUST, S_QCONV, S_TAVE, S_P_RESID_PRE, S_P_RESID, S_PCORR_RESID,
     S_U_RESID_PRE, S_U_RESID = S_U_RESID_PRE + 3, S_GF_RESID_PRE = S_U_RESID + 3, S_GF_RESID = S_GF_RESID_PRE + 10,
-    S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_NUM
+    S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_RAD_ACTIVE, S_NUM
 };
 
 template <typename R>

@@ -189,7 +189,13 @@ class GpuSolver:
         a, b, c = C.c_double(), C.c_double(), C.c_double()
         n = C.c_longlong()
         self._check(self.lib.gfm_gpu_kernel_times(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(n)))
-        return {"adi_ms": a.value, "assemble_ms": b.value, "other_ms": c.value, "launches": n.value}
+        return {"adi_ms": a.value, "gflow_ms": b.value, "other_ms": c.value, "launches": n.value}
+
+    def iteration_profile(self) -> dict:
+        k, a = C.c_longlong(), C.c_longlong()
+        v = C.c_double()
+        self._check(self.lib.gfm_gpu_iteration_profile(self.h, C.byref(k), C.byref(a), C.byref(v)))
+        return {"kernels_per_iter": k.value, "adi_kernels_per_iter": a.value, "adi_cell_visits_per_iter": v.value}
 
     def reset_kernel_times(self) -> None:
         self._check(self.lib.gfm_gpu_reset_kernel_times(self.h))

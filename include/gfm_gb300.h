@@ -207,10 +207,18 @@ int  gfm_gpu_adlbl3(gfm_handle *h, double *xt, const double *ap,
 /* Emission-only radiation QE on the device from the current T, P
  * (rad_qe_only, Rad_emis.f90:411-466 with RAD0 Rad0.f90:112-157). */
 int  gfm_gpu_rad_emission(gfm_handle *h);
-/* Device time of the dominant kernels accumulated since the last reset. */
-int  gfm_gpu_kernel_times(gfm_handle *h, double *adi_ms, double *assemble_ms,
+/* Device times (CUDA events on the handle's stream) accumulated since the
+ * last reset: adi_ms = line-solver batches, gflow_ms = whole GFLOW calls
+ * (first to last iteration of each gfm_gpu_gflow), other_ms reserved;
+ * launches = kernels launched by gfm_gpu_gflow. */
+int  gfm_gpu_kernel_times(gfm_handle *h, double *adi_ms, double *gflow_ms,
                           double *other_ms, long long *launches);
 int  gfm_gpu_reset_kernel_times(gfm_handle *h);
+/* Shape of one captured iteration: kernel launches per GFLOW, line-solver
+ * kernel launches per GFLOW, and cells x plane-visits of all line solves. */
+int  gfm_gpu_iteration_profile(gfm_handle *h, long long *kernels_per_iter,
+                               long long *adi_kernels_per_iter,
+                               double *adi_cell_visits_per_iter);
 /* Last error text of this handle (never NULL). */
 const char *gfm_gpu_last_error(gfm_handle *h);
 void gfm_gpu_destroy(gfm_handle *h);

@@ -1,0 +1,42 @@
+"""Line solver through gfm_gpu_adlbl3 on manufactured systems
+(the reference's solver self-test recipe, Solvers.f90:1670-1823)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gfm_gb300 import Case, GpuSolver, abi, configs
+from oracle import pyoracle
+from oracle.pyoracle import Oracle
+from tests.test_oracle_adi import manufactured
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("cls", [(0, 0, 0), (1, 0, 0), (0, 1, 0)])
+def test_march_matches_oracle_adlbl3(cls):
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_MARCH)
+    xg = g.adlbl3(x0, ap, as6, bs, *rng, 2)
+    o = Oracle(case)
+    lib = pyoracle.load()
+    xo = x0.copy()
+    ptrs = (abi._dp * 6)(*[abi.dptr(a) for a in as6])
+    lib.gfo_adlbl3(o.o, abi.dptr(xo), abi.dptr(ap), ptrs, abi.dptr(bs), *rng, 2)
+    err = np.abs(xg - xo)[open_].max() / np.abs(xo[open_]).max()
+    assert err < 1e-13, err
+    g.close()
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-10), (abi.GFM_PREC_MIXED, 1e-4)])
+def test_redblack_converges_to_manufactured_solution(prec, tol):
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
+    ib = case.ibcell()
+    x0[ib >= 1] = sol[ib >= 1]
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+    x = g.adlbl3(x0, ap, as6, bs, *rng, 100)
+    err = np.abs(x - sol)[open_].max() / np.abs(sol[open_]).max()
+    assert err < tol, err
+    g.close()
