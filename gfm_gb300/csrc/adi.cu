@@ -158,6 +158,176 @@ __global__ void k_adlbl3_rb(GeoT<R> g, AdiBatch<R> b, int colour, int max_planes
 }
 
 // ---------------------------------------------------------------------------
+// Red-black form.  The tridiagonal matrix of every y- and z-line is constant
+// during one ADLBL3 call, so its Thomas pivots are factored once: PT (as in
+// ADLZY/ADLYZ) and IA = 1/ALP, with IA = 0 marking the rows the reference
+// copies unchanged (|ALP| <= 1e-20 or a blocked cell).  Within one plane visit
+// the x-neighbour part of the right-hand side, BS + AS12*XT(I+2) +
+// AS11*XT(I-2), is constant (neighbour planes have the other colour) and is
+// summed first, as the reference does.  Threads map to (plane, line) with the
+// plane index fastest, so each step of the sequential line recurrence reads
+// consecutive same-colour planes: coalesced across the warp.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct RbBatch {
+    Sys<R> sys[8];
+    AdiScratch<R> scr[8];
+    int nsys;
+};
+
+__device__ __forceinline__ int rb_nplanes(int ib, int ie) { return (ie - ib) / 2 + 1; }
+
+// factor every y-line and z-line of every plane (both colours)
+template <typename R>
+__global__ void k_rb_factor(GeoT<R> g, RbBatch<R> b) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const long long ny = (long long)npl * nK, nz = (long long)npl * nJ;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ny + nz; t += (long long)gridDim.x * blockDim.x) {
+        if (t < ny) {
+            const int I = s.ib + 2 * (int)(t % npl), K = s.kb + 2 * (int)(t / npl);
+            R pt_prev = R(0);
+            for (int J = s.jb; J <= s.je; J += 2) {
+                const long long o = pidx(g, I, J, K);
+                R alp = s.ap[o] - pt_prev * s.as[2][o];
+                R pt, ia;
+                if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) { pt = R(0); ia = R(0); }
+                else { pt = s.as[3][o] / alp; ia = R(1) / alp; }
+                w.pty[o] = pt;
+                w.iay[o] = ia;
+                pt_prev = pt;
+            }
+        } else {
+            const long long u = t - ny;
+            const int I = s.ib + 2 * (int)(u % npl), J = s.jb + 2 * (int)(u / npl);
+            R pt_prev = R(0);
+            for (int K = s.kb; K <= s.ke; K += 2) {
+                const long long o = pidx(g, I, J, K);
+                R alp = s.ap[o] - pt_prev * s.as[4][o];
+                R pt, ia;
+                if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) { pt = R(0); ia = R(0); }
+                else { pt = s.as[5][o] / alp; ia = R(1) / alp; }
+                w.ptz[o] = pt;
+                w.iaz[o] = ia;
+                pt_prev = pt;
+            }
+        }
+    }
+}
+
+// One line of one pass, software-pipelined: the inputs of D consecutive
+// steps are loaded before the dependent recurrence runs over them, so a thread
+// keeps ~D x 8 independent loads in flight.  Consecutive elements of a y-line
+// are PX apart, of a z-line PX*HY apart; x-neighbours I+-2 are +-1.  Offsets
+// are 32-bit (a parity-split field holds < 2^31 elements, checked at create).
+template <typename R> struct Pipe { static constexpr int D = 8; };
+template <> struct Pipe<double> { static constexpr int D = 4; };
+
+template <typename R, bool FIRST, bool ZLINE>
+__device__ __forceinline__ void rb_line(const R* __restrict__ xt, const R* __restrict__ bs, const R* __restrict__ a_xp,
+                                        const R* __restrict__ a_xm, const R* __restrict__ a_op, const R* __restrict__ a_om,
+                                        const R* __restrict__ a_sub, const R* __restrict__ ia, const R* __restrict__ pt,
+                                        R* __restrict__ bsx, R* __restrict__ out, int o0, int step, int ostep, int n) {
+    constexpr int D = Pipe<R>::D;
+    R qt_prev = xt[o0 - step];
+    int c = 0, o = o0;
+    for (; c + D <= n; c += D, o += D * step) {
+        R vb[D], vo1[D], vo2[D], vx1[D], vx2[D], vs[D], vi[D], vc[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int q = o + d * step;
+            if (FIRST) vb[d] = bs[q] + a_xp[q] * xt[q + 1] + a_xm[q] * xt[q - 1];
+            else vb[d] = bsx[q];
+            vo1[d] = a_op[q]; vo2[d] = a_om[q];
+            vx1[d] = xt[q + ostep]; vx2[d] = xt[q - ostep];
+            vs[d] = a_sub[q]; vi[d] = ia[q]; vc[d] = xt[q];
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int q = o + d * step;
+            if (FIRST && !ZLINE) bsx[q] = vb[d];
+            R qt = vi[d] == R(0) ? vc[d] : ((vb[d] + vo1[d] * vx1[d] + vo2[d] * vx2[d]) + vs[d] * qt_prev) * vi[d];
+            out[q] = qt;
+            qt_prev = qt;
+        }
+    }
+    for (; c < n; ++c, o += step) {
+        R b = FIRST ? bs[o] + a_xp[o] * xt[o + 1] + a_xm[o] * xt[o - 1] : bsx[o];
+        if (FIRST && !ZLINE) bsx[o] = b;
+        const R iv = ia[o];
+        R qt = iv == R(0) ? xt[o] : ((b + a_op[o] * xt[o + ostep] + a_om[o] * xt[o - ostep]) + a_sub[o] * qt_prev) * iv;
+        out[o] = qt;
+        qt_prev = qt;
+    }
+    // back-substitution from the far boundary
+    R nxt = xt[o0 + n * step];
+    c = n - 1;
+    o = o0 + c * step;
+    for (; c + 1 >= D; c -= D, o -= D * step) {
+        R vp[D], vq[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) { vp[d] = pt[o - d * step]; vq[d] = out[o - d * step]; }
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            R v = nxt * vp[d] + vq[d];
+            out[o - d * step] = v;
+            nxt = v;
+        }
+    }
+    for (; c >= 0; --c, o -= step) {
+        R v = nxt * pt[o] + out[o];
+        out[o] = v;
+        nxt = v;
+    }
+}
+
+// one pass (both directions) over the planes of one colour; the first pass of a
+// visit (L=1) computes BSX (y-lines store it), the second reads it
+template <typename R, bool FIRST>
+__global__ void k_rb_pass(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    if (sweep >= s.nim) return;
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = rb_nplanes(s.ib, s.ie);
+    const int npc = (npl - colour + 1) / 2;   // planes of this colour
+    const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const long long ny = (long long)npc * nK, nz = (long long)npc * nJ;
+    const int sy = g.PX, sz = g.PX * g.HY;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ny + nz; t += (long long)gridDim.x * blockDim.x) {
+        if (t < ny) {
+            const int I = s.ib + 2 * (2 * (int)(t % npc) + colour), K = s.kb + 2 * (int)(t / npc);
+            rb_line<R, FIRST, false>(s.xt, s.bs, s.as[1], s.as[0], s.as[5], s.as[4], s.as[2], w.iay, w.pty, w.bsx, w.xt2,
+                                     (int)pidx(g, I, s.jb, K), sy, sz, nJ);
+        } else {
+            const long long u = t - ny;
+            const int I = s.ib + 2 * (2 * (int)(u % npc) + colour), J = s.jb + 2 * (int)(u / npc);
+            rb_line<R, FIRST, true>(s.xt, s.bs, s.as[1], s.as[0], s.as[3], s.as[2], s.as[4], w.iaz, w.ptz, w.bsx, w.xt3,
+                                    (int)pidx(g, I, J, s.kb), sz, sy, nK);
+        }
+    }
+}
+
+// XT = (XT2 + XT3)/2 on the planes of one colour
+template <typename R>
+__global__ void k_rb_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    if (sweep >= s.nim) return;
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = rb_nplanes(s.ib, s.ie);
+    const int npc = (npl - colour + 1) / 2;
+    const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const long long n = (long long)npc * nJ * nK;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int I = s.ib + 2 * (2 * (int)(t % npc) + colour);
+        const long long r = t / npc;
+        const int J = s.jb + 2 * (int)(r % nJ), K = s.kb + 2 * (int)(r / nJ);
+        const long long o = pidx(g, I, J, K);
+        s.xt[o] = (w.xt2[o] + w.xt3[o]) / R(2);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // calc_residual: per-cell |sum a_nb x_nb + b - a_p x| / max(terms)
 // ---------------------------------------------------------------------------
 template <typename R>
@@ -219,15 +389,32 @@ void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>*
     if (mode == GFM_ADI_MARCH) {
         k_adlbl3_march<R><<<nsys, threads, 0, st>>>(g, b);
     } else {
-        int per_colour = (max_np + 1) / 2;
+        RbBatch<R> rb;
+        rb.nsys = nsys;
+        long long max_lines = 0, max_cells = 0;
         int nim = 0;
-        for (int e = 0; e < nsys; ++e) nim = sys[e].nim > nim ? sys[e].nim : nim;
-        // equations with fewer sweeps drop out of later launches
+        for (int e = 0; e < nsys; ++e) {
+            rb.sys[e] = sys[e];
+            rb.scr[e] = scr[e];
+            const Sys<R>& q = sys[e];
+            long long np_ = (q.ie - q.ib) / 2 + 1, nK = (q.ke - q.kb) / 2 + 1, nJ = (q.je - q.jb) / 2 + 1;
+            max_lines = np_ * (nK + nJ) > max_lines ? np_ * (nK + nJ) : max_lines;
+            max_cells = np_ * nK * nJ > max_cells ? np_ * nK * nJ : max_cells;
+            nim = q.nim > nim ? q.nim : nim;
+        }
+        const int T = 128;
+        dim3 gf((unsigned)((max_lines + T - 1) / T), nsys);
+        k_rb_factor<R><<<gf, T, 0, st>>>(g, rb);
+        dim3 gp((unsigned)((max_lines / 2 + T) / T), nsys);
+        dim3 ga((unsigned)((max_cells / 2 + 255) / 256 < 2048 ? (max_cells / 2 + 255) / 256 : 2048), nsys);
         for (int ns = 0; ns < nim; ++ns)
-            for (int half = 0; half < 2; ++half) {
-                k_adlbl3_rb<R><<<nsys * per_colour, threads, 0, st>>>(g, b, 0, per_colour, ns);
-                k_adlbl3_rb<R><<<nsys * per_colour, threads, 0, st>>>(g, b, 1, per_colour, ns);
-            }
+            for (int half = 0; half < 2; ++half)
+                for (int colour = 0; colour < 2; ++colour) {
+                    k_rb_pass<R, true><<<gp, T, 0, st>>>(g, rb, colour, ns);
+                    k_rb_avg<R><<<ga, 256, 0, st>>>(g, rb, colour, ns);
+                    k_rb_pass<R, false><<<gp, T, 0, st>>>(g, rb, colour, ns);
+                    k_rb_avg<R><<<ga, 256, 0, st>>>(g, rb, colour, ns);
+                }
     }
 }
 

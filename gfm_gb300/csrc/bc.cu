@@ -344,6 +344,17 @@ __global__ void k_t_roundtrip(R* T, long long n, double t0) {
         T[t] = R(((double)T[t] * t0) / t0);
 }
 
+// count non-finite values of an uploaded reference-layout array
+__global__ void k_count_nonfinite(const double* __restrict__ a, long long n, unsigned int* cnt) {
+    unsigned int local = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        local += isfinite(a[t]) ? 0u : 1u;
+    if (local) atomicAdd(cnt, local);
+}
+void launch_count_nonfinite(const double* a, long long n, unsigned int* cnt, cudaStream_t s) {
+    k_count_nonfinite<<<gridn(n), kBlk, 0, s>>>(a, n, cnt);
+}
+
 // ---------------------------------------------------------------------------
 // layout conversion
 // ---------------------------------------------------------------------------

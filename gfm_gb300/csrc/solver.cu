@@ -56,6 +56,7 @@ struct gfm_handle {
     int* d_wall = nullptr;
     int n_wall = 0;
     double* d_stage = nullptr;      // doubled-layout staging buffer (N doubles)
+    unsigned int* d_bad = nullptr;  // non-finite counter of uploaded arrays
     double* h_scal = nullptr;       // pinned copy of the device scalars
     int pref_i1 = 0, pref_j1 = 0, pref_k1 = 0, pref_i2 = 0, pref_j2 = 0, pref_k2 = 0;
     double pref_f1 = 1, pref_f2 = 0;
@@ -401,7 +402,8 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
         for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASs[s][q], CB))) return rc;
     for (int e = 0; e < 8; ++e)
         if ((rc = dalloc(h, &scr[e].xt2, NS)) || (rc = dalloc(h, &scr[e].xt3, NS)) || (rc = dalloc(h, &scr[e].pty, NS)) ||
-            (rc = dalloc(h, &scr[e].ptz, NS)))
+            (rc = dalloc(h, &scr[e].ptz, NS)) || (rc = dalloc(h, &scr[e].iay, NS)) || (rc = dalloc(h, &scr[e].iaz, NS)) ||
+            (rc = dalloc(h, &scr[e].bsx, NS)))
             return rc;
     if ((rc = dalloc(h, &c.qconv, gr->b_cnt > 0 ? gr->b_cnt : 1))) return rc;
     return GFM_OK;
@@ -458,7 +460,7 @@ void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>*
         double cells = (double)((sys[e].ie - sys[e].ib) / 2 + 1) * ((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);
         h->adi_cells_visits += cells * 2.0 * sys[e].nim;   // each sweep visits every plane twice
     }
-    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 4LL * nim;
+    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 1 + 16LL * nim;
 }
 
 template <typename R>
@@ -579,26 +581,37 @@ int upload_fields(gfm_handle* h, Ctx<R>& c, const gfm_fields* f) {
     const long long N = h->N;
     const GeoT<R>& g = c.g;
     cudaStream_t st = h->stream;
-    auto put = [&](const double* src, R* dst) -> int {
+    const char* bad_name = nullptr;
+    auto put_named = [&](const double* src, R* dst, const char* name) -> int {
         if (!src) return GFM_OK;
+        CK(cudaMemsetAsync(h->d_bad, 0, sizeof(unsigned int), st));
         CK(cudaMemcpyAsync(h->d_stage, src, N * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_count_nonfinite(h->d_stage, N, h->d_bad, st);
         launch_to_split(g, h->d_stage, dst, st);
+        unsigned int nb = 0;
+        CK(cudaMemcpyAsync(&nb, h->d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (nb && !bad_name) bad_name = name;
         return GFM_OK;
     };
+    auto put = [&](const double* src, R* dst) -> int { return put_named(src, dst, "field"); };
     int rc;
-    if ((rc = put(f->p, c.P)) || (rc = put(f->t, c.T)) || (rc = put(f->dnst, c.DNST)) || (rc = put(f->theta, c.THETA)) ||
+    if ((rc = put_named(f->p, c.P, "p")) || (rc = put_named(f->t, c.T, "t")) || (rc = put_named(f->dnst, c.DNST, "dnst")))
+        return rc;
+    if ((rc = put(f->theta, c.THETA)) ||
         (rc = put(f->tmu, c.TMU)) || (rc = put(f->gama, c.GAMA)) || (rc = put(f->crate, c.CRATE)) ||
         (rc = put(f->hrate, c.HRATE)) || (rc = put(f->bs_hprev, c.BSH)))
         return rc;
-    for (int l = 0; l < 3; ++l) if ((rc = put(f->ug ? f->ug + l * N : nullptr, c.UG[l]))) return rc;
+    for (int l = 0; l < 3; ++l) if ((rc = put_named(f->ug ? f->ug + l * N : nullptr, c.UG[l], "ug"))) return rc;
     for (int l = 0; l < 9; ++l) {
         if (l == 7) continue;
-        if ((rc = put(f->gf ? f->gf + l * N : nullptr, c.GF[l]))) return rc;
+        if ((rc = put_named(f->gf ? f->gf + l * N : nullptr, c.GF[l], "gf"))) return rc;
     }
     long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
     if (f->qa) { CK(cudaMemcpyAsync(h->d_stage, f->qa, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QA, st); }
     if (f->qe) { CK(cudaMemcpyAsync(h->d_stage, f->qe, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QE, st); }
     CK(cudaStreamSynchronize(st));
+    if (bad_name) { h->err = std::string("non-finite values in uploaded array ") + bad_name; return GFM_E_NAN; }
     return GFM_OK;
 }
 
@@ -727,6 +740,7 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     g.CB = (long long)g.PX * g.HY * g.HZ;
     h->CB = g.CB;
     h->NS = 8 * g.CB;
+    if (h->NS >= (1LL << 31)) { h->err = "grid too large for 32-bit field offsets"; return GFM_E_UNSUPPORTED; }
     {
         std::vector<int8_t> ibs((size_t)h->NS, 1);
         for (int K = 1; K <= hg.LP; ++K)
@@ -769,7 +783,7 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     c.patch = pp; c.cell_patch_start = i2; c.cell_patch_list = i3; c.n_patch = (int)patches.size();
     c.intp_mode = im;
     if ((rc = dalloc(h, &c.scal, S_NUM + 128)) || (rc = dalloc(h, &c.partials, (long long)kRedSlots * kRedBlocks)) ||
-        (rc = dalloc(h, &h->d_stage, h->N)))
+        (rc = dalloc(h, &h->d_stage, h->N)) || (rc = dalloc(h, &h->d_bad, 1)))
         return rc;
     {
         Nist* dn = nullptr;

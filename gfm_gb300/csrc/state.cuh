@@ -90,6 +90,7 @@ struct Sys {
 template <typename R>
 struct AdiScratch {
     R *xt2, *xt3, *pty, *ptz;
+    R *iay, *iaz, *bsx;   // red-black form: inverse pivots of the factored lines, x-neighbour RHS
 };
 
 // ---- launchers (defined in the kernel translation units) --------------------
@@ -126,6 +127,8 @@ struct FinishSpec {
 void launch_finish(const double* partials, double* scal, const FinishSpec& f, double ncells, cudaStream_t s);
 template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int K1, int I2, int J2, int K2, double F1,
                                            double F2, cudaStream_t s);
+
+void launch_count_nonfinite(const double* a, long long n, unsigned int* cnt, cudaStream_t s);
 
 // layout conversion doubled <-> parity split (host-layout arrays on device)
 template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);

@@ -89,16 +89,17 @@ def test_mixed_precision_tiny():
     assert sg["res_mass"] == pytest.approx(so["res_mass"], rel=1e-3)
 
 
-def test_nan_in_state_is_reported_not_propagated():
+def test_nan_in_uploaded_state_is_rejected():
+    # a NaN temperature would otherwise be absorbed silently: the density
+    # bound max(rho, 1e-20) maps NaN to 1e-20, as the reference's MAX does
     case = Case(configs.tiny_furnace())
     g = GpuSolver(case)
     f = case.initial_fields()
     f.arrays["t"][3, 5, 7] = np.nan   # an open cell
-    g.upload(f)
-    g.initsv()
     with pytest.raises(GfmError) as ei:
-        g.gflow(3)
+        g.upload(f)
     assert ei.value.rc == abi.GFM_E_NAN
+    assert "t" in str(ei.value)
     g.close()
 
 
