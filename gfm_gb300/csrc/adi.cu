@@ -328,29 +328,34 @@ __global__ void k_rb_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
 }
 
 // ---------------------------------------------------------------------------
-// calc_residual: per-cell |sum a_nb x_nb + b - a_p x| / max(terms)
+// calc_residual: per-cell |sum a_nb x_nb + b - a_p x| / max(terms), evaluated
+// in the solver's arithmetic type (the FP64 path keeps the reference's FP64
+// operation order); the per-thread sums and the block partials are FP64.
+// Neighbours I+-2, J+-2, K+-2 of a class are +-1, +-PX, +-PX*HY apart.
 // ---------------------------------------------------------------------------
 template <typename R>
 __global__ void k_residual(GeoT<R> g, Sys<R> s, double* partials, int slot) {
     __shared__ double sh[32];
     const int ni = (s.ie - s.ib) / 2 + 1, nj = (s.je - s.jb) / 2 + 1, nk = (s.ke - s.kb) / 2 + 1;
-    const long long n = (long long)ni * nj * nk;
+    const int n = ni * nj * nk;
+    const int sy = g.PX, sz = g.PX * g.HY;
+    const R* __restrict__ xt = s.xt;
     double acc = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        int i = s.ib + 2 * (int)(t % ni);
-        long long r = t / ni;
-        int j = s.jb + 2 * (int)(r % nj), k = s.kb + 2 * (int)(r / nj);
-        long long o = pidx(g, i, j, k);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = s.ib + 2 * (t % ni);
+        const int r = t / ni;
+        const int j = s.jb + 2 * (r % nj), k = s.kb + 2 * (r / nj);
+        const int o = (int)pidx(g, i, j, k);
         if (g.ib[o] > 0) continue;
-        double t1 = (double)s.as[0][o] * (double)A(s.xt, i - 2, j, k), t2 = (double)s.as[1][o] * (double)A(s.xt, i + 2, j, k);
-        double t3 = (double)s.as[2][o] * (double)A(s.xt, i, j - 2, k), t4 = (double)s.as[3][o] * (double)A(s.xt, i, j + 2, k);
-        double t5 = (double)s.as[4][o] * (double)A(s.xt, i, j, k - 2), t6 = (double)s.as[5][o] * (double)A(s.xt, i, j, k + 2);
-        double t7 = (double)s.ap[o] * (double)s.xt[o], t8 = (double)s.bs[o];
-        double em = fabs(t1);
+        R t1 = s.as[0][o] * xt[o - 1], t2 = s.as[1][o] * xt[o + 1];
+        R t3 = s.as[2][o] * xt[o - sy], t4 = s.as[3][o] * xt[o + sy];
+        R t5 = s.as[4][o] * xt[o - sz], t6 = s.as[5][o] * xt[o + sz];
+        R t7 = s.ap[o] * xt[o], t8 = s.bs[o];
+        R em = fabs(t1);
         em = fabs(t2) > em ? fabs(t2) : em; em = fabs(t3) > em ? fabs(t3) : em; em = fabs(t4) > em ? fabs(t4) : em;
         em = fabs(t5) > em ? fabs(t5) : em; em = fabs(t6) > em ? fabs(t6) : em; em = fabs(t7) > em ? fabs(t7) : em;
         em = fabs(t8) > em ? fabs(t8) : em;
-        acc += fabs(t1 + t2 + t3 + t4 + t5 + t6 + t8 - t7) / em;   // 0/0 -> NaN as in the reference
+        acc += (double)(fabs(t1 + t2 + t3 + t4 + t5 + t6 + t8 - t7) / em);   // 0/0 -> NaN as in the reference
     }
     double v = block_sum(acc, sh);
     if (threadIdx.x == 0) partials[slot * kRedBlocks + blockIdx.x] = v;

@@ -688,7 +688,7 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
             sfp = -(R(c.p.taur) * c.THETA[o] * c.DNST[o] * c.GF[kEps][o] / (c.GF[kK][o] + R(kSmall20)));
         } else if (NELG == 10) {
             const R cbl0 = R(2.5 * sqrt(c.p.epsr) / c.p.taur * pow(c.p.cmu, 0.75));
-            R cbl = cbl0 * R(pow((double)c.GF[kK][o], 1.5));
+            R cbl = cbl0 * pow(c.GF[kK][o], R(1.5));
             const R BIGV = R(1.0e20);
             bool pen = false;
             if (g.MP > 8 && IBC(g, I + 1, J, K) == 1) { bs = bs + BIGV * cbl / (g.X[I + 1] - g.X[I]); pen = true; }
@@ -805,34 +805,36 @@ __device__ void ther(Ctx<R>& c, long long o) {
     R k = c.GF[kK][o];
     R g0 = R(c.p.cmu) * R(c.p.reyg) * R(c.p.epsr) / R(2.0 * c.p.taur) * (k * k) / eps * c.DNST[o];
     c.TMU[o] = g0;
-    c.GAMA[o] = R(2) / R(c.p.reyg) * (g0 + R(pow((double)c.T[o] / c.p.trdg, c.p.amu)));
+    c.GAMA[o] = R(2) / R(c.p.reyg) * (g0 + pow(c.T[o] / R(c.p.trdg), R(c.p.amu)));
 }
 
 template <typename R>
 __global__ void k_props(Ctx<R> c, Range rg) {
-    const Nist* nist = c.nist;
+    const NistT<R>& nist = *c.nist;
     const GeoT<R>& g = c.g;
     long long n = rg.count();
-    const double G0 = c.scal[S_G0];
+    const R G0 = R(c.scal[S_G0]);
+    const R t0 = R(c.p.t0), h0 = R(c.p.h_0), t_mx = R(c.p.t_mx), t_mn = R(c.p.t_mn);
+    const R p_mx = R(c.p.p_mx), p_mn = R(c.p.p_mn), wt0 = R(c.p.wt0);
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
         if (g.ib[o] >= 1) continue;
-        double y[9];
-        for (int l = 0; l < 9; ++l) y[l] = l == 7 ? 0.0 : (double)c.GF[l][o];
+        R y[9];
+        for (int l = 0; l < 9; ++l) y[l] = l == 7 ? R(0) : c.GF[l][o];
         conc(y, 1);
-        double T = enth_to_t(*nist, y, 1, y[kH], (double)c.T[o], c.p.t0, c.p.h_0);
-        if (T > c.p.t_mx) { T = c.p.t_mx; y[kH] = t_to_enth(*nist, y, 1, T, c.p.t0, c.p.h_0); }
-        else if (T < c.p.t_mn) { T = c.p.t_mn; y[kH] = t_to_enth(*nist, y, 1, T, c.p.t0, c.p.h_0); }
-        double pp = (double)c.P[o] - G0;
-        pp = pp < c.p.p_mx ? pp : c.p.p_mx;
-        pp = pp > c.p.p_mn ? pp : c.p.p_mn;
-        double rho = dnst_calc<double>(y, 1, pp, T, c.p.wt0);
-        for (int l = 0; l < 9; ++l) if (l != 7) c.GF[l][o] = R(y[l]);
-        c.T[o] = R(T);
-        c.P[o] = R(pp);
-        c.DNST[o] = R(rho);
+        R T = enth_to_t<R>(nist, y, 1, y[kH], c.T[o], t0, h0);
+        if (T > t_mx) { T = t_mx; y[kH] = t_to_enth<R>(nist, y, 1, T, t0, h0); }
+        else if (T < t_mn) { T = t_mn; y[kH] = t_to_enth<R>(nist, y, 1, T, t0, h0); }
+        R pp = c.P[o] - G0;
+        pp = pp < p_mx ? pp : p_mx;
+        pp = pp > p_mn ? pp : p_mn;
+        R rho = dnst_calc<R>(y, 1, pp, T, wt0);
+        for (int l = 0; l < 9; ++l) if (l != 7) c.GF[l][o] = y[l];
+        c.T[o] = T;
+        c.P[o] = pp;
+        c.DNST[o] = rho;
         ther(c, o);
     }
 }

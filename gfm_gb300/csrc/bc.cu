@@ -70,9 +70,9 @@ __global__ void k_extr_io(Ctx<R> c) {
             else c.GF[L - 1][o] = rmax2(g0, R(0));
         }
         {
-            double y[9];
-            for (int l = 0; l < 9; ++l) y[l] = l == 7 ? 0.0 : (double)c.GF[l][o];
-            c.T[o] = R(enth_to_t(*c.nist, y, 1, y[kH], (double)c.T[o], c.p.t0, c.p.h_0));
+            R y[9];
+            for (int l = 0; l < 9; ++l) y[l] = l == 7 ? R(0) : c.GF[l][o];
+            c.T[o] = enth_to_t<R>(*c.nist, y, 1, y[kH], c.T[o], R(c.p.t0), R(c.p.h_0));
         }
         dnst_at(c, o);
         R area = area_cc(g, e.I, e.J, e.K, e.IX);

@@ -46,11 +46,13 @@ constexpr int kYF = 0, kYO2 = 1, kH = 2, kK = 3, kEps = 4, kYCO2 = 5, kYN2 = 6, 
 // NIST Shomate coefficient sets (Setup.f90:103-141): species order CH4, O2,
 // CO2, N2, H2O; [species][0=lo,1=hi].  These are physical data that have to be
 // identical to the reference's for parity.
-struct Nist {
-    double a[5][2], b[5][2], c[5][2], d[5][2], e[5][2], f[5][2], h[5][2];
-    double cut[5];
+template <typename R>
+struct NistT {
+    R a[5][2], b[5][2], c[5][2], d[5][2], e[5][2], f[5][2], h[5][2];
+    R cut[5];
     int gidx[5];
 };
+using Nist = NistT<double>;
 // Host copy of the table; device code receives a pointer to a __constant__
 // copy (see kernels), so every function below takes the table explicitly.
 inline const Nist& nist_host() {
@@ -64,6 +66,20 @@ inline const Nist& nist_host() {
         {{-74.8731, -74.8731}, {0.0, 0.0}, {-393.5224, -393.5224}, {0.0, 0.0}, {-241.8264, -241.8264}},
         {1300.0, 6000.0, 1200.0, 6000.0, 1700.0},       // cutT, Var_mod.f90:417-422
         {kYF, kYO2, kYCO2, kYN2, kYH2O}};               // gf_chem_index, Setup.f90:85-89
+    return t;
+}
+// The table rounded to the arithmetic type of a kernel.
+template <typename R>
+inline NistT<R> nist_cast(const Nist& n) {
+    NistT<R> t;
+    for (int s = 0; s < 5; ++s) {
+        for (int k = 0; k < 2; ++k) {
+            t.a[s][k] = R(n.a[s][k]); t.b[s][k] = R(n.b[s][k]); t.c[s][k] = R(n.c[s][k]); t.d[s][k] = R(n.d[s][k]);
+            t.e[s][k] = R(n.e[s][k]); t.f[s][k] = R(n.f[s][k]); t.h[s][k] = R(n.h[s][k]);
+        }
+        t.cut[s] = R(n.cut[s]);
+        t.gidx[s] = n.gidx[s];
+    }
     return t;
 }
 
@@ -104,13 +120,15 @@ GFM_HD R dnst_calc(R* y, long s, R p, R t, R wt0) {
 // Shomate mixture coefficients with the reference's f_mix/h_mix accumulation
 // (f_mix = d_mix + Y*F and h_mix = e_mix + Y*H inside the species loop,
 // Prop.f90:398-418).
-struct ShomateMix { double a, b, c, d, e, f, h; int lohi[5]; };
+template <typename R>
+struct ShomateMix { R a, b, c, d, e, f, h; int lohi[5]; };
 
-GFM_HD void shomate_mix(const Nist& N, const double* y, long s, double real_T, ShomateMix& m) {
-    m.a = m.b = m.c = m.d = m.e = m.f = m.h = 0.0;
+template <typename R>
+GFM_HD void shomate_mix(const NistT<R>& N, const R* y, long s, R real_T, ShomateMix<R>& m) {
+    m.a = m.b = m.c = m.d = m.e = m.f = m.h = R(0);
     for (int n = 0; n < 5; ++n) {
         int set = (real_T < N.cut[n]) ? 0 : 1;
-        double yy = y[N.gidx[n] * s];
+        R yy = y[N.gidx[n] * s];
         m.a = m.a + yy * N.a[n][set];
         m.b = m.b + yy * N.b[n][set];
         m.c = m.c + yy * N.c[n][set];
@@ -122,41 +140,49 @@ GFM_HD void shomate_mix(const Nist& N, const double* y, long s, double real_T, S
     }
 }
 
+// Newton stopping test on |dT| (T in kK).  FP64 uses the reference's 1e-11
+// (Var_mod.f90:398); FP32 stops at 1e-6 kK, where the next quadratic step is
+// already below the FP32 resolution of T.
+template <typename R> struct EnthTol { static constexpr double v = kTolEnth; };
+template <> struct EnthTol<float> { static constexpr double v = 1.0e-6; };
+
 // T_to_enth (Prop.f90:525-565): returns normalised enthalpy.
-GFM_HD double t_to_enth(const Nist& N, const double* y, long s, double T, double t0, double h0) {
-    double w_mix = wmix(y, s);
-    double real_T = T * t0;
-    ShomateMix m;
+template <typename R>
+GFM_HD R t_to_enth(const NistT<R>& N, const R* y, long s, R T, R t0, R h0) {
+    R w_mix = wmix(y, s);
+    R real_T = T * t0;
+    ShomateMix<R> m;
     shomate_mix(N, y, s, real_T, m);
-    double tn = real_T / 1000.0;
-    double ef = tn * (m.a + tn * ((m.b / 2.0) + tn * ((m.c / 3.0) + tn * (m.d / 4.0)))) - (m.e / tn) + m.f - m.h;
-    return ef * 1.0e6 / (w_mix * h0);
+    R tn = real_T / R(1000);
+    R ef = tn * (m.a + tn * ((m.b / R(2)) + tn * ((m.c / R(3)) + tn * (m.d / R(4))))) - (m.e / tn) + m.f - m.h;
+    return ef * R(1.0e6) / (w_mix * h0);
 }
 
 // enth_to_T (Prop.f90:369-505): Newton on the Shomate integral with the
 // reference's in-loop coefficient-set switches for CH4, CO2 and H2O.
 // Returns the normalised temperature.
-GFM_HD double enth_to_t(const Nist& N, const double* y, long s, double h_norm, double T, double t0, double h0) {
-    double w_mix = wmix(y, s);
-    double h_s = h_norm * h0;
-    double h_molar = h_s * w_mix / 1.0e6;
-    double real_T = T * t0;
-    ShomateMix m;
+template <typename R>
+GFM_HD R enth_to_t(const NistT<R>& N, const R* y, long s, R h_norm, R T, R t0, R h0) {
+    R w_mix = wmix(y, s);
+    R h_s = h_norm * h0;
+    R h_molar = h_s * w_mix / R(1.0e6);
+    R real_T = T * t0;
+    ShomateMix<R> m;
     shomate_mix(N, y, s, real_T, m);
-    double T_old = real_T / 1000.0;
-    double T_new = T_old;   // the reference keeps the module value of an earlier call here
+    R T_old = real_T / R(1000);
+    R T_new = T_old;   // the reference keeps the module value of an earlier call here
     for (int it = 0; it < kNmaxEnth; ++it) {
-        double gp = m.a + T_old * (m.b + T_old * (m.c + T_old * m.d)) + m.e / (T_old * T_old);
-        if (gp == 0.0) break;
-        double g0 = T_old * (m.a + T_old * ((m.b / 2.0) + T_old * ((m.c / 3.0) + T_old * (m.d / 4.0)))) -
-                    (m.e / T_old) + m.f - m.h;
-        double dT = (g0 - h_molar) / gp;
+        R gp = m.a + T_old * (m.b + T_old * (m.c + T_old * m.d)) + m.e / (T_old * T_old);
+        if (gp == R(0)) break;
+        R g0 = T_old * (m.a + T_old * ((m.b / R(2)) + T_old * ((m.c / R(3)) + T_old * (m.d / R(4))))) -
+               (m.e / T_old) + m.f - m.h;
+        R dT = (g0 - h_molar) / gp;
         T_new = T_old - dT;
-        if (fabs(dT) < kTolEnth) break;
+        if (fabs(dT) < R(EnthTol<R>::v)) break;
         T_old = T_new;
         for (int nn = 0; nn < 5; nn += 2) {      // CH4, CO2, H2O (O2, N2 have one set)
-            double yy = y[N.gidx[nn] * s];
-            if (T_new * 1000.0 < N.cut[nn] && m.lohi[nn] != 0) {
+            R yy = y[N.gidx[nn] * s];
+            if (T_new * R(1000) < N.cut[nn] && m.lohi[nn] != 0) {
                 m.a = m.a - yy * N.a[nn][1]; m.b = m.b - yy * N.b[nn][1]; m.c = m.c - yy * N.c[nn][1];
                 m.d = m.d - yy * N.d[nn][1]; m.e = m.e - yy * N.e[nn][1];
                 m.f = m.d - yy * N.f[nn][1]; m.h = m.e - yy * N.h[nn][1];
@@ -165,7 +191,7 @@ GFM_HD double enth_to_t(const Nist& N, const double* y, long s, double h_norm, d
                 m.d = m.d + yy * N.d[nn][0]; m.e = m.e + yy * N.e[nn][0];
                 m.f = m.d + yy * N.f[nn][0]; m.h = m.e + yy * N.h[nn][0];
             }
-            if (T_new * 1000.0 >= N.cut[nn] && m.lohi[nn] != 1) {
+            if (T_new * R(1000) >= N.cut[nn] && m.lohi[nn] != 1) {
                 m.a = m.a - yy * N.a[nn][0]; m.b = m.b - yy * N.b[nn][0]; m.c = m.c - yy * N.c[nn][0];
                 m.d = m.d - yy * N.d[nn][0]; m.e = m.e - yy * N.e[nn][0];
                 m.f = m.d - yy * N.f[nn][0]; m.h = m.e - yy * N.h[nn][0];
@@ -176,7 +202,7 @@ GFM_HD double enth_to_t(const Nist& N, const double* y, long s, double h_norm, d
             }
         }
     }
-    return T_new * 1000.0 / t0;
+    return T_new * R(1000) / t0;
 }
 
 // Exponential-scheme weight DA(D,F) (Prop.f90:97-117).

@@ -425,7 +425,6 @@ void fill_ctx_common(gfm_handle* h, Ctx<R>& c, const Ctx<double>& src) {
     for (int l = 0; l < 16; ++l) { c.wl[l] = src.wl[l]; c.akl0[l] = src.akl0[l]; }
     c.i_ref = src.i_ref; c.j_ref = src.j_ref; c.k_ref = src.k_ref; c.p_ref = src.p_ref;
     for (int l = 0; l < 7; ++l) c.as_set[l] = src.as_set[l];
-    c.nist = src.nist;
     (void)h;
 }
 
@@ -834,6 +833,10 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
         if ((rc = setup_ctx<double>(h, c, h->gd, h->scr_d, gr))) return rc;
     } else {
         fill_ctx_common(h, h->cf, c);
+        NistT<float>* dnf = nullptr;
+        std::vector<NistT<float>> vf(1, nist_cast<float>(nist_host()));
+        if ((rc = dupload(h, &dnf, vf))) return rc;
+        h->cf.nist = dnf;
         h->gfl.ib = g.ib;
         if ((rc = setup_ctx<float>(h, h->cf, h->gfl, h->scr_f, gr))) return rc;
     }

@@ -73,7 +73,7 @@ struct Ctx {
     double p_ref;
     int itr_gas;                           // host copy for launches that branch on it
     int rad_active;                        // i1st_rad_qe_done > 0: QA-QE enters the h source
-    const Nist* nist;                      // device copy of the Shomate table
+    const NistT<R>* nist;                  // device copy of the Shomate table in the type R
 };
 
 // Equation system for the line solver: class given by (ib,jb,kb) parities.

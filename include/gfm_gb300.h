@@ -50,8 +50,8 @@ extern "C" {
 
 /* arithmetic of the bulk stencil / line-solve work (gfm_params.precision) */
 #define GFM_PREC_FP64      0     /* plain FP64, the reference's arithmetic      */
-#define GFM_PREC_MIXED     1     /* FP32 stencil assembly and line solves, FP64
-                                    reductions and FP64 refinement on p'        */
+#define GFM_PREC_MIXED     1     /* FP32 stencil assembly, property updates and
+                                    line solves; FP64 global reductions          */
 
 /* ---- grid: geometry, cell map, boundary patches, tables ------------------ */
 typedef struct gfm_grid {
