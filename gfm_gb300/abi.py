@@ -23,6 +23,7 @@ GFM_E_UNSUPPORTED = -4
 GFM_E_NOMEM = -5
 GFM_E_TIMEOUT = -6
 GFM_E_NODEVICE = -7
+GFM_E_LIMIT = -8
 
 GFM_ADI_MARCH = 0
 GFM_ADI_REDBLACK = 1
@@ -164,6 +165,8 @@ SIGNATURES = [
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     ("gfm_gpu_last_error", C.c_char_p, [C.c_void_p]),
     ("gfm_gpu_destroy", None, [C.c_void_p]),
+    ("gfm_adlbl3_noalloc", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.POINTER(C.c_void_p), C.c_void_p] + [C.c_int] * 7 + [C.c_void_p]),
 ]
 
 _lib = None

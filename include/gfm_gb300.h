@@ -41,6 +41,7 @@ extern "C" {
 #define GFM_E_NOMEM       (-5)   /* allocation failed                       */
 #define GFM_E_TIMEOUT     (-6)   /* bounded device wait ran out             */
 #define GFM_E_NODEVICE    (-7)   /* no CUDA device / extension not usable   */
+#define GFM_E_LIMIT       (-8)   /* input beyond a fixed size limit         */
 
 /* ADI line-solver ordering (gfm_params.adi_mode) */
 #define GFM_ADI_MARCH      0     /* reference order: x-plane Gauss-Seidel march,
@@ -222,6 +223,36 @@ int  gfm_gpu_iteration_profile(gfm_handle *h, long long *kernels_per_iter,
 /* Last error text of this handle (never NULL). */
 const char *gfm_gpu_last_error(gfm_handle *h);
 void gfm_gpu_destroy(gfm_handle *h);
+
+/* ---- line solve without any device allocation ---------------------------- */
+/* No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory -- code running inside a host program that owns all
+ * of it (another framework's caching allocator, a pool sized once at start-up,
+ * a process under a device-memory quota) must not call cudaMalloc behind that
+ * host's back, so it cannot create a gfm_gpu handle.
+ *
+ * Same solve as gfm_gpu_adlbl3 in GFM_ADI_MARCH order with FP64 arithmetic, but
+ * every array is a DEVICE pointer owned by the caller, in the reference layout
+ * (column-major A(MP,NP,LP), mp*np*lp doubles each; ibcell mp*np*lp int16):
+ * xt is solved in place, ap, the six as[q] (the array of six pointers itself is
+ * host memory) and bs are read.  Nothing is allocated: the working storage is
+ * one fixed device array inside the library, 2 MiB per GPU that loads it, held
+ * until the process exits.  Limit: one x-plane of the solved class may hold at
+ * most 65536 (J,K) points, ((je-jb)/2+1)*((ke-kb)/2+1) <= 65536; larger planes
+ * return GFM_E_LIMIT.  Index ranges as for gfm_gpu_adlbl3; pointers that are
+ * not device memory of the current device return GFM_E_ARG.
+ *
+ * The kernel is queued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and the call returns without waiting for it.  The first call on each
+ * device looks up the address of the working storage (cudaGetSymbolAddress);
+ * make that first call before any stream capture starts.  Every call uses the
+ * same working storage, so calls whose kernels can overlap on the GPU (other
+ * streams, other host threads) race and give wrong results: order them. */
+int  gfm_adlbl3_noalloc(int mp, int np, int lp, const int16_t *ibcell,
+                        double *xt, const double *ap,
+                        const double *const as[6], const double *bs,
+                        int ib, int ie, int jb, int je, int kb, int ke,
+                        int nim, void *stream);
 
 #ifdef __cplusplus
 }
