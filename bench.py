@@ -129,11 +129,12 @@ class ClockSampler:
 
 
 def load_traffic(prec: str):
-    """Per-launch DRAM traffic of the line-solver kernel from a committed ncu summary."""
+    """DRAM traffic of one colour visit of the line solver (pass L=1, average,
+    pass L=2, average) from the committed ncu summary of the same workload."""
     p = ROOT / "profiles" / f"ncu_adi_{prec}_192x96x64.json"
     if p.exists():
         try:
-            return json.loads(p.read_text()).get("dram_bytes_per_launch")
+            return json.loads(p.read_text())
         except Exception:
             return None
     return None
@@ -313,7 +314,10 @@ def run_ours(args):
                     "pinned": bool(getattr(fields, "_pinned", False)),
                     "path": "gfm_gpu_upload + K x gfm_gpu_gflow(1) + gfm_gpu_download"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "frac": (achieved / peak) if achieved else None,
+                         "traffic": traffic.get("dram_bytes_per_colour_visit") if traffic else None,
+                         "traffic_unit": "DRAM bytes per colour visit (4 launches) of the 192x96x64 P equation, ncu",
+                         "traffic_algorithmic": traffic.get("algorithmic_bytes_per_colour_visit") if traffic else None,
                          "peak_kind": peak_kind, "kernel": "ADLBL3 line solver (plane updates)",
                          "algorithmic_bytes": f"{BYTES_PER_CELL_VISIT} x {w} B per cell per plane visit",
                          "adi_launches": adi_launches, "adi_ms": adi_ms},

@@ -10,11 +10,11 @@
 // Plane order:
 //   GFM_ADI_MARCH    the reference's Gauss-Seidel march: planes IB..IE then
 //                    IE..IB, NIM times, one CTA per equation walking the planes;
-//   GFM_ADI_REDBLACK all even planes at once, then all odd planes (twice per
-//                    sweep, NIM sweeps), one CTA per (equation, plane).
-// Scratch: PT of the y-lines and of the z-lines, and the pass results XT2/XT3,
-// live in per-equation class-sized device buffers (QT is stored in XT2/XT3 and
-// back-substituted in place).
+//                    PT and the pass results XT2/XT3 live in field-sized
+//                    scratch (QT is stored in XT2/XT3 and back-substituted in
+//                    place);
+//   GFM_ADI_REDBLACK all planes of one colour at once, twice per sweep, NIM
+//                    sweeps, on a colour-split copy of the system (below).
 #include "state.cuh"
 
 namespace gfm {
@@ -144,29 +144,40 @@ __global__ void k_adlbl3_march(GeoT<R> g, AdiBatch<R> b) {
     }
 }
 
-// red-black: one CTA per (equation, plane of the requested colour)
-template <typename R>
-__global__ void k_adlbl3_rb(GeoT<R> g, AdiBatch<R> b, int colour, int max_planes, int sweep) {
-    int e = blockIdx.x / max_planes, pl = blockIdx.x % max_planes;
-    if (e >= b.nsys) return;
-    const Sys<R>& s = b.sys[e];
-    if (sweep >= s.nim) return;
-    int npl = (s.ie - s.ib) / 2 + 1;
-    int p = 2 * pl + colour;
-    if (p >= npl) return;
-    adlz<R, false>(g, s, b.scr[e], s.ib + 2 * p);
-}
-
 // ---------------------------------------------------------------------------
-// Red-black form.  The tridiagonal matrix of every y- and z-line is constant
-// during one ADLBL3 call, so its Thomas pivots are factored once: PT (as in
-// ADLZY/ADLYZ) and IA = 1/ALP, with IA = 0 marking the rows the reference
-// copies unchanged (|ALP| <= 1e-20 or a blocked cell).  Within one plane visit
-// the x-neighbour part of the right-hand side, BS + AS12*XT(I+2) +
-// AS11*XT(I-2), is constant (neighbour planes have the other colour) and is
-// summed first, as the reference does.  Threads map to (plane, line) with the
-// plane index fastest, so each step of the sequential line recurrence reads
-// consecutive same-colour planes: coalesced across the warp.
+// Red-black order (GFM_ADI_REDBLACK) on a colour-split copy of the system.
+//
+// Planes of one colour are updated together; each plane update is still ADLZ
+// (L = 1, 2: every y-line and z-line solved from the plane as it was before
+// the pass, then averaged).  Three things make it fast on GB300:
+//
+//  * Colour split.  For the duration of one ADLBL3 call the unknown and the
+//    factored rows live in arrays where the x-index xi = I>>1 of the class is
+//    split by parity, element (xi,yj,zk) at (xi&1)*CBH + (zk*HY+yj)*PXH + xi>>1.
+//    Planes of one colour are then unit-stride, so a warp whose lanes are
+//    consecutive same-colour planes reads whole sectors; the x-neighbours
+//    I+-2 are the other half at the same or the adjacent position.
+//  * Factor once.  The tridiagonal matrix of every line is fixed during the
+//    call, so its Thomas pivots are computed once and every row is stored
+//    pre-scaled by IA = 1/ALP in two vector records per line direction:
+//        A = (AS_op*IA, AS_om*IA, AS_sub*IA, PT),  B = (BS*IA, AS12*IA, AS11*IA, 0)
+//    (op/om: the two in-plane neighbours across the line, sub: the previous
+//    point of the line).  Rows the reference copies unchanged (|ALP| <= 1e-20
+//    or a blocked cell) have zero coefficients and PT = -0.0, a value no other
+//    row stores (a zero PT of any other row is +0.0).  A forward step
+//    is then QT = B.x + B.y*XT(I+2) + B.z*XT(I-2) + A.x*XT(op) + A.y*XT(om)
+//    + A.z*QT(prev), the reference's (BSY + AS_sub*QT(prev))/ALP with the
+//    division applied to each term.  Within a pass the x-neighbour part is
+//    constant: the first pass of a visit stores it (SBY/SBZ), the second
+//    reads it.
+//  * Segmented recurrences.  Each line is cut into S segments, one warp per
+//    segment (lane = plane).  The forward and the back substitution are
+//    affine recurrences: every thread runs its segment from a zero start,
+//    keeping the values and the running product of the multipliers in
+//    registers; a scan over the S segment maps in shared memory gives each
+//    segment its true start, and the thread corrects its values in place.
+//    The non-recurrent part of every row is computed before the recurrence
+//    runs, so all loads of a segment are in flight together.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct RbBatch {
@@ -175,155 +186,254 @@ struct RbBatch {
     int nsys;
 };
 
-__device__ __forceinline__ int rb_nplanes(int ib, int ie) { return (ie - ib) / 2 + 1; }
-
-// factor every y-line and z-line of every plane (both colours)
 template <typename R>
-__global__ void k_rb_factor(GeoT<R> g, RbBatch<R> b) {
+__device__ __forceinline__ int sidx(const GeoT<R>& g, int xi, int yj, int zk) {
+    return (xi & 1) * g.CBH + (zk * g.HY + yj) * g.PXH + (xi >> 1);
+}
+__device__ __forceinline__ int rb_nplanes(int ib, int ie) { return (ie - ib) / 2 + 1; }
+// the copy-row marker PT = -0.0
+__device__ __forceinline__ bool rb_copy(float pt) { return __float_as_uint(pt) == 0x80000000u; }
+__device__ __forceinline__ bool rb_copy(double pt) {
+    return (unsigned long long)__double_as_longlong(pt) == 0x8000000000000000ull;
+}
+__device__ __forceinline__ int rb_class(int ib, int jb, int kb) { return (ib & 1) | ((jb & 1) << 1) | ((kb & 1) << 2); }
+
+// XT of the whole class -> split copy
+template <typename R>
+__global__ void k_rbs_in(GeoT<R> g, RbBatch<R> b) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const R* __restrict__ xt = s.xt + (long long)rb_class(s.ib, s.jb, s.kb) * g.CB;
+    const int n = g.HX * g.HY * g.HZ;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int xi = t % g.HX, r = t / g.HX;
+        const int yj = r % g.HY, zk = r / g.HY;
+        w.xs[sidx(g, xi, yj, zk)] = xt[(zk * g.HY + yj) * g.PX + xi];
+    }
+}
+
+// Factored, pre-scaled rows of every y-line and z-line of every plane (both
+// colours), thread per line with the plane index fastest.  The pivot chain is
+// ADLZY/ADLYZ's: ALP = AP - PT(prev)*AS_sub, PT = AS_next/ALP.  Rows are read
+// C at a time before the chain runs over them, so a thread keeps C rows of
+// loads in flight.
+template <typename R>
+__global__ void k_rbs_factor(GeoT<R> g, RbBatch<R> b) {
+    constexpr int C = 8;
     const Sys<R>& s = b.sys[blockIdx.y];
     const AdiScratch<R>& w = b.scr[blockIdx.y];
     const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const long long ny = (long long)npl * nK, nz = (long long)npl * nJ;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ny + nz; t += (long long)gridDim.x * blockDim.x) {
-        if (t < ny) {
-            const int I = s.ib + 2 * (int)(t % npl), K = s.kb + 2 * (int)(t / npl);
-            R pt_prev = R(0);
-            for (int J = s.jb; J <= s.je; J += 2) {
-                const long long o = pidx(g, I, J, K);
-                R alp = s.ap[o] - pt_prev * s.as[2][o];
-                R pt, ia;
-                if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) { pt = R(0); ia = R(0); }
-                else { pt = s.as[3][o] / alp; ia = R(1) / alp; }
-                w.pty[o] = pt;
-                w.iay[o] = ia;
-                pt_prev = pt;
+    const int ny = npl * nK, nz = npl * nJ;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ny + nz; t += gridDim.x * blockDim.x) {
+        const bool zl = t >= ny;
+        const int u = zl ? t - ny : t;
+        const int I = s.ib + 2 * (u % npl);
+        // y-line (I,*,K): sub AS(J-2)=as[2], next AS(J+2)=as[3], across as[5]/as[4]
+        // z-line (I,J,*): sub AS(K-2)=as[4], next AS(K+2)=as[5], across as[3]/as[2]
+        const R* __restrict__ a_sub = s.as[zl ? 4 : 2];
+        const R* __restrict__ a_next = s.as[zl ? 5 : 3];
+        const R* __restrict__ a_op = s.as[zl ? 3 : 5];
+        const R* __restrict__ a_om = s.as[zl ? 2 : 4];
+        Quad<R>* __restrict__ qa = zl ? w.za : w.ya;
+        Quad<R>* __restrict__ qb = zl ? w.zb : w.yb;
+        const int n = zl ? nK : nJ;
+        const int J0 = zl ? s.jb + 2 * (u / npl) : s.jb, K0 = zl ? s.kb : s.kb + 2 * (u / npl);
+        const int o0 = (int)pidx(g, I, J0, K0), q0 = sidx(g, I >> 1, J0 >> 1, K0 >> 1);
+        const int ostep = zl ? g.PX * g.HY : g.PX, qstep = zl ? g.HY * g.PXH : g.PXH;
+        R pt_prev = R(0);
+        for (int e0 = 0; e0 < n; e0 += C) {
+            R vap[C], vsub[C], vnext[C], vop[C], vom[C], vbs[C], va1[C], va0[C];
+            bool blk[C];
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
+                if (e0 + i < n) {
+                    const int o = o0 + (e0 + i) * ostep;
+                    vap[i] = s.ap[o]; vsub[i] = a_sub[o]; vnext[i] = a_next[o];
+                    vop[i] = a_op[o]; vom[i] = a_om[o]; vbs[i] = s.bs[o];
+                    va1[i] = s.as[1][o]; va0[i] = s.as[0][o];
+                    blk[i] = g.ib[o] >= 1;
+                }
             }
-        } else {
-            const long long u = t - ny;
-            const int I = s.ib + 2 * (int)(u % npl), J = s.jb + 2 * (int)(u / npl);
-            R pt_prev = R(0);
-            for (int K = s.kb; K <= s.ke; K += 2) {
-                const long long o = pidx(g, I, J, K);
-                R alp = s.ap[o] - pt_prev * s.as[4][o];
-                R pt, ia;
-                if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) { pt = R(0); ia = R(0); }
-                else { pt = s.as[5][o] / alp; ia = R(1) / alp; }
-                w.ptz[o] = pt;
-                w.iaz[o] = ia;
-                pt_prev = pt;
+#pragma unroll
+            for (int i = 0; i < C; ++i) {
+                if (e0 + i < n) {
+                    const int q = q0 + (e0 + i) * qstep;
+                    const R alp = vap[i] - pt_prev * vsub[i];
+                    Quad<R> A, B;
+                    if (fabs(alp) <= R(1.0e-20) || blk[i]) {
+                        A = Quad<R>{R(0), R(0), R(0), -R(0)};
+                        B = Quad<R>{R(0), R(0), R(0), R(0)};
+                        pt_prev = R(0);
+                    } else {
+                        const R ia = R(1) / alp;
+                        const R pt = vnext[i] / alp;
+                        A = Quad<R>{vop[i] * ia, vom[i] * ia, vsub[i] * ia, pt + R(0)};   // +0.0: no -0.0 here
+                        B = Quad<R>{vbs[i] * ia, va1[i] * ia, va0[i] * ia, R(0)};
+                        pt_prev = pt;
+                    }
+                    qa[q] = A;
+                    qb[q] = B;
+                }
             }
         }
     }
 }
 
-// One line of one pass, software-pipelined: the inputs of D consecutive
-// steps are loaded before the dependent recurrence runs over them, so a thread
-// keeps ~D x 8 independent loads in flight.  Consecutive elements of a y-line
-// are PX apart, of a z-line PX*HY apart; x-neighbours I+-2 are +-1.  Offsets
-// are 32-bit (a parity-split field holds < 2^31 elements, checked at create).
-template <typename R> struct Pipe { static constexpr int D = 8; };
-template <> struct Pipe<double> { static constexpr int D = 4; };
+// at most M elements per segment, held in registers; S <= 32 segments per line
+template <typename R> struct RbSeg { static constexpr int M = 8; };
 
-template <typename R, bool FIRST, bool ZLINE>
-__device__ __forceinline__ void rb_line(const R* __restrict__ xt, const R* __restrict__ bs, const R* __restrict__ a_xp,
-                                        const R* __restrict__ a_xm, const R* __restrict__ a_op, const R* __restrict__ a_om,
-                                        const R* __restrict__ a_sub, const R* __restrict__ ia, const R* __restrict__ pt,
-                                        R* __restrict__ bsx, R* __restrict__ out, int o0, int step, int ostep, int n) {
-    constexpr int D = Pipe<R>::D;
-    R qt_prev = xt[o0 - step];
-    int c = 0, o = o0;
-    for (; c + D <= n; c += D, o += D * step) {
-        R vb[D], vo1[D], vo2[D], vx1[D], vx2[D], vs[D], vi[D], vc[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const int q = o + d * step;
-            if (FIRST) vb[d] = bs[q] + a_xp[q] * xt[q + 1] + a_xm[q] * xt[q - 1];
-            else vb[d] = bsx[q];
-            vo1[d] = a_op[q]; vo2[d] = a_om[q];
-            vx1[d] = xt[q + ostep]; vx2[d] = xt[q - ostep];
-            vs[d] = a_sub[q]; vi[d] = ia[q]; vc[d] = xt[q];
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const int q = o + d * step;
-            if (FIRST && !ZLINE) bsx[q] = vb[d];
-            R qt = vi[d] == R(0) ? vc[d] : ((vb[d] + vo1[d] * vx1[d] + vo2[d] * vx2[d]) + vs[d] * qt_prev) * vi[d];
-            out[q] = qt;
-            qt_prev = qt;
-        }
-    }
-    for (; c < n; ++c, o += step) {
-        R b = FIRST ? bs[o] + a_xp[o] * xt[o + 1] + a_xm[o] * xt[o - 1] : bsx[o];
-        if (FIRST && !ZLINE) bsx[o] = b;
-        const R iv = ia[o];
-        R qt = iv == R(0) ? xt[o] : ((b + a_op[o] * xt[o + ostep] + a_om[o] * xt[o - ostep]) + a_sub[o] * qt_prev) * iv;
-        out[o] = qt;
-        qt_prev = qt;
-    }
-    // back-substitution from the far boundary
-    R nxt = xt[o0 + n * step];
-    c = n - 1;
-    o = o0 + c * step;
-    for (; c + 1 >= D; c -= D, o -= D * step) {
-        R vp[D], vq[D];
-#pragma unroll
-        for (int d = 0; d < D; ++d) { vp[d] = pt[o - d * step]; vq[d] = out[o - d * step]; }
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            R v = nxt * vp[d] + vq[d];
-            out[o - d * step] = v;
-            nxt = v;
-        }
-    }
-    for (; c >= 0; --c, o -= step) {
-        R v = nxt * pt[o] + out[o];
-        out[o] = v;
-        nxt = v;
-    }
-}
-
-// one pass (both directions) over the planes of one colour; the first pass of a
-// visit (L=1) computes BSX (y-lines store it), the second reads it
-template <typename R, bool FIRST>
-__global__ void k_rb_pass(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
-    const Sys<R>& s = b.sys[blockIdx.y];
-    if (sweep >= s.nim) return;
-    const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const int npl = rb_nplanes(s.ib, s.ie);
-    const int npc = (npl - colour + 1) / 2;   // planes of this colour
-    const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const long long ny = (long long)npc * nK, nz = (long long)npc * nJ;
-    const int sy = g.PX, sz = g.PX * g.HY;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < ny + nz; t += (long long)gridDim.x * blockDim.x) {
-        if (t < ny) {
-            const int I = s.ib + 2 * (2 * (int)(t % npc) + colour), K = s.kb + 2 * (int)(t / npc);
-            rb_line<R, FIRST, false>(s.xt, s.bs, s.as[1], s.as[0], s.as[5], s.as[4], s.as[2], w.iay, w.pty, w.bsx, w.xt2,
-                                     (int)pidx(g, I, s.jb, K), sy, sz, nJ);
-        } else {
-            const long long u = t - ny;
-            const int I = s.ib + 2 * (2 * (int)(u % npc) + colour), J = s.jb + 2 * (int)(u / npc);
-            rb_line<R, FIRST, true>(s.xt, s.bs, s.as[1], s.as[0], s.as[3], s.as[2], s.as[4], w.iaz, w.ptz, w.bsx, w.xt3,
-                                    (int)pidx(g, I, J, s.kb), sz, sy, nK);
-        }
-    }
-}
-
-// XT = (XT2 + XT3)/2 on the planes of one colour
-template <typename R>
-__global__ void k_rb_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+// One pass of all y- and z-lines of the planes of one colour.  Block = S warps
+// x 32 lanes; lane = one line (32 consecutive line slots), warp = segment.
+template <typename R, int S, bool FIRST>
+__global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+    constexpr int M = RbSeg<R>::M;
+    __shared__ R sA[S][32], sB[S][32];
     const Sys<R>& s = b.sys[blockIdx.y];
     if (sweep >= s.nim) return;
     const AdiScratch<R>& w = b.scr[blockIdx.y];
     const int npl = rb_nplanes(s.ib, s.ie);
     const int npc = (npl - colour + 1) / 2;
     const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const long long n = (long long)npc * nJ * nK;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-        const int I = s.ib + 2 * (2 * (int)(t % npc) + colour);
-        const long long r = t / npc;
-        const int J = s.jb + 2 * (int)(r % nJ), K = s.kb + 2 * (int)(r / nJ);
-        const long long o = pidx(g, I, J, K);
-        s.xt[o] = (w.xt2[o] + w.xt3[o]) / R(2);
+    const int ny = npc * nK, nz = npc * nJ;
+    if ((int)blockIdx.x * 32 >= ny + nz) return;   // whole block
+    const int lane = threadIdx.x & 31, seg = threadIdx.x >> 5;
+    const int t = blockIdx.x * 32 + lane;
+    const bool active = t < ny + nz;
+    const int xh = (s.ib >> 1) + colour;           // xi of the first plane of this colour
+    const int h = xh & 1;
+    const int hb = h * g.CBH + (xh >> 1);
+    const int SZ = g.HY * g.PXH;
+    const int dxp = (1 - 2 * h) * g.CBH + h, dxm = dxp - 1;   // x-neighbours I+2, I-2 in the other half
+    const bool zl = active && t >= ny;
+    int base = 0, step = 0, ostep = 0, n = 0;
+    if (active) {
+        if (!zl) {
+            const int r = t % npc, kk = t / npc;
+            base = hb + ((s.kb >> 1) + kk) * SZ + (s.jb >> 1) * g.PXH + r;
+            step = g.PXH; ostep = SZ; n = nJ;
+        } else {
+            const int u = t - ny, r = u % npc, jj = u / npc;
+            base = hb + (s.kb >> 1) * SZ + ((s.jb >> 1) + jj) * g.PXH + r;
+            step = SZ; ostep = g.PXH; n = nK;
+        }
+    }
+    const R* __restrict__ x = w.xs;
+    const Quad<R>* __restrict__ QA = zl ? w.za : w.ya;
+    const Quad<R>* __restrict__ QB = zl ? w.zb : w.yb;
+    R* __restrict__ sb = zl ? w.sbz : w.sby;
+    R* __restrict__ out = zl ? w.x3 : w.x2;
+    const int m = (n + S - 1) / S;
+    const int e0 = seg * m;
+    int cnt = n - e0;
+    cnt = cnt < 0 ? 0 : (cnt > m ? m : cnt);
+
+    // non-recurrent part of every row of the segment
+    R rr[M], al[M], pv[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        if (i < cnt) {
+            const int o = base + (e0 + i) * step;
+            const Quad<R> A = QA[o];
+            R v;
+            if (FIRST) {
+                const Quad<R> B = QB[o];
+                const R bx = B.x + B.y * x[o + dxp] + B.z * x[o + dxm];
+                sb[o] = bx;
+                v = bx + A.x * x[o + ostep] + A.y * x[o - ostep];
+            } else {
+                v = sb[o] + A.x * x[o + ostep] + A.y * x[o - ostep];
+            }
+            if (rb_copy(A.w)) v = x[o];
+            rr[i] = v;
+            al[i] = A.z;
+            pv[i] = A.w;
+        }
+    }
+    // forward recurrence of the segment from a zero start
+    R q[M], P[M];
+    R qc = R(0), Pc = R(1);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        if (i < cnt) {
+            qc = rr[i] + al[i] * qc;
+            Pc = al[i] * Pc;
+            q[i] = qc;
+            P[i] = Pc;
+        }
+    }
+    sA[seg][lane] = cnt > 0 ? Pc : R(1);
+    sB[seg][lane] = cnt > 0 ? qc : R(0);
+    __syncthreads();
+    R qin = active ? x[base - step] : R(0);        // XT one step below the line (JBML / KBML)
+    for (int k = 0; k < seg; ++k) qin = sA[k][lane] * qin + sB[k][lane];
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+        if (i < cnt) q[i] = q[i] + P[i] * qin;
+    __syncthreads();
+
+    // back substitution of the segment from a zero end value
+    R xc = R(0), Rc = R(1);
+#pragma unroll
+    for (int i = M - 1; i >= 0; --i) {
+        if (i < cnt) {
+            xc = pv[i] * xc + q[i];
+            Rc = pv[i] * Rc;
+            q[i] = xc;
+            P[i] = Rc;
+        }
+    }
+    sA[seg][lane] = cnt > 0 ? Rc : R(1);
+    sB[seg][lane] = cnt > 0 ? xc : R(0);
+    __syncthreads();
+    R xin = active ? x[base + n * step] : R(0);    // XT one step above the line (JEPL / KEPL), never updated
+    for (int k = S - 1; k > seg; --k) xin = sA[k][lane] * xin + sB[k][lane];
+#pragma unroll
+    for (int i = 0; i < M; ++i)
+        if (i < cnt) out[base + (e0 + i) * step] = q[i] + P[i] * xin;
+}
+
+// XT = (XT2 + XT3)/2 on the planes of one colour (split copy).  Grid x runs
+// over the planes of the colour (unit stride); each thread row handles
+// kAvgRows (J,K) rows, kAvgRows*8 rows per block, loads issued together.
+constexpr int kAvgRows = 8;
+template <typename R>
+__global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    if (sweep >= s.nim) return;
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = rb_nplanes(s.ib, s.ie);
+    const int npc = (npl - colour + 1) / 2;
+    const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= npc) return;
+    const int xh = (s.ib >> 1) + colour;
+    const int hb = (xh & 1) * g.CBH + (xh >> 1) + r + ((s.kb >> 1) * g.HY + (s.jb >> 1)) * g.PXH;
+    const int row0 = (blockIdx.z * blockDim.y + threadIdx.y) * kAvgRows;
+    int o[kAvgRows];
+    R a[kAvgRows], c[kAvgRows];
+#pragma unroll
+    for (int i = 0; i < kAvgRows; ++i) {
+        const int row = row0 + i;
+        const int jj = row % nJ, kk = row / nJ;
+        o[i] = hb + (kk * g.HY + jj) * g.PXH;
+        if (row < nJ * nK) { a[i] = w.x2[o[i]]; c[i] = w.x3[o[i]]; }
+    }
+#pragma unroll
+    for (int i = 0; i < kAvgRows; ++i)
+        if (row0 + i < nJ * nK) w.xs[o[i]] = (a[i] + c[i]) / R(2);
+}
+
+// split copy -> XT on the solve range
+template <typename R>
+__global__ void k_rbs_out(GeoT<R> g, RbBatch<R> b) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const int n = npl * nJ * nK;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int p = t % npl, rest = t / npl;
+        const int I = s.ib + 2 * p, J = s.jb + 2 * (rest % nJ), K = s.kb + 2 * (rest / nJ);
+        s.xt[pidx(g, I, J, K)] = w.xs[sidx(g, I >> 1, J >> 1, K >> 1)];
     }
 }
 
@@ -374,6 +484,31 @@ void launch_residual(const Ctx<R>& c, const Sys<R>& s, int slot, cudaStream_t st
     k_residual<R><<<(int)nb, 256, 0, st>>>(c.g, s, c.partials, slot);
 }
 
+// Segments per line: the smallest power of two that keeps a segment within
+// the M registers of one thread (lines of up to 32*M points, checked at create).
+template <typename R>
+int rb_segments(int n) {
+    int S = 1;
+    while (S < 32 && S * RbSeg<R>::M < n) S *= 2;
+    return S;
+}
+template <typename R, bool FIRST>
+void rb_pass_s(int S, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns, cudaStream_t st) {
+    switch (S) {
+        case 1: k_rbs_pass<R, 1, FIRST><<<gp, 32, 0, st>>>(g, rb, colour, ns); break;
+        case 2: k_rbs_pass<R, 2, FIRST><<<gp, 64, 0, st>>>(g, rb, colour, ns); break;
+        case 4: k_rbs_pass<R, 4, FIRST><<<gp, 128, 0, st>>>(g, rb, colour, ns); break;
+        case 8: k_rbs_pass<R, 8, FIRST><<<gp, 256, 0, st>>>(g, rb, colour, ns); break;
+        case 16: k_rbs_pass<R, 16, FIRST><<<gp, 512, 0, st>>>(g, rb, colour, ns); break;
+        default: k_rbs_pass<R, 32, FIRST><<<gp, 1024, 0, st>>>(g, rb, colour, ns); break;
+    }
+}
+template <typename R>
+void rb_pass(int S, bool first, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns, cudaStream_t st) {
+    if (first) rb_pass_s<R, true>(S, gp, g, rb, colour, ns, st);
+    else rb_pass_s<R, false>(S, gp, g, rb, colour, ns, st);
+}
+
 // scratch buffers are passed through Sys-aligned array set by the host
 template <typename R>
 void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, int mode, cudaStream_t st) {
@@ -396,8 +531,9 @@ void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>*
     } else {
         RbBatch<R> rb;
         rb.nsys = nsys;
-        long long max_lines = 0, max_cells = 0;
-        int nim = 0;
+        long long max_lines = 0, max_cells = 0, max_slots = 0, max_np = 1, max_rows = 1;
+        const long long max_class = (long long)g.HX * g.HY * g.HZ;
+        int nim = 0, max_n = 1;
         for (int e = 0; e < nsys; ++e) {
             rb.sys[e] = sys[e];
             rb.scr[e] = scr[e];
@@ -405,21 +541,29 @@ void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>*
             long long np_ = (q.ie - q.ib) / 2 + 1, nK = (q.ke - q.kb) / 2 + 1, nJ = (q.je - q.jb) / 2 + 1;
             max_lines = np_ * (nK + nJ) > max_lines ? np_ * (nK + nJ) : max_lines;
             max_cells = np_ * nK * nJ > max_cells ? np_ * nK * nJ : max_cells;
+            max_slots = (np_ + 1) / 2 * (nK + nJ) > max_slots ? (np_ + 1) / 2 * (nK + nJ) : max_slots;
+            max_np = np_ > max_np ? np_ : max_np;
+            max_rows = nK * nJ > max_rows ? nK * nJ : max_rows;
+            max_n = (int)(nK > max_n ? nK : max_n);
+            max_n = (int)(nJ > max_n ? nJ : max_n);
             nim = q.nim > nim ? q.nim : nim;
         }
-        const int T = 128;
-        dim3 gf((unsigned)((max_lines + T - 1) / T), nsys);
-        k_rb_factor<R><<<gf, T, 0, st>>>(g, rb);
-        dim3 gp((unsigned)((max_lines / 2 + T) / T), nsys);
-        dim3 ga((unsigned)((max_cells / 2 + 255) / 256 < 2048 ? (max_cells / 2 + 255) / 256 : 2048), nsys);
+        const int S = rb_segments<R>(max_n);
+        auto blocks = [](long long n, int t) { long long b = (n + t - 1) / t; return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b)); };
+        k_rbs_in<R><<<dim3(blocks(max_class, 256), nsys), 256, 0, st>>>(g, rb);
+        k_rbs_factor<R><<<dim3(blocks(max_lines, 128), nsys), 128, 0, st>>>(g, rb);
+        // line slots of one colour: ceil(planes/2) x (nK + nJ), 32 per block
+        const dim3 gp((unsigned)((max_slots + 31) / 32), nsys);
+        const dim3 ga((unsigned)((max_np + 1) / 2 + 31) / 32, nsys, (unsigned)((max_rows + 8 * kAvgRows - 1) / (8 * kAvgRows)));
         for (int ns = 0; ns < nim; ++ns)
             for (int half = 0; half < 2; ++half)
                 for (int colour = 0; colour < 2; ++colour) {
-                    k_rb_pass<R, true><<<gp, T, 0, st>>>(g, rb, colour, ns);
-                    k_rb_avg<R><<<ga, 256, 0, st>>>(g, rb, colour, ns);
-                    k_rb_pass<R, false><<<gp, T, 0, st>>>(g, rb, colour, ns);
-                    k_rb_avg<R><<<ga, 256, 0, st>>>(g, rb, colour, ns);
+                    rb_pass<R>(S, true, gp, g, rb, colour, ns, st);
+                    k_rbs_avg<R><<<ga, dim3(32, 8), 0, st>>>(g, rb, colour, ns);
+                    rb_pass<R>(S, false, gp, g, rb, colour, ns, st);
+                    k_rbs_avg<R><<<ga, dim3(32, 8), 0, st>>>(g, rb, colour, ns);
                 }
+        k_rbs_out<R><<<dim3(blocks(max_cells, 256), nsys), 256, 0, st>>>(g, rb);
     }
 }
 

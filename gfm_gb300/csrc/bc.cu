@@ -103,13 +103,39 @@ __device__ void extr_wall_one(const Ctx<R>& c, const ExtrRec& e) {
     dnst_at(c, o);
 }
 
-// wall cells whose six axis neighbours are walls read the cell above them
-// (EXT1 falls through, Extr.f90:626-660): one thread per (I,J) column, K
-// ascending, as the Fortran loop visits them
+// Wall cells whose six axis neighbours are walls read the cell above them,
+// (I,J,K+2) (EXT1 falls through, Extr.f90:626-660).  The Fortran loop visits
+// K ascending, so every such cell reads the value its source had before this
+// EXTR call: the sources are gathered first (k_extr_ft_gather), then written
+// (k_extr_ft_apply), one thread per cell.
 template <typename R>
-__global__ void k_extr_ft(Ctx<R> c) {
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_ft_cols; t += gridDim.x * blockDim.x)
-        for (int q = c.ft_col_start[t]; q < c.ft_col_start[t + 1]; ++q) extr_wall_one(c, c.extr_ft[q]);
+__global__ void k_extr_ft_gather(Ctx<R> c) {
+    const GeoT<R>& g = c.g;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_ft; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_ft[t];
+        const long long o1 = pidx(g, e.I1, e.J1, e.K1), o2 = pidx(g, e.I2, e.J2, e.K2);
+        R* v = c.ft_buf + (long long)t * kFtVals;
+        v[0] = c.P[o1] * R(e.F1) + c.P[o2] * R(e.F2);
+        v[1] = c.TMU[o2];
+        v[2] = c.GAMA[o2];
+        for (int L = 1; L <= 7; ++L) v[2 + L] = c.GF[L - 1][o1];
+        v[10] = c.T[o1];
+    }
+}
+template <typename R>
+__global__ void k_extr_ft_apply(Ctx<R> c) {
+    const GeoT<R>& g = c.g;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_ft; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_ft[t];
+        const long long o = pidx(g, e.I, e.J, e.K);
+        const R* v = c.ft_buf + (long long)t * kFtVals;
+        c.P[o] = v[0];
+        c.TMU[o] = v[1];
+        c.GAMA[o] = v[2];
+        for (int L = 1; L <= 7; ++L) c.GF[L - 1][o] = v[2 + L];
+        c.T[o] = v[10];   // walls adiabatic until a first full radiation call
+        dnst_at(c, o);
+    }
 }
 template <typename R>
 __global__ void k_extr_wall(Ctx<R> c) {
@@ -424,7 +450,10 @@ __global__ void k_finish(const double* __restrict__ partials, double* scal, Fini
 // ---------------------------------------------------------------------------
 template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s) {
     k_extr_io<R><<<gridn(c.n_extr_io), kBlk, 0, s>>>(c);
-    if (c.n_ft_cols > 0) k_extr_ft<R><<<gridn(c.n_ft_cols), kBlk, 0, s>>>(c);
+    if (c.n_extr_ft > 0) {
+        k_extr_ft_gather<R><<<gridn(c.n_extr_ft), kBlk, 0, s>>>(c);
+        k_extr_ft_apply<R><<<gridn(c.n_extr_ft), kBlk, 0, s>>>(c);
+    }
     if (c.n_extr_wall > 0) k_extr_wall<R><<<gridn(c.n_extr_wall), kBlk, 0, s>>>(c);
 }
 template <typename R> void launch_extrv(const Ctx<R>& c, int mex, cudaStream_t s) {

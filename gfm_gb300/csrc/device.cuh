@@ -26,6 +26,7 @@ struct GeoT {
     int MP, NP, LP;
     int HX, HY, HZ, PX;        // half extents (MP/2+1 ...) and padded row pitch
     long long CB;              // elements per parity class
+    int PXH, CBH;              // colour-split copy of one class: row pitch, elements per half
     int MPM1, MPM2, NPM1, NPM2, LPM1, LPM2;
     int NJY1, NJY2, LKZ1, LKZ2;
     int NJY1V[4], NJY2V[4], LKZ1V[4], LKZ2V[4];

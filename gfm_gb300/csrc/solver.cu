@@ -370,6 +370,8 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
     g.HX = hg.MP / 2 + 1; g.HY = hg.NP / 2 + 1; g.HZ = hg.LP / 2 + 1;
     g.PX = ((g.HX + 15) / 16) * 16;
     g.CB = (long long)g.PX * g.HY * g.HZ;
+    g.PXH = ((g.HX + 1) / 2 + 15) / 16 * 16;
+    g.CBH = g.PXH * g.HY * g.HZ;
     g.MPM1 = hg.MP - 1; g.MPM2 = hg.MP - 2; g.NPM1 = hg.NP - 1; g.NPM2 = hg.NP - 2; g.LPM1 = hg.LP - 1; g.LPM2 = hg.LP - 2;
     g.NJY1 = 4; g.NJY2 = g.NPM2; g.LKZ1 = 4; g.LKZ2 = g.LPM2;
     g.NJY1V[1] = 4; g.NJY2V[1] = g.NPM2; g.NJY1V[2] = 5; g.NJY2V[2] = hg.NP - 3; g.NJY1V[3] = 4; g.NJY2V[3] = g.NPM2;
@@ -400,12 +402,22 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
     }
     for (int s = 0; s < 3; ++s)
         for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASs[s][q], CB))) return rc;
-    for (int e = 0; e < 8; ++e)
-        if ((rc = dalloc(h, &scr[e].xt2, NS)) || (rc = dalloc(h, &scr[e].xt3, NS)) || (rc = dalloc(h, &scr[e].pty, NS)) ||
-            (rc = dalloc(h, &scr[e].ptz, NS)) || (rc = dalloc(h, &scr[e].iay, NS)) || (rc = dalloc(h, &scr[e].iaz, NS)) ||
-            (rc = dalloc(h, &scr[e].bsx, NS)))
-            return rc;
+    for (int e = 0; e < 8; ++e) {
+        AdiScratch<R>& w = scr[e];
+        if (h->adi_mode == GFM_ADI_MARCH) {
+            if ((rc = dalloc(h, &w.xt2, NS)) || (rc = dalloc(h, &w.xt3, NS)) || (rc = dalloc(h, &w.pty, NS)) ||
+                (rc = dalloc(h, &w.ptz, NS)))
+                return rc;
+        } else {
+            const long long NH = 2LL * g.CBH;
+            R** arrs[] = {&w.xs, &w.x2, &w.x3, &w.sby, &w.sbz};
+            for (R** a : arrs) if ((rc = dalloc(h, a, NH))) return rc;
+            Quad<R>** quads[] = {&w.ya, &w.yb, &w.za, &w.zb};
+            for (Quad<R>** a : quads) if ((rc = dalloc(h, a, NH))) return rc;
+        }
+    }
     if ((rc = dalloc(h, &c.qconv, gr->b_cnt > 0 ? gr->b_cnt : 1))) return rc;
+    if ((rc = dalloc(h, &c.ft_buf, (long long)kFtVals * (c.n_extr_ft > 0 ? c.n_extr_ft : 1)))) return rc;
     return GFM_OK;
 }
 
@@ -459,7 +471,7 @@ void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>*
         double cells = (double)((sys[e].ie - sys[e].ib) / 2 + 1) * ((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);
         h->adi_cells_visits += cells * 2.0 * sys[e].nim;   // each sweep visits every plane twice
     }
-    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 1 + 16LL * nim;
+    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 3 + 16LL * nim;
 }
 
 template <typename R>
@@ -737,9 +749,15 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     g.HX = hg.MP / 2 + 1; g.HY = hg.NP / 2 + 1; g.HZ = hg.LP / 2 + 1;
     g.PX = ((g.HX + 15) / 16) * 16;
     g.CB = (long long)g.PX * g.HY * g.HZ;
+    g.PXH = ((g.HX + 1) / 2 + 15) / 16 * 16;
+    g.CBH = g.PXH * g.HY * g.HZ;
     h->CB = g.CB;
     h->NS = 8 * g.CB;
-    if (h->NS >= (1LL << 31)) { h->err = "grid too large for 32-bit field offsets"; return GFM_E_UNSUPPORTED; }
+    if (h->NS >= (1LL << 31) || 2LL * ((g.HX + 1) / 2 + 16) * g.HY * g.HZ >= (1LL << 31)) {
+        h->err = "grid too large for 32-bit field offsets";
+        return GFM_E_UNSUPPORTED;
+    }
+    if (g.HY > 256 || g.HZ > 256) { h->err = "line solver: more than 256 points on a y- or z-line"; return GFM_E_UNSUPPORTED; }
     {
         std::vector<int8_t> ibs((size_t)h->NS, 1);
         for (int K = 1; K <= hg.LP; ++K)

@@ -5,6 +5,8 @@
 
 namespace gfm {
 
+constexpr int kFtVals = 11;   // P, TMU, GAMA, GF(1..7), T
+
 // Boundary-cell record for EXTR (Extr.f90:31-250): indices and weights are
 // fixed by IBCELL and the grid, so they are computed once on the host.
 struct ExtrRec {
@@ -56,6 +58,7 @@ struct Ctx {
     int n_extr_io, n_extr_wall, n_extr_ft;
     const int* ft_col_start;               // fall-through wall cells grouped by (I,J) column
     int n_ft_cols;
+    R* ft_buf;                             // source values of the fall-through cells (kFtVals each)
     const ExtrvRec* extrv;
     int n_extrv[3];                        // records per direction, stored back to back
     const Patch* patch;
@@ -86,11 +89,20 @@ struct Sys {
     int ib, ie, jb, je, kb, ke, nim;
 };
 
-// Per-equation scratch of the line solver (class-sized device buffers)
+// Four values of one line row, loaded as one vector.
+template <typename R>
+struct __align__(4 * sizeof(R)) Quad { R x, y, z, w; };
+
+// Per-equation scratch of the line solver.
+//  march order: XT2, XT3, PT of y- and z-lines, indexed like the fields (pidx);
+//  red-black order: colour-split arrays (2*CBH elements each, see adi.cu): the
+//  unknown XS, the pass results X2/X3, the scaled x-neighbour right-hand sides
+//  of the y- and z-lines, and the factored rows of both line directions.
 template <typename R>
 struct AdiScratch {
     R *xt2, *xt3, *pty, *ptz;
-    R *iay, *iaz, *bsx;   // red-black form: inverse pivots of the factored lines, x-neighbour RHS
+    R *xs, *x2, *x3, *sby, *sbz;
+    Quad<R> *ya, *yb, *za, *zb;
 };
 
 // ---- launchers (defined in the kernel translation units) --------------------
