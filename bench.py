@@ -141,7 +141,8 @@ def load_traffic(prec: str):
 
 
 def cpu_baseline_oracle(steps: int = 1):
-    """The CPU oracle (FP64 restatement of the reference, 1 core) on the same case."""
+    """The CPU oracle (FP64 restatement of the reference, 1 core) on the same
+    case; returns its rate, its time and its fields after `steps` iterations."""
     from gfm_gb300 import Case, configs
     from oracle.pyoracle import Oracle
     case = Case(configs.large_furnace())
@@ -150,7 +151,43 @@ def cpu_baseline_oracle(steps: int = 1):
     t0 = time.perf_counter()
     o.gflow(steps)
     dt = time.perf_counter() - t0
-    return case.ncells * steps / dt, dt
+    fields = o.download()
+    o.close()
+    return case.ncells * steps / dt, dt, fields
+
+
+FIELD_ERRORS = (("u", "ug", 0), ("v", "ug", 1), ("w", "ug", 2), ("p", "p", None), ("T", "t", None),
+                ("k", "gf", 3), ("eps", "gf", 4))
+
+
+def field_errors(case, got, ref) -> dict:
+    """Max and L2 error of each reported field relative to the reference's max
+    and L2 norm, over the open positions (IBCELL <= 0)."""
+    import numpy as np
+    open_ = case.ibcell() <= 0
+    out = {}
+    for name, key, comp in FIELD_ERRORS:
+        a = got.arrays[key] if comp is None else got.arrays[key][comp]
+        b = ref.arrays[key] if comp is None else ref.arrays[key][comp]
+        a, b = a[open_], b[open_]
+        d = np.abs(a - b)
+        out[name] = {"max": float(d.max() / max(np.abs(b).max(), 1e-300)),
+                     "l2": float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))}
+    return out
+
+
+def time_to_residual(case, adi, prec, thresh: float, max_iter: int) -> dict:
+    """Iterations and device time from the fresh start until res_mass < thresh,
+    with the solver's own convergence test (BGCON = thresh)."""
+    from gfm_gb300 import GpuSolver
+    s = GpuSolver(case, adi_mode=adi, precision=prec, bgcon=thresh)
+    s.start()
+    s.reset_kernel_times()
+    st, nd = s.gflow(max_iter)
+    ms = s.kernel_times()["gflow_ms"]
+    s.close()
+    return {"threshold": thresh, "reached": bool(st["converged"]), "iterations": nd, "seconds": ms / 1e3,
+            "res_mass_last": st["res_mass"]}
 
 
 def _replica_worker(args):
@@ -293,14 +330,33 @@ def run_ours(args):
         s64.close()
 
     cpu = None
+    ferr = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            v, dt = cpu_baseline_oracle(1)
+            v, dt, fo = cpu_baseline_oracle(1)
             cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
                    "sample": f"1 outer iteration of the FP64 oracle (C++ restatement of GFLOW) on the same "
                              f"192x96x64 furnace after INITSV, {dt:.1f}s on one host core"}
+            # the GPU path from the same start, one iteration: error of every
+            # reported field, in the benchmarked plane order and in the
+            # reference's march order (which isolates the arithmetic)
+            ferr = {"after_iterations": 1, "reference": "FP64 oracle (march order)"}
+            for name, mode in ((args.adi, adi), ("march", abi.GFM_ADI_MARCH)):
+                if name in ferr:
+                    continue
+                s1 = GpuSolver(case, adi_mode=mode, precision=prec)
+                s1.start()
+                s1.gflow(1)
+                ferr[name] = field_errors(case, s1.download(), fo)
+                s1.close()
         except Exception as e:   # the baseline is reported, never required
             cpu = {"value": None, "unit": UNIT, "cores": 1, "kind": "port", "sample": f"failed: {e}"}
+
+    ttr = None
+    if rank == 0 and args.ttr:
+        ttr = {"mixed" if prec == abi.GFM_PREC_MIXED else "fp64": time_to_residual(case, adi, prec, args.ttr, args.ttr_max)}
+        if prec == abi.GFM_PREC_MIXED and not args.no_plain:
+            ttr["fp64"] = time_to_residual(case, adi, abi.GFM_PREC_FP64, args.ttr, args.ttr_max)
 
     if rank == 0:
         line = {
@@ -322,6 +378,8 @@ def run_ours(args):
                          "algorithmic_bytes": f"{BYTES_PER_CELL_VISIT} x {w} B per cell per plane visit",
                          "adi_launches": adi_launches, "adi_ms": adi_ms},
             "cpu_baseline": cpu,
+            "field_error": ferr,
+            "time_to_residual": ttr,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -344,6 +402,9 @@ def main():
     ap.add_argument("--adi", choices=["redblack", "march"], default="redblack")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--ttr", type=float, default=None,
+                    help="also measure the time from the fresh start to res_mass < TTR (mixed and FP64)")
+    ap.add_argument("--ttr-max", type=int, default=3000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

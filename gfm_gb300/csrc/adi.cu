@@ -472,6 +472,47 @@ __global__ void k_residual(GeoT<R> g, Sys<R> s, double* partials, int slot) {
 }
 
 // ---------------------------------------------------------------------------
+// Iterative refinement of a line solve (mixed precision, p' equation): the
+// right-hand side of the correction system, r = BS + sum AS*XT_nb - AP*XT,
+// evaluated in FP64 from the stored coefficients and the current XT, and the
+// update XT += DX on the solve range.  Rows the line solver copies unchanged
+// (blocked cells) get r = 0.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_refine_rhs(GeoT<R> g, Sys<R> s, R* rhs) {
+    const int ni = (s.ie - s.ib) / 2 + 1, nj = (s.je - s.jb) / 2 + 1, nk = (s.ke - s.kb) / 2 + 1;
+    const int n = ni * nj * nk;
+    const int sy = g.PX, sz = g.PX * g.HY;
+    const R* __restrict__ xt = s.xt;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = s.ib + 2 * (t % ni);
+        const int r = t / ni;
+        const int j = s.jb + 2 * (r % nj), k = s.kb + 2 * (r / nj);
+        const int o = (int)pidx(g, i, j, k);
+        double v = 0.0;
+        if (g.ib[o] < 1) {
+            v = (double)s.bs[o] + (double)s.as[0][o] * (double)xt[o - 1] + (double)s.as[1][o] * (double)xt[o + 1] +
+                (double)s.as[2][o] * (double)xt[o - sy] + (double)s.as[3][o] * (double)xt[o + sy] +
+                (double)s.as[4][o] * (double)xt[o - sz] + (double)s.as[5][o] * (double)xt[o + sz] -
+                (double)s.ap[o] * (double)xt[o];
+        }
+        rhs[o] = R(v);
+    }
+}
+template <typename R>
+__global__ void k_refine_add(GeoT<R> g, Sys<R> s, const R* __restrict__ dx) {
+    const int ni = (s.ie - s.ib) / 2 + 1, nj = (s.je - s.jb) / 2 + 1, nk = (s.ke - s.kb) / 2 + 1;
+    const int n = ni * nj * nk;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int i = s.ib + 2 * (t % ni);
+        const int r = t / ni;
+        const int j = s.jb + 2 * (r % nj), k = s.kb + 2 * (r / nj);
+        const int o = (int)pidx(g, i, j, k);
+        s.xt[o] = s.xt[o] + dx[o];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 template <typename R>
@@ -567,6 +608,22 @@ void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>*
     }
 }
 
+template <typename R>
+void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& s, R* rhs, cudaStream_t st) {
+    const long long n = (long long)((s.ie - s.ib) / 2 + 1) * ((s.je - s.jb) / 2 + 1) * ((s.ke - s.kb) / 2 + 1);
+    long long nb = (n + 255) / 256;
+    k_refine_rhs<R><<<(int)(nb < 1 ? 1 : (nb > 4096 ? 4096 : nb)), 256, 0, st>>>(g, s, rhs);
+}
+template <typename R>
+void launch_refine_add(const GeoT<R>& g, const Sys<R>& s, const R* dx, cudaStream_t st) {
+    const long long n = (long long)((s.ie - s.ib) / 2 + 1) * ((s.je - s.jb) / 2 + 1) * ((s.ke - s.kb) / 2 + 1);
+    long long nb = (n + 255) / 256;
+    k_refine_add<R><<<(int)(nb < 1 ? 1 : (nb > 4096 ? 4096 : nb)), 256, 0, st>>>(g, s, dx);
+}
+template void launch_refine_rhs<float>(const GeoT<float>&, const Sys<float>&, float*, cudaStream_t);
+template void launch_refine_rhs<double>(const GeoT<double>&, const Sys<double>&, double*, cudaStream_t);
+template void launch_refine_add<float>(const GeoT<float>&, const Sys<float>&, const float*, cudaStream_t);
+template void launch_refine_add<double>(const GeoT<double>&, const Sys<double>&, const double*, cudaStream_t);
 template void launch_residual<double>(const Ctx<double>&, const Sys<double>&, int, cudaStream_t);
 template void launch_residual<float>(const Ctx<float>&, const Sys<float>&, int, cudaStream_t);
 template void launch_adlbl3_scr<double>(const GeoT<double>&, const Sys<double>*, const AdiScratch<double>*, int, int, cudaStream_t);

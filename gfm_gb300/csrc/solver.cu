@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <type_traits>
 #include <cmath>
 #include <initializer_list>
 #include <cstdio>
@@ -392,7 +393,7 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
         if ((rc = dalloc(h, &c.GF[l], NS))) return rc;
     }
     for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASm[q], NS))) return rc;
-    R** cent[] = {&c.APc, &c.BSp, &c.BSq, &c.QA, &c.QE};
+    R** cent[] = {&c.APc, &c.BSp, &c.BSq, &c.QA, &c.QE, &c.DPc, &c.BSr};
     for (R** p : cent) if ((rc = dalloc(h, p, CB))) return rc;
     for (int q = 0; q < 6; ++q) if ((rc = dalloc(h, &c.ASc[q], CB))) return rc;
     for (int l = 0; l < 7; ++l) {
@@ -515,7 +516,24 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     R* asc[6];
     for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
     Sys<R> spc = sys_of<R>(c.FZ, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[4]);
-    adi_call(h, g, &spc, scr, 1, st);
+    if (std::is_same<R, float>::value && spc.nim >= 2) {
+        // Mixed precision: iterative refinement.  The first half of the sweeps
+        // runs on p' itself; the rest runs on the correction system A dp = r
+        // with r = b - A p' evaluated in FP64, from dp = 0 (zero on the line
+        // ends and on copied rows), and p' += dp.  For a stationary splitting
+        // iteration this is the same sequence of iterates in exact arithmetic.
+        const int nim = spc.nim, n1 = (nim + 1) / 2;
+        spc.nim = n1;
+        adi_call(h, g, &spc, scr, 1, st);
+        cudaMemsetAsync(c.DPc, 0, sizeof(R) * h->CB, st);
+        launch_refine_rhs(g, spc, c.BSr, st);
+        Sys<R> sd = sys_of<R>(c.DPc, c.APc, asc, c.BSr, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, nim - n1);
+        adi_call(h, g, &sd, scr, 1, st);
+        launch_refine_add(g, spc, c.DPc, st);
+        spc.nim = nim;
+    } else {
+        adi_call(h, g, &spc, scr, 1, st);
+    }
     launch_residual(c, spc, SL_PC_POST, st);
     launch_velcorr(c, st);
     // exit balance (EXTRV, FLX1D, FACTOR), INTPV

@@ -48,6 +48,7 @@ struct Ctx {
     R *FZ;
     R *APm, *ASm[6], *BSm, *SFPm;          // momentum, face classes
     R *APc, *ASc[6], *BSp, *BSq;           // pressure / p', centre class
+    R *DPc, *BSr;                          // p' refinement: correction and its right-hand side (mixed)
     R *APs[7], *BSs[7], *FZs[7], *SFPs[7]; // scalar equations L=1..7 at index L-1
     R *ASs[3][6];                          // coefficient sets shared by equal sigma
     int as_set[7];
@@ -128,6 +129,8 @@ template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
+template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
+template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);
 template <typename R> void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
                                              int mode, cudaStream_t s);
 // deterministic finish of block partials: op 0 sum, 1 max, 2 residual

@@ -126,7 +126,8 @@ class Case:
 class GpuSolver:
     """GB300 SIMPLER solver for one case; fields stay resident on the device."""
 
-    def __init__(self, case: Case, adi_mode: int | None = None, precision: int | None = None):
+    def __init__(self, case: Case, adi_mode: int | None = None, precision: int | None = None,
+                 bgcon: float | None = None):
         self.case = case
         self.lib = case.lib
         n = self.lib.gfm_gpu_device_count()
@@ -137,6 +138,8 @@ class GpuSolver:
             prm.adi_mode = adi_mode
         if precision is not None:
             prm.precision = precision
+        if bgcon is not None:
+            prm.bgcon = bgcon   # convergence threshold on res_mass (Sphase.f90:193)
         self.params = prm
         h = C.c_void_p()
         rc = self.lib.gfm_gpu_create(C.byref(case.grid), C.byref(prm), C.byref(h))

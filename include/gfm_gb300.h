@@ -52,7 +52,8 @@ extern "C" {
 /* arithmetic of the bulk stencil / line-solve work (gfm_params.precision) */
 #define GFM_PREC_FP64      0     /* plain FP64, the reference's arithmetic      */
 #define GFM_PREC_MIXED     1     /* FP32 stencil assembly, property updates and
-                                    line solves; FP64 global reductions          */
+                                    line solves; FP64 global reductions and an
+                                    FP64-residual refinement step on p'         */
 
 /* ---- grid: geometry, cell map, boundary patches, tables ------------------ */
 typedef struct gfm_grid {
