@@ -176,18 +176,25 @@ def field_errors(case, got, ref) -> dict:
     return out
 
 
-def time_to_residual(case, adi, prec, thresh: float, max_iter: int) -> dict:
+def time_to_residual(case, adi, prec, thresh: float, max_iter: int, lp=None) -> dict:
     """Iterations and device time from the fresh start until res_mass < thresh,
-    with the solver's own convergence test (BGCON = thresh)."""
+    with the solver's own convergence test (BGCON = thresh); with `lp`, every
+    p' solve starts from the learned guess."""
     from gfm_gb300 import GpuSolver
     s = GpuSolver(case, adi_mode=adi, precision=prec, bgcon=thresh)
     s.start()
+    if lp is not None:
+        s.set_lp(lp)
     s.reset_kernel_times()
     st, nd = s.gflow(max_iter)
     ms = s.kernel_times()["gflow_ms"]
     s.close()
-    return {"threshold": thresh, "reached": bool(st["converged"]), "iterations": nd, "seconds": ms / 1e3,
-            "res_mass_last": st["res_mass"]}
+    out = {"threshold": thresh, "reached": bool(st["converged"]), "iterations": nd, "seconds": ms / 1e3,
+           "ms_per_iteration": ms / max(nd, 1), "res_mass_last": st["res_mass"], "pcorr_resid_last": st["pcorr_resid"]}
+    if lp is not None:
+        out["lp_used_last"] = st["lp_used"]
+        out["lp_ratio_last"] = st["lp_ratio"]
+    return out
 
 
 def _replica_worker(args):
@@ -358,6 +365,21 @@ def run_ours(args):
         if prec == abi.GFM_PREC_MIXED and not args.no_plain:
             ttr["fp64"] = time_to_residual(case, adi, abi.GFM_PREC_FP64, args.ttr, args.ttr_max)
 
+    learned = None
+    if rank == 0 and args.learned:
+        # learned p' guess: trained here on seeded variants of the 48x24x16
+        # furnace, applied to this workload; time to the same residual
+        from gfm_gb300.lp import train_default
+        t0 = time.perf_counter()
+        log = []
+        lp = train_default((case.mp // 2 - 2, case.np // 2 - 2, case.lp // 2 - 2), log=log)
+        train_s = time.perf_counter() - t0
+        thr = args.ttr or 1e-3
+        learned = {"train_seconds": train_s, "training": log,
+                   "plain": time_to_residual(case, adi, prec, thr, args.ttr_max),
+                   "learned": time_to_residual(case, adi, prec, thr, args.ttr_max, lp=lp)}
+        lp.close()
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -380,6 +402,7 @@ def run_ours(args):
             "cpu_baseline": cpu,
             "field_error": ferr,
             "time_to_residual": ttr,
+            "learned_p_prime": learned,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -405,6 +428,8 @@ def main():
     ap.add_argument("--ttr", type=float, default=None,
                     help="also measure the time from the fresh start to res_mass < TTR (mixed and FP64)")
     ap.add_argument("--ttr-max", type=int, default=3000)
+    ap.add_argument("--learned", action="store_true",
+                    help="also train the learned p' guess and measure time-to-residual with it")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -100,6 +100,7 @@ class GfmIterStats(C.Structure):
         ("q_react", C.c_double), ("q_exhaust", C.c_double), ("q_conv_total", C.c_double),
         ("q_global_bal", C.c_double),
         ("tave", C.c_double), ("tmean_ex", C.c_double),
+        ("lp_used", C.c_int), ("lp_ratio", C.c_double),
     ]
 
     def as_dict(self) -> dict:
@@ -165,6 +166,17 @@ SIGNATURES = [
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),
     ("gfm_gpu_last_error", C.c_char_p, [C.c_void_p]),
     ("gfm_gpu_destroy", None, [C.c_void_p]),
+    ("gfm_lp_create", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.POINTER(C.c_void_p)]),
+    ("gfm_lp_destroy", None, [C.c_void_p]),
+    ("gfm_lp_num_params", C.c_int, []),
+    ("gfm_lp_get_params", C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    ("gfm_lp_set_params", C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    ("gfm_lp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    ("gfm_lp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
+                                    C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    ("gfm_lp_last_error", C.c_char_p, []),
+    ("gfm_gpu_pcorr_sample", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    ("gfm_gpu_set_lp", C.c_int, [C.c_void_p, C.c_void_p]),
     ("gfm_adlbl3_noalloc", C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.POINTER(C.c_void_p), C.c_void_p] + [C.c_int] * 7 + [C.c_void_p]),
 ]

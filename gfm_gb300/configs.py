@@ -125,6 +125,40 @@ def large_furnace(**kw) -> FurnaceCase:
     return FurnaceCase(name="furnace_192x96x64", nx=192, ny=96, nz=64, inlets=_burner_inlets(), **kw)
 
 
+def furnace_variant(seed: int, nx: int = 48, ny: int = 24, nz: int = 16, aspect: float | None = None,
+                    **kw) -> FurnaceCase:
+    """A seeded variant of the burner furnace: burner velocity uniform in
+    20-60 m/s and air temperature uniform in 1200-1700 K; with `aspect`, the
+    box length is aspect x 2.0 m.  Used for the learned p' guess's training
+    systems (variants of the 48x24x16 case) and for the batched runs."""
+    import random
+    rnd = random.Random(seed)
+    u = rnd.uniform(20.0, 60.0)
+    t_air = rnd.uniform(1200.0, 1700.0)
+    inl = _burner_inlets()
+    inl[0].u_ms = u
+    inl[1].t_k = inl[2].t_k = t_air
+    if aspect is not None:
+        kw["lx"] = aspect * 2.0
+    kw.setdefault("seed", 1000003 * (seed + 1))
+    return FurnaceCase(name=f"furnace_{nx}x{ny}x{nz}_v{seed}", nx=nx, ny=ny, nz=nz, inlets=inl, **kw)
+
+
+def batch_variants(n: int = 64, seed: int = 7) -> list:
+    """n furnace variants with grid, box aspect, burner velocity and air
+    temperature drawn from a seed: nx in 32..128, ny in 16..64, nz in 12..48
+    cells, aspect 1.5-3.0 (all extents even)."""
+    import random
+    rnd = random.Random(seed)
+    out = []
+    for i in range(n):
+        nx = 2 * rnd.randint(16, 64)
+        ny = 2 * rnd.randint(8, 32)
+        nz = 2 * rnd.randint(6, 24)
+        out.append(furnace_variant(seed * 7919 + i, nx, ny, nz, aspect=rnd.uniform(1.5, 3.0)))
+    return out
+
+
 def tiny_furnace(nx=12, ny=8, nz=6, **kw) -> FurnaceCase:
     """A few hundred cells: every cell can be checked against the oracle quickly."""
     inl = [

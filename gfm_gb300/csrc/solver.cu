@@ -6,6 +6,8 @@
 
 #include <array>
 #include <type_traits>
+
+#include <cuda_bf16.h>
 #include <cmath>
 #include <initializer_list>
 #include <cstdio>
@@ -17,6 +19,7 @@
 
 #include "../../include/gfm_gb300.h"
 #include "state.cuh"
+#include "lp.cuh"
 
 using namespace gfm;
 
@@ -77,6 +80,10 @@ struct gfm_handle {
     long long kernels_per_iter = 0;     // kernel nodes of the captured iteration
     long long adi_kernels_per_iter = 0;
     double adi_cells_visits = 0;        // cells x plane visits per iteration (all line solves)
+    // learned p' initial guess (not owned)
+    gfm::lp::Net* lp = nullptr;
+    void* lp_feats = nullptr;           // BF16 inputs, 16 channels per voxel
+    int lp_nx = 0, lp_ny = 0, lp_nz = 0;
 };
 
 namespace {
@@ -513,6 +520,12 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     launch_mom_finish(c, st);
     // pressure correction
     launch_pcorr_source(c, st);
+    if (h->lp) {
+        // learned start for p' (FZ on the centres is zero here)
+        launch_lp_features(c, h->lp_feats, h->lp_nx, h->lp_ny, h->lp_nz, st);
+        h->lp->forward(static_cast<const __nv_bfloat16*>(h->lp_feats), h->lp_nx, h->lp_ny, h->lp_nz, st);
+        launch_lp_guess(c, h->lp->OUT, c.FZ, h->lp_nx, h->lp_ny, h->lp_nz, st);
+    }
     R* asc[6];
     for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
     Sys<R> spc = sys_of<R>(c.FZ, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesg[4]);
@@ -697,6 +710,8 @@ void fill_stats(gfm_handle* h, gfm_iter_stats* s, int converged) {
     double tb = v[S_TAVE_DEN];
     s->tave = tb != 0.0 ? v[S_TAVE] * h->params.t0 / tb : 0.0;
     s->tmean_ex = v[S_TMEAN_EX];
+    s->lp_used = h->lp ? (int)v[S_LP_USED] : 0;
+    s->lp_ratio = h->lp ? v[S_LP_RATIO] : 0.0;
 }
 
 }  // namespace
@@ -1036,6 +1051,64 @@ extern "C" int gfm_gpu_adlbl3(gfm_handle* h, double* xt, const double* ap, const
         return GFM_E_ARG;
     return h->prec == GFM_PREC_FP64 ? adlbl3_user(h, h->cd, h->scr_d, xt, ap, as, bs, ib, ie, jb, je, kb, ke, nim)
                                     : adlbl3_user(h, h->cf, h->scr_f, xt, ap, as, bs, ib, ie, jb, je, kb, ke, nim);
+}
+
+namespace {
+template <typename R>
+int pcorr_sample(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, int nsweeps, void* feats, float* target) {
+    const GeoT<R>& g = c.g;
+    cudaStream_t st = h->stream;
+    const int nx = g.MP / 2 - 2, ny = g.NP / 2 - 2, nz = g.LP / 2 - 2;
+    launch_lp_features(c, feats, nx, ny, nz, st);
+    CK(cudaMemsetAsync(c.DPc, 0, sizeof(R) * h->CB, st));
+    R* asc[6];
+    for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
+    Sys<R> s = sys_of<R>(c.DPc, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, nsweeps);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st);
+    launch_lp_target(c, c.DPc, target, nx, ny, nz, st);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    return GFM_OK;
+}
+bool on_this_device(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    int dev = -1;
+    cudaGetDevice(&dev);
+    return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
+}
+}  // namespace
+
+extern "C" int gfm_gpu_pcorr_sample(gfm_handle* h, int nsweeps, void* feats, float* target, int* dims) {
+    if (!h || !feats || !target || nsweeps < 0) return GFM_E_ARG;
+    const HostGrid& g = h->hg;
+    const int nx = g.MP / 2 - 2, ny = g.NP / 2 - 2, nz = g.LP / 2 - 2;
+    if (dims) { dims[0] = nx; dims[1] = ny; dims[2] = nz; }
+    if (!on_this_device(feats) || !on_this_device(target)) { h->err = "pcorr_sample: buffers must be device memory"; return GFM_E_ARG; }
+    return h->prec == GFM_PREC_FP64 ? pcorr_sample(h, h->cd, h->scr_d, nsweeps, feats, target)
+                                    : pcorr_sample(h, h->cf, h->scr_f, nsweeps, feats, target);
+}
+
+extern "C" int gfm_gpu_set_lp(gfm_handle* h, gfm_lp* lp) {
+    if (!h) return GFM_E_ARG;
+    gfm::lp::Net* n = reinterpret_cast<gfm::lp::Net*>(lp);
+    const int nx = h->hg.MP / 2 - 2, ny = h->hg.NP / 2 - 2, nz = h->hg.LP / 2 - 2;
+    if (n) {
+        int rc = n->check_dims(nx, ny, nz);
+        if (rc != GFM_OK) { h->err = "set_lp: the network's grid is smaller than the p' solve range, or an extent is odd"; return rc; }
+        if (!h->lp_feats || (long long)h->lp_nx * h->lp_ny * h->lp_nz < (long long)nx * ny * nz) {
+            uint16_t* f = nullptr;
+            int r2 = dalloc(h, &f, (long long)nx * ny * nz * 16);
+            if (r2) return r2;
+            h->lp_feats = f;
+        }
+        h->lp_nx = nx; h->lp_ny = ny; h->lp_nz = nz;
+    }
+    h->lp = n;
+    // the captured iteration changes: capture again at the next gfm_gpu_gflow
+    if (h->graph_exec) { cudaGraphExecDestroy(h->graph_exec); h->graph_exec = nullptr; }
+    if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+    return GFM_OK;
 }
 
 extern "C" int gfm_gpu_kernel_times(gfm_handle* h, double* adi_ms, double* assemble_ms, double* other_ms, long long* launches) {

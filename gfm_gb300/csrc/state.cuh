@@ -35,7 +35,8 @@ enum Scal {
     S_RES_MASS = 0, S_RES_MASS_MAX, S_GFEX, S_GFIN0, S_GFIN, S_FACTOR, S_FADJ, S_G0, S_TMEAN_EX,
     S_Q_REACT, S_Q_EXHAUST, S_QCONV, S_TAVE, S_P_RESID_PRE, S_P_RESID, S_PCORR_RESID,
     S_U_RESID_PRE, S_U_RESID = S_U_RESID_PRE + 3, S_GF_RESID_PRE = S_U_RESID + 3, S_GF_RESID = S_GF_RESID_PRE + 10,
-    S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_RAD_ACTIVE, S_NUM
+    S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_RAD_ACTIVE,
+    S_LP_SCALE, S_LP_USED, S_LP_RATIO, S_LP_ALPHA, S_LP_TSCALE, S_NUM
 };
 
 template <typename R>
@@ -144,6 +145,12 @@ template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int 
                                            double F2, cudaStream_t s);
 
 void launch_count_nonfinite(const double* a, long long n, unsigned int* cnt, cudaStream_t s);
+
+// learned p' initial guess (lpsolve.cu): network inputs (BF16, 16 channels per
+// voxel of the p' solve range), guess + fallback into x, training target
+template <typename R> void launch_lp_features(const Ctx<R>& c, void* feats, int nx, int ny, int nz, cudaStream_t s);
+template <typename R> void launch_lp_guess(const Ctx<R>& c, const float* out16, R* x, int nx, int ny, int nz, cudaStream_t s);
+template <typename R> void launch_lp_target(const Ctx<R>& c, const R* x, float* tgt, int nx, int ny, int nz, cudaStream_t s);
 
 // layout conversion doubled <-> parity split (host-layout arrays on device)
 template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);

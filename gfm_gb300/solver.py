@@ -188,6 +188,11 @@ class GpuSolver:
                                             ib, ie, jb, je, kb, ke, nim))
         return x
 
+    def set_lp(self, lp) -> None:
+        """Start every p' solve from the network's guess (None: from zero)."""
+        self._check(self.lib.gfm_gpu_set_lp(self.h, lp.h if lp is not None else None))
+        self._lp = lp   # keep the network alive while the solver uses it
+
     def kernel_times(self) -> dict:
         a, b, c = C.c_double(), C.c_double(), C.c_double()
         n = C.c_longlong()

@@ -127,6 +127,8 @@ typedef struct gfm_iter_stats {
     double factor, gfin, gfex;
     double q_react, q_exhaust, q_conv_total, q_global_bal;
     double tave, tmean_ex;
+    int    lp_used;              /* learned p' guess kept (1) or replaced by 0 */
+    double lp_ratio;             /* |b - A x_guess| / |b| of that guess         */
 } gfm_iter_stats;
 
 /* ---- synthetic furnace specification (stands in for gd/sbc files) -------- */
@@ -171,6 +173,8 @@ typedef struct gfm_case {
 
 /* Opaque GPU solver handle. */
 typedef struct gfm_handle gfm_handle;
+/* Opaque learned p' initial-guess network. */
+typedef struct gfm_lp gfm_lp;
 
 /* ---- host side: synthetic case construction ------------------------------ */
 /* Builds grid, constants and the fresh-start state the reference reaches after
@@ -224,6 +228,45 @@ int  gfm_gpu_iteration_profile(gfm_handle *h, long long *kernels_per_iter,
 /* Last error text of this handle (never NULL). */
 const char *gfm_gpu_last_error(gfm_handle *h);
 void gfm_gpu_destroy(gfm_handle *h);
+
+/* ---- learned initial guess for the p' equation --------------------------- */
+/* No counterpart in the reference (which starts every p' solve from zero,
+ * Gslv3v.f90:157-161).  A 3-D convolutional encoder-decoder (BF16 tensor-core
+ * kernels, FP32 accumulation) maps the Jacobi-scaled right-hand side of the
+ * p' system on the voxel grid of its solve range (nx = MP/2-2, ny = NP/2-2,
+ * nz = LP/2-2, all even) to the shape of p' (unit RMS); in the solver the
+ * guess is that shape times the factor minimising the p' residual, and the
+ * line solver starts from it.
+ * Inputs are BF16 tensors of 16 channels per voxel, voxel (z*ny+y)*nx+x;
+ * targets and outputs are FP32, one value per voxel.  Device pointers; calls
+ * are queued on `stream` (NULL = legacy default stream). */
+int  gfm_lp_create(int nx, int ny, int nz, uint64_t seed, gfm_lp **out);
+void gfm_lp_destroy(gfm_lp *lp);
+int  gfm_lp_num_params(void);
+/* FP32 parameters / accumulated gradients to host (either may be NULL);
+ * setting the parameters resets the optimiser. */
+int  gfm_lp_get_params(gfm_lp *lp, float *params, float *grads);
+int  gfm_lp_set_params(gfm_lp *lp, const float *params);
+int  gfm_lp_forward(gfm_lp *lp, const void *feats, float *out,
+                    int nx, int ny, int nz, void *stream);
+/* One sample: forward, loss (mean squared error over open voxels, returned in
+ * *loss when not NULL, which waits for the stream), gradients; an Adam step
+ * with learning rate lr when update != 0. */
+int  gfm_lp_train_step(gfm_lp *lp, const void *feats, const float *target,
+                       int nx, int ny, int nz, float lr, int update,
+                       double *loss, void *stream);
+const char *gfm_lp_last_error(void);
+/* Training sample from the p' system of the handle's last iteration: inputs
+ * to `feats`, and to `target` the system's solution after `nsweeps` line-
+ * solver sweeps from zero, scaled to unit RMS over the open cells.  dims
+ * receives nx, ny, nz.  Synchronous. */
+int  gfm_gpu_pcorr_sample(gfm_handle *h, int nsweeps, void *feats,
+                          float *target, int *dims);
+/* Use the network's guess as the start of every p' solve (NULL: start from
+ * zero, as the reference).  The guess g is scaled by alpha minimising
+ * |b - alpha*A g| (FP64) and kept when that residual is below |b|, the
+ * residual of the zero start (gfm_iter_stats.lp_used, lp_ratio). */
+int  gfm_gpu_set_lp(gfm_handle *h, gfm_lp *lp);
 
 /* ---- line solve without any device allocation ---------------------------- */
 /* No counterpart in the reference: an addition for callers that cannot

@@ -25,7 +25,7 @@ def test_every_declared_symbol_is_exported():
 
 def test_struct_sizes_are_plausible():
     # ctypes mirrors must line up with the header's field order
-    assert C.sizeof(abi.GfmIterStats) == 4 * 2 + 8 * (2 + 3 + 6 + 20 + 3 + 4 + 2)
+    assert C.sizeof(abi.GfmIterStats) == 4 * 2 + 8 * (2 + 3 + 6 + 20 + 3 + 4 + 2) + 16
     assert abi.GfmParams.ntimesg.offset % 4 == 0
 
 
