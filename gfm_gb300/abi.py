@@ -157,6 +157,8 @@ SIGNATURES = [
     ("gfm_gpu_upload", C.c_int, [C.c_void_p, C.POINTER(GfmFields)]),
     ("gfm_gpu_initsv", C.c_int, [C.c_void_p]),
     ("gfm_gpu_gflow", C.c_int, [C.c_void_p, C.c_int, C.POINTER(GfmIterStats), C.POINTER(C.c_int)]),
+    ("gfm_gpu_gflow_batch", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.POINTER(GfmIterStats),
+                                      C.POINTER(C.c_int)]),
     ("gfm_gpu_download", C.c_int, [C.c_void_p, C.POINTER(GfmFields)]),
     ("gfm_gpu_adlbl3", C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(_dp), _dp,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),

@@ -950,55 +950,114 @@ int capture_iteration(gfm_handle* h) {
 }
 }  // namespace
 
-extern "C" int gfm_gpu_gflow(gfm_handle* h, int n_iter, gfm_iter_stats* out, int* n_done) {
-    if (!h || n_iter < 0) return GFM_E_ARG;
-    int done = 0, conv = 0;
-    if (h->use_graph && !h->graph_exec) {
-        int rc = capture_iteration(h);
+namespace {
+// One SPHASE pass split in two, so that several handles can have an
+// iteration in flight at once: iter_launch queues GFLOW and the read-back of
+// the statistics on the handle's stream; iter_finish waits for them and
+// applies the convergence test and the emission cadence (Sphase.f90:37-235).
+int iter_launch(gfm_handle* h) {
+    h->itr_gas += 1;
+    h->h_flags[0] = (double)h->itr_gas;
+    h->h_flags[1] = (double)h->rad_active;
+    if (h->use_graph) {
+        cudaError_t e = cudaGraphLaunch(h->graph_exec, h->stream);
+        if (e != cudaSuccess) { h->err = std::string("graph launch: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
+        h->launches += h->kernels_per_iter;
+    } else {
+        int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
         if (rc) return rc;
     }
-    cudaEventRecord(h->ev_g0, h->stream);
-    for (int it = 0; it < n_iter; ++it) {
-        h->itr_gas += 1;
-        h->h_flags[0] = (double)h->itr_gas;
-        h->h_flags[1] = (double)h->rad_active;
-        if (h->use_graph) {
-            cudaError_t e = cudaGraphLaunch(h->graph_exec, h->stream);
-            if (e != cudaSuccess) { h->err = std::string("graph launch: ") + cudaGetErrorString(e); return GFM_E_CUDA; }
-            h->launches += h->kernels_per_iter;
-        } else {
-            int rc = h->prec == GFM_PREC_FP64 ? gflow_once(h, h->cd, h->scr_d) : gflow_once(h, h->cf, h->scr_f);
-            if (rc) return rc;
-        }
-        double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
-        cudaError_t e = cudaMemcpyAsync(h->h_scal, scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, h->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
-        for (int q = 0; q + 1 < h->n_ev; q += 2) {
-            float ms = 0.f;
-            if (cudaEventElapsedTime(&ms, h->ev[q], h->ev[q + 1]) == cudaSuccess) h->adi_ms += ms;
-        }
-        ++done;
-        if (!std::isfinite(h->h_scal[S_RES_MASS])) { h->err = "res_mass is not finite"; if (n_done) *n_done = done; fill_stats(h, out, 0); return GFM_E_NAN; }
-        if (h->h_scal[S_RES_MASS] < h->params.bgcon) { conv = 1; break; }
-        if (h->params.rad_emission) {
-            h->cnt_qe += 1;
-            if (h->cnt_qe >= h->params.rad_qe_frequency && h->itr_gas > 50) {
-                if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
-                else launch_rad_emission(h->cf, h->stream);
-                h->rad_active = 1;
-                h->cnt_qe = 0;
-            }
+    double* scal = h->prec == GFM_PREC_FP64 ? h->cd.scal : h->cf.scal;
+    cudaError_t e = cudaMemcpyAsync(h->h_scal, scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    return GFM_OK;
+}
+// *conv = 1 when res_mass < BGCON
+int iter_finish(gfm_handle* h, int* conv) {
+    *conv = 0;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    for (int q = 0; q + 1 < h->n_ev; q += 2) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, h->ev[q], h->ev[q + 1]) == cudaSuccess) h->adi_ms += ms;
+    }
+    if (!std::isfinite(h->h_scal[S_RES_MASS])) { h->err = "res_mass is not finite"; return GFM_E_NAN; }
+    if (h->h_scal[S_RES_MASS] < h->params.bgcon) { *conv = 1; return GFM_OK; }
+    if (h->params.rad_emission) {
+        h->cnt_qe += 1;
+        if (h->cnt_qe >= h->params.rad_qe_frequency && h->itr_gas > 50) {
+            if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
+            else launch_rad_emission(h->cf, h->stream);
+            h->rad_active = 1;
+            h->cnt_qe = 0;
         }
     }
+    return GFM_OK;
+}
+int ensure_graph(gfm_handle* h) {
+    if (h->use_graph && !h->graph_exec) return capture_iteration(h);
+    return GFM_OK;
+}
+void close_timing(gfm_handle* h) {
     cudaEventRecord(h->ev_g1, h->stream);
     if (cudaEventSynchronize(h->ev_g1) == cudaSuccess) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, h->ev_g0, h->ev_g1) == cudaSuccess) h->asm_ms += ms;
     }
+}
+}  // namespace
+
+extern "C" int gfm_gpu_gflow(gfm_handle* h, int n_iter, gfm_iter_stats* out, int* n_done) {
+    if (!h || n_iter < 0) return GFM_E_ARG;
+    int done = 0, conv = 0;
+    int rc = ensure_graph(h);
+    if (rc) return rc;
+    cudaEventRecord(h->ev_g0, h->stream);
+    for (int it = 0; it < n_iter; ++it) {
+        if ((rc = iter_launch(h))) return rc;
+        rc = iter_finish(h, &conv);
+        ++done;
+        if (rc) { if (n_done) *n_done = done; fill_stats(h, out, 0); return rc; }
+        if (conv) break;
+    }
+    close_timing(h);
     fill_stats(h, out, conv);
     if (n_done) *n_done = done;
     return GFM_OK;
+}
+
+extern "C" int gfm_gpu_gflow_batch(gfm_handle* const* hs, int n, int n_iter, gfm_iter_stats* out, int* n_done) {
+    if (!hs || n <= 0 || n_iter < 0) return GFM_E_ARG;
+    for (int i = 0; i < n; ++i) if (!hs[i]) return GFM_E_ARG;
+    std::vector<int> done(n, 0), conv(n, 0);
+    for (int i = 0; i < n; ++i) {
+        int rc = ensure_graph(hs[i]);
+        if (rc) return rc;
+        cudaEventRecord(hs[i]->ev_g0, hs[i]->stream);
+    }
+    int status = GFM_OK;
+    for (int it = 0; it < n_iter && status == GFM_OK; ++it) {
+        int active = 0;
+        for (int i = 0; i < n; ++i) {
+            if (conv[i]) continue;
+            int rc = iter_launch(hs[i]);
+            if (rc) { status = rc; break; }
+            ++active;
+        }
+        if (status != GFM_OK || active == 0) break;
+        for (int i = 0; i < n; ++i) {
+            if (conv[i]) continue;
+            int rc = iter_finish(hs[i], &conv[i]);
+            ++done[i];
+            if (rc) { status = rc; break; }
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        close_timing(hs[i]);
+        if (out) fill_stats(hs[i], out + i, conv[i]);
+        if (n_done) n_done[i] = done[i];
+    }
+    return status;
 }
 
 extern "C" int gfm_gpu_download(gfm_handle* h, gfm_fields* f) {

@@ -123,6 +123,23 @@ class Case:
             pass
 
 
+def gflow_batch(solvers: list, n_iter: int) -> tuple[list, list]:
+    """n_iter iterations of several independent solvers with their GPU work
+    overlapped (gfm_gpu_gflow_batch); returns each solver's stats and count."""
+    if not solvers:
+        return [], []
+    lib = solvers[0].lib
+    n = len(solvers)
+    hs = (C.c_void_p * n)(*[s.h for s in solvers])
+    st = (abi.GfmIterStats * n)()
+    nd = (C.c_int * n)()
+    rc = lib.gfm_gpu_gflow_batch(hs, n, n_iter, st, nd)
+    if rc != abi.GFM_OK:
+        msgs = "; ".join(lib.gfm_gpu_last_error(s.h).decode() for s in solvers if lib.gfm_gpu_last_error(s.h))
+        raise GfmError(rc, msgs)
+    return [st[i].as_dict() for i in range(n)], [nd[i] for i in range(n)]
+
+
 class GpuSolver:
     """GB300 SIMPLER solver for one case; fields stay resident on the device."""
 

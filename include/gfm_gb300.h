@@ -201,6 +201,13 @@ int  gfm_gpu_initsv(gfm_handle *h);
  * res_mass < BGCON.  `out` (may be NULL) receives the last iteration's stats;
  * `n_done` (may be NULL) the number of iterations run. */
 int  gfm_gpu_gflow(gfm_handle *h, int n_iter, gfm_iter_stats *out, int *n_done);
+/* The same for n independent handles (furnace variants) at once: every
+ * iteration is queued on all handles' streams before any is waited for, so
+ * their kernels overlap on the GPU.  A handle stops at its own convergence;
+ * out[i] / n_done[i] (either may be NULL) receive each handle's result.  No
+ * counterpart in the reference, which runs one furnace per process. */
+int  gfm_gpu_gflow_batch(gfm_handle *const *hs, int n, int n_iter,
+                         gfm_iter_stats *out, int *n_done);
 /* Device -> host fields (reference layout). */
 int  gfm_gpu_download(gfm_handle *h, gfm_fields *f);
 /* One ADLBL3 call on a user system (Adlbl3.f90:10-97): xt, ap, as (6 arrays
