@@ -20,12 +20,12 @@ struct Range {
         long long ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / 2 + 1, nk = (k1 - k0) / 2 + 1;
         return (i1 < i0 || j1 < j0 || k1 < k0) ? 0 : ni * nj * nk;
     }
-    __device__ void at(long long t, int& I, int& J, int& K) const {
-        int ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / 2 + 1;
-        I = i0 + 2 * (int)(t % ni);
-        long long r = t / ni;
-        J = j0 + 2 * (int)(r % nj);
-        K = k0 + 2 * (int)(r / nj);
+    __device__ void at(int t, int& I, int& J, int& K) const {
+        const int ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / 2 + 1;
+        I = i0 + 2 * (t % ni);
+        const int r = t / ni;
+        J = j0 + 2 * (r % nj);
+        K = k0 + 2 * (r / nj);
     }
 };
 
@@ -166,11 +166,11 @@ __global__ void k_wallfn(Ctx<R> c, const int* __restrict__ wl, int n) {
                 A(c.THETA, I, J, K) = A(c.THETA, In, Jn, Kn) * x01 + A(c.THETA, Ifar, Jfar, Kfar) * x02;
                 theta_done = true;
             }
-            R cc = R(pow((double)A(c.T, In, Jn, Kn) / c.p.trdg, c.p.amu));
+            R cc = pow(A(c.T, In, Jn, Kn) / R(c.p.trdg), R(c.p.amu));
             R blvm = rt20 * A(c.DNST, In, Jn, Kn) * sqrt(A(c.GF[kK], In, Jn, Kn)) / cc;
             R vgam = cc / R(c.p.reyg2);
             R blv = blvm * dist;
-            R gama0 = vgam * R(tgamf((double)blv));
+            R gama0 = vgam * tgamf<R>(blv);
             gmax = rmax(gama0, gmax);
         }
         A(c.GAMA, I, J, K) = gmax;
@@ -182,10 +182,10 @@ __global__ void k_wallfn(Ctx<R> c, const int* __restrict__ wl, int n) {
 template <typename R>
 __global__ void k_copy_faces(Ctx<R> c) {
     const GeoT<R>& g = c.g;
-    long long n = g.CB;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < 3 * n; t += (long long)gridDim.x * blockDim.x) {
-        int iu = (int)(t / n);
-        long long off = (1LL << iu) * g.CB + (t % n);   // class 1 (x), 2 (y), 4 (z)
+    const int n = (int)g.CB;
+    GFM_FOR(t, 3 * n) {
+        const int iu = t / n;
+        const int off = (1 << iu) * n + (t - iu * n);   // class 1 (x), 2 (y), 4 (z)
         c.FZ[off] = c.UG[iu][off];
     }
 }
@@ -199,7 +199,7 @@ __global__ void k_mom_assemble(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     const R zero = R(0);
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         const long long o = pidx(g, I, J, K);
@@ -366,7 +366,7 @@ __global__ void k_p_assemble(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     const R zero = R(0);
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         const long long o = pidx(g, I, J, K);
@@ -416,7 +416,7 @@ template <typename R>
 __global__ void k_bound_p(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -433,7 +433,7 @@ template <typename R, int IU1>
 __global__ void k_mom_prep(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -461,7 +461,7 @@ template <typename R>
 __global__ void k_mom_finish(Ctx<R> c, Range rg, int iu) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -481,7 +481,7 @@ __global__ void k_pcorr_source(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
     double rsum = 0.0, rmx = 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -514,7 +514,7 @@ __global__ void k_pcorr_source(Ctx<R> c, Range rg) {
 
 template <typename R>
 __global__ void k_zero_centres(Ctx<R> c) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < c.g.CB; t += (long long)gridDim.x * blockDim.x)
+    GFM_FOR(t, c.g.CB)
         c.FZ[t] = R(0);   // class 0 = cell centres
 }
 
@@ -523,7 +523,7 @@ template <typename R, int IU1>
 __global__ void k_velcorr(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -547,7 +547,7 @@ __global__ void k_fuel_source(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
     const R zero = R(0);
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -638,7 +638,7 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
     double qreact = 0.0;
     const int itr_gas = (int)c.scal[S_ITR_GAS];
     const bool rad_active = c.scal[S_RAD_ACTIVE] > 0.0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         const long long o = pidx(g, I, J, K);
@@ -775,7 +775,7 @@ __global__ void k_scalar_finish(Ctx<R> c, Range rg, int L) {
     R* fz = c.FZs[L - 1];
     R* gf = c.GF[L - 1];
     long long n = rg.count();
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -792,7 +792,7 @@ __global__ void k_scalar_finish(Ctx<R> c, Range rg, int L) {
 // FZ(L) <- GF(L) on all centres before the solve (Gslv3g.f90:51-55)
 template <typename R>
 __global__ void k_copy_centres(const R* __restrict__ src, R* __restrict__ dst, long long n) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) dst[t] = src[t];
+    GFM_FOR(t, n) dst[t] = src[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -816,7 +816,7 @@ __global__ void k_props(Ctx<R> c, Range rg) {
     const R G0 = R(c.scal[S_G0]);
     const R t0 = R(c.p.t0), h0 = R(c.p.h_0), t_mx = R(c.p.t_mx), t_mn = R(c.p.t_mn);
     const R p_mx = R(c.p.p_mx), p_mn = R(c.p.p_mn), wt0 = R(c.p.wt0);
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);
@@ -846,7 +846,7 @@ __global__ void k_tave(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     long long n = rg.count();
     double a = 0, b = 0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, n) {
         int I, J, K;
         rg.at(t, I, J, K);
         long long o = pidx(g, I, J, K);

@@ -239,13 +239,13 @@ __global__ void k_intpv(Ctx<R> c, int IU, int stage, int m0, int m1, int mstep, 
     if (m1 < m0 || n1 < n0 || l1 < l0) return;
     const long long tot = (long long)nm * nn * nl;
     R* u = c.UG[IU - 1];
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
+    GFM_FOR(t, tot) {
         // fastest-varying index is the one mapping to I
-        int a = (int)(t % nm), b = (int)((t / nm) % nn), d = (int)(t / ((long long)nm * nn));
+        int a = t % nm, b = (t / nm) % nn, d = t / (nm * nn);
         int M, N, L;
         if (IU == 1) { M = m0 + mstep * a; N = n0 + nstep * b; L = l0 + lstep * d; }
-        else if (IU == 2) { L = l0 + lstep * (t % nl); long long r = t / nl; M = m0 + mstep * (int)(r % nm); N = n0 + nstep * (int)(r / nm); }
-        else { N = n0 + nstep * (int)(t % nn); long long r = t / nn; L = l0 + lstep * (int)(r % nl); M = m0 + mstep * (int)(r / nl); }
+        else if (IU == 2) { L = l0 + lstep * (t % nl); int r = t / nl; M = m0 + mstep * (r % nm); N = n0 + nstep * (r / nm); }
+        else { N = n0 + nstep * (t % nn); int r = t / nn; L = l0 + lstep * (r % nl); M = m0 + mstep * (r / nl); }
         int I, J, K;
         if (IU == 1) { I = M; J = N; K = L; } else if (IU == 2) { J = M; K = N; I = L; } else { K = M; I = N; J = L; }
         int b0 = IBC(g, I, J, K);
@@ -282,10 +282,10 @@ __global__ void k_intp(Ctx<R> c, int stage) {
     else { i0 = 3; i1 = g.MPM1; j0 = 2; j1 = g.NP; js = 1; k0 = 2; k1 = g.LP; ks = 1; }
     const int ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / js + 1, nk = (k1 - k0) / ks + 1;
     const long long tot = (long long)ni * nj * nk;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
-        int I = i0 + 2 * (int)(t % ni);
-        long long r = t / ni;
-        int J = j0 + js * (int)(r % nj), K = k0 + ks * (int)(r / nj);
+    GFM_FOR(t, tot) {
+        int I = i0 + 2 * (t % ni);
+        int r = t / ni;
+        int J = j0 + js * (r % nj), K = k0 + ks * (r / nj);
         const long long o = pidx(g, I, J, K);
         int mode = c.intp_mode[o];
         if (mode == 0) continue;
@@ -332,10 +332,10 @@ __global__ void k_rad_emission(Ctx<R> c) {
     const int hx = g.HX, hy = g.HY, hz = g.HZ;
     const long long tot = (long long)hx * hy * hz;
     const double sgn = c.p.sig * c.p.ri * c.p.ri;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < tot; t += (long long)gridDim.x * blockDim.x) {
-        int ia = (int)(t % hx);
-        long long r = t / hx;
-        int ja = (int)(r % hy), ka = (int)(r / hy);
+    GFM_FOR(t, tot) {
+        int ia = t % hx;
+        int r = t / hx;
+        int ja = r % hy, ka = r / hy;
         int I = 2 * ia, J = 2 * ja, K = 2 * ka;
         if (I < 2 || J < 2 || K < 2) continue;
         const long long o = pidx(g, I, J, K);

@@ -36,11 +36,17 @@ struct GeoT {
 };
 using Geo = GeoT<double>;
 
+// Offsets are formed in 32-bit arithmetic: a field holds fewer than 2^31
+// elements (checked when a handle is created).
 template <typename R>
 __host__ __device__ __forceinline__ long long pidx(const GeoT<R>& g, int I, int J, int K) {
     int c = (I & 1) | ((J & 1) << 1) | ((K & 1) << 2);
-    return (long long)c * g.CB + ((long long)(K >> 1) * g.HY + (J >> 1)) * g.PX + (I >> 1);
+    return (long long)(c * (int)g.CB + ((K >> 1) * g.HY + (J >> 1)) * g.PX + (I >> 1));
 }
+
+// grid-stride loop over [0, n) in 32-bit arithmetic (n < 2^31)
+#define GFM_FOR(t, n) \
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x, t##_end = (int)(n); t < t##_end; t += gridDim.x * blockDim.x)
 template <typename R>
 __device__ __forceinline__ int IBC(const GeoT<R>& g, int I, int J, int K) { return g.ib[pidx(g, I, J, K)]; }
 

@@ -221,10 +221,11 @@ GFM_HD R da(R d, R f) {
 }
 
 // Log-law wall factor TGAMF (Gflow.f90:417-426).
-GFM_HD double tgamf(double b) {
-    if (b < 11.5) return 1.0;
-    double g0 = b / (log(9 * b) * 2.5);
-    return g0 > 1.0 ? g0 : 1.0;
+template <typename R>
+GFM_HD R tgamf(R b) {
+    if (b < R(11.5)) return R(1);
+    R g0 = b / (log(R(9) * b) * R(2.5));
+    return g0 > R(1) ? g0 : R(1);
 }
 
 // Gray-band emissivity EMF (Rad_fun.f90:97-115).
