@@ -280,7 +280,10 @@ __global__ void k_rbs_factor(GeoT<R> g, RbBatch<R> b) {
 }
 
 // at most M elements per segment, held in registers; S <= 32 segments per line
-template <typename R> struct RbSeg { static constexpr int M = 8; };
+#ifndef GFM_RB_M
+#define GFM_RB_M 8
+#endif
+template <typename R> struct RbSeg { static constexpr int M = GFM_RB_M; };
 
 // One pass of all y- and z-lines of the planes of one colour.  Block = S warps
 // x 32 lanes; lane = one line (32 consecutive line slots), warp = segment.
@@ -395,7 +398,10 @@ __global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, in
 // XT = (XT2 + XT3)/2 on the planes of one colour (split copy).  Grid x runs
 // over the planes of the colour (unit stride); each thread row handles
 // kAvgRows (J,K) rows, kAvgRows*8 rows per block, loads issued together.
-constexpr int kAvgRows = 8;
+#ifndef GFM_AVG_ROWS
+#define GFM_AVG_ROWS 8
+#endif
+constexpr int kAvgRows = GFM_AVG_ROWS;
 template <typename R>
 __global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
     const Sys<R>& s = b.sys[blockIdx.y];
@@ -527,10 +533,13 @@ void launch_residual(const Ctx<R>& c, const Sys<R>& s, int slot, cudaStream_t st
 
 // Segments per line: the smallest power of two that keeps a segment within
 // the M registers of one thread (lines of up to 32*M points, checked at create).
+#ifndef GFM_RB_MIN_SEGMENTS
+#define GFM_RB_MIN_SEGMENTS 1
+#endif
 template <typename R>
 int rb_segments(int n) {
     int S = 1;
-    while (S < 32 && S * RbSeg<R>::M < n) S *= 2;
+    while (S < 32 && (S * RbSeg<R>::M < n || S < GFM_RB_MIN_SEGMENTS)) S *= 2;
     return S;
 }
 template <typename R, bool FIRST>

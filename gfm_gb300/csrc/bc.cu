@@ -428,9 +428,10 @@ __global__ void k_cells_from_split(GeoT<R> g, const R* __restrict__ src, double*
 // ---------------------------------------------------------------------------
 // deterministic finish of block partials (FinishSpec in state.cuh)
 // ---------------------------------------------------------------------------
+// one block per item; each block adds its 1024 partials in a fixed order
 __global__ void k_finish(const double* __restrict__ partials, double* scal, FinishSpec f, double ncells) {
     __shared__ double sh[32];
-    for (int q = 0; q < f.n; ++q) {
+    for (int q = blockIdx.x; q < f.n; q += gridDim.x) {
         const double* p = partials + (long long)f.slot[q] * kRedBlocks;
         double v = f.op[q] == 1 ? -1.0e308 : 0.0;
         for (int b = threadIdx.x; b < kRedBlocks; b += blockDim.x) v = f.op[q] == 1 ? (p[b] > v ? p[b] : v) : v + p[b];
@@ -494,7 +495,7 @@ template <typename R> void launch_factor(const Ctx<R>& c, cudaStream_t s) {
     k_factor<<<1, 32, 0, s>>>(c.scal, c.p.gmfr, c.p.t0, c.p.f_mx, c.p.f_mn);
 }
 void launch_finish(const double* partials, double* scal, const FinishSpec& f, double ncells, cudaStream_t s) {
-    k_finish<<<1, 256, 0, s>>>(partials, scal, f, ncells);
+    k_finish<<<f.n > 0 ? f.n : 1, 256, 0, s>>>(partials, scal, f, ncells);
 }
 template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int K1, int I2, int J2, int K2, double F1, double F2,
                                            cudaStream_t s) {

@@ -69,78 +69,91 @@ struct Grid3 {
 
 // ---- convolution (forward and input gradient) ---------------------------------
 // out[v][co] = bias[co] + sum_t sum_ci in[v + d_t][ci] * W[t][co][ci]
-// One warp computes 16 consecutive voxels x all COUT channels; the 27*COUT*CIN
-// weights of the layer sit in shared memory.  Rows of the A fragment are
-// voxels, columns input channels; B columns are output channels.
+// A block computes a 16 x 4 x 2 voxel tile: the input tile with a one-voxel
+// halo (18 x 6 x 4 voxels) and the layer's 27*COUT*CIN weights are staged in
+// shared memory once, then warp w computes the 16 voxels of row (w%4, w/4)
+// for every tap from there.  The staged channel stride is CIN+8, which keeps
+// the eight voxel rows of an A fragment on distinct banks.  Rows of the A
+// fragment are voxels, columns input channels; B columns are output channels.
+constexpr int kTX = 16, kTY = 4, kTZ = 2;
+// one block per tile: with a block staging its halo while others compute,
+// this measured faster than resident blocks walking the tiles
+constexpr long long kConvBlocks = 1LL << 30;
+constexpr int kHX = kTX + 2, kHY = kTY + 2, kHZ = kTZ + 2, kHalo = kHX * kHY * kHZ;
+template <int CIN, int COUT>
+constexpr size_t conv_smem() { return (size_t)(27 * COUT * CIN + kHalo * (CIN + 8)) * sizeof(bf16); }
+
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(256) k_conv(Grid3 gd, const bf16* __restrict__ in, int in_cs, int in_co,
                                              const bf16* __restrict__ w, const float* __restrict__ bias,
                                              bf16* __restrict__ out, float* __restrict__ out_f, int out_cs, int out_co,
                                              int relu) {
+    constexpr int CP = CIN + 8;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     bf16* sw = reinterpret_cast<bf16*>(smem_raw);
-    constexpr int NW = 27 * COUT * CIN;
-    for (int i = threadIdx.x; i < NW; i += blockDim.x) sw[i] = w[i];
-    __syncthreads();
+    bf16* sx = sw + 27 * COUT * CIN;
+    {   // the layer's weights, once per block
+        const uint32_t* w32 = reinterpret_cast<const uint32_t*>(w);
+        uint32_t* sw32 = reinterpret_cast<uint32_t*>(sw);
+        for (int i = threadIdx.x; i < 27 * COUT * CIN / 2; i += blockDim.x) sw32[i] = w32[i];
+    }
+    const int tx_n = (gd.nx + kTX - 1) / kTX, ty_n = (gd.ny + kTY - 1) / kTY, tz_n = (gd.nz + kTZ - 1) / kTZ;
+    const int ntiles = tx_n * ty_n * tz_n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int g = lane >> 2, tq = lane & 3;
-    const int nv = gd.nvox();
-    const int v0 = (blockIdx.x * (blockDim.x >> 5) + warp) * 16;
-    if (v0 >= nv) return;
-    // the two voxels of this thread's A rows
-    int vx[2], vy[2], vz[2];
-    bool vin[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int v = v0 + g + 8 * h;
-        vin[h] = v < nv;
-        const int vv = vin[h] ? v : 0;
-        vx[h] = vv % gd.nx;
-        vy[h] = (vv / gd.nx) % gd.ny;
-        vz[h] = vv / (gd.nx * gd.ny);
-    }
-    float acc[COUT / 8][4];
-#pragma unroll
-    for (int n = 0; n < COUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
-    for (int t = 0; t < 27; ++t) {
-        const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
-        const bf16* src[2];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int x = vx[h] + dx, y = vy[h] + dy, z = vz[h] + dz;
-            const bool ok = vin[h] && x >= 0 && x < gd.nx && y >= 0 && y < gd.ny && z >= 0 && z < gd.nz;
-            src[h] = ok ? in + (size_t)((z * gd.ny + y) * gd.nx + x) * in_cs + in_co : nullptr;
+    const int ty = warp & 3, tz = warp >> 2;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int x0 = (tile % tx_n) * kTX, y0 = ((tile / tx_n) % ty_n) * kTY, z0 = (tile / (tx_n * ty_n)) * kTZ;
+        __syncthreads();   // the previous tile's reads of sx are done
+        // halo tile, 32-bit words of channel pairs, zero outside the grid
+        for (int i = threadIdx.x; i < kHalo * (CIN / 2); i += blockDim.x) {
+            const int h = i / (CIN / 2), k = i % (CIN / 2);
+            const int hx = h % kHX, hy = (h / kHX) % kHY, hz = h / (kHX * kHY);
+            const int x = x0 - 1 + hx, y = y0 - 1 + hy, z = z0 - 1 + hz;
+            uint32_t v = 0u;
+            if (x >= 0 && x < gd.nx && y >= 0 && y < gd.ny && z >= 0 && z < gd.nz)
+                v = ld_pair(in + (size_t)((z * gd.ny + y) * gd.nx + x) * in_cs + in_co + 2 * k);
+            *reinterpret_cast<uint32_t*>(sx + (size_t)h * CP + 2 * k) = v;
         }
+        __syncthreads();
+        float acc[COUT / 8][4];
 #pragma unroll
-        for (int kc = 0; kc < CIN / 16; ++kc) {
-            uint32_t a[4];
-            const int c0 = kc * 16 + 2 * tq;
-            a[0] = src[0] ? ld_pair(src[0] + c0) : 0u;
-            a[1] = src[1] ? ld_pair(src[1] + c0) : 0u;
-            a[2] = src[0] ? ld_pair(src[0] + c0 + 8) : 0u;
-            a[3] = src[1] ? ld_pair(src[1] + c0 + 8) : 0u;
+        for (int n = 0; n < COUT / 8; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.f;
+        for (int t = 0; t < 27; ++t) {
+            const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+            const int hrow = ((tz + dz + 1) * kHY + (ty + dy + 1)) * kHX + dx + 1;
+            const bf16* r0 = sx + (size_t)(hrow + g) * CP;
+            const bf16* r1 = sx + (size_t)(hrow + g + 8) * CP;
 #pragma unroll
-            for (int n = 0; n < COUT / 8; ++n) {
-                const bf16* wr = sw + ((size_t)t * COUT + n * 8 + g) * CIN + c0;
-                uint32_t b[2] = {ld_pair(wr), ld_pair(wr + 8)};
-                mma16816(acc[n], a, b);
+            for (int kc = 0; kc < CIN / 16; ++kc) {
+                const int c0 = kc * 16 + 2 * tq;
+                uint32_t a[4] = {ld_pair(r0 + c0), ld_pair(r1 + c0), ld_pair(r0 + c0 + 8), ld_pair(r1 + c0 + 8)};
+#pragma unroll
+                for (int n = 0; n < COUT / 8; ++n) {
+                    const bf16* wr = sw + ((size_t)t * COUT + n * 8 + g) * CIN + c0;
+                    uint32_t b[2] = {ld_pair(wr), ld_pair(wr + 8)};
+                    mma16816(acc[n], a, b);
+                }
             }
         }
-    }
-    // epilogue: bias, relu, store (rows g and g+8, columns 2tq, 2tq+1 of each n-tile)
+        // epilogue: bias, relu, store (rows g and g+8, columns 2tq, 2tq+1 of each n-tile)
+        const int y = y0 + ty, z = z0 + tz;
+        if (y >= gd.ny || z >= gd.nz) continue;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int v = v0 + g + 8 * h;
-        if (v >= nv) continue;
+        for (int h = 0; h < 2; ++h) {
+            const int x = x0 + g + 8 * h;
+            if (x >= gd.nx) continue;
+            const int v = (z * gd.ny + y) * gd.nx + x;
 #pragma unroll
-        for (int n = 0; n < COUT / 8; ++n) {
-            const int co = n * 8 + 2 * tq;
-            float r0 = acc[n][2 * h], r1 = acc[n][2 * h + 1];
-            if (bias) { r0 += bias[co]; r1 += bias[co + 1]; }
-            if (relu) { r0 = fmaxf(r0, 0.f); r1 = fmaxf(r1, 0.f); }
-            const size_t o = (size_t)v * out_cs + out_co + co;
-            if (out_f) { out_f[o] = r0; out_f[o + 1] = r1; }
-            else *reinterpret_cast<uint32_t*>(out + o) = pack2(__float2bfloat16_rn(r0), __float2bfloat16_rn(r1));
+            for (int n = 0; n < COUT / 8; ++n) {
+                const int co = n * 8 + 2 * tq;
+                float q0 = acc[n][2 * h], q1 = acc[n][2 * h + 1];
+                if (bias) { q0 += bias[co]; q1 += bias[co + 1]; }
+                if (relu) { q0 = fmaxf(q0, 0.f); q1 = fmaxf(q1, 0.f); }
+                const size_t o = (size_t)v * out_cs + out_co + co;
+                if (out_f) { out_f[o] = q0; out_f[o + 1] = q1; }
+                else *reinterpret_cast<uint32_t*>(out + o) = pack2(__float2bfloat16_rn(q0), __float2bfloat16_rn(q1));
+            }
         }
     }
 }
@@ -270,13 +283,16 @@ __global__ void k_pool_bwd(Grid3 fine, const bf16* __restrict__ dskip, int ds_cs
         din[(size_t)v * c + ch] = __float2bfloat16_rn(s);
     }
 }
+// one thread per fine voxel, channels copied 8 at a time (16-byte vectors:
+// c, out_cs and out_co are multiples of 8)
 __global__ void k_up(Grid3 fine, const bf16* __restrict__ in, bf16* __restrict__ out, int out_cs, int out_co, int c) {
-    const int n = fine.nvox() * c;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int ch = i % c, v = i / c;
+    const int n = fine.nvox();
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         const int x = v % fine.nx, y = (v / fine.nx) % fine.ny, z = v / (fine.nx * fine.ny);
         const int vc = ((z / 2) * (fine.ny / 2) + y / 2) * (fine.nx / 2) + x / 2;
-        out[(size_t)v * out_cs + out_co + ch] = in[(size_t)vc * c + ch];
+        const uint4* src = reinterpret_cast<const uint4*>(in + (size_t)vc * c);
+        uint4* dst = reinterpret_cast<uint4*>(out + (size_t)v * out_cs + out_co);
+        for (int q = 0; q < c / 8; ++q) dst[q] = src[q];
     }
 }
 __global__ void k_up_bwd(Grid3 fine, const bf16* __restrict__ dout, int do_cs, int do_co, bf16* __restrict__ din, int c) {
@@ -371,16 +387,16 @@ inline int nblk(long long n, int t = 256) {
 
 template <int CIN, int COUT>
 int conv_attr() {
-    const size_t smem = (size_t)27 * CIN * COUT * sizeof(bf16);
-    return cudaFuncSetAttribute(k_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+    return cudaFuncSetAttribute(k_conv<CIN, COUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)conv_smem<CIN, COUT>()) == cudaSuccess;
 }
 template <int CIN, int COUT>
 void conv(const Grid3& gd, const bf16* in, int in_cs, int in_co, const bf16* w, const float* bias, bf16* out, float* out_f,
           int out_cs, int out_co, bool relu, cudaStream_t st) {
-    const size_t smem = (size_t)27 * CIN * COUT * sizeof(bf16);
-    const long long nv = (long long)gd.nx * gd.ny * gd.nz;
-    const int blocks = (int)((nv + 127) / 128);   // 8 warps x 16 voxels
-    k_conv<CIN, COUT><<<blocks, 256, smem, st>>>(gd, in, in_cs, in_co, w, bias, out, out_f, out_cs, out_co, relu ? 1 : 0);
+    const long long ntiles = (long long)((gd.nx + kTX - 1) / kTX) * ((gd.ny + kTY - 1) / kTY) * ((gd.nz + kTZ - 1) / kTZ);
+    const int blocks = (int)(ntiles < kConvBlocks ? ntiles : kConvBlocks);
+    k_conv<CIN, COUT><<<blocks, 256, conv_smem<CIN, COUT>(), st>>>(gd, in, in_cs, in_co, w, bias, out, out_f, out_cs,
+                                                                    out_co, relu ? 1 : 0);
 }
 template <int CIN, int COUT>
 void wgrad(const Grid3& gd, const bf16* dy, int dy_cs, int dy_co, const bf16* x, int x_cs, int x_co, float* dw,
@@ -473,7 +489,7 @@ void Net::forward(const bf16* X, int nx, int ny, int nz, cudaStream_t st) {
     k_pool<<<nblk((long long)c.nx * c.ny * c.nz * 16), 256, 0, st>>>(f, CAT, 48, 0, P0, 16);
     conv<16, 32>(c, P0, 16, 0, w16[2], bias(2), A2, nullptr, 32, 0, true, st);
     conv<32, 32>(c, A2, 32, 0, w16[3], bias(3), E1, nullptr, 32, 0, true, st);
-    k_up<<<nblk((long long)nx * ny * nz * 32), 256, 0, st>>>(f, E1, CAT, 48, 16, 32);
+    k_up<<<nblk((long long)nx * ny * nz), 256, 0, st>>>(f, E1, CAT, 48, 16, 32);
     conv<48, 16>(f, CAT, 48, 0, w16[4], bias(4), A3, nullptr, 16, 0, true, st);
     conv<16, 16>(f, A3, 16, 0, w16[5], bias(5), nullptr, OUT, 16, 0, false, st);
 }

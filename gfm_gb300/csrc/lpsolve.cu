@@ -46,14 +46,17 @@ __global__ void k_lp_scale_part(Ctx<R> c, int nx, int ny, int nz) {
         c.partials[kSlotLpN * kRedBlocks + blockIdx.x] = sb;
     }
 }
-// s = sqrt(mean (BS/AP)^2), summed in block order
+// sum of the first nb partials of a slot by one block, in a fixed order; valid in thread 0
+__device__ double fixed_sum(const double* partials, int slot, int nb, double* sh) {
+    double v = 0.0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) v += partials[slot * kRedBlocks + q];
+    return block_sum(v, sh);
+}
+// s = sqrt(mean (BS/AP)^2)
 __global__ void k_lp_scale_fin(const double* partials, double* scal, int nb) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (int q = 0; q < nb; ++q) {
-        a += partials[kSlotLpQ * kRedBlocks + q];
-        b += partials[kSlotLpN * kRedBlocks + q];
-    }
+    __shared__ double sh[32];
+    const double a = fixed_sum(partials, kSlotLpQ, nb, sh), b = fixed_sum(partials, kSlotLpN, nb, sh);
+    if (threadIdx.x != 0) return;
     const double s = b > 0.0 ? sqrt(a / b) : 0.0;
     scal[S_LP_SCALE] = (s > 1.0e-30 && isfinite(s)) ? s : 1.0;
 }
@@ -66,10 +69,11 @@ __global__ void k_lp_feat(Ctx<R> c, __nv_bfloat16* __restrict__ feats, int nx, i
         const double ap = (double)c.APc[o];
         const bool open = c.g.ib[o] < 1 && ap != 0.0;
         const float q = open ? (float)((double)c.BSq[o] / ap * inv) : 0.f;
-        __nv_bfloat16* f = feats + (size_t)v * 16;
-        f[0] = __float2bfloat16_rn(q);
-        f[1] = __float2bfloat16_rn(open ? 1.f : 0.f);
-        for (int ch = 2; ch < 16; ++ch) f[ch] = __float2bfloat16_rn(0.f);
+        const uint32_t w0 = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(q)) |
+                            ((uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(open ? 1.f : 0.f)) << 16);
+        uint4* f = reinterpret_cast<uint4*>(feats + (size_t)v * 16);
+        f[0] = make_uint4(w0, 0u, 0u, 0u);
+        f[1] = make_uint4(0u, 0u, 0u, 0u);
     }
 }
 // x = g (network output, channel 0) on open voxels of the solve range
@@ -110,13 +114,10 @@ __global__ void k_lp_check_part(Ctx<R> c, const R* x, int nx, int ny, int nz) {
 // alpha = (Mg.b)/(Mg.Mg); residual ratio |b - alpha Mg|/|b| = sqrt(1 - (Mg.b)^2/(|Mg|^2 |b|^2));
 // the guess is kept when that ratio is below 1
 __global__ void k_lp_decide(const double* partials, double* scal, int nb) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double gb = 0.0, gg = 0.0, bb = 0.0;
-    for (int q = 0; q < nb; ++q) {
-        gb += partials[kSlotLpGB * kRedBlocks + q];
-        gg += partials[kSlotLpGG * kRedBlocks + q];
-        bb += partials[kSlotLpBB * kRedBlocks + q];
-    }
+    __shared__ double sh[32];
+    const double gb = fixed_sum(partials, kSlotLpGB, nb, sh), gg = fixed_sum(partials, kSlotLpGG, nb, sh),
+                 bb = fixed_sum(partials, kSlotLpBB, nb, sh);
+    if (threadIdx.x != 0) return;
     const double alpha = gg > 0.0 ? gb / gg : 0.0;
     const double r2 = (gg > 0.0 && bb > 0.0) ? 1.0 - gb * gb / (gg * bb) : 1.0;
     const double ratio = sqrt(r2 > 0.0 ? r2 : 0.0);
@@ -156,12 +157,9 @@ __global__ void k_lp_tnorm_part(Ctx<R> c, const R* x, int nx, int ny, int nz) {
     }
 }
 __global__ void k_lp_tnorm_fin(const double* partials, double* scal, int nb) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double a = 0.0, b = 0.0;
-    for (int q = 0; q < nb; ++q) {
-        a += partials[kSlotLpQ * kRedBlocks + q];
-        b += partials[kSlotLpN * kRedBlocks + q];
-    }
+    __shared__ double sh[32];
+    const double a = fixed_sum(partials, kSlotLpQ, nb, sh), b = fixed_sum(partials, kSlotLpN, nb, sh);
+    if (threadIdx.x != 0) return;
     const double s = b > 0.0 ? sqrt(a / b) : 0.0;
     scal[S_LP_TSCALE] = (s > 1.0e-300 && isfinite(s)) ? s : 1.0;
 }
@@ -185,7 +183,7 @@ void launch_lp_features(const Ctx<R>& c, void* feats, int nx, int ny, int nz, cu
     const long long n = (long long)nx * ny * nz;
     const int nb = lp_blocks(n);
     k_lp_scale_part<R><<<nb, 256, 0, s>>>(c, nx, ny, nz);
-    k_lp_scale_fin<<<1, 32, 0, s>>>(c.partials, c.scal, nb);
+    k_lp_scale_fin<<<1, 256, 0, s>>>(c.partials, c.scal, nb);
     k_lp_feat<R><<<lp_blocks(n), 256, 0, s>>>(c, static_cast<__nv_bfloat16*>(feats), nx, ny, nz);
 }
 template <typename R>
@@ -194,7 +192,7 @@ void launch_lp_guess(const Ctx<R>& c, const float* out16, R* x, int nx, int ny, 
     const int nb = lp_blocks(n);
     k_lp_guess<R><<<nb, 256, 0, s>>>(c, out16, x, nx, ny, nz);
     k_lp_check_part<R><<<nb, 256, 0, s>>>(c, x, nx, ny, nz);
-    k_lp_decide<<<1, 32, 0, s>>>(c.partials, c.scal, nb);
+    k_lp_decide<<<1, 256, 0, s>>>(c.partials, c.scal, nb);
     k_lp_apply<R><<<nb, 256, 0, s>>>(c, x, nx, ny, nz);
 }
 template <typename R>
@@ -202,7 +200,7 @@ void launch_lp_target(const Ctx<R>& c, const R* x, float* tgt, int nx, int ny, i
     const long long n = (long long)nx * ny * nz;
     const int nb = lp_blocks(n);
     k_lp_tnorm_part<R><<<nb, 256, 0, s>>>(c, x, nx, ny, nz);
-    k_lp_tnorm_fin<<<1, 32, 0, s>>>(c.partials, c.scal, nb);
+    k_lp_tnorm_fin<<<1, 256, 0, s>>>(c.partials, c.scal, nb);
     k_lp_target<R><<<nb, 256, 0, s>>>(c, x, tgt, nx, ny, nz);
 }
 
