@@ -84,6 +84,7 @@ struct gfm_handle {
     gfm::lp::Net* lp = nullptr;
     void* lp_feats = nullptr;           // BF16 inputs, 16 channels per voxel
     int lp_nx = 0, lp_ny = 0, lp_nz = 0;
+    bool rb_fused = false;              // red-black order: fused plane visits (GFM_RB_FUSED=1)
 };
 
 namespace {
@@ -471,7 +472,7 @@ template <typename R>
 void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>* scr, int nsys, cudaStream_t st) {
     // external records: inside a captured graph these become real event nodes
     if (h->n_ev + 2 <= 16) cudaEventRecordWithFlags(h->ev[h->n_ev], st, cudaEventRecordExternal);
-    launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st);
+    const int launched = launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st, h->rb_fused);
     if (h->n_ev + 2 <= 16) { cudaEventRecordWithFlags(h->ev[h->n_ev + 1], st, cudaEventRecordExternal); h->n_ev += 2; }
     int nim = 0;
     for (int e = 0; e < nsys; ++e) {
@@ -479,7 +480,7 @@ void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>*
         double cells = (double)((sys[e].ie - sys[e].ib) / 2 + 1) * ((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);
         h->adi_cells_visits += cells * 2.0 * sys[e].nim;   // each sweep visits every plane twice
     }
-    h->adi_kernels_per_iter += h->adi_mode == GFM_ADI_MARCH ? 1 : 3 + 16LL * nim;
+    h->adi_kernels_per_iter += launched;
 }
 
 template <typename R>
@@ -774,6 +775,11 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     h->ncells = gr->ncells;
     cudaError_t ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { h->err = cudaGetErrorString(ce); return GFM_E_CUDA; }
+    if (prepare_line_solver() != GFM_OK) { h->err = "cannot raise the line solver's shared-memory limit"; return GFM_E_CUDA; }
+    {
+        const char* fz = std::getenv("GFM_RB_FUSED");
+        h->rb_fused = fz && fz[0] == '1';
+    }
     cudaEventCreate(&h->ev_adi0);
     cudaEventCreate(&h->ev_adi1);
     // double geometry first: its int8 map is shared by the float copy
@@ -1092,7 +1098,7 @@ int adlbl3_user(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, double* xt, const 
     if ((rc = put(xt, c.FZ)) || (rc = put(ap, c.APm)) || (rc = put(bs, c.BSm))) return rc;
     for (int q = 0; q < 6; ++q) if ((rc = put(as[q], c.ASm[q]))) return rc;
     Sys<R> s = sys_of<R>(c.FZ, c.APm, c.ASm, c.BSm, ib, ie, jb, je, kb, ke, nim);
-    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_fused);
     launch_from_split(g, c.FZ, h->d_stage, st);
     CK(cudaMemcpyAsync(xt, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1123,7 +1129,7 @@ int pcorr_sample(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, int nsweeps, void
     R* asc[6];
     for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
     Sys<R> s = sys_of<R>(c.DPc, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, nsweeps);
-    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_fused);
     launch_lp_target(c, c.DPc, target, nx, ny, nz, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());

@@ -132,8 +132,11 @@ template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
 template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
 template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);
-template <typename R> void launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
-                                             int mode, cudaStream_t s);
+// returns the number of kernels it launched
+// allow_fused: use the fused plane visit where the planes fit in shared memory
+template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
+                                            int mode, cudaStream_t s, bool allow_fused);
+int prepare_line_solver();   // once per process, before any stream capture
 // deterministic finish of block partials: op 0 sum, 1 max, 2 residual
 // (sum/NCELLS floored at 1e-16, NaN -> 1e-16), 3 sum/NCELLS
 struct FinishSpec {

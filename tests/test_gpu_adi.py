@@ -29,8 +29,12 @@ def test_march_matches_oracle_adlbl3(cls):
     g.close()
 
 
+@pytest.mark.parametrize("fused", ["0", "1"])
 @pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-10), (abi.GFM_PREC_MIXED, 1e-4)])
-def test_redblack_converges_to_manufactured_solution(prec, tol):
+def test_redblack_converges_to_manufactured_solution(prec, tol, fused, monkeypatch):
+    # both red-black forms: segmented passes on the colour-split copy, and
+    # fused plane visits (GFM_RB_FUSED=1, read when the handle is created)
+    monkeypatch.setenv("GFM_RB_FUSED", fused)
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
     ib = case.ibcell()
