@@ -176,6 +176,8 @@ SIGNATURES = [
     ("gfm_lp_forward", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     ("gfm_lp_train_step", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_float,
                                     C.c_int, C.POINTER(C.c_double), C.c_void_p]),
+    ("gfm_lp_set_tensor_path", C.c_int, [C.c_void_p, C.c_int]),
+    ("gfm_lp_tensor_status", C.c_int, [C.c_void_p]),
     ("gfm_lp_last_error", C.c_char_p, []),
     ("gfm_gpu_pcorr_sample", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     ("gfm_gpu_set_lp", C.c_int, [C.c_void_p, C.c_void_p]),

@@ -18,7 +18,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libgfm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["asm.cu", "adi.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lpsolve.cu"]
+CUDA_SOURCES = ["asm.cu", "adi.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lp_tc.cu", "lpsolve.cu"]
 CXX_SOURCES = ["case_build.cpp"]
 
 

@@ -62,10 +62,6 @@ __device__ __forceinline__ uint32_t pack2(bf16 lo, bf16 hi) {
     return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
 }
 
-struct Grid3 {
-    int nx, ny, nz;
-    __device__ __forceinline__ int nvox() const { return nx * ny * nz; }
-};
 
 // ---- convolution (forward and input gradient) ---------------------------------
 // out[v][co] = bias[co] + sum_t sum_ci in[v + d_t][ci] * W[t][co][ci]
@@ -161,15 +157,14 @@ __global__ void __launch_bounds__(256) k_conv(Grid3 gd, const bf16* __restrict__
 // ---- weight gradient ------------------------------------------------------------
 // dW[t][co][ci] += sum_v dy[v][co] * x[v + d_t][ci]: a GEMM with M = co, N = ci,
 // K = voxels.  Block (chunk of voxels, tap): each warp takes 16-voxel slices
-// of the chunk; the warps' partial sums meet in shared memory and leave with
-// one FP32 atomic per weight.
+// of the chunk; the warps' sums are added in warp order and the block writes
+// its partial to part[chunk][t][co][ci]; k_wgrad_sum adds the chunks in
+// order, so the gradient does not depend on scheduling.
 constexpr int kWgChunk = 2048;   // voxels per block
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(256) k_wgrad(Grid3 gd, const bf16* __restrict__ dy, int dy_cs, int dy_co,
-                                              const bf16* __restrict__ x, int x_cs, int x_co, float* __restrict__ dw) {
-    __shared__ float red[COUT * CIN];
-    for (int i = threadIdx.x; i < COUT * CIN; i += blockDim.x) red[i] = 0.f;
-    __syncthreads();
+                                              const bf16* __restrict__ x, int x_cs, int x_co, float* __restrict__ part) {
+    __shared__ float red[8][COUT * CIN];
     const int t = blockIdx.y;
     const int dx = t % 3 - 1, dyy = (t / 3) % 3 - 1, dz = t / 9 - 1;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -224,35 +219,48 @@ __global__ void __launch_bounds__(256) k_wgrad(Grid3 gd, const bf16* __restrict_
             }
         }
     }
-    // D (M=co x N=ci): d0,d1 = (co g, ci 2tq..+1), d2,d3 = (co g+8, ...)
+    // D (M=co x N=ci): d0,d1 = (co g, ci 2tq..+1), d2,d3 = (co g+8, ...); each
+    // element of the warp's tile is held by exactly one lane
+    float* mine = red[warp];
 #pragma unroll
     for (int m = 0; m < COUT / 16; ++m)
 #pragma unroll
         for (int n = 0; n < CIN / 8; ++n) {
             const int co = m * 16 + g, ci = n * 8 + 2 * tq;
-            atomicAdd(&red[co * CIN + ci], acc[m][n][0]);
-            atomicAdd(&red[co * CIN + ci + 1], acc[m][n][1]);
-            atomicAdd(&red[(co + 8) * CIN + ci], acc[m][n][2]);
-            atomicAdd(&red[(co + 8) * CIN + ci + 1], acc[m][n][3]);
+            mine[co * CIN + ci] = acc[m][n][0];
+            mine[co * CIN + ci + 1] = acc[m][n][1];
+            mine[(co + 8) * CIN + ci] = acc[m][n][2];
+            mine[(co + 8) * CIN + ci + 1] = acc[m][n][3];
         }
     __syncthreads();
-    for (int i = threadIdx.x; i < COUT * CIN; i += blockDim.x) atomicAdd(&dw[(size_t)t * COUT * CIN + i], red[i]);
+    for (int i = threadIdx.x; i < COUT * CIN; i += blockDim.x) {
+        float s = 0.f;
+        for (int w = 0; w < nwarp; ++w) s += red[w][i];
+        part[((size_t)blockIdx.x * 27 + t) * COUT * CIN + i] = s;
+    }
+}
+// dw[i] += sum over chunks of part[chunk][i], in chunk order
+__global__ void k_wgrad_sum(int nchunk, int n, const float* __restrict__ part, float* __restrict__ dw) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * n + i];
+        dw[i] += s;
+    }
 }
 
-// bias gradient: db[co] += sum_v dy[v][co]
+// bias gradient: db[co] += sum_v dy[v][co]; one block per channel, fixed order
 __global__ void k_bgrad(int nv, int cout, const bf16* __restrict__ dy, int dy_cs, int dy_co, float* __restrict__ db) {
-    __shared__ float red[64];
-    for (int i = threadIdx.x; i < cout; i += blockDim.x) red[i] = 0.f;
-    __syncthreads();
-    const int co = threadIdx.x % cout;
-    const int lanes = blockDim.x / cout;
+    __shared__ float sh[256];
+    const int co = blockIdx.x;
     float s = 0.f;
-    if ((int)threadIdx.x < lanes * cout)
-        for (int v = blockIdx.x * lanes + threadIdx.x / cout; v < nv; v += gridDim.x * lanes)
-            s += __bfloat162float(dy[(size_t)v * dy_cs + dy_co + co]);
-    if ((int)threadIdx.x < lanes * cout) atomicAdd(&red[co], s);
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) s += __bfloat162float(dy[(size_t)v * dy_cs + dy_co + co]);
+    sh[threadIdx.x] = s;
     __syncthreads();
-    for (int i = threadIdx.x; i < cout; i += blockDim.x) atomicAdd(&db[i], red[i]);
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) db[co] += sh[0];
 }
 
 // ---- pooling, upsampling, activation gradient -----------------------------------
@@ -399,11 +407,13 @@ void conv(const Grid3& gd, const bf16* in, int in_cs, int in_co, const bf16* w, 
                                                                     out_co, relu ? 1 : 0);
 }
 template <int CIN, int COUT>
-void wgrad(const Grid3& gd, const bf16* dy, int dy_cs, int dy_co, const bf16* x, int x_cs, int x_co, float* dw,
+void wgrad(const Grid3& gd, const bf16* dy, int dy_cs, int dy_co, const bf16* x, int x_cs, int x_co, float* dw, float* part,
            cudaStream_t st) {
     const long long nv = (long long)gd.nx * gd.ny * gd.nz;
-    dim3 grid((unsigned)((nv + kWgChunk - 1) / kWgChunk), 27);
-    k_wgrad<CIN, COUT><<<grid, 256, 0, st>>>(gd, dy, dy_cs, dy_co, x, x_cs, x_co, dw);
+    const int nchunk = (int)((nv + kWgChunk - 1) / kWgChunk);
+    k_wgrad<CIN, COUT><<<dim3(nchunk, 27), 256, 0, st>>>(gd, dy, dy_cs, dy_co, x, x_cs, x_co, part);
+    const int n = 27 * CIN * COUT;
+    k_wgrad_sum<<<nblk(n), 256, 0, st>>>(nchunk, n, part, dw);
 }
 
 int Net::create(int nx, int ny, int nz, uint64_t seed) {
@@ -423,8 +433,10 @@ int Net::create(int nx, int ny, int nz, uint64_t seed) {
               cudaMalloc((void**)&lacc, 2 * sizeof(double)) == cudaSuccess;
     for (int l = 0; l < kNumLayers; ++l) {
         const long long nw = 27LL * kLayers[l].cin * kLayers[l].cout;
-        ok = ok && bal(&w16[l], nw) && bal(&wt16[l], nw);
+        ok = ok && bal(&w16[l], nw) && bal(&wt16[l], nw) && bal(&wtc[l], nw);
     }
+    ok = ok && cudaMalloc((void**)&tc_err, sizeof(int)) == cudaSuccess;
+    ok = ok && fal(&wg_part, ((v0 + kWgChunk - 1) / kWgChunk) * 27LL * 1024);   // chunks x taps x the largest cout*cin
     ok = ok && bal(&A1, v0 * 16) && bal(&CAT, v0 * 48) && bal(&P0, v1 * 16) && bal(&A2, v1 * 32) && bal(&E1, v1 * 32) &&
          bal(&A3, v0 * 16) && fal(&OUT, v0 * 16) && bal(&dOUT, v0 * 16) && bal(&dA3, v0 * 16) && bal(&dCAT, v0 * 48) &&
          bal(&dE1, v1 * 32) && bal(&dA2, v1 * 32) && bal(&dP0, v1 * 16) && bal(&dE0, v0 * 16) && bal(&dA1, v0 * 16);
@@ -451,6 +463,8 @@ int Net::create(int nx, int ny, int nz, uint64_t seed) {
         }
     }
     if (cudaMemcpy(p32, h.data(), sizeof(float) * np, cudaMemcpyHostToDevice) != cudaSuccess) return GFM_E_CUDA;
+    cudaMemset(tc_err, 0, sizeof(int));
+    if (prepare_tc() != GFM_OK) { err = "cannot raise the shared-memory limit of the tcgen05 convolutions"; return GFM_E_CUDA; }
     cudaMemset(g32, 0, sizeof(float) * np);
     cudaMemset(m32, 0, sizeof(float) * np);
     cudaMemset(v32, 0, sizeof(float) * np);
@@ -459,11 +473,13 @@ int Net::create(int nx, int ny, int nz, uint64_t seed) {
 }
 
 void Net::release() {
-    void* ps[] = {p32, g32, m32, v32, nopen, lacc, A1, CAT, P0, A2, E1, A3, OUT, dOUT, dA3, dCAT, dE1, dA2, dP0, dE0, dA1};
+    void* ps[] = {p32, g32, m32, v32, nopen, lacc, A1, CAT, P0, A2, E1, A3, OUT, dOUT, dA3, dCAT, dE1, dA2, dP0, dE0, dA1, tc_err,
+                  wg_part};
     for (void* p : ps) if (p) cudaFree(p);
     for (int l = 0; l < kNumLayers; ++l) {
         if (w16[l]) cudaFree(w16[l]);
         if (wt16[l]) cudaFree(wt16[l]);
+        if (wtc[l]) cudaFree(wtc[l]);
     }
 }
 
@@ -471,6 +487,7 @@ void Net::stage(cudaStream_t st) {
     for (int l = 0; l < kNumLayers; ++l) {
         const int n = 27 * kLayers[l].cin * kLayers[l].cout;
         k_stage<<<nblk(n), 256, 0, st>>>(kLayers[l].cin, kLayers[l].cout, p32 + weight_offset(l), w16[l], wt16[l]);
+        stage_tc(kLayers[l].cin, kLayers[l].cout, p32 + weight_offset(l), wtc[l], st);
     }
 }
 
@@ -484,14 +501,29 @@ void Net::forward(const bf16* X, int nx, int ny, int nz, cudaStream_t st) {
     const Grid3 f{nx, ny, nz}, c{nx / 2, ny / 2, nz / 2};
     const float* b = p32;
     auto bias = [&](int l) { return b + weight_offset(l) + 27 * kLayers[l].cin * kLayers[l].cout; };
-    conv<16, 16>(f, X, 16, 0, w16[0], bias(0), A1, nullptr, 16, 0, true, st);
-    conv<16, 16>(f, A1, 16, 0, w16[1], bias(1), CAT, nullptr, 48, 0, true, st);
+    if (use_tc) {
+        conv_tc<16, 16>(f, X, 16, 0, wtc[0], bias(0), A1, nullptr, 16, 0, true, tc_err, st);
+        conv_tc<16, 16>(f, A1, 16, 0, wtc[1], bias(1), CAT, nullptr, 48, 0, true, tc_err, st);
+    } else {
+        conv<16, 16>(f, X, 16, 0, w16[0], bias(0), A1, nullptr, 16, 0, true, st);
+        conv<16, 16>(f, A1, 16, 0, w16[1], bias(1), CAT, nullptr, 48, 0, true, st);
+    }
     k_pool<<<nblk((long long)c.nx * c.ny * c.nz * 16), 256, 0, st>>>(f, CAT, 48, 0, P0, 16);
-    conv<16, 32>(c, P0, 16, 0, w16[2], bias(2), A2, nullptr, 32, 0, true, st);
-    conv<32, 32>(c, A2, 32, 0, w16[3], bias(3), E1, nullptr, 32, 0, true, st);
+    if (use_tc) {
+        conv_tc<16, 32>(c, P0, 16, 0, wtc[2], bias(2), A2, nullptr, 32, 0, true, tc_err, st);
+        conv_tc<32, 32>(c, A2, 32, 0, wtc[3], bias(3), E1, nullptr, 32, 0, true, tc_err, st);
+    } else {
+        conv<16, 32>(c, P0, 16, 0, w16[2], bias(2), A2, nullptr, 32, 0, true, st);
+        conv<32, 32>(c, A2, 32, 0, w16[3], bias(3), E1, nullptr, 32, 0, true, st);
+    }
     k_up<<<nblk((long long)nx * ny * nz), 256, 0, st>>>(f, E1, CAT, 48, 16, 32);
-    conv<48, 16>(f, CAT, 48, 0, w16[4], bias(4), A3, nullptr, 16, 0, true, st);
-    conv<16, 16>(f, A3, 16, 0, w16[5], bias(5), nullptr, OUT, 16, 0, false, st);
+    if (use_tc) {
+        conv_tc<48, 16>(f, CAT, 48, 0, wtc[4], bias(4), A3, nullptr, 16, 0, true, tc_err, st);
+        conv_tc<16, 16>(f, A3, 16, 0, wtc[5], bias(5), nullptr, OUT, 16, 0, false, tc_err, st);
+    } else {
+        conv<48, 16>(f, CAT, 48, 0, w16[4], bias(4), A3, nullptr, 16, 0, true, st);
+        conv<16, 16>(f, A3, 16, 0, w16[5], bias(5), nullptr, OUT, 16, 0, false, st);
+    }
 }
 
 // gradients of the loss for one sample, accumulated into g32
@@ -504,37 +536,37 @@ void Net::backward(const bf16* X, const float* T, int nx, int ny, int nz, cudaSt
     k_count_open<<<nblk(v0), 256, 0, st>>>(v0, X, nopen);
     k_loss<<<nblk(v0), 256, 0, st>>>(v0, OUT, X, T, nopen, dOUT, lacc);
     // c6: A3 -> OUT (linear)
-    wgrad<16, 16>(f, dOUT, 16, 0, A3, 16, 0, dw(5), st);
-    k_bgrad<<<64, 256, 0, st>>>(v0, 16, dOUT, 16, 0, db(5));
+    wgrad<16, 16>(f, dOUT, 16, 0, A3, 16, 0, dw(5), wg_part, st);
+    k_bgrad<<<16, 256, 0, st>>>(v0, 16, dOUT, 16, 0, db(5));
     conv<16, 16>(f, dOUT, 16, 0, wt16[5], nullptr, dA3, nullptr, 16, 0, false, st);
     k_relu_bwd<<<nblk((long long)v0 * 16), 256, 0, st>>>(v0, 16, dA3, 16, 0, A3, 16, 0);
     // c5: CAT -> A3
-    wgrad<48, 16>(f, dA3, 16, 0, CAT, 48, 0, dw(4), st);
-    k_bgrad<<<64, 256, 0, st>>>(v0, 16, dA3, 16, 0, db(4));
+    wgrad<48, 16>(f, dA3, 16, 0, CAT, 48, 0, dw(4), wg_part, st);
+    k_bgrad<<<16, 256, 0, st>>>(v0, 16, dA3, 16, 0, db(4));
     conv<16, 48>(f, dA3, 16, 0, wt16[4], nullptr, dCAT, nullptr, 48, 0, false, st);
     // up: E1 -> CAT[16:48]
     k_up_bwd<<<nblk((long long)v1 * 32), 256, 0, st>>>(f, dCAT, 48, 16, dE1, 32);
     k_relu_bwd<<<nblk((long long)v1 * 32), 256, 0, st>>>(v1, 32, dE1, 32, 0, E1, 32, 0);
     // c4: A2 -> E1
-    wgrad<32, 32>(c, dE1, 32, 0, A2, 32, 0, dw(3), st);
-    k_bgrad<<<64, 256, 0, st>>>(v1, 32, dE1, 32, 0, db(3));
+    wgrad<32, 32>(c, dE1, 32, 0, A2, 32, 0, dw(3), wg_part, st);
+    k_bgrad<<<32, 256, 0, st>>>(v1, 32, dE1, 32, 0, db(3));
     conv<32, 32>(c, dE1, 32, 0, wt16[3], nullptr, dA2, nullptr, 32, 0, false, st);
     k_relu_bwd<<<nblk((long long)v1 * 32), 256, 0, st>>>(v1, 32, dA2, 32, 0, A2, 32, 0);
     // c3: P0 -> A2
-    wgrad<16, 32>(c, dA2, 32, 0, P0, 16, 0, dw(2), st);
-    k_bgrad<<<64, 256, 0, st>>>(v1, 32, dA2, 32, 0, db(2));
+    wgrad<16, 32>(c, dA2, 32, 0, P0, 16, 0, dw(2), wg_part, st);
+    k_bgrad<<<32, 256, 0, st>>>(v1, 32, dA2, 32, 0, db(2));
     conv<32, 16>(c, dA2, 32, 0, wt16[2], nullptr, dP0, nullptr, 16, 0, false, st);
     // pool: E0 = CAT[0:16] -> P0; E0 also feeds c5 directly
     k_pool_bwd<<<nblk((long long)v0 * 16), 256, 0, st>>>(f, dCAT, 48, 0, dP0, dE0, 16);
     k_relu_bwd<<<nblk((long long)v0 * 16), 256, 0, st>>>(v0, 16, dE0, 16, 0, CAT, 48, 0);
     // c2: A1 -> E0
-    wgrad<16, 16>(f, dE0, 16, 0, A1, 16, 0, dw(1), st);
-    k_bgrad<<<64, 256, 0, st>>>(v0, 16, dE0, 16, 0, db(1));
+    wgrad<16, 16>(f, dE0, 16, 0, A1, 16, 0, dw(1), wg_part, st);
+    k_bgrad<<<16, 256, 0, st>>>(v0, 16, dE0, 16, 0, db(1));
     conv<16, 16>(f, dE0, 16, 0, wt16[1], nullptr, dA1, nullptr, 16, 0, false, st);
     k_relu_bwd<<<nblk((long long)v0 * 16), 256, 0, st>>>(v0, 16, dA1, 16, 0, A1, 16, 0);
     // c1: X -> A1
-    wgrad<16, 16>(f, dA1, 16, 0, X, 16, 0, dw(0), st);
-    k_bgrad<<<64, 256, 0, st>>>(v0, 16, dA1, 16, 0, db(0));
+    wgrad<16, 16>(f, dA1, 16, 0, X, 16, 0, dw(0), wg_part, st);
+    k_bgrad<<<16, 256, 0, st>>>(v0, 16, dA1, 16, 0, db(0));
 }
 
 void Net::adam(float lr, int step, cudaStream_t st) {
@@ -631,5 +663,19 @@ extern "C" int gfm_lp_train_step(gfm_lp* lp, const void* feats, const float* tar
         *loss = h[1] > 0 ? h[0] / h[1] : 0.0;
     }
     return cudaGetLastError() == cudaSuccess ? GFM_OK : GFM_E_CUDA;
+}
+extern "C" int gfm_lp_set_tensor_path(gfm_lp* lp, int tcgen05) {
+    if (!lp) return GFM_E_ARG;
+    reinterpret_cast<Net*>(lp)->use_tc = tcgen05 != 0;
+    return GFM_OK;
+}
+// 1 when a tcgen05 convolution tile gave up waiting for its MMAs (its output is then invalid)
+extern "C" int gfm_lp_tensor_status(gfm_lp* lp) {
+    if (!lp) return GFM_E_ARG;
+    Net* n = reinterpret_cast<Net*>(lp);
+    int v = 0;
+    if (cudaDeviceSynchronize() != cudaSuccess) return GFM_E_CUDA;
+    if (cudaMemcpy(&v, n->tc_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return GFM_E_CUDA;
+    return v;
 }
 extern "C" const char* gfm_lp_last_error(void) { return g_lp_err.c_str(); }

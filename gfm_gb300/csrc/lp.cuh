@@ -14,6 +14,11 @@ namespace lp {
 struct LayerSpec {
     int cin, cout;
 };
+// voxel grid, x fastest: voxel (z*ny + y)*nx + x
+struct Grid3 {
+    int nx, ny, nz;
+    __host__ __device__ __forceinline__ int nvox() const { return nx * ny * nz; }
+};
 constexpr int kNumLayers = 6;
 constexpr int kFeatChannels = 2;   // Jacobi-scaled right-hand side, open-cell mask
 extern const LayerSpec kLayers[kNumLayers];
@@ -32,6 +37,11 @@ struct Net {
                   *dE0 = nullptr, *dA1 = nullptr;
     float* nopen = nullptr;
     double* lacc = nullptr;                  // squared error, open-voxel count of the last step
+    // forward convolutions on tcgen05 (lp_tc.cu): weights in the operand order, expiry flag
+    __nv_bfloat16* wtc[kNumLayers] = {};
+    int* tc_err = nullptr;
+    float* wg_part = nullptr;                // per-chunk weight-gradient partials (fixed-order sums)
+    bool use_tc = true;
     std::string err;
 
     int create(int nx, int ny, int nz, uint64_t seed);
@@ -42,6 +52,13 @@ struct Net {
     void backward(const __nv_bfloat16* feats, const float* target, int nx, int ny, int nz, cudaStream_t st);
     void adam(float lr, int step, cudaStream_t st);
 };
+
+// tcgen05 forward convolution (lp_tc.cu)
+int prepare_tc();
+void stage_tc(int cin, int cout, const float* wf, __nv_bfloat16* wtc, cudaStream_t st);
+template <int CIN, int COUT>
+void conv_tc(const Grid3& gd, const __nv_bfloat16* in, int in_cs, int in_co, const __nv_bfloat16* wtc, const float* bias,
+             __nv_bfloat16* out, float* out_f, int out_cs, int out_co, bool relu, int* err, cudaStream_t st);
 
 }  // namespace lp
 }  // namespace gfm

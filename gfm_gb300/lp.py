@@ -55,6 +55,14 @@ class LearnedPressure:
         assert p.size == self.n
         self._check(self.lib.gfm_lp_set_params(self.h, p.ctypes.data_as(C.POINTER(C.c_float))))
 
+    def set_tensor_path(self, tcgen05: bool) -> None:
+        """Forward convolutions on tcgen05 (True) or mma.sync (False)."""
+        self._check(self.lib.gfm_lp_set_tensor_path(self.h, 1 if tcgen05 else 0))
+
+    def tensor_status(self) -> int:
+        """1 if a tcgen05 tile gave up waiting for its MMAs (output invalid)."""
+        return self.lib.gfm_lp_tensor_status(self.h)
+
     def forward(self, feats, dims) -> "torch.Tensor":
         torch = _torch()
         out = torch.empty(int(np.prod(dims)), dtype=torch.float32, device=feats.device)

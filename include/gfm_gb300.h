@@ -262,6 +262,12 @@ int  gfm_lp_forward(gfm_lp *lp, const void *feats, float *out,
 int  gfm_lp_train_step(gfm_lp *lp, const void *feats, const float *target,
                        int nx, int ny, int nz, float lr, int update,
                        double *loss, void *stream);
+/* Forward convolutions on the tcgen05 tensor cores (1, the default) or on
+ * warp-level mma.sync (0); gradients always use mma.sync.  Status: 1 when
+ * a tcgen05 tile gave up its bounded wait for its MMAs since creation (its
+ * output is then invalid), 0 otherwise; waits for the device. */
+int  gfm_lp_set_tensor_path(gfm_lp *lp, int tcgen05);
+int  gfm_lp_tensor_status(gfm_lp *lp);
 const char *gfm_lp_last_error(void);
 /* Training sample from the p' system of the handle's last iteration: inputs
  * to `feats`, and to `target` the system's solution after `nsweeps` line-

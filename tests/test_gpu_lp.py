@@ -42,6 +42,27 @@ def test_forward_matches_cpu_reference(torch):
     lp.close()
 
 
+@pytest.mark.parametrize("dims", [(8, 16, 2), (24, 20, 6)])
+def test_tcgen05_forward_matches_mma_sync_and_reference(torch, dims):
+    """The forward pass with its convolutions on tcgen05 (tensor memory
+    accumulators) agrees with the mma.sync path and the CPU reference."""
+    from gfm_gb300.lp import LearnedPressure
+    rng = np.random.default_rng(9)
+    p = lp_ref.init_params(6)
+    lp = LearnedPressure(dims, seed=1)
+    lp.set_params(p)
+    x, t, xb, tb = _sample(rng, dims, torch)
+    lp.set_tensor_path(False)
+    a = lp.forward(xb, dims).cpu().numpy()
+    lp.set_tensor_path(True)
+    b = lp.forward(xb, dims).cpu().numpy()
+    assert lp.tensor_status() == 0
+    want = lp_ref.forward(p, x)["out"][..., 0].reshape(-1)
+    assert np.linalg.norm(b - a) / np.linalg.norm(a) < 1e-2
+    assert np.linalg.norm(b - want) / np.linalg.norm(want) < 1e-2
+    lp.close()
+
+
 def test_gradients_match_cpu_reference(torch):
     from gfm_gb300.lp import LearnedPressure
     dims = (8, 8, 4)
@@ -91,6 +112,20 @@ def test_training_reduces_error_of_the_p_prime_guess(torch):
     assert np.mean(hist[-40:]) < np.mean(hist[:40])
     assert after < 0.8, (before, after)   # the zero start has relative error 1
     lp.close()
+
+
+def test_training_is_deterministic(torch):
+    """Gradients are summed in a fixed order, so two trainings on the same
+    samples give the same parameters bit for bit."""
+    from gfm_gb300.lp import LearnedPressure, collect_samples
+    train = collect_samples([configs.small_furnace()], iters=12, every=3, nsweeps=20, start=3)
+    ps = []
+    for _ in range(2):
+        lp = LearnedPressure(train[0][2], seed=5)
+        lp.fit(train, steps=30, lr=2e-3, seed=1)
+        ps.append(lp.params())
+        lp.close()
+    assert np.array_equal(ps[0], ps[1])
 
 
 def test_trained_guess_lowers_the_p_prime_residual_of_the_same_iteration(torch):
