@@ -372,7 +372,7 @@ def run_ours(args):
         from gfm_gb300.lp import train_default
         t0 = time.perf_counter()
         log = []
-        lp = train_default((case.mp // 2 - 2, case.np // 2 - 2, case.lp // 2 - 2), log=log)
+        lp = train_default((case.mp // 2 - 2, case.np // 2 - 2, case.lp // 2 - 2), log=log, steps=args.lp_steps)
         train_s = time.perf_counter() - t0
         thr = args.ttr or 1e-3
         learned = {"train_seconds": train_s, "training": log,
@@ -484,6 +484,7 @@ def main():
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--learned", action="store_true",
                     help="also train the learned p' guess and measure time-to-residual with it")
+    ap.add_argument("--lp-steps", type=int, default=1500, help="Adam steps per learning rate (two rates)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

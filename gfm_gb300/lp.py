@@ -117,16 +117,17 @@ def pcorr_sample(solver: GpuSolver, nsweeps: int):
     return feats, tgt, dims
 
 
-def train_default(dims: tuple, seed: int = 3, variants: int = 8, log: list | None = None) -> LearnedPressure:
+def train_default(dims: tuple, seed: int = 3, variants: int = 8, log: list | None = None,
+                  steps: int = 1500) -> LearnedPressure:
     """The standard recipe: p' systems of `variants` seeded variants of the
     48x24x16 furnace (one every 5 outer iterations from 5 to 120, targets from
-    60 sweeps), 1500 Adam steps at 2e-3 and 1500 at 5e-4.  `dims` sizes the
-    network's buffers for the largest grid it will be applied to."""
+    60 sweeps), `steps` Adam steps at 2e-3 and as many at 5e-4.  `dims` sizes
+    the network's buffers for the largest grid it will be applied to."""
     from . import configs
     samples = collect_samples([configs.furnace_variant(s) for s in range(variants)], iters=120, every=5, nsweeps=60,
                               start=5)
     lp = LearnedPressure(dims, seed=seed)
-    for lr, steps in ((2e-3, 1500), (5e-4, 1500)):
+    for lr in (2e-3, 5e-4):
         h = lp.fit(samples, steps=steps, lr=lr, seed=seed)
         if log is not None:
             log.append({"lr": lr, "steps": steps, "loss_first": float(np.mean(h[:50])), "loss_last": float(np.mean(h[-50:]))})
