@@ -203,6 +203,8 @@ __device__ __forceinline__ int rb_class(int ib, int jb, int kb) { return (ib & 1
 // XT of the whole class -> split copy
 template <typename R>
 __global__ void k_rbs_in(GeoT<R> g, RbBatch<R> b) {
+    pdl_wait();
+    pdl_trigger();
     const Sys<R>& s = b.sys[blockIdx.y];
     const AdiScratch<R>& w = b.scr[blockIdx.y];
     const R* __restrict__ xt = s.xt + (long long)rb_class(s.ib, s.jb, s.kb) * g.CB;
@@ -221,6 +223,8 @@ __global__ void k_rbs_in(GeoT<R> g, RbBatch<R> b) {
 // loads in flight.
 template <typename R>
 __global__ void k_rbs_factor(GeoT<R> g, RbBatch<R> b) {
+    pdl_wait();
+    pdl_trigger();
     constexpr int C = 8;
     const Sys<R>& s = b.sys[blockIdx.y];
     const AdiScratch<R>& w = b.scr[blockIdx.y];
@@ -286,13 +290,29 @@ __global__ void k_rbs_factor(GeoT<R> g, RbBatch<R> b) {
 #define GFM_RB_M 8
 #endif
 template <typename R> struct RbSeg { static constexpr int M = GFM_RB_M; };
+// minimum resident pass blocks per SM (blocks of up to 512 threads).  A
+// 64-register cap (2) measured 7 % slower than the compiler's own choice.
+#ifndef GFM_RB_MINB
+#define GFM_RB_MINB 1
+#endif
 
 // One pass of all y- and z-lines of the planes of one colour.  Block = S warps
 // x 32 lanes; lane = one line (32 consecutive line slots), warp = segment.
-template <typename R, int S, bool FIRST>
-__global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+// Pass L=1 (FIRST) reads XT and writes X2/X3 and the scaled x-neighbour
+// terms; pass L=2 writes X2B/X3B, which an averaging launch brings into XT.
+// Pass L=2 reads XT too, or with AVG, for the cells of the solve range, the
+// average (X2+X3)/2 of its colour's pass L=1 -- the value the averaging
+// launch between the passes would have stored in XT, computed the same way,
+// so that launch is left out.  (Averaging in pass L=1 as well, with X2B/X3B
+// seeded from XT, removes the other launch but measured slower: pass L=1
+// then needs ten neighbour loads a row.)
+template <typename R, int S, bool FIRST, bool AVG>
+__global__ void __launch_bounds__(32 * S, (32 * S <= 512 ? GFM_RB_MINB : 1))
+    k_rbs_pass(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
     constexpr int M = RbSeg<R>::M;
     __shared__ R sA[S][32], sB[S][32];
+    pdl_wait();
+    pdl_trigger();
     const Sys<R>& s = b.sys[blockIdx.y];
     if (sweep >= s.nim) return;
     const AdiScratch<R>& w = b.scr[blockIdx.y];
@@ -311,26 +331,35 @@ __global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, in
     const int dxp = (1 - 2 * h) * g.CBH + h, dxm = dxp - 1;   // x-neighbours I+2, I-2 in the other half
     const bool zl = active && t >= ny;
     int base = 0, step = 0, ostep = 0, n = 0;
+    bool up_in = false, dn_in = false;             // the neighbour lines at +-ostep lie in the solve range
     if (active) {
         if (!zl) {
             const int r = t % npc, kk = t / npc;
             base = hb + ((s.kb >> 1) + kk) * SZ + (s.jb >> 1) * g.PXH + r;
             step = g.PXH; ostep = SZ; n = nJ;
+            up_in = kk + 1 < nK; dn_in = kk > 0;
         } else {
             const int u = t - ny, r = u % npc, jj = u / npc;
             base = hb + (s.kb >> 1) * SZ + ((s.jb >> 1) + jj) * g.PXH + r;
             step = SZ; ostep = g.PXH; n = nK;
+            up_in = jj + 1 < nJ; dn_in = jj > 0;
         }
     }
     const R* __restrict__ x = w.xs;
+    const R* __restrict__ x2 = w.x2;
+    const R* __restrict__ x3 = w.x3;
     const Quad<R>* __restrict__ QA = zl ? w.za : w.ya;
     const Quad<R>* __restrict__ QB = zl ? w.zb : w.yb;
     R* __restrict__ sb = zl ? w.sbz : w.sby;
-    R* __restrict__ out = zl ? w.x3 : w.x2;
+    R* __restrict__ out = FIRST ? (zl ? w.x3 : w.x2) : (zl ? w.x3b : w.x2b);
     const int m = (n + S - 1) / S;
     const int e0 = seg * m;
     int cnt = n - e0;
     cnt = cnt < 0 ? 0 : (cnt > m ? m : cnt);
+    // XT one step below and one step above the line (JBML / KBML, JEPL / KEPL):
+    // never updated by the pass, so loaded up front with the rows
+    const R xlo = active ? x[base - step] : R(0);
+    const R xhi = active ? x[base + n * step] : R(0);
 
     // non-recurrent part of every row of the segment
     R rr[M], al[M], pv[M];
@@ -340,15 +369,18 @@ __global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, in
             const int o = base + (e0 + i) * step;
             const Quad<R> A = QA[o];
             R v;
+            const int ou = o + ostep, od = o - ostep;
+            const R xu = AVG && up_in ? (x2[ou] + x3[ou]) / R(2) : x[ou];
+            const R xd = AVG && dn_in ? (x2[od] + x3[od]) / R(2) : x[od];
             if (FIRST) {
                 const Quad<R> B = QB[o];
                 const R bx = B.x + B.y * x[o + dxp] + B.z * x[o + dxm];
                 sb[o] = bx;
-                v = bx + A.x * x[o + ostep] + A.y * x[o - ostep];
+                v = bx + A.x * xu + A.y * xd;
             } else {
-                v = sb[o] + A.x * x[o + ostep] + A.y * x[o - ostep];
+                v = sb[o] + A.x * xu + A.y * xd;
             }
-            if (rb_copy(A.w)) v = x[o];
+            if (rb_copy(A.w)) v = AVG ? (x2[o] + x3[o]) / R(2) : x[o];
             rr[i] = v;
             al[i] = A.z;
             pv[i] = A.w;
@@ -369,7 +401,7 @@ __global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, in
     sA[seg][lane] = cnt > 0 ? Pc : R(1);
     sB[seg][lane] = cnt > 0 ? qc : R(0);
     __syncthreads();
-    R qin = active ? x[base - step] : R(0);        // XT one step below the line (JBML / KBML)
+    R qin = xlo;
     for (int k = 0; k < seg; ++k) qin = sA[k][lane] * qin + sB[k][lane];
 #pragma unroll
     for (int i = 0; i < M; ++i)
@@ -390,7 +422,7 @@ __global__ void __launch_bounds__(32 * S) k_rbs_pass(GeoT<R> g, RbBatch<R> b, in
     sA[seg][lane] = cnt > 0 ? Rc : R(1);
     sB[seg][lane] = cnt > 0 ? xc : R(0);
     __syncthreads();
-    R xin = active ? x[base + n * step] : R(0);    // XT one step above the line (JEPL / KEPL), never updated
+    R xin = xhi;
     for (int k = S - 1; k > seg; --k) xin = sA[k][lane] * xin + sB[k][lane];
 #pragma unroll
     for (int i = 0; i < M; ++i)
@@ -658,11 +690,16 @@ size_t rbv_smem(const Sys<R>& q) {
 #define GFM_AVG_ROWS 8
 #endif
 constexpr int kAvgRows = GFM_AVG_ROWS;
+// second: average the pass-2 results X2B/X3B (else the pass-1 results X2/X3)
 template <typename R>
-__global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
+__global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep, int second) {
+    pdl_wait();
+    pdl_trigger();
     const Sys<R>& s = b.sys[blockIdx.y];
     if (sweep >= s.nim) return;
     const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const R* __restrict__ x2 = second ? w.x2b : w.x2;
+    const R* __restrict__ x3 = second ? w.x3b : w.x3;
     const int npl = rb_nplanes(s.ib, s.ie);
     const int npc = (npl - colour + 1) / 2;
     const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
@@ -678,7 +715,7 @@ __global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
         const int row = row0 + i;
         const int jj = row % nJ, kk = row / nJ;
         o[i] = hb + (kk * g.HY + jj) * g.PXH;
-        if (row < nJ * nK) { a[i] = w.x2[o[i]]; c[i] = w.x3[o[i]]; }
+        if (row < nJ * nK) { a[i] = x2[o[i]]; c[i] = x3[o[i]]; }
     }
 #pragma unroll
     for (int i = 0; i < kAvgRows; ++i)
@@ -688,6 +725,8 @@ __global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
 // split copy -> XT on the solve range
 template <typename R>
 __global__ void k_rbs_out(GeoT<R> g, RbBatch<R> b) {
+    pdl_wait();
+    pdl_trigger();
     const Sys<R>& s = b.sys[blockIdx.y];
     const AdiScratch<R>& w = b.scr[blockIdx.y];
     const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
@@ -798,27 +837,30 @@ int rb_segments(int n) {
     while (S < 32 && (S * RbSeg<R>::M < n || S < GFM_RB_MIN_SEGMENTS)) S *= 2;
     return S;
 }
-template <typename R, bool FIRST>
-void rb_pass_s(int S, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns, cudaStream_t st) {
+template <typename R, bool FIRST, bool AVG>
+void rb_pass_s(bool pdl, int S, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns, cudaStream_t st) {
     switch (S) {
-        case 1: k_rbs_pass<R, 1, FIRST><<<gp, 32, 0, st>>>(g, rb, colour, ns); break;
-        case 2: k_rbs_pass<R, 2, FIRST><<<gp, 64, 0, st>>>(g, rb, colour, ns); break;
-        case 4: k_rbs_pass<R, 4, FIRST><<<gp, 128, 0, st>>>(g, rb, colour, ns); break;
-        case 8: k_rbs_pass<R, 8, FIRST><<<gp, 256, 0, st>>>(g, rb, colour, ns); break;
-        case 16: k_rbs_pass<R, 16, FIRST><<<gp, 512, 0, st>>>(g, rb, colour, ns); break;
-        default: k_rbs_pass<R, 32, FIRST><<<gp, 1024, 0, st>>>(g, rb, colour, ns); break;
+        case 1: launch_k(pdl, k_rbs_pass<R, 1, FIRST, AVG>, gp, 32, 0, st, g, rb, colour, ns); break;
+        case 2: launch_k(pdl, k_rbs_pass<R, 2, FIRST, AVG>, gp, 64, 0, st, g, rb, colour, ns); break;
+        case 4: launch_k(pdl, k_rbs_pass<R, 4, FIRST, AVG>, gp, 128, 0, st, g, rb, colour, ns); break;
+        case 8: launch_k(pdl, k_rbs_pass<R, 8, FIRST, AVG>, gp, 256, 0, st, g, rb, colour, ns); break;
+        case 16: launch_k(pdl, k_rbs_pass<R, 16, FIRST, AVG>, gp, 512, 0, st, g, rb, colour, ns); break;
+        default: launch_k(pdl, k_rbs_pass<R, 32, FIRST, AVG>, gp, 1024, 0, st, g, rb, colour, ns); break;
     }
 }
+// pass L=1, or pass L=2 reading XT (avg false) or the pass L=1 average
 template <typename R>
-void rb_pass(int S, bool first, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns, cudaStream_t st) {
-    if (first) rb_pass_s<R, true>(S, gp, g, rb, colour, ns, st);
-    else rb_pass_s<R, false>(S, gp, g, rb, colour, ns, st);
+void rb_pass(bool pdl, int S, bool first, bool avg, dim3 gp, const GeoT<R>& g, const RbBatch<R>& rb, int colour, int ns,
+             cudaStream_t st) {
+    if (first) rb_pass_s<R, true, false>(pdl, S, gp, g, rb, colour, ns, st);
+    else if (avg) rb_pass_s<R, false, true>(pdl, S, gp, g, rb, colour, ns, st);
+    else rb_pass_s<R, false, false>(pdl, S, gp, g, rb, colour, ns, st);
 }
 
 // scratch buffers are passed through Sys-aligned array set by the host
 template <typename R>
 int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, int mode, cudaStream_t st,
-                      bool allow_fused) {
+                      int rb_flags) {
     AdiBatch<R> b;
     b.nsys = nsys;
     int max_np = 1, max_lines = 1;
@@ -859,7 +901,7 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
         auto blocks = [](long long n, int t) { long long b = (n + t - 1) / t; return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b)); };
         // fused plane visits when every system's plane fits in shared memory
         size_t smem = 0;
-        bool fused = allow_fused;
+        bool fused = (rb_flags & kRbFused) != 0;
         long long max_pm = 0;
         for (int e = 0; e < nsys; ++e) {
             const size_t sm = rbv_smem(sys[e]);
@@ -881,21 +923,23 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
             return 3 + 4 * nim;
         }
         const int S = rb_segments<R>(max_n);
-        k_rbs_in<R><<<dim3(blocks(max_class, 256), nsys), 256, 0, st>>>(g, rb);
-        k_rbs_factor<R><<<dim3(blocks(max_lines, 128), nsys), 128, 0, st>>>(g, rb);
+        const bool pdl = (rb_flags & kRbPdl) != 0;
+        const bool avg2 = (rb_flags & kRbAvgInPass) != 0;            // pass L=2 averages pass L=1
+        launch_k(pdl, k_rbs_in<R>, dim3(blocks(max_class, 256), nsys), 256, 0, st, g, rb);
+        launch_k(pdl, k_rbs_factor<R>, dim3(blocks(max_lines, 128), nsys), 128, 0, st, g, rb);
         // line slots of one colour: ceil(planes/2) x (nK + nJ), 32 per block
         const dim3 gp((unsigned)((max_slots + 31) / 32), nsys);
         const dim3 ga((unsigned)((max_np + 1) / 2 + 31) / 32, nsys, (unsigned)((max_rows + 8 * kAvgRows - 1) / (8 * kAvgRows)));
         for (int ns = 0; ns < nim; ++ns)
             for (int half = 0; half < 2; ++half)
                 for (int colour = 0; colour < 2; ++colour) {
-                    rb_pass<R>(S, true, gp, g, rb, colour, ns, st);
-                    k_rbs_avg<R><<<ga, dim3(32, 8), 0, st>>>(g, rb, colour, ns);
-                    rb_pass<R>(S, false, gp, g, rb, colour, ns, st);
-                    k_rbs_avg<R><<<ga, dim3(32, 8), 0, st>>>(g, rb, colour, ns);
+                    rb_pass<R>(pdl, S, true, false, gp, g, rb, colour, ns, st);
+                    if (!avg2) launch_k(pdl, k_rbs_avg<R>, ga, dim3(32, 8), 0, st, g, rb, colour, ns, 0);
+                    rb_pass<R>(pdl, S, false, avg2, gp, g, rb, colour, ns, st);
+                    launch_k(pdl, k_rbs_avg<R>, ga, dim3(32, 8), 0, st, g, rb, colour, ns, 1);
                 }
-        k_rbs_out<R><<<dim3(blocks(max_cells, 256), nsys), 256, 0, st>>>(g, rb);
-        return 3 + 16 * nim;
+        launch_k(pdl, k_rbs_out<R>, dim3(blocks(max_cells, 256), nsys), 256, 0, st, g, rb);
+        return 3 + (avg2 ? 12 : 16) * nim;
     }
 }
 
@@ -927,8 +971,8 @@ template void launch_refine_add<double>(const GeoT<double>&, const Sys<double>&,
 template void launch_residual<double>(const Ctx<double>&, const Sys<double>&, int, cudaStream_t);
 template void launch_residual<float>(const Ctx<float>&, const Sys<float>&, int, cudaStream_t);
 template int launch_adlbl3_scr<double>(const GeoT<double>&, const Sys<double>*, const AdiScratch<double>*, int, int,
-                                       cudaStream_t, bool);
+                                       cudaStream_t, int);
 template int launch_adlbl3_scr<float>(const GeoT<float>&, const Sys<float>*, const AdiScratch<float>*, int, int, cudaStream_t,
-                                      bool);
+                                      int);
 
 }  // namespace gfm

@@ -50,6 +50,34 @@ __host__ __device__ __forceinline__ long long pidx(const GeoT<R>& g, int I, int 
 template <typename R>
 __device__ __forceinline__ int IBC(const GeoT<R>& g, int I, int J, int K) { return g.ib[pidx(g, I, J, K)]; }
 
+// Programmatic dependent launch.  A kernel launched by launch_k with pdl set
+// may begin (block scheduling, prologue) while the kernel before it in the
+// stream is still finishing.  pdl_wait() returns once that kernel has
+// completed and its writes are visible, so every kernel launched this way
+// calls it before it touches global memory; completion is then transitive
+// along the chain.  pdl_trigger() lets the next kernel begin launching.  Both
+// are no-ops in a kernel launched without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+inline void launch_k(bool pdl, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args... args) {
+    if (!pdl) {
+        k<<<grid, block, smem, st>>>(args...);
+        return;
+    }
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // Scalar constants of the run (gfm_params plus derived complements).
 struct Prm {
     double t0, h_0, dnst0, ug0, gmfr, pg0, r0;

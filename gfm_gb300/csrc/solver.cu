@@ -84,7 +84,8 @@ struct gfm_handle {
     gfm::lp::Net* lp = nullptr;
     void* lp_feats = nullptr;           // BF16 inputs, 16 channels per voxel
     int lp_nx = 0, lp_ny = 0, lp_nz = 0;
-    bool rb_fused = false;              // red-black order: fused plane visits (GFM_RB_FUSED=1)
+    int rb_flags = kRbPdl | kRbAvgInPass;   // red-black options (environment at create): GFM_RB_FUSED=1 adds
+                                            // kRbFused; GFM_PDL=0 drops kRbPdl; GFM_RB_AVG_IN_PASS=0 drops kRbAvgInPass
 };
 
 namespace {
@@ -419,7 +420,7 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
                 return rc;
         } else {
             const long long NH = 2LL * g.CBH;
-            R** arrs[] = {&w.xs, &w.x2, &w.x3, &w.sby, &w.sbz};
+            R** arrs[] = {&w.xs, &w.x2, &w.x3, &w.sby, &w.sbz, &w.x2b, &w.x3b};
             for (R** a : arrs) if ((rc = dalloc(h, a, NH))) return rc;
             Quad<R>** quads[] = {&w.ya, &w.yb, &w.za, &w.zb};
             for (Quad<R>** a : quads) if ((rc = dalloc(h, a, NH))) return rc;
@@ -472,7 +473,7 @@ template <typename R>
 void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>* scr, int nsys, cudaStream_t st) {
     // external records: inside a captured graph these become real event nodes
     if (h->n_ev + 2 <= 16) cudaEventRecordWithFlags(h->ev[h->n_ev], st, cudaEventRecordExternal);
-    const int launched = launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st, h->rb_fused);
+    const int launched = launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st, h->rb_flags);
     if (h->n_ev + 2 <= 16) { cudaEventRecordWithFlags(h->ev[h->n_ev + 1], st, cudaEventRecordExternal); h->n_ev += 2; }
     int nim = 0;
     for (int e = 0; e < nsys; ++e) {
@@ -778,7 +779,10 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     if (prepare_line_solver() != GFM_OK) { h->err = "cannot raise the line solver's shared-memory limit"; return GFM_E_CUDA; }
     {
         const char* fz = std::getenv("GFM_RB_FUSED");
-        h->rb_fused = fz && fz[0] == '1';
+        const char* pd = std::getenv("GFM_PDL");
+        const char* ap = std::getenv("GFM_RB_AVG_IN_PASS");
+        h->rb_flags = (fz && fz[0] == '1' ? kRbFused : 0) | (pd && pd[0] == '0' ? 0 : kRbPdl) |
+                      (ap && ap[0] == '0' ? 0 : kRbAvgInPass);
     }
     cudaEventCreate(&h->ev_adi0);
     cudaEventCreate(&h->ev_adi1);
@@ -1098,7 +1102,7 @@ int adlbl3_user(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, double* xt, const 
     if ((rc = put(xt, c.FZ)) || (rc = put(ap, c.APm)) || (rc = put(bs, c.BSm))) return rc;
     for (int q = 0; q < 6; ++q) if ((rc = put(as[q], c.ASm[q]))) return rc;
     Sys<R> s = sys_of<R>(c.FZ, c.APm, c.ASm, c.BSm, ib, ie, jb, je, kb, ke, nim);
-    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_fused);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_flags);
     launch_from_split(g, c.FZ, h->d_stage, st);
     CK(cudaMemcpyAsync(xt, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -1129,7 +1133,7 @@ int pcorr_sample(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr, int nsweeps, void
     R* asc[6];
     for (int q = 0; q < 6; ++q) asc[q] = c.ASc[q];
     Sys<R> s = sys_of<R>(c.DPc, c.APc, asc, c.BSq, 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, nsweeps);
-    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_fused);
+    launch_adlbl3_scr(g, &s, scr, 1, h->adi_mode, st, h->rb_flags);
     launch_lp_target(c, c.DPc, target, nx, ny, nz, st);
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());

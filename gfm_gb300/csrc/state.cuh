@@ -103,7 +103,7 @@ struct __align__(4 * sizeof(R)) Quad { R x, y, z, w; };
 template <typename R>
 struct AdiScratch {
     R *xt2, *xt3, *pty, *ptz;
-    R *xs, *x2, *x3, *sby, *sbz;
+    R *xs, *x2, *x3, *sby, *sbz, *x2b, *x3b;
     Quad<R> *ya, *yb, *za, *zb;
 };
 
@@ -132,10 +132,15 @@ template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
 template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
 template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);
+// red-black line-solver options: kRbFused uses the fused plane visit where the
+// planes fit in shared memory; kRbPdl launches the segmented passes, averages
+// and copies with programmatic dependent launch; kRbAvgInPass lets pass L=2
+// average the pass L=1 results where it reads them, in place of the averaging
+// launch between the passes
+constexpr int kRbFused = 1, kRbPdl = 2, kRbAvgInPass = 4;
 // returns the number of kernels it launched
-// allow_fused: use the fused plane visit where the planes fit in shared memory
 template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
-                                            int mode, cudaStream_t s, bool allow_fused);
+                                            int mode, cudaStream_t s, int rb_flags);
 int prepare_line_solver();   // once per process, before any stream capture
 // deterministic finish of block partials: op 0 sum, 1 max, 2 residual
 // (sum/NCELLS floored at 1e-16, NaN -> 1e-16), 3 sum/NCELLS

@@ -44,3 +44,23 @@ def test_redblack_converges_to_manufactured_solution(prec, tol, fused, monkeypat
     err = np.abs(x - sol)[open_].max() / np.abs(sol[open_]).max()
     assert err < tol, err
     g.close()
+
+
+@pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])
+@pytest.mark.parametrize("cls", [(0, 0, 0), (0, 1, 1)])
+def test_redblack_launch_forms_agree_bit_for_bit(prec, cls, monkeypatch):
+    """Pass L=2 averaging the pass L=1 results where it reads them (default)
+    and the separate averaging launch compute the same values in the same
+    order, with and without programmatic dependent launch: identical
+    iterates."""
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
+    out = []
+    for avg, pdl in (("1", "1"), ("0", "1"), ("1", "0"), ("0", "0")):
+        monkeypatch.setenv("GFM_RB_AVG_IN_PASS", avg)
+        monkeypatch.setenv("GFM_PDL", pdl)
+        g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+        out.append(g.adlbl3(x0, ap, as6, bs, *rng, 5))
+        g.close()
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
