@@ -111,6 +111,19 @@ class GfmIterStats(C.Structure):
         return out
 
 
+class GfmRadTotals(C.Structure):
+    _fields_ = [
+        ("qe_sum_from_open", C.c_double), ("qa_sum_to_open", C.c_double),
+        ("qa_sum_to_wall", C.c_double), ("qa_sum_to_inlet", C.c_double), ("qa_sum_to_exit", C.c_double),
+        ("qa_sum_to_melt", C.c_double),
+        ("tot_qe_h2o_co2", C.c_double), ("tot_qe_soot", C.c_double),
+        ("n_emitters", C.c_int), ("reserved", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
+
+
 class GfmInletSpec(C.Structure):
     _fields_ = [
         ("y0", C.c_double), ("y1", C.c_double), ("z0", C.c_double), ("z1", C.c_double),
@@ -163,6 +176,7 @@ SIGNATURES = [
     ("gfm_gpu_adlbl3", C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(_dp), _dp,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("gfm_gpu_rad_emission", C.c_int, [C.c_void_p]),
+    ("gfm_gpu_rad_transfer", C.c_int, [C.c_void_p, C.POINTER(GfmRadTotals)]),
     ("gfm_gpu_kernel_times", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     ("gfm_gpu_reset_kernel_times", C.c_int, [C.c_void_p]),
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),

@@ -18,7 +18,10 @@ BUILD = PKG / "_build"
 LIB = PKG / "libgfm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["asm.cu", "adi.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lp_tc.cu", "lpsolve.cu"]
+CUDA_SOURCES = ["asm.cu", "adi.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lp_tc.cu", "lpsolve.cu", "rad.cu"]
+# per-file flags: the radiation transfer rounds every product and sum as the
+# reference does (angle ties and energy splits must break the same way)
+FILE_FLAGS = {"rad.cu": ["--fmad=false"]}
 CXX_SOURCES = ["case_build.cpp"]
 
 
@@ -51,8 +54,8 @@ def build(verbose: bool = False, force: bool = False) -> pathlib.Path:
         src, obj = CSRC / s, BUILD / (s + ".o")
         if force or _needs(obj, src):
             extra = os.environ.get("GFM_NVCC_EXTRA", "").split()
-            jobs.append([cc, "-std=c++17", *ARCH, "-O3", "-lineinfo", *extra, "-Xcompiler", "-fPIC",
-                         "-c", str(src), "-o", str(obj)])
+            jobs.append([cc, "-std=c++17", *ARCH, "-O3", "-lineinfo", *FILE_FLAGS.get(s, []), *extra,
+                         "-Xcompiler", "-fPIC", "-c", str(src), "-o", str(obj)])
     for s in CXX_SOURCES:
         src, obj = CSRC / s, BUILD / (s + ".o")
         if force or _needs(obj, src):

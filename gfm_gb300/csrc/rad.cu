@@ -1,0 +1,612 @@
+// rad.cu -- volume radiation transfer on the device: the volume part of
+// RAD_EMIS (combustion/Code/Rad_emis.f90:120-377).
+//
+//   k_rad_mark    wall markers: IBCELL 1 -> 101..311 where a neighbour is open
+//                 (Rad_emis.f90:144-178), on a cell map of its own
+//   k_rad_akl     RAD0 with ID_RAD=10 (Rad0.f90:112-166): AKL = EMF(AKL0, OPL)
+//                 of the hot open cells, band-emission totals
+//   k_rad_trace   the QRNF emitter loop (Qrn.f90:58-154) with QREF
+//                 (Qre.f90:31-515) and QRTX/QRTY/QRTZ (Qrtx.f90:15-209,
+//                 Qrty.f90:9-224, Qrtz.f90:15-234)
+//   k_rad_reduce  QAL summed over the blocks, QA = sum over bands (QRN1,
+//                 Qrn.f90:250-259)
+//
+// One CTA traces one emitter at a time (cells in the reference's loop order,
+// a grid-stride over the emitters); emitters are independent, so the CTAs of
+// the grid trace different emitters at once.  Within an emitter the reference
+// is sequential; the CTA keeps its order where it matters:
+//   * the slab arrays QTX1, QTX2, Q2M and their flags live in shared memory
+//     (global scratch when they do not fit);
+//   * the far-face angles of a slab (SANG2), the reference's outward scan
+//     with its early exit, are run by one thread per transverse axis;
+//   * the spread across the first transverse axis (part 1 of QRTX/Y/Z) touches
+//     only its own row of the slab arrays: one thread per row, the reference's
+//     order inside the row;
+//   * the spread across the second transverse axis (part 2) touches only its
+//     own column, except for the wall-corner split, which in a box reaches
+//     only from the first and the last column into their neighbour.  So the
+//     first column runs alone, then the interior columns in parallel, then
+//     the last column: every slab-array element receives its additions in the
+//     reference's order.  An interior column that reaches a corner split (an
+//     obstacle inside the box, or the reference's undefined case on the
+//     emitter's own column) is reported as unsupported;
+//   * absorption into the slab's cells is per cell.
+// QAL is accumulated per CTA in its own copy (fixed emitter order) and the
+// copies are summed in CTA order, so the result is deterministic; it differs
+// from the reference's single running sum only by the association of the
+// additions.
+//
+// Angles come from rad_atand, the same operations as the oracle's ATAND; this
+// translation unit is compiled with --fmad=false so that no multiply-add is
+// fused where the reference rounds twice, and angle ties break the same way.
+#include "state.cuh"
+
+namespace gfm {
+namespace {
+
+constexpr double kSmall16 = 1.0e-16;
+constexpr double kTgMn = 300.0;     // TG_MN (Rad0.f90:42)
+constexpr int kRadThreads = 128;
+
+// atan(x) in degrees: reduction to [0,1] by atan(x) = pi/2 - atan(1/x), to
+// [0, tan(pi/12)] by atan(a) = pi/6 + atan((a*sqrt(3)-1)/(a+sqrt(3)))
+// (Abramowitz & Stegun 4.4.34), Maclaurin series to t^29 (A&S 4.4.42) by
+// Horner's rule in t^2 with fused multiply-adds.
+__device__ double rad_atand(double x) {
+    const double PI = 3.14159265358979323846;
+    const double SQRT3 = 1.73205080756887729353;
+    const double TAN_PI_12 = 0.26794919243112270647;
+    double a = fabs(x);
+    const bool inv = a > 1.0;
+    if (inv) a = 1.0 / a;
+    const bool sh = a > TAN_PI_12;
+    if (sh) a = (a * SQRT3 - 1.0) / (a + SQRT3);
+    const double z = a * a;
+    double p = 1.0 / 29.0;
+#pragma unroll
+    for (int n = 13; n >= 0; --n) p = fma(p, z, ((n & 1) ? -1.0 : 1.0) / (double)(2 * n + 1));
+    double r = a * p;
+    if (sh) r = PI / 6.0 + r;
+    if (inv) r = PI / 2.0 - r;
+    const double d = r * (180.0 / PI);
+    return x < 0.0 ? -d : d;
+}
+
+__global__ void k_rad_mark(RadArgs a) {
+    const int n = a.MZ * a.NZ * a.LZ;
+    GFM_FOR(c, n) {
+        const int I = 2 * (c % a.MZ + 1), J = 2 * ((c / a.MZ) % a.NZ + 1), K = 2 * (c / (a.MZ * a.NZ) + 1);
+        auto ibc = [&](int i, int j, int k) { return (int)a.g.ib[pidx(a.g, i, j, k)]; };
+        int v = ibc(I, J, K);
+        if (v == 1) {
+            const int KM2 = max(K - 2, 2), KP2 = min(K + 2, a.LP);
+            const int JM2 = max(J - 2, 2), JP2 = min(J + 2, a.NP);
+            const int IM2 = max(I - 2, 2), IP2 = min(I + 2, a.MP);
+            if (ibc(I, J, KM2) <= 0) v = 301;
+            else if (ibc(I, J, KP2) <= 0) v = 311;
+            else if (ibc(I, JM2, K) <= 0) v = 201;
+            else if (ibc(I, JP2, K) <= 0) v = 211;
+            else if (ibc(IM2, J, K) <= 0) v = 101;
+            else if (ibc(IP2, J, K) <= 0) v = 111;
+        }
+        a.ibr[c] = (int16_t)v;
+    }
+}
+
+__device__ void rad_debx(const RadArgs& a, double t, double* deb) {   // DEBX, Rad_fun.f90:83-101
+    double eb0 = 0.0;
+    for (int l = 1; l <= a.NWL - 1; ++l) {
+        const double x1 = a.deb0[l - 1] / t;
+        const double eb1 = rif3(x1);
+        deb[l - 1] = eb1 - eb0;
+        if (deb[l - 1] <= 1.0e-3) deb[l - 1] = 0.0; else eb0 = eb1;
+    }
+    deb[a.NWL - 1] = 1.0 - eb0;
+}
+
+// RAD0 (ID_RAD=10), gray bands: AKLG = AKL0, AKLS = 0.  Also the cell
+// temperature in kelvin (T*T0), the one the transfer reads.  Block partials of
+// the two band-emission totals are summed on the host in block order.
+template <typename R>
+__global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict__ T) {
+    __shared__ double sh[2][256];
+    const int n = a.MZ * a.NZ * a.LZ;
+    double sg_tot = 0.0, ss_tot = 0.0;
+    GFM_FOR(c, n) {
+        const int I = 2 * (c % a.MZ + 1), J = 2 * ((c / a.MZ) % a.NZ + 1), K = 2 * (c / (a.MZ * a.NZ) + 1);
+        const double t = (double)T[pidx(a.g, I, J, K)] * a.t0;
+        a.tcell[c] = t;
+        for (int l = 0; l < a.NWL; ++l) a.akl[c + (long long)l * n] = 0.0;
+        if (!(a.ibr[c] <= 0 && t >= kTgMn)) continue;
+        const double dx = a.g.DX[I], dr = a.g.DR[J], dz = a.g.DZ[K];
+        const double vol = dx * dr * a.g.RS[J] * dz;                  // VOL_C at a cell centre (VOL_C0)
+        const double sa = ((dx * dr) + (dr * dz) + (dx * dz)) * 2.0;
+        if (sa <= kSmall16) continue;
+        const double opl = 6.0 * vol / sa;
+        if (opl <= 1.0e-10) continue;
+        double deb[kRadMaxBands];
+        rad_debx(a, t, deb);
+        const double t2 = t * t;
+        const double area_sgn_t4 = sa * a.sgn * (t2 * t2);
+        double sg = 0.0, ss = 0.0;
+        for (int l = 0; l < a.NWL; ++l) {
+            a.akl[c + (long long)l * n] = emf(a.akl0[l], opl);
+            sg = sg + deb[l] * emf(a.akl0[l], opl);
+            ss = ss + deb[l] * emf(0.0, opl);
+        }
+        sg_tot += area_sgn_t4 * sg;
+        ss_tot += area_sgn_t4 * ss;
+    }
+    sh[0][threadIdx.x] = sg_tot;
+    sh[1][threadIdx.x] = ss_tot;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) { sh[0][threadIdx.x] += sh[0][threadIdx.x + s]; sh[1][threadIdx.x] += sh[1][threadIdx.x + s]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { a.akl_part[2 * blockIdx.x] = sh[0][0]; a.akl_part[2 * blockIdx.x + 1] = sh[1][0]; }
+}
+
+// One march direction of QREF: d = slab axis, u = first transverse axis (the
+// part-1 spread, the part-2 columns), v = second (the part-1 rows, the part-2
+// spread).  x-flux: u = y, v = z (QRTX); y-flux: u = x, v = z (QRTY); z-flux:
+// u = x, v = y (QRTZ).  Slab arrays are indexed e = (v/2-1)*DA + (u/2-1).
+struct Dir {
+    int d, u, v;
+    int Dd, Du, Dv, DA, DB, A;
+    int d0, u0, v0;
+    int sd, su, sv;              // cell-index strides of the three axes
+    const double *cd, *cu, *cv;  // coordinates (shared-memory copies, 1-based)
+    double *angU1, *angU2, *angV1, *angV2;   // ANG(.,1), ANG(.,2) of u and v (1-based)
+    int direct1, direct2;        // IBCELL codes deposited whole in part 2 (and 4)
+};
+
+struct Slab {   // scratch of one CTA
+    double *q1, *q2, *qm;        // QTX1, QTX2, Q2M: [l*A + e]
+    unsigned char *f1, *f2, *fm; // IQT1, IQT2, IQTM
+};
+
+__device__ __forceinline__ bool rad_corner(int d, int ibc1) {
+    return d == 0 ? ibc1 > 100 : (d == 1 ? ibc1 >= 100 : ibc1 > 1);
+}
+
+template <int NW>
+__device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int slab, int v1, double ang0u) {
+    const int NWL = NW > 0 ? NW : a.NWL;
+    double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
+    const int bb = v1 / 2;
+    const int cbase = (slab / 2 - 1) * D.sd + (v1 / 2 - 1) * D.sv;
+    for (int UPM = -2; UPM <= 2; UPM += 4) {
+        double A11 = 0.0, A12 = 0.0;
+        const int uend = UPM < 0 ? 2 : D.Du;
+        for (int u1 = D.u0; UPM > 0 ? u1 <= uend - UPM : u1 >= uend - UPM; u1 += UPM) {
+            if (A11 >= ang0u) break;
+            const int u12 = u1 + UPM / 2;
+            A12 = D.angU1[u12];
+            const double DANG = A12 - A11;
+            if (DANG <= 1.0e-10) { A11 = A12; continue; }
+            double A21 = A11;
+            const int e = (bb - 1) * D.DA + (u1 / 2 - 1);
+            if (S.f1[e]) { A11 = A12; continue; }
+            if (u1 == D.u0) {
+                for (int l = 0; l < NWL; ++l) Q11[l] = S.q1[l * D.A + e] * 0.5;
+                if (UPM > 0) for (int l = 0; l < NWL; ++l) S.q1[l * D.A + e] = 0.0;
+            } else {
+                for (int l = 0; l < NWL; ++l) { Q11[l] = S.q1[l * D.A + e]; S.q1[l * D.A + e] = 0.0; }
+            }
+            if (u1 != D.u0 || UPM > 0) S.f1[e] = 1;
+            for (int l = 0; l < NWL; ++l) Q12[l] = Q11[l];
+            for (int u2 = u1; UPM > 0 ? u2 <= uend : u2 >= uend; u2 += UPM) {
+                const int e2 = (bb - 1) * D.DA + (u2 / 2 - 1);
+                if (a.ibr[cbase + (u2 / 2 - 1) * D.su] < 1) {
+                    const double A22 = D.angU2[u2 + UPM / 2];
+                    if (A22 <= A21) continue;
+                    if (A22 < A12) {
+                        const double FIJ = (A22 - A21) / DANG;
+                        for (int l = 0; l < NWL; ++l) {
+                            if (Q11[l] < kSmall16) continue;
+                            const double Q21 = Q11[l] * FIJ;
+                            S.qm[l * D.A + e2] = S.qm[l * D.A + e2] + Q21;
+                            Q12[l] = Q12[l] - Q21;
+                        }
+                        S.fm[e2] = 0;
+                        A21 = A22;
+                        continue;
+                    }
+                }
+                for (int l = 0; l < NWL; ++l) S.qm[l * D.A + e2] = S.qm[l * D.A + e2] + Q12[l];
+                S.fm[e2] = 0;
+                break;
+            }
+            A11 = A12;
+        }
+    }
+}
+
+template <int NW>
+__device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int slab, int u1, double ang0v, int* err) {
+    const int NWL = NW > 0 ? NW : a.NWL;
+    double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
+    const int aa = u1 / 2;
+    const int cbase = (slab / 2 - 1) * D.sd + (u1 / 2 - 1) * D.su;
+    const bool edge = u1 == 2 || u1 == D.Du;
+    for (int KM = -2; KM <= 2; KM += 4) {
+        double A11 = 0.0, A12 = 0.0;
+        const int vend = KM < 0 ? 2 : D.Dv;
+        for (int v1 = D.v0; KM > 0 ? v1 <= vend - KM : v1 >= vend - KM; v1 += KM) {
+            if (A11 >= ang0v) break;
+            const int v12 = v1 + KM / 2;
+            A12 = D.angV1[v12];
+            const double DANG = A12 - A11;
+            if (DANG <= 1.0e-10) { A11 = A12; continue; }
+            double A21 = A11;
+            const int e = (v1 / 2 - 1) * D.DA + (aa - 1);
+            if (S.fm[e]) { A11 = A12; continue; }
+            if (v1 == D.v0) {
+                for (int l = 0; l < NWL; ++l) Q11[l] = S.qm[l * D.A + e] * 0.5;
+                if (KM > 0) for (int l = 0; l < NWL; ++l) S.qm[l * D.A + e] = 0.0;
+            } else {
+                for (int l = 0; l < NWL; ++l) { Q11[l] = S.qm[l * D.A + e]; S.qm[l * D.A + e] = 0.0; }
+            }
+            if (v1 != D.v0 || KM > 0) S.fm[e] = 1;
+            const int ibc1 = a.ibr[cbase + (v1 / 2 - 1) * D.sv];
+            if (ibc1 == D.direct1 || ibc1 == D.direct2 || ibc1 == 4) {
+                for (int l = 0; l < NWL; ++l) S.q2[l * D.A + e] = S.q2[l * D.A + e] + Q11[l];
+                S.f2[e] = 0;
+                A11 = A12;
+                continue;
+            }
+            for (int l = 0; l < NWL; ++l) Q12[l] = Q11[l];
+            for (int v2 = v1; KM > 0 ? v2 <= vend : v2 >= vend; v2 += KM) {
+                const int v2m = v2 + KM / 2;
+                const int e2 = (v2 / 2 - 1) * D.DA + (aa - 1);
+                const int ibc2 = a.ibr[cbase + (v2 / 2 - 1) * D.sv];
+                bool to330 = ibc1 <= 0 && ibc2 >= 1;
+                if (!to330) {
+                    if (rad_corner(D.d, ibc1) && ibc2 == 1) {
+                        if (!edge) atomicOr(err, 1);   // interior corner split: outside the supported geometry
+                        const int ut = u1 < D.u0 ? u1 + 2 : u1 - 2;
+                        const int et = (v2 / 2 - 1) * D.DA + (ut / 2 - 1);
+                        const int e2m = (v2 / 2 - KM / 2 - 1) * D.DA + (aa - 1);
+                        for (int l = 0; l < NWL; ++l) {
+                            if (Q12[l] < kSmall16) continue;
+                            const double Q21 = Q12[l] * 0.5;
+                            S.q2[l * D.A + et] = S.q2[l * D.A + et] + Q21;
+                            S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
+                        }
+                        S.f2[et] = 0;
+                        S.f2[e2m] = 0;
+                        break;
+                    }
+                    if (v2m > D.Dv || v2m < 2) {
+                        to330 = true;
+                    } else {
+                        const double A22 = D.angV2[v2m];
+                        if ((A22 - A21) <= 1.0e-10) continue;
+                        if (A22 < A12) {
+                            const double FIJ = (A22 - A21) / DANG;
+                            for (int l = 0; l < NWL; ++l) {
+                                if (Q11[l] < kSmall16) continue;
+                                const double Q21 = Q11[l] * FIJ;
+                                S.q2[l * D.A + e2] = S.q2[l * D.A + e2] + Q21;
+                                Q12[l] = Q12[l] - Q21;
+                            }
+                            S.f2[e2] = 0;
+                            A21 = A22;
+                            continue;
+                        }
+                    }
+                }
+                for (int l = 0; l < NWL; ++l) S.q2[l * D.A + e2] = S.q2[l * D.A + e2] + Q12[l];
+                S.f2[e2] = 0;
+                break;
+            }
+            A11 = A12;
+        }
+    }
+}
+
+// Is row v1 (part 1) / column u1 (part 2) visited?  The reference skips the
+// rows before the emitter whose near angle is outside the cone and stops at
+// the first such row after it.
+__device__ __forceinline__ bool rad_visit(const double* ang2, int p, int p0, double ang0) {
+    if (p < p0) return !(ang2[p + 1] >= ang0);
+    for (int q = p0 + 2; q <= p; q += 2)
+        if (ang2[q - 1] >= ang0) return false;
+    return true;
+}
+
+struct RadAcc {   // per-thread sums of the deposits by destination
+    double melt, exit, inlet, wall, open;
+};
+
+template <int NW>
+__device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* qalp, const double* qel1,
+                              double* qel, double* ang0, RadAcc& acc, int* err) {
+    const int NWL = NW > 0 ? NW : a.NWL;
+    const int n = a.MZ * a.NZ * a.LZ;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    // ALLOCATE and initialise the slab arrays of this direction
+    for (int i = tid; i < D.A * NWL; i += nth) { S.q1[i] = 0.0; S.q2[i] = 0.0; S.qm[i] = 0.0; }
+    for (int i = tid; i < D.A; i += nth) { S.f1[i] = 1; S.f2[i] = 1; S.fm[i] = 1; }
+    __syncthreads();
+    const int e0 = (D.v0 / 2 - 1) * D.DA + (D.u0 / 2 - 1);
+    for (int s = -1; s <= 1; s += 2) {
+        if (tid == 0) {
+            for (int l = 0; l < NWL; ++l) S.q1[l * D.A + e0] = qel1[l];
+            S.f1[e0] = 0;
+            for (int l = 0; l < NWL; ++l) qel[l] = qel[l] + qel1[l];
+            // SANG1 for an open cell
+            const double b = fabs(D.cd[D.d0 + s] - D.cd[D.d0]);
+            if (b < kSmall16) { ang0[0] = 90.0; ang0[1] = 90.0; }
+            else {
+                ang0[0] = rad_atand(fabs(D.cu[D.u0 + s] - D.cu[D.u0]) / b);
+                ang0[1] = rad_atand(fabs(D.cv[D.v0 + s] - D.cv[D.v0]) / b);
+            }
+        }
+        __syncthreads();
+        const double ang0u = ang0[0], ang0v = ang0[1];
+        for (int p = 1 + tid; p <= D.Du; p += nth) { D.angU1[p] = ang0u; D.angU2[p] = ang0u; }
+        for (int p = 1 + tid; p <= D.Dv; p += nth) { D.angV1[p] = ang0v; D.angV2[p] = ang0v; }
+        __syncthreads();
+        if (tid == 0) { D.angU1[D.u0] = 0.0; D.angU2[D.u0] = 0.0; D.angV1[D.v0] = 0.0; D.angV2[D.v0] = 0.0; }
+        __syncthreads();
+        const int dend = s < 0 ? 2 : D.Dd;
+        for (int slab = D.d0 + 2 * s; s > 0 ? slab <= dend : slab >= dend; slab += 2 * s) {
+            // SANG2: far-face angles of the slab, the outward scan with its
+            // exit, one thread per transverse axis
+            int far = slab + s;
+            far = min(far, D.Dd);
+            const double b = fabs(D.cd[far] - D.cd[D.d0]);
+            if (tid == 0 || tid == 32) {
+                const bool isu = tid == 0;
+                const int P = isu ? D.Du : D.Dv, p0 = isu ? D.u0 : D.v0;
+                const double* c = isu ? D.cu : D.cv;
+                double* out = isu ? D.angU2 : D.angV2;
+                const double lim = isu ? ang0u : ang0v;
+                for (int M = -1; M <= 1; M += 2) {
+                    const int pend = M < 0 ? 2 : P;
+                    for (int pp = p0 + M; M > 0 ? pp <= pend : pp >= pend; pp += 2 * M) {
+                        const double aa = b < kSmall16 ? 90.0 : rad_atand(fabs(c[pp] - c[p0]) / b);
+                        if (aa >= lim) break;
+                        out[pp] = aa;
+                    }
+                }
+            }
+            __syncthreads();
+            // part 1: one thread per row
+            {
+                const int nrows = (D.Dv - 4) / 2;   // rows 4 .. Dv-2
+                for (int r = tid; r < nrows; r += nth) {
+                    const int v1 = 4 + 2 * r;
+                    if (rad_visit(D.angV2, v1, D.v0, ang0v)) part1_row<NW>(a, D, S, slab, v1, ang0u);
+                }
+            }
+            __syncthreads();
+            // part 2: first column, interior columns, last column
+            if (tid == 0 && rad_visit(D.angU2, 2, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, 2, ang0v, err);
+            __syncthreads();
+            {
+                const int ncols = (D.Du - 4) / 2;   // columns 4 .. Du-2
+                for (int r = tid; r < ncols; r += nth) {
+                    const int u1 = 4 + 2 * r;
+                    if (rad_visit(D.angU2, u1, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, u1, ang0v, err);
+                }
+            }
+            __syncthreads();
+            if (tid == 0 && rad_visit(D.angU2, D.Du, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err);
+            __syncthreads();
+            // absorption in the slab's cells
+            const bool end = slab == dend;
+            for (int e = tid; e < D.A; e += nth) {
+                if (S.f2[e]) continue;
+                const int ua = e % D.DA + 1, vb = e / D.DA + 1;
+                const int c = (slab / 2 - 1) * D.sd + (ua - 1) * D.su + (vb - 1) * D.sv;
+                const int ib = a.ibr[c];
+                for (int l = 0; l < NWL; ++l) {
+                    const double q = S.q2[l * D.A + e];
+                    if (q < kSmall16) continue;
+                    double* qa = qalp + c + (long long)l * n;
+                    if (ib >= 1 || end) {
+                        *qa = *qa + q;
+                        if (ib == 4) acc.melt += q;
+                        else if (ib == 3) acc.exit += q;
+                        else if (ib == 2) acc.inlet += q;
+                        else acc.wall += q;
+                    } else {
+                        const double qa0 = q * a.akl[c + (long long)l * n];
+                        *qa = *qa + qa0;
+                        S.q1[l * D.A + e] = q - qa0;
+                        S.f1[e] = 0;
+                        acc.open += qa0;
+                    }
+                    S.q2[l * D.A + e] = 0.0;
+                    S.f2[e] = 1;
+                }
+            }
+            __syncthreads();
+            for (int p = 1 + tid; p <= D.Du; p += nth) D.angU1[p] = D.angU2[p];
+            for (int p = 1 + tid; p <= D.Dv; p += nth) D.angV1[p] = D.angV2[p];
+            __syncthreads();
+        }
+    }
+}
+
+template <int NW>
+__global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a) {
+    extern __shared__ __align__(16) unsigned char rad_smem[];
+    __shared__ double s_deb[kRadMaxBands], s_qel0[kRadMaxBands], s_qel1[kRadMaxBands], s_qel[kRadMaxBands];
+    __shared__ double s_ang0[2];
+    __shared__ double s_red[kRadThreads];
+    const int NWL = NW > 0 ? NW : a.NWL;
+    const int n = a.MZ * a.NZ * a.LZ;
+    const int tid = threadIdx.x;
+    // shared layout: coordinates X(1..MP), R(1..NP), Z(1..LP); ANG1/2/3 (two
+    // columns each); then the slab arrays (here or in global scratch)
+    double* sx = reinterpret_cast<double*>(rad_smem);
+    double* sr = sx + (a.MP + 2);
+    double* sz = sr + (a.NP + 2);
+    double* ang = sz + (a.LP + 2);
+    double* ang1 = ang;                          // ANG1(.,1), ANG1(.,2)
+    double* ang2 = ang1 + 2 * (a.MP + 2);
+    double* ang3 = ang2 + 2 * (a.NP + 2);
+    double* arr = ang3 + 2 * (a.LP + 2);
+    Slab S;
+    if (a.slab_in_smem) {
+        S.q1 = arr;
+    } else {
+        S.q1 = a.scratch + (long long)blockIdx.x * 3 * a.A * NWL;
+    }
+    S.q2 = S.q1 + (long long)a.A * NWL;
+    S.qm = S.q2 + (long long)a.A * NWL;
+    unsigned char* flags = a.slab_in_smem ? reinterpret_cast<unsigned char*>(S.qm + (long long)a.A * NWL)
+                                          : a.fscratch + (long long)blockIdx.x * 3 * a.A;
+    S.f1 = flags;
+    S.f2 = flags + a.A;
+    S.fm = flags + 2 * a.A;
+    for (int i = 1 + tid; i <= a.MP; i += blockDim.x) sx[i] = a.g.X[i];
+    for (int i = 1 + tid; i <= a.NP; i += blockDim.x) sr[i] = a.g.Rr[i];
+    for (int i = 1 + tid; i <= a.LP; i += blockDim.x) sz[i] = a.g.Z[i];
+    double* qalp = a.qal_part + (long long)blockIdx.x * n * NWL;
+    for (long long i = tid; i < (long long)n * NWL; i += blockDim.x) qalp[i] = 0.0;
+    RadAcc acc{0.0, 0.0, 0.0, 0.0, 0.0};
+    double qe_sum = 0.0;
+    int n_emit = 0;
+    __syncthreads();
+
+    for (int c = blockIdx.x; c < n; c += gridDim.x) {
+        // emitters in the reference's loop order: I outer, K inner
+        const int KD2 = c % a.LZ + 1, JD2 = (c / a.LZ) % a.NZ + 1, ID2 = c / (a.LZ * a.NZ) + 1;
+        const int I0 = 2 * ID2, J0 = 2 * JD2, K0 = 2 * KD2;
+        const int cc = (ID2 - 1) + a.MZ * ((JD2 - 1) + a.NZ * (KD2 - 1));
+        if (a.ibr[cc] >= 1) continue;
+        const double t = a.tcell[cc];
+        if (t <= kTgMn) continue;
+        if (tid == 0) {
+            rad_debx(a, t, s_deb);
+            const double t2 = t * t;
+            const double g0 = a.sgn * (t2 * t2);
+            for (int l = 0; l < NWL; ++l) {
+                s_qel0[l] = s_deb[l] * a.akl[cc + (long long)l * n] * g0;
+                s_qel[l] = 0.0;
+            }
+        }
+        __syncthreads();
+        for (int d = 0; d < 3; ++d) {
+            Dir D;
+            D.d = d;
+            D.u = d == 0 ? 1 : 0;
+            D.v = d == 2 ? 1 : 2;
+            const int dims[3] = {a.MP, a.NP, a.LP};
+            const int pos[3] = {I0, J0, K0};
+            const int strides[3] = {1, a.MZ, a.MZ * a.NZ};
+            const double* crd[3] = {sx, sr, sz};
+            double* angs[3] = {ang1, ang2, ang3};
+            const int angw[3] = {a.MP + 2, a.NP + 2, a.LP + 2};
+            const double* dface[3] = {a.g.DX, a.g.DR, a.g.DZ};
+            D.Dd = dims[d]; D.Du = dims[D.u]; D.Dv = dims[D.v];
+            D.DA = D.Du / 2; D.DB = D.Dv / 2; D.A = D.DA * D.DB;
+            D.d0 = pos[d]; D.u0 = pos[D.u]; D.v0 = pos[D.v];
+            D.sd = strides[d]; D.su = strides[D.u]; D.sv = strides[D.v];
+            D.cd = crd[d]; D.cu = crd[D.u]; D.cv = crd[D.v];
+            D.angU1 = angs[D.u]; D.angU2 = angs[D.u] + angw[D.u];
+            D.angV1 = angs[D.v]; D.angV2 = angs[D.v] + angw[D.v];
+            D.direct1 = 100 * (d + 1) + 1; D.direct2 = 100 * (d + 1) + 11;
+            if (tid == 0)
+                for (int l = 0; l < NWL; ++l) s_qel1[l] = s_qel0[l] * dface[D.u][D.u0] * dface[D.v][D.v0];
+            __syncthreads();
+            rad_direction<NW>(a, D, S, qalp, s_qel1, s_qel, s_ang0, acc, a.err);
+        }
+        if (tid == 0) {
+            double qe = s_qel[0];
+            for (int l = 1; l < NWL; ++l) qe = qe + s_qel[l];
+            a.qe[cc] = qe;
+            qe_sum += qe;
+            ++n_emit;
+        }
+        __syncthreads();
+    }
+    // block totals in a fixed order
+    double vals[5] = {acc.melt, acc.exit, acc.inlet, acc.wall, acc.open};
+    for (int k = 0; k < 5; ++k) {
+        s_red[tid] = vals[k];
+        __syncthreads();
+        for (int st = kRadThreads / 2; st > 0; st >>= 1) {
+            if (tid < st) s_red[tid] += s_red[tid + st];
+            __syncthreads();
+        }
+        if (tid == 0) a.tot_part[8 * blockIdx.x + k] = s_red[0];
+        __syncthreads();
+    }
+    if (tid == 0) {
+        a.tot_part[8 * blockIdx.x + 5] = qe_sum;
+        a.tot_part[8 * blockIdx.x + 6] = (double)n_emit;
+    }
+}
+
+// QAL = sum of the CTA copies in CTA order; QA = sum over bands (QRN1)
+__global__ void k_rad_reduce(RadArgs a, int nparts) {
+    const int n = a.MZ * a.NZ * a.LZ;
+    GFM_FOR(c, n) {
+        double g0 = 0.0;
+        for (int l = 0; l < a.NWL; ++l) {
+            double s = 0.0;
+            for (int b = 0; b < nparts; ++b) s += a.qal_part[(long long)b * n * a.NWL + (long long)l * n + c];
+            g0 = g0 + s;
+        }
+        a.qa[c] = g0;
+    }
+}
+
+__global__ void k_rad_zero(double* p, int n) {
+    GFM_FOR(i, n) p[i] = 0.0;
+}
+
+template <typename R>
+__global__ void k_rad_t_roundtrip(R* T, long long n, double t0) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        T[t] = R(((double)T[t] * t0) / t0);
+}
+
+size_t rad_smem_fixed(const RadArgs& a) {
+    return sizeof(double) * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2) + 2 * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2)));
+}
+size_t rad_smem_slab(const RadArgs& a) { return (size_t)3 * a.A * a.NWL * sizeof(double) + (size_t)3 * a.A; }
+
+template <int NW>
+int rad_trace_launch(const RadArgs& a, int grid, size_t smem, cudaStream_t st) {
+    if (cudaFuncSetAttribute(k_rad_trace<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return GFM_E_CUDA;
+    k_rad_trace<NW><<<grid, kRadThreads, smem, st>>>(a);
+    return GFM_OK;
+}
+
+}  // namespace
+
+size_t rad_shared_bytes(const RadArgs& a, bool with_slab) {
+    return rad_smem_fixed(a) + (with_slab ? rad_smem_slab(a) : 0);
+}
+
+template <typename R>
+int launch_rad_transfer(RadArgs a, R* T, long long nT, int grid, cudaStream_t st) {
+    const int n = a.MZ * a.NZ * a.LZ;
+    const int gb = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+    k_rad_mark<<<gb, 256, 0, st>>>(a);
+    k_rad_akl<R><<<a.akl_blocks, 256, 0, st>>>(a, T);
+    k_rad_zero<<<gb, 256, 0, st>>>(a.qe, n);
+    const size_t smem = rad_shared_bytes(a, a.slab_in_smem != 0);
+    int rc;
+    switch (a.NWL) {
+        case 4: rc = rad_trace_launch<4>(a, grid, smem, st); break;
+        case 10: rc = rad_trace_launch<10>(a, grid, smem, st); break;
+        default: rc = rad_trace_launch<0>(a, grid, smem, st); break;
+    }
+    if (rc != GFM_OK) return rc;
+    k_rad_reduce<<<gb, 256, 0, st>>>(a, grid);
+    k_rad_t_roundtrip<R><<<1024, 256, 0, st>>>(T, nT, a.t0);
+    return GFM_OK;
+}
+template int launch_rad_transfer<double>(RadArgs, double*, long long, int, cudaStream_t);
+template int launch_rad_transfer<float>(RadArgs, float*, long long, int, cudaStream_t);
+
+}  // namespace gfm

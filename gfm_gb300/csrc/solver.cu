@@ -84,6 +84,14 @@ struct gfm_handle {
     gfm::lp::Net* lp = nullptr;
     void* lp_feats = nullptr;           // BF16 inputs, 16 channels per voxel
     int lp_nx = 0, lp_ny = 0, lp_nz = 0;
+    // volume radiation transfer (allocated by the first gfm_gpu_rad_transfer)
+    GeoT<double> rad_g{};               // FP64 geometry of the transfer (coordinates uploaded in mixed mode)
+    int16_t* rad_ibr = nullptr;
+    double *rad_akl = nullptr, *rad_tcell = nullptr, *rad_qal = nullptr, *rad_qe = nullptr, *rad_qa = nullptr;
+    double *rad_tot = nullptr, *rad_akl_part = nullptr, *rad_scratch = nullptr;
+    unsigned char* rad_fscratch = nullptr;
+    int* rad_err = nullptr;
+    int rad_grid = 0, rad_akl_blocks = 0, rad_in_smem = 0;
     int rb_flags = kRbPdl | kRbAvgInPass;   // red-black options (environment at create): GFM_RB_FUSED=1 adds
                                             // kRbFused; GFM_PDL=0 drops kRbPdl; GFM_RB_AVG_IN_PASS=0 drops kRbAvgInPass
 };
@@ -1073,6 +1081,115 @@ extern "C" int gfm_gpu_gflow_batch(gfm_handle* const* hs, int n, int n_iter, gfm
 extern "C" int gfm_gpu_download(gfm_handle* h, gfm_fields* f) {
     if (!h || !f) return GFM_E_ARG;
     return h->prec == GFM_PREC_FP64 ? download_fields(h, h->cd, f) : download_fields(h, h->cf, f);
+}
+
+namespace {
+constexpr size_t kRadSmemLimit = 227 * 1024;
+// device buffers of the volume transfer, once per handle: one trace CTA per SM
+int rad_alloc(gfm_handle* h, RadArgs& a) {
+    const long long nc = (long long)a.MZ * a.NZ * a.LZ;
+    if (!h->rad_ibr) {
+        // the transfer works in FP64: in mixed mode the handle's FP64 geometry
+        // holds only IBCELL, so the coordinates are uploaded for it here
+        h->rad_g = h->gd;
+        if (!h->rad_g.X) {
+            const HostGrid& hg = h->hg;
+            double *x, *dx, *r, *dr, *rs, *z, *dz;
+            int rc;
+            if ((rc = dupload(h, &x, hg.X)) || (rc = dupload(h, &dx, hg.DX)) || (rc = dupload(h, &r, hg.R)) ||
+                (rc = dupload(h, &dr, hg.DR)) || (rc = dupload(h, &rs, hg.RS)) || (rc = dupload(h, &z, hg.Z)) ||
+                (rc = dupload(h, &dz, hg.DZ)))
+                return rc;
+            h->rad_g.X = x; h->rad_g.DX = dx; h->rad_g.Rr = r; h->rad_g.DR = dr; h->rad_g.RS = rs;
+            h->rad_g.Z = z; h->rad_g.DZ = dz;
+        }
+        int dev = 0, sms = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        h->rad_grid = sms > 0 ? sms : 1;
+        h->rad_akl_blocks = (int)std::min<long long>((nc + 255) / 256, 1024);
+        h->rad_in_smem = rad_shared_bytes(a, true) <= kRadSmemLimit;
+        int rc;
+        if ((rc = dalloc(h, &h->rad_ibr, nc)) || (rc = dalloc(h, &h->rad_akl, nc * a.NWL)) ||
+            (rc = dalloc(h, &h->rad_tcell, nc)) || (rc = dalloc(h, &h->rad_qal, nc * a.NWL * h->rad_grid)) ||
+            (rc = dalloc(h, &h->rad_qe, nc)) || (rc = dalloc(h, &h->rad_qa, nc)) ||
+            (rc = dalloc(h, &h->rad_tot, 8LL * h->rad_grid)) || (rc = dalloc(h, &h->rad_akl_part, 2LL * h->rad_akl_blocks)) ||
+            (rc = dalloc(h, &h->rad_err, 1)))
+            return rc;
+        if (!h->rad_in_smem) {
+            if ((rc = dalloc(h, &h->rad_scratch, 3LL * a.A * a.NWL * h->rad_grid)) ||
+                (rc = dalloc(h, &h->rad_fscratch, 3LL * a.A * h->rad_grid)))
+                return rc;
+        }
+    }
+    a.g = h->rad_g;
+    a.ibr = h->rad_ibr; a.akl = h->rad_akl; a.tcell = h->rad_tcell; a.qal_part = h->rad_qal;
+    a.qe = h->rad_qe; a.qa = h->rad_qa; a.tot_part = h->rad_tot; a.akl_part = h->rad_akl_part;
+    a.scratch = h->rad_scratch; a.fscratch = h->rad_fscratch; a.err = h->rad_err;
+    a.slab_in_smem = h->rad_in_smem;
+    a.akl_blocks = h->rad_akl_blocks;
+    return GFM_OK;
+}
+}  // namespace
+
+extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
+    if (!h) return GFM_E_ARG;
+    const Ctx<double>& cdb = h->cd;
+    if (cdb.nwl < 1 || cdb.nwl > kRadMaxBands) { h->err = "radiation transfer: 1 to 16 bands"; return GFM_E_UNSUPPORTED; }
+    RadArgs a{};
+    a.g = h->gd;
+    a.MP = h->gd.MP; a.NP = h->gd.NP; a.LP = h->gd.LP;
+    a.MZ = a.MP / 2; a.NZ = a.NP / 2; a.LZ = a.LP / 2;
+    a.NWL = cdb.nwl;
+    a.A = std::max(a.NZ * a.LZ, std::max(a.MZ * a.LZ, a.MZ * a.NZ));
+    a.t0 = h->params.t0;
+    a.sgn = h->params.sig * h->params.ri * h->params.ri;                          // SGN (Rad0.f90:33)
+    for (int l = 0; l < a.NWL; ++l) {
+        a.akl0[l] = cdb.akl0[l];
+        a.deb0[l] = h->params.hck / h->params.ri / cdb.wl[l];                      // DEB0 (Rad0.f90:34)
+    }
+    int rc = rad_alloc(h, a);
+    if (rc) return rc;
+    cudaStream_t st = h->stream;
+    CK(cudaMemsetAsync(h->rad_err, 0, sizeof(int), st));
+    const long long nT = 8 * h->gd.CB;
+    if (h->prec == GFM_PREC_FP64) {
+        if ((rc = launch_rad_transfer<double>(a, h->cd.T, nT, h->rad_grid, st))) { h->err = "radiation transfer launch"; return rc; }
+        launch_cells_to_split(h->gd, a.qe, h->cd.QE, st);
+        launch_cells_to_split(h->gd, a.qa, h->cd.QA, st);
+    } else {
+        if ((rc = launch_rad_transfer<float>(a, h->cf.T, nT, h->rad_grid, st))) { h->err = "radiation transfer launch"; return rc; }
+        launch_cells_to_split(h->gfl, a.qe, h->cf.QE, st);
+        launch_cells_to_split(h->gfl, a.qa, h->cf.QA, st);
+    }
+    std::vector<double> tot(8 * (size_t)h->rad_grid), akp(2 * (size_t)h->rad_akl_blocks);
+    int err = 0;
+    CK(cudaMemcpyAsync(tot.data(), h->rad_tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(akp.data(), h->rad_akl_part, akp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&err, h->rad_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (err) {
+        h->err = "radiation transfer: a wall-corner split inside the box (geometry outside the supported set)";
+        return GFM_E_UNSUPPORTED;
+    }
+    h->rad_active = 1;
+    if (out) {
+        std::memset(out, 0, sizeof *out);
+        for (int b = 0; b < h->rad_grid; ++b) {   // block order
+            out->qa_sum_to_melt += tot[8 * b + 0];
+            out->qa_sum_to_exit += tot[8 * b + 1];
+            out->qa_sum_to_inlet += tot[8 * b + 2];
+            out->qa_sum_to_wall += tot[8 * b + 3];
+            out->qa_sum_to_open += tot[8 * b + 4];
+            out->qe_sum_from_open += tot[8 * b + 5];
+            out->n_emitters += (int)tot[8 * b + 6];
+        }
+        for (int b = 0; b < h->rad_akl_blocks; ++b) {
+            out->tot_qe_h2o_co2 += akp[2 * b];
+            out->tot_qe_soot += akp[2 * b + 1];
+        }
+    }
+    return GFM_OK;
 }
 
 extern "C" int gfm_gpu_rad_emission(gfm_handle* h) {

@@ -107,6 +107,29 @@ struct AdiScratch {
     Quad<R> *ya, *yb, *za, *zb;
 };
 
+// ---- volume radiation transfer (rad.cu) ---------------------------------------
+constexpr int kRadMaxBands = 16;
+struct RadArgs {
+    GeoT<double> g;              // coordinates (1-based), parity-split IBCELL, pidx
+    int MP, NP, LP, MZ, NZ, LZ, NWL;
+    int A;                       // cells of the largest slab of the three directions
+    int slab_in_smem;            // slab arrays in shared memory (else in scratch/fscratch)
+    int akl_blocks;              // blocks of k_rad_akl (akl_part holds 2 per block)
+    double t0, sgn;              // T0; SIG*RI*RI
+    double akl0[kRadMaxBands];   // band absorption coefficients (1/m)
+    double deb0[kRadMaxBands];   // HCK/RI/WL
+    int16_t* ibr;                // IBCELL with the wall markers, per cell (MZ,NZ,LZ)
+    double *akl, *tcell;         // AKL (cell + l*ncell), T*T0 per cell
+    double *qal_part;            // one QAL copy per trace block
+    double *qe, *qa;             // QE, QA per cell (MZ,NZ,LZ)
+    double *tot_part, *akl_part; // block totals (8 per trace block, 2 per akl block)
+    double* scratch;             // slab arrays when they do not fit in shared memory
+    unsigned char* fscratch;
+    int* err;                    // bit 0: geometry outside the supported set
+};
+size_t rad_shared_bytes(const RadArgs& a, bool with_slab);
+template <typename R> int launch_rad_transfer(RadArgs a, R* T, long long nT, int grid, cudaStream_t s);
+
 // ---- launchers (defined in the kernel translation units) --------------------
 template <typename R> void launch_wallfn(const Ctx<R>& c, const int* wall_list, int n_wall, cudaStream_t s);
 template <typename R> void launch_copy_faces_to_fz(const Ctx<R>& c, cudaStream_t s);

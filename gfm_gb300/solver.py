@@ -196,6 +196,12 @@ class GpuSolver:
     def rad_emission(self) -> None:
         self._check(self.lib.gfm_gpu_rad_emission(self.h))
 
+    def rad_transfer(self) -> dict:
+        """Volume radiation transfer from the current T (QE and QA replaced); the totals in W."""
+        t = abi.GfmRadTotals()
+        self._check(self.lib.gfm_gpu_rad_transfer(self.h, C.byref(t)))
+        return t.as_dict()
+
     def adlbl3(self, xt, ap, as6, bs, ib, ie, jb, je, kb, ke, nim) -> np.ndarray:
         x = np.ascontiguousarray(xt, dtype=np.float64).copy()
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in as6]

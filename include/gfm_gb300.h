@@ -220,6 +220,31 @@ int  gfm_gpu_adlbl3(gfm_handle *h, double *xt, const double *ap,
 /* Emission-only radiation QE on the device from the current T, P
  * (rad_qe_only, Rad_emis.f90:411-466 with RAD0 Rad0.f90:112-157). */
 int  gfm_gpu_rad_emission(gfm_handle *h);
+
+/* Totals of one volume radiation transfer, W (Qrn.f90:73-87, Qre.f90:511-514,
+ * Rad0.f90:137-148). */
+typedef struct gfm_rad_totals {
+    double qe_sum_from_open;     /* emission of the traced open cells          */
+    double qa_sum_to_open;       /* absorbed in open cells                     */
+    double qa_sum_to_wall, qa_sum_to_inlet, qa_sum_to_exit, qa_sum_to_melt;
+                                 /* deposited on boundary cells, by IBCELL      */
+    double tot_qe_h2o_co2, tot_qe_soot;    /* RAD0 band-emission totals         */
+    int    n_emitters;           /* open cells with T > TG_MN that were traced  */
+    int    reserved;
+} gfm_rad_totals;
+/* Volume radiation transfer on the device from the current T: the volume part
+ * of CALL RAD_EMIS (A0main.f90:232) -- wall markers (Rad_emis.f90:144-178),
+ * RAD0 with ID_RAD=10 (Rad0.f90:112-166), the QRNF emitter loop
+ * (Qrn.f90:58-229) with QREF and QRTX/QRTY/QRTZ (Qre.f90:31-515,
+ * Qrtx.f90:15-209, Qrty.f90:9-224, Qrtz.f90:15-234), and QA = sum of QAL over
+ * the bands (QRN1, Qrn.f90:250-259).  QE and QA of the handle are replaced and
+ * the enthalpy source uses QA - QE from then on (Source.f90:437-439).  The
+ * wall exchange that follows in QRNF (wall_q_amb, wallq, qrn2) is not done.
+ * `out` (may be NULL) receives the totals.  Grids whose slab work arrays
+ * exceed the device limit, or geometries that reach the reference's
+ * undefined corner case (a wall-corner split on the emitter's own column),
+ * return GFM_E_UNSUPPORTED / GFM_E_LIMIT. */
+int  gfm_gpu_rad_transfer(gfm_handle *h, gfm_rad_totals *out);
 /* Device times (CUDA events on the handle's stream) accumulated since the
  * last reset: adi_ms = line-solver batches, gflow_ms = whole GFLOW calls
  * (first to last iteration of each gfm_gpu_gflow), other_ms reserved;

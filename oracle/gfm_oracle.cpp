@@ -17,7 +17,7 @@ namespace {
 
 typedef std::vector<double> vec;
 
-const double ZERO = 0.0, ONE = 1.0, TWO = 2.0;
+const double ZERO = 0.0, ONE = 1.0, TWO = 2.0, HALF = 0.5;
 const double small20 = 1.0e-20, small16 = 1.0e-16, BIG = 1.0e+20;
 const double WF = 16.0426, WO2 = 31.9988, WCO2 = 44.0098, WH2O = 18.0152, WN2 = 28.0134;
 const int IYF = 1, IYO2 = 2, IH = 3, IK = 4, IEPS = 5, IYCO2 = 6, IYN2 = 7, IYH2O = 9;
@@ -1577,6 +1577,767 @@ struct Oracle {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Volume radiation transfer, restated from
+//   RAD_EMIS   Rad_emis.f90:144-189  wall markers with open neighbours, T*T0
+//   RAD0       Rad0.f90:112-166      AKL = EMF(AKL0, OPL) (ID_RAD=10), totals
+//   QRNF       Qrn.f90:58-229        emitter loop (emission/absorption part)
+//   QREF       Qre.f90:31-515        per emitter: x, y and z fluxes
+//   QRTX/Y/Z   Qrtx.f90:15-209, Qrty.f90:9-224, Qrtz.f90:15-234
+//   QRN1       Qrn.f90:244-275       QA = sum over bands of QAL
+// and the unmarking and T/T0 of Rad_emis.f90:364-377.  The wall exchange that
+// QRNF runs afterwards (wall_q_amb, wallq, qrn2) is not part of this.
+// ---------------------------------------------------------------------------
+
+// atan(x) in degrees (the Fortran intrinsic ATAND).  Own implementation, the
+// same operations as the GPU kernel's: |x| > 1 is reduced by
+// atan(x) = pi/2 - atan(1/x), then a > tan(pi/12) by
+// atan(a) = pi/6 + atan((a*sqrt(3) - 1)/(a + sqrt(3))) (Abramowitz & Stegun
+// 4.4.34 with tan(pi/6) = 1/sqrt(3)), and the reduced argument t goes through
+// the Maclaurin series atan(t) = sum_{n=0}^{14} (-1)^n t^(2n+1)/(2n+1)
+// (A&S 4.4.42), Horner's rule in t^2 with fused multiply-adds.
+double ATAND(double x) {
+    const double PI = 3.14159265358979323846;
+    const double SQRT3 = 1.73205080756887729353;
+    const double TAN_PI_12 = 0.26794919243112270647;
+    double a = std::fabs(x);
+    const bool inv = a > 1.0;
+    if (inv) a = 1.0 / a;
+    const bool sh = a > TAN_PI_12;
+    if (sh) a = (a * SQRT3 - 1.0) / (a + SQRT3);
+    const double z = a * a;
+    double p = 1.0 / 29.0;
+    for (int n = 13; n >= 0; --n) p = std::fma(p, z, ((n & 1) ? -1.0 : 1.0) / (double)(2 * n + 1));
+    double r = a * p;
+    if (sh) r = PI / 6.0 + r;
+    if (inv) r = PI / 2.0 - r;
+    const double d = r * (180.0 / PI);
+    return x < 0.0 ? -d : d;
+}
+
+struct RadVolume {
+    Oracle& o;
+    int MP, NP, LP, MZ, NZ, LZ, NWL;
+    long NC;
+    std::vector<int> IBR;            // IBCELL with the wall markers, one value per cell (even positions)
+    vec AKL, QAL, QEL;               // (MZ,NZ,LZ,NWL)
+    vec DEB, DEB0, QEL0, QEL1, Q11, Q12;
+    double ANG0[4];
+    vec ANG1, ANG2, ANG3;            // ANG1(MP,2), ANG2(NP,2), ANG3(LP,2), 1-based
+    int DA, DB;                      // extents of the slab arrays of the current direction
+    vec QTX1, QTX2, Q2M;
+    std::vector<char> IQT1, IQTM, IQT2;
+    double SGN, TG_MN;
+    double qa_sum_to_melt = 0, qa_sum_to_exit = 0, qa_sum_to_inlet = 0, qa_sum_to_wall = 0, qa_sum_to_open = 0;
+    double qe_sum_from_open = 0, tot_qe_h2o_co2 = 0, tot_qe_soot = 0;
+    double qa_sum_bnd, qa_sum_vol, c_melt, c_exit, c_inlet, c_wall, c_open;
+    int n_emit = 0;
+
+    explicit RadVolume(Oracle& oo) : o(oo) {
+        MP = o.MP; NP = o.NP; LP = o.LP; MZ = o.MZ; NZ = o.NZ; LZ = o.LZ; NWL = o.NWL;
+        NC = (long)MZ * NZ * LZ;
+        DEB.assign(NWL + 1, 0.0); DEB0.assign(NWL + 1, 0.0); QEL0.assign(NWL + 1, 0.0); QEL1.assign(NWL + 1, 0.0);
+        Q11.assign(NWL + 1, 0.0); Q12.assign(NWL + 1, 0.0);
+        ANG1.assign(2 * (MP + 2), 0.0); ANG2.assign(2 * (NP + 2), 0.0); ANG3.assign(2 * (LP + 2), 0.0);
+    }
+    long cell(int id2, int jd2, int kd2) const { return (long)(id2 - 1) + (long)MZ * ((long)(jd2 - 1) + (long)NZ * (kd2 - 1)); }
+    int ibr(int i, int j, int k) const { return IBR[cell(i / 2, j / 2, k / 2)]; }
+    double& akl(int id2, int jd2, int kd2, int l) { return AKL[cell(id2, jd2, kd2) + (long)(l - 1) * NC]; }
+    double& qal(int id2, int jd2, int kd2, int l) { return QAL[cell(id2, jd2, kd2) + (long)(l - 1) * NC]; }
+    double& qel(int id2, int jd2, int kd2, int l) { return QEL[cell(id2, jd2, kd2) + (long)(l - 1) * NC]; }
+    double& ang1(int i, int c) { return ANG1[(c - 1) * (MP + 2) + i]; }
+    double& ang2(int j, int c) { return ANG2[(c - 1) * (NP + 2) + j]; }
+    double& ang3(int k, int c) { return ANG3[(c - 1) * (LP + 2) + k]; }
+    double& qtx1(int a, int b, int l) { return QTX1[((long)(l - 1) * DB + (b - 1)) * DA + (a - 1)]; }
+    double& qtx2(int a, int b, int l) { return QTX2[((long)(l - 1) * DB + (b - 1)) * DA + (a - 1)]; }
+    double& q2m(int a, int b, int l) { return Q2M[((long)(l - 1) * DB + (b - 1)) * DA + (a - 1)]; }
+    char& iqt1(int a, int b) { return IQT1[(long)(b - 1) * DA + (a - 1)]; }
+    char& iqtm(int a, int b) { return IQTM[(long)(b - 1) * DA + (a - 1)]; }
+    char& iqt2(int a, int b) { return IQT2[(long)(b - 1) * DA + (a - 1)]; }
+    double X(int i) const { return o.X[i]; }
+    double R(int j) const { return o.R[j]; }
+    double Z(int k) const { return o.Z[k]; }
+    static double T4(double t) { double t2 = t * t; return t2 * t2; }
+
+    void alloc_slab(int da, int db) {   // ALLOCATE + zero/.TRUE. at the start of a direction
+        DA = da; DB = db;
+        QTX1.assign((long)DA * DB * NWL, 0.0); QTX2.assign((long)DA * DB * NWL, 0.0); Q2M.assign((long)DA * DB * NWL, 0.0);
+        IQT1.assign((long)DA * DB, 1); IQTM.assign((long)DA * DB, 1); IQT2.assign((long)DA * DB, 1);
+    }
+    void DEBX(double TG0) {   // Rad_fun.f90:83-101
+        double EB0 = 0;
+        for (int L = 1; L <= NWL - 1; ++L) {
+            double X1 = DEB0[L] / TG0;
+            double EB1 = RIF3(X1);
+            DEB[L] = EB1 - EB0;
+            if (DEB[L] <= 1.0e-3) DEB[L] = ZERO; else EB0 = EB1;
+        }
+        DEB[NWL] = ONE - EB0;
+    }
+    // absorption of the power arriving at one slab cell (the loop bodies of
+    // Qre.f90:185-219 / 336-369 / 486-522); a, b index the slab arrays
+    void absorb(int I, int J, int K, int a, int b, bool end) {
+        if (iqt2(a, b)) return;
+        const int ID2 = I / 2, JD2 = J / 2, KD2 = K / 2;
+        for (int L = 1; L <= NWL; ++L) {
+            if (qtx2(a, b, L) < small16) continue;
+            const int ib = ibr(I, J, K);
+            if (ib >= 1 || end) {
+                qal(ID2, JD2, KD2, L) = qal(ID2, JD2, KD2, L) + qtx2(a, b, L);
+                qa_sum_bnd = qa_sum_bnd + qtx2(a, b, L);
+                if (ib == 4) c_melt = c_melt + qtx2(a, b, L);
+                else if (ib == 3) c_exit = c_exit + qtx2(a, b, L);
+                else if (ib == 2) c_inlet = c_inlet + qtx2(a, b, L);
+                else c_wall = c_wall + qtx2(a, b, L);
+            } else {
+                double QA0 = qtx2(a, b, L) * akl(ID2, JD2, KD2, L);
+                qal(ID2, JD2, KD2, L) = qal(ID2, JD2, KD2, L) + QA0;
+                qtx1(a, b, L) = qtx2(a, b, L) - QA0;
+                iqt1(a, b) = 0;
+                qa_sum_vol = qa_sum_vol + QA0;
+                c_open = c_open + QA0;
+            }
+            qtx2(a, b, L) = 0;
+            iqt2(a, b) = 1;
+        }
+    }
+
+    // ---- QRTX (Qrtx.f90:15-209) ----------------------------------------------
+    void QRTX(int I0, int J0, int K0, int I10, int I1) {
+        int J2 = 0;   // the spread's DO variable, as the corner branch reads it (J1 == J0 never occurs in a box)
+        int I2 = I1 + (I1 - I10) / 2;
+        I2 = std::min(I2, MP);
+        for (int JM = -1; JM <= 1; JM += 2) {
+            const int JEND = JM < 0 ? 2 : NP;
+            for (int JJ = J0 + JM; JM > 0 ? JJ <= JEND : JJ >= JEND; JJ += JM * 2) {
+                double a2;
+                double b = std::fabs(X(I2) - X(I0));
+                if (b < small16) a2 = 90; else a2 = ATAND(std::fabs(R(JJ) - R(J0)) / b);
+                if (a2 >= ANG0[2]) break;
+                ang2(JJ, 2) = a2;
+            }
+        }
+        for (int KM = -1; KM <= 1; KM += 2) {
+            const int KEND = KM < 0 ? 2 : LP;
+            for (int KK = K0 + KM; KM > 0 ? KK <= KEND : KK >= KEND; KK += KM * 2) {
+                double a3;
+                double b = std::fabs(X(I2) - X(I0));
+                if (b < small16) a3 = 90; else a3 = ATAND(std::fabs(Z(KK) - Z(K0)) / b);
+                if (a3 >= ANG0[3]) break;
+                ang3(KK, 2) = a3;
+            }
+        }
+        for (int K1 = 4; K1 <= LP - 2; K1 += 2) {
+            if (K1 < K0 && ang3(K1 + 1, 2) >= ANG0[3]) continue;
+            if (K1 > K0 && ang3(K1 - 1, 2) >= ANG0[3]) break;
+            const int KD2 = K1 / 2;
+            for (int JPM = -2; JPM <= 2; JPM += 4) {
+                double A11 = 0, A12 = 0;
+                const int JEND = JPM < 0 ? 2 : NP;
+                for (int J1 = J0; JPM > 0 ? J1 <= JEND - JPM : J1 >= JEND - JPM; J1 += JPM) {
+                    if (A11 >= ANG0[2]) break;
+                    const int J12 = J1 + JPM / 2;
+                    A12 = ang2(J12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int J1D2 = J1 / 2;
+                    if (iqt1(J1D2, KD2)) { A11 = A12; continue; }
+                    if (J1 == J0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = qtx1(J1D2, KD2, L) * HALF;
+                        if (JPM > 0) for (int L = 1; L <= NWL; ++L) qtx1(J1D2, KD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = qtx1(J1D2, KD2, L); qtx1(J1D2, KD2, L) = ZERO; }
+                    }
+                    if (J1 != J0 || JPM > 0) iqt1(J1D2, KD2) = 1;
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (J2 = J1; JPM > 0 ? J2 <= JEND : J2 >= JEND; J2 += JPM) {
+                        const int J2D2 = J2 / 2;
+                        if (ibr(I1, J2, K1) < 1) {
+                            const int J2M = J2 + JPM / 2;
+                            const double A22 = ang2(J2M, 2);
+                            if (A22 <= A21) continue;
+                            if (A22 < A12) {
+                                const double FIJ = (A22 - A21) / DANG;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q11[L] < small16) continue;
+                                    double Q21 = Q11[L] * FIJ;
+                                    q2m(J2D2, KD2, L) = q2m(J2D2, KD2, L) + Q21;
+                                    Q12[L] = Q12[L] - Q21;
+                                }
+                                iqtm(J2D2, KD2) = 0;
+                                A21 = A22;
+                                continue;
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) q2m(J2D2, KD2, L) = q2m(J2D2, KD2, L) + Q12[L];
+                        iqtm(J2D2, KD2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+        for (int J1 = 2; J1 <= NP; J1 += 2) {
+            if (J1 < J0 && ang2(J1 + 1, 2) >= ANG0[2]) continue;
+            if (J1 > J0 && ang2(J1 - 1, 2) >= ANG0[2]) break;
+            const int JD2 = J1 / 2;
+            for (int KM = -2; KM <= 2; KM += 4) {
+                double A11 = 0, A12 = 0;
+                const int KEND = KM < 0 ? 2 : LP;
+                for (int K1 = K0; KM > 0 ? K1 <= KEND - KM : K1 >= KEND - KM; K1 += KM) {
+                    if (A11 >= ANG0[3]) break;
+                    const int K12 = K1 + KM / 2;
+                    A12 = ang3(K12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int KD2 = K1 / 2;
+                    if (iqtm(JD2, KD2)) { A11 = A12; continue; }
+                    if (K1 == K0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = q2m(JD2, KD2, L) * HALF;
+                        if (KM > 0) for (int L = 1; L <= NWL; ++L) q2m(JD2, KD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = q2m(JD2, KD2, L); q2m(JD2, KD2, L) = ZERO; }
+                    }
+                    if (K1 != K0 || KM > 0) iqtm(JD2, KD2) = 1;
+                    const int IBC1 = ibr(I1, J1, K1);
+                    if (IBC1 == 101 || IBC1 == 111 || IBC1 == 4) {
+                        for (int L = 1; L <= NWL; ++L) qtx2(JD2, KD2, L) = qtx2(JD2, KD2, L) + Q11[L];
+                        iqt2(JD2, KD2) = 0;
+                        A11 = A12;
+                        continue;
+                    }
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (int K2 = K1; KM > 0 ? K2 <= KEND : K2 >= KEND; K2 += KM) {
+                        const int K2M = K2 + KM / 2, K2D2 = K2 / 2;
+                        const int IBC2 = ibr(I1, J1, K2);
+                        bool to330 = IBC1 <= 0 && IBC2 >= 1;
+                        if (!to330) {
+                            if (IBC1 > 100 && IBC2 == 1) {
+                                if (J1 < J0) J2 = J1 + 2; else if (J1 > J0) J2 = J1 - 2;
+                                const int J2D2 = J2 / 2, K2D2M = K2D2 - KM / 2;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q12[L] < small16) continue;
+                                    double Q21 = Q12[L] * HALF;
+                                    qtx2(J2D2, K2D2, L) = qtx2(J2D2, K2D2, L) + Q21;
+                                    qtx2(JD2, K2D2M, L) = qtx2(JD2, K2D2M, L) + Q21;
+                                }
+                                iqt2(J2D2, K2D2) = 0;
+                                iqt2(JD2, K2D2M) = 0;
+                                break;
+                            }
+                            if (K2M > LP || K2M < 2) to330 = true;
+                            else {
+                                const double A22 = ang3(K2M, 2);
+                                if ((A22 - A21) <= 1.0e-10) continue;
+                                if (A22 < A12) {
+                                    const double FIJ = (A22 - A21) / DANG;
+                                    for (int L = 1; L <= NWL; ++L) {
+                                        if (Q11[L] < small16) continue;
+                                        double Q21 = Q11[L] * FIJ;
+                                        qtx2(JD2, K2D2, L) = qtx2(JD2, K2D2, L) + Q21;
+                                        Q12[L] = Q12[L] - Q21;
+                                    }
+                                    iqt2(JD2, K2D2) = 0;
+                                    A21 = A22;
+                                    continue;
+                                }
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) qtx2(JD2, K2D2, L) = qtx2(JD2, K2D2, L) + Q12[L];
+                        iqt2(JD2, K2D2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+    }
+
+    // ---- QRTY (Qrty.f90:9-224) -------------------------------------------------
+    void QRTY(int I0, int J0, int K0, int J10, int J1) {
+        int I2 = 0;   // the spread's DO variable, as the corner branch reads it (I1 == I0 never occurs in a box)
+        int J2 = J1 + (J1 - J10) / 2;
+        J2 = std::min(J2, NP);
+        for (int IM = -1; IM <= 1; IM += 2) {
+            const int IEND = IM < 0 ? 2 : MP;
+            for (int II = I0 + IM; IM > 0 ? II <= IEND : II >= IEND; II += IM * 2) {
+                double a1;
+                double b = std::fabs(R(J2) - R(J0));
+                if (b < small16) a1 = 90; else a1 = ATAND(std::fabs(X(II) - X(I0)) / b);
+                if (a1 >= ANG0[1]) break;
+                ang1(II, 2) = a1;
+            }
+        }
+        for (int KM = -1; KM <= 1; KM += 2) {
+            const int KEND = KM < 0 ? 2 : LP;
+            for (int KK = K0 + KM; KM > 0 ? KK <= KEND : KK >= KEND; KK += KM * 2) {
+                double a3;
+                double b = std::fabs(R(J2) - R(J0));
+                if (b < small16) a3 = 90; else a3 = ATAND(std::fabs(Z(KK) - Z(K0)) / b);
+                if (a3 >= ANG0[3]) break;
+                ang3(KK, 2) = a3;
+            }
+        }
+        for (int K1 = 4; K1 <= LP - 2; K1 += 2) {
+            if (K1 < K0 && ang3(K1 + 1, 2) >= ANG0[3]) continue;
+            if (K1 > K0 && ang3(K1 - 1, 2) >= ANG0[3]) break;
+            const int KD2 = K1 / 2;
+            for (int IPM = -2; IPM <= 2; IPM += 4) {
+                double A11 = 0, A12 = 0;
+                const int IEND = IPM < 0 ? 2 : MP;
+                for (int I1 = I0; IPM > 0 ? I1 <= IEND - IPM : I1 >= IEND - IPM; I1 += IPM) {
+                    if (A11 >= ANG0[1]) break;
+                    const int I12 = I1 + IPM / 2;
+                    A12 = ang1(I12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int I1D2 = I1 / 2;
+                    if (iqt1(I1D2, KD2)) { A11 = A12; continue; }
+                    if (I1 == I0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = qtx1(I1D2, KD2, L) * HALF;
+                        if (IPM > 0) for (int L = 1; L <= NWL; ++L) qtx1(I1D2, KD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = qtx1(I1D2, KD2, L); qtx1(I1D2, KD2, L) = ZERO; }
+                    }
+                    if (I1 != I0 || IPM > 0) iqt1(I1D2, KD2) = 1;
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (I2 = I1; IPM > 0 ? I2 <= IEND : I2 >= IEND; I2 += IPM) {
+                        const int I2D2 = I2 / 2;
+                        if (ibr(I2, J1, K1) < 1) {
+                            const int I2M = I2 + IPM / 2;
+                            const double A22 = ang1(I2M, 2);
+                            if (A22 <= A21) continue;
+                            if (A22 < A12) {
+                                const double FIJ = (A22 - A21) / DANG;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q11[L] < small16) continue;
+                                    double Q21 = Q11[L] * FIJ;
+                                    q2m(I2D2, KD2, L) = q2m(I2D2, KD2, L) + Q21;
+                                    Q12[L] = Q12[L] - Q21;
+                                }
+                                iqtm(I2D2, KD2) = 0;
+                                A21 = A22;
+                                continue;
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) q2m(I2D2, KD2, L) = q2m(I2D2, KD2, L) + Q12[L];
+                        iqtm(I2D2, KD2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+        for (int I1 = 2; I1 <= MP; I1 += 2) {
+            if (I1 < I0 && ang1(I1 + 1, 2) >= ANG0[1]) continue;
+            if (I1 > I0 && ang1(I1 - 1, 2) >= ANG0[1]) break;
+            const int ID2 = I1 / 2;
+            for (int KM = -2; KM <= 2; KM += 4) {
+                double A11 = 0, A12 = 0;
+                const int KEND = KM < 0 ? 2 : LP;
+                for (int K1 = K0; KM > 0 ? K1 <= KEND - KM : K1 >= KEND - KM; K1 += KM) {
+                    if (A11 >= ANG0[3]) break;
+                    const int K12 = K1 + KM / 2;
+                    A12 = ang3(K12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int KD2 = K1 / 2;
+                    if (iqtm(ID2, KD2)) { A11 = A12; continue; }
+                    if (K1 == K0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = q2m(ID2, KD2, L) * HALF;
+                        if (KM > 0) for (int L = 1; L <= NWL; ++L) q2m(ID2, KD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = q2m(ID2, KD2, L); q2m(ID2, KD2, L) = ZERO; }
+                    }
+                    if (K1 != K0 || KM > 0) iqtm(ID2, KD2) = 1;
+                    const int IBC1 = ibr(I1, J1, K1);
+                    if (IBC1 == 201 || IBC1 == 211 || IBC1 == 4) {
+                        for (int L = 1; L <= NWL; ++L) qtx2(ID2, KD2, L) = qtx2(ID2, KD2, L) + Q11[L];
+                        iqt2(ID2, KD2) = 0;
+                        A11 = A12;
+                        continue;
+                    }
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (int K2 = K1; KM > 0 ? K2 <= KEND : K2 >= KEND; K2 += KM) {
+                        const int K2M = K2 + KM / 2, K2D2 = K2 / 2;
+                        const int IBC2 = ibr(I1, J1, K2);
+                        bool to330 = IBC1 <= 0 && IBC2 >= 1;
+                        if (!to330) {
+                            if (IBC1 >= 100 && IBC2 == 1) {
+                                if (I1 < I0) I2 = I1 + 2; else if (I1 > I0) I2 = I1 - 2;
+                                const int I2D2 = I2 / 2, K2D2M = K2D2 - KM / 2;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q12[L] < small16) continue;
+                                    double Q21 = Q12[L] * HALF;
+                                    qtx2(I2D2, K2D2, L) = qtx2(I2D2, K2D2, L) + Q21;
+                                    qtx2(ID2, K2D2M, L) = qtx2(ID2, K2D2M, L) + Q21;
+                                }
+                                iqt2(I2D2, K2D2) = 0;
+                                iqt2(ID2, K2D2M) = 0;
+                                break;
+                            }
+                            if (K2M > LP || K2M < 2) to330 = true;
+                            else {
+                                const double A22 = ang3(K2M, 2);
+                                if ((A22 - A21) <= 1.0e-10) continue;
+                                if (A22 < A12) {
+                                    const double FIJ = (A22 - A21) / DANG;
+                                    for (int L = 1; L <= NWL; ++L) {
+                                        if (Q11[L] < small16) continue;
+                                        double Q21 = Q11[L] * FIJ;
+                                        qtx2(ID2, K2D2, L) = qtx2(ID2, K2D2, L) + Q21;
+                                        Q12[L] = Q12[L] - Q21;
+                                    }
+                                    iqt2(ID2, K2D2) = 0;
+                                    A21 = A22;
+                                    continue;
+                                }
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) qtx2(ID2, K2D2, L) = qtx2(ID2, K2D2, L) + Q12[L];
+                        iqt2(ID2, K2D2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+    }
+
+    // ---- QRTZ (Qrtz.f90:15-234) -------------------------------------------------
+    void QRTZ(int I0, int J0, int K0, int K10, int K1) {
+        int I2 = 0;   // the spread's DO variable, as the corner branch reads it (I1 == I0 never occurs in a box)
+        int K2 = K1 + (K1 - K10) / 2;
+        K2 = std::min(K2, LP);
+        for (int IM = -1; IM <= 1; IM += 2) {
+            const int IEND = IM < 0 ? 2 : MP;
+            for (int II = I0 + IM; IM > 0 ? II <= IEND : II >= IEND; II += IM * 2) {
+                double a1;
+                double b = std::fabs(Z(K2) - Z(K0));
+                if (b < small16) a1 = 90; else a1 = ATAND(std::fabs(X(II) - X(I0)) / b);
+                if (a1 >= ANG0[1]) break;
+                ang1(II, 2) = a1;
+            }
+        }
+        for (int JM = -1; JM <= 1; JM += 2) {
+            const int JEND = JM < 0 ? 2 : NP;
+            for (int JJ = J0 + JM; JM > 0 ? JJ <= JEND : JJ >= JEND; JJ += JM * 2) {
+                double a2;
+                double b = std::fabs(Z(K2) - Z(K0));
+                if (b < small16) a2 = 90; else a2 = ATAND(std::fabs(R(JJ) - R(J0)) / b);
+                if (a2 >= ANG0[2]) break;
+                ang2(JJ, 2) = a2;
+            }
+        }
+        for (int J1 = 4; J1 <= NP - 2; J1 += 2) {
+            if (J1 < J0 && ang2(J1 + 1, 2) >= ANG0[2]) continue;
+            if (J1 > J0 && ang2(J1 - 1, 2) >= ANG0[2]) break;
+            const int JD2 = J1 / 2;
+            for (int IPM = -2; IPM <= 2; IPM += 4) {
+                double A11 = 0, A12 = 0;
+                const int IEND = IPM < 0 ? 2 : MP;
+                for (int I1 = I0; IPM > 0 ? I1 <= IEND - IPM : I1 >= IEND - IPM; I1 += IPM) {
+                    if (A11 >= ANG0[1]) break;
+                    const int I12 = I1 + IPM / 2;
+                    A12 = ang1(I12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int I1D2 = I1 / 2;
+                    if (iqt1(I1D2, JD2)) { A11 = A12; continue; }
+                    if (I1 == I0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = qtx1(I1D2, JD2, L) * HALF;
+                        if (IPM > 0) for (int L = 1; L <= NWL; ++L) qtx1(I1D2, JD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = qtx1(I1D2, JD2, L); qtx1(I1D2, JD2, L) = ZERO; }
+                    }
+                    if (I1 != I0 || IPM > 0) iqt1(I1D2, JD2) = 1;
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (I2 = I1; IPM > 0 ? I2 <= IEND : I2 >= IEND; I2 += IPM) {
+                        const int I2D2 = I2 / 2;
+                        if (ibr(I2, J1, K1) < 1) {
+                            const int I2M = I2 + IPM / 2;
+                            const double A22 = ang1(I2M, 2);
+                            if (A22 <= A21) continue;
+                            if (A22 < A12) {
+                                const double FIJ = (A22 - A21) / DANG;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q11[L] < small16) continue;
+                                    double Q21 = Q11[L] * FIJ;
+                                    q2m(I2D2, JD2, L) = q2m(I2D2, JD2, L) + Q21;
+                                    Q12[L] = Q12[L] - Q21;
+                                }
+                                iqtm(I2D2, JD2) = 0;
+                                A21 = A22;
+                                continue;
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) q2m(I2D2, JD2, L) = q2m(I2D2, JD2, L) + Q12[L];
+                        iqtm(I2D2, JD2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+        for (int I1 = 2; I1 <= MP; I1 += 2) {
+            if (I1 < I0 && ang1(I1 + 1, 2) >= ANG0[1]) continue;
+            if (I1 > I0 && ang1(I1 - 1, 2) >= ANG0[1]) break;
+            const int ID2 = I1 / 2;
+            for (int JM = -2; JM <= 2; JM += 4) {
+                double A11 = 0, A12 = 0;
+                const int JEND = JM < 0 ? 2 : NP;
+                for (int J1 = J0; JM > 0 ? J1 <= JEND - JM : J1 >= JEND - JM; J1 += JM) {
+                    if (A11 >= ANG0[2]) break;
+                    const int J12 = J1 + JM / 2;
+                    A12 = ang2(J12, 1);
+                    const double DANG = A12 - A11;
+                    if (DANG <= 1.0e-10) { A11 = A12; continue; }
+                    double A21 = A11;
+                    const int JD2 = J1 / 2;
+                    if (iqtm(ID2, JD2)) { A11 = A12; continue; }
+                    if (J1 == J0) {
+                        for (int L = 1; L <= NWL; ++L) Q11[L] = q2m(ID2, JD2, L) * HALF;
+                        if (JM > 0) for (int L = 1; L <= NWL; ++L) q2m(ID2, JD2, L) = ZERO;
+                    } else {
+                        for (int L = 1; L <= NWL; ++L) { Q11[L] = q2m(ID2, JD2, L); q2m(ID2, JD2, L) = ZERO; }
+                    }
+                    if (J1 != J0 || JM > 0) iqtm(ID2, JD2) = 1;
+                    const int IBC1 = ibr(I1, J1, K1);
+                    if (IBC1 == 301 || IBC1 == 311 || IBC1 == 4) {
+                        for (int L = 1; L <= NWL; ++L) qtx2(ID2, JD2, L) = qtx2(ID2, JD2, L) + Q11[L];
+                        iqt2(ID2, JD2) = 0;
+                        A11 = A12;
+                        continue;
+                    }
+                    for (int L = 1; L <= NWL; ++L) Q12[L] = Q11[L];
+                    for (int J2 = J1; JM > 0 ? J2 <= JEND : J2 >= JEND; J2 += JM) {
+                        const int J2M = J2 + JM / 2, J2D2 = J2 / 2;
+                        const int IBC2 = ibr(I1, J2, K1);
+                        bool to330 = IBC1 <= 0 && IBC2 >= 1;
+                        if (!to330) {
+                            if (IBC1 > 1 && IBC2 == 1) {
+                                if (I1 < I0) I2 = I1 + 2; else if (I1 > I0) I2 = I1 - 2;
+                                const int I2D2 = I2 / 2, J2D2M = J2D2 - JM / 2;
+                                for (int L = 1; L <= NWL; ++L) {
+                                    if (Q12[L] < small16) continue;
+                                    double Q21 = Q12[L] * HALF;
+                                    qtx2(I2D2, J2D2, L) = qtx2(I2D2, J2D2, L) + Q21;
+                                    qtx2(ID2, J2D2M, L) = qtx2(ID2, J2D2M, L) + Q21;
+                                }
+                                iqt2(I2D2, J2D2) = 0;
+                                iqt2(ID2, J2D2M) = 0;
+                                break;
+                            }
+                            if (J2M > NP || J2M < 2) to330 = true;
+                            else {
+                                const double A22 = ang2(J2M, 2);
+                                if ((A22 - A21) <= 1.0e-10) continue;
+                                if (A22 < A12) {
+                                    const double FIJ = (A22 - A21) / DANG;
+                                    for (int L = 1; L <= NWL; ++L) {
+                                        if (Q11[L] < small16) continue;
+                                        double Q21 = Q11[L] * FIJ;
+                                        qtx2(ID2, J2D2, L) = qtx2(ID2, J2D2, L) + Q21;
+                                        Q12[L] = Q12[L] - Q21;
+                                    }
+                                    iqt2(ID2, J2D2) = 0;
+                                    A21 = A22;
+                                    continue;
+                                }
+                            }
+                        }
+                        for (int L = 1; L <= NWL; ++L) qtx2(ID2, J2D2, L) = qtx2(ID2, J2D2, L) + Q12[L];
+                        iqt2(ID2, J2D2) = 0;
+                        break;
+                    }
+                    A11 = A12;
+                }
+            }
+        }
+    }
+
+    // ---- QREF (Qre.f90:31-515); ANG0 follows SANG1 for an open cell -----------
+    void QREF(int I0, int J0, int K0) {
+        qa_sum_bnd = qa_sum_vol = 0;
+        c_melt = c_exit = c_inlet = c_wall = c_open = 0;
+        const int I0D2 = I0 / 2, J0D2 = J0 / 2, K0D2 = K0 / 2;
+        for (int L = 1; L <= NWL; ++L) qel(I0D2, J0D2, K0D2, L) = ZERO;
+        if (ibr(I0, J0, K0) >= 1) return;
+        const double G0 = SGN * T4(o.a3(o.T, I0, J0, K0));
+        for (int L = 1; L <= NWL; ++L) QEL0[L] = DEB[L] * akl(I0D2, J0D2, K0D2, L) * G0;
+
+        // x-flux
+        for (int L = 1; L <= NWL; ++L) QEL1[L] = QEL0[L] * o.DR[J0] * o.DZ[K0];
+        alloc_slab(NZ, LZ);
+        for (int IPM = -2; IPM <= 2; IPM += 4) {
+            for (int L = 1; L <= NWL; ++L) qtx1(J0D2, K0D2, L) = QEL1[L];
+            iqt1(J0D2, K0D2) = 0;
+            for (int L = 1; L <= NWL; ++L) qel(I0D2, J0D2, K0D2, L) = qel(I0D2, J0D2, K0D2, L) + QEL1[L];
+            {
+                const int i1 = I0 + IPM / 2, j1 = J0 + IPM / 2, k1 = K0 + IPM / 2;
+                ANG0[1] = 0;
+                double b = std::fabs(X(i1) - X(I0));
+                if (b < small16) { ANG0[2] = 90; ANG0[3] = 90; }
+                else { ANG0[2] = ATAND(std::fabs(R(j1) - R(J0)) / b); ANG0[3] = ATAND(std::fabs(Z(k1) - Z(K0)) / b); }
+            }
+            for (int j = 1; j <= NP; ++j) { ang2(j, 1) = ANG0[2]; ang2(j, 2) = ANG0[2]; }
+            ang2(J0, 1) = ang2(J0, 2) = ZERO;
+            for (int k = 1; k <= LP; ++k) { ang3(k, 1) = ANG0[3]; ang3(k, 2) = ANG0[3]; }
+            ang3(K0, 1) = ang3(K0, 2) = ZERO;
+            const int IEND = IPM < 0 ? 2 : MP;
+            for (int I = I0 + IPM; IPM > 0 ? I <= IEND : I >= IEND; I += IPM) {
+                QRTX(I0, J0, K0, I - IPM, I);
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) absorb(I, J, K, J / 2, K / 2, I == IEND);
+                for (int j = 1; j <= NP; ++j) ang2(j, 1) = ang2(j, 2);
+                for (int k = 1; k <= LP; ++k) ang3(k, 1) = ang3(k, 2);
+            }
+        }
+        // y-flux
+        for (int L = 1; L <= NWL; ++L) QEL1[L] = QEL0[L] * o.DX[I0] * o.DZ[K0];
+        alloc_slab(MZ, LZ);
+        for (int JPM = -2; JPM <= 2; JPM += 4) {
+            for (int L = 1; L <= NWL; ++L) qtx1(I0D2, K0D2, L) = QEL1[L];
+            iqt1(I0D2, K0D2) = 0;
+            for (int L = 1; L <= NWL; ++L) qel(I0D2, J0D2, K0D2, L) = qel(I0D2, J0D2, K0D2, L) + QEL1[L];
+            {
+                const int i1 = I0 + JPM / 2, j1 = J0 + JPM / 2, k1 = K0 + JPM / 2;
+                ANG0[2] = 0;
+                double b = std::fabs(R(j1) - R(J0));
+                if (b < small16) { ANG0[1] = 90; ANG0[3] = 90; }
+                else { ANG0[1] = ATAND(std::fabs(X(i1) - X(I0)) / b); ANG0[3] = ATAND(std::fabs(Z(k1) - Z(K0)) / b); }
+            }
+            for (int i = 1; i <= MP; ++i) { ang1(i, 1) = ANG0[1]; ang1(i, 2) = ANG0[1]; }
+            ang1(I0, 1) = ang1(I0, 2) = ZERO;
+            for (int k = 1; k <= LP; ++k) { ang3(k, 1) = ANG0[3]; ang3(k, 2) = ANG0[3]; }
+            ang3(K0, 1) = ang3(K0, 2) = ZERO;
+            const int JEND = JPM < 0 ? 2 : NP;
+            for (int J = J0 + JPM; JPM > 0 ? J <= JEND : J >= JEND; J += JPM) {
+                QRTY(I0, J0, K0, J - JPM, J);
+                for (int I = 2; I <= MP; I += 2)
+                    for (int K = 2; K <= LP; K += 2) absorb(I, J, K, I / 2, K / 2, J == JEND);
+                for (int i = 1; i <= MP; ++i) ang1(i, 1) = ang1(i, 2);
+                for (int k = 1; k <= LP; ++k) ang3(k, 1) = ang3(k, 2);
+            }
+        }
+        // z-flux
+        for (int L = 1; L <= NWL; ++L) QEL1[L] = QEL0[L] * o.DX[I0] * o.DR[J0];
+        alloc_slab(MZ, NZ);
+        for (int KPM = -2; KPM <= 2; KPM += 4) {
+            for (int L = 1; L <= NWL; ++L) qtx1(I0D2, J0D2, L) = QEL1[L];
+            iqt1(I0D2, J0D2) = 0;
+            for (int L = 1; L <= NWL; ++L) qel(I0D2, J0D2, K0D2, L) = qel(I0D2, J0D2, K0D2, L) + QEL1[L];
+            {
+                const int i1 = I0 + KPM / 2, j1 = J0 + KPM / 2, k1 = K0 + KPM / 2;
+                ANG0[3] = 0;
+                double b = std::fabs(Z(k1) - Z(K0));
+                if (b < small16) { ANG0[1] = 90; ANG0[2] = 90; }
+                else { ANG0[1] = ATAND(std::fabs(X(i1) - X(I0)) / b); ANG0[2] = ATAND(std::fabs(R(j1) - R(J0)) / b); }
+            }
+            for (int i = 1; i <= MP; ++i) { ang1(i, 1) = ANG0[1]; ang1(i, 2) = ANG0[1]; }
+            ang1(I0, 1) = ang1(I0, 2) = ZERO;
+            for (int j = 1; j <= NP; ++j) { ang2(j, 1) = ANG0[2]; ang2(j, 2) = ANG0[2]; }
+            ang2(J0, 1) = ang2(J0, 2) = ZERO;
+            const int KEND = KPM < 0 ? 2 : LP;
+            for (int K = K0 + KPM; KPM > 0 ? K <= KEND : K >= KEND; K += KPM) {
+                QRTZ(I0, J0, K0, K - KPM, K);
+                for (int I = 2; I <= MP; I += 2)
+                    for (int J = 2; J <= NP; J += 2) absorb(I, J, K, I / 2, J / 2, K == KEND);
+                for (int i = 1; i <= MP; ++i) ang1(i, 1) = ang1(i, 2);
+                for (int j = 1; j <= NP; ++j) ang2(j, 1) = ang2(j, 2);
+            }
+        }
+        double qe = qel(I0D2, J0D2, K0D2, 1);
+        for (int L = 2; L <= NWL; ++L) qe = qe + qel(I0D2, J0D2, K0D2, L);
+        o.QE[o.cix(I0D2, J0D2, K0D2)] = qe;
+        qe_sum_from_open = qe_sum_from_open + qe;
+    }
+
+    void run() {
+        // wall markers (Rad_emis.f90:144-178) on a copy of IBCELL's cell values
+        IBR.assign(NC, 0);
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) IBR[cell(I / 2, J / 2, K / 2)] = o.ibcell(I, J, K);
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    if (ibr(I, J, K) != 1) continue;
+                    const int KM2 = std::max(K - 2, 2), KP2 = std::min(K + 2, LP);
+                    const int JM2 = std::max(J - 2, 2), JP2 = std::min(J + 2, NP);
+                    const int IM2 = std::max(I - 2, 2), IP2 = std::min(I + 2, MP);
+                    int& m = IBR[cell(I / 2, J / 2, K / 2)];
+                    if (ibr(I, J, KM2) <= 0) m = 301;
+                    else if (ibr(I, J, KP2) <= 0) m = 311;
+                    else if (ibr(I, JM2, K) <= 0) m = 201;
+                    else if (ibr(I, JP2, K) <= 0) m = 211;
+                    else if (ibr(IM2, J, K) <= 0) m = 101;
+                    else if (ibr(IP2, J, K) <= 0) m = 111;
+                }
+        for (auto& t : o.T) t = t * o.pr.t0;
+        // RAD0 (Rad0.f90:22-42, 112-166) with gray bands: AKLG = AKL0, AKLS = 0
+        SGN = o.pr.sig * o.pr.ri * o.pr.ri;
+        for (int L = 1; L <= NWL; ++L) DEB0[L] = o.pr.hck / o.pr.ri / o.WL[L - 1];
+        TG_MN = 300;
+        AKL.assign(NC * NWL, 0.0);
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    const double T_RAD = o.a3(o.T, I, J, K);
+                    if (!(ibr(I, J, K) <= 0 && T_RAD >= TG_MN)) continue;   // walls: emissivities, used only by the wall exchange
+                    const double VOL = o.VOL_C(I, J, K);
+                    const double SA = ((o.DX[I] * o.DR[J]) + (o.DR[J] * o.DZ[K]) + (o.DX[I] * o.DZ[K])) * TWO;
+                    if (SA <= small16) continue;
+                    const double OPL = 6.0 * VOL / SA;
+                    if (OPL <= 1.0e-10) continue;
+                    DEBX(T_RAD);
+                    const double area_sgn_t4 = SA * SGN * T4(T_RAD);
+                    double sg = ZERO, ss = ZERO;
+                    for (int L = 1; L <= NWL; ++L) {
+                        akl(I / 2, J / 2, K / 2, L) = EMF(o.AKL0[L - 1], OPL);
+                        sg = sg + DEB[L] * EMF(o.AKL0[L - 1], OPL);
+                        ss = ss + DEB[L] * EMF(ZERO, OPL);
+                    }
+                    tot_qe_h2o_co2 = tot_qe_h2o_co2 + (area_sgn_t4 * sg);
+                    tot_qe_soot = tot_qe_soot + (area_sgn_t4 * ss);
+                }
+        // QRNF (Qrn.f90:58-154)
+        std::fill(o.QE.begin(), o.QE.end(), 0.0);
+        std::fill(o.QA.begin(), o.QA.end(), 0.0);
+        QEL.assign(NC * NWL, 0.0);
+        QAL.assign(NC * NWL, 0.0);
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    if (ibr(I, J, K) >= 1) continue;
+                    if (o.a3(o.T, I, J, K) <= TG_MN) continue;
+                    DEBX(o.a3(o.T, I, J, K));
+                    QREF(I, J, K);
+                    ++n_emit;
+                    qa_sum_to_melt = qa_sum_to_melt + c_melt;
+                    qa_sum_to_exit = qa_sum_to_exit + c_exit;
+                    qa_sum_to_inlet = qa_sum_to_inlet + c_inlet;
+                    qa_sum_to_wall = qa_sum_to_wall + c_wall;
+                    qa_sum_to_open = qa_sum_to_open + c_open;
+                }
+        // QRN1 (Qrn.f90:250-259): QA of every cell
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    double G0 = 0;
+                    for (int L = 1; L <= NWL; ++L) G0 = G0 + qal(I / 2, J / 2, K / 2, L);
+                    o.QA[o.cix(I / 2, J / 2, K / 2)] = G0;
+                }
+        for (auto& t : o.T) t = t / o.pr.t0;
+        o.i1st_rad_qe_done = 1;
+    }
+};
+
 void copy_in(vec& dst, const double* src, long n) { dst.assign(src, src + n); }
 vec one_based(const double* src, int n) {
     vec v(n + 3, 0.0);
@@ -1737,6 +2498,27 @@ double gfo_calc_residual(void* vo, const double* xt, const double* ap, const dou
 double gfo_da(double d, double f) { return DA(d, f); }
 double gfo_tgamf(double b) { return TGAMF(b); }
 double gfo_emf(double xkl, double xl0) { return EMF(xkl, xl0); }
+double gfo_atand(double x) { return ATAND(x); }
+
+int gfo_rad_transfer(void* vo, gfm_rad_totals* out) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || o->NWL < 1) return GFM_E_ARG;
+    RadVolume rv(*o);
+    rv.run();
+    if (out) {
+        std::memset(out, 0, sizeof *out);
+        out->qe_sum_from_open = rv.qe_sum_from_open;
+        out->qa_sum_to_open = rv.qa_sum_to_open;
+        out->qa_sum_to_wall = rv.qa_sum_to_wall;
+        out->qa_sum_to_inlet = rv.qa_sum_to_inlet;
+        out->qa_sum_to_exit = rv.qa_sum_to_exit;
+        out->qa_sum_to_melt = rv.qa_sum_to_melt;
+        out->tot_qe_h2o_co2 = rv.tot_qe_h2o_co2;
+        out->tot_qe_soot = rv.tot_qe_soot;
+        out->n_emitters = rv.n_emit;
+    }
+    return GFM_OK;
+}
 double gfo_rif3(double x) { return RIF3(x); }
 double gfo_zy1(const double* x, const double* y, double x1, int n) { return ZY1(x, y, x1, n); }
 double gfo_t_to_enth(const double* y, double t_norm) {

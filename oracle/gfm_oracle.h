@@ -41,6 +41,10 @@ double gfo_calc_residual(void *o, const double *xt, const double *ap, const doub
 double gfo_da(double d, double f);
 double gfo_tgamf(double b);
 double gfo_emf(double xkl, double xl0);
+double gfo_atand(double x);
+/* Volume radiation transfer (RAD0 + QRNF/QREF/QRTX/Y/Z + QRN1): sets QE and
+ * QA of the state from its T and switches the radiation source term on. */
+int   gfo_rad_transfer(void *o, gfm_rad_totals *out);
 double gfo_rif3(double x);
 double gfo_zy1(const double *x, const double *y, double x1, int n);
 /* y: 9 GF components; returns normalised enthalpy / temperature */

@@ -43,11 +43,13 @@ def load(check_bounds: bool = False) -> C.CDLL:
     lib.gfo_adlbl3.argtypes = [C.c_void_p, dp, dp, C.POINTER(dp), dp] + [C.c_int] * 7
     lib.gfo_calc_residual.restype = C.c_double
     lib.gfo_calc_residual.argtypes = [C.c_void_p, dp, dp, C.POINTER(dp), dp] + [C.c_int] * 6
-    for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1"):
+    lib.gfo_rad_transfer.argtypes = [C.c_void_p, C.POINTER(abi.GfmRadTotals)]
+    for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1", "gfo_atand"):
         getattr(lib, n).restype = C.c_double
     lib.gfo_da.argtypes = [C.c_double, C.c_double]
     lib.gfo_tgamf.argtypes = [C.c_double]
     lib.gfo_emf.argtypes = [C.c_double, C.c_double]
+    lib.gfo_atand.argtypes = [C.c_double]
     lib.gfo_rif3.argtypes = [C.c_double]
     lib.gfo_zy1.argtypes = [dp, dp, C.c_double, C.c_int]
     lib.gfo_t_to_enth.argtypes = [dp, C.c_double]
@@ -82,6 +84,14 @@ class Oracle:
 
     def gflow_steps(self, stop_after: int) -> None:
         self.lib.gfo_gflow_steps(self.o, stop_after)
+
+    def rad_transfer(self) -> dict:
+        """Volume radiation transfer from the current T; QE and QA are replaced."""
+        t = abi.GfmRadTotals()
+        rc = self.lib.gfo_rad_transfer(self.o, C.byref(t))
+        if rc != 0:
+            raise RuntimeError(f"gfo_rad_transfer: {rc}")
+        return t.as_dict()
 
     def download(self) -> Fields:
         out = Fields.empty(self.case.mp, self.case.np, self.case.lp)
