@@ -365,6 +365,13 @@ def run_ours(args):
         if prec == abi.GFM_PREC_MIXED and not args.no_plain:
             ttr["fp64"] = time_to_residual(case, adi, abi.GFM_PREC_FP64, args.ttr, args.ttr_max)
 
+    rad = None
+    if rank == 0 and not args.no_rad:
+        try:
+            rad = rad_transfer_leg(not args.no_cpu_baseline)
+        except Exception as e:   # reported, never required
+            rad = {"failed": str(e)}
+
     learned = None
     if rank == 0 and args.learned:
         # learned p' guess: trained here on seeded variants of the 48x24x16
@@ -403,6 +410,7 @@ def run_ours(args):
             "field_error": ferr,
             "time_to_residual": ttr,
             "learned_p_prime": learned,
+            "rad_transfer": rad,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -413,6 +421,58 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def rad_transfer_leg(with_cpu: bool) -> dict:
+    """Volume radiation transfer (RAD0 + the QRNF emitter loop with QREF and
+    QRTX/QRTY/QRTZ, Qrn.f90:58-229) of the 48x24x16 furnace from the state
+    after 30 FP64 iterations: the whole call timed on the host around the
+    synchronous gfm_gpu_rad_transfer, next to the FP64 oracle on one host core
+    from the same state, and the largest per-cell difference of QA and QE."""
+    import numpy as np
+    from gfm_gb300 import Case, GpuSolver, abi, configs
+    case = Case(configs.small_furnace())
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_MARCH, precision=abi.GFM_PREC_FP64)
+    g.start()
+    g.gflow(30)
+    state = g.download()
+    g.rad_transfer()   # first call: buffers, kernel attributes
+    times = []
+    for _ in range(3):
+        g.upload(state)
+        t0 = time.perf_counter()
+        tot = g.rad_transfer()
+        times.append(time.perf_counter() - t0)
+    fg = g.download()
+    g.close()
+    gpu_s = sorted(times)[len(times) // 2]
+    out = {"workload": "volume radiation transfer, furnace_48x24x16 (18,432 cells), "
+                       f"{case.grid.nwl} gray bands, state after 30 FP64 iterations",
+           "emitters": tot["n_emitters"], "seconds": gpu_s, "seconds_all": times,
+           "emitters_per_s": tot["n_emitters"] / gpu_s,
+           "timing": "host wall clock around the synchronous call (median of 3)",
+           "energy_balance": (tot["qe_sum_from_open"] - sum(tot[k] for k in (
+               "qa_sum_to_open", "qa_sum_to_wall", "qa_sum_to_inlet", "qa_sum_to_exit", "qa_sum_to_melt")))
+           / tot["qe_sum_from_open"],
+           "totals": tot}
+    if with_cpu:
+        from oracle.pyoracle import Oracle
+        o = Oracle(case, state)
+        t0 = time.perf_counter()
+        o.rad_transfer()
+        cpu_s = time.perf_counter() - t0
+        fo = o.download()
+        o.close()
+        qa_g, qa_o = fg.arrays["qa"], fo.arrays["qa"]
+        sel = qa_o > 1e-9 * qa_o.max()
+        qe_o = fo.arrays["qe"]
+        hot = qe_o > 0
+        out["cpu_baseline"] = {"seconds": cpu_s, "cores": 1, "kind": "port",
+                               "sample": "the whole transfer of the same state, FP64 oracle on one host core"}
+        out["speedup_vs_cpu"] = cpu_s / gpu_s
+        out["max_rel_err"] = {"qa": float(np.max(np.abs(qa_g[sel] - qa_o[sel]) / qa_o[sel])),
+                              "qe": float(np.max(np.abs(fg.arrays["qe"][hot] - qe_o[hot]) / qe_o[hot]))}
+    return out
 
 
 def run_batched(args):
@@ -476,6 +536,7 @@ def main():
     ap.add_argument("--adi", choices=["redblack", "march"], default="redblack")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-rad", action="store_true", help="skip the volume radiation transfer leg")
     ap.add_argument("--ttr", type=float, default=None,
                     help="also measure the time from the fresh start to res_mass < TTR (mixed and FP64)")
     ap.add_argument("--ttr-max", type=int, default=3000)

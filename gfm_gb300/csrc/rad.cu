@@ -164,6 +164,8 @@ struct Dir {
 struct Slab {   // scratch of one CTA
     double *q1, *q2, *qm;        // QTX1, QTX2, Q2M: [l*A + e]
     unsigned char *f1, *f2, *fm; // IQT1, IQT2, IQTM
+    int16_t* ib;                 // IBCELL (with wall markers) of the current slab's cells: [e]
+    double *tU, *tV;             // far-face angle candidates of the current slab (1-based positions)
 };
 
 __device__ __forceinline__ bool rad_corner(int d, int ibc1) {
@@ -175,7 +177,6 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
     const int NWL = NW > 0 ? NW : a.NWL;
     double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
     const int bb = v1 / 2;
-    const int cbase = (slab / 2 - 1) * D.sd + (v1 / 2 - 1) * D.sv;
     for (int UPM = -2; UPM <= 2; UPM += 4) {
         double A11 = 0.0, A12 = 0.0;
         const int uend = UPM < 0 ? 2 : D.Du;
@@ -198,7 +199,7 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
             for (int l = 0; l < NWL; ++l) Q12[l] = Q11[l];
             for (int u2 = u1; UPM > 0 ? u2 <= uend : u2 >= uend; u2 += UPM) {
                 const int e2 = (bb - 1) * D.DA + (u2 / 2 - 1);
-                if (a.ibr[cbase + (u2 / 2 - 1) * D.su] < 1) {
+                if (S.ib[e2] < 1) {
                     const double A22 = D.angU2[u2 + UPM / 2];
                     if (A22 <= A21) continue;
                     if (A22 < A12) {
@@ -228,7 +229,6 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
     const int NWL = NW > 0 ? NW : a.NWL;
     double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
     const int aa = u1 / 2;
-    const int cbase = (slab / 2 - 1) * D.sd + (u1 / 2 - 1) * D.su;
     const bool edge = u1 == 2 || u1 == D.Du;
     for (int KM = -2; KM <= 2; KM += 4) {
         double A11 = 0.0, A12 = 0.0;
@@ -249,7 +249,7 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
                 for (int l = 0; l < NWL; ++l) { Q11[l] = S.qm[l * D.A + e]; S.qm[l * D.A + e] = 0.0; }
             }
             if (v1 != D.v0 || KM > 0) S.fm[e] = 1;
-            const int ibc1 = a.ibr[cbase + (v1 / 2 - 1) * D.sv];
+            const int ibc1 = S.ib[e];
             if (ibc1 == D.direct1 || ibc1 == D.direct2 || ibc1 == 4) {
                 for (int l = 0; l < NWL; ++l) S.q2[l * D.A + e] = S.q2[l * D.A + e] + Q11[l];
                 S.f2[e] = 0;
@@ -260,7 +260,7 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
             for (int v2 = v1; KM > 0 ? v2 <= vend : v2 >= vend; v2 += KM) {
                 const int v2m = v2 + KM / 2;
                 const int e2 = (v2 / 2 - 1) * D.DA + (aa - 1);
-                const int ibc2 = a.ibr[cbase + (v2 / 2 - 1) * D.sv];
+                const int ibc2 = S.ib[e2];
                 bool to330 = ibc1 <= 0 && ibc2 >= 1;
                 if (!to330) {
                     if (rad_corner(D.d, ibc1) && ibc2 == 1) {
@@ -353,21 +353,35 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
         __syncthreads();
         const int dend = s < 0 ? 2 : D.Dd;
         for (int slab = D.d0 + 2 * s; s > 0 ? slab <= dend : slab >= dend; slab += 2 * s) {
-            // SANG2: far-face angles of the slab, the outward scan with its
-            // exit, one thread per transverse axis
+            // the slab's IBCELL codes, and SANG2: the far-face angles of every
+            // transverse face in parallel, then the reference's outward scan
+            // with its early exit, one thread per transverse axis
             int far = slab + s;
             far = min(far, D.Dd);
             const double b = fabs(D.cd[far] - D.cd[D.d0]);
+            for (int e = tid; e < D.A; e += nth)
+                S.ib[e] = a.ibr[(slab / 2 - 1) * D.sd + (e % D.DA) * D.su + (e / D.DA) * D.sv];
+            {
+                const int nu = D.Du / 2, nv = D.Dv / 2;   // odd positions 1 .. Du-1 and 1 .. Dv-1
+                for (int i = tid; i < nu + nv; i += nth) {
+                    const bool isu = i < nu;
+                    const int pp = 2 * (isu ? i : i - nu) + 1;
+                    const double* c = isu ? D.cu : D.cv;
+                    const int p0 = isu ? D.u0 : D.v0;
+                    (isu ? S.tU : S.tV)[pp] = b < kSmall16 ? 90.0 : rad_atand(fabs(c[pp] - c[p0]) / b);
+                }
+            }
+            __syncthreads();
             if (tid == 0 || tid == 32) {
                 const bool isu = tid == 0;
                 const int P = isu ? D.Du : D.Dv, p0 = isu ? D.u0 : D.v0;
-                const double* c = isu ? D.cu : D.cv;
+                const double* cand = isu ? S.tU : S.tV;
                 double* out = isu ? D.angU2 : D.angV2;
                 const double lim = isu ? ang0u : ang0v;
                 for (int M = -1; M <= 1; M += 2) {
                     const int pend = M < 0 ? 2 : P;
                     for (int pp = p0 + M; M > 0 ? pp <= pend : pp >= pend; pp += 2 * M) {
-                        const double aa = b < kSmall16 ? 90.0 : rad_atand(fabs(c[pp] - c[p0]) / b);
+                        const double aa = cand[pp];
                         if (aa >= lim) break;
                         out[pp] = aa;
                     }
@@ -402,7 +416,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 if (S.f2[e]) continue;
                 const int ua = e % D.DA + 1, vb = e / D.DA + 1;
                 const int c = (slab / 2 - 1) * D.sd + (ua - 1) * D.su + (vb - 1) * D.sv;
-                const int ib = a.ibr[c];
+                const int ib = S.ib[e];
                 for (int l = 0; l < NWL; ++l) {
                     const double q = S.q2[l * D.A + e];
                     if (q < kSmall16) continue;
@@ -450,8 +464,11 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a) {
     double* ang1 = ang;                          // ANG1(.,1), ANG1(.,2)
     double* ang2 = ang1 + 2 * (a.MP + 2);
     double* ang3 = ang2 + 2 * (a.NP + 2);
-    double* arr = ang3 + 2 * (a.LP + 2);
+    double* tmp = ang3 + 2 * (a.LP + 2);         // angle candidates: (MP+2) + (NP+2) + (LP+2)
+    int16_t* sib = reinterpret_cast<int16_t*>(tmp + (a.MP + 2) + (a.NP + 2) + (a.LP + 2));
+    double* arr = reinterpret_cast<double*>(sib + ((a.A + 7) / 8) * 8);
     Slab S;
+    S.ib = sib;
     if (a.slab_in_smem) {
         S.q1 = arr;
     } else {
@@ -512,6 +529,11 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a) {
             D.angU1 = angs[D.u]; D.angU2 = angs[D.u] + angw[D.u];
             D.angV1 = angs[D.v]; D.angV2 = angs[D.v] + angw[D.v];
             D.direct1 = 100 * (d + 1) + 1; D.direct2 = 100 * (d + 1) + 11;
+            {
+                double* tmps[3] = {tmp, tmp + (a.MP + 2), tmp + (a.MP + 2) + (a.NP + 2)};
+                S.tU = tmps[D.u];
+                S.tV = tmps[D.v];
+            }
             if (tid == 0)
                 for (int l = 0; l < NWL; ++l) s_qel1[l] = s_qel0[l] * dface[D.u][D.u0] * dface[D.v][D.v0];
             __syncthreads();
@@ -568,8 +590,8 @@ __global__ void k_rad_t_roundtrip(R* T, long long n, double t0) {
         T[t] = R(((double)T[t] * t0) / t0);
 }
 
-size_t rad_smem_fixed(const RadArgs& a) {
-    return sizeof(double) * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2) + 2 * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2)));
+size_t rad_smem_fixed(const RadArgs& a) {   // coordinates, ANG1/2/3, angle candidates, slab IBCELL
+    return sizeof(double) * (4 * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2))) + sizeof(int16_t) * (((size_t)a.A + 7) / 8 * 8);
 }
 size_t rad_smem_slab(const RadArgs& a) { return (size_t)3 * a.A * a.NWL * sizeof(double) + (size_t)3 * a.A; }
 
