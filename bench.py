@@ -303,7 +303,12 @@ def run_ours(args):
     solver2.upload(fields)
     solver2.initsv()
     solver2.gflow(max(args.warmup, 0))
-    host_state = solver2.download()
+    state = solver2.download()
+    host_state = pinned_fields(case)            # the step's inputs, in pinned host memory
+    for k, v in state.arrays.items():
+        host_state.arrays[k][...] = v
+    for a in ("itr_gas", "do_rad_qe_only_cnt", "i1st_rad_qe_done", "factor", "fadj", "gfin0", "q_h_in"):
+        setattr(host_state, a, getattr(state, a))
     out = pinned_fields(case)
     import ctypes as C
     barrier(dist)

@@ -370,17 +370,6 @@ __global__ void k_t_roundtrip(R* T, long long n, double t0) {
         T[t] = R(((double)T[t] * t0) / t0);
 }
 
-// count non-finite values of an uploaded reference-layout array
-__global__ void k_count_nonfinite(const double* __restrict__ a, long long n, unsigned int* cnt) {
-    unsigned int local = 0;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
-        local += isfinite(a[t]) ? 0u : 1u;
-    if (local) atomicAdd(cnt, local);
-}
-void launch_count_nonfinite(const double* a, long long n, unsigned int* cnt, cudaStream_t s) {
-    k_count_nonfinite<<<gridn(n), kBlk, 0, s>>>(a, n, cnt);
-}
-
 // ---------------------------------------------------------------------------
 // layout conversion
 // ---------------------------------------------------------------------------
@@ -393,6 +382,22 @@ __global__ void k_to_split(GeoT<R> g, const double* __restrict__ src, R* __restr
         int J = (int)(r % g.NP) + 1, K = (int)(r / g.NP) + 1;
         dst[pidx(g, I, J, K)] = R(src[t]);
     }
+}
+// conversion of an uploaded field with its count of non-finite values, one
+// read of the source (which may be mapped host memory)
+template <typename R>
+__global__ void k_to_split_count(GeoT<R> g, const double* __restrict__ src, R* __restrict__ dst, unsigned int* cnt) {
+    const long long n = (long long)g.MP * g.NP * g.LP;
+    unsigned int local = 0;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int I = (int)(t % g.MP) + 1;
+        long long r = t / g.MP;
+        int J = (int)(r % g.NP) + 1, K = (int)(r / g.NP) + 1;
+        const double v = src[t];
+        local += isfinite(v) ? 0u : 1u;
+        dst[pidx(g, I, J, K)] = R(v);
+    }
+    if (local) atomicAdd(cnt, local);
 }
 template <typename R>
 __global__ void k_from_split(GeoT<R> g, const R* __restrict__ src, double* __restrict__ dst) {
@@ -504,6 +509,9 @@ template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int 
 template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s) {
     k_to_split<R><<<gridn((long long)g.MP * g.NP * g.LP), kBlk, 0, s>>>(g, src, dst);
 }
+template <typename R> void launch_to_split_count(const GeoT<R>& g, const double* src, R* dst, unsigned int* cnt, cudaStream_t s) {
+    k_to_split_count<R><<<gridn((long long)g.MP * g.NP * g.LP), kBlk, 0, s>>>(g, src, dst, cnt);
+}
 template <typename R> void launch_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s) {
     k_from_split<R><<<gridn((long long)g.MP * g.NP * g.LP), kBlk, 0, s>>>(g, src, dst);
 }
@@ -523,6 +531,7 @@ template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* sr
     template void launch_factor<R>(const Ctx<R>&, cudaStream_t);                                                   \
     template void launch_pref_idx<R>(const Ctx<R>&, int, int, int, int, int, int, double, double, cudaStream_t);  \
     template void launch_to_split<R>(const GeoT<R>&, const double*, R*, cudaStream_t);                             \
+    template void launch_to_split_count<R>(const GeoT<R>&, const double*, R*, unsigned int*, cudaStream_t);        \
     template void launch_from_split<R>(const GeoT<R>&, const R*, double*, cudaStream_t);                           \
     template void launch_cells_to_split<R>(const GeoT<R>&, const double*, R*, cudaStream_t);                       \
     template void launch_cells_from_split<R>(const GeoT<R>&, const R*, double*, cudaStream_t);

@@ -41,6 +41,13 @@ struct HostGrid {
 
 }  // namespace
 
+constexpr int kXferSlots = 22;   // P T DNST THETA TMU GAMA CRATE HRATE BSH, UG x3, GF x8, QA, QE
+// Copies of one transfer go round-robin over this many streams.  From 1 to 8
+// streams the rate stayed at about 215 GB/s host-to-device and 173 GB/s back
+// (1.71 GB of FP64 state); kernels reading and writing page-locked host arrays
+// in place reached the same rates, so the copies are kept.
+constexpr int kXferStreams = 2;
+
 struct gfm_handle {
     int prec = GFM_PREC_FP64;
     int adi_mode = GFM_ADI_MARCH;
@@ -60,6 +67,12 @@ struct gfm_handle {
     int* d_wall = nullptr;
     int n_wall = 0;
     double* d_stage = nullptr;      // doubled-layout staging buffer (N doubles)
+    // upload/download of the whole state: one staging slot per field, host
+    // copies on their own stream, ordered by events against the layout kernels
+    double* d_stage_all = nullptr;  // kXferSlots x N doubles (allocated at the first transfer)
+    unsigned int* d_bad_all = nullptr;
+    cudaStream_t copy_stream[kXferStreams]{};   // fields go round-robin over these
+    cudaEvent_t ev_xfer[kXferSlots + 1]{};
     unsigned int* d_bad = nullptr;  // non-finite counter of uploaded arrays
     double* h_scal = nullptr;       // pinned copy of the device scalars
     int pref_i1 = 0, pref_j1 = 0, pref_k1 = 0, pref_i2 = 0, pref_j2 = 0, pref_k2 = 0;
@@ -628,71 +641,100 @@ int initsv_dev(gfm_handle* h, Ctx<R>& c) {
     return GFM_OK;
 }
 
+// staging slots, copy stream and events of the whole-state transfers
+int xfer_prepare(gfm_handle* h) {
+    if (h->d_stage_all) return GFM_OK;
+    int rc;
+    if ((rc = dalloc(h, &h->d_stage_all, (long long)kXferSlots * h->N)) || (rc = dalloc(h, &h->d_bad_all, kXferSlots)))
+        return rc;
+    for (int s = 0; s < kXferStreams; ++s) CK(cudaStreamCreateWithFlags(&h->copy_stream[s], cudaStreamNonBlocking));
+    for (int i = 0; i <= kXferSlots; ++i) CK(cudaEventCreateWithFlags(&h->ev_xfer[i], cudaEventDisableTiming));
+    return GFM_OK;
+}
+
+// One field of a whole-state transfer: host array, device array, element
+// count (N for the doubled-layout fields, the cell count for QA/QE).
+template <typename R>
+struct XferItem {
+    double* host;
+    R* dev;
+    bool cells;
+    const char* name;
+};
+
+template <typename R>
+int xfer_items(gfm_handle* h, Ctx<R>& c, const gfm_fields* f, std::vector<XferItem<R>>& it) {
+    const long long N = h->N;
+    auto add = [&](double* host, R* dev, bool cells, const char* name) { if (host) it.push_back({host, dev, cells, name}); };
+    add(f->p, c.P, false, "p"); add(f->t, c.T, false, "t"); add(f->dnst, c.DNST, false, "dnst");
+    add(f->theta, c.THETA, false, "theta"); add(f->tmu, c.TMU, false, "tmu"); add(f->gama, c.GAMA, false, "gama");
+    add(f->crate, c.CRATE, false, "crate"); add(f->hrate, c.HRATE, false, "hrate"); add(f->bs_hprev, c.BSH, false, "bs_hprev");
+    for (int l = 0; l < 3; ++l) add(f->ug ? f->ug + l * N : nullptr, c.UG[l], false, "ug");
+    for (int l = 0; l < 9; ++l) if (l != 7) add(f->gf ? f->gf + l * N : nullptr, c.GF[l], false, "gf");
+    add(f->qa, c.QA, true, "qa");
+    add(f->qe, c.QE, true, "qe");
+    return (int)it.size() <= kXferSlots ? GFM_OK : GFM_E_ARG;
+}
+
+// Host -> device: every field's copy is queued on the copy stream into its own
+// staging slot; the compute stream waits for each copy, counts its non-finite
+// values and converts it to the device layout while later copies run.
 template <typename R>
 int upload_fields(gfm_handle* h, Ctx<R>& c, const gfm_fields* f) {
     const long long N = h->N;
     const GeoT<R>& g = c.g;
     cudaStream_t st = h->stream;
-    const char* bad_name = nullptr;
-    auto put_named = [&](const double* src, R* dst, const char* name) -> int {
-        if (!src) return GFM_OK;
-        CK(cudaMemsetAsync(h->d_bad, 0, sizeof(unsigned int), st));
-        CK(cudaMemcpyAsync(h->d_stage, src, N * sizeof(double), cudaMemcpyHostToDevice, st));
-        launch_count_nonfinite(h->d_stage, N, h->d_bad, st);
-        launch_to_split(g, h->d_stage, dst, st);
-        unsigned int nb = 0;
-        CK(cudaMemcpyAsync(&nb, h->d_bad, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        if (nb && !bad_name) bad_name = name;
-        return GFM_OK;
-    };
-    auto put = [&](const double* src, R* dst) -> int { return put_named(src, dst, "field"); };
     int rc;
-    if ((rc = put_named(f->p, c.P, "p")) || (rc = put_named(f->t, c.T, "t")) || (rc = put_named(f->dnst, c.DNST, "dnst")))
-        return rc;
-    if ((rc = put(f->theta, c.THETA)) ||
-        (rc = put(f->tmu, c.TMU)) || (rc = put(f->gama, c.GAMA)) || (rc = put(f->crate, c.CRATE)) ||
-        (rc = put(f->hrate, c.HRATE)) || (rc = put(f->bs_hprev, c.BSH)))
-        return rc;
-    for (int l = 0; l < 3; ++l) if ((rc = put_named(f->ug ? f->ug + l * N : nullptr, c.UG[l], "ug"))) return rc;
-    for (int l = 0; l < 9; ++l) {
-        if (l == 7) continue;
-        if ((rc = put_named(f->gf ? f->gf + l * N : nullptr, c.GF[l], "gf"))) return rc;
+    if ((rc = xfer_prepare(h))) return rc;
+    std::vector<XferItem<R>> it;
+    if ((rc = xfer_items(h, c, f, it))) return rc;
+    const long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    CK(cudaMemsetAsync(h->d_bad_all, 0, kXferSlots * sizeof(unsigned int), st));
+    // the staging slots may still be read by earlier work on the compute stream
+    CK(cudaEventRecord(h->ev_xfer[kXferSlots], st));
+    for (int s = 0; s < kXferStreams; ++s) CK(cudaStreamWaitEvent(h->copy_stream[s], h->ev_xfer[kXferSlots], 0));
+    for (size_t i = 0; i < it.size(); ++i) {
+        double* slot = h->d_stage_all + (long long)i * N;
+        const long long n = it[i].cells ? ncell : N;
+        cudaStream_t cs = h->copy_stream[i % kXferStreams];
+        CK(cudaMemcpyAsync(slot, it[i].host, n * sizeof(double), cudaMemcpyHostToDevice, cs));
+        CK(cudaEventRecord(h->ev_xfer[i], cs));
+        CK(cudaStreamWaitEvent(st, h->ev_xfer[i], 0));
+        if (it[i].cells) launch_cells_to_split(g, slot, it[i].dev, st);
+        else launch_to_split_count(g, slot, it[i].dev, h->d_bad_all + i, st);
     }
-    long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
-    if (f->qa) { CK(cudaMemcpyAsync(h->d_stage, f->qa, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QA, st); }
-    if (f->qe) { CK(cudaMemcpyAsync(h->d_stage, f->qe, ncell * sizeof(double), cudaMemcpyHostToDevice, st)); launch_cells_to_split(g, h->d_stage, c.QE, st); }
+    unsigned int nb[kXferSlots] = {};
+    CK(cudaMemcpyAsync(nb, h->d_bad_all, kXferSlots * sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
-    if (bad_name) { h->err = std::string("non-finite values in uploaded array ") + bad_name; return GFM_E_NAN; }
+    for (size_t i = 0; i < it.size(); ++i)
+        if (nb[i]) { h->err = std::string("non-finite values in uploaded array ") + it[i].name; return GFM_E_NAN; }
     return GFM_OK;
 }
 
+// Device -> host: the compute stream converts every field into its staging
+// slot; the copy stream sends each slot to the host as soon as it is ready.
 template <typename R>
 int download_fields(gfm_handle* h, Ctx<R>& c, gfm_fields* f) {
     const long long N = h->N;
     const GeoT<R>& g = c.g;
     cudaStream_t st = h->stream;
-    auto get = [&](const R* src, double* dst) -> int {
-        if (!dst) return GFM_OK;
-        launch_from_split(g, src, h->d_stage, st);
-        CK(cudaMemcpyAsync(dst, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        return GFM_OK;
-    };
     int rc;
-    if ((rc = get(c.P, f->p)) || (rc = get(c.T, f->t)) || (rc = get(c.DNST, f->dnst)) || (rc = get(c.THETA, f->theta)) ||
-        (rc = get(c.TMU, f->tmu)) || (rc = get(c.GAMA, f->gama)) || (rc = get(c.CRATE, f->crate)) ||
-        (rc = get(c.HRATE, f->hrate)) || (rc = get(c.BSH, f->bs_hprev)))
-        return rc;
-    for (int l = 0; l < 3; ++l) if ((rc = get(c.UG[l], f->ug ? f->ug + l * N : nullptr))) return rc;
-    for (int l = 0; l < 9; ++l) {
-        if (l == 7) { if (f->gf) std::memset(f->gf + 7 * N, 0, N * sizeof(double)); continue; }
-        if ((rc = get(c.GF[l], f->gf ? f->gf + l * N : nullptr))) return rc;
+    if ((rc = xfer_prepare(h))) return rc;
+    std::vector<XferItem<R>> it;
+    if ((rc = xfer_items(h, c, f, it))) return rc;
+    const long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    for (size_t i = 0; i < it.size(); ++i) {
+        double* slot = h->d_stage_all + (long long)i * N;
+        if (it[i].cells) launch_cells_from_split(g, it[i].dev, slot, st);
+        else launch_from_split(g, it[i].dev, slot, st);
+        cudaStream_t cs = h->copy_stream[i % kXferStreams];
+        CK(cudaEventRecord(h->ev_xfer[i], st));
+        CK(cudaStreamWaitEvent(cs, h->ev_xfer[i], 0));
+        CK(cudaMemcpyAsync(it[i].host, slot, (it[i].cells ? ncell : N) * sizeof(double), cudaMemcpyDeviceToHost, cs));
     }
-    long long ncell = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
-    if (f->qa) { launch_cells_from_split(g, c.QA, h->d_stage, st); CK(cudaMemcpyAsync(f->qa, h->d_stage, ncell * sizeof(double), cudaMemcpyDeviceToHost, st)); }
-    if (f->qe) { launch_cells_from_split(g, c.QE, h->d_stage, st); CK(cudaMemcpyAsync(f->qe, h->d_stage, ncell * sizeof(double), cudaMemcpyDeviceToHost, st)); }
+    for (int s = 0; s < kXferStreams; ++s) CK(cudaStreamSynchronize(h->copy_stream[s]));
     CK(cudaStreamSynchronize(st));
+    if (f->gf) std::memset(f->gf + 7 * N, 0, N * sizeof(double));   // GF(..,8) is not a field of this path
     f->itr_gas = h->itr_gas;
     f->do_rad_qe_only_cnt = h->cnt_qe;
     f->i1st_rad_qe_done = h->rad_active;
@@ -1335,6 +1377,9 @@ extern "C" void gfm_gpu_destroy(gfm_handle* h) {
     if (h->ev_g1) cudaEventDestroy(h->ev_g1);
     if (h->ev_adi0) cudaEventDestroy(h->ev_adi0);
     if (h->ev_adi1) cudaEventDestroy(h->ev_adi1);
+    for (int i = 0; i <= kXferSlots; ++i) if (h->ev_xfer[i]) cudaEventDestroy(h->ev_xfer[i]);
+    for (int s = 0; s < kXferStreams; ++s)
+        if (h->copy_stream[s]) { cudaStreamSynchronize(h->copy_stream[s]); cudaStreamDestroy(h->copy_stream[s]); }
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -175,7 +175,6 @@ void launch_finish(const double* partials, double* scal, const FinishSpec& f, do
 template <typename R> void launch_pref_idx(const Ctx<R>& c, int I1, int J1, int K1, int I2, int J2, int K2, double F1,
                                            double F2, cudaStream_t s);
 
-void launch_count_nonfinite(const double* a, long long n, unsigned int* cnt, cudaStream_t s);
 
 // learned p' initial guess (lpsolve.cu): network inputs (BF16, 16 channels per
 // voxel of the p' solve range), guess + fallback into x, training target
@@ -185,6 +184,7 @@ template <typename R> void launch_lp_target(const Ctx<R>& c, const R* x, float* 
 
 // layout conversion doubled <-> parity split (host-layout arrays on device)
 template <typename R> void launch_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);
+template <typename R> void launch_to_split_count(const GeoT<R>& g, const double* src, R* dst, unsigned int* cnt, cudaStream_t s);
 template <typename R> void launch_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s);
 template <typename R> void launch_cells_to_split(const GeoT<R>& g, const double* src, R* dst, cudaStream_t s);
 template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* src, double* dst, cudaStream_t s);

@@ -138,3 +138,47 @@ def test_batched_iterations_match_single_handle_runs():
         for name in ("p", "t", "ug"):
             assert np.array_equal(f1.arrays[name], f0.arrays[name]), name
         s.close()
+
+
+def _pinned_like(fields):
+    torch = pytest.importorskip("torch")
+    out = fields.copy()
+    for k, v in fields.arrays.items():
+        a = torch.empty(v.shape, dtype=torch.float64, pin_memory=True).numpy()
+        a[...] = v
+        out.arrays[k] = a
+    return out
+
+
+@pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])
+def test_pinned_host_arrays_transfer_with_the_same_results(prec):
+    """Page-locked host arrays (the fast copies of the end-to-end leg): the
+    state that crosses is the same bit for bit as through pageable arrays, and
+    non-finite inputs are still found per field."""
+    case = Case(configs.tiny_furnace())
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+    g.start()
+    g.gflow(3)
+    pageable = g.download()
+    pinned = _pinned_like(case.initial_fields())
+    import ctypes as C
+    f = pinned.to_c()
+    g._check(g.lib.gfm_gpu_download(g.h, C.byref(f)))
+    pinned.update_scalars(f)
+    for k in pageable.arrays:
+        assert np.array_equal(pinned.arrays[k], pageable.arrays[k]), k
+    g2 = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+    g2.upload(pinned)
+    back = g2.download()
+    for k in pageable.arrays:
+        assert np.array_equal(back.arrays[k], pageable.arrays[k]), k
+    s1, _ = g.gflow(2)
+    s2, _ = g2.gflow(2)
+    assert s1["res_mass"] == s2["res_mass"]
+    bad = _pinned_like(case.initial_fields())
+    bad.arrays["dnst"][3, 5, 7] = np.inf
+    with pytest.raises(GfmError) as ei:
+        g2.upload(bad)
+    assert ei.value.rc == abi.GFM_E_NAN and "dnst" in str(ei.value)
+    g.close()
+    g2.close()
