@@ -105,8 +105,10 @@ __device__ void rad_debx(const RadArgs& a, double t, double* deb) {   // DEBX, R
 }
 
 // RAD0 (ID_RAD=10), gray bands: AKLG = AKL0, AKLS = 0.  Also the cell
-// temperature in kelvin (T*T0), the one the transfer reads.  Block partials of
-// the two band-emission totals are summed on the host in block order.
+// temperature in kelvin (T*T0), the one the transfer reads, and for every
+// emitter (open, T > TG_MN) QREF's emission per unit area of each band,
+// QEL0 = DEB*AKL*SGN*T^4 (Qre.f90:80-86), with the same DEB.  Block partials
+// of the two band-emission totals are summed on the host in block order.
 template <typename R>
 __global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict__ T) {
     __shared__ double sh[2][256];
@@ -116,7 +118,7 @@ __global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict_
         const int I = 2 * (c % a.MZ + 1), J = 2 * ((c / a.MZ) % a.NZ + 1), K = 2 * (c / (a.MZ * a.NZ) + 1);
         const double t = (double)T[pidx(a.g, I, J, K)] * a.t0;
         a.tcell[c] = t;
-        for (int l = 0; l < a.NWL; ++l) a.akl[c + (long long)l * n] = 0.0;
+        for (int l = 0; l < a.NWL; ++l) { a.akl[c + (long long)l * n] = 0.0; a.qel0[c + (long long)l * n] = 0.0; }
         if (!(a.ibr[c] <= 0 && t >= kTgMn)) continue;
         const double dx = a.g.DX[I], dr = a.g.DR[J], dz = a.g.DZ[K];
         const double vol = dx * dr * a.g.RS[J] * dz;                  // VOL_C at a cell centre (VOL_C0)
@@ -129,8 +131,12 @@ __global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict_
         const double t2 = t * t;
         const double area_sgn_t4 = sa * a.sgn * (t2 * t2);
         double sg = 0.0, ss = 0.0;
+        const bool emitter = t > kTgMn;
+        const double g0 = a.sgn * (t2 * t2);
         for (int l = 0; l < a.NWL; ++l) {
-            a.akl[c + (long long)l * n] = emf(a.akl0[l], opl);
+            const double akl = emf(a.akl0[l], opl);
+            a.akl[c + (long long)l * n] = akl;
+            if (emitter) a.qel0[c + (long long)l * n] = deb[l] * akl * g0;
             sg = sg + deb[l] * emf(a.akl0[l], opl);
             ss = ss + deb[l] * emf(0.0, opl);
         }
@@ -322,7 +328,7 @@ struct RadAcc {   // per-thread sums of the deposits by destination
 
 template <int NW>
 __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* qalp, const double* qel1,
-                              double* qel, double* ang0, RadAcc& acc, int* err) {
+                              double* ang0, RadAcc& acc, int* err) {
     const int NWL = NW > 0 ? NW : a.NWL;
     const int n = a.MZ * a.NZ * a.LZ;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -335,7 +341,6 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
         if (tid == 0) {
             for (int l = 0; l < NWL; ++l) S.q1[l * D.A + e0] = qel1[l];
             S.f1[e0] = 0;
-            for (int l = 0; l < NWL; ++l) qel[l] = qel[l] + qel1[l];
             // SANG1 for an open cell
             const double b = fabs(D.cd[D.d0 + s] - D.cd[D.d0]);
             if (b < kSmall16) { ang0[0] = 90.0; ang0[1] = 90.0; }
@@ -446,106 +451,89 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
     }
 }
 
+// One march direction d of QREF for every emitter of the grid-stride: the
+// three directions are independent apart from the order of their QAL
+// additions, so they run as three launches at once, each with the shared
+// memory of its own slab.
 template <int NW>
-__global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a) {
+__global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
     extern __shared__ __align__(16) unsigned char rad_smem[];
-    __shared__ double s_deb[kRadMaxBands], s_qel0[kRadMaxBands], s_qel1[kRadMaxBands], s_qel[kRadMaxBands];
+    __shared__ double s_qel1[kRadMaxBands];
     __shared__ double s_ang0[2];
     __shared__ double s_red[kRadThreads];
     const int NWL = NW > 0 ? NW : a.NWL;
     const int n = a.MZ * a.NZ * a.LZ;
     const int tid = threadIdx.x;
+    Dir D;
+    D.d = d;
+    D.u = d == 0 ? 1 : 0;
+    D.v = d == 2 ? 1 : 2;
+    const int dims[3] = {a.MP, a.NP, a.LP};
+    D.Dd = dims[d]; D.Du = dims[D.u]; D.Dv = dims[D.v];
+    D.DA = D.Du / 2; D.DB = D.Dv / 2; D.A = D.DA * D.DB;
+    const int strides[3] = {1, a.MZ, a.MZ * a.NZ};
+    D.sd = strides[d]; D.su = strides[D.u]; D.sv = strides[D.v];
+    D.direct1 = 100 * (d + 1) + 1; D.direct2 = 100 * (d + 1) + 11;
     // shared layout: coordinates X(1..MP), R(1..NP), Z(1..LP); ANG1/2/3 (two
-    // columns each); then the slab arrays (here or in global scratch)
+    // columns each); angle candidates; the slab's IBCELL; then the slab arrays
+    // (here or in global scratch)
     double* sx = reinterpret_cast<double*>(rad_smem);
     double* sr = sx + (a.MP + 2);
     double* sz = sr + (a.NP + 2);
-    double* ang = sz + (a.LP + 2);
-    double* ang1 = ang;                          // ANG1(.,1), ANG1(.,2)
+    double* ang1 = sz + (a.LP + 2);              // ANG1(.,1), ANG1(.,2)
     double* ang2 = ang1 + 2 * (a.MP + 2);
     double* ang3 = ang2 + 2 * (a.NP + 2);
     double* tmp = ang3 + 2 * (a.LP + 2);         // angle candidates: (MP+2) + (NP+2) + (LP+2)
     int16_t* sib = reinterpret_cast<int16_t*>(tmp + (a.MP + 2) + (a.NP + 2) + (a.LP + 2));
-    double* arr = reinterpret_cast<double*>(sib + ((a.A + 7) / 8) * 8);
+    double* arr = reinterpret_cast<double*>(sib + ((D.A + 7) / 8) * 8);
+    {
+        const double* crd[3] = {sx, sr, sz};
+        double* angs[3] = {ang1, ang2, ang3};
+        const int angw[3] = {a.MP + 2, a.NP + 2, a.LP + 2};
+        double* tmps[3] = {tmp, tmp + (a.MP + 2), tmp + (a.MP + 2) + (a.NP + 2)};
+        D.cd = crd[d]; D.cu = crd[D.u]; D.cv = crd[D.v];
+        D.angU1 = angs[D.u]; D.angU2 = angs[D.u] + angw[D.u];
+        D.angV1 = angs[D.v]; D.angV2 = angs[D.v] + angw[D.v];
+        D.d0 = D.u0 = D.v0 = 0;
+        (void)tmps;
+    }
     Slab S;
     S.ib = sib;
-    if (a.slab_in_smem) {
-        S.q1 = arr;
-    } else {
-        S.q1 = a.scratch + (long long)blockIdx.x * 3 * a.A * NWL;
+    {
+        double* tmps[3] = {tmp, tmp + (a.MP + 2), tmp + (a.MP + 2) + (a.NP + 2)};
+        S.tU = tmps[D.u];
+        S.tV = tmps[D.v];
     }
-    S.q2 = S.q1 + (long long)a.A * NWL;
-    S.qm = S.q2 + (long long)a.A * NWL;
-    unsigned char* flags = a.slab_in_smem ? reinterpret_cast<unsigned char*>(S.qm + (long long)a.A * NWL)
-                                          : a.fscratch + (long long)blockIdx.x * 3 * a.A;
+    S.q1 = a.slab_in_smem[d] ? arr : a.scratch[d] + (long long)blockIdx.x * 3 * D.A * NWL;
+    S.q2 = S.q1 + (long long)D.A * NWL;
+    S.qm = S.q2 + (long long)D.A * NWL;
+    unsigned char* flags = a.slab_in_smem[d] ? reinterpret_cast<unsigned char*>(S.qm + (long long)D.A * NWL)
+                                             : a.fscratch[d] + (long long)blockIdx.x * 3 * D.A;
     S.f1 = flags;
-    S.f2 = flags + a.A;
-    S.fm = flags + 2 * a.A;
+    S.f2 = flags + D.A;
+    S.fm = flags + 2 * D.A;
     for (int i = 1 + tid; i <= a.MP; i += blockDim.x) sx[i] = a.g.X[i];
     for (int i = 1 + tid; i <= a.NP; i += blockDim.x) sr[i] = a.g.Rr[i];
     for (int i = 1 + tid; i <= a.LP; i += blockDim.x) sz[i] = a.g.Z[i];
-    double* qalp = a.qal_part + (long long)blockIdx.x * n * NWL;
+    const long long part = a.part_base[d] + blockIdx.x;
+    double* qalp = a.qal_part + part * n * NWL;
     for (long long i = tid; i < (long long)n * NWL; i += blockDim.x) qalp[i] = 0.0;
+    const double* dface[3] = {a.g.DX, a.g.DR, a.g.DZ};
     RadAcc acc{0.0, 0.0, 0.0, 0.0, 0.0};
-    double qe_sum = 0.0;
-    int n_emit = 0;
     __syncthreads();
 
     for (int c = blockIdx.x; c < n; c += gridDim.x) {
         // emitters in the reference's loop order: I outer, K inner
         const int KD2 = c % a.LZ + 1, JD2 = (c / a.LZ) % a.NZ + 1, ID2 = c / (a.LZ * a.NZ) + 1;
-        const int I0 = 2 * ID2, J0 = 2 * JD2, K0 = 2 * KD2;
         const int cc = (ID2 - 1) + a.MZ * ((JD2 - 1) + a.NZ * (KD2 - 1));
-        if (a.ibr[cc] >= 1) continue;
-        const double t = a.tcell[cc];
-        if (t <= kTgMn) continue;
-        if (tid == 0) {
-            rad_debx(a, t, s_deb);
-            const double t2 = t * t;
-            const double g0 = a.sgn * (t2 * t2);
-            for (int l = 0; l < NWL; ++l) {
-                s_qel0[l] = s_deb[l] * a.akl[cc + (long long)l * n] * g0;
-                s_qel[l] = 0.0;
-            }
-        }
+        if (a.ibr[cc] >= 1 || a.tcell[cc] <= kTgMn) continue;
+        const int pos[3] = {2 * ID2, 2 * JD2, 2 * KD2};
+        D.d0 = pos[d]; D.u0 = pos[D.u]; D.v0 = pos[D.v];
+        if (tid == 0)   // power through one face of the emitter (QEL1, Qre.f90:118/241/384)
+            for (int l = 0; l < NWL; ++l)
+                s_qel1[l] = a.qel0[cc + (long long)l * n] * dface[D.u][D.u0] * dface[D.v][D.v0];
         __syncthreads();
-        for (int d = 0; d < 3; ++d) {
-            Dir D;
-            D.d = d;
-            D.u = d == 0 ? 1 : 0;
-            D.v = d == 2 ? 1 : 2;
-            const int dims[3] = {a.MP, a.NP, a.LP};
-            const int pos[3] = {I0, J0, K0};
-            const int strides[3] = {1, a.MZ, a.MZ * a.NZ};
-            const double* crd[3] = {sx, sr, sz};
-            double* angs[3] = {ang1, ang2, ang3};
-            const int angw[3] = {a.MP + 2, a.NP + 2, a.LP + 2};
-            const double* dface[3] = {a.g.DX, a.g.DR, a.g.DZ};
-            D.Dd = dims[d]; D.Du = dims[D.u]; D.Dv = dims[D.v];
-            D.DA = D.Du / 2; D.DB = D.Dv / 2; D.A = D.DA * D.DB;
-            D.d0 = pos[d]; D.u0 = pos[D.u]; D.v0 = pos[D.v];
-            D.sd = strides[d]; D.su = strides[D.u]; D.sv = strides[D.v];
-            D.cd = crd[d]; D.cu = crd[D.u]; D.cv = crd[D.v];
-            D.angU1 = angs[D.u]; D.angU2 = angs[D.u] + angw[D.u];
-            D.angV1 = angs[D.v]; D.angV2 = angs[D.v] + angw[D.v];
-            D.direct1 = 100 * (d + 1) + 1; D.direct2 = 100 * (d + 1) + 11;
-            {
-                double* tmps[3] = {tmp, tmp + (a.MP + 2), tmp + (a.MP + 2) + (a.NP + 2)};
-                S.tU = tmps[D.u];
-                S.tV = tmps[D.v];
-            }
-            if (tid == 0)
-                for (int l = 0; l < NWL; ++l) s_qel1[l] = s_qel0[l] * dface[D.u][D.u0] * dface[D.v][D.v0];
-            __syncthreads();
-            rad_direction<NW>(a, D, S, qalp, s_qel1, s_qel, s_ang0, acc, a.err);
-        }
-        if (tid == 0) {
-            double qe = s_qel[0];
-            for (int l = 1; l < NWL; ++l) qe = qe + s_qel[l];
-            a.qe[cc] = qe;
-            qe_sum += qe;
-            ++n_emit;
-        }
+        rad_direction<NW>(a, D, S, qalp, s_qel1, s_ang0, acc, a.err);
         __syncthreads();
     }
     // block totals in a fixed order
@@ -557,17 +545,47 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a) {
             if (tid < st) s_red[tid] += s_red[tid + st];
             __syncthreads();
         }
-        if (tid == 0) a.tot_part[8 * blockIdx.x + k] = s_red[0];
+        if (tid == 0) a.tot_part[8 * part + k] = s_red[0];
         __syncthreads();
-    }
-    if (tid == 0) {
-        a.tot_part[8 * blockIdx.x + 5] = qe_sum;
-        a.tot_part[8 * blockIdx.x + 6] = (double)n_emit;
     }
 }
 
+// QE of every emitter (QREF's QEL accumulation, Qre.f90:121/244/387, and the
+// band sum, Qre.f90:503-507): the six faces' powers in the order x-, x+, y-,
+// y+, z-, z+; block totals of the emission and of the emitter count.
+__global__ void __launch_bounds__(256) k_rad_qe(RadArgs a) {
+    __shared__ double sh[2][256];
+    const int n = a.MZ * a.NZ * a.LZ;
+    double qs = 0.0, cnt = 0.0;
+    GFM_FOR(c, n) {
+        a.qe[c] = 0.0;
+        if (a.ibr[c] >= 1 || a.tcell[c] <= kTgMn) continue;
+        const int I = 2 * (c % a.MZ + 1), J = 2 * ((c / a.MZ) % a.NZ + 1), K = 2 * (c / (a.MZ * a.NZ) + 1);
+        double qe = 0.0;
+        for (int l = 0; l < a.NWL; ++l) {
+            const double q0 = a.qel0[c + (long long)l * n];
+            const double fx = q0 * a.g.DR[J] * a.g.DZ[K], fy = q0 * a.g.DX[I] * a.g.DZ[K], fz = q0 * a.g.DX[I] * a.g.DR[J];
+            double q = 0.0;
+            q = q + fx; q = q + fx; q = q + fy; q = q + fy; q = q + fz; q = q + fz;
+            qe = l == 0 ? q : qe + q;
+        }
+        a.qe[c] = qe;
+        qs += qe;
+        cnt += 1.0;
+    }
+    sh[0][threadIdx.x] = qs;
+    sh[1][threadIdx.x] = cnt;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) { sh[0][threadIdx.x] += sh[0][threadIdx.x + s]; sh[1][threadIdx.x] += sh[1][threadIdx.x + s]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { a.qe_part[2 * blockIdx.x] = sh[0][0]; a.qe_part[2 * blockIdx.x + 1] = sh[1][0]; }
+}
+
 // QAL = sum of the CTA copies in CTA order; QA = sum over bands (QRN1)
-__global__ void k_rad_reduce(RadArgs a, int nparts) {
+__global__ void k_rad_reduce(RadArgs a) {
+    const int nparts = a.part_base[3];
     const int n = a.MZ * a.NZ * a.LZ;
     GFM_FOR(c, n) {
         double g0 = 0.0;
@@ -580,55 +598,91 @@ __global__ void k_rad_reduce(RadArgs a, int nparts) {
     }
 }
 
-__global__ void k_rad_zero(double* p, int n) {
-    GFM_FOR(i, n) p[i] = 0.0;
-}
-
 template <typename R>
 __global__ void k_rad_t_roundtrip(R* T, long long n, double t0) {
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
         T[t] = R(((double)T[t] * t0) / t0);
 }
 
-size_t rad_smem_fixed(const RadArgs& a) {   // coordinates, ANG1/2/3, angle candidates, slab IBCELL
-    return sizeof(double) * (4 * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2))) + sizeof(int16_t) * (((size_t)a.A + 7) / 8 * 8);
+size_t rad_smem_fixed(const RadArgs& a, int A) {   // coordinates, ANG1/2/3, angle candidates, slab IBCELL
+    return sizeof(double) * (4 * ((size_t)(a.MP + 2) + (a.NP + 2) + (a.LP + 2))) + sizeof(int16_t) * (((size_t)A + 7) / 8 * 8);
 }
-size_t rad_smem_slab(const RadArgs& a) { return (size_t)3 * a.A * a.NWL * sizeof(double) + (size_t)3 * a.A; }
+size_t rad_smem_slab(const RadArgs& a, int A) { return (size_t)3 * A * a.NWL * sizeof(double) + (size_t)3 * A; }
+int rad_slab_cells(const RadArgs& a, int d) {
+    return d == 0 ? (a.NP / 2) * (a.LP / 2) : (d == 1 ? (a.MP / 2) * (a.LP / 2) : (a.MP / 2) * (a.NP / 2));
+}
+template <int NW>
+int rad_plan_nw(RadArgs& a, int sms) {
+    // dynamic shared memory available to one CTA: the device's opt-in
+    // maximum less the kernel's static shared memory
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa{};
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_rad_trace<NW>) != cudaSuccess)
+        return GFM_E_CUDA;
+    const size_t limit = (size_t)optin - fa.sharedSizeBytes;
+    if (cudaFuncSetAttribute(k_rad_trace<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit) != cudaSuccess)
+        return GFM_E_CUDA;
+    int base = 0;
+    for (int d = 0; d < 3; ++d) {
+        const int A = rad_slab_cells(a, d);
+        const size_t with = rad_smem_fixed(a, A) + rad_smem_slab(a, A);
+        a.slab_in_smem[d] = with <= limit;
+        a.smem[d] = a.slab_in_smem[d] ? with : rad_smem_fixed(a, A);
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rad_trace<NW>, kRadThreads, a.smem[d]) != cudaSuccess)
+            return GFM_E_CUDA;
+        occ = occ < 1 ? 1 : (occ > 4 ? 4 : occ);
+        a.grid[d] = sms * occ;
+        a.part_base[d] = base;
+        base += a.grid[d];
+    }
+    a.part_base[3] = base;
+    return GFM_OK;
+}
 
 template <int NW>
-int rad_trace_launch(const RadArgs& a, int grid, size_t smem, cudaStream_t st) {
-    if (cudaFuncSetAttribute(k_rad_trace<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return GFM_E_CUDA;
-    k_rad_trace<NW><<<grid, kRadThreads, smem, st>>>(a);
-    return GFM_OK;
+void rad_trace_launch(const RadArgs& a, cudaStream_t const* st) {
+    for (int d = 0; d < 3; ++d) k_rad_trace<NW><<<a.grid[d], kRadThreads, a.smem[d], st[d]>>>(a, d);
 }
 
 }  // namespace
 
-size_t rad_shared_bytes(const RadArgs& a, bool with_slab) {
-    return rad_smem_fixed(a) + (with_slab ? rad_smem_slab(a) : 0);
+int rad_plan(RadArgs& a, int sms) {
+    switch (a.NWL) {
+        case 4: return rad_plan_nw<4>(a, sms);
+        case 10: return rad_plan_nw<10>(a, sms);
+        default: return rad_plan_nw<0>(a, sms);
+    }
 }
 
+// st[0] is the caller's stream; the x-, y- and z-directions run on st[0..2],
+// forked after the per-cell kernels (ev[0]) and joined before the sums
+// (ev[1], ev[2]).
 template <typename R>
-int launch_rad_transfer(RadArgs a, R* T, long long nT, int grid, cudaStream_t st) {
+int launch_rad_transfer(RadArgs a, R* T, long long nT, cudaStream_t const* st, cudaEvent_t const* ev) {
     const int n = a.MZ * a.NZ * a.LZ;
     const int gb = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
-    k_rad_mark<<<gb, 256, 0, st>>>(a);
-    k_rad_akl<R><<<a.akl_blocks, 256, 0, st>>>(a, T);
-    k_rad_zero<<<gb, 256, 0, st>>>(a.qe, n);
-    const size_t smem = rad_shared_bytes(a, a.slab_in_smem != 0);
-    int rc;
+    k_rad_mark<<<gb, 256, 0, st[0]>>>(a);
+    k_rad_akl<R><<<a.akl_blocks, 256, 0, st[0]>>>(a, T);
+    k_rad_qe<<<a.akl_blocks, 256, 0, st[0]>>>(a);
+    if (cudaEventRecord(ev[0], st[0]) != cudaSuccess || cudaStreamWaitEvent(st[1], ev[0], 0) != cudaSuccess ||
+        cudaStreamWaitEvent(st[2], ev[0], 0) != cudaSuccess)
+        return GFM_E_CUDA;
     switch (a.NWL) {
-        case 4: rc = rad_trace_launch<4>(a, grid, smem, st); break;
-        case 10: rc = rad_trace_launch<10>(a, grid, smem, st); break;
-        default: rc = rad_trace_launch<0>(a, grid, smem, st); break;
+        case 4: rad_trace_launch<4>(a, st); break;
+        case 10: rad_trace_launch<10>(a, st); break;
+        default: rad_trace_launch<0>(a, st); break;
     }
-    if (rc != GFM_OK) return rc;
-    k_rad_reduce<<<gb, 256, 0, st>>>(a, grid);
-    k_rad_t_roundtrip<R><<<1024, 256, 0, st>>>(T, nT, a.t0);
-    return GFM_OK;
+    if (cudaEventRecord(ev[1], st[1]) != cudaSuccess || cudaEventRecord(ev[2], st[2]) != cudaSuccess ||
+        cudaStreamWaitEvent(st[0], ev[1], 0) != cudaSuccess || cudaStreamWaitEvent(st[0], ev[2], 0) != cudaSuccess)
+        return GFM_E_CUDA;
+    k_rad_reduce<<<gb, 256, 0, st[0]>>>(a);
+    k_rad_t_roundtrip<R><<<1024, 256, 0, st[0]>>>(T, nT, a.t0);
+    return cudaGetLastError() == cudaSuccess ? GFM_OK : GFM_E_CUDA;
 }
-template int launch_rad_transfer<double>(RadArgs, double*, long long, int, cudaStream_t);
-template int launch_rad_transfer<float>(RadArgs, float*, long long, int, cudaStream_t);
+template int launch_rad_transfer<double>(RadArgs, double*, long long, cudaStream_t const*, cudaEvent_t const*);
+template int launch_rad_transfer<float>(RadArgs, float*, long long, cudaStream_t const*, cudaEvent_t const*);
 
 }  // namespace gfm

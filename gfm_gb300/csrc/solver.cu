@@ -98,13 +98,10 @@ struct gfm_handle {
     void* lp_feats = nullptr;           // BF16 inputs, 16 channels per voxel
     int lp_nx = 0, lp_ny = 0, lp_nz = 0;
     // volume radiation transfer (allocated by the first gfm_gpu_rad_transfer)
-    GeoT<double> rad_g{};               // FP64 geometry of the transfer (coordinates uploaded in mixed mode)
-    int16_t* rad_ibr = nullptr;
-    double *rad_akl = nullptr, *rad_tcell = nullptr, *rad_qal = nullptr, *rad_qe = nullptr, *rad_qa = nullptr;
-    double *rad_tot = nullptr, *rad_akl_part = nullptr, *rad_scratch = nullptr;
-    unsigned char* rad_fscratch = nullptr;
-    int* rad_err = nullptr;
-    int rad_grid = 0, rad_akl_blocks = 0, rad_in_smem = 0;
+    RadArgs rad{};                      // buffers and launch plan of the transfer (once per handle)
+    bool rad_ready = false;
+    cudaStream_t rad_stream[2]{};       // the y- and z-direction traces run beside the x-direction
+    cudaEvent_t rad_ev[3]{};
     int rb_flags = kRbPdl | kRbAvgInPass;   // red-black options (environment at create): GFM_RB_FUSED=1 adds
                                             // kRbFused; GFM_PDL=0 drops kRbPdl; GFM_RB_AVG_IN_PASS=0 drops kRbAvgInPass
 };
@@ -1126,50 +1123,48 @@ extern "C" int gfm_gpu_download(gfm_handle* h, gfm_fields* f) {
 }
 
 namespace {
-constexpr size_t kRadSmemLimit = 227 * 1024;
-// device buffers of the volume transfer, once per handle: one trace CTA per SM
-int rad_alloc(gfm_handle* h, RadArgs& a) {
+// buffers, streams and the launch plan of the volume transfer, once per handle
+int rad_prepare(gfm_handle* h, const RadArgs& in) {
+    if (h->rad_ready) return GFM_OK;
+    RadArgs a = in;
     const long long nc = (long long)a.MZ * a.NZ * a.LZ;
-    if (!h->rad_ibr) {
-        // the transfer works in FP64: in mixed mode the handle's FP64 geometry
-        // holds only IBCELL, so the coordinates are uploaded for it here
-        h->rad_g = h->gd;
-        if (!h->rad_g.X) {
-            const HostGrid& hg = h->hg;
-            double *x, *dx, *r, *dr, *rs, *z, *dz;
-            int rc;
-            if ((rc = dupload(h, &x, hg.X)) || (rc = dupload(h, &dx, hg.DX)) || (rc = dupload(h, &r, hg.R)) ||
-                (rc = dupload(h, &dr, hg.DR)) || (rc = dupload(h, &rs, hg.RS)) || (rc = dupload(h, &z, hg.Z)) ||
-                (rc = dupload(h, &dz, hg.DZ)))
-                return rc;
-            h->rad_g.X = x; h->rad_g.DX = dx; h->rad_g.Rr = r; h->rad_g.DR = dr; h->rad_g.RS = rs;
-            h->rad_g.Z = z; h->rad_g.DZ = dz;
-        }
-        int dev = 0, sms = 0;
-        CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        h->rad_grid = sms > 0 ? sms : 1;
-        h->rad_akl_blocks = (int)std::min<long long>((nc + 255) / 256, 1024);
-        h->rad_in_smem = rad_shared_bytes(a, true) <= kRadSmemLimit;
+    // the transfer works in FP64: in mixed mode the handle's FP64 geometry
+    // holds only IBCELL, so the coordinates are uploaded for it here
+    if (!a.g.X) {
+        const HostGrid& hg = h->hg;
+        double *x, *dx, *r, *dr, *rs, *z, *dz;
         int rc;
-        if ((rc = dalloc(h, &h->rad_ibr, nc)) || (rc = dalloc(h, &h->rad_akl, nc * a.NWL)) ||
-            (rc = dalloc(h, &h->rad_tcell, nc)) || (rc = dalloc(h, &h->rad_qal, nc * a.NWL * h->rad_grid)) ||
-            (rc = dalloc(h, &h->rad_qe, nc)) || (rc = dalloc(h, &h->rad_qa, nc)) ||
-            (rc = dalloc(h, &h->rad_tot, 8LL * h->rad_grid)) || (rc = dalloc(h, &h->rad_akl_part, 2LL * h->rad_akl_blocks)) ||
-            (rc = dalloc(h, &h->rad_err, 1)))
+        if ((rc = dupload(h, &x, hg.X)) || (rc = dupload(h, &dx, hg.DX)) || (rc = dupload(h, &r, hg.R)) ||
+            (rc = dupload(h, &dr, hg.DR)) || (rc = dupload(h, &rs, hg.RS)) || (rc = dupload(h, &z, hg.Z)) ||
+            (rc = dupload(h, &dz, hg.DZ)))
             return rc;
-        if (!h->rad_in_smem) {
-            if ((rc = dalloc(h, &h->rad_scratch, 3LL * a.A * a.NWL * h->rad_grid)) ||
-                (rc = dalloc(h, &h->rad_fscratch, 3LL * a.A * h->rad_grid)))
-                return rc;
-        }
+        a.g.X = x; a.g.DX = dx; a.g.Rr = r; a.g.DR = dr; a.g.RS = rs; a.g.Z = z; a.g.DZ = dz;
     }
-    a.g = h->rad_g;
-    a.ibr = h->rad_ibr; a.akl = h->rad_akl; a.tcell = h->rad_tcell; a.qal_part = h->rad_qal;
-    a.qe = h->rad_qe; a.qa = h->rad_qa; a.tot_part = h->rad_tot; a.akl_part = h->rad_akl_part;
-    a.scratch = h->rad_scratch; a.fscratch = h->rad_fscratch; a.err = h->rad_err;
-    a.slab_in_smem = h->rad_in_smem;
-    a.akl_blocks = h->rad_akl_blocks;
+    int dev = 0, sms = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int rc = rad_plan(a, sms > 0 ? sms : 1);
+    if (rc) { h->err = "radiation transfer: launch plan"; return rc; }
+    a.akl_blocks = (int)std::min<long long>((nc + 255) / 256, 1024);
+    const long long parts = a.part_base[3];
+    if ((rc = dalloc(h, &a.ibr, nc)) || (rc = dalloc(h, &a.akl, nc * a.NWL)) || (rc = dalloc(h, &a.qel0, nc * a.NWL)) ||
+        (rc = dalloc(h, &a.tcell, nc)) || (rc = dalloc(h, &a.qal_part, nc * a.NWL * parts)) ||
+        (rc = dalloc(h, &a.qe, nc)) || (rc = dalloc(h, &a.qa, nc)) || (rc = dalloc(h, &a.tot_part, 8 * parts)) ||
+        (rc = dalloc(h, &a.akl_part, 2LL * a.akl_blocks)) || (rc = dalloc(h, &a.qe_part, 2LL * a.akl_blocks)) ||
+        (rc = dalloc(h, &a.err, 1)))
+        return rc;
+    for (int d = 0; d < 3; ++d) {
+        a.scratch[d] = nullptr;
+        a.fscratch[d] = nullptr;
+        if (a.slab_in_smem[d]) continue;
+        const long long A = d == 0 ? (a.NP / 2) * (a.LP / 2) : (d == 1 ? (a.MP / 2) * (a.LP / 2) : (a.MP / 2) * (a.NP / 2));
+        if ((rc = dalloc(h, &a.scratch[d], 3 * A * a.NWL * a.grid[d])) || (rc = dalloc(h, &a.fscratch[d], 3 * A * a.grid[d])))
+            return rc;
+    }
+    for (int s = 0; s < 2; ++s) CK(cudaStreamCreateWithFlags(&h->rad_stream[s], cudaStreamNonBlocking));
+    for (int e = 0; e < 3; ++e) CK(cudaEventCreateWithFlags(&h->rad_ev[e], cudaEventDisableTiming));
+    h->rad = a;
+    h->rad_ready = true;
     return GFM_OK;
 }
 }  // namespace
@@ -1178,37 +1173,43 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
     if (!h) return GFM_E_ARG;
     const Ctx<double>& cdb = h->cd;
     if (cdb.nwl < 1 || cdb.nwl > kRadMaxBands) { h->err = "radiation transfer: 1 to 16 bands"; return GFM_E_UNSUPPORTED; }
-    RadArgs a{};
-    a.g = h->gd;
-    a.MP = h->gd.MP; a.NP = h->gd.NP; a.LP = h->gd.LP;
-    a.MZ = a.MP / 2; a.NZ = a.NP / 2; a.LZ = a.LP / 2;
-    a.NWL = cdb.nwl;
-    a.A = std::max(a.NZ * a.LZ, std::max(a.MZ * a.LZ, a.MZ * a.NZ));
-    a.t0 = h->params.t0;
-    a.sgn = h->params.sig * h->params.ri * h->params.ri;                          // SGN (Rad0.f90:33)
-    for (int l = 0; l < a.NWL; ++l) {
-        a.akl0[l] = cdb.akl0[l];
-        a.deb0[l] = h->params.hck / h->params.ri / cdb.wl[l];                      // DEB0 (Rad0.f90:34)
+    if (!h->rad_ready) {
+        RadArgs a{};
+        a.g = h->gd;
+        a.MP = h->gd.MP; a.NP = h->gd.NP; a.LP = h->gd.LP;
+        a.MZ = a.MP / 2; a.NZ = a.NP / 2; a.LZ = a.LP / 2;
+        a.NWL = cdb.nwl;
+        a.t0 = h->params.t0;
+        a.sgn = h->params.sig * h->params.ri * h->params.ri;                      // SGN (Rad0.f90:33)
+        for (int l = 0; l < a.NWL; ++l) {
+            a.akl0[l] = cdb.akl0[l];
+            a.deb0[l] = h->params.hck / h->params.ri / cdb.wl[l];                  // DEB0 (Rad0.f90:34)
+        }
+        int rc = rad_prepare(h, a);
+        if (rc) return rc;
     }
-    int rc = rad_alloc(h, a);
-    if (rc) return rc;
+    const RadArgs& a = h->rad;
     cudaStream_t st = h->stream;
-    CK(cudaMemsetAsync(h->rad_err, 0, sizeof(int), st));
+    const cudaStream_t streams[3] = {st, h->rad_stream[0], h->rad_stream[1]};
+    CK(cudaMemsetAsync(a.err, 0, sizeof(int), st));
     const long long nT = 8 * h->gd.CB;
+    int rc;
     if (h->prec == GFM_PREC_FP64) {
-        if ((rc = launch_rad_transfer<double>(a, h->cd.T, nT, h->rad_grid, st))) { h->err = "radiation transfer launch"; return rc; }
+        if ((rc = launch_rad_transfer<double>(a, h->cd.T, nT, streams, h->rad_ev))) { h->err = "radiation transfer launch"; return rc; }
         launch_cells_to_split(h->gd, a.qe, h->cd.QE, st);
         launch_cells_to_split(h->gd, a.qa, h->cd.QA, st);
     } else {
-        if ((rc = launch_rad_transfer<float>(a, h->cf.T, nT, h->rad_grid, st))) { h->err = "radiation transfer launch"; return rc; }
+        if ((rc = launch_rad_transfer<float>(a, h->cf.T, nT, streams, h->rad_ev))) { h->err = "radiation transfer launch"; return rc; }
         launch_cells_to_split(h->gfl, a.qe, h->cf.QE, st);
         launch_cells_to_split(h->gfl, a.qa, h->cf.QA, st);
     }
-    std::vector<double> tot(8 * (size_t)h->rad_grid), akp(2 * (size_t)h->rad_akl_blocks);
+    const int parts = a.part_base[3];
+    std::vector<double> tot(8 * (size_t)parts), akp(2 * (size_t)a.akl_blocks), qep(2 * (size_t)a.akl_blocks);
     int err = 0;
-    CK(cudaMemcpyAsync(tot.data(), h->rad_tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(akp.data(), h->rad_akl_part, akp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&err, h->rad_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(tot.data(), a.tot_part, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(akp.data(), a.akl_part, akp.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(qep.data(), a.qe_part, qep.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&err, a.err, sizeof(int), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (err) {
         h->err = "radiation transfer: a wall-corner split inside the box (geometry outside the supported set)";
@@ -1217,19 +1218,21 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
     h->rad_active = 1;
     if (out) {
         std::memset(out, 0, sizeof *out);
-        for (int b = 0; b < h->rad_grid; ++b) {   // block order
+        for (int b = 0; b < parts; ++b) {   // x-, y-, z-direction CTAs, each in CTA order
             out->qa_sum_to_melt += tot[8 * b + 0];
             out->qa_sum_to_exit += tot[8 * b + 1];
             out->qa_sum_to_inlet += tot[8 * b + 2];
             out->qa_sum_to_wall += tot[8 * b + 3];
             out->qa_sum_to_open += tot[8 * b + 4];
-            out->qe_sum_from_open += tot[8 * b + 5];
-            out->n_emitters += (int)tot[8 * b + 6];
         }
-        for (int b = 0; b < h->rad_akl_blocks; ++b) {
+        double ne = 0.0;
+        for (int b = 0; b < a.akl_blocks; ++b) {
             out->tot_qe_h2o_co2 += akp[2 * b];
             out->tot_qe_soot += akp[2 * b + 1];
+            out->qe_sum_from_open += qep[2 * b];
+            ne += qep[2 * b + 1];
         }
+        out->n_emitters = (int)ne;
     }
     return GFM_OK;
 }
@@ -1378,6 +1381,8 @@ extern "C" void gfm_gpu_destroy(gfm_handle* h) {
     if (h->ev_adi0) cudaEventDestroy(h->ev_adi0);
     if (h->ev_adi1) cudaEventDestroy(h->ev_adi1);
     for (int i = 0; i <= kXferSlots; ++i) if (h->ev_xfer[i]) cudaEventDestroy(h->ev_xfer[i]);
+    for (int e = 0; e < 3; ++e) if (h->rad_ev[e]) cudaEventDestroy(h->rad_ev[e]);
+    for (int q = 0; q < 2; ++q) if (h->rad_stream[q]) { cudaStreamSynchronize(h->rad_stream[q]); cudaStreamDestroy(h->rad_stream[q]); }
     for (int s = 0; s < kXferStreams; ++s)
         if (h->copy_stream[s]) { cudaStreamSynchronize(h->copy_stream[s]); cudaStreamDestroy(h->copy_stream[s]); }
     if (h->stream) cudaStreamDestroy(h->stream);

@@ -112,23 +112,30 @@ constexpr int kRadMaxBands = 16;
 struct RadArgs {
     GeoT<double> g;              // coordinates (1-based), parity-split IBCELL, pidx
     int MP, NP, LP, MZ, NZ, LZ, NWL;
-    int A;                       // cells of the largest slab of the three directions
-    int slab_in_smem;            // slab arrays in shared memory (else in scratch/fscratch)
-    int akl_blocks;              // blocks of k_rad_akl (akl_part holds 2 per block)
+    int akl_blocks;              // blocks of k_rad_akl and k_rad_qe (2 totals per block each)
+    // per march direction (x, y, z): slab arrays in shared memory (else in
+    // scratch/fscratch), dynamic shared memory, CTAs, first QAL copy
+    int slab_in_smem[3];
+    size_t smem[3];
+    int grid[3];
+    int part_base[4];            // part_base[3]: QAL copies in all
     double t0, sgn;              // T0; SIG*RI*RI
     double akl0[kRadMaxBands];   // band absorption coefficients (1/m)
     double deb0[kRadMaxBands];   // HCK/RI/WL
     int16_t* ibr;                // IBCELL with the wall markers, per cell (MZ,NZ,LZ)
     double *akl, *tcell;         // AKL (cell + l*ncell), T*T0 per cell
+    double* qel0;                // QEL0 of the emitters (cell + l*ncell)
     double *qal_part;            // one QAL copy per trace block
     double *qe, *qa;             // QE, QA per cell (MZ,NZ,LZ)
-    double *tot_part, *akl_part; // block totals (8 per trace block, 2 per akl block)
-    double* scratch;             // slab arrays when they do not fit in shared memory
-    unsigned char* fscratch;
+    double *tot_part, *akl_part, *qe_part;   // block totals (8 per trace CTA, 2 per akl / qe block)
+    double* scratch[3];          // slab arrays when they do not fit in shared memory
+    unsigned char* fscratch[3];
     int* err;                    // bit 0: geometry outside the supported set
 };
-size_t rad_shared_bytes(const RadArgs& a, bool with_slab);
-template <typename R> int launch_rad_transfer(RadArgs a, R* T, long long nT, int grid, cudaStream_t s);
+// fills slab_in_smem, smem, grid and part_base from the grid, the band count
+// and the SM count
+int rad_plan(RadArgs& a, int sms);
+template <typename R> int launch_rad_transfer(RadArgs a, R* T, long long nT, cudaStream_t const* st, cudaEvent_t const* ev);
 
 // ---- launchers (defined in the kernel translation units) --------------------
 template <typename R> void launch_wallfn(const Ctx<R>& c, const int* wall_list, int n_wall, cudaStream_t s);
