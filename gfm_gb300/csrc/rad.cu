@@ -4,17 +4,21 @@
 //   k_rad_mark    wall markers: IBCELL 1 -> 101..311 where a neighbour is open
 //                 (Rad_emis.f90:144-178), on a cell map of its own
 //   k_rad_akl     RAD0 with ID_RAD=10 (Rad0.f90:112-166): AKL = EMF(AKL0, OPL)
-//                 of the hot open cells, band-emission totals
-//   k_rad_trace   the QRNF emitter loop (Qrn.f90:58-154) with QREF
-//                 (Qre.f90:31-515) and QRTX/QRTY/QRTZ (Qrtx.f90:15-209,
-//                 Qrty.f90:9-224, Qrtz.f90:15-234)
-//   k_rad_reduce  QAL summed over the blocks, QA = sum over bands (QRN1,
+//                 of the hot open cells, band-emission totals, and QREF's
+//                 per-area band emission QEL0 of every emitter
+//   k_rad_qe      QE of every emitter (QREF's six face powers and band sum)
+//   k_rad_trace   the QRNF emitter loop (Qrn.f90:58-154) with the x-, y- or
+//                 z-flux of QREF (Qre.f90:31-515) and QRTX/QRTY/QRTZ
+//                 (Qrtx.f90:15-209, Qrty.f90:9-224, Qrtz.f90:15-234): one
+//                 launch per direction, the three on three streams at once
+//   k_rad_reduce  QAL summed over the CTAs, QA = sum over bands (QRN1,
 //                 Qrn.f90:250-259)
 //
-// One CTA traces one emitter at a time (cells in the reference's loop order,
-// a grid-stride over the emitters); emitters are independent, so the CTAs of
-// the grid trace different emitters at once.  Within an emitter the reference
-// is sequential; the CTA keeps its order where it matters:
+// A CTA of direction d traces that direction for one emitter at a time (cells
+// in the reference's loop order, a grid-stride over the emitters); emitters
+// and directions are independent, so many are in flight at once, each
+// direction's CTAs sized by its own slab.  Within one emitter and direction
+// the reference is sequential; the CTA keeps its order where it matters:
 //   * the slab arrays QTX1, QTX2, Q2M and their flags live in shared memory
 //     (global scratch when they do not fit);
 //   * the far-face angles of a slab (SANG2), the reference's outward scan
@@ -32,9 +36,9 @@
 //     emitter's own column) is reported as unsupported;
 //   * absorption into the slab's cells is per cell.
 // QAL is accumulated per CTA in its own copy (fixed emitter order) and the
-// copies are summed in CTA order, so the result is deterministic; it differs
-// from the reference's single running sum only by the association of the
-// additions.
+// copies are summed in a fixed order (x-direction CTAs, then y, then z), so
+// the result is deterministic; it differs from the reference's single running
+// sum only by the association of the additions.
 //
 // Angles come from rad_atand, the same operations as the oracle's ATAND; this
 // translation unit is compiled with --fmad=false so that no multiply-add is
