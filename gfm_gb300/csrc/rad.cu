@@ -49,6 +49,13 @@ namespace gfm {
 namespace {
 
 constexpr double kSmall16 = 1.0e-16;
+
+// A double's IEEE bit pattern as a signed 64-bit integer.  Two non-negative
+// doubles, or any double and a positive one, compare the same way as these
+// integers (no NaN occurs here), so the frequent comparisons of angles and of
+// powers against SMALL16 run on the integer pipe, GB300's FP64 pipe being
+// narrow; the results are those of the floating-point comparisons.
+__device__ __forceinline__ long long rb(double x) { return __double_as_longlong(x); }
 constexpr double kTgMn = 300.0;     // TG_MN (Rad0.f90:42)
 constexpr int kRadThreads = 128;
 
@@ -191,7 +198,7 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
         double A11 = 0.0, A12 = 0.0;
         const int uend = UPM < 0 ? 2 : D.Du;
         for (int u1 = D.u0; UPM > 0 ? u1 <= uend - UPM : u1 >= uend - UPM; u1 += UPM) {
-            if (A11 >= ang0u) break;
+            if (rb(A11) >= rb(ang0u)) break;
             const int u12 = u1 + UPM / 2;
             A12 = D.angU1[u12];
             const double DANG = A12 - A11;
@@ -211,11 +218,11 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
                 const int e2 = (bb - 1) * D.DA + (u2 / 2 - 1);
                 if (S.ib[e2] < 1) {
                     const double A22 = D.angU2[u2 + UPM / 2];
-                    if (A22 <= A21) continue;
-                    if (A22 < A12) {
+                    if (rb(A22) <= rb(A21)) continue;
+                    if (rb(A22) < rb(A12)) {
                         const double FIJ = (A22 - A21) / DANG;
                         for (int l = 0; l < NWL; ++l) {
-                            if (Q11[l] < kSmall16) continue;
+                            if (rb(Q11[l]) < rb(kSmall16)) continue;
                             const double Q21 = Q11[l] * FIJ;
                             S.qm[l * D.A + e2] = S.qm[l * D.A + e2] + Q21;
                             Q12[l] = Q12[l] - Q21;
@@ -244,7 +251,7 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
         double A11 = 0.0, A12 = 0.0;
         const int vend = KM < 0 ? 2 : D.Dv;
         for (int v1 = D.v0; KM > 0 ? v1 <= vend - KM : v1 >= vend - KM; v1 += KM) {
-            if (A11 >= ang0v) break;
+            if (rb(A11) >= rb(ang0v)) break;
             const int v12 = v1 + KM / 2;
             A12 = D.angV1[v12];
             const double DANG = A12 - A11;
@@ -279,7 +286,7 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
                         const int et = (v2 / 2 - 1) * D.DA + (ut / 2 - 1);
                         const int e2m = (v2 / 2 - KM / 2 - 1) * D.DA + (aa - 1);
                         for (int l = 0; l < NWL; ++l) {
-                            if (Q12[l] < kSmall16) continue;
+                            if (rb(Q12[l]) < rb(kSmall16)) continue;
                             const double Q21 = Q12[l] * 0.5;
                             S.q2[l * D.A + et] = S.q2[l * D.A + et] + Q21;
                             S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
@@ -293,10 +300,10 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
                     } else {
                         const double A22 = D.angV2[v2m];
                         if ((A22 - A21) <= 1.0e-10) continue;
-                        if (A22 < A12) {
+                        if (rb(A22) < rb(A12)) {
                             const double FIJ = (A22 - A21) / DANG;
                             for (int l = 0; l < NWL; ++l) {
-                                if (Q11[l] < kSmall16) continue;
+                                if (rb(Q11[l]) < rb(kSmall16)) continue;
                                 const double Q21 = Q11[l] * FIJ;
                                 S.q2[l * D.A + e2] = S.q2[l * D.A + e2] + Q21;
                                 Q12[l] = Q12[l] - Q21;
@@ -318,12 +325,16 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
 
 // Is row v1 (part 1) / column u1 (part 2) visited?  The reference skips the
 // rows before the emitter whose near angle is outside the cone and stops at
-// the first such row after it.
-__device__ __forceinline__ bool rad_visit(const double* ang2, int p, int p0, double ang0) {
-    if (p < p0) return !(ang2[p + 1] >= ang0);
-    for (int q = p0 + 2; q <= p; q += 2)
-        if (ang2[q - 1] >= ang0) return false;
-    return true;
+// the first row after it whose near angle is; `exit` is that row (or beyond
+// the range), found once per slab.
+__device__ __forceinline__ bool rad_visit(const double* ang2, int p, int p0, double ang0, int exit) {
+    if (p < p0) return rb(ang2[p + 1]) < rb(ang0);
+    return p < exit;
+}
+__device__ int rad_exit(const double* ang2, int p0, int last, double ang0) {
+    for (int q = p0 + 2; q <= last; q += 2)
+        if (rb(ang2[q - 1]) >= rb(ang0)) return q;
+    return last + 2;
 }
 
 struct RadAcc {   // per-thread sums of the deposits by destination
@@ -341,6 +352,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
     for (int i = tid; i < D.A; i += nth) { S.f1[i] = 1; S.f2[i] = 1; S.fm[i] = 1; }
     __syncthreads();
     const int e0 = (D.v0 / 2 - 1) * D.DA + (D.u0 / 2 - 1);
+    __shared__ int exits[2];
     for (int s = -1; s <= 1; s += 2) {
         if (tid == 0) {
             for (int l = 0; l < NWL; ++l) S.q1[l * D.A + e0] = qel1[l];
@@ -391,10 +403,12 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                     const int pend = M < 0 ? 2 : P;
                     for (int pp = p0 + M; M > 0 ? pp <= pend : pp >= pend; pp += 2 * M) {
                         const double aa = cand[pp];
-                        if (aa >= lim) break;
+                        if (rb(aa) >= rb(lim)) break;
                         out[pp] = aa;
                     }
                 }
+                // the first part-2 column (u) / part-1 row (v) after the emitter that ends its loop
+                exits[isu ? 0 : 1] = isu ? rad_exit(out, p0, P, lim) : rad_exit(out, p0, P - 2, lim);
             }
             __syncthreads();
             // part 1: one thread per row
@@ -402,22 +416,22 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 const int nrows = (D.Dv - 4) / 2;   // rows 4 .. Dv-2
                 for (int r = tid; r < nrows; r += nth) {
                     const int v1 = 4 + 2 * r;
-                    if (rad_visit(D.angV2, v1, D.v0, ang0v)) part1_row<NW>(a, D, S, slab, v1, ang0u);
+                    if (rad_visit(D.angV2, v1, D.v0, ang0v, exits[1])) part1_row<NW>(a, D, S, slab, v1, ang0u);
                 }
             }
             __syncthreads();
             // part 2: first column, interior columns, last column
-            if (tid == 0 && rad_visit(D.angU2, 2, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, 2, ang0v, err);
+            if (tid == 0 && rad_visit(D.angU2, 2, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, 2, ang0v, err);
             __syncthreads();
             {
                 const int ncols = (D.Du - 4) / 2;   // columns 4 .. Du-2
                 for (int r = tid; r < ncols; r += nth) {
                     const int u1 = 4 + 2 * r;
-                    if (rad_visit(D.angU2, u1, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, u1, ang0v, err);
+                    if (rad_visit(D.angU2, u1, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, u1, ang0v, err);
                 }
             }
             __syncthreads();
-            if (tid == 0 && rad_visit(D.angU2, D.Du, D.u0, ang0u)) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err);
+            if (tid == 0 && rad_visit(D.angU2, D.Du, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err);
             __syncthreads();
             // absorption in the slab's cells
             const bool end = slab == dend;
@@ -428,7 +442,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 const int ib = S.ib[e];
                 for (int l = 0; l < NWL; ++l) {
                     const double q = S.q2[l * D.A + e];
-                    if (q < kSmall16) continue;
+                    if (rb(q) < rb(kSmall16)) continue;
                     double* qa = qalp + c + (long long)l * n;
                     if (ib >= 1 || end) {
                         *qa = *qa + q;
