@@ -107,3 +107,21 @@ def test_mixed_precision_transfer_runs_and_conserves_energy():
     assert np.isfinite(st["res_mass"])
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("kappa,wl_um", [
+    (tuple(float(k) for k in np.geomspace(0.05, 5.0, 10)), (1.0, 1.5, 2.0, 3.0, 4.0, 6.0, 8.0, 12.0, 20.0, 1000.0)),
+    ((0.3, 1.5), (4.0, 1000.0)),
+])
+def test_transfer_matches_oracle_for_other_band_sets(kappa, wl_um):
+    """10 bands (the count of the 384x160x96 configuration, kappa log-uniform
+    on 0.05-5 1/m) and 2 bands take the kernel's other instantiations."""
+    cfg = configs.tiny_furnace(nx=16, ny=10, nz=8, kappa=kappa, wl_um=wl_um)
+    case, o = _state(cfg, 8)
+    g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    g.upload(o.download())
+    tg = g.rad_transfer()
+    to = o.rad_transfer()
+    _compare(g.download(), o.download(), tg, to)
+    g.close()
+    o.close()

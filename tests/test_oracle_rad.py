@@ -66,3 +66,19 @@ def test_only_hot_open_cells_emit_and_absorption_stays_in_the_box(traced):
     assert np.all(qe[ib >= 1] == 0)
     assert np.all(qa >= 0) and np.all(qe >= 0)
     assert tot["n_emitters"] == int(np.count_nonzero(qe > 0))
+
+
+@pytest.mark.parametrize("nb", [1, 2, 10])
+def test_transfer_conserves_energy_for_other_band_counts(nb):
+    kappa = tuple(float(k) for k in np.geomspace(0.05, 5.0, nb)) if nb > 1 else (0.7,)
+    wl = tuple(float(w) for w in np.geomspace(1.5, 40.0, nb - 1)) + (1000.0,) if nb > 1 else (1000.0,)
+    case = Case(configs.tiny_furnace(kappa=kappa, wl_um=wl))
+    o = Oracle(case)
+    o.initsv()
+    o.gflow(10)
+    t = o.rad_transfer()
+    absorbed = sum(t[k] for k in ("qa_sum_to_open", "qa_sum_to_wall", "qa_sum_to_inlet", "qa_sum_to_exit",
+                                  "qa_sum_to_melt"))
+    assert t["qe_sum_from_open"] > 0
+    assert abs(t["qe_sum_from_open"] - absorbed) <= 1e-12 * t["qe_sum_from_open"]
+    o.close()
