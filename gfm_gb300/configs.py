@@ -119,6 +119,13 @@ def small_furnace(**kw) -> FurnaceCase:
     return FurnaceCase(name="furnace_48x24x16", nx=48, ny=24, nz=16, inlets=_burner_inlets(), **kw)
 
 
+def medium_furnace(**kw) -> FurnaceCase:
+    """96 x 48 x 32 cells (147,456): the same furnace at half the resolution,
+    for kernel captures on a state larger than L2 but a few hundred MB."""
+    kw.setdefault("inlet_jitter", 0.05)
+    return FurnaceCase(name="furnace_96x48x32", nx=96, ny=48, nz=32, inlets=_burner_inlets(), **kw)
+
+
 def large_furnace(**kw) -> FurnaceCase:
     """192 x 96 x 64 cells (1,179,648), inlet velocities jittered +-5%."""
     kw.setdefault("inlet_jitter", 0.05)

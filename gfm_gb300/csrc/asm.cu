@@ -131,7 +131,7 @@ __device__ R flwd(const Ctx<R>& c, int I, int J, int K, int ix, int m, R sgm) {
 template <typename R>
 __global__ void k_wallfn(Ctx<R> c, const int* __restrict__ wl, int n) {
     const GeoT<R>& g = c.g;
-    const R rt20 = R(c.p.reyg2 * sqrt(c.p.epsr) * pow(c.p.cmu, 0.25));
+    const R rt20 = R(c.p.rt20);
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
         int I = wl[3 * t], J = wl[3 * t + 1], K = wl[3 * t + 2];
         // neighbour n = w + s*e_d writes w with distance d(n,w); order of last writer
@@ -166,8 +166,8 @@ __global__ void k_wallfn(Ctx<R> c, const int* __restrict__ wl, int n) {
                 A(c.THETA, I, J, K) = A(c.THETA, In, Jn, Kn) * x01 + A(c.THETA, Ifar, Jfar, Kfar) * x02;
                 theta_done = true;
             }
-            R cc = pow(A(c.T, In, Jn, Kn) / R(c.p.trdg), R(c.p.amu));
-            R blvm = rt20 * A(c.DNST, In, Jn, Kn) * sqrt(A(c.GF[kK], In, Jn, Kn)) / cc;
+            R cc = r_pow(A(c.T, In, Jn, Kn) / R(c.p.trdg), R(c.p.amu));
+            R blvm = rt20 * A(c.DNST, In, Jn, Kn) * r_sqrt(A(c.GF[kK], In, Jn, Kn)) / cc;
             R vgam = cc / R(c.p.reyg2);
             R blv = blvm * dist;
             R gama0 = vgam * tgamf<R>(blv);
@@ -687,8 +687,8 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
             bs = R(2) / R(c.p.reyg * c.p.epsr) * c.THETA[o] * c.TMU[o] * c.GTE[o] - zero;
             sfp = -(R(c.p.taur) * c.THETA[o] * c.DNST[o] * c.GF[kEps][o] / (c.GF[kK][o] + R(kSmall20)));
         } else if (NELG == 10) {
-            const R cbl0 = R(2.5 * sqrt(c.p.epsr) / c.p.taur * pow(c.p.cmu, 0.75));
-            R cbl = cbl0 * pow(c.GF[kK][o], R(1.5));
+            const R cbl0 = R(c.p.cbl0);
+            R cbl = cbl0 * r_pow(c.GF[kK][o], R(1.5));
             const R BIGV = R(1.0e20);
             bool pen = false;
             if (g.MP > 8 && IBC(g, I + 1, J, K) == 1) { bs = bs + BIGV * cbl / (g.X[I + 1] - g.X[I]); pen = true; }
@@ -805,7 +805,7 @@ __device__ void ther(Ctx<R>& c, long long o) {
     R k = c.GF[kK][o];
     R g0 = R(c.p.cmu) * R(c.p.reyg) * R(c.p.epsr) / R(2.0 * c.p.taur) * (k * k) / eps * c.DNST[o];
     c.TMU[o] = g0;
-    c.GAMA[o] = R(2) / R(c.p.reyg) * (g0 + pow(c.T[o] / R(c.p.trdg), R(c.p.amu)));
+    c.GAMA[o] = R(2) / R(c.p.reyg) * (g0 + r_pow(c.T[o] / R(c.p.trdg), R(c.p.amu)));
 }
 
 template <typename R>

@@ -91,6 +91,10 @@ struct Prm {
     double rf_hsource, h_g;
     double sig, ri, hck;
     int react, wall_sink;
+    // constants of the run that the reference recomputes in its cell loops,
+    // evaluated once on the host:
+    double rt20;   // REYG2*SQRT(EPSR)*CMU**0.25 (Gflow.f90:74, wall functions)
+    double cbl0;   // 2.5*SQRT(EPSR)/TAUR*CMU**0.75 (Source.f90:579, epsilon wall penalty)
 };
 
 // Deterministic FP64 reductions: every block writes one partial per slot into

@@ -205,6 +205,18 @@ GFM_HD R enth_to_t(const NistT<R>& N, const R* y, long s, R h_norm, R T, R t0, R
     return T_new * R(1000) / t0;
 }
 
+// Elementary functions in the arithmetic of the path: the float versions in
+// the mixed path (no promotion to FP64, whose pipe is narrow on GB300), the
+// double versions exactly as in the FP64 path.
+GFM_HD float r_exp(float x) { return expf(x); }
+GFM_HD double r_exp(double x) { return exp(x); }
+GFM_HD float r_log(float x) { return logf(x); }
+GFM_HD double r_log(double x) { return log(x); }
+GFM_HD float r_pow(float a, float b) { return powf(a, b); }
+GFM_HD double r_pow(double a, double b) { return pow(a, b); }
+GFM_HD float r_sqrt(float x) { return sqrtf(x); }
+GFM_HD double r_sqrt(double x) { return sqrt(x); }
+
 // Exponential-scheme weight DA(D,F) (Prop.f90:97-117).
 template <typename R>
 GFM_HD R da(R d, R f) {
@@ -215,7 +227,7 @@ GFM_HD R da(R d, R f) {
         const R sixth = R(1.0) / R(6.0);
         return d / (R(1) + pe * (R(0.5) + pe * (sixth + pe / R(24.0))));
     } else if (pe <= R(2.0e+1)) {
-        return fa / (exp(pe) - R(1));
+        return fa / (r_exp(pe) - R(1));
     }
     return R(0);
 }
@@ -224,7 +236,7 @@ GFM_HD R da(R d, R f) {
 template <typename R>
 GFM_HD R tgamf(R b) {
     if (b < R(11.5)) return R(1);
-    R g0 = b / (log(R(9) * b) * R(2.5));
+    R g0 = b / (r_log(R(9) * b) * R(2.5));
     return g0 > R(1) ? g0 : R(1);
 }
 

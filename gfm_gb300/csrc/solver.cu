@@ -922,6 +922,8 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     for (int i = 0; i < 12; ++i) p.sigma[i] = prm->sigma[i];
     p.rf_hsource = prm->rf_hsource; p.h_g = prm->h_g;
     p.sig = prm->sig; p.ri = prm->ri; p.hck = prm->hck;
+    p.rt20 = p.reyg2 * std::sqrt(p.epsr) * std::pow(p.cmu, 0.25);
+    p.cbl0 = 2.5 * std::sqrt(p.epsr) / p.taur * std::pow(p.cmu, 0.75);
     p.react = prm->react; p.wall_sink = prm->wall_sink;
     c.nwl = gr->nwl;
     for (int l = 0; l < gr->nwl; ++l) { c.wl[l] = gr->wl[l]; c.akl0[l] = gr->akl0[l]; }
