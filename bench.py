@@ -272,7 +272,7 @@ def run_ours(args):
     if world > 1:
         import torch
         torch.cuda.set_device(local)
-    case = Case(configs.large_furnace() if args.case == "large" else configs.medium_furnace())
+    case = Case({"large": configs.large_furnace, "medium": configs.medium_furnace, "xl": configs.xl_furnace}[args.case]())
     solver = GpuSolver(case, adi_mode=adi, precision=prec)
     solver.start()
     solver.gflow(max(args.warmup, 0))
@@ -397,8 +397,10 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * dev_s / nd, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "fp32" if args.prec == "mixed" else "fp64", "data": "synthetic",
-            "config": {"workload": WORKLOAD if args.case == "large" else f"{case.cfg.name}: GFLOW steady SIMPLER outer "
-                                   "iteration (kernel-capture case, not the benchmark workload)",
+            "config": {"workload": WORKLOAD if args.case == "large" else (
+                           f"{case.cfg.name}: GFLOW steady SIMPLER outer iteration, {ncells:,} cells, "
+                           + ("10 gray bands; the combustion space of the large coupled configuration, no melt coupling"
+                              if args.case == "xl" else "kernel-capture case, not the benchmark workload")),
                        "cells": ncells, "precision": args.prec, "adi_order": args.adi,
                        "l2": "inputs larger than L2 (device state ~%.1f GB)" % (state_bytes * (0.5 if w == 4 else 1) * 3 / 1e9),
                        "parallelism": f"replicas x{world}", "res_mass_last": st["res_mass"]},
@@ -544,8 +546,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-rad", action="store_true", help="skip the volume radiation transfer leg")
-    ap.add_argument("--case", choices=["large", "medium"], default="large",
-                    help="medium: the same furnace at 96x48x32, for kernel captures (not the benchmark workload)")
+    ap.add_argument("--case", choices=["large", "medium", "xl"], default="large",
+                    help="medium: the same furnace at 96x48x32, for kernel captures; xl: 384x160x96 with 10 bands "
+                         "(neither is the benchmark workload)")
     ap.add_argument("--ttr", type=float, default=None,
                     help="also measure the time from the fresh start to res_mass < TTR (mixed and FP64)")
     ap.add_argument("--ttr-max", type=int, default=3000)

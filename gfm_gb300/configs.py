@@ -9,6 +9,7 @@ the openings' positions are this project's choice.
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 from .abi import GFM_ADI_MARCH, GFM_PREC_FP64, GfmCaseSpec, GfmInletSpec
@@ -130,6 +131,21 @@ def large_furnace(**kw) -> FurnaceCase:
     """192 x 96 x 64 cells (1,179,648), inlet velocities jittered +-5%."""
     kw.setdefault("inlet_jitter", 0.05)
     return FurnaceCase(name="furnace_192x96x64", nx=192, ny=96, nz=64, inlets=_burner_inlets(), **kw)
+
+
+def xl_furnace(seed: int = 5, **kw) -> FurnaceCase:
+    """384 x 160 x 96 cells (5,898,240) with 10 gray bands whose absorption
+    coefficients are drawn log-uniform on 0.05-5 1/m from `seed` (band edges
+    geometric from 1.2 to 40 um, the last band open to 1000 um): the
+    combustion space of the large coupled configuration, without its melt
+    coupling."""
+    import random
+    rnd = random.Random(seed)
+    kappa = tuple(math.exp(rnd.uniform(math.log(0.05), math.log(5.0))) for _ in range(10))
+    wl = tuple(1.2 * (40.0 / 1.2) ** (i / 8.0) for i in range(9)) + (1000.0,)
+    kw.setdefault("inlet_jitter", 0.05)
+    return FurnaceCase(name="furnace_384x160x96", nx=384, ny=160, nz=96, inlets=_burner_inlets(), kappa=kappa,
+                       wl_um=wl, **kw)
 
 
 def furnace_variant(seed: int, nx: int = 48, ny: int = 24, nz: int = 16, aspect: float | None = None,
