@@ -86,7 +86,8 @@ class ClockSampler:
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_bench_{gpu}.csv"
+        # the raw samples; GFM_BENCH_OUT names the folder (default bench_out/)
+        self.path = pathlib.Path(os.environ.get("GFM_BENCH_OUT", str(ROOT / "bench_out"))) / f"clocks_bench_{gpu}.csv"
 
     def __enter__(self):
         try:

@@ -1578,7 +1578,7 @@ struct Oracle {
 };
 
 // ---------------------------------------------------------------------------
-// Volume radiation transfer (SURVEY row a14), restated from
+// Volume radiation transfer, restated from
 //   RAD_EMIS   Rad_emis.f90:144-189  wall markers with open neighbours, T*T0
 //   RAD0       Rad0.f90:112-166      AKL = EMF(AKL0, OPL) (ID_RAD=10), totals
 //   QRNF       Qrn.f90:58-229        emitter loop (emission/absorption part)
