@@ -194,8 +194,14 @@ __global__ void k_copy_faces(Ctx<R> c) {
 // Momentum: SRC1 (Source.f90:664-809) + GSLVX1/GSLV3X1/ECELL/VOL1
 // (Gslv3x.f90:9-200) on the face class of direction IU1.
 // ---------------------------------------------------------------------------
+// 4 blocks of 256 per SM: the 64-register cap the compiler applies without
+// launch bounds (it assumes 1024-thread blocks; free, it takes 101).  5 and 6
+// (48 and 40 registers, small spills) measured within 0.2 % of it.
+#ifndef GFM_MOM_MINB
+#define GFM_MOM_MINB 4
+#endif
 template <typename R, int IU1>
-__global__ void k_mom_assemble(Ctx<R> c, Range rg) {
+__global__ void __launch_bounds__(kBlock, GFM_MOM_MINB) k_mom_assemble(Ctx<R> c, Range rg) {
     const GeoT<R>& g = c.g;
     const R zero = R(0);
     long long n = rg.count();
