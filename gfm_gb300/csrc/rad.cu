@@ -646,7 +646,7 @@ int rad_plan_nw(RadArgs& a, int sms) {
     for (int d = 0; d < 3; ++d) {
         const int A = rad_slab_cells(a, d);
         const size_t with = rad_smem_fixed(a, A) + rad_smem_slab(a, A);
-        a.slab_in_smem[d] = with <= limit;
+        a.slab_in_smem[d] = with <= limit && !a.slab_global;
         a.smem[d] = a.slab_in_smem[d] ? with : rad_smem_fixed(a, A);
         int occ = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rad_trace<NW>, kRadThreads, a.smem[d]) != cudaSuccess)

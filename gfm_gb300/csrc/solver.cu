@@ -1145,6 +1145,12 @@ int rad_prepare(gfm_handle* h, const RadArgs& in) {
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    {
+        // GFM_RAD_GLOBAL_SLAB=1 (read at the first transfer): the slab arrays
+        // in global scratch even where they fit in shared memory
+        const char* gs = std::getenv("GFM_RAD_GLOBAL_SLAB");
+        a.slab_global = gs && gs[0] == '1';
+    }
     int rc = rad_plan(a, sms > 0 ? sms : 1);
     if (rc) { h->err = "radiation transfer: launch plan"; return rc; }
     a.akl_blocks = (int)std::min<long long>((nc + 255) / 256, 1024);

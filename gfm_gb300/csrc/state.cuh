@@ -116,6 +116,7 @@ struct RadArgs {
     // per march direction (x, y, z): slab arrays in shared memory (else in
     // scratch/fscratch), dynamic shared memory, CTAs, first QAL copy
     int slab_in_smem[3];
+    int slab_global;             // put the slab arrays in global scratch even where they fit (tests)
     size_t smem[3];
     int grid[3];
     int part_base[4];            // part_base[3]: QAL copies in all

@@ -125,3 +125,18 @@ def test_transfer_matches_oracle_for_other_band_sets(kappa, wl_um):
     _compare(g.download(), o.download(), tg, to)
     g.close()
     o.close()
+
+
+def test_transfer_with_the_slab_arrays_in_global_memory(monkeypatch):
+    """Grids whose slab arrays exceed shared memory (at 192x96x64 the z-slab
+    needs 442 KB) keep them in global scratch; forced here on a small grid,
+    the same results as the oracle."""
+    monkeypatch.setenv("GFM_RAD_GLOBAL_SLAB", "1")
+    case, o = _state(configs.tiny_furnace(nx=16, ny=10, nz=8), 12)
+    g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    g.upload(o.download())
+    tg = g.rad_transfer()
+    to = o.rad_transfer()
+    _compare(g.download(), o.download(), tg, to)
+    g.close()
+    o.close()
