@@ -24,6 +24,7 @@ GFM_E_NOMEM = -5
 GFM_E_TIMEOUT = -6
 GFM_E_NODEVICE = -7
 GFM_E_LIMIT = -8
+GFM_E_IO = -9
 
 GFM_ADI_MARCH = 0
 GFM_ADI_REDBLACK = 1
@@ -157,14 +158,51 @@ class GfmCaseSpec(C.Structure):
     ]
 
 
+class GfmRestartTail(C.Structure):
+    _fields_ = [
+        ("mz", C.c_int), ("nz", C.c_int), ("t_surf_prev", _dp),
+        ("i1st_rad_done", C.c_int), ("itr_rad", C.c_int), ("itr_gend", C.c_int), ("interval_rad", C.c_int),
+    ]
+
+
 class GfmCase(C.Structure):
-    _fields_ = [("grid", GfmGrid), ("params", GfmParams), ("fields", GfmFields), ("priv", C.c_void_p)]
+    _fields_ = [("grid", GfmGrid), ("params", GfmParams), ("fields", GfmFields), ("priv", C.c_void_p),
+                ("tail", GfmRestartTail)]
+
+
+class GfmCaseFiles(C.Structure):
+    _fields_ = [("gd", C.c_char_p), ("sbc", C.c_char_p), ("relax", C.c_char_p), ("it", C.c_char_p),
+                ("rg", C.c_char_p), ("kinetic", C.c_char_p)]
+
+
+class GfmCaseOptions(C.Structure):
+    _fields_ = [
+        ("sigma_eps", C.c_double), ("wall_sink", C.c_int), ("t_wall_k", C.c_double), ("rad_emission", C.c_int),
+        ("kappa", C.c_double * 16), ("maxgi", C.c_int), ("adi_mode", C.c_int), ("precision", C.c_int),
+    ]
+
+
+class GfmCaseSummary(C.Structure):
+    _fields_ = [
+        ("ncells", C.c_int), ("area_melt_surf", C.c_double),
+        ("fr_f", C.c_double), ("fr_ox", C.c_double), ("fr_n2", C.c_double),
+        ("heat_in_fuel", C.c_double), ("q_h_in", C.c_double), ("gmfr", C.c_double), ("gfin0", C.c_double),
+        ("irstyp", C.c_int), ("id_rad", C.c_int), ("interval_rad", C.c_int),
+        ("n_inlet_blocks", C.c_int), ("n_exhausts", C.c_int), ("n_wall_blocks", C.c_int), ("n_melt_cells", C.c_int),
+        ("restarted", C.c_int), ("itr_gas", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 # (name, restype, argtypes) of every entry point declared in include/gfm_gb300.h
 SIGNATURES = [
     ("gfm_case_build", C.c_int, [C.POINTER(GfmCaseSpec), C.c_char_p, C.POINTER(GfmCase)]),
     ("gfm_case_free", None, [C.POINTER(GfmCase)]),
+    ("gfm_case_read", C.c_int, [C.POINTER(GfmCaseFiles), C.POINTER(GfmCaseOptions), C.POINTER(GfmCase),
+                                C.POINTER(GfmCaseSummary)]),
+    ("gfm_restart_write", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmFields), C.POINTER(GfmRestartTail)]),
     ("gfm_gpu_device_count", C.c_int, []),
     ("gfm_gpu_create", C.c_int, [C.POINTER(GfmGrid), C.POINTER(GfmParams), C.POINTER(C.c_void_p)]),
     ("gfm_gpu_upload", C.c_int, [C.c_void_p, C.POINTER(GfmFields)]),

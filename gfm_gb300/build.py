@@ -22,7 +22,7 @@ CUDA_SOURCES = ["asm.cu", "adi.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu",
 # per-file flags: the radiation transfer rounds every product and sum as the
 # reference does (angle ties and energy splits must break the same way)
 FILE_FLAGS = {"rad.cu": ["--fmad=false"]}
-CXX_SOURCES = ["case_build.cpp"]
+CXX_SOURCES = ["case_build.cpp", "case_files.cpp"]
 
 
 def nvcc() -> str:

@@ -70,19 +70,80 @@ class Fields:
 
 
 class Case:
-    """A built synthetic furnace (host arrays owned by the native library)."""
+    """A built case (host arrays owned by the native library): a synthetic
+    furnace (``Case(cfg)``) or a GFM case directory (``Case.from_files``)."""
 
-    def __init__(self, cfg: FurnaceCase, lib: C.CDLL | None = None):
+    def __init__(self, cfg: FurnaceCase | None, lib: C.CDLL | None = None):
         self.cfg = cfg
         self.lib = lib or abi.load_library()
-        self.spec = cfg.to_spec()
         self.c = abi.GfmCase()
+        self.summary = None
+        if cfg is None:
+            return
+        self.name = cfg.name
+        self.spec = cfg.to_spec()
         rc = self.lib.gfm_case_build(C.byref(self.spec), str(abi.KINETIC_PATH).encode(), C.byref(self.c))
         if rc != abi.GFM_OK:
             raise GfmError(rc, "gfm_case_build failed")
+        self._dims()
+
+    def _dims(self) -> None:
         g = self.c.grid
         self.mp, self.np, self.lp = g.mp, g.np, g.lp
         self.ncells = g.ncells
+
+    @classmethod
+    def from_files(cls, case_dir, runum: str, relax=None, kinetic=None, restart: bool = False,
+                   sigma_eps: float = 1.0, wall_sink: bool = False, t_wall_k: float = 1700.0,
+                   rad_emission: bool = False, kappa=None, maxgi: int = 0,
+                   adi_mode: int = abi.GFM_ADI_MARCH, precision: int = abi.GFM_PREC_FP64,
+                   lib: C.CDLL | None = None) -> "Case":
+        """The start-up the Fortran host does from a case directory: reads
+        gd<runum>c.dat, sbc<runum>c.dat, it<runum>t.dat (when present),
+        relaxfactorc.txt (``relax``, default: in the case directory) and the
+        kinetics table, and with ``restart`` the restart file rg<runum>c.d
+        (A0main.f90:158-190).  ``summary`` holds what GRID3/SBC derived."""
+        import pathlib
+        d = pathlib.Path(case_dir)
+        it = d / f"it{runum}t.dat"
+        paths = {
+            "gd": d / f"gd{runum}c.dat", "sbc": d / f"sbc{runum}c.dat",
+            "relax": pathlib.Path(relax) if relax else d / "relaxfactorc.txt",
+            "it": it if it.exists() else None,
+            "rg": d / f"rg{runum}c.d" if restart else None,
+            "kinetic": pathlib.Path(kinetic) if kinetic else abi.KINETIC_PATH,
+        }
+        self = cls(None, lib)
+        self.name = f"case{runum}"
+        self._paths = {k: (str(v).encode() if v is not None else None) for k, v in paths.items()}
+        files = abi.GfmCaseFiles(**self._paths)
+        opt = abi.GfmCaseOptions()
+        opt.sigma_eps, opt.wall_sink, opt.t_wall_k, opt.rad_emission = sigma_eps, int(wall_sink), t_wall_k, int(rad_emission)
+        for l, k in enumerate(kappa or []):
+            opt.kappa[l] = k
+        opt.maxgi, opt.adi_mode, opt.precision = maxgi, adi_mode, precision
+        summ = abi.GfmCaseSummary()
+        rc = self.lib.gfm_case_read(C.byref(files), C.byref(opt), C.byref(self.c), C.byref(summ))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, f"gfm_case_read failed for {d} ({runum})")
+        self.summary = summ.as_dict()
+        self._dims()
+        return self
+
+    def t_surf_prev(self) -> np.ndarray:
+        """T_surf_prev(MZ,NZ) (K) as an (NZ, MZ) C-order array."""
+        t = self.c.tail
+        return np.ctypeslib.as_array(t.t_surf_prev, shape=(t.mz * t.nz,)).reshape(t.nz, t.mz).copy()
+
+    def write_restart(self, path, fields: "Fields | None" = None) -> None:
+        """Writes rg####c.d (SAV3F layout, Sav3f.f90:21-88) of ``fields``
+        (default: the case's own start-up fields) with this case's restart
+        tail."""
+        fld = fields if fields is not None else self.initial_fields()
+        f = fld.to_c()
+        rc = self.lib.gfm_restart_write(str(path).encode(), C.byref(self.c.grid), C.byref(f), C.byref(self.c.tail))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, f"gfm_restart_write failed for {path}")
 
     @property
     def grid(self) -> abi.GfmGrid:

@@ -42,6 +42,7 @@ extern "C" {
 #define GFM_E_TIMEOUT     (-6)   /* bounded device wait ran out             */
 #define GFM_E_NODEVICE    (-7)   /* no CUDA device / extension not usable   */
 #define GFM_E_LIMIT       (-8)   /* input beyond a fixed size limit         */
+#define GFM_E_IO          (-9)   /* input file missing, short or malformed  */
 
 /* ADI line-solver ordering (gfm_params.adi_mode) */
 #define GFM_ADI_MARCH      0     /* reference order: x-plane Gauss-Seidel march,
@@ -163,12 +164,26 @@ typedef struct gfm_case_spec {
     int    adi_mode, precision;
 } gfm_case_spec;
 
-/* A built case: host-owned arrays allocated by gfm_case_build. */
+/* The records of the restart file rg####c.d that follow the per-cell fields
+ * and are not part of gfm_fields (Sav3f.f90:75-82, Initsv.f90:290-303). */
+typedef struct gfm_restart_tail {
+    int     mz, nz;              /* extents of T_surf_prev: MP/2, NP/2          */
+    double *t_surf_prev;         /* T_surf_prev(MZ,NZ): melt-surface T (K) the
+                                    next melt_surf_T relaxes against           */
+    int     i1st_rad_done;       /* a full radiation call has run               */
+    int     itr_rad, itr_gend;   /* radiation call count, end of the current
+                                    gas-iteration interval                     */
+    int     interval_rad;        /* gas iterations between radiation calls      */
+} gfm_restart_tail;
+
+/* A built case: host-owned arrays allocated by gfm_case_build or
+ * gfm_case_read. */
 typedef struct gfm_case {
     gfm_grid   grid;
     gfm_params params;
     gfm_fields fields;
     void      *priv;             /* owns the storage behind the pointers       */
+    gfm_restart_tail tail;       /* restart records beyond the fields           */
 } gfm_case;
 
 /* Opaque GPU solver handle. */
@@ -184,6 +199,69 @@ typedef struct gfm_lp gfm_lp;
 int  gfm_case_build(const gfm_case_spec *spec, const char *kinetic_path,
                     gfm_case *out);
 void gfm_case_free(gfm_case *c);
+
+/* ---- host side: a case from the reference's own input files -------------- */
+/* Paths of the files a GFM case directory holds. */
+typedef struct gfm_case_files {
+    const char *gd;       /* gd####c.dat: grid and cell map (Grid3.f90:31-280)   */
+    const char *sbc;      /* sbc####c.dat: &INPUT, inlet blocks, exhausts, wall
+                             properties, &RADIN, band edges (Setup.f90:227-335,
+                             Sbc.f90:57-355)                                     */
+    const char *relax;    /* relaxfactorc.txt (Setup.f90:443-509)                */
+    const char *it;       /* it####t.dat melt-surface temperatures
+                             (Initsv.f90:394-547); needed when the cell map has
+                             melt-surface cells (IBCELL=4), else may be NULL     */
+    const char *rg;       /* rg####c.d restart (Initsv.f90:225-316); NULL: fresh
+                             start by gen_initial_guess (Initsv.f90:97-162)      */
+    const char *kinetic;  /* Kinetic.d (Setup.f90:858-888)                       */
+} gfm_case_files;
+
+/* Choices the input files do not carry. */
+typedef struct gfm_case_options {
+    double sigma_eps;     /* turbulent Prandtl number of epsilon, sigma(5); the
+                             reference's value is 1.0 (Var_mod.f90:211-212)      */
+    int    wall_sink;     /* fixed-temperature wall sink every iteration
+                             (Source.f90:473-509); the reference starts it only
+                             after its first full radiation call: 0            */
+    double t_wall_k;      /* wall-patch temperature of that sink (K)             */
+    int    rad_emission;  /* emission-only radiation source (rad_qe_only)        */
+    double kappa[16];     /* gray absorption coefficient per band (1/m), in the
+                             place of the band model of RAD_GAS                  */
+    int    maxgi;         /* > 0: replaces &INPUT MAXGI                           */
+    int    adi_mode, precision;
+} gfm_case_options;
+
+/* What GRID3 and SBC derived, as the reference prints it at the head of
+ * summary####c.txt (Utility.f90:99-105), plus the run controls read. */
+typedef struct gfm_case_summary {
+    int    ncells;              /* open cells                                  */
+    double area_melt_surf;      /* m2 (Grid3.f90:288-293)                      */
+    double fr_f, fr_ox, fr_n2;  /* inlet fuel, O2, N2 mass flows (kg/s)        */
+    double heat_in_fuel;        /* FR_F*Q0 (W)                                 */
+    double q_h_in;              /* sum of inlet mdot*h (W)                     */
+    double gmfr, gfin0;         /* &INPUT GMFR (kg/s); inflow / GMFR           */
+    int    irstyp, id_rad, interval_rad;
+    int    n_inlet_blocks, n_exhausts, n_wall_blocks, n_melt_cells;
+    int    restarted;           /* the fields come from files->rg              */
+    int    itr_gas;             /* restored iteration count (0 on a fresh start) */
+} gfm_case_summary;
+
+/* GRID3 + SETUP + SBC + INITSV (fresh start or restart) from the case files:
+ * the start-up a Fortran host does before the first GFLOW
+ * (A0main.f90:158-190).  Parse errors return GFM_E_IO; cell maps with
+ * half-blocked cells (IBCELL<0, Grid3.f90:236) and two-phase cases return
+ * GFM_E_UNSUPPORTED.  summary may be NULL. */
+int  gfm_case_read(const gfm_case_files *files, const gfm_case_options *opt,
+                   gfm_case *out, gfm_case_summary *summary);
+
+/* Writes the restart file rg####c.d of the state (grid, fields, tail) in
+ * the record layout of SAV3F (Sav3f.f90:21-88): sequential unformatted,
+ * 4-byte little-endian record-length markers, one (P, U(i+1), V(j+1),
+ * W(k+1), T, THETA) record and one GF(1:7) record per cell centre in I, J, K
+ * loop order, then bs_hprev, T_surf_prev, FACTOR/FADJ, i1st_rad_qe_done,
+ * i1st_rad_done, itr_gas, itr_rad/itr_gend and interval_rad. */
+int  gfm_restart_write(const char *path, const gfm_grid *grid,
+                       const gfm_fields *f, const gfm_restart_tail *tail);
 
 /* ---- GPU solver ---------------------------------------------------------- */
 /* Query: number of CUDA devices usable (>=1) or a negative status. */

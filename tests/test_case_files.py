@@ -1,0 +1,279 @@
+"""The reference's own case files through gfm_case_read and the restart file
+through gfm_restart_write, on the TC21 case 0041 fixtures (a 40 tpd glass
+furnace: 40x48x36 doubled grid, ports, a side flue and a melt surface).
+
+Pins against the reference's run of this case (tests/golden/case0041, made by
+tests/golden/make_case0041.py from the reference package):
+
+  - summary0041c.txt: open cells, melt area, inlet mass flows, fuel heat and
+    inlet enthalpy flow, printed with 14 digits: agreement to 1e-13;
+  - Tave0041c.plt at iteration 7540: the mass-weighted mean gas temperature
+    of the restart file's fields, 1e-12;
+  - convg/gresid/Tave logs of the fresh start: the oracle's first iterations
+    on the same inputs follow the reference's history; the tolerances below
+    are the measured agreement with headroom (the logged run is not exactly
+    reproducible, see the docstring of that test).
+"""
+import json
+import lzma
+import pathlib
+import shutil
+import struct
+
+import numpy as np
+import pytest
+
+from gfm_gb300 import Case, GfmError, abi
+
+from .test_case_build import propagate_ref
+
+GOLD = pathlib.Path(__file__).parent / "golden" / "case0041"
+REF = json.loads((GOLD / "case0041_reference.json").read_text())
+INPUTS = ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt")
+
+
+@pytest.fixture(scope="module")
+def case_dir(tmp_path_factory):
+    d = tmp_path_factory.mktemp("case0041")
+    for n in INPUTS:
+        shutil.copyfile(GOLD / n, d / n)
+    (d / "rg0041c.d").write_bytes(lzma.decompress((GOLD / "rg0041c.d.xz").read_bytes()))
+    return d
+
+
+@pytest.fixture(scope="module")
+def fresh(case_dir):
+    return Case.from_files(case_dir, "0041")
+
+
+@pytest.fixture(scope="module")
+def restarted(case_dir):
+    return Case.from_files(case_dir, "0041", restart=True)
+
+
+def arr(ptr, n):
+    return np.ctypeslib.as_array(ptr, shape=(n,)).copy()
+
+
+def records(path) -> list:
+    """Sequential unformatted records: 4-byte little-endian length markers."""
+    b = pathlib.Path(path).read_bytes()
+    out, p = [], 0
+    while p < len(b):
+        (n,) = struct.unpack_from("<i", b, p)
+        out.append(b[p + 4:p + 4 + n])
+        (m,) = struct.unpack_from("<i", b, p + 4 + n)
+        assert m == n
+        p += 8 + n
+    return out
+
+
+def test_rg_fixture_is_the_reference_file():
+    import hashlib
+    raw = lzma.decompress((GOLD / "rg0041c.d.xz").read_bytes())
+    assert len(raw) == REF["rg_bytes"] and hashlib.sha256(raw).hexdigest() == REF["rg_sha256"]
+
+
+def test_summary_matches_the_reference_run(fresh):
+    s = fresh.summary
+    assert s["ncells"] == REF["ncells"] == fresh.ncells == 4407
+    assert s["area_melt_surf"] == pytest.approx(REF["area_melt_surf"], rel=1e-13)
+    for k in ("fr_f", "fr_ox", "fr_n2", "heat_in_fuel", "q_h_in"):
+        assert s[k] == pytest.approx(REF[k], rel=1e-13), k
+    assert s["fr_f"] + s["fr_ox"] + s["fr_n2"] == pytest.approx(REF["fr_total"], rel=1e-13)
+    assert s["gmfr"] == 0.9242821 and s["gfin0"] == pytest.approx(REF["fr_total"] / 0.9242821, rel=1e-13)
+    assert (s["irstyp"], s["id_rad"], s["interval_rad"]) == (1, 1, 100)
+    assert (s["n_inlet_blocks"], s["n_exhausts"], s["n_wall_blocks"], s["n_melt_cells"]) == (3, 1, 0, 300)
+    assert s["restarted"] == 0 and s["itr_gas"] == 0
+
+
+def test_grid_lines(fresh):
+    g = fresh.grid
+    x, dx = arr(g.x, 40), arr(g.dx, 40)
+    r, z = arr(g.r, 48), arr(g.z, 36)
+    # listed points of gd0041c.dat and the linear fill between them by
+    # repeated addition (Grid3.f90:79-109), so interior points carry its rounding
+    close = lambda a, b: a == pytest.approx(b, abs=1e-14)
+    assert (x[0], x[2]) == (-0.31, -0.31) and x[39] == x[38] and close(x[38], 7.31)
+    assert close(x[6], 0.0) and close(x[36], 7.0) and close(x[7], 7.0 / 30)
+    assert dx[0] == 0 and dx[1] == 0 and dx[39] == 0 and close(dx[37], 0.31)
+    assert r[2] == -0.31 and r[47] == r[46] and close(r[46], 3.31)
+    assert close(r[4], 0.0) and close(r[6], 0.375) and close(r[18], 1.1)
+    assert (z[0], z[2]) == (0.0, 0.0) and z[35] == z[34] and close(z[34], 1.81) and close(z[6], 0.358)
+    assert fresh.params.gmfr == 0.9242821 and fresh.params.q0 * fresh.params.h_0 == pytest.approx(5e7, rel=1e-15)
+
+
+def gd_cell_map(path) -> dict:
+    """The cell-centre map of a gd file, read by rows (Grid3.f90:233-249)."""
+    lines = pathlib.Path(path).read_text().splitlines()
+    p = lines.index(next(l for l in lines if l.startswith("Computational")))
+    mp, np_, lp = 40, 48, 36
+    cells, k1, p = {}, 0, p + 1
+    while k1 < lp:
+        k2 = int(lines[p]); p += 1
+        i1 = 0
+        while i1 < mp:
+            l = lines[p]; p += 1
+            i2 = int(l[:4])
+            digits = l[6:6 + np_ // 2]
+            for k in range(k1 + 2, k2 + 1, 2):
+                for i in range(i1 + 2, i2 + 1, 2):
+                    for jj, ch in enumerate(digits):
+                        cells[(i, 2 * jj + 2, k)] = int(ch)
+            i1 = i2
+        k1 = k2
+    return cells
+
+
+def test_cell_map_and_propagation(fresh):
+    cells = gd_cell_map(GOLD / "gd0041c.dat")
+    ref, ncells = propagate_ref(cells, 40, 48, 36)
+    assert ncells == 4407
+    assert np.array_equal(fresh.ibcell(), ref)
+    ib = fresh.ibcell()
+    # the flue at I=2 (x=-0.31), J=8..18, K=16..26, and the melt surface at K=2
+    assert (ib[15:26:2, 7:18:2, 1] == 3).all()
+    assert (ib[1, 5:44:2, 7:36:2] == 4).all()
+
+
+def test_inlet_cells_carry_the_sbc_states(fresh):
+    f = fresh.initial_fields()
+    p = fresh.params
+    # fuel jet 1: I=6, J=26..30, K=8..12, 373.15 K, U=78.40 m/s, W=11.02 m/s (sbc0041c.dat)
+    for (i, j, k) in ((6, 26, 8), (6, 30, 12)):
+        a = (k - 1, j - 1, i - 1)
+        assert f.arrays["t"][a] == 373.15 / p.t0
+        assert f.arrays["ug"][0][a] == 78.4012815121033 / p.ug0
+        assert f.arrays["ug"][2][a] == 11.0185818229249 / p.ug0
+        assert f.arrays["gf"][0][a] == 1.0
+    # the pressure reference cell is an inlet (Sbc.f90:57-63)
+    g = fresh.grid
+    assert fresh.ibcell()[g.k_ref - 1, g.j_ref - 1, g.i_ref - 1] == 2 and (g.i_ref, g.j_ref, g.k_ref) == (6, 28, 10)
+
+
+def test_melt_surface_temperature_keeps_the_mean(fresh):
+    """melt_surf_T relaxes it0041t.dat against T_surf_prev (= the mean on a
+    fresh start) and rescales to the file's mean surface temperature."""
+    f = fresh.initial_fields()
+    ib = fresh.ibcell()
+    dx, dr = arr(fresh.grid.dx, 40), arr(fresh.grid.dr, 48)
+    num = area = 0.0
+    tsp = fresh.t_surf_prev()
+    for j in range(4, 47, 2):
+        for i in range(4, 39, 2):
+            if ib[1, j - 1, i - 1] != 4:
+                continue
+            t = f.arrays["t"][1, j - 1, i - 1] * fresh.params.t0
+            assert t == pytest.approx(tsp[j // 2 - 1, i // 2 - 1], rel=1e-15)
+            num += t * dx[i - 1] * dr[j - 1]
+            area += dx[i - 1] * dr[j - 1]
+    assert num / area == pytest.approx(1578.58003559575, rel=1e-13)
+    assert area == pytest.approx(21.0, rel=1e-13)
+
+
+def tave(case, f) -> float:
+    """T_ave_calc (Utility.f90:1485-1509): mass-weighted mean over open cells."""
+    ib = case.ibcell()
+    dx, dr, dz = arr(case.grid.dx, case.mp), arr(case.grid.dr, case.np), arr(case.grid.dz, case.lp)
+    T, D = f.arrays["t"], f.arrays["dnst"]
+    num = den = 0.0
+    for k in range(4, case.lp - 1, 2):
+        for j in range(4, case.np - 1, 2):
+            for i in range(4, case.mp - 1, 2):
+                if ib[k - 1, j - 1, i - 1] != 0:
+                    continue
+                vol = dx[i - 1] * dr[j - 1] * dz[k - 1]
+                num += T[k - 1, j - 1, i - 1] * D[k - 1, j - 1, i - 1] * vol
+                den += D[k - 1, j - 1, i - 1] * vol
+    return num * case.params.t0 / den
+
+
+def test_restart_reproduces_the_logged_mean_temperature(restarted):
+    s = restarted.summary
+    assert s["restarted"] == 1 and s["itr_gas"] == REF["tave_iteration"] == 7540
+    f = restarted.initial_fields()
+    assert f.itr_gas == 7540 and f.i1st_rad_qe_done == 1
+    assert restarted.params.maxgi == 100 + 7540          # Initsv.f90:310
+    t = restarted.c.tail
+    assert (t.i1st_rad_done, t.interval_rad) == (1, 100)
+    assert tave(restarted, f) == pytest.approx(REF["tave_last"], rel=1e-12)
+
+
+def test_restart_writer_matches_the_reference_layout(restarted, case_dir, tmp_path):
+    """Writing the restarted state gives the reference file's record layout,
+    and every value read_restart_data takes back from it unchanged."""
+    out = tmp_path / "rg0041c.d"
+    restarted.write_restart(out)
+    a, b = records(out), records(case_dir / "rg0041c.d")
+    assert [len(x) for x in a] == [len(x) for x in b] and len(a) == 17288
+    assert out.stat().st_size == REF["rg_bytes"]
+    ib = restarted.ibcell()
+    n = 0
+    for i in range(2, 41, 2):
+        for j in range(2, 49, 2):
+            for k in range(2, 37, 2):
+                ga, gb = struct.unpack("<6d", a[2 * n]), struct.unpack("<6d", b[2 * n])
+                fa, fb = struct.unpack("<7d", a[2 * n + 1]), struct.unpack("<7d", b[2 * n + 1])
+                c = ib[k - 1, j - 1, i - 1]
+                assert ga[0] == gb[0]                        # P everywhere
+                if c != 2:
+                    assert ga[5] == gb[5] and fa == fb       # THETA, GF(1:7)
+                    if c != 4:
+                        assert ga[4] == gb[4]                # T
+                n += 1
+    tail_a, tail_b = a[2 * n:], b[2 * n:]
+    assert tail_a[0] == tail_b[0]                            # bs_hprev
+    assert tail_a[2:] == tail_b[2:]                          # FACTOR/FADJ, flags, counters
+
+
+def test_restart_round_trip(fresh, case_dir, tmp_path):
+    """A written restart read back gives the written values."""
+    d = tmp_path / "rt"
+    d.mkdir()
+    for n in INPUTS:
+        shutil.copyfile(case_dir / n, d / n)
+    f0 = fresh.initial_fields()
+    f0.itr_gas = 321
+    fresh.write_restart(d / "rg0041c.d", f0)
+    back = Case.from_files(d, "0041", restart=True)
+    f1 = back.initial_fields()
+    ib = fresh.ibcell()
+    cells = np.zeros_like(ib, dtype=bool)
+    cells[1::2, 1::2, 1::2] = True
+    open_ = cells & (ib != 2)
+    assert np.array_equal(f1.arrays["p"][cells], f0.arrays["p"][cells])
+    assert np.array_equal(f1.arrays["theta"][open_], f0.arrays["theta"][open_])
+    for l in range(7):
+        want = f0.arrays["gf"][l][open_]
+        if l == 4:   # THER floors epsilon at 1e-12 on reading (Prop.f90:137), walls included
+            want = np.maximum(want, 1e-12)
+        assert np.array_equal(f1.arrays["gf"][l][open_], want)
+    assert np.array_equal(f1.arrays["bs_hprev"], f0.arrays["bs_hprev"])
+    assert f1.itr_gas == 321 and back.params.maxgi == 100 + 321
+    assert np.array_equal(back.t_surf_prev().shape, (24, 20))
+
+
+def test_bad_inputs_fail_loudly(case_dir, tmp_path):
+    d = tmp_path / "bad"
+    d.mkdir()
+    for n in INPUTS:
+        shutil.copyfile(case_dir / n, d / n)
+    with pytest.raises(GfmError) as e:
+        Case.from_files(d, "0042")
+    assert e.value.rc == abi.GFM_E_IO
+    with pytest.raises(GfmError) as e:
+        Case.from_files(d, "0041", restart=True)              # no rg file in this directory
+    assert e.value.rc == abi.GFM_E_IO
+    # a half-blocked cell (digit 9 -> IBCELL=-1) is outside the supported set
+    gd = (d / "gd0041c.dat").read_text()
+    (d / "gd0041c.dat").write_text(gd.replace("  36  110000000000000000000011", "  36  110000000009000000000011", 1))
+    with pytest.raises(GfmError) as e:
+        Case.from_files(d, "0041")
+    assert e.value.rc == abi.GFM_E_UNSUPPORTED
+    # the pressure reference must be an inlet cell
+    (d / "gd0041c.dat").write_text(gd)
+    sbc = (d / "sbc0041c.dat").read_text()
+    (d / "sbc0041c.dat").write_text(sbc.replace(" 6 28 10 0.0", " 8 28 10 0.0", 1))
+    with pytest.raises(GfmError) as e:
+        Case.from_files(d, "0041")
+    assert e.value.rc == abi.GFM_E_ARG
