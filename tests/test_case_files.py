@@ -277,3 +277,62 @@ def test_bad_inputs_fail_loudly(case_dir, tmp_path):
     with pytest.raises(GfmError) as e:
         Case.from_files(d, "0041")
     assert e.value.rc == abi.GFM_E_ARG
+
+
+# The reference's log of its fresh start of this case (convg0041c.plt,
+# gresid0041c.plt, gresid_xtra0041c.plt, Tave0041c.plt: iterations 1-5, 16
+# digits).  The "Epsilon" and "k" headers of gresid_xtra are swapped relative
+# to its values (k first); the tuples below are in value order.
+LOG_RES_MASS = (0.2985359321599242, 0.2700955799889087, 0.2857126586271239, 0.1378441122572042,
+                0.08171331197792968)
+LOG_P_RESID = (0.1315384926041019E-01, 0.6451466365006027E-04)
+LOG_U_RESID = ((0.1534590348758814E-05, 0.8211714142368694E-06, 0.8542377300008967E-06),
+               (0.2631044519351460E-05, 0.1179198308858852E-05, 0.6866643781345008E-06))
+# fuel, O2, CO2, N2, k, epsilon
+LOG_GF_RESID = ((0.2352936966024888E-01, 0.3192019319314679E-07, 0.4953635900594193E-08, 0.1760168965803307E-08,
+                 0.9570927785310652E-03, 0.4984251105679393E-02),
+                (0.3437604262284921E-02, 0.9048710242313167E-06, 0.1004209171771160E-06, 0.7629674415593974E-08,
+                 0.1856709982830847E-02, 0.2653345457272462E-02))
+# mean mass residual at iterations 10, 20 and 40; by iteration 100 the
+# reference's radiation calls have started and the histories part
+LOG_RES_MASS_LATER = {10: 0.6759043998754580E-01, 20: 0.4114411424620206E-01, 40: 0.7401200402133306E-02}
+LOG_TAVE = (1500.4644446183, 1501.6341231513, 1502.8394718408)
+LOG_TMEAN_EX = (1500.0, 1500.0009295316, 1499.8240966245)
+
+
+def check_against_log(stats: list) -> None:
+    """Agreement of per-iteration statistics with the reference's log of its
+    fresh start.  The logged run started from the inputs of its time; the
+    shipped it0041t.dat is the melt-surface distribution after the melt
+    cycling, and replacing it by a uniform one already moves the first
+    residual by 1.5e-4, so the bounds are the measured agreement (mean
+    temperature 1e-9 at the first iteration, residuals 1e-5 to 6e-3) with
+    headroom, not rounding bounds."""
+    for n, s in enumerate(stats[:5]):
+        assert s["res_mass"] == pytest.approx(LOG_RES_MASS[n], rel=4e-3), n
+    for it, v in LOG_RES_MASS_LATER.items():
+        if it <= len(stats):
+            assert stats[it - 1]["res_mass"] == pytest.approx(v, rel=1e-2), it
+    for n in range(2):
+        s = stats[n]
+        assert s["gf_resid"][2] == 1e-16                        # the enthalpy 0/0 residual floor
+        assert s["p_resid"] == pytest.approx(LOG_P_RESID[n], rel=2e-3), n
+        for c in range(3):
+            assert s["u_resid"][c] == pytest.approx(LOG_U_RESID[n][c], rel=1.5e-2), (n, c)
+        ours = (s["gf_resid"][0], s["gf_resid"][1], s["gf_resid"][5], s["gf_resid"][6], s["gf_resid"][3],
+                s["gf_resid"][4])
+        for c, tol in enumerate((6e-3, 5e-4, 5e-4, 5e-4, 2e-3, 2e-3)):
+            assert ours[c] == pytest.approx(LOG_GF_RESID[n][c], rel=tol), (n, c)
+    assert stats[0]["tave"] == pytest.approx(LOG_TAVE[0], rel=1e-8)
+    for n in range(3):
+        assert stats[n]["tave"] == pytest.approx(LOG_TAVE[n], rel=5e-7), n
+        assert stats[n]["tmean_ex"] == pytest.approx(LOG_TMEAN_EX[n], rel=1e-7), n
+
+
+def test_oracle_follows_the_reference_log_of_the_fresh_start(fresh):
+    from oracle.pyoracle import Oracle
+    o = Oracle(fresh)
+    o.initsv()
+    stats = [o.gflow(1)[0] for _ in range(40)]
+    o.close()
+    check_against_log(stats)
