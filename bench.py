@@ -378,6 +378,13 @@ def run_ours(args):
         except Exception as e:   # reported, never required
             rad = {"failed": str(e)}
 
+    tc21 = None
+    if rank == 0 and not args.no_tc21:
+        try:
+            tc21 = tc21_leg(not args.no_cpu_baseline)
+        except Exception as e:   # reported, never required
+            tc21 = {"failed": str(e)}
+
     learned = None
     if rank == 0 and args.learned:
         # learned p' guess: trained here on seeded variants of the 48x24x16
@@ -421,6 +428,7 @@ def run_ours(args):
             "time_to_residual": ttr,
             "learned_p_prime": learned,
             "rad_transfer": rad,
+            "tc21_case0041": tc21,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -431,6 +439,47 @@ def run_ours(args):
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def tc21_leg(with_cpu: bool, iters: int = 200) -> dict:
+    """The reference's own TC21 case 0041 (40x48x36 doubled grid, 4,407 open
+    cells), read from its case files (tests/golden/case0041): seconds per
+    outer iteration on the GPU in the reference's plane order (FP64) and in the
+    fast form (mixed precision, red-black), device time over `iters`
+    iterations after 20 warm-up iterations, next to the FP64 oracle on one
+    host core.  A grid this small is bound by launch latency, not HBM."""
+    import pathlib
+    import shutil
+    import tempfile
+    from gfm_gb300 import Case, GpuSolver, abi
+    gold = pathlib.Path(__file__).resolve().parent / "tests" / "golden" / "case0041"
+    with tempfile.TemporaryDirectory() as d:
+        for n in ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt"):
+            shutil.copyfile(gold / n, pathlib.Path(d) / n)
+        case = Case.from_files(d, "0041")
+    out = {"workload": f"TC21 case 0041 from its case files, {case.ncells:,} open cells, fresh start",
+           "timing": f"device time of {iters} iterations after 20 warm-up iterations"}
+    for name, adi, prec in (("fp64_march", abi.GFM_ADI_MARCH, abi.GFM_PREC_FP64),
+                            ("mixed_redblack", abi.GFM_ADI_REDBLACK, abi.GFM_PREC_MIXED)):
+        g = GpuSolver(case, adi_mode=adi, precision=prec)
+        g.start()
+        g.gflow(20)
+        g.reset_kernel_times()
+        st, nd = g.gflow(iters)
+        ms = g.kernel_times()["gflow_ms"] / nd
+        out[name] = {"ms_per_iteration": ms, "res_mass_last": st["res_mass"], "iterations": nd}
+        g.close()
+    if with_cpu:
+        from oracle.pyoracle import Oracle
+        o = Oracle(case)
+        o.initsv()
+        o.gflow(20)
+        t0 = time.perf_counter()
+        o.gflow(20)
+        out["cpu_oracle_ms_per_iteration"] = (time.perf_counter() - t0) / 20 * 1e3
+        o.close()
+        out["speedup_fp64_march"] = out["cpu_oracle_ms_per_iteration"] / out["fp64_march"]["ms_per_iteration"]
+    return out
 
 
 def rad_transfer_leg(with_cpu: bool) -> dict:
@@ -547,6 +596,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-rad", action="store_true", help="skip the volume radiation transfer leg")
+    ap.add_argument("--no-tc21", action="store_true", help="skip the TC21 case 0041 leg")
     ap.add_argument("--case", choices=["large", "medium", "xl"], default="large",
                     help="medium: the same furnace at 96x48x32, for kernel captures; xl: 384x160x96 with 10 bands "
                          "(neither is the benchmark workload)")

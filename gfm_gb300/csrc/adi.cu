@@ -16,6 +16,7 @@
 //   GFM_ADI_REDBLACK all planes of one colour at once, twice per sweep, NIM
 //                    sweeps, on a colour-split copy of the system (below).
 #include <algorithm>
+#include <cstdlib>
 
 #include "state.cuh"
 
@@ -23,100 +24,106 @@ namespace gfm {
 
 #define A(arr, I, J, K) (arr)[pidx(g, (I), (J), (K))]
 
-// y-line Thomas (ADLZY, Adlbl3.f90:147-181): writes XT2 for line (I,*,K)
-template <typename R, bool EXACT_DIV>
-__device__ void adlzy(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, int IPL, int IML, int K) {
-    const int LD = 2;
-    const int KPL = K + LD, KML = K - LD;
-    const int JBML = s.jb - LD;
+// One line of ADLZY (y-line, Adlbl3.f90:147-181) or ADLYZ (z-line,
+// Adlbl3.f90:187-221): the Thomas forward sweep and back substitution over
+// the n rows o0, o0+step, ..., writing PT and QT (then the solution) to pt/q.
+// Within a class every neighbour of a row is a fixed offset: +-1 for I+-2,
+// +-PX for J+-2, +-HY*PX for K+-2.  as[a_sub]/as[a_next] couple the line's
+// previous/next row; as[1]/as[0] the planes I+2/I-2; as[a_p]/as[a_m] the
+// in-plane neighbours across the line at +-d_pm.
+// The rows are taken NB at a time: their loads (coefficients, the right-hand
+// side with its four neighbour terms, the copy test) are issued together
+// before the pivot chain runs over them, so a step of the chain waits for
+// arithmetic only.  Every value is formed by the same expression as in a
+// row-by-row loop (NB = 1), so the results are the same bits; the right-hand
+// side of a copied row is formed and not used.
+template <typename R, int NB>
+__device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, R* __restrict__ q, long long o0, int n,
+                         long long step, int a_sub, int a_next, int a_p, int a_m, long long d_pm) {
+    const R* __restrict__ xt = s.xt;
+    const R* __restrict__ ap = s.ap;
+    const R* __restrict__ bs = s.bs;
+    const R* __restrict__ as_sub = s.as[a_sub];
+    const R* __restrict__ as_next = s.as[a_next];
+    const R* __restrict__ as_ip = s.as[1];
+    const R* __restrict__ as_im = s.as[0];
+    const R* __restrict__ as_p = s.as[a_p];
+    const R* __restrict__ as_m = s.as[a_m];
+    const int8_t* __restrict__ ib = g.ib;
     R pt_prev = R(0);
-    R qt_prev = A(s.xt, I, JBML, K);
-    for (int J = s.jb; J <= s.je; J += LD) {
-        const long long o = pidx(g, I, J, K);
-        R alp = s.ap[o] - pt_prev * s.as[2][o];
-        R bsy = s.bs[o];
-        R pt, qt;
-        if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) {
-            pt = R(0);
-            qt = s.xt[o];
-        } else {
-            bsy = bsy + s.as[1][o] * A(s.xt, IPL, J, K) + s.as[0][o] * A(s.xt, IML, J, K);
-            bsy = bsy + s.as[5][o] * A(s.xt, I, J, KPL) + s.as[4][o] * A(s.xt, I, J, KML);
-            if (EXACT_DIV) {
-                pt = s.as[3][o] / alp;
-                qt = (bsy + s.as[2][o] * qt_prev) / alp;
-            } else {
-                R ra = R(1) / alp;
-                pt = s.as[3][o] * ra;
-                qt = (bsy + s.as[2][o] * qt_prev) * ra;
-            }
+    R qt_prev = xt[o0 - step];   // QT of the row before the line: XT there
+    long long ob = o0;   // first row of the batch
+#pragma unroll 1
+    for (int r0 = 0; r0 < n; r0 += NB, ob += NB * step) {
+        R ap_[NB], sub_[NB], nxt_[NB], bsy_[NB], x_[NB];
+        bool cp_[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 + c >= n) break;
+            const long long o = ob + c * step;
+            ap_[c] = ap[o];
+            sub_[c] = as_sub[o];
+            nxt_[c] = as_next[o];
+            R bsy = bs[o];
+            bsy = bsy + as_ip[o] * xt[o + 1] + as_im[o] * xt[o - 1];
+            bsy = bsy + as_p[o] * xt[o + d_pm] + as_m[o] * xt[o - d_pm];
+            bsy_[c] = bsy;
+            x_[c] = xt[o];
+            cp_[c] = ib[o] >= 1;
         }
-        w.pty[o] = pt;
-        w.xt2[o] = qt;
-        pt_prev = pt;
-        qt_prev = qt;
-    }
-    R nxt = A(s.xt, I, s.je + LD, K);   // XT2(JEPL) = XT(I,JEPL,K), never updated
-    for (int J = s.je; J >= s.jb; J -= LD) {
-        const long long o = pidx(g, I, J, K);
-        R v = nxt * w.pty[o] + w.xt2[o];
-        w.xt2[o] = v;
-        nxt = v;
-    }
-}
-
-// z-line Thomas (ADLYZ, Adlbl3.f90:187-221): writes XT3 for line (I,J,*)
-template <typename R, bool EXACT_DIV>
-__device__ void adlyz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, int IPL, int IML, int J) {
-    const int LD = 2;
-    const int JPL = J + LD, JML = J - LD;
-    const int KBML = s.kb - LD;
-    R pt_prev = R(0);
-    R qt_prev = A(s.xt, I, J, KBML);
-    for (int K = s.kb; K <= s.ke; K += LD) {
-        const long long o = pidx(g, I, J, K);
-        R alp = s.ap[o] - pt_prev * s.as[4][o];
-        R bsy = s.bs[o];
-        R pt, qt;
-        if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) {
-            pt = R(0);
-            qt = s.xt[o];
-        } else {
-            bsy = bsy + s.as[1][o] * A(s.xt, IPL, J, K) + s.as[0][o] * A(s.xt, IML, J, K);
-            bsy = bsy + s.as[3][o] * A(s.xt, I, JPL, K) + s.as[2][o] * A(s.xt, I, JML, K);
-            if (EXACT_DIV) {
-                pt = s.as[5][o] / alp;
-                qt = (bsy + s.as[4][o] * qt_prev) / alp;
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 + c >= n) break;
+            R alp = ap_[c] - pt_prev * sub_[c];
+            R p_, q_;
+            if (fabs(alp) <= R(1.0e-20) || cp_[c]) {
+                p_ = R(0);
+                q_ = x_[c];
             } else {
-                R ra = R(1) / alp;
-                pt = s.as[5][o] * ra;
-                qt = (bsy + s.as[4][o] * qt_prev) * ra;
+                p_ = nxt_[c] / alp;
+                q_ = (bsy_[c] + sub_[c] * qt_prev) / alp;
             }
+            const long long o = ob + c * step;
+            pt[o] = p_;
+            q[o] = q_;
+            pt_prev = p_;
+            qt_prev = q_;
         }
-        w.ptz[o] = pt;
-        w.xt3[o] = qt;
-        pt_prev = pt;
-        qt_prev = qt;
     }
-    R nxt = A(s.xt, I, J, s.ke + LD);   // XT3(KEPL) = XT(I,J,KEPL)
-    for (int K = s.ke; K >= s.kb; K -= LD) {
-        const long long o = pidx(g, I, J, K);
-        R v = nxt * w.ptz[o] + w.xt3[o];
-        w.xt3[o] = v;
-        nxt = v;
+    // back substitution from the row after the line, whose value is XT there
+    ob = o0 + (long long)(n - 1) * step;   // last row of the batch
+    R nxt = xt[ob + step];
+#pragma unroll 1
+    for (int r0 = n - 1; r0 >= 0; r0 -= NB, ob -= NB * step) {
+        R pt_[NB], q_[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 - c < 0) break;
+            pt_[c] = pt[ob - c * step];
+            q_[c] = q[ob - c * step];
+        }
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 - c < 0) break;
+            R v = nxt * pt_[c] + q_[c];
+            q[ob - c * step] = v;
+            nxt = v;
+        }
     }
 }
 
 // ADLZ (Adlbl3.f90:103-141) on plane I by the whole CTA.
-template <typename R, bool EXACT_DIV>
+template <typename R, int NB>
 __device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I) {
     const int LD = 2;
-    const int IPL = I + LD, IML = I - LD;
     const int nK = (s.ke - s.kb) / LD + 1, nJ = (s.je - s.jb) / LD + 1;
     for (int L = 1; L <= 2; ++L) {
+        const long long dJ = g.PX, dK = (long long)g.HY * g.PX;
         for (int t = threadIdx.x; t < nK + nJ; t += blockDim.x) {
-            if (t < nK) adlzy<R, EXACT_DIV>(g, s, w, I, IPL, IML, s.kb + LD * t);
-            else adlyz<R, EXACT_DIV>(g, s, w, I, IPL, IML, s.jb + LD * (t - nK));
+            if (t < nK)   // y-line (I,*,K): XT2, PT of y
+                adl_line<R, NB>(g, s, w.pty, w.xt2, pidx(g, I, s.jb, s.kb + LD * t), nJ, dJ, 2, 3, 5, 4, dK);
+            else          // z-line (I,J,*): XT3, PT of z
+                adl_line<R, NB>(g, s, w.ptz, w.xt3, pidx(g, I, s.jb + LD * (t - nK), s.kb), nK, dK, 4, 5, 3, 2, dJ);
         }
         __syncthreads();
         for (int t = threadIdx.x; t < nK * nJ; t += blockDim.x) {
@@ -135,15 +142,28 @@ struct AdiBatch {
     int nsys;
 };
 
-// reference march: one CTA per equation
-template <typename R>
-__global__ void k_adlbl3_march(GeoT<R> g, AdiBatch<R> b) {
+// reference march: one CTA per equation; NB rows of a line per load batch.
+// At most kMarchThreads threads (a plane with more lines loops over them):
+// the batched loads take up to 247 registers a thread.
+constexpr int kMarchThreads = 256;
+template <typename R, int NB>
+__global__ void __launch_bounds__(kMarchThreads) k_adlbl3_march(GeoT<R> g, AdiBatch<R> b) {
     const Sys<R>& s = b.sys[blockIdx.x];
     const AdiScratch<R>& w = b.scr[blockIdx.x];
     for (int ns = 0; ns < s.nim; ++ns) {
-        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, true>(g, s, w, I);
-        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, true>(g, s, w, I);
+        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB>(g, s, w, I);
+        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB>(g, s, w, I);
     }
+}
+
+// rows per load batch of the march: 4, or 1 when GFM_MARCH_ROWS=1 (the
+// row-by-row loop, kept to show both give the same bits)
+static int march_rows() {
+    static const int v = [] {
+        const char* e = std::getenv("GFM_MARCH_ROWS");
+        return (e && std::atoi(e) == 1) ? 1 : 4;
+    }();
+    return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -876,7 +896,9 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
     if (threads > 1024) threads = 1024;
     if (threads < 64) threads = 64;
     if (mode == GFM_ADI_MARCH) {
-        k_adlbl3_march<R><<<nsys, threads, 0, st>>>(g, b);
+        if (threads > kMarchThreads) threads = kMarchThreads;
+        if (march_rows() == 1) k_adlbl3_march<R, 1><<<nsys, threads, 0, st>>>(g, b);
+        else k_adlbl3_march<R, 4><<<nsys, threads, 0, st>>>(g, b);
         return 1;
     } else {
         RbBatch<R> rb;

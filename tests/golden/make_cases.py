@@ -1,0 +1,91 @@
+"""Fixtures of three of the reference's shipped combustion-space cases.
+
+  case0041  TC21 40 tpd glass furnace, burners on the left side (40x48x36
+            doubled grid, 4,407 open cells), with its converged restart file
+  case0040  the same furnace with another port and flue layout (4,377 cells)
+  case1207  a longer end-fired furnace (154x28x30 doubled grid, 8,263 cells,
+            42 inlet blocks)
+
+For each case the input files are copied unchanged (gd, sbc, it and the
+shared relaxfactorc.txt), and <case>_reference.json records what the
+reference's own run of the case printed:
+
+  - summary####c.txt head   open cells, melt-surface area, inlet mass flows
+                            and the fuel heat input (Utility.f90:99-105), and
+                            the energy in with the inlet flow, q_h_in
+                            (Sbc.f90:172, printed at Utility.f90:131)
+  - convg####c.plt          mean and maximum mass residual of the first 40
+                            iterations of the run's fresh start
+  - Tave####c.plt           mean gas and exit temperatures of its first 3
+                            iterations (T_ave_calc, Utility.f90:1485-1509) and
+                            the mean gas temperature of the last iteration
+
+For case0041 the converged restart file rg0041c.d is stored xz-compressed.
+
+Run from the repository root with the reference package root as argument:
+
+    python tests/golden/make_cases.py /path/to/GFM_Source_Package_2015-08
+"""
+import hashlib
+import json
+import lzma
+import pathlib
+import re
+import shutil
+import sys
+
+HERE = pathlib.Path(__file__).resolve().parent
+CASES = {"0041": True, "0040": False, "1207": False}   # runum: keep the restart file
+
+
+def data_rows(path: pathlib.Path) -> list:
+    return [l.split() for l in path.read_text().splitlines() if l.strip() and not l.lstrip().startswith("#")]
+
+
+def summary_value(text: str, label: str) -> float:
+    m = re.search(re.escape(label) + r"\s+([-+0-9.E]+)", text)
+    assert m, label
+    return float(m.group(1))
+
+
+def main(pkg_root: str) -> None:
+    src = pathlib.Path(pkg_root) / "combustion"
+    for num, keep_rg in CASES.items():
+        case = src / f"case{num}"
+        out = HERE / f"case{num}"
+        out.mkdir(exist_ok=True)
+        for name in (f"gd{num}c.dat", f"sbc{num}c.dat", f"it{num}t.dat"):
+            shutil.copyfile(case / name, out / name)
+        shutil.copyfile(src / "relaxfactorc.txt", out / "relaxfactorc.txt")
+        summ = (case / f"summary{num}c.txt").read_text()
+        ref = {
+            "source": f"combustion/case{num} of the reference package",
+            "ncells": int(summary_value(summ, "Number of cells in combustion grid:")),
+            "area_melt_surf": summary_value(summ, "Melt surface area:"),
+            "fr_f": summary_value(summ, "Fuel in flow rate:"),
+            "fr_ox": summary_value(summ, "Oxygen in flow rate:"),
+            "fr_n2": summary_value(summ, "Nitrogen in flow rate:"),
+            "fr_total": summary_value(summ, "Total in flow rate:"),
+            "heat_in_fuel": summary_value(summ, "Heat value in with fuel:"),
+            "q_h_in": summary_value(summ, "Energy in with flow:"),
+        }
+        conv = data_rows(case / f"convg{num}c.plt")
+        assert int(conv[0][0]) == 1
+        ref["res_mass"] = [float(r[1]) for r in conv[:40]]
+        ref["res_mass_max"] = [float(r[2]) for r in conv[:40]]
+        tave = data_rows(case / f"Tave{num}c.plt")
+        ref["tave"] = [float(r[1]) for r in tave[:3]]
+        ref["tmean_ex"] = [float(r[2]) for r in tave[:3]]
+        ref["tave_iteration_last"] = int(tave[-1][0])
+        ref["tave_last"] = float(tave[-1][1])
+        if keep_rg:
+            raw = (case / f"rg{num}c.d").read_bytes()
+            (out / f"rg{num}c.d.xz").write_bytes(lzma.compress(raw, preset=9))
+            ref["rg_sha256"] = hashlib.sha256(raw).hexdigest()
+            ref["rg_bytes"] = len(raw)
+        (out / f"case{num}_reference.json").write_text(json.dumps(ref, indent=1) + "\n")
+        print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1])
