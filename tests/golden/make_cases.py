@@ -20,7 +20,11 @@ reference's own run of the case printed:
                             iterations (T_ave_calc, Utility.f90:1485-1509) and
                             the mean gas temperature of the last iteration
 
-For case0041 the converged restart file rg0041c.d is stored xz-compressed.
+The first 48 lines of each per-iteration log (convg, gresid, gresid_xtra,
+Tave and, where the run wrote them, the pre-solve gresidp and gresid_xtrap)
+are copied unchanged into logs/, as the byte-level reference of their
+format.  For case0041 the converged restart file rg0041c.d is stored
+xz-compressed.
 
 Run from the repository root with the reference package root as argument:
 
@@ -57,6 +61,12 @@ def main(pkg_root: str) -> None:
         for name in (f"gd{num}c.dat", f"sbc{num}c.dat", f"it{num}t.dat"):
             shutil.copyfile(case / name, out / name)
         shutil.copyfile(src / "relaxfactorc.txt", out / "relaxfactorc.txt")
+        (out / "logs").mkdir(exist_ok=True)
+        for log in ("convg", "gresid", "gresidp", "gresid_xtra", "gresid_xtrap", "Tave"):
+            f = case / f"{log}{num}c.plt"
+            if f.exists():
+                head = f.read_bytes().split(b"\r\n")[:48]
+                (out / "logs" / f.name).write_bytes(b"\r\n".join(head) + b"\r\n")
         summ = (case / f"summary{num}c.txt").read_text()
         ref = {
             "source": f"combustion/case{num} of the reference package",
