@@ -203,6 +203,7 @@ SIGNATURES = [
     ("gfm_case_read", C.c_int, [C.POINTER(GfmCaseFiles), C.POINTER(GfmCaseOptions), C.POINTER(GfmCase),
                                 C.POINTER(GfmCaseSummary)]),
     ("gfm_restart_write", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmFields), C.POINTER(GfmRestartTail)]),
+    ("gfm_case_write_files", C.c_int, [C.POINTER(GfmCaseSpec), C.c_char_p, C.c_char_p]),
     ("gfm_gpu_device_count", C.c_int, []),
     ("gfm_gpu_create", C.c_int, [C.POINTER(GfmGrid), C.POINTER(GfmParams), C.POINTER(C.c_void_p)]),
     ("gfm_gpu_upload", C.c_int, [C.c_void_p, C.POINTER(GfmFields)]),

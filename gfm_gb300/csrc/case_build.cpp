@@ -518,18 +518,17 @@ using gfm::host::CaseInputs;
 using gfm::host::CaseStore;
 using gfm::host::InletBlock;
 
-extern "C" int gfm_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* out) {
-    using namespace gfm::host;
-    if (!sp || !out || !kinetic_path) return GFM_E_ARG;
-    std::memset(out, 0, sizeof *out);
+namespace gfm {
+namespace host {
+
+// The synthetic furnace of a gfm_case_spec as the inputs a case directory
+// would give: grid, cell map (before the propagation) and CaseInputs.
+int synth_inputs(const gfm_case_spec* sp, CaseStore& s, CaseInputs& in) {
     if (sp->nx < 4 || sp->ny < 4 || sp->nz < 4 || sp->nx > 4096 || sp->ny > 4096 || sp->nz > 4096)
         return GFM_E_ARG;
     if (sp->n_inlets < 1 || sp->n_inlets > 8 || sp->nwl < 1 || sp->nwl > 16) return GFM_E_ARG;
     if (!(sp->lx > 0 && sp->ly > 0 && sp->lz > 0)) return GFM_E_ARG;
 
-    CaseStore* S = new (std::nothrow) CaseStore;
-    if (!S) return GFM_E_NOMEM;
-    CaseStore& s = *S;
     const int mp = 2 * sp->nx + 4, np = 2 * sp->ny + 4, lp = 2 * sp->nz + 4;
     s.mp = mp; s.np = np; s.lp = lp;
     const long N = s.n();
@@ -548,7 +547,6 @@ extern "C" int gfm_case_build(const gfm_case_spec* sp, const char* kinetic_path,
             for (int i = 2; i <= mp; i += 2)
                 if (i == 2 || i == mp || j == 2 || j == np || k == 2 || k == lp) IB(i, j, k) = 1;
     const double hy = sp->ly / sp->ny, hz = sp->lz / sp->nz;
-    CaseInputs in;
     in.inlets.resize(sp->n_inlets);
     for (int n = 0; n < sp->n_inlets; ++n) {
         const gfm_inlet_spec& is = sp->inlets[n];
@@ -617,7 +615,22 @@ extern "C" int gfm_case_build(const gfm_case_spec* sp, const char* kinetic_path,
     in.noise_amp = sp->noise_amp; in.seed = sp->seed;
     in.nr0 = 100;
     in.interval_rad = 100; in.initial_gitr = 0;
-    return gfm::host::finish_case(S, in, kinetic_path, out, nullptr);
+    return GFM_OK;
+}
+
+}  // namespace host
+}  // namespace gfm
+
+extern "C" int gfm_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* out) {
+    using namespace gfm::host;
+    if (!sp || !out || !kinetic_path) return GFM_E_ARG;
+    std::memset(out, 0, sizeof *out);
+    CaseStore* S = new (std::nothrow) CaseStore;
+    if (!S) return GFM_E_NOMEM;
+    CaseInputs in;
+    int rc = synth_inputs(sp, *S, in);
+    if (rc != GFM_OK) { delete S; return rc; }
+    return finish_case(S, in, kinetic_path, out, nullptr);
 }
 
 extern "C" void gfm_case_free(gfm_case* c) {

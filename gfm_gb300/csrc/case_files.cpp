@@ -21,6 +21,7 @@
 #include "case_store.h"
 #include "physics.h"
 
+#include <algorithm>
 #include <cctype>
 #include <cmath>
 #include <cstdio>
@@ -617,4 +618,160 @@ extern "C" int gfm_restart_write(const char* path, const gfm_grid* grid, const g
          w.rec(&q1, 4) && w.rec(&rd, 4) && w.rec(&itr, 4) && w.rec(ir2, 8) && w.rec(&ivr, 4);
     if (std::fclose(w.fp) != 0) ok = false;
     return ok ? GFM_OK : GFM_E_IO;
+}
+
+// ---- the synthetic furnace as a case directory ----------------------------------
+namespace {
+
+struct Out {
+    FILE* fp = nullptr;
+    bool ok = true;
+    explicit Out(const std::string& path) : fp(std::fopen(path.c_str(), "wb")) { ok = fp != nullptr; }
+    ~Out() { if (fp) std::fclose(fp); }
+    // CR-LF line ends, as the reference's case files have them
+    void line(const std::string& s) {
+        if (ok && (std::fwrite(s.data(), 1, s.size(), fp) != s.size() || std::fwrite("\r\n", 1, 2, fp) != 2)) ok = false;
+    }
+    bool close() {
+        bool r = ok && std::fclose(fp) == 0;
+        fp = nullptr;
+        return r;
+    }
+};
+
+// shortest decimal that reads back as the same double
+std::string num(double v) {
+    char b[40];
+    for (int p = 15; p <= 17; ++p) {
+        std::snprintf(b, sizeof b, "%.*g", p, v);
+        if (std::strtod(b, nullptr) == v) break;
+    }
+    std::string s(b);
+    if (s.find_first_of(".eEn") == std::string::npos) s += ".";   // a real, as the GUI writes them
+    return s;
+}
+
+}  // namespace
+
+extern "C" int gfm_case_write_files(const gfm_case_spec* sp, const char* dir, const char* runum) {
+    using namespace gfm::host;
+    if (!sp || !dir || !runum || std::strlen(runum) == 0 || std::strlen(runum) > 16) return GFM_E_ARG;
+    // what the files cannot carry: the seeded perturbation of the fresh
+    // start and a turbulent Prandtl number of k other than the reference's
+    if (sp->noise_amp != 0.0 || sp->sigma_k != 1.0) return GFM_E_UNSUPPORTED;
+    CaseStore s;
+    CaseInputs in;
+    int rc = synth_inputs(sp, s, in);
+    if (rc != GFM_OK) return rc;
+    const std::string d(dir), r(runum);
+    const int mp = s.mp, np = s.np, lp = s.lp;
+    auto IB = [&](int i, int j, int k) { return (int)s.ibcell[s.at(i, j, k)]; };
+
+    {   // gd####c.dat: coordinate lines by their two ends, cell map by runs
+        Out f(d + "/gd" + r + "c.dat");
+        f.line("Combustion Space");
+        f.line("    r0, mp, np, lp, surf_length_c, surf_width_c, ndp0, npt0, nsp0, nr0, grid_type");
+        f.line("    1.0 " + std::to_string(mp) + " " + std::to_string(np) + " " + std::to_string(lp) + " 0 0 0 0 7 " +
+               std::to_string(in.nr0) + " 1");
+        const char* titles[3] = {"X grid points", "Y grid points", "Z grid points"};
+        const int ext[3] = {mp, np, lp};
+        const double len[3] = {sp->lx, sp->ly, sp->lz};
+        for (int a = 0; a < 3; ++a) {
+            f.line(titles[a]);
+            f.line("   3   0.");
+            f.line("  " + std::to_string(ext[a] - 1) + "   " + num(len[a]));
+        }
+        f.line("Computational and blocked cells");
+        auto row = [&](int i, int k) {
+            std::string t;
+            for (int j = 2; j <= np; j += 2) t.push_back((char)('0' + IB(i, j, k)));
+            return t;
+        };
+        auto layer = [&](int k) {
+            std::vector<std::string> v;
+            for (int i = 2; i <= mp; i += 2) v.push_back(row(i, k));
+            return v;
+        };
+        for (int k = 2; k <= lp; k += 2) {
+            std::vector<std::string> cur = layer(k);
+            if (k < lp && layer(k + 2) == cur) continue;   // the layer holds up to the next listed K
+            char b[16];
+            std::snprintf(b, sizeof b, "%4d", k);
+            f.line(b);
+            for (int n = 0; n < (int)cur.size(); ++n) {
+                if (n + 1 < (int)cur.size() && cur[n + 1] == cur[n]) continue;
+                std::snprintf(b, sizeof b, "%4d  ", 2 * n + 2);
+                f.line(b + cur[n]);
+            }
+        }
+        f.line("");
+        f.line("&GRD");
+        f.line("/");
+        if (!f.close()) return GFM_E_IO;
+    }
+    {   // sbc####c.dat
+        Out f(d + "/sbc" + r + "c.dat");
+        f.line("&INPUT");
+        f.line(std::string("   REACT=") + (in.react ? ".TRUE." : ".FALSE."));
+        f.line("   IRSTYP=0,MAXGI=" + std::to_string(in.maxgi) + ",ID_RAD=" + (sp->rad_emission ? "1" : "-1"));
+        f.line("   MS=0,interval_rad=" + std::to_string(in.interval_rad));
+        f.line("   GMFR=" + num(in.gmfr));
+        f.line("   PG0=" + num(in.pg0));
+        f.line("   Q0=" + num(in.q0_jkg));
+        f.line("   BGCON=" + num(in.bgcon));
+        f.line("   T_init=" + num(in.t_init_k));
+        f.line("   initial_gitr=" + std::to_string(in.initial_gitr));
+        f.line("/");
+        f.line(" " + std::to_string(in.i_ref) + " " + std::to_string(in.j_ref) + " " + std::to_string(in.k_ref) + " " +
+               num(in.p_ref_pa));
+        for (const InletBlock& b : in.inlets) {
+            f.line(" " + std::to_string(b.i1) + " " + std::to_string(b.j1) + " " + std::to_string(b.k1) + " " +
+                   std::to_string(b.i2) + " " + std::to_string(b.j2) + " " + std::to_string(b.k2) + " " +
+                   std::to_string(b.iu));
+            f.line(" " + num(b.t_k) + " " + num(b.yf) + " " + num(b.yox) + " " + num(b.yn2) + " " + num(b.yco2) + " " +
+                   num(b.yh2o) + " " + num(b.yck) + " " + num(b.u) + " " + num(b.v) + " " + num(b.w));
+        }
+        f.line(" 0 0 0 0 0 0 0");
+        f.line("Exhausts:");
+        // the flue: exit cells on the x=lx wall, x-normal, positive direction,
+        // fixed radiation temperature
+        int j1 = np, j2 = 0, k1 = lp, k2 = 0;
+        for (int k = 2; k <= lp; k += 2)
+            for (int j = 2; j <= np; j += 2)
+                if (IB(mp, j, k) == 3) { j1 = std::min(j1, j); j2 = std::max(j2, j); k1 = std::min(k1, k); k2 = std::max(k2, k); }
+        f.line(" 1");
+        f.line(" " + std::to_string(mp) + " " + std::to_string(j1) + " " + std::to_string(k1) + " " + std::to_string(mp) +
+               " " + std::to_string(j2) + " " + std::to_string(k2));
+        f.line(" 1 0 1 0.9 " + num(sp->t_wall_k));
+        f.line("Wall Properties:");
+        f.line(" 0 0 0 0 0 0 0");
+        f.line("&RADIN");
+        f.line("   NWL=" + std::to_string(sp->nwl) + ",RI=" + num(in.ri) + ",H_G=" + num(in.h_g));
+        f.line("/");
+        std::string wl;
+        for (int l = 0; l < sp->nwl; ++l) wl += (l ? " " : "") + num(sp->wl_um[l]);
+        f.line(wl);
+        if (!f.close()) return GFM_E_IO;
+    }
+    {   // relaxfactorc.txt, in the reference's line order (Setup.f90:443-509)
+        Out f(d + "/relaxfactorc.txt");
+        f.line("!Relaxation factors for equation loops");
+        f.line(num(0.6) + " ! general value");
+        for (int l = 0; l < 7; ++l) f.line(num(in.rfl[l]));
+        f.line("!Relaxation factors for certain variables");
+        f.line(num(0.7) + " ! general value");
+        for (int l : {0, 1, 2, 17, 20}) f.line(num(in.rf[l]));
+        f.line(num(in.rf_tsurf) + " ! surface temperature");
+        f.line("0.5 ! minor species");
+        f.line("0.2 ! soot");
+        f.line("!Soot related relaxation factors and bounds");
+        f.line(num(in.rf_hsource) + " ! enthalpy source term");
+        for (const char* v : {"0.3", "0.3", "0.3", "0.8", "4.0d-3", "0.0", "0.0"}) f.line(v);
+        f.line("!Number of sweeps in equation solver for specified items");
+        f.line("2 ! general value");
+        for (int l = 0; l < 12; ++l) f.line(std::to_string(in.ntimesg[l]));
+        f.line("4 ! minor species");
+        if (!f.close()) return GFM_E_IO;
+    }
+    return GFM_OK;
 }

@@ -67,6 +67,10 @@ struct CaseInputs {
     int interval_rad = 100, initial_gitr = 100;
 };
 
+// The synthetic furnace of a gfm_case_spec as the inputs a case directory
+// would give: grid, cell map (before the propagation) and CaseInputs.
+int synth_inputs(const gfm_case_spec* sp, CaseStore& s, CaseInputs& in);
+
 // Builds the rest of the case from the grid and cell map in *S (IBCELL
 // before the 27-neighbour propagation) and the inputs; takes ownership of S
 // (freed on error).  Returns a GFM status.

@@ -184,6 +184,26 @@ class Case:
             pass
 
 
+def write_case_files(cfg: FurnaceCase, case_dir, runum: str, lib: C.CDLL | None = None) -> None:
+    """Writes a synthetic furnace as a GFM case directory (gd/sbc/relaxfactorc
+    files, gfm_case_write_files); Case.from_files of it, given the options the
+    files do not carry (see case_options), rebuilds Case(cfg)."""
+    lib = lib or abi.load_library()
+    spec = cfg.to_spec()
+    rc = lib.gfm_case_write_files(C.byref(spec), str(case_dir).encode(), runum.encode())
+    if rc != abi.GFM_OK:
+        raise GfmError(rc, f"gfm_case_write_files failed for {case_dir}")
+
+
+def case_options(cfg: FurnaceCase) -> dict:
+    """The keyword options of Case.from_files that a synthetic furnace's case
+    files do not carry."""
+    s = cfg.to_spec()
+    return {"sigma_eps": s.sigma_eps, "wall_sink": bool(s.wall_sink), "t_wall_k": s.t_wall_k,
+            "rad_emission": bool(s.rad_emission), "kappa": list(s.kappa)[:s.nwl],
+            "adi_mode": s.adi_mode, "precision": s.precision}
+
+
 def gflow_batch(solvers: list, n_iter: int) -> tuple[list, list]:
     """n_iter iterations of several independent solvers with their GPU work
     overlapped (gfm_gpu_gflow_batch); returns each solver's stats and count."""

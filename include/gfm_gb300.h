@@ -10,8 +10,9 @@
  *   CALL rad_qe_only                 combustion/Code/Sphase.f90:226
  *
  * plus the start-up work a Fortran host would otherwise do before the first
- * GFLOW (SETUP/SBC/INITSV, combustion/Code/A0main.f90:158-190) for the
- * synthetic furnace cases.
+ * GFLOW (GRID3/SETUP/SBC/INITSV, combustion/Code/A0main.f90:158-190), for the
+ * synthetic furnace cases and from a GFM case directory's own files, and the
+ * restart file of SAV3F (combustion/Code/Sav3f.f90:21-88).
  *
  * Layout at the boundary is the reference's own: every field is a Fortran
  * column-major array over the doubled staggered grid A(MP,NP,LP) (I fastest,
@@ -253,6 +254,18 @@ typedef struct gfm_case_summary {
  * GFM_E_UNSUPPORTED.  summary may be NULL. */
 int  gfm_case_read(const gfm_case_files *files, const gfm_case_options *opt,
                    gfm_case *out, gfm_case_summary *summary);
+
+/* Writes the synthetic furnace of a gfm_case_spec as a GFM case directory:
+ * gd<runum>c.dat, sbc<runum>c.dat and relaxfactorc.txt in dir, in the
+ * formats GRID3, SETUP and SBC read (Grid3.f90:31-280, Setup.f90:227-509,
+ * Sbc.f90:57-355).  No reference counterpart: the reference's GUI writes
+ * these files.  gfm_case_read of the written files, with the spec's
+ * sigma_eps, wall sink, wall temperature, emission switch, kappa, line order
+ * and precision as options, gives the case gfm_case_build gives.  A spec with
+ * a seeded perturbation (noise_amp) or sigma_k other than 1 returns
+ * GFM_E_UNSUPPORTED: the files cannot carry them. */
+int  gfm_case_write_files(const gfm_case_spec *spec, const char *dir,
+                          const char *runum);
 
 /* Writes the restart file rg####c.d of the state (grid, fields, tail) in
  * the record layout of SAV3F (Sav3f.f90:21-88): sequential unformatted,

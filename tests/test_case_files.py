@@ -27,7 +27,7 @@ import struct
 import numpy as np
 import pytest
 
-from gfm_gb300 import Case, GfmError, abi
+from gfm_gb300 import Case, GfmError, abi, configs
 
 from .test_case_build import propagate_ref
 
@@ -374,3 +374,54 @@ def test_oracle_follows_the_reference_log_of_the_fresh_start(num, tmp_path):
     stats = [o.gflow(1)[0] for _ in range(40)]
     o.close()
     check_against_log(num, stats)
+
+
+def case_arrays(case) -> dict:
+    """Every grid, constant and start-up field array of a built case."""
+    g, f = case.grid, case.initial_fields()
+    out = {"params": bytes(case.params)}
+    n = case.mp * case.np * case.lp
+    for nm, cnt in (("x", case.mp), ("dx", case.mp), ("r", case.np), ("dr", case.np), ("rs", case.np),
+                    ("z", case.lp), ("dz", case.lp)):
+        out[nm] = np.ctypeslib.as_array(getattr(g, nm), shape=(cnt,)).tobytes()
+    out["ibcell"] = case.ibcell().tobytes()
+    out["scalars"] = repr((g.ncells, g.i_ref, g.j_ref, g.k_ref, g.p_ref, g.b_cnt, g.nr0, g.nwl))
+    for nm in ("b_typ", "b_i", "b_j", "b_k", "b_orient", "b_direct"):
+        out[nm] = np.ctypeslib.as_array(getattr(g, nm), shape=(g.b_cnt,)).tobytes()
+    out["b_t"] = np.ctypeslib.as_array(g.b_t, shape=(g.b_cnt,)).tobytes()
+    for nm in ("rtim", "delrt", "hrt", "delr", "timed", "hrd"):
+        out[nm] = np.ctypeslib.as_array(getattr(g, nm), shape=(g.nr0,)).tobytes()
+    out["wl"] = np.ctypeslib.as_array(g.wl, shape=(g.nwl,)).tobytes()
+    out["akl0"] = np.ctypeslib.as_array(g.akl0, shape=(g.nwl,)).tobytes()
+    for k, v in f.arrays.items():
+        out["f_" + k] = v.tobytes()
+    out["f_scalars"] = repr((f.itr_gas, f.factor, f.fadj, f.gfin0, f.q_h_in))
+    return out
+
+
+@pytest.mark.parametrize("mk", [
+    lambda: configs.tiny_furnace(noise_amp=0.0),
+    lambda: configs.small_furnace(noise_amp=0.0, wall_sink=1),
+    lambda: configs.furnace_variant(5, 24, 12, 8, noise_amp=0.0, inlet_jitter=0.05),
+], ids=["tiny", "small", "variant"])
+def test_synthetic_furnace_as_case_files(mk, tmp_path):
+    """gfm_case_write_files writes a synthetic furnace as the reference's case
+    files; reading them back gives the case gfm_case_build gives, bit for bit."""
+    from gfm_gb300.solver import case_options, write_case_files
+    cfg = mk()
+    write_case_files(cfg, tmp_path, "0077")
+    back = Case.from_files(tmp_path, "0077", **case_options(cfg))
+    a, b = case_arrays(Case(cfg)), case_arrays(back)
+    assert a.keys() == b.keys()
+    diff = [k for k in a if a[k] != b[k]]
+    assert not diff, diff
+    # the files are in the reference's own layout: CR-LF records, &INPUT first
+    sbc = (tmp_path / "sbc0077c.dat").read_bytes()
+    assert sbc.startswith(b"&INPUT\r\n") and b"Exhausts:\r\n" in sbc and b"&RADIN\r\n" in sbc
+
+
+def test_case_files_cannot_carry_a_perturbed_start(tmp_path):
+    from gfm_gb300.solver import write_case_files
+    with pytest.raises(GfmError) as e:
+        write_case_files(configs.tiny_furnace(), tmp_path, "0077")   # noise_amp 0.01
+    assert e.value.rc == abi.GFM_E_UNSUPPORTED
