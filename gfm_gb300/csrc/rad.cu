@@ -27,13 +27,19 @@
 //     only its own row of the slab arrays: one thread per row, the reference's
 //     order inside the row;
 //   * the spread across the second transverse axis (part 2) touches only its
-//     own column, except for the wall-corner split, which in a box reaches
-//     only from the first and the last column into their neighbour.  So the
-//     first column runs alone, then the interior columns in parallel, then
-//     the last column: every slab-array element receives its additions in the
-//     reference's order.  An interior column that reaches a corner split (an
-//     obstacle inside the box, or the reference's undefined case on the
-//     emitter's own column) is reported as unsupported;
+//     own column, except for the wall-corner split, which also adds into the
+//     neighbouring column toward the emitter (on the emitter's own column,
+//     into the column the spread's loop variable last held: two past the last
+//     column below the emitter that split, else where the slab's last part-1
+//     spread ended).  The first column runs alone, then the interior columns
+//     in parallel, then the last column.  The interior columns' splits into
+//     other columns are listed and added after the interior phase, in the
+//     reference's column order; in a box only the first and the last column
+//     split, so every slab-array element receives its additions in the
+//     reference's order, and with obstacles (ports, a stepped crown) the
+//     listed additions are associated differently by a few roundings.  A
+//     list that overflows or a target outside the slab is reported as
+//     unsupported;
 //   * absorption into the slab's cells is per cell.
 // QAL is accumulated per CTA in its own copy (fixed emitter order) and the
 // copies are summed in a fixed order (x-direction CTAs, then y, then z), so
@@ -185,15 +191,31 @@ struct Slab {   // scratch of one CTA
     double *tU, *tV;             // far-face angle candidates of the current slab (1-based positions)
 };
 
+// Corner-split additions of the interior columns into other columns,
+// gathered during the parallel part 2 of one slab: capc entries per column in
+// the CTA's global scratch, in the column's own order; and, in shared
+// memory, the two values that decide the emitter column's target.
+struct SplitList {
+    int* maxbelow;               // largest column below the emitter that split (0: none)
+    unsigned long long* last1;   // (row << 32) | (u2 + 8) of the slab's last part-1 spread
+    int* cnt;                    // [column]: entries used
+    int* meta;                   // [column][entry][3]: target row, target column (-1: emitter's), band mask
+    double* q;                   // [column][entry][band]
+    int capc, nw;
+};
+
 __device__ __forceinline__ bool rad_corner(int d, int ibc1) {
     return d == 0 ? ibc1 > 100 : (d == 1 ? ibc1 >= 100 : ibc1 > 1);
 }
 
 template <int NW>
-__device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int slab, int v1, double ang0u) {
+__device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int slab, int v1, double ang0u,
+                          const SplitList& SL) {
     const int NWL = NW > 0 ? NW : a.NWL;
     double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
     const int bb = v1 / 2;
+    int last_u2 = 0;
+    bool spread = false;
     for (int UPM = -2; UPM <= 2; UPM += 4) {
         double A11 = 0.0, A12 = 0.0;
         const int uend = UPM < 0 ? 2 : D.Du;
@@ -214,7 +236,8 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
             }
             if (u1 != D.u0 || UPM > 0) S.f1[e] = 1;
             for (int l = 0; l < NWL; ++l) Q12[l] = Q11[l];
-            for (int u2 = u1; UPM > 0 ? u2 <= uend : u2 >= uend; u2 += UPM) {
+            int u2 = u1;
+            for (; UPM > 0 ? u2 <= uend : u2 >= uend; u2 += UPM) {
                 const int e2 = (bb - 1) * D.DA + (u2 / 2 - 1);
                 if (S.ib[e2] < 1) {
                     const double A22 = D.angU2[u2 + UPM / 2];
@@ -236,13 +259,18 @@ __device__ void part1_row(const RadArgs& a, const Dir& D, const Slab& S, int sla
                 S.fm[e2] = 0;
                 break;
             }
+            last_u2 = u2;   // the loop variable as the loop leaves it
+            spread = true;
             A11 = A12;
         }
     }
+    // rows run in parallel: the reference's last spread is the highest row's
+    if (spread) atomicMax(SL.last1, ((unsigned long long)v1 << 32) | (unsigned)(last_u2 + 8));
 }
 
 template <int NW>
-__device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int slab, int u1, double ang0v, int* err) {
+__device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int slab, int u1, double ang0v, int* err,
+                          const SplitList& SL) {
     const int NWL = NW > 0 ? NW : a.NWL;
     double Q11[NW > 0 ? NW : kRadMaxBands], Q12[NW > 0 ? NW : kRadMaxBands];
     const int aa = u1 / 2;
@@ -281,17 +309,42 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
                 bool to330 = ibc1 <= 0 && ibc2 >= 1;
                 if (!to330) {
                     if (rad_corner(D.d, ibc1) && ibc2 == 1) {
-                        if (!edge) atomicOr(err, 1);   // interior corner split: outside the supported geometry
-                        const int ut = u1 < D.u0 ? u1 + 2 : u1 - 2;
-                        const int et = (v2 / 2 - 1) * D.DA + (ut / 2 - 1);
+                        // half into the neighbouring column toward the emitter
+                        // (the emitter's own column: resolved after the
+                        // interior phase), half into this column's previous row
+                        const int ut = u1 < D.u0 ? u1 + 2 : (u1 > D.u0 ? u1 - 2 : -1);
+                        if (u1 < D.u0) atomicMax(SL.maxbelow, u1);
                         const int e2m = (v2 / 2 - KM / 2 - 1) * D.DA + (aa - 1);
-                        for (int l = 0; l < NWL; ++l) {
-                            if (rb(Q12[l]) < rb(kSmall16)) continue;
-                            const double Q21 = Q12[l] * 0.5;
-                            S.q2[l * D.A + et] = S.q2[l * D.A + et] + Q21;
-                            S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
+                        if (edge) {
+                            const int et = (v2 / 2 - 1) * D.DA + (ut / 2 - 1);
+                            for (int l = 0; l < NWL; ++l) {
+                                if (rb(Q12[l]) < rb(kSmall16)) continue;
+                                const double Q21 = Q12[l] * 0.5;
+                                S.q2[l * D.A + et] = S.q2[l * D.A + et] + Q21;
+                                S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
+                            }
+                            S.f2[et] = 0;
+                        } else {
+                            // only this column's thread writes its entries
+                            const int k = SL.cnt[aa - 1];
+                            const long long ent = (long long)(aa - 1) * SL.capc + k;
+                            unsigned msk = 0;
+                            for (int l = 0; l < NWL; ++l) {
+                                if (rb(Q12[l]) < rb(kSmall16)) continue;
+                                const double Q21 = Q12[l] * 0.5;
+                                if (k < SL.capc) SL.q[ent * SL.nw + l] = Q21;
+                                msk |= 1u << l;
+                                S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
+                            }
+                            if (k < SL.capc) {
+                                SL.meta[3 * ent] = v2;
+                                SL.meta[3 * ent + 1] = ut;
+                                SL.meta[3 * ent + 2] = (int)msk;
+                                SL.cnt[aa - 1] = k + 1;
+                            } else {
+                                atomicOr(err, 1);   // more splits in one column than the list holds
+                            }
                         }
-                        S.f2[et] = 0;
                         S.f2[e2m] = 0;
                         break;
                     }
@@ -323,6 +376,31 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
     }
 }
 
+// The listed splits of the interior columns, in the reference's column order
+// (and, within a column, its order); the emitter column's target is two past
+// the last column below the emitter that split, else where the slab's last
+// part-1 spread ended.  One thread.
+__device__ void rad_apply_splits(const RadArgs& a, const Dir& D, const Slab& S, const SplitList& SL, int* err) {
+    const int NWL = a.NWL;
+    int tgt_emitter = -1;
+    if (*SL.maxbelow >= 2) tgt_emitter = *SL.maxbelow + 2;
+    else if (*SL.last1 != 0ull) tgt_emitter = (int)(unsigned)(*SL.last1 & 0xffffffffull) - 8;
+    for (int c = 1; c <= D.DA; ++c) {   // source columns 2, 4, .. in the reference's order
+        const int m = SL.cnt[c - 1];
+        for (int k = 0; k < m; ++k) {
+            const long long ent = (long long)(c - 1) * SL.capc + k;
+            const int row = SL.meta[3 * ent];
+            const int col = SL.meta[3 * ent + 1] >= 0 ? SL.meta[3 * ent + 1] : tgt_emitter;
+            const unsigned msk = (unsigned)SL.meta[3 * ent + 2];
+            if (col < 2 || col > D.Du || (col & 1) || row < 2 || row > D.Dv) { atomicOr(err, 1); continue; }
+            const int et = (row / 2 - 1) * D.DA + (col / 2 - 1);
+            for (int l = 0; l < NWL; ++l)
+                if (msk & (1u << l)) S.q2[l * D.A + et] = S.q2[l * D.A + et] + SL.q[ent * SL.nw + l];
+            S.f2[et] = 0;
+        }
+    }
+}
+
 // Is row v1 (part 1) / column u1 (part 2) visited?  The reference skips the
 // rows before the emitter whose near angle is outside the cone and stops at
 // the first row after it whose near angle is; `exit` is that row (or beyond
@@ -343,7 +421,7 @@ struct RadAcc {   // per-thread sums of the deposits by destination
 
 template <int NW>
 __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* qalp, const double* qel1,
-                              double* ang0, RadAcc& acc, int* err) {
+                              double* ang0, RadAcc& acc, int* err, const SplitList& SL) {
     const int NWL = NW > 0 ? NW : a.NWL;
     const int n = a.MZ * a.NZ * a.LZ;
     const int tid = threadIdx.x, nth = blockDim.x;
@@ -382,6 +460,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
             const double b = fabs(D.cd[far] - D.cd[D.d0]);
             for (int e = tid; e < D.A; e += nth)
                 S.ib[e] = a.ibr[(slab / 2 - 1) * D.sd + (e % D.DA) * D.su + (e / D.DA) * D.sv];
+            for (int e = tid; e < D.DA; e += nth) SL.cnt[e] = 0;
             {
                 const int nu = D.Du / 2, nv = D.Dv / 2;   // odd positions 1 .. Du-1 and 1 .. Dv-1
                 for (int i = tid; i < nu + nv; i += nth) {
@@ -393,6 +472,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 }
             }
             __syncthreads();
+            if (tid == 0) { *SL.maxbelow = 0; *SL.last1 = 0ull; }
             if (tid == 0 || tid == 32) {
                 const bool isu = tid == 0;
                 const int P = isu ? D.Du : D.Dv, p0 = isu ? D.u0 : D.v0;
@@ -416,22 +496,25 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 const int nrows = (D.Dv - 4) / 2;   // rows 4 .. Dv-2
                 for (int r = tid; r < nrows; r += nth) {
                     const int v1 = 4 + 2 * r;
-                    if (rad_visit(D.angV2, v1, D.v0, ang0v, exits[1])) part1_row<NW>(a, D, S, slab, v1, ang0u);
+                    if (rad_visit(D.angV2, v1, D.v0, ang0v, exits[1])) part1_row<NW>(a, D, S, slab, v1, ang0u, SL);
                 }
             }
             __syncthreads();
             // part 2: first column, interior columns, last column
-            if (tid == 0 && rad_visit(D.angU2, 2, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, 2, ang0v, err);
+            if (tid == 0 && rad_visit(D.angU2, 2, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, 2, ang0v, err, SL);
             __syncthreads();
             {
                 const int ncols = (D.Du - 4) / 2;   // columns 4 .. Du-2
                 for (int r = tid; r < ncols; r += nth) {
                     const int u1 = 4 + 2 * r;
-                    if (rad_visit(D.angU2, u1, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, u1, ang0v, err);
+                    if (rad_visit(D.angU2, u1, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, u1, ang0v, err, SL);
                 }
             }
             __syncthreads();
-            if (tid == 0 && rad_visit(D.angU2, D.Du, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err);
+            if (tid == 0) {
+                rad_apply_splits(a, D, S, SL, err);
+                if (rad_visit(D.angU2, D.Du, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err, SL);
+            }
             __syncthreads();
             // absorption in the slab's cells
             const bool end = slab == dend;
@@ -479,6 +562,8 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
     __shared__ double s_qel1[kRadMaxBands];
     __shared__ double s_ang0[2];
     __shared__ double s_red[kRadThreads];
+    __shared__ int s_maxbelow;
+    __shared__ unsigned long long s_last1;
     const int NWL = NW > 0 ? NW : a.NWL;
     const int n = a.MZ * a.NZ * a.LZ;
     const int tid = threadIdx.x;
@@ -530,6 +615,10 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
     S.f1 = flags;
     S.f2 = flags + D.A;
     S.fm = flags + 2 * D.A;
+    const long long cta_cols = (long long)blockIdx.x * D.DA;
+    const SplitList SL{&s_maxbelow, &s_last1, a.split_cnt[d] + cta_cols,
+                       a.split_meta[d] + 3 * cta_cols * a.split_capc[d],
+                       a.split_q[d] + cta_cols * a.split_capc[d] * a.NWL, a.split_capc[d], a.NWL};
     for (int i = 1 + tid; i <= a.MP; i += blockDim.x) sx[i] = a.g.X[i];
     for (int i = 1 + tid; i <= a.NP; i += blockDim.x) sr[i] = a.g.Rr[i];
     for (int i = 1 + tid; i <= a.LP; i += blockDim.x) sz[i] = a.g.Z[i];
@@ -551,7 +640,7 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
             for (int l = 0; l < NWL; ++l)
                 s_qel1[l] = a.qel0[cc + (long long)l * n] * dface[D.u][D.u0] * dface[D.v][D.v0];
         __syncthreads();
-        rad_direction<NW>(a, D, S, qalp, s_qel1, s_ang0, acc, a.err);
+        rad_direction<NW>(a, D, S, qalp, s_qel1, s_ang0, acc, a.err, SL);
         __syncthreads();
     }
     // block totals in a fixed order

@@ -1169,6 +1169,16 @@ int rad_prepare(gfm_handle* h, const RadArgs& in) {
         if ((rc = dalloc(h, &a.scratch[d], 3 * A * a.NWL * a.grid[d])) || (rc = dalloc(h, &a.fscratch[d], 3 * A * a.grid[d])))
             return rc;
     }
+    // corner-split lists: per CTA and part-2 column up to min(Dv, 64) entries
+    // (a column splits at most once per source row and spread direction)
+    for (int d = 0; d < 3; ++d) {
+        const int Du = d == 0 ? a.NP : a.MP, Dv = d == 2 ? a.NP : a.LP;
+        const long long cols = (long long)(Du / 2) * a.grid[d];
+        a.split_capc[d] = std::min(Dv, 64);
+        if ((rc = dalloc(h, &a.split_cnt[d], cols)) || (rc = dalloc(h, &a.split_meta[d], 3 * cols * a.split_capc[d])) ||
+            (rc = dalloc(h, &a.split_q[d], cols * a.split_capc[d] * a.NWL)))
+            return rc;
+    }
     for (int s = 0; s < 2; ++s) CK(cudaStreamCreateWithFlags(&h->rad_stream[s], cudaStreamNonBlocking));
     for (int e = 0; e < 3; ++e) CK(cudaEventCreateWithFlags(&h->rad_ev[e], cudaEventDisableTiming));
     h->rad = a;

@@ -132,6 +132,12 @@ struct RadArgs {
     double* scratch[3];          // slab arrays when they do not fit in shared memory
     unsigned char* fscratch[3];
     int* err;                    // bit 0: geometry outside the supported set
+    // per direction and CTA: the corner-split additions of the interior
+    // columns of one slab, split_capc entries per column (rad.cu)
+    int split_capc[3];
+    int* split_cnt[3];           // [cta][column]
+    int* split_meta[3];          // [cta][column][entry][row, target column, band mask]
+    double* split_q[3];          // [cta][column][entry][band]
 };
 // fills slab_in_smem, smem, grid and part_base from the grid, the band count
 // and the SM count

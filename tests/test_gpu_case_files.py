@@ -152,3 +152,25 @@ def test_march_row_batches_give_the_same_bits():
         assert r.returncode == 0, r.stderr
         out.append(r.stdout.strip().splitlines()[-1])
     assert out[0] == out[1]
+
+
+@pytest.mark.parametrize("num", ("0041", "1207"))
+def test_rad_transfer_matches_oracle_on_reference_cases(num, tmp_path):
+    """The volume radiation transfer on the reference's own geometries (ports,
+    a side flue, a stepped crown, a melt surface), gray kappa 0.5 1/m in every
+    band, from the state after 3 FP64 iterations; tolerances of test_gpu_rad.
+    Their obstacles make interior columns and the emitter's own column reach
+    wall-corner splits (TC21: about 460k and 8.8k per transfer), which the
+    kernel lists and adds in the reference's column order."""
+    from .test_gpu_rad import _compare
+    case = read_case(num, tmp_path, kappa=[0.5] * 16)
+    o = Oracle(case)
+    o.initsv()
+    o.gflow(3)
+    g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    g.upload(o.download())
+    tg = g.rad_transfer()
+    to = o.rad_transfer()
+    _compare(g.download(), o.download(), tg, to)
+    g.close()
+    o.close()
