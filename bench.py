@@ -471,8 +471,36 @@ def tc21_leg(with_cpu: bool, iters: int = 200) -> dict:
         ms = g.kernel_times()["gflow_ms"] / nd
         out[name] = {"ms_per_iteration": ms, "res_mass_last": st["res_mass"], "iterations": nd}
         g.close()
+    # the volume radiation transfer on this geometry (ports, flue, stepped
+    # crown), gray kappa 0.5 1/m in its 10 bands, state after 3 FP64 iterations
+    with tempfile.TemporaryDirectory() as d:
+        for n in ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt"):
+            shutil.copyfile(gold / n, pathlib.Path(d) / n)
+        rcase = Case.from_files(d, "0041", kappa=[0.5] * 16)
+    from oracle.pyoracle import Oracle
+    o = Oracle(rcase)
+    o.initsv()
+    o.gflow(3)
+    state = o.download()
+    g = GpuSolver(rcase, precision=abi.GFM_PREC_FP64)
+    g.upload(state)
+    g.rad_transfer()
+    ts = []
+    for _ in range(3):
+        g.upload(state)
+        t0 = time.perf_counter()
+        tot = g.rad_transfer()
+        ts.append(time.perf_counter() - t0)
+    g.close()
+    out["rad_transfer"] = {"emitters": tot["n_emitters"], "bands": rcase.grid.nwl, "seconds": sorted(ts)[1],
+                           "timing": "host wall clock around the synchronous call (median of 3)"}
     if with_cpu:
-        from oracle.pyoracle import Oracle
+        t0 = time.perf_counter()
+        o.rad_transfer()
+        out["rad_transfer"]["cpu_oracle_seconds"] = time.perf_counter() - t0
+        out["rad_transfer"]["vs_cpu_oracle"] = out["rad_transfer"]["cpu_oracle_seconds"] / out["rad_transfer"]["seconds"]
+    o.close()
+    if with_cpu:
         o = Oracle(case)
         o.initsv()
         o.gflow(20)

@@ -174,3 +174,20 @@ def test_rad_transfer_matches_oracle_on_reference_cases(num, tmp_path):
     _compare(g.download(), o.download(), tg, to)
     g.close()
     o.close()
+
+
+def test_restart_with_emission_and_wall_sink_fp64_matches_oracle(case_dir):
+    """From the converged restart (itr_gas 7540) with the emission-only
+    radiation source and the fixed-temperature wall sink on (melt-surface
+    patches at the melt temperature): 12 FP64 iterations, one emission update
+    at the tenth, against the oracle."""
+    case = Case.from_files(case_dir, "0041", restart=True, rad_emission=True, wall_sink=True, kappa=[0.5] * 16)
+    sg, so, fg, fo, mask = pair(case, 12)
+    err = field_errors(fg, fo, mask)
+    assert max(err.values()) < FP64_TOL, err
+    assert fg.i1st_rad_qe_done == fo.i1st_rad_qe_done == 1
+    qe_g, qe_o = fg.arrays["qe"], fo.arrays["qe"]
+    assert np.count_nonzero(qe_o) > 0
+    assert np.linalg.norm(qe_g - qe_o) / np.linalg.norm(qe_o) < FP64_TOL
+    for a, b in zip(sg, so):
+        assert a["q_conv_total"] == pytest.approx(b["q_conv_total"], rel=FP64_TOL)
