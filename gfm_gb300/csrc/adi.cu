@@ -31,6 +31,9 @@ namespace gfm {
 // +-PX for J+-2, +-HY*PX for K+-2.  as[a_sub]/as[a_next] couple the line's
 // previous/next row; as[1]/as[0] the planes I+2/I-2; as[a_p]/as[a_m] the
 // in-plane neighbours across the line at +-d_pm.
+// PT and QT of row r live at pt/q[l0 + r*lstep]: field-sized scratch
+// indexed like the system (l0 = o0, lstep = step) or the plane's scratch in
+// shared memory.
 // The rows are taken NB at a time: their loads (coefficients, the right-hand
 // side with its four neighbour terms, the copy test) are issued together
 // before the pivot chain runs over them, so a step of the chain waits for
@@ -38,8 +41,9 @@ namespace gfm {
 // row-by-row loop (NB = 1), so the results are the same bits; the right-hand
 // side of a copied row is formed and not used.
 template <typename R, int NB>
-__device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, R* __restrict__ q, long long o0, int n,
-                         long long step, int a_sub, int a_next, int a_p, int a_m, long long d_pm) {
+__device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, R* __restrict__ q, long long l0,
+                         long long lstep, long long o0, int n, long long step, int a_sub, int a_next, int a_p, int a_m,
+                         long long d_pm) {
     const R* __restrict__ xt = s.xt;
     const R* __restrict__ ap = s.ap;
     const R* __restrict__ bs = s.bs;
@@ -52,9 +56,9 @@ __device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, 
     const int8_t* __restrict__ ib = g.ib;
     R pt_prev = R(0);
     R qt_prev = xt[o0 - step];   // QT of the row before the line: XT there
-    long long ob = o0;   // first row of the batch
+    long long ob = o0, lb = l0;   // first row of the batch
 #pragma unroll 1
-    for (int r0 = 0; r0 < n; r0 += NB, ob += NB * step) {
+    for (int r0 = 0; r0 < n; r0 += NB, ob += NB * step, lb += NB * lstep) {
         R ap_[NB], sub_[NB], nxt_[NB], bsy_[NB], x_[NB];
         bool cp_[NB];
 #pragma unroll
@@ -83,53 +87,65 @@ __device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, 
                 p_ = nxt_[c] / alp;
                 q_ = (bsy_[c] + sub_[c] * qt_prev) / alp;
             }
-            const long long o = ob + c * step;
-            pt[o] = p_;
-            q[o] = q_;
+            const long long l = lb + c * lstep;
+            pt[l] = p_;
+            q[l] = q_;
             pt_prev = p_;
             qt_prev = q_;
         }
     }
     // back substitution from the row after the line, whose value is XT there
-    ob = o0 + (long long)(n - 1) * step;   // last row of the batch
-    R nxt = xt[ob + step];
+    R nxt = xt[o0 + (long long)n * step];
+    lb = l0 + (long long)(n - 1) * lstep;   // last row of the batch
 #pragma unroll 1
-    for (int r0 = n - 1; r0 >= 0; r0 -= NB, ob -= NB * step) {
+    for (int r0 = n - 1; r0 >= 0; r0 -= NB, lb -= NB * lstep) {
         R pt_[NB], q_[NB];
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
             if (r0 - c < 0) break;
-            pt_[c] = pt[ob - c * step];
-            q_[c] = q[ob - c * step];
+            pt_[c] = pt[lb - c * lstep];
+            q_[c] = q[lb - c * lstep];
         }
 #pragma unroll
         for (int c = 0; c < NB; ++c) {
             if (r0 - c < 0) break;
             R v = nxt * pt_[c] + q_[c];
-            q[ob - c * step] = v;
+            q[lb - c * lstep] = v;
             nxt = v;
         }
     }
 }
 
-// ADLZ (Adlbl3.f90:103-141) on plane I by the whole CTA.
-template <typename R, int NB>
-__device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I) {
+// ADLZ (Adlbl3.f90:103-141) on plane I by the whole CTA.  With SM the lines'
+// PT and QT live in the plane's scratch in shared memory (four arrays of
+// nJ*nK, element (J,K) at ((K-kb)/2)*nJ + (J-jb)/2), else in the field-sized
+// scratch; the values are the same either way.
+template <typename R, int NB, bool SM>
+__device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, R* sm) {
     const int LD = 2;
     const int nK = (s.ke - s.kb) / LD + 1, nJ = (s.je - s.jb) / LD + 1;
+    const long long P = (long long)nJ * nK;
+    R* pty = SM ? sm : w.pty;
+    R* xt2 = SM ? sm + P : w.xt2;
+    R* ptz = SM ? sm + 2 * P : w.ptz;
+    R* xt3 = SM ? sm + 3 * P : w.xt3;
     for (int L = 1; L <= 2; ++L) {
         const long long dJ = g.PX, dK = (long long)g.HY * g.PX;
         for (int t = threadIdx.x; t < nK + nJ; t += blockDim.x) {
-            if (t < nK)   // y-line (I,*,K): XT2, PT of y
-                adl_line<R, NB>(g, s, w.pty, w.xt2, pidx(g, I, s.jb, s.kb + LD * t), nJ, dJ, 2, 3, 5, 4, dK);
-            else          // z-line (I,J,*): XT3, PT of z
-                adl_line<R, NB>(g, s, w.ptz, w.xt3, pidx(g, I, s.jb + LD * (t - nK), s.kb), nK, dK, 4, 5, 3, 2, dJ);
+            if (t < nK) {   // y-line (I,*,K): XT2, PT of y
+                const long long o0 = pidx(g, I, s.jb, s.kb + LD * t);
+                adl_line<R, NB>(g, s, pty, xt2, SM ? (long long)t * nJ : o0, SM ? 1 : dJ, o0, nJ, dJ, 2, 3, 5, 4, dK);
+            } else {        // z-line (I,J,*): XT3, PT of z
+                const long long o0 = pidx(g, I, s.jb + LD * (t - nK), s.kb);
+                adl_line<R, NB>(g, s, ptz, xt3, SM ? (long long)(t - nK) : o0, SM ? nJ : dK, o0, nK, dK, 4, 5, 3, 2, dJ);
+            }
         }
         __syncthreads();
         for (int t = threadIdx.x; t < nK * nJ; t += blockDim.x) {
             int K = s.kb + LD * (t / nJ), J = s.jb + LD * (t % nJ);
             long long o = pidx(g, I, J, K);
-            s.xt[o] = (w.xt2[o] + w.xt3[o]) / R(2);
+            const long long l = SM ? t : o;
+            s.xt[o] = (xt2[l] + xt3[l]) / R(2);
         }
         __syncthreads();
     }
@@ -142,17 +158,21 @@ struct AdiBatch {
     int nsys;
 };
 
-// reference march: one CTA per equation; NB rows of a line per load batch.
+// reference march: one CTA per equation; NB rows of a line per load batch;
+// with SM the plane's line scratch in dynamic shared memory.
 // At most kMarchThreads threads (a plane with more lines loops over them):
 // the batched loads take up to 247 registers a thread.
 constexpr int kMarchThreads = 256;
-template <typename R, int NB>
+constexpr size_t kMarchMaxSmem = 227 * 1024;   // opt-in dynamic shared memory of one CTA
+template <typename R, int NB, bool SM>
 __global__ void __launch_bounds__(kMarchThreads) k_adlbl3_march(GeoT<R> g, AdiBatch<R> b) {
+    extern __shared__ __align__(16) unsigned char march_smem[];
+    R* sm = reinterpret_cast<R*>(march_smem);
     const Sys<R>& s = b.sys[blockIdx.x];
     const AdiScratch<R>& w = b.scr[blockIdx.x];
     for (int ns = 0; ns < s.nim; ++ns) {
-        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB>(g, s, w, I);
-        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB>(g, s, w, I);
+        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB, SM>(g, s, w, I, sm);
+        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB, SM>(g, s, w, I, sm);
     }
 }
 
@@ -897,8 +917,15 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
     if (threads < 64) threads = 64;
     if (mode == GFM_ADI_MARCH) {
         if (threads > kMarchThreads) threads = kMarchThreads;
-        if (march_rows() == 1) k_adlbl3_march<R, 1><<<nsys, threads, 0, st>>>(g, b);
-        else k_adlbl3_march<R, 4><<<nsys, threads, 0, st>>>(g, b);
+        size_t plane = 0;   // the largest plane of the batch
+        for (int e = 0; e < nsys; ++e) {
+            const size_t p = (size_t)((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);
+            plane = p > plane ? p : plane;
+        }
+        const size_t smem = 4 * plane * sizeof(R);
+        if (march_rows() == 1) k_adlbl3_march<R, 1, false><<<nsys, threads, 0, st>>>(g, b);
+        else if (smem <= kMarchMaxSmem) k_adlbl3_march<R, 4, true><<<nsys, threads, smem, st>>>(g, b);
+        else k_adlbl3_march<R, 4, false><<<nsys, threads, 0, st>>>(g, b);
         return 1;
     } else {
         RbBatch<R> rb;
@@ -970,7 +997,11 @@ int prepare_line_solver() {
     const bool ok = cudaFuncSetAttribute(k_rbv_visit<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbvMaxSmem) ==
                         cudaSuccess &&
                     cudaFuncSetAttribute(k_rbv_visit<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kRbvMaxSmem) == cudaSuccess;
+                                         (int)kRbvMaxSmem) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_adlbl3_march<float, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMarchMaxSmem) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_adlbl3_march<double, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMarchMaxSmem) == cudaSuccess;
     return ok ? GFM_OK : GFM_E_CUDA;
 }
 
