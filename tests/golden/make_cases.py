@@ -1,10 +1,13 @@
-"""Fixtures of three of the reference's shipped combustion-space cases.
+"""Fixtures of the reference's shipped combustion-space cases.
 
   case0041  TC21 40 tpd glass furnace, burners on the left side (40x48x36
             doubled grid, 4,407 open cells), with its converged restart file
   case0040  the same furnace with another port and flue layout (4,377 cells)
   case1207  a longer end-fired furnace (154x28x30 doubled grid, 8,263 cells,
             42 inlet blocks)
+  and the other shipped cases: 0020 and 0021 (the fresh starts kept in
+  case0020oldrun, case0021oldrun), 0054 and 0055 (case0054-start,
+  case0055-start), 0056, and 1206 (the end-fired furnace's other case)
 
 For each case the input files are copied unchanged (gd, sbc, it and the
 shared relaxfactorc.txt), and <case>_reference.json records what the
@@ -39,7 +42,11 @@ import shutil
 import sys
 
 HERE = pathlib.Path(__file__).resolve().parent
-CASES = {"0041": True, "0040": False, "1207": False}   # runum: keep the restart file
+# runum: (case directory in the package, keep the restart file); for 0020,
+# 0021, 0054 and 0055 the directory holding the run's fresh start
+CASES = {"0041": ("case0041", True), "0040": ("case0040", False), "1207": ("case1207", False),
+         "0020": ("case0020oldrun", False), "0021": ("case0021oldrun", False), "0054": ("case0054-start", False),
+         "0055": ("case0055-start", False), "0056": ("case0056", False), "1206": ("case1206", False)}
 
 
 def data_rows(path: pathlib.Path) -> list:
@@ -54,8 +61,8 @@ def summary_value(text: str, label: str) -> float:
 
 def main(pkg_root: str) -> None:
     src = pathlib.Path(pkg_root) / "combustion"
-    for num, keep_rg in CASES.items():
-        case = src / f"case{num}"
+    for num, (dirname, keep_rg) in CASES.items():
+        case = src / dirname
         out = HERE / f"case{num}"
         out.mkdir(exist_ok=True)
         for name in (f"gd{num}c.dat", f"sbc{num}c.dat", f"it{num}t.dat"):
@@ -69,7 +76,7 @@ def main(pkg_root: str) -> None:
                 (out / "logs" / f.name).write_bytes(b"\r\n".join(head) + b"\r\n")
         summ = (case / f"summary{num}c.txt").read_text()
         ref = {
-            "source": f"combustion/case{num} of the reference package",
+            "source": f"combustion/{dirname} of the reference package",
             "ncells": int(summary_value(summ, "Number of cells in combustion grid:")),
             "area_melt_surf": summary_value(summ, "Melt surface area:"),
             "fr_f": summary_value(summ, "Fuel in flow rate:"),

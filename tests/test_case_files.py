@@ -1,11 +1,13 @@
 """The reference's own case files through gfm_case_read and the restart file
-through gfm_restart_write, on three of its shipped cases (tests/golden, made
-by tests/golden/make_cases.py from the reference package):
+through gfm_restart_write, on its shipped cases (tests/golden, made by
+tests/golden/make_cases.py from the reference package):
 
   case0041  TC21 40 tpd glass furnace (40x48x36 doubled grid, 4,407 cells):
             ports, a side flue, a melt surface, and its converged restart file
-  case0040  the same furnace with another port and flue layout (4,377 cells)
-  case1207  a longer end-fired furnace (154x28x30, 8,263 cells, 42 inlets)
+  case0040  the same furnace with another port and flue layout (4,377 cells),
+            and cases 0020, 0021, 0054, 0055, 0056 of that furnace family
+  case1207  a longer end-fired furnace (154x28x30, 8,263 cells, 42 inlets),
+            and case 1206 of that furnace
 
 Pins against the reference's runs of these cases:
 
@@ -35,7 +37,15 @@ GOLDEN = pathlib.Path(__file__).parent / "golden"
 GOLD = GOLDEN / "case0041"
 REF = json.loads((GOLD / "case0041_reference.json").read_text())
 INPUTS = ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt")
-CASES = ("0041", "0040", "1207")
+CASES = ("0041", "0040", "1207", "0020", "0021", "0054", "0055", "0056", "1206")
+# the shipped sbc files of the end-fired furnace carry hotter inlets than the
+# run that printed the summary (see test_summary_matches_the_reference_run)
+SUMMARY_SBC_CHANGED = {"1206", "1207"}
+# the logs in case0020oldrun and case0021oldrun come from an earlier version
+# of the program: from the same 1500 K start their mean exit temperature is
+# 2066 K at iteration 1 and their inlet enthalpy flow differs by 2%, while the
+# mean gas temperature and the residuals follow as in the other cases
+OLD_VERSION = {"0020", "0021"}
 
 
 def case_inputs(num: str) -> tuple:
@@ -99,16 +109,18 @@ def test_rg_fixture_is_the_reference_file():
 @pytest.mark.parametrize("num", CASES)
 def test_summary_matches_the_reference_run(num, tmp_path):
     """The start-up figures the reference printed for its run of the case.
-    For case 1207 the inlet enthalpy flow is left out: the printed 0.378 MW
-    comes from a run with colder inlets than the shipped sbc1207c.dat (1400 K
-    air), whose velocities the GUI recomputed for the same mass flows, so
-    those still agree; only SBC sets q_h_in (Sbc.f90:54,176)."""
+    For cases 1206 and 1207 the inlet enthalpy flow is left out: the printed
+    0.378 MW comes from a run with colder inlets than the shipped sbc files
+    (1400 K air), whose velocities the GUI recomputed for the same mass
+    flows, so those still agree; only SBC sets q_h_in (Sbc.f90:54,176).  For
+    the earlier program version of cases 0020 and 0021 it is left out too."""
     case = read_case(num, tmp_path)
     _, _, ref = case_inputs(num)
     s = case.summary
     assert s["ncells"] == ref["ncells"] == case.ncells
     assert s["area_melt_surf"] == pytest.approx(ref["area_melt_surf"], rel=1e-13)
-    for k in ("fr_f", "fr_ox", "fr_n2", "heat_in_fuel") + (("q_h_in",) if num != "1207" else ()):
+    skip_q = num in SUMMARY_SBC_CHANGED or num in OLD_VERSION
+    for k in ("fr_f", "fr_ox", "fr_n2", "heat_in_fuel") + (() if skip_q else ("q_h_in",)):
         assert s[k] == pytest.approx(ref[k], rel=1e-13), k
     assert s["fr_f"] + s["fr_ox"] + s["fr_n2"] == pytest.approx(ref["fr_total"], rel=1e-13)
     assert s["restarted"] == 0 and s["itr_gas"] == 0
@@ -325,9 +337,12 @@ LOG_GF_RESID = ((0.2352936966024888E-01, 0.3192019319314679E-07, 0.4953635900594
                  0.9570927785310652E-03, 0.4984251105679393E-02),
                 (0.3437604262284921E-02, 0.9048710242313167E-06, 0.1004209171771160E-06, 0.7629674415593974E-08,
                  0.1856709982830847E-02, 0.2653345457272462E-02))
-# measured agreement of the first 5 mass residuals and of the mean gas
-# temperature at iteration 1 with each case's log (bounds = about 2x that)
-LOG_TOL = {"0041": (4e-3, 1e-8), "0040": (1e-3, 1e-8), "1207": (8e-3, 1e-6)}
+# bounds on the agreement with each case's log, about twice the measured
+# one: mass residual over iterations 1-5, mean gas temperature at iteration
+# 1, mass residual at iterations 10, 20 and 40
+LOG_TOL = {"0041": (4e-3, 1e-8, 1.2e-2), "0040": (1e-3, 1e-8, 1.2e-2), "1207": (8e-3, 1e-6, 1.2e-2),
+           "0020": (4e-3, 1e-8, 1.5e-2), "0021": (5e-3, 1e-8, 3e-2), "0054": (1e-3, 1e-8, 1.2e-2),
+           "0055": (4e-3, 1e-8, 1.2e-2), "0056": (1e-3, 1e-8, 1.2e-2), "1206": (1.5e-2, 1e-6, 1.5e-2)}
 
 
 def check_against_log(num: str, stats: list) -> None:
@@ -337,21 +352,22 @@ def check_against_log(num: str, stats: list) -> None:
     after melt cycling (replacing case 0041's by a uniform one already moves
     its first residual by 1.5e-4), and case 1207's inlets were colder than
     its shipped sbc file says.  The bounds are the measured agreement with
-    headroom (mean gas temperature 1e-9-2e-7 at iteration 1, mass residual
-    1.5e-4-3e-3 over iterations 1-5 and within 6e-3 at 10, 20 and 40), not
+    headroom (mean gas temperature 7e-10-2e-7 at iteration 1, mass residual
+    3.6e-4-7e-3 over iterations 1-5 and within 1.8e-2 at 10, 20 and 40), not
     rounding bounds.  By iteration 100 the reference's radiation calls have
     started and the histories part."""
     _, _, ref = case_inputs(num)
-    tol5, tol_t1 = LOG_TOL[num]
+    tol5, tol_t1, tol_late = LOG_TOL[num]
     for n, s in enumerate(stats[:5]):
         assert s["res_mass"] == pytest.approx(ref["res_mass"][n], rel=tol5), n
     for it in (10, 20, 40):
         if it <= len(stats):
-            assert stats[it - 1]["res_mass"] == pytest.approx(ref["res_mass"][it - 1], rel=1.2e-2), it
+            assert stats[it - 1]["res_mass"] == pytest.approx(ref["res_mass"][it - 1], rel=tol_late), it
     assert stats[0]["tave"] == pytest.approx(ref["tave"][0], rel=tol_t1)
     for n in range(3):
-        assert stats[n]["tave"] == pytest.approx(ref["tave"][n], rel=5e-7), n
-        assert stats[n]["tmean_ex"] == pytest.approx(ref["tmean_ex"][n], rel=1e-7), n
+        assert stats[n]["tave"] == pytest.approx(ref["tave"][n], rel=1e-6), n
+        if num not in OLD_VERSION:
+            assert stats[n]["tmean_ex"] == pytest.approx(ref["tmean_ex"][n], rel=1e-7), n
     if num != "0041":
         return
     for n in range(2):

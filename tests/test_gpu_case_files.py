@@ -1,7 +1,7 @@
 """The GPU path on the reference's own cases (tests/golden): TC21 case 0041
 read from its gd/sbc/it/relaxfactor files (fresh start) and from its
-converged restart file, cases 0040 and 1207 from their files, against the
-oracle on the same inputs and against the reference's logs of the fresh
+converged restart file, the other shipped cases from their files, against
+the oracle on the same inputs and against the reference's logs of the fresh
 starts.  Tolerances as in test_gpu_parity: 1e-9 relative L2 per field for
 FP64 in the reference plane order, 1e-4 for the mixed form."""
 import lzma
