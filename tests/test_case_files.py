@@ -441,3 +441,41 @@ def test_case_files_cannot_carry_a_perturbed_start(tmp_path):
     with pytest.raises(GfmError) as e:
         write_case_files(configs.tiny_furnace(), tmp_path, "0077")   # noise_amp 0.01
     assert e.value.rc == abi.GFM_E_UNSUPPORTED
+
+
+def test_fortran_input_spellings_read_the_same(tmp_path):
+    """The same case written in other spellings that list-directed and
+    namelist input accept (lower-case keys, D exponents, blanks around '=',
+    commas as separators, r*c repeat counts, LF line ends) reads to the same
+    case; truncated files return GFM_E_IO."""
+    (tmp_path / "a").mkdir()
+    base = read_case("0041", tmp_path / "a")
+    d = tmp_path / "b"
+    d.mkdir()
+    for n in INPUTS:
+        shutil.copyfile(GOLD / n, d / n)
+    def swap(text, a, b):
+        assert a in text, a
+        return text.replace(a, b, 1)
+    sbc = (d / "sbc0041c.dat").read_text()          # universal newlines: LF from here on
+    sbc = swap(sbc, "   GMFR=0.9242821", "   gmfr = 9.242821D-1")
+    sbc = swap(sbc, " 6 26 8 6 30 12 1", " 6, 26, 8, 6, 30, 12, 1")
+    sbc = swap(sbc, " 0 0 0 0 0 0 0 \nExhausts:", " 7*0\nExhausts:")
+    (d / "sbc0041c.dat").write_text(sbc)
+    gd = (d / "gd0041c.dat").read_text()
+    (d / "gd0041c.dat").write_text(swap(gd, "   7   0.\n", "   7,   0.0D0\n"))
+    assert b"\r" not in (d / "sbc0041c.dat").read_bytes()
+    other = Case.from_files(d, "0041")
+    a, b = case_arrays(base), case_arrays(other)
+    assert [k for k in a if a[k] != b[k]] == []
+    assert other.summary["n_inlet_blocks"] == 3
+    for name, keep in (("gd0041c.dat", 20), ("sbc0041c.dat", 30), ("relaxfactorc.txt", 12), ("it0041t.dat", 15)):
+        e = tmp_path / f"cut_{name}"
+        e.mkdir()
+        for n in INPUTS:
+            shutil.copyfile(GOLD / n, e / n)
+        lines = (e / name).read_bytes().split(b"\n")
+        (e / name).write_bytes(b"\n".join(lines[:keep]))
+        with pytest.raises(GfmError) as err:
+            Case.from_files(e, "0041")
+        assert err.value.rc == abi.GFM_E_IO, name
