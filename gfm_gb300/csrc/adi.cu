@@ -116,11 +116,103 @@ __device__ void adl_line(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt, 
     }
 }
 
+// The pivots of a line: ALP = AP - PT(prev)*AS_sub and PT = AS_next/ALP,
+// the expressions of ADLZY/ADLYZ, for every row; rows the reference copies
+// (|ALP| <= 1e-20 or blocked) store ALP = 0 and PT = 0.  The coefficients are
+// fixed during one ADLBL3 call, so these are the values every plane visit of
+// the call would compute.
+template <typename R>
+__device__ void adl_pivots(const GeoT<R>& g, const Sys<R>& s, R* __restrict__ pt_out, R* __restrict__ alp_out,
+                           long long o0, int n, long long step, int a_sub, int a_next) {
+    const R* __restrict__ ap = s.ap;
+    const R* __restrict__ as_sub = s.as[a_sub];
+    const R* __restrict__ as_next = s.as[a_next];
+    R pt_prev = R(0);
+    for (int r = 0; r < n; ++r) {
+        const long long o = o0 + (long long)r * step;
+        R alp = ap[o] - pt_prev * as_sub[o];
+        R p_;
+        if (fabs(alp) <= R(1.0e-20) || g.ib[o] >= 1) {
+            p_ = R(0);
+            alp = R(0);
+        } else {
+            p_ = as_next[o] / alp;
+        }
+        pt_out[o] = p_;
+        alp_out[o] = alp;
+        pt_prev = p_;
+    }
+}
+
+// One line as adl_line, with the pivots of the call (adl_pivots) loaded
+// instead of formed: QT = (BSY + AS_sub*QT(prev))/ALP, the same expression,
+// one division per row.  PT and QT go to the plane's shared-memory scratch.
+template <typename R, int NB>
+__device__ void adl_line_piv(const GeoT<R>& g, const Sys<R>& s, const R* __restrict__ piv_pt,
+                             const R* __restrict__ piv_alp, R* __restrict__ pt, R* __restrict__ q, long long l0,
+                             long long lstep, long long o0, int n, long long step, int a_sub, int a_p, int a_m,
+                             long long d_pm) {
+    const R* __restrict__ xt = s.xt;
+    const R* __restrict__ bs = s.bs;
+    const R* __restrict__ as_sub = s.as[a_sub];
+    const R* __restrict__ as_ip = s.as[1];
+    const R* __restrict__ as_im = s.as[0];
+    const R* __restrict__ as_p = s.as[a_p];
+    const R* __restrict__ as_m = s.as[a_m];
+    R qt_prev = xt[o0 - step];
+    long long ob = o0, lb = l0;
+#pragma unroll 1
+    for (int r0 = 0; r0 < n; r0 += NB, ob += NB * step, lb += NB * lstep) {
+        R alp_[NB], sub_[NB], pt_[NB], bsy_[NB], x_[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 + c >= n) break;
+            const long long o = ob + c * step;
+            alp_[c] = piv_alp[o];
+            pt_[c] = piv_pt[o];
+            sub_[c] = as_sub[o];
+            R bsy = bs[o];
+            bsy = bsy + as_ip[o] * xt[o + 1] + as_im[o] * xt[o - 1];
+            bsy = bsy + as_p[o] * xt[o + d_pm] + as_m[o] * xt[o - d_pm];
+            bsy_[c] = bsy;
+            x_[c] = xt[o];
+        }
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 + c >= n) break;
+            const R q_ = alp_[c] == R(0) ? x_[c] : (bsy_[c] + sub_[c] * qt_prev) / alp_[c];
+            const long long l = lb + c * lstep;
+            pt[l] = pt_[c];
+            q[l] = q_;
+            qt_prev = q_;
+        }
+    }
+    R nxt = xt[o0 + (long long)n * step];
+    lb = l0 + (long long)(n - 1) * lstep;
+#pragma unroll 1
+    for (int r0 = n - 1; r0 >= 0; r0 -= NB, lb -= NB * lstep) {
+        R p_[NB], q_[NB];
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 - c < 0) break;
+            p_[c] = pt[lb - c * lstep];
+            q_[c] = q[lb - c * lstep];
+        }
+#pragma unroll
+        for (int c = 0; c < NB; ++c) {
+            if (r0 - c < 0) break;
+            R v = nxt * p_[c] + q_[c];
+            q[lb - c * lstep] = v;
+            nxt = v;
+        }
+    }
+}
+
 // ADLZ (Adlbl3.f90:103-141) on plane I by the whole CTA.  With SM the lines'
 // PT and QT live in the plane's scratch in shared memory (four arrays of
 // nJ*nK, element (J,K) at ((K-kb)/2)*nJ + (J-jb)/2), else in the field-sized
 // scratch; the values are the same either way.
-template <typename R, int NB, bool SM>
+template <typename R, int NB, bool SM, bool PIV = false>
 __device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, R* sm) {
     const int LD = 2;
     const int nK = (s.ke - s.kb) / LD + 1, nJ = (s.je - s.jb) / LD + 1;
@@ -134,10 +226,12 @@ __device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, 
         for (int t = threadIdx.x; t < nK + nJ; t += blockDim.x) {
             if (t < nK) {   // y-line (I,*,K): XT2, PT of y
                 const long long o0 = pidx(g, I, s.jb, s.kb + LD * t);
-                adl_line<R, NB>(g, s, pty, xt2, SM ? (long long)t * nJ : o0, SM ? 1 : dJ, o0, nJ, dJ, 2, 3, 5, 4, dK);
+                if (PIV) adl_line_piv<R, NB>(g, s, w.pty, w.xt2, pty, xt2, (long long)t * nJ, 1, o0, nJ, dJ, 2, 5, 4, dK);
+                else adl_line<R, NB>(g, s, pty, xt2, SM ? (long long)t * nJ : o0, SM ? 1 : dJ, o0, nJ, dJ, 2, 3, 5, 4, dK);
             } else {        // z-line (I,J,*): XT3, PT of z
                 const long long o0 = pidx(g, I, s.jb + LD * (t - nK), s.kb);
-                adl_line<R, NB>(g, s, ptz, xt3, SM ? (long long)(t - nK) : o0, SM ? nJ : dK, o0, nK, dK, 4, 5, 3, 2, dJ);
+                if (PIV) adl_line_piv<R, NB>(g, s, w.ptz, w.xt3, ptz, xt3, (long long)(t - nK), nJ, o0, nK, dK, 4, 3, 2, dJ);
+                else adl_line<R, NB>(g, s, ptz, xt3, SM ? (long long)(t - nK) : o0, SM ? nJ : dK, o0, nK, dK, 4, 5, 3, 2, dJ);
             }
         }
         __syncthreads();
@@ -158,21 +252,37 @@ struct AdiBatch {
     int nsys;
 };
 
+// Pivots of every y- and z-line of every plane of the batch's systems, one
+// thread per line: y-line pivots into PTY/XT2, z-line pivots into PTZ/XT3 of
+// the field-sized scratch, which the shared-memory march does not use.
+template <typename R>
+__global__ void k_march_pivots(GeoT<R> g, AdiBatch<R> b) {
+    const Sys<R>& s = b.sys[blockIdx.y];
+    const AdiScratch<R>& w = b.scr[blockIdx.y];
+    const int npl = (s.ie - s.ib) / 2 + 1, nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
+    const long long dJ = g.PX, dK = (long long)g.HY * g.PX;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < npl * (nK + nJ); t += gridDim.x * blockDim.x) {
+        const int I = s.ib + 2 * (t % npl), u = t / npl;
+        if (u < nK) adl_pivots<R>(g, s, w.pty, w.xt2, pidx(g, I, s.jb, s.kb + 2 * u), nJ, dJ, 2, 3);
+        else adl_pivots<R>(g, s, w.ptz, w.xt3, pidx(g, I, s.jb + 2 * (u - nK), s.kb), nK, dK, 4, 5);
+    }
+}
+
 // reference march: one CTA per equation; NB rows of a line per load batch;
 // with SM the plane's line scratch in dynamic shared memory.
 // At most kMarchThreads threads (a plane with more lines loops over them):
 // the batched loads take up to 247 registers a thread.
 constexpr int kMarchThreads = 256;
 constexpr size_t kMarchMaxSmem = 227 * 1024;   // opt-in dynamic shared memory of one CTA
-template <typename R, int NB, bool SM>
+template <typename R, int NB, bool SM, bool PIV = false>
 __global__ void __launch_bounds__(kMarchThreads) k_adlbl3_march(GeoT<R> g, AdiBatch<R> b) {
     extern __shared__ __align__(16) unsigned char march_smem[];
     R* sm = reinterpret_cast<R*>(march_smem);
     const Sys<R>& s = b.sys[blockIdx.x];
     const AdiScratch<R>& w = b.scr[blockIdx.x];
     for (int ns = 0; ns < s.nim; ++ns) {
-        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB, SM>(g, s, w, I, sm);
-        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB, SM>(g, s, w, I, sm);
+        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm);
+        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm);
     }
 }
 
@@ -924,7 +1034,16 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
         }
         const size_t smem = 4 * plane * sizeof(R);
         if (march_rows() == 1) k_adlbl3_march<R, 1, false><<<nsys, threads, 0, st>>>(g, b);
-        else if (smem <= kMarchMaxSmem) k_adlbl3_march<R, 4, true><<<nsys, threads, smem, st>>>(g, b);
+        else if (smem <= kMarchMaxSmem) {
+            // pivots of the call first, then the march dividing once per row
+            int lines = 1;
+            for (int e = 0; e < nsys; ++e)
+                lines = std::max(lines, ((sys[e].ie - sys[e].ib) / 2 + 1) *
+                                            ((sys[e].ke - sys[e].kb) / 2 + 1 + (sys[e].je - sys[e].jb) / 2 + 1));
+            k_march_pivots<R><<<dim3((lines + 127) / 128, nsys), 128, 0, st>>>(g, b);
+            k_adlbl3_march<R, 4, true, true><<<nsys, threads, smem, st>>>(g, b);
+            return 2;
+        }
         else k_adlbl3_march<R, 4, false><<<nsys, threads, 0, st>>>(g, b);
         return 1;
     } else {
@@ -998,9 +1117,9 @@ int prepare_line_solver() {
                         cudaSuccess &&
                     cudaFuncSetAttribute(k_rbv_visit<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kRbvMaxSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_adlbl3_march<float, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    cudaFuncSetAttribute(k_adlbl3_march<float, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMarchMaxSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_adlbl3_march<double, 4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    cudaFuncSetAttribute(k_adlbl3_march<double, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMarchMaxSmem) == cudaSuccess;
     return ok ? GFM_OK : GFM_E_CUDA;
 }
