@@ -286,8 +286,10 @@ __global__ void __launch_bounds__(kMarchThreads) k_adlbl3_march(GeoT<R> g, AdiBa
     }
 }
 
-// rows per load batch of the march: 4, or 1 when GFM_MARCH_ROWS=1 (the
-// row-by-row loop, kept to show both give the same bits)
+// rows per load batch of the march: 4 (with the pivots of the call and the
+// plane's scratch in shared memory where it fits), or 1 when GFM_MARCH_ROWS=1:
+// the reference's row-by-row loop with field-sized scratch, kept to show that
+// both give the same bits
 static int march_rows() {
     static const int v = [] {
         const char* e = std::getenv("GFM_MARCH_ROWS");

@@ -135,10 +135,12 @@ print(h.hexdigest())
 
 
 def test_march_row_batches_give_the_same_bits():
-    """The march loads a line's rows four at a time before the pivot chain
-    runs over them; GFM_MARCH_ROWS=1 runs the row-by-row loop.  Two FP64 and
-    two mixed iterations of TC21 give the same bits either way (each run is
-    its own process: the variable is read once)."""
+    """The default march computes the pivots of each call once, loads a
+    line's rows four at a time and keeps the plane's line scratch in shared
+    memory; GFM_MARCH_ROWS=1 runs the reference's row-by-row loop with
+    field-sized scratch.  Two FP64 and two mixed iterations of TC21 give the
+    same bits either way (each run is its own process: the variable is read
+    once)."""
     import os
     import pathlib
     import subprocess
