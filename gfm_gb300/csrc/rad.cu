@@ -196,9 +196,10 @@ struct Slab {   // scratch of one CTA
 // the CTA's global scratch, in the column's own order; and, in shared
 // memory, the two values that decide the emitter column's target.
 struct SplitList {
+    int* any;                    // an interior column listed a split in this slab
     int* maxbelow;               // largest column below the emitter that split (0: none)
     unsigned long long* last1;   // (row << 32) | (u2 + 8) of the slab's last part-1 spread
-    int* cnt;                    // [column]: entries used
+    int* cnt;                    // [column]: entries used (zero between slabs)
     int* meta;                   // [column][entry][3]: target row, target column (-1: emitter's), band mask
     double* q;                   // [column][entry][band]
     int capc, nw;
@@ -336,6 +337,7 @@ __device__ void part2_col(const RadArgs& a, const Dir& D, const Slab& S, int sla
                                 msk |= 1u << l;
                                 S.q2[l * D.A + e2m] = S.q2[l * D.A + e2m] + Q21;
                             }
+                            *SL.any = 1;
                             if (k < SL.capc) {
                                 SL.meta[3 * ent] = v2;
                                 SL.meta[3 * ent + 1] = ut;
@@ -387,7 +389,9 @@ __device__ void rad_apply_splits(const RadArgs& a, const Dir& D, const Slab& S, 
     else if (*SL.last1 != 0ull) tgt_emitter = (int)(unsigned)(*SL.last1 & 0xffffffffull) - 8;
     for (int c = 1; c <= D.DA; ++c) {   // source columns 2, 4, .. in the reference's order
         const int m = SL.cnt[c - 1];
-        for (int k = 0; k < m; ++k) {
+        if (m == 0) continue;
+        SL.cnt[c - 1] = 0;
+        for (int k = 0; k < (m < SL.capc ? m : SL.capc); ++k) {
             const long long ent = (long long)(c - 1) * SL.capc + k;
             const int row = SL.meta[3 * ent];
             const int col = SL.meta[3 * ent + 1] >= 0 ? SL.meta[3 * ent + 1] : tgt_emitter;
@@ -460,7 +464,6 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
             const double b = fabs(D.cd[far] - D.cd[D.d0]);
             for (int e = tid; e < D.A; e += nth)
                 S.ib[e] = a.ibr[(slab / 2 - 1) * D.sd + (e % D.DA) * D.su + (e / D.DA) * D.sv];
-            for (int e = tid; e < D.DA; e += nth) SL.cnt[e] = 0;
             {
                 const int nu = D.Du / 2, nv = D.Dv / 2;   // odd positions 1 .. Du-1 and 1 .. Dv-1
                 for (int i = tid; i < nu + nv; i += nth) {
@@ -472,7 +475,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
                 }
             }
             __syncthreads();
-            if (tid == 0) { *SL.maxbelow = 0; *SL.last1 = 0ull; }
+            if (tid == 0) { *SL.any = 0; *SL.maxbelow = 0; *SL.last1 = 0ull; }
             if (tid == 0 || tid == 32) {
                 const bool isu = tid == 0;
                 const int P = isu ? D.Du : D.Dv, p0 = isu ? D.u0 : D.v0;
@@ -512,7 +515,7 @@ __device__ void rad_direction(const RadArgs& a, Dir& D, const Slab& S, double* q
             }
             __syncthreads();
             if (tid == 0) {
-                rad_apply_splits(a, D, S, SL, err);
+                if (*SL.any) rad_apply_splits(a, D, S, SL, err);
                 if (rad_visit(D.angU2, D.Du, D.u0, ang0u, exits[0])) part2_col<NW>(a, D, S, slab, D.Du, ang0v, err, SL);
             }
             __syncthreads();
@@ -562,7 +565,7 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
     __shared__ double s_qel1[kRadMaxBands];
     __shared__ double s_ang0[2];
     __shared__ double s_red[kRadThreads];
-    __shared__ int s_maxbelow;
+    __shared__ int s_any, s_maxbelow;
     __shared__ unsigned long long s_last1;
     const int NWL = NW > 0 ? NW : a.NWL;
     const int n = a.MZ * a.NZ * a.LZ;
@@ -616,9 +619,10 @@ __global__ void __launch_bounds__(kRadThreads) k_rad_trace(RadArgs a, int d) {
     S.f2 = flags + D.A;
     S.fm = flags + 2 * D.A;
     const long long cta_cols = (long long)blockIdx.x * D.DA;
-    const SplitList SL{&s_maxbelow, &s_last1, a.split_cnt[d] + cta_cols,
+    const SplitList SL{&s_any, &s_maxbelow, &s_last1, a.split_cnt[d] + cta_cols,
                        a.split_meta[d] + 3 * cta_cols * a.split_capc[d],
                        a.split_q[d] + cta_cols * a.split_capc[d] * a.NWL, a.split_capc[d], a.NWL};
+    for (int e = tid; e < D.DA; e += blockDim.x) SL.cnt[e] = 0;
     for (int i = 1 + tid; i <= a.MP; i += blockDim.x) sx[i] = a.g.X[i];
     for (int i = 1 + tid; i <= a.NP; i += blockDim.x) sr[i] = a.g.Rr[i];
     for (int i = 1 + tid; i <= a.LP; i += blockDim.x) sz[i] = a.g.Z[i];
