@@ -17,6 +17,7 @@
 //                    sweeps, on a colour-split copy of the system (below).
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 
 #include "state.cuh"
 
@@ -213,7 +214,7 @@ __device__ void adl_line_piv(const GeoT<R>& g, const Sys<R>& s, const R* __restr
 // nJ*nK, element (J,K) at ((K-kb)/2)*nJ + (J-jb)/2), else in the field-sized
 // scratch; the values are the same either way.
 template <typename R, int NB, bool SM, bool PIV = false>
-__device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, R* sm) {
+__device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, int I, R* sm, int wy) {
     const int LD = 2;
     const int nK = (s.ke - s.kb) / LD + 1, nJ = (s.je - s.jb) / LD + 1;
     const long long P = (long long)nJ * nK;
@@ -223,7 +224,17 @@ __device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, 
     R* xt3 = SM ? sm + 3 * P : w.xt3;
     for (int L = 1; L <= 2; ++L) {
         const long long dJ = g.PX, dK = (long long)g.HY * g.PX;
-        for (int t = threadIdx.x; t < nK + nJ; t += blockDim.x) {
+        // contiguous (wy == 0): thread t takes lines t, t + blockDim.x, .. of
+        // the y-lines followed by the z-lines; split: warps [0, wy) take the
+        // y-lines, the other warps the z-lines, each spread over its warps
+        int v0 = threadIdx.x, vstep = blockDim.x, vend = nK + nJ, off = 0;
+        if (wy > 0) {
+            const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            if (wp < wy) { v0 = lane * wy + wp; vstep = 32 * wy; vend = nK; }
+            else { v0 = lane * (nw - wy) + (wp - wy); vstep = 32 * (nw - wy); vend = nJ; off = nK; }
+        }
+        for (int v = v0; v < vend; v += vstep) {
+            const int t = v + off;
             if (t < nK) {   // y-line (I,*,K): XT2, PT of y
                 const long long o0 = pidx(g, I, s.jb, s.kb + LD * t);
                 if (PIV) adl_line_piv<R, NB>(g, s, w.pty, w.xt2, pty, xt2, (long long)t * nJ, 1, o0, nJ, dJ, 2, 5, 4, dK);
@@ -250,6 +261,7 @@ struct AdiBatch {
     Sys<R> sys[8];
     AdiScratch<R> scr[8];
     int nsys;
+    int wy[8];    // march layout of each system: 0 contiguous, else the warps of the y-lines
 };
 
 // Pivots of every y- and z-line of every plane of the batch's systems, one
@@ -281,8 +293,8 @@ __global__ void __launch_bounds__(kMarchThreads) k_adlbl3_march(GeoT<R> g, AdiBa
     const Sys<R>& s = b.sys[blockIdx.x];
     const AdiScratch<R>& w = b.scr[blockIdx.x];
     for (int ns = 0; ns < s.nim; ++ns) {
-        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm);
-        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm);
+        for (int I = s.ib; I <= s.ie; I += 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm, b.wy[blockIdx.x]);
+        for (int I = s.ie; I >= s.ib; I -= 2) adlz<R, NB, SM, PIV>(g, s, w, I, sm, b.wy[blockIdx.x]);
     }
 }
 
@@ -296,6 +308,43 @@ static int march_rows() {
         return (e && std::atoi(e) == 1) ? 1 : 4;
     }();
     return v;
+}
+// GFM_MARCH_LAYOUT=contiguous keeps thread t on lines t, t + blockDim.x, ..
+// (kept to show that the split layout gives the same bits)
+static bool march_contiguous() {
+    static const bool v = [] {
+        const char* e = std::getenv("GFM_MARCH_LAYOUT");
+        return e && std::strcmp(e, "contiguous") == 0;
+    }();
+    return v;
+}
+
+// Rows of line recurrence a warp issues in one plane: a y-line is nJ rows, a
+// z-line nK rows, and a warp whose lanes hold both kinds in one round runs
+// both branches, one after the other.  The key of a layout is the largest
+// warp's rows, then the rows of the busiest SM sub-partition (warp w on
+// sub-partition w mod 4): a line's rows are a chain of dependent divisions,
+// and the narrow FP64 pipe of a sub-partition costs the same per warp
+// instruction whatever the number of active lanes.
+static long long march_layout_cost(int nJ, int nK, int warps, int wy) {
+    long long smsp[4] = {0, 0, 0, 0}, wmax = 0;
+    const int T = warps * 32;
+    for (int w = 0; w < warps; ++w) {
+        long long c = 0;
+        if (wy == 0) {
+            for (int r0 = 32 * w; r0 < nK + nJ; r0 += T) {
+                const int e = std::min(r0 + 32, nK + nJ);
+                c += (r0 < nK ? nJ : 0) + (e > nK ? nK : 0);
+            }
+        } else if (w < wy) {
+            for (int t = w; t < nK; t += 32 * wy) c += nJ;
+        } else {
+            for (int u = w - wy; u < nJ; u += 32 * (warps - wy)) c += nK;
+        }
+        smsp[w % 4] += c;
+        wmax = std::max(wmax, c);
+    }
+    return (wmax << 24) + std::max(std::max(smsp[0], smsp[1]), std::max(smsp[2], smsp[3]));
 }
 
 // ---------------------------------------------------------------------------
@@ -338,6 +387,7 @@ struct RbBatch {
     Sys<R> sys[8];
     AdiScratch<R> scr[8];
     int nsys;
+    int wy[8];    // march layout of each system: 0 contiguous, else the warps of the y-lines
 };
 
 template <typename R>
@@ -1015,6 +1065,7 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
                       int rb_flags) {
     AdiBatch<R> b;
     b.nsys = nsys;
+    for (int e = 0; e < 8; ++e) b.wy[e] = 0;
     int max_np = 1, max_lines = 1;
     for (int e = 0; e < nsys; ++e) {
         b.sys[e] = sys[e];
@@ -1029,6 +1080,33 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
     if (threads < 64) threads = 64;
     if (mode == GFM_ADI_MARCH) {
         if (threads > kMarchThreads) threads = kMarchThreads;
+        if (march_rows() != 1 && !march_contiguous()) {
+            // the CTA size and, per system, the layout of least cost
+            // (march_layout_cost); the batch's systems run side by side
+            long long best = -1;
+            int best_warps = threads / 32, best_wy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int warps : {threads / 32, 4, 8}) {   // on a tie, the first
+                if (warps * 32 > kMarchThreads) continue;
+                long long worst = 0;
+                int wy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                for (int e = 0; e < nsys; ++e) {
+                    const int nJ = (sys[e].je - sys[e].jb) / 2 + 1, nK = (sys[e].ke - sys[e].kb) / 2 + 1;
+                    long long c = march_layout_cost(nJ, nK, warps, 0);
+                    for (int y = 1; y < warps; ++y) {
+                        const long long cy = march_layout_cost(nJ, nK, warps, y);
+                        if (cy < c) { c = cy; wy[e] = y; }
+                    }
+                    worst = std::max(worst, c);
+                }
+                if (best < 0 || worst < best) {
+                    best = worst;
+                    best_warps = warps;
+                    for (int e = 0; e < 8; ++e) best_wy[e] = wy[e];
+                }
+            }
+            threads = best_warps * 32;
+            for (int e = 0; e < 8; ++e) b.wy[e] = best_wy[e];
+        }
         size_t plane = 0;   // the largest plane of the batch
         for (int e = 0; e < nsys; ++e) {
             const size_t p = (size_t)((sys[e].je - sys[e].jb) / 2 + 1) * ((sys[e].ke - sys[e].kb) / 2 + 1);

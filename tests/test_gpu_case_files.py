@@ -136,11 +136,13 @@ print(h.hexdigest())
 
 def test_march_row_batches_give_the_same_bits():
     """The default march computes the pivots of each call once, loads a
-    line's rows four at a time and keeps the plane's line scratch in shared
-    memory; GFM_MARCH_ROWS=1 runs the reference's row-by-row loop with
+    line's rows four at a time, keeps the plane's line scratch in shared
+    memory and gives a plane's y-lines and z-lines their own warps;
+    GFM_MARCH_LAYOUT=contiguous keeps thread t on lines t, t + blockDim, ..
+    of both kinds; GFM_MARCH_ROWS=1 runs the reference's row-by-row loop with
     field-sized scratch.  Two FP64 and two mixed iterations of TC21 give the
-    same bits either way (each run is its own process: the variable is read
-    once)."""
+    same bits all three ways (each run is its own process: the variables are
+    read once)."""
     import os
     import pathlib
     import subprocess
@@ -148,12 +150,12 @@ def test_march_row_batches_give_the_same_bits():
     root = str(pathlib.Path(__file__).resolve().parents[1])
     code = _MARCH_RUN.format(root=root, gold=str(GOLD), inputs=INPUTS)
     out = []
-    for rows in ("4", "1"):
-        env = dict(os.environ, GFM_MARCH_ROWS=rows)
+    for rows, layout in (("4", "split"), ("4", "contiguous"), ("1", "contiguous")):
+        env = dict(os.environ, GFM_MARCH_ROWS=rows, GFM_MARCH_LAYOUT=layout)
         r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=600)
         assert r.returncode == 0, r.stderr
         out.append(r.stdout.strip().splitlines()[-1])
-    assert out[0] == out[1]
+    assert out[0] == out[1] == out[2]
 
 
 @pytest.mark.parametrize("num", ("0041", "1207"))
