@@ -325,9 +325,11 @@ static bool march_contiguous() {
 // warp's rows, then the rows of the busiest SM sub-partition (warp w on
 // sub-partition w mod 4): a line's rows are a chain of dependent divisions,
 // and the narrow FP64 pipe of a sub-partition costs the same per warp
-// instruction whatever the number of active lanes.
+// instruction whatever the number of active lanes.  Last, the most lanes a
+// warp uses: a warp load over fewer lines touches fewer cache lines.
 static long long march_layout_cost(int nJ, int nK, int warps, int wy) {
     long long smsp[4] = {0, 0, 0, 0}, wmax = 0;
+    int lanes = 0;
     const int T = warps * 32;
     for (int w = 0; w < warps; ++w) {
         long long c = 0;
@@ -335,16 +337,20 @@ static long long march_layout_cost(int nJ, int nK, int warps, int wy) {
             for (int r0 = 32 * w; r0 < nK + nJ; r0 += T) {
                 const int e = std::min(r0 + 32, nK + nJ);
                 c += (r0 < nK ? nJ : 0) + (e > nK ? nK : 0);
+                lanes = std::max(lanes, e - r0);
             }
         } else if (w < wy) {
             for (int t = w; t < nK; t += 32 * wy) c += nJ;
+            lanes = std::max(lanes, std::min(32, (nK - w + wy - 1) / wy));
         } else {
             for (int u = w - wy; u < nJ; u += 32 * (warps - wy)) c += nK;
+            lanes = std::max(lanes, std::min(32, (nJ - (w - wy) + warps - wy - 1) / (warps - wy)));
         }
         smsp[w % 4] += c;
         wmax = std::max(wmax, c);
     }
-    return (wmax << 24) + std::max(std::max(smsp[0], smsp[1]), std::max(smsp[2], smsp[3]));
+    const long long sub = std::max(std::max(smsp[0], smsp[1]), std::max(smsp[2], smsp[3]));
+    return (wmax << 40) + (sub << 8) + std::max(lanes, 0);
 }
 
 // ---------------------------------------------------------------------------
@@ -387,7 +393,6 @@ struct RbBatch {
     Sys<R> sys[8];
     AdiScratch<R> scr[8];
     int nsys;
-    int wy[8];    // march layout of each system: 0 contiguous, else the warps of the y-lines
 };
 
 template <typename R>
@@ -1085,7 +1090,7 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
             // (march_layout_cost); the batch's systems run side by side
             long long best = -1;
             int best_warps = threads / 32, best_wy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int warps : {threads / 32, 4, 8}) {   // on a tie, the first
+            for (int warps : {4, 8, threads / 32}) {   // on a tie, the first
                 if (warps * 32 > kMarchThreads) continue;
                 long long worst = 0;
                 int wy[8] = {0, 0, 0, 0, 0, 0, 0, 0};
