@@ -222,8 +222,10 @@ def run_reference(args):
     ncpu = os.cpu_count() or 1
     mem = os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES")
     cores = max(1, min(ncpu, int(mem // (6 * 2 ** 30))))
+    # a bounded sample: at most 2 timed and 3 untimed outer iterations per
+    # replica (one iteration of this furnace takes 16 s or more on a core)
     steps = max(1, min(args.steps, 2))
-    warm = 0
+    warm = max(0, min(args.warmup, 3))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(cores) as pool:
@@ -239,7 +241,7 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "cells": ncells, "replicas": cores},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{cores} independent replicas x {steps} outer iteration(s) of the FP64 oracle "
-                                   f"(C++ restatement of the Fortran GFLOW), wall {wall:.1f}s"},
+                                   f"(C++ restatement of the Fortran GFLOW) after {warm} untimed, wall {wall:.1f}s"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
