@@ -246,13 +246,18 @@ __device__ void adlz(const GeoT<R>& g, const Sys<R>& s, const AdiScratch<R>& w, 
             }
         }
         __syncthreads();
+        // a plane with one z-row (KB >= KE) takes the y-line pass alone and
+        // is done after it (Adlbl3.f90:124-130); the z-lines solved
+        // alongside are not used
+        const bool one_row = s.kb >= s.ke;
         for (int t = threadIdx.x; t < nK * nJ; t += blockDim.x) {
             int K = s.kb + LD * (t / nJ), J = s.jb + LD * (t % nJ);
             long long o = pidx(g, I, J, K);
             const long long l = SM ? t : o;
-            s.xt[o] = (xt2[l] + xt3[l]) / R(2);
+            s.xt[o] = one_row ? xt2[l] : (xt2[l] + xt3[l]) / R(2);
         }
         __syncthreads();
+        if (one_row) return;
     }
 }
 
@@ -522,6 +527,7 @@ __global__ void __launch_bounds__(32 * S, (32 * S <= 512 ? GFM_RB_MINB : 1))
     pdl_trigger();
     const Sys<R>& s = b.sys[blockIdx.y];
     if (sweep >= s.nim) return;
+    if (!FIRST && s.kb >= s.ke) return;            // one z-row: the y-line pass alone (Adlbl3.f90:124-130)
     const AdiScratch<R>& w = b.scr[blockIdx.y];
     const int npl = rb_nplanes(s.ib, s.ie);
     const int npc = (npl - colour + 1) / 2;
@@ -636,260 +642,6 @@ __global__ void __launch_bounds__(32 * S, (32 * S <= 512 ? GFM_RB_MINB : 1))
         if (i < cnt) out[base + (e0 + i) * step] = q[i] + P[i] * xin;
 }
 
-// ---------------------------------------------------------------------------
-// Fused plane visit (red-black order, planes that fit in shared memory;
-// enabled with GFM_RB_FUSED=1).  Measured on the 192x96x64 furnace it is
-// slower than the segmented passes above (9.24 against 8.29 ms per
-// iteration): one CTA per plane leaves SMs idle for a single equation and a
-// thread's rows are fetched with little memory-level parallelism.  It stays
-// as the form a staged (bulk-copy) record pipeline would build on.
-//
-// One CTA runs a whole ADLZ plane update, L = 1 and 2 with their averages,
-// for one plane of the current colour: the plane of XT with its one-cell
-// border, the pass results XT2/XT3 and the scaled x-neighbour right-hand
-// sides SBY/SBZ stay in shared memory, so a colour visit is one launch and
-// XT is read and written once.  The system lives in a plane-major copy,
-// element (p, kk, jj) at ((p+1)*(nK+2) + kk+1)*(nJ+2) + jj+1 for plane p of
-// the system, K = kb+2kk, J = jb+2jj, including the border planes, rows and
-// columns, and the factored rows (same records as above) use the same index.
-// Within the CTA the y-lines, then the z-lines, are cut into segments as in
-// k_rbs_pass: Sy = min(nJ, T/nK) segments of at most M rows per y-line,
-// Sz = min(nK, T/nJ) per z-line, with the segment scans in shared memory.
-// ---------------------------------------------------------------------------
-constexpr int kRbvThreads = 512;
-constexpr int kRbvM = 16;
-constexpr size_t kRbvMaxSmem = 227 * 1024;   // opt-in dynamic shared memory of one CTA
-
-template <typename R>
-__global__ void k_rbv_in(GeoT<R> g, RbBatch<R> b) {
-    const Sys<R>& s = b.sys[blockIdx.y];
-    const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const int RJ = nJ + 2, PL = RJ * (nK + 2), n = (npl + 2) * PL;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int p = t / PL - 1, rem = t % PL;
-        const int kk = rem / RJ - 1, jj = rem % RJ - 1;
-        w.xs[t] = s.xt[pidx(g, s.ib + 2 * p, s.jb + 2 * jj, s.kb + 2 * kk)];
-    }
-}
-
-// factored rows in the plane-major index; thread per line, plane fastest
-template <typename R>
-__global__ void k_rbv_factor(GeoT<R> g, RbBatch<R> b) {
-    constexpr int C = 8;
-    const Sys<R>& s = b.sys[blockIdx.y];
-    const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const int RJ = nJ + 2, PL = RJ * (nK + 2);
-    const int ny = npl * nK, nz = npl * nJ;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < ny + nz; t += gridDim.x * blockDim.x) {
-        const bool zl = t >= ny;
-        const int u = zl ? t - ny : t;
-        const int p = u % npl, I = s.ib + 2 * p;
-        const R* __restrict__ a_sub = s.as[zl ? 4 : 2];
-        const R* __restrict__ a_next = s.as[zl ? 5 : 3];
-        const R* __restrict__ a_op = s.as[zl ? 3 : 5];
-        const R* __restrict__ a_om = s.as[zl ? 2 : 4];
-        Quad<R>* __restrict__ qa = zl ? w.za : w.ya;
-        Quad<R>* __restrict__ qb = zl ? w.zb : w.yb;
-        const int n = zl ? nK : nJ;
-        const int jj0 = zl ? u / npl : 0, kk0 = zl ? 0 : u / npl;
-        const int o0 = (int)pidx(g, I, s.jb + 2 * jj0, s.kb + 2 * kk0);
-        const int q0 = (p + 1) * PL + (kk0 + 1) * RJ + jj0 + 1;
-        const int ostep = zl ? g.PX * g.HY : g.PX, qstep = zl ? RJ : 1;
-        R pt_prev = R(0);
-        for (int e0 = 0; e0 < n; e0 += C) {
-            R vap[C], vsub[C], vnext[C], vop[C], vom[C], vbs[C], va1[C], va0[C];
-            bool blk[C];
-#pragma unroll
-            for (int i = 0; i < C; ++i) {
-                if (e0 + i < n) {
-                    const int o = o0 + (e0 + i) * ostep;
-                    vap[i] = s.ap[o]; vsub[i] = a_sub[o]; vnext[i] = a_next[o];
-                    vop[i] = a_op[o]; vom[i] = a_om[o]; vbs[i] = s.bs[o];
-                    va1[i] = s.as[1][o]; va0[i] = s.as[0][o];
-                    blk[i] = g.ib[o] >= 1;
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < C; ++i) {
-                if (e0 + i < n) {
-                    const int q = q0 + (e0 + i) * qstep;
-                    const R alp = vap[i] - pt_prev * vsub[i];
-                    Quad<R> A, B;
-                    if (fabs(alp) <= R(1.0e-20) || blk[i]) {
-                        A = Quad<R>{R(0), R(0), R(0), -R(0)};
-                        B = Quad<R>{R(0), R(0), R(0), R(0)};
-                        pt_prev = R(0);
-                    } else {
-                        const R ia = R(1) / alp;
-                        const R pt = vnext[i] / alp;
-                        A = Quad<R>{vop[i] * ia, vom[i] * ia, vsub[i] * ia, pt + R(0)};   // +0.0: no -0.0 here
-                        B = Quad<R>{vbs[i] * ia, va1[i] * ia, va0[i] * ia, R(0)};
-                        pt_prev = pt;
-                    }
-                    qa[q] = A;
-                    qb[q] = B;
-                }
-            }
-        }
-    }
-}
-
-template <typename R>
-__global__ void __launch_bounds__(kRbvThreads) k_rbv_visit(GeoT<R> g, RbBatch<R> b, int colour, int sweep) {
-    constexpr int M = kRbvM;
-    extern __shared__ __align__(16) unsigned char rbv_smem[];
-    const Sys<R>& s = b.sys[blockIdx.y];
-    if (sweep >= s.nim) return;
-    const int npl = rb_nplanes(s.ib, s.ie);
-    const int p = 2 * blockIdx.x + colour;
-    if (p >= npl) return;   // whole block
-    const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const int RJ = nJ + 2, PL = RJ * (nK + 2), NC = nJ * nK;
-    const int T = blockDim.x;
-    R* X = reinterpret_cast<R*>(rbv_smem);
-    R* X2 = X + PL;
-    R* X3 = X2 + NC;
-    R* SBY = X3 + NC;
-    R* SBZ = SBY + NC;
-    R* sA = SBZ + NC;
-    R* sB = sA + T;
-    const int Sy = min(nJ, T / nK), my = (nJ + Sy - 1) / Sy;
-    const int Sz = min(nK, T / nJ), mz = (nK + Sz - 1) / Sz;
-    const int pbase = (p + 1) * PL;
-    const R* __restrict__ xg = w.xs;
-    for (int i = threadIdx.x; i < PL; i += T) X[i] = xg[pbase + i];
-    __syncthreads();
-    const int t = threadIdx.x;
-    for (int L = 1; L <= 2; ++L) {
-        for (int ph = 0; ph < 2; ++ph) {
-            const bool zp = ph == 1;   // y-lines (I,*,K) first, then z-lines (I,J,*)
-            const int S = zp ? Sz : Sy, m = zp ? mz : my, n = zp ? nK : nJ;
-            const int nt = (zp ? nJ : nK) * S;
-            const bool act = t < nt;
-            const int line = act ? (zp ? t % nJ : t / S) : 0;
-            const int seg = act ? (zp ? t / nJ : t % S) : 0;
-            const int e0 = seg * m;
-            int cnt = act ? n - e0 : 0;
-            cnt = cnt < 0 ? 0 : (cnt > m ? m : cnt);
-            const Quad<R>* __restrict__ QA = zp ? w.za : w.ya;
-            const Quad<R>* __restrict__ QB = zp ? w.zb : w.yb;
-            R* SB = zp ? SBZ : SBY;
-            R rr[M], al[M], pv[M];
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                if (i < cnt) {
-                    const int kk = zp ? e0 + i : line, jj = zp ? line : e0 + i;
-                    const int gi = pbase + (kk + 1) * RJ + jj + 1;
-                    const int c = kk * nJ + jj;
-                    const Quad<R> A = QA[gi];
-                    R bx;
-                    if (L == 1) {
-                        const Quad<R> B = QB[gi];
-                        bx = B.x + B.y * xg[gi + PL] + B.z * xg[gi - PL];
-                        SB[c] = bx;
-                    } else {
-                        bx = SB[c];
-                    }
-                    const int xc = (kk + 1) * RJ + jj + 1;
-                    const int xop = zp ? xc + 1 : xc + RJ, xom = zp ? xc - 1 : xc - RJ;
-                    R v = bx + A.x * X[xop] + A.y * X[xom];
-                    if (rb_copy(A.w)) v = X[xc];
-                    rr[i] = v;
-                    al[i] = A.z;
-                    pv[i] = A.w;
-                }
-            }
-            R q[M], P[M];
-            R qc = R(0), Pc = R(1);
-#pragma unroll
-            for (int i = 0; i < M; ++i) {
-                if (i < cnt) {
-                    qc = rr[i] + al[i] * qc;
-                    Pc = al[i] * Pc;
-                    q[i] = qc;
-                    P[i] = Pc;
-                }
-            }
-            sA[t] = cnt > 0 ? Pc : R(1);
-            sB[t] = cnt > 0 ? qc : R(0);
-            __syncthreads();
-            if (act) {
-                R qin = zp ? X[line + 1] : X[(line + 1) * RJ];   // the border below the line
-                for (int k = 0; k < seg; ++k) {
-                    const int idx = zp ? k * nJ + line : line * S + k;
-                    qin = sA[idx] * qin + sB[idx];
-                }
-#pragma unroll
-                for (int i = 0; i < M; ++i)
-                    if (i < cnt) q[i] = q[i] + P[i] * qin;
-            }
-            __syncthreads();
-            R xcv = R(0), Rc = R(1);
-#pragma unroll
-            for (int i = M - 1; i >= 0; --i) {
-                if (i < cnt) {
-                    xcv = pv[i] * xcv + q[i];
-                    Rc = pv[i] * Rc;
-                    q[i] = xcv;
-                    P[i] = Rc;
-                }
-            }
-            sA[t] = cnt > 0 ? Rc : R(1);
-            sB[t] = cnt > 0 ? xcv : R(0);
-            __syncthreads();
-            if (act) {
-                R xin = zp ? X[(nK + 1) * RJ + line + 1] : X[(line + 1) * RJ + nJ + 1];   // the border above, never updated
-                for (int k = S - 1; k > seg; --k) {
-                    const int idx = zp ? k * nJ + line : line * S + k;
-                    xin = sA[idx] * xin + sB[idx];
-                }
-                R* dst = zp ? X3 : X2;
-#pragma unroll
-                for (int i = 0; i < M; ++i)
-                    if (i < cnt) dst[zp ? (e0 + i) * nJ + line : line * nJ + e0 + i] = q[i] + P[i] * xin;
-            }
-            __syncthreads();
-        }
-        for (int c = t; c < NC; c += T) {
-            const int kk = c / nJ, jj = c % nJ;
-            X[(kk + 1) * RJ + jj + 1] = (X2[c] + X3[c]) / R(2);
-        }
-        __syncthreads();
-    }
-    for (int c = t; c < NC; c += T) {
-        const int kk = c / nJ, jj = c % nJ;
-        w.xs[pbase + (kk + 1) * RJ + jj + 1] = X[(kk + 1) * RJ + jj + 1];
-    }
-}
-
-template <typename R>
-__global__ void k_rbv_out(GeoT<R> g, RbBatch<R> b) {
-    const Sys<R>& s = b.sys[blockIdx.y];
-    const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const int npl = rb_nplanes(s.ib, s.ie), nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
-    const int RJ = nJ + 2, PL = RJ * (nK + 2), n = npl * nJ * nK;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int p = t % npl, rest = t / npl;
-        const int jj = rest % nJ, kk = rest / nJ;
-        s.xt[pidx(g, s.ib + 2 * p, s.jb + 2 * jj, s.kb + 2 * kk)] = w.xs[(p + 1) * PL + (kk + 1) * RJ + jj + 1];
-    }
-}
-
-// shared memory of one fused visit, or 0 when the system does not qualify
-template <typename R>
-size_t rbv_smem(const Sys<R>& q) {
-    const long long nK = (q.ke - q.kb) / 2 + 1, nJ = (q.je - q.jb) / 2 + 1;
-    if (nK > kRbvThreads || nJ > kRbvThreads) return 0;
-    const long long Sy = std::min(nJ, kRbvThreads / nK), Sz = std::min(nK, kRbvThreads / nJ);
-    if ((nJ + Sy - 1) / Sy > kRbvM || (nK + Sz - 1) / Sz > kRbvM) return 0;
-    const long long words = (nJ + 2) * (nK + 2) + 4 * nJ * nK + 2 * kRbvThreads;
-    const size_t bytes = (size_t)words * sizeof(R);
-    return bytes <= kRbvMaxSmem ? bytes : 0;
-}
-
 // XT = (XT2 + XT3)/2 on the planes of one colour (split copy).  Grid x runs
 // over the planes of the colour (unit stride); each thread row handles
 // kAvgRows (J,K) rows, kAvgRows*8 rows per block, loads issued together.
@@ -905,8 +657,11 @@ __global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep, int se
     const Sys<R>& s = b.sys[blockIdx.y];
     if (sweep >= s.nim) return;
     const AdiScratch<R>& w = b.scr[blockIdx.y];
-    const R* __restrict__ x2 = second ? w.x2b : w.x2;
-    const R* __restrict__ x3 = second ? w.x3b : w.x3;
+    // one z-row (KB >= KE): the plane takes its pass L=1 y-line result and
+    // nothing else (Adlbl3.f90:124-130); pass L=2 left it untouched
+    const bool one_row = s.kb >= s.ke;
+    const R* __restrict__ x2 = second && !one_row ? w.x2b : w.x2;
+    const R* __restrict__ x3 = second && !one_row ? w.x3b : w.x3;
     const int npl = rb_nplanes(s.ib, s.ie);
     const int npc = (npl - colour + 1) / 2;
     const int nK = (s.ke - s.kb) / 2 + 1, nJ = (s.je - s.jb) / 2 + 1;
@@ -926,7 +681,7 @@ __global__ void k_rbs_avg(GeoT<R> g, RbBatch<R> b, int colour, int sweep, int se
     }
 #pragma unroll
     for (int i = 0; i < kAvgRows; ++i)
-        if (row0 + i < nJ * nK) w.xs[o[i]] = (a[i] + c[i]) / R(2);
+        if (row0 + i < nJ * nK) w.xs[o[i]] = one_row ? a[i] : (a[i] + c[i]) / R(2);
 }
 
 // split copy -> XT on the solve range
@@ -1152,29 +907,6 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
             nim = q.nim > nim ? q.nim : nim;
         }
         auto blocks = [](long long n, int t) { long long b = (n + t - 1) / t; return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b)); };
-        // fused plane visits when every system's plane fits in shared memory
-        size_t smem = 0;
-        bool fused = (rb_flags & kRbFused) != 0;
-        long long max_pm = 0;
-        for (int e = 0; e < nsys; ++e) {
-            const size_t sm = rbv_smem(sys[e]);
-            fused = fused && sm > 0;
-            smem = std::max(smem, sm);
-            const Sys<R>& q = sys[e];
-            const long long pm = (long long)((q.ie - q.ib) / 2 + 3) * ((q.ke - q.kb) / 2 + 3) * ((q.je - q.jb) / 2 + 3);
-            max_pm = std::max(max_pm, pm);
-        }
-        if (fused) {
-            k_rbv_in<R><<<dim3(blocks(max_pm, 256), nsys), 256, 0, st>>>(g, rb);
-            k_rbv_factor<R><<<dim3(blocks(max_lines, 128), nsys), 128, 0, st>>>(g, rb);
-            const dim3 gv((unsigned)((max_np + 1) / 2), nsys);
-            for (int ns = 0; ns < nim; ++ns)
-                for (int half = 0; half < 2; ++half)
-                    for (int colour = 0; colour < 2; ++colour)
-                        k_rbv_visit<R><<<gv, kRbvThreads, smem, st>>>(g, rb, colour, ns);
-            k_rbv_out<R><<<dim3(blocks(max_cells, 256), nsys), 256, 0, st>>>(g, rb);
-            return 3 + 4 * nim;
-        }
         const int S = rb_segments<R>(max_n);
         const bool pdl = (rb_flags & kRbPdl) != 0;
         const bool avg2 = (rb_flags & kRbAvgInPass) != 0;            // pass L=2 averages pass L=1
@@ -1196,13 +928,9 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
     }
 }
 
-// raise the shared-memory limit of the fused visit once, before any capture
+// raise the shared-memory limits of the line-solver kernels once, before any capture
 int prepare_line_solver() {
-    const bool ok = cudaFuncSetAttribute(k_rbv_visit<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbvMaxSmem) ==
-                        cudaSuccess &&
-                    cudaFuncSetAttribute(k_rbv_visit<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kRbvMaxSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_adlbl3_march<float, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const bool ok = cudaFuncSetAttribute(k_adlbl3_march<float, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMarchMaxSmem) == cudaSuccess &&
                     cudaFuncSetAttribute(k_adlbl3_march<double, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMarchMaxSmem) == cudaSuccess;

@@ -13,8 +13,13 @@
 //
 // Scratch: PT and XT2 of the y-lines and PT and XT3 of the z-lines of ONE
 // x-plane at a time, kNaMaxPlanePoints points each (4 x 65536 doubles = 2 MiB
-// per GPU, held from library load to process exit).  Planes with more points
-// than that are rejected with GFM_E_LIMIT.  Every scratch element a call reads
+// per GPU, held until the process exits).  The CUDA runtime may load this
+// file's module, and with it the array, only when the entry point is first
+// called on a device (lazy module loading): a host that reserves the device's
+// memory for its own pool at start-up should make one call first (nim = 0
+// does no device work) so the array is in place before the pool takes the
+// rest.  Planes with more points than the limit are rejected with
+// GFM_E_LIMIT.  Every scratch element a call reads
 // was written earlier in the same call, so nothing has to be cleared between
 // calls.  All calls share the one array: calls whose kernels overlap on the GPU
 // (concurrent streams, or several host threads) race on it and give wrong
@@ -31,7 +36,7 @@ constexpr int kNaMaxDevices = 64;
 
 // The working storage.  Host code must not pass `gfm_noalloc_scratch` itself to
 // a kernel: on the host the name is only a stand-in for the device symbol.  Its
-// device address is looked up with cudaGetSymbolAddress, once per device.
+// device address is looked up with cudaGetSymbolAddress (na_scratch below).
 static __device__ __align__(256) double gfm_noalloc_scratch[4 * kNaMaxPlanePoints];
 
 namespace {
@@ -126,11 +131,16 @@ __device__ void na_plane(const NaSys& s, double* __restrict__ scr, int I) {
             }
         }
         __syncthreads();
+        // a plane with a single z-row (KB >= KE) takes its first y-line pass
+        // and nothing more (Adlbl3.f90:124-130); the z-lines solved above
+        // are not used
+        const bool one_row = s.kb >= s.ke;
         for (int t = threadIdx.x; t < npt; t += blockDim.x) {
             const int kk = t / nJ, jj = t % nJ;
-            xt[fidx(s, I, s.jb + 2 * jj, s.kb + 2 * kk)] = (xt2[t] + xt3[t]) / 2.0;
+            xt[fidx(s, I, s.jb + 2 * jj, s.kb + 2 * kk)] = one_row ? xt2[t] : (xt2[t] + xt3[t]) / 2.0;
         }
         __syncthreads();
+        if (one_row) return;
     }
 }
 
@@ -146,18 +156,29 @@ __global__ void k_adlbl3_noalloc(NaSys s, double* scr) {
 std::mutex g_na_mu;
 double* g_na_ptr[kNaMaxDevices] = {};
 
-// Device address of the scratch on the current device, looked up on the first
-// call per device and cached.
-int na_scratch(double** out) {
+// Device address of the scratch array in the current context.  It is looked
+// up on every call: an address kept from an earlier call belongs to the
+// context that was current then, and a reset of the device or another
+// context made current on the same device would leave it pointing at memory
+// that is no longer mapped.  While `stream` is capturing, no lookup is made
+// (it may load the module); the address found by this device's last call
+// outside a capture is used, and without one the call returns
+// GFM_E_UNSUPPORTED.
+int na_scratch(cudaStream_t stream, double** out) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return GFM_E_CUDA;
     if (dev < 0 || dev >= kNaMaxDevices) return GFM_E_UNSUPPORTED;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess) return GFM_E_CUDA;
     std::lock_guard<std::mutex> lk(g_na_mu);
-    if (!g_na_ptr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, gfm_noalloc_scratch) != cudaSuccess || !p) return GFM_E_CUDA;
-        g_na_ptr[dev] = static_cast<double*>(p);
+    if (cs != cudaStreamCaptureStatusNone) {
+        if (!g_na_ptr[dev]) return GFM_E_UNSUPPORTED;
+        *out = g_na_ptr[dev];
+        return GFM_OK;
     }
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, gfm_noalloc_scratch) != cudaSuccess || !p) return GFM_E_CUDA;
+    g_na_ptr[dev] = static_cast<double*>(p);
     *out = g_na_ptr[dev];
     return GFM_OK;
 }
@@ -191,7 +212,7 @@ extern "C" int gfm_adlbl3_noalloc(int mp, int np, int lp, const int16_t* ibcell,
     const void* ptrs[] = {ibcell, xt, ap, as[0], as[1], as[2], as[3], as[4], as[5], bs};
     for (const void* p : ptrs) if (!on_device(p, dev)) return GFM_E_ARG;
     double* scr = nullptr;
-    int rc = na_scratch(&scr);
+    int rc = na_scratch(static_cast<cudaStream_t>(stream), &scr);
     if (rc != GFM_OK) return rc;
     if (nim == 0) return GFM_OK;
     NaSys s;

@@ -169,12 +169,11 @@ template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
 template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
 template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);
-// red-black line-solver options: kRbFused uses the fused plane visit where the
-// planes fit in shared memory; kRbPdl launches the segmented passes, averages
-// and copies with programmatic dependent launch; kRbAvgInPass lets pass L=2
-// average the pass L=1 results where it reads them, in place of the averaging
-// launch between the passes
-constexpr int kRbFused = 1, kRbPdl = 2, kRbAvgInPass = 4;
+// red-black line-solver options: kRbPdl launches the segmented passes,
+// averages and copies with programmatic dependent launch; kRbAvgInPass lets
+// pass L=2 average the pass L=1 results where it reads them, in place of the
+// averaging launch between the passes
+constexpr int kRbPdl = 2, kRbAvgInPass = 4;
 // returns the number of kernels it launched
 template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
                                             int mode, cudaStream_t s, int rb_flags);

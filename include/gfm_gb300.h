@@ -416,11 +416,18 @@ int  gfm_gpu_set_lp(gfm_handle *h, gfm_lp *lp);
  * not device memory of the current device return GFM_E_ARG.
  *
  * The kernel is queued on `stream` (a cudaStream_t; NULL = the legacy default
- * stream) and the call returns without waiting for it.  The first call on each
- * device looks up the address of the working storage (cudaGetSymbolAddress);
- * make that first call before any stream capture starts.  Every call uses the
- * same working storage, so calls whose kernels can overlap on the GPU (other
- * streams, other host threads) race and give wrong results: order them. */
+ * stream) and the call returns without waiting for it.  Each call looks up the
+ * device address of the working storage in the current context
+ * (cudaGetSymbolAddress); a call on a capturing stream uses the address found
+ * by the last call on that device outside a capture, so make the first call on
+ * each device before any stream capture starts.  The CUDA runtime may load the
+ * working storage only at the first call on a device (lazy module loading): a
+ * host that reserves the device's memory for its own pool should make one call
+ * with nim = 0 (no device work) before it does.  A plane with a single z-row
+ * (kb == ke) takes the y-line pass alone, as the reference's ADLZ does
+ * (Adlbl3.f90:124-130).  Every call uses the same working storage, so calls
+ * whose kernels can overlap on the GPU (other streams, other host threads)
+ * race and give wrong results: order them. */
 int  gfm_adlbl3_noalloc(int mp, int np, int lp, const int16_t *ibcell,
                         double *xt, const double *ap,
                         const double *const as[6], const double *bs,

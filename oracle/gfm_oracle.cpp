@@ -856,12 +856,27 @@ struct Oracle {
                 for (int J = JB; J <= JE; J += LD) XT[ix(I, J, K)] = (p2(XT2, J, K) + p2(XT3, J, K)) / TWO;
         }
     }
+    // Plane order of the sweeps.  GFM_ADI_MARCH is the reference's (Adlbl3.f90:39-51):
+    // planes IB..IE, then IE..IB, NIM times.  GFM_ADI_REDBLACK is the order the GPU's
+    // production line solver uses: per sweep, twice, first every plane IB, IB+4, ..
+    // ("colour 0"), then every plane IB+2, IB+6, .. ("colour 1").  Planes of one
+    // colour are not neighbours (a plane update reads the planes I-2 and I+2 only),
+    // so visiting them one after another here equals visiting them all at once.  Each
+    // visit is the reference's ADLZ unchanged; only the order of the visits differs.
     void ADLBL3(vec& XT, int IB, int IE, int JB, int JE, int KB, int KE, int NIM) {
         const int LD = 2;
         if (JE == 2) { JBML = JB; JEPL = JE; } else { JBML = JB - LD; JEPL = JE + LD; }
         XT2.assign((long)NP * LP, 0.0);
         XT3.assign((long)NP * LP, 0.0);
         for (int Ns = 1; Ns <= NIM; ++Ns) {
+            if (pr.adi_mode == GFM_ADI_REDBLACK) {
+                for (int half = 0; half < 2; ++half)
+                    for (int colour = 0; colour < 2; ++colour)
+                        for (int I = IB + LD * colour; I <= IE; I += 2 * LD) {
+                            IPL = I + LD; IML = I - LD; ADLZ(XT, LD, I, JB, JE, KB, KE);
+                        }
+                continue;
+            }
             for (int I = IB; I <= IE; I += LD) { IPL = I + LD; IML = I - LD; ADLZ(XT, LD, I, JB, JE, KB, KE); }
             for (int I = IE; I >= IB; I -= LD) { IPL = I + LD; IML = I - LD; ADLZ(XT, LD, I, JB, JE, KB, KE); }
         }

@@ -63,12 +63,19 @@ def load(check_bounds: bool = False) -> C.CDLL:
 class Oracle:
     """FP64 restatement of GFLOW/SPHASE on one case's host state."""
 
-    def __init__(self, case: Case, fields: Fields | None = None, check_bounds: bool = False):
+    def __init__(self, case: Case, fields: Fields | None = None, check_bounds: bool = False,
+                 adi_mode: int | None = None):
+        """adi_mode: plane order of the line solves (abi.GFM_ADI_MARCH, the
+        reference's, or abi.GFM_ADI_REDBLACK, the GPU production order); None
+        keeps the case's."""
         self.lib = load(check_bounds)
         self.case = case
         fld = fields if fields is not None else case.initial_fields()
         f = fld.to_c()   # pointers into fld's arrays: fld must outlive the call
-        self.o = self.lib.gfo_create(C.byref(case.grid), C.byref(case.params), C.byref(f))
+        prm = abi.GfmParams.from_buffer_copy(case.params)
+        if adi_mode is not None:
+            prm.adi_mode = adi_mode
+        self.o = self.lib.gfo_create(C.byref(case.grid), C.byref(prm), C.byref(f))
         del fld
         if not self.o:
             raise RuntimeError("gfo_create failed")

@@ -29,12 +29,8 @@ def test_march_matches_oracle_adlbl3(cls):
     g.close()
 
 
-@pytest.mark.parametrize("fused", ["0", "1"])
 @pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-10), (abi.GFM_PREC_MIXED, 1e-4)])
-def test_redblack_converges_to_manufactured_solution(prec, tol, fused, monkeypatch):
-    # both red-black forms: segmented passes on the colour-split copy, and
-    # fused plane visits (GFM_RB_FUSED=1, read when the handle is created)
-    monkeypatch.setenv("GFM_RB_FUSED", fused)
+def test_redblack_converges_to_manufactured_solution(prec, tol):
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
     ib = case.ibcell()
@@ -44,6 +40,50 @@ def test_redblack_converges_to_manufactured_solution(prec, tol, fused, monkeypat
     err = np.abs(x - sol)[open_].max() / np.abs(sol[open_]).max()
     assert err < tol, err
     g.close()
+
+
+def _oracle_adlbl3(case, adi, ap, as6, bs, x0, rng, nim):
+    o = Oracle(case, adi_mode=adi)
+    xo = x0.copy()
+    ptrs = (abi._dp * 6)(*[abi.dptr(a) for a in as6])
+    pyoracle.load().gfo_adlbl3(o.o, abi.dptr(xo), abi.dptr(ap), ptrs, abi.dptr(bs), *rng, nim)
+    o.close()
+    return xo
+
+
+@pytest.mark.parametrize("cls", [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)])
+@pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-13), (abi.GFM_PREC_MIXED, 1e-5)])
+def test_redblack_matches_the_redblack_oracle(cls, prec, tol):
+    """Two sweeps in the red-black plane order against the oracle's ADLBL3 in
+    the same order, on each face class: the same iterate up to rounding
+    (FP64) or to FP32 rounding (mixed)."""
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+    xg = g.adlbl3(x0, ap, as6, bs, *rng, 2)
+    g.close()
+    xo = _oracle_adlbl3(case, abi.GFM_ADI_REDBLACK, ap, as6, bs, x0, rng, 2)
+    err = np.abs(xg - xo)[open_].max() / np.abs(xo[open_]).max()
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("adi", [abi.GFM_ADI_MARCH, abi.GFM_ADI_REDBLACK])
+def test_single_z_row_takes_the_y_pass_alone(adi):
+    """A solve range with one z-row (kb == ke): the reference's ADLZ copies the
+    first y-line pass into XT and leaves the plane (Adlbl3.f90:124-130)."""
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
+    ib0, ie, jb, je, kb, ke = rng
+    one = (ib0, ie, jb, je, kb + 6, kb + 6)
+    g = GpuSolver(case, adi_mode=adi)
+    xg = g.adlbl3(x0, ap, as6, bs, *one, 2)
+    g.close()
+    xo = _oracle_adlbl3(case, adi, ap, as6, bs, x0, one, 2)
+    sel = np.zeros_like(open_)
+    sel[kb + 5, jb - 1:je:2, ib0 - 1:ie:2] = True
+    sel &= open_
+    assert np.abs(xg - xo)[sel].max() / np.abs(xo[sel]).max() < 1e-13
+    assert np.array_equal(xg[~sel], x0[~sel])
 
 
 @pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])

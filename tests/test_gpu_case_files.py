@@ -31,7 +31,7 @@ def case_dir(tmp_path_factory):
 def pair(case, n, adi=abi.GFM_ADI_MARCH, prec=abi.GFM_PREC_FP64):
     g = GpuSolver(case, adi_mode=adi, precision=prec)
     g.start()
-    o = Oracle(case)
+    o = Oracle(case, adi_mode=adi)
     o.initsv()
     sg = [g.gflow(1)[0] for _ in range(n)]
     so = [o.gflow(1)[0] for _ in range(n)]
@@ -84,6 +84,19 @@ def test_fresh_start_mixed_matches_oracle(case_dir):
     assert max(v for k, v in err.items() if k not in ("u", "v", "w")) < MIXED_TOL, msg
     assert max(err["u"], err["v"], err["w"]) < 5e-4, msg
     assert sg[-1]["res_mass"] == pytest.approx(so[-1]["res_mass"], rel=1e-3)
+
+
+@pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, FP64_TOL), (abi.GFM_PREC_MIXED, MIXED_TOL)])
+def test_fresh_start_redblack_matches_the_redblack_oracle(case_dir, prec, tol):
+    """The benchmarked line order (red-black planes) against the oracle run in
+    the same plane order: one iteration of TC21 case 0041 from its files,
+    FP64 within 1e-9 and the mixed form within 1e-4 relative L2 per field."""
+    case = Case.from_files(case_dir, "0041")
+    sg, so, fg, fo, mask = pair(case, 1, abi.GFM_ADI_REDBLACK, prec)
+    err = field_errors(fg, fo, mask)
+    msg = " ".join(f"{k}={v:.3e}" for k, v in err.items())
+    assert max(err.values()) < tol, msg
+    assert sg[-1]["res_mass"] == pytest.approx(so[-1]["res_mass"], rel=tol * 10)
 
 
 def test_redblack_mixed_converges_like_the_reference_log(case_dir):

@@ -36,7 +36,7 @@ def run_pair(cfg, n, adi=abi.GFM_ADI_MARCH, prec=abi.GFM_PREC_FP64):
     case = Case(cfg)
     g = GpuSolver(case, adi_mode=adi, precision=prec)
     g.start()
-    o = Oracle(case)
+    o = Oracle(case, adi_mode=adi)
     o.initsv()
     sg, _ = g.gflow(n)
     so, _ = o.gflow(n)
@@ -86,6 +86,34 @@ def test_mixed_precision_tiny():
     err = field_errors(fg, fo, mask)
     worst = max(err.values())
     assert worst < MIXED_TOL, err
+    assert sg["res_mass"] == pytest.approx(so["res_mass"], rel=1e-3)
+
+
+# The benchmarked path: red-black plane order, against the oracle run in the
+# same plane order (the reference's ADLZ plane update, visited colour by
+# colour).  The two differ only in rounding: the GPU scales each row by a
+# stored reciprocal pivot and runs the line recurrences in segments.
+def test_fp64_redblack_tiny_20_iterations():
+    sg, so, fg, fo, mask = run_pair(configs.tiny_furnace(), 20, adi=abi.GFM_ADI_REDBLACK)
+    err = field_errors(fg, fo, mask)
+    assert max(err.values()) < FP64_TOL, err
+    assert sg["res_mass"] == pytest.approx(so["res_mass"], rel=FP64_TOL)
+
+
+def test_fp64_redblack_small_furnace_one_iteration():
+    sg, so, fg, fo, mask = run_pair(configs.small_furnace(), 1, adi=abi.GFM_ADI_REDBLACK)
+    err = field_errors(fg, fo, mask)
+    assert max(err.values()) < FP64_TOL, err
+    for k in ("res_mass", "res_mass_max", "p_resid", "gfex", "factor", "q_react", "q_exhaust", "q_conv_total", "tave"):
+        assert sg[k] == pytest.approx(so[k], rel=1e-9, abs=1e-300), k
+
+
+@pytest.mark.parametrize("cfg,n", [(configs.tiny_furnace(), 10), (configs.small_furnace(), 1)],
+                         ids=["tiny_10", "small_1"])
+def test_mixed_redblack_matches_the_redblack_oracle(cfg, n):
+    sg, so, fg, fo, mask = run_pair(cfg, n, adi=abi.GFM_ADI_REDBLACK, prec=abi.GFM_PREC_MIXED)
+    err = field_errors(fg, fo, mask)
+    assert max(err.values()) < MIXED_TOL, err
     assert sg["res_mass"] == pytest.approx(so["res_mass"], rel=1e-3)
 
 
