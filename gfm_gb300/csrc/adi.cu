@@ -907,8 +907,12 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
             nim = q.nim > nim ? q.nim : nim;
         }
         auto blocks = [](long long n, int t) { long long b = (n + t - 1) / t; return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b)); };
-        const int S = rb_segments<R>(max_n);
         const bool pdl = (rb_flags & kRbPdl) != 0;
+        if (rb_flags & kRbPlane) {
+            const int n = launch_rbp(g, sys, scr, nsys, st, pdl);
+            if (n > 0) return n;
+        }
+        const int S = rb_segments<R>(max_n);
         const bool avg2 = (rb_flags & kRbAvgInPass) != 0;            // pass L=2 averages pass L=1
         launch_k(pdl, k_rbs_in<R>, dim3(blocks(max_class, 256), nsys), 256, 0, st, g, rb);
         launch_k(pdl, k_rbs_factor<R>, dim3(blocks(max_lines, 128), nsys), 128, 0, st, g, rb);
@@ -934,7 +938,7 @@ int prepare_line_solver() {
                                          (int)kMarchMaxSmem) == cudaSuccess &&
                     cudaFuncSetAttribute(k_adlbl3_march<double, 4, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kMarchMaxSmem) == cudaSuccess;
-    return ok ? GFM_OK : GFM_E_CUDA;
+    return ok ? prepare_rbp() : GFM_E_CUDA;
 }
 
 template <typename R>

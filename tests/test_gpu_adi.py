@@ -51,12 +51,16 @@ def _oracle_adlbl3(case, adi, ap, as6, bs, x0, rng, nim):
     return xo
 
 
+@pytest.mark.parametrize("plane", ["1", "0"])
 @pytest.mark.parametrize("cls", [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)])
 @pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-13), (abi.GFM_PREC_MIXED, 1e-5)])
-def test_redblack_matches_the_redblack_oracle(cls, prec, tol):
+def test_redblack_matches_the_redblack_oracle(cls, prec, tol, plane, monkeypatch):
     """Two sweeps in the red-black plane order against the oracle's ADLBL3 in
     the same order, on each face class: the same iterate up to rounding
-    (FP64) or to FP32 rounding (mixed)."""
+    (FP64) or to FP32 rounding (mixed).  Both forms of the order: one CTA per
+    plane visit (default), and the segmented colour passes (GFM_RB_PLANE=0,
+    read when the handle is created)."""
+    monkeypatch.setenv("GFM_RB_PLANE", plane)
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
     g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
@@ -67,10 +71,12 @@ def test_redblack_matches_the_redblack_oracle(cls, prec, tol):
     assert err < tol, err
 
 
-@pytest.mark.parametrize("adi", [abi.GFM_ADI_MARCH, abi.GFM_ADI_REDBLACK])
-def test_single_z_row_takes_the_y_pass_alone(adi):
+@pytest.mark.parametrize("adi,plane", [(abi.GFM_ADI_MARCH, "1"), (abi.GFM_ADI_REDBLACK, "1"),
+                                       (abi.GFM_ADI_REDBLACK, "0")])
+def test_single_z_row_takes_the_y_pass_alone(adi, plane, monkeypatch):
     """A solve range with one z-row (kb == ke): the reference's ADLZ copies the
     first y-line pass into XT and leaves the plane (Adlbl3.f90:124-130)."""
+    monkeypatch.setenv("GFM_RB_PLANE", plane)
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
     ib0, ie, jb, je, kb, ke = rng
@@ -89,10 +95,11 @@ def test_single_z_row_takes_the_y_pass_alone(adi):
 @pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])
 @pytest.mark.parametrize("cls", [(0, 0, 0), (0, 1, 1)])
 def test_redblack_launch_forms_agree_bit_for_bit(prec, cls, monkeypatch):
-    """Pass L=2 averaging the pass L=1 results where it reads them (default)
-    and the separate averaging launch compute the same values in the same
-    order, with and without programmatic dependent launch: identical
-    iterates."""
+    """Segmented colour passes (GFM_RB_PLANE=0): pass L=2 averaging the pass
+    L=1 results where it reads them (default) and the separate averaging
+    launch compute the same values in the same order, with and without
+    programmatic dependent launch: identical iterates."""
+    monkeypatch.setenv("GFM_RB_PLANE", "0")
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
     out = []
@@ -104,3 +111,19 @@ def test_redblack_launch_forms_agree_bit_for_bit(prec, cls, monkeypatch):
         g.close()
     for o in out[1:]:
         assert np.array_equal(o, out[0])
+
+
+@pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])
+def test_plane_visit_with_and_without_dependent_launch(prec, monkeypatch):
+    """The plane-visit form gives identical iterates with and without
+    programmatic dependent launch of its kernels."""
+    monkeypatch.setenv("GFM_RB_PLANE", "1")
+    case = Case(configs.small_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case, (0, 1, 1))
+    out = []
+    for pdl in ("1", "0"):
+        monkeypatch.setenv("GFM_PDL", pdl)
+        g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+        out.append(g.adlbl3(x0, ap, as6, bs, *rng, 5))
+        g.close()
+    assert np.array_equal(out[0], out[1])
