@@ -8,18 +8,21 @@
 //   XP  the unknown with a one-point border on every side, plane p of the
 //       class (I = IB + 2p, p = -1 .. npl) holding (nJ+2) x (nK+2) points,
 //       K fastest: element (p, jj, kk) at ((p+1)(nJ+2) + jj+1)(nK+2) + kk+1;
-//   YA, YB  the rows of the y-lines (I, *, K), K fastest within the plane
-//       ((p nJ + jj) nK + kk): YA = (AS21, AS31, AS32, 1/ALP), YB = (BS, AS11,
-//       AS12, PT) with the Thomas pivots of the line, ALP = AP - PT(prev) AS21,
-//       PT = AS22/ALP (ADLZY, Adlbl3.f90:147-181);
-//   ZA, ZP  the rows of the z-lines (I, J, *), J fastest ((p nK + kk) nJ + jj):
-//       ZA = (AS31, AS21, AS22, 1/ALP), ZP = PT with ALP = AP - PT(prev) AS31,
-//       PT = AS32/ALP (ADLYZ, Adlbl3.f90:187-221).
+//   YC, YX, YP  the rows of the y-lines (I, *, K), K fastest within the plane
+//       ((p nJ + jj) nK + kk): YC = (AS21, AS31, AS32, BS), YX = (AS11, AS12)
+//       and YP = (1/ALP, PT) with the Thomas pivots of the line,
+//       ALP = AP - PT(prev) AS21, PT = AS22/ALP (ADLZY, Adlbl3.f90:147-181);
+//   ZC, ZP  the rows of the z-lines (I, J, *), J fastest ((p nK + kk) nJ + jj):
+//       ZC = (AS31, AS21, AS22, -), ZP = (1/ALP, PT) with ALP = AP - PT(prev)
+//       AS31, PT = AS32/ALP (ADLYZ, Adlbl3.f90:187-221).
 //
 // The matrices do not change during the call, so the pivots are the values
 // every visit of the reference would form.  A row the reference copies
 // unchanged (|ALP| <= 1e-20 or a blocked cell) stores 1/ALP = 0 and PT = -0.0,
-// a value no other row stores.
+// a value no other row stores.  The coefficients are rewritten by a tiled
+// transpose (k_rbp_fill); the pivots by one thread per line walking its rows
+// (k_rbp_pivots), with the loads of the next rows in flight while the chain
+// runs over the current ones.
 //
 // A visit (k_rbp_visit) loads its plane of XP into shared memory, runs the
 // y-lines of pass L=1 (which also form the x-neighbour part of the right-hand
@@ -42,13 +45,17 @@ namespace gfm {
 namespace {
 
 template <typename R>
+struct __align__(2 * sizeof(R)) Pair { R x, y; };
+
+template <typename R>
 struct RbpBatch {
     Sys<R> sys[8];
     R* xp[8];
-    Quad<R>* ya[8];
-    Quad<R>* yb[8];
-    Quad<R>* za[8];
-    R* zp[8];
+    Quad<R>* yc[8];
+    Pair<R>* yx[8];
+    Pair<R>* yp[8];
+    Quad<R>* zc[8];
+    Pair<R>* zp[8];
     int nsys;
 };
 
@@ -120,19 +127,82 @@ __global__ void k_rbp_copy(GeoT<R> g, RbpBatch<R> b) {
 }
 
 // ---------------------------------------------------------------------------
-// Records and pivots of every line, once per call.  A thread walks one line
-// (plane p, fixed cross index) row by row, the pivot chain of ADLZY/ADLYZ;
-// lanes take 32 neighbouring planes, so the loads of the class arrays are
-// contiguous.  The records of one row go through a shared-memory tile and
-// leave with the cross index fastest, contiguous in the record layout.
-// Block 32 x 8: 32 planes x 8 lines; grid x over (plane tiles) x (line
-// tiles), y = system.  ZL: z-lines (rows along K, lines indexed by J), else
-// y-lines (rows along J, lines indexed by K).
+// The coefficients of the records (YC, YX of the y-lines; ZC of the z-lines),
+// once per call, through a 32-plane x 16-line tile in shared memory: read with
+// the plane index fastest (contiguous in the class arrays), written with the
+// line index fastest (contiguous in the records).  Block (32, 8); grid x over
+// (plane tiles) x (line tiles), y = row (J of a y-line record, K of a z-line
+// record), z = system.
 // ---------------------------------------------------------------------------
 template <typename R, bool ZL>
-__global__ void __launch_bounds__(256) k_rbp_factor(GeoT<R> g, RbpBatch<R> b) {
-    __shared__ Quad<R> ta[2][32][9];
-    __shared__ Quad<R> tb[2][32][9];
+__global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b) {
+    constexpr int NF = ZL ? 3 : 6;
+    __shared__ R tile[NF][16][33];
+    pdl_wait();
+    pdl_trigger();
+    const int e = blockIdx.z;
+    const Sys<R>& s = b.sys[e];
+    const PlaneDims d = dims_of(s);
+    const int nlines = ZL ? d.nJ : d.nK, nrows = ZL ? d.nK : d.nJ;
+    const int row = blockIdx.y;
+    if (row >= nrows) return;
+    const int ntp = (d.npl + 31) / 32;
+    const int p0 = (blockIdx.x % ntp) * 32, l0 = (blockIdx.x / ntp) * 16;
+    if (l0 >= nlines) return;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    // y-line record: AS21, AS31, AS32, BS, AS11, AS12; z-line record: AS31, AS21, AS22
+    const R* src[NF];
+    if (ZL) {
+        src[0] = s.as[4]; src[1] = s.as[2]; src[2] = s.as[3];
+    } else {
+        src[0] = s.as[2]; src[1] = s.as[4]; src[2] = s.as[5];
+        src[3 % NF] = s.bs; src[4 % NF] = s.as[0]; src[5 % NF] = s.as[1];
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int ll = ty + 8 * r, p = p0 + tx, l = l0 + ll;
+        if (p < d.npl && l < nlines) {
+            const int I = s.ib + 2 * p;
+            const int o = (int)(ZL ? pidx(g, I, s.jb + 2 * l, s.kb + 2 * row) : pidx(g, I, s.jb + 2 * row, s.kb + 2 * l));
+#pragma unroll
+            for (int f = 0; f < NF; ++f) tile[f][ll][tx] = src[f][o];
+        }
+    }
+    __syncthreads();
+    const int tid = ty * 32 + tx;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        const int idx = tid + 256 * r;
+        const int ll = idx & 15, pl = idx >> 4;
+        const int p = p0 + pl, l = l0 + ll;
+        if (p < d.npl && l < nlines) {
+            if (ZL) {
+                b.zc[e][(p * d.nK + row) * d.nJ + l] = Quad<R>{tile[0][ll][pl], tile[1][ll][pl], tile[2][ll][pl], R(0)};
+            } else {
+                const int q = (p * d.nJ + row) * d.nK + l;
+                b.yc[e][q] = Quad<R>{tile[0][ll][pl], tile[1][ll][pl], tile[2][ll][pl], tile[3 % NF][ll][pl]};
+                b.yx[e][q] = Pair<R>{tile[4 % NF][ll][pl], tile[5 % NF][ll][pl]};
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pivots of every line, once per call: a thread walks one line (plane p, a
+// fixed cross index) row by row through the pivot chain of ADLZY/ADLYZ.
+// Lanes take 32 neighbouring planes, so each row's loads are contiguous in
+// the class arrays; the rows are taken kPivRows at a time, the loads of the
+// next batch issued before the chain runs over the current one.  A batch's
+// pivots leave through a tile in shared memory with the line index fastest,
+// contiguous in the records.  Block (32, 8): 32 planes x 8 lines; grid x over
+// (plane tiles) x (line tiles), y = system.  ZL: z-lines (rows along K, lines
+// indexed by J), else y-lines (rows along J, lines indexed by K).
+// ---------------------------------------------------------------------------
+constexpr int kPivRows = 8;
+template <typename R, bool ZL>
+__global__ void __launch_bounds__(256) k_rbp_pivots(GeoT<R> g, RbpBatch<R> b) {
+    constexpr int C = kPivRows;
+    __shared__ Pair<R> tile[C][8][33];
     pdl_wait();
     pdl_trigger();
     const int e = blockIdx.y;
@@ -145,65 +215,70 @@ __global__ void __launch_bounds__(256) k_rbp_factor(GeoT<R> g, RbpBatch<R> b) {
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int p = p0 + tx, l = l0 + ty;
     const bool act = p < d.npl && l < nlines;
-    // y-line (I,*,K): sub AS21 = as[2], next AS22 = as[3], across AS31/AS32 = as[4]/as[5]
-    // z-line (I,J,*): sub AS31 = as[4], next AS32 = as[5], across AS21/AS22 = as[2]/as[3]
+    // y-line (I,*,K): sub AS21 = as[2], next AS22 = as[3]; z-line (I,J,*): sub AS31 = as[4], next AS32 = as[5]
     const R* __restrict__ a_sub = s.as[ZL ? 4 : 2];
     const R* __restrict__ a_next = s.as[ZL ? 5 : 3];
-    const R* __restrict__ a_c0 = s.as[ZL ? 2 : 4];
-    const R* __restrict__ a_c1 = s.as[ZL ? 3 : 5];
+    const R* __restrict__ a_p = s.ap;
+    const int8_t* __restrict__ ibc = g.ib;
     const int I = s.ib + 2 * p;
     const int ostep = ZL ? (int)(pidx(g, 0, 0, 2) - pidx(g, 0, 0, 0)) : (int)(pidx(g, 0, 2, 0) - pidx(g, 0, 0, 0));
     const int o0 = act ? (int)(ZL ? pidx(g, I, s.jb + 2 * l, s.kb) : pidx(g, I, s.jb, s.kb + 2 * l)) : 0;
-    // writer side: thread (tx, ty) -> plane p0 + (tid / 8), line l0 + (tid % 8)
     const int tid = ty * 32 + tx;
-    const int wp = p0 + (tid >> 3), wl = l0 + (tid & 7);
-    const bool wact = wp < d.npl && wl < nlines;
+    R cap[C], csub[C], cnxt[C];
+    bool cblk[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) {
+        if (act && c < nrows) {
+            const int o = o0 + c * ostep;
+            cap[c] = a_p[o]; csub[c] = a_sub[o]; cnxt[c] = a_next[o]; cblk[c] = ibc[o] >= 1;
+        }
+    }
     R pt_prev = R(0);
-    for (int r = 0; r < nrows; ++r) {
-        const int buf = r & 1;
-        if (act) {
-            const int o = o0 + r * ostep;
-            const R ap = s.ap[o], sub = a_sub[o], nxt = a_next[o];
-            const R c0 = a_c0[o], c1 = a_c1[o];
-            const bool blk = g.ib[o] >= 1;
-            const R alp = ap - pt_prev * sub;
-            Quad<R> A, B;
-            R ia, pt;
-            if (fabs(alp) <= R(1.0e-20) || blk) {
-                ia = R(0);
-                pt = -R(0);
-                pt_prev = R(0);
-            } else {
-                ia = R(1) / alp;
-                pt = nxt / alp + R(0);   // +0.0: no -0.0 here
-                pt_prev = pt;
+    for (int r0 = 0; r0 < nrows; r0 += C) {
+        R nap[C], nsub[C], nnxt[C];
+        bool nblk[C];
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            const int r = r0 + C + c;
+            if (act && r < nrows) {
+                const int o = o0 + r * ostep;
+                nap[c] = a_p[o]; nsub[c] = a_sub[o]; nnxt[c] = a_next[o]; nblk[c] = ibc[o] >= 1;
             }
-            if (ZL) {
-                A = Quad<R>{sub, c0, c1, ia};                      // (AS31, AS21, AS22, 1/ALP)
-                B = Quad<R>{pt, R(0), R(0), R(0)};
-            } else {
-                A = Quad<R>{sub, c0, c1, ia};                      // (AS21, AS31, AS32, 1/ALP)
-                B = Quad<R>{s.bs[o], s.as[0][o], s.as[1][o], pt};  // (BS, AS11, AS12, PT)
+        }
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            if (act && r0 + c < nrows) {
+                const R alp = cap[c] - pt_prev * csub[c];
+                R ia, pt;
+                if (fabs(alp) <= R(1.0e-20) || cblk[c]) {
+                    ia = R(0);
+                    pt = -R(0);
+                    pt_prev = R(0);
+                } else {
+                    ia = R(1) / alp;
+                    pt = cnxt[c] / alp + R(0);   // +0.0: no -0.0 here
+                    pt_prev = pt;
+                }
+                tile[c][ty][tx] = Pair<R>{ia, pt};
             }
-            ta[buf][tx][ty] = A;
-            tb[buf][tx][ty] = B;
         }
         __syncthreads();
-        if (wact) {
-            const Quad<R> A = ta[buf][tid >> 3][tid & 7];
-            const Quad<R> B = tb[buf][tid >> 3][tid & 7];
-            if (ZL) {
-                const int q = (wp * d.nK + r) * d.nJ + wl;
-                b.za[e][q] = A;
-                b.zp[e][q] = B.x;
-            } else {
-                const int q = (wp * d.nJ + r) * d.nK + wl;
-                b.ya[e][q] = A;
-                b.yb[e][q] = B;
+        // C rows x 8 lines x 32 planes, the line index fastest
+#pragma unroll
+        for (int i = 0; i < C; ++i) {
+            const int idx = tid + 256 * i;
+            const int ll = idx & 7, pl = (idx >> 3) & 31, c = idx >> 8;
+            const int pw = p0 + pl, lw = l0 + ll, rw = r0 + c;
+            if (pw < d.npl && lw < nlines && rw < nrows) {
+                if (ZL) b.zp[e][(pw * d.nK + rw) * d.nJ + lw] = tile[c][ll][pl];
+                else b.yp[e][(pw * d.nJ + rw) * d.nK + lw] = tile[c][ll][pl];
             }
         }
-        // the next row writes the other buffer; the barrier of that row
-        // orders this row's reads before the buffer is written again
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < C; ++c) {
+            cap[c] = nap[c]; csub[c] = nsub[c]; cnxt[c] = nnxt[c]; cblk[c] = nblk[c];
+        }
     }
 }
 
@@ -248,34 +323,36 @@ __device__ __forceinline__ void rbp_pass(const RbpBatch<R>& b, int e, const Plan
         if (i < cnt) {
             const int row = e0 + i;
             const int c = c0 + row * rstep;
-            R bx, pt;
+            // A = (AS_sub, AS_across-, AS_across+, -), W = (1/ALP, PT)
+            R bx;
             Quad<R> A;
+            Pair<R> W;
             if (ZL) {
                 const int q = (p * d.nK + row) * d.nJ + line;
-                A = b.za[e][q];
-                pt = b.zp[e][q];
+                A = b.zc[e][q];
+                W = b.zp[e][q];
                 bx = bxs[bx0 + row * bstep];
             } else {
                 const int q = (p * d.nJ + row) * d.nK + line;
-                A = b.ya[e][q];
-                const Quad<R> B = b.yb[e][q];
-                pt = B.w;
+                A = b.yc[e][q];
+                W = b.yp[e][q];
                 if (FIRST) {
+                    const Pair<R> X = b.yx[e][q];
                     const R* __restrict__ xp = b.xp[e];
                     const R xm = xp[xp_index(d, p - 1, row, line)];
                     const R xq = xp[xp_index(d, p + 1, row, line)];
-                    bx = (B.x + B.z * xq) + B.y * xm;   // BS + AS12 XT(I+2) + AS11 XT(I-2)
+                    bx = (A.w + X.y * xq) + X.x * xm;   // BS + AS12 XT(I+2) + AS11 XT(I-2)
                     bxs[bx0 + row * bstep] = bx;
                 } else {
                     bx = bxs[bx0 + row * bstep];
                 }
             }
             // y: + AS32 XT(K+2) + AS31 XT(K-2); z: + AS22 XT(J+2) + AS21 XT(J-2)
-            const R v = A.w * ((bx + A.z * src[c + across]) + A.y * src[c - across]);
-            const bool cp = rbp_copy(pt);
+            const R v = W.x * ((bx + A.z * src[c + across]) + A.y * src[c - across]);
+            const bool cp = rbp_copy(W.y);
             rr[i] = cp ? src[c] : v;
-            al[i] = A.x * A.w;   // AS_sub/ALP; 0 on a copied row
-            pv[i] = pt;
+            al[i] = A.x * W.x;   // AS_sub/ALP; 0 on a copied row
+            pv[i] = W.y;
         }
     }
     // forward elimination of the segment from a zero start: q = r + a q(prev)
@@ -334,6 +411,21 @@ __host__ __device__ __forceinline__ size_t rbp_smem_bytes(const PlaneDims& d, in
     return (size_t)(2 * (d.nJ + 2) * PS + d.nJ * PS + 2 * nt) * sizeof(R);
 }
 
+// Asynchronous prefetch of [ptr, ptr + bytes) into L2 (whole 16-byte units
+// around the range; the arrays given here extend past every range asked for).
+__device__ __forceinline__ void l2_prefetch(const void* ptr, size_t bytes) {
+    unsigned long long a = (unsigned long long)ptr, end = a + bytes;
+    a &= ~15ull;
+    end = (end + 15) & ~15ull;
+    while (a < end) {
+        const unsigned n = (unsigned)((end - a) < (1ull << 20) ? (end - a) : (1ull << 20));
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
+        a += n;
+    }
+}
+
+constexpr int kLoadUnroll = 12;
+
 // One colour visit: every plane p = colour, colour + 2, .. of the call's
 // planes (I = IB + 2p), one CTA each.
 template <typename R, int NT, int M>
@@ -356,14 +448,39 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
     R* sA = bxs + d.nJ * PS;
     R* sB = sA + NT;
     R* __restrict__ xp = b.xp[e];
-    // the plane with its border; the border also into xb (the line ends)
     const int XJ = d.nK + 2, np = (d.nJ + 2) * XJ;
     const int base = (p + 1) * np;
-    for (int t = threadIdx.x; t < np; t += NT) {
-        const int jr = t / XJ, kr = t - jr * XJ;
-        const R v = xp[base + t];
-        xa[jr * PS + kr] = v;
-        if (jr == 0 || jr == d.nJ + 1 || kr == 0 || kr == d.nK + 1) xb[jr * PS + kr] = v;
+    if (threadIdx.x == 0) {
+        // everything the visit reads from global memory, on its way to L2
+        // while the plane is loaded: the records of the plane and the two
+        // neighbouring planes of XP
+        const size_t pc = (size_t)d.nJ * d.nK;
+        l2_prefetch(b.yc[e] + p * pc, pc * sizeof(Quad<R>));
+        l2_prefetch(b.yp[e] + p * pc, pc * sizeof(Pair<R>));
+        l2_prefetch(b.yx[e] + p * pc, pc * sizeof(Pair<R>));
+        l2_prefetch(xp + base - np, (size_t)np * sizeof(R));
+        l2_prefetch(xp + base + np, (size_t)np * sizeof(R));
+        l2_prefetch(b.zc[e] + p * pc, pc * sizeof(Quad<R>));
+        l2_prefetch(b.zp[e] + p * pc, pc * sizeof(Pair<R>));
+    }
+    // the plane with its border; the border also into xb (the line ends).
+    // kLoadUnroll points a thread, their loads issued together
+    for (int t0 = 0; t0 < np; t0 += kLoadUnroll * NT) {
+        R v[kLoadUnroll];
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u) {
+            const int t = t0 + u * NT + threadIdx.x;
+            if (t < np) v[u] = xp[base + t];
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadUnroll; ++u) {
+            const int t = t0 + u * NT + threadIdx.x;
+            if (t < np) {
+                const int jr = t / XJ, kr = t - jr * XJ;
+                xa[jr * PS + kr] = v[u];
+                if (jr == 0 || jr == d.nJ + 1 || kr == 0 || kr == d.nK + 1) xb[jr * PS + kr] = v[u];
+            }
+        }
     }
     __syncthreads();
     // pass L=1: y-lines into xb, then the z-lines averaged into it
@@ -404,37 +521,40 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     b.nsys = nsys;
     size_t smem = 0;
     int max_np = 0, max_nj = 0, max_nk = 0, nim = 0;
-    int ft_y = 0, ft_z = 0;
     for (int e = 0; e < nsys; ++e) {
         const PlaneDims d = dims_of(sys[e]);
         if (!rbp_pass_fits(d.nK, d.nJ) || !rbp_pass_fits(d.nJ, d.nK)) return 0;
         smem = std::max(smem, rbp_smem_bytes<R>(d, kRbpThreads));
         b.sys[e] = sys[e];
+        // the records in the scratch of the segmented form (2*CBH elements each)
+        const long long NH = 2LL * g.CBH;
         b.xp[e] = scr[e].xs;
-        b.ya[e] = scr[e].ya;
-        b.yb[e] = scr[e].yb;
-        b.za[e] = scr[e].za;
-        b.zp[e] = scr[e].x2;
+        b.yc[e] = scr[e].ya;
+        b.yx[e] = reinterpret_cast<Pair<R>*>(scr[e].yb);
+        b.yp[e] = reinterpret_cast<Pair<R>*>(scr[e].yb) + NH;
+        b.zc[e] = scr[e].za;
+        b.zp[e] = reinterpret_cast<Pair<R>*>(scr[e].zb);
         max_np = std::max(max_np, d.npl);
         max_nj = std::max(max_nj, d.nJ);
         max_nk = std::max(max_nk, d.nK);
         nim = std::max(nim, sys[e].nim);
-        ft_y = std::max(ft_y, ((d.npl + 31) / 32) * ((d.nK + 7) / 8));
-        ft_z = std::max(ft_z, ((d.npl + 31) / 32) * ((d.nJ + 7) / 8));
     }
     if (smem > kRbpMaxSmem) return 0;
     const unsigned tiles_in = (unsigned)(((max_np + 2 + 31) / 32) * ((max_nk + 2 + 31) / 32));
     const unsigned tiles_out = (unsigned)(((max_np + 31) / 32) * ((max_nk + 31) / 32));
+    const unsigned ptiles = (unsigned)((max_np + 31) / 32);
     launch_k(pdl, k_rbp_copy<R, true>, dim3(tiles_in, max_nj + 2, nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_factor<R, false>, dim3((unsigned)ft_y, nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_factor<R, true>, dim3((unsigned)ft_z, nsys), dim3(32, 8), 0, st, g, b);
+    launch_k(pdl, k_rbp_fill<R, false>, dim3(ptiles * ((max_nk + 15) / 16), max_nj, nsys), dim3(32, 8), 0, st, g, b);
+    launch_k(pdl, k_rbp_fill<R, true>, dim3(ptiles * ((max_nj + 15) / 16), max_nk, nsys), dim3(32, 8), 0, st, g, b);
+    launch_k(pdl, k_rbp_pivots<R, false>, dim3(ptiles * ((max_nk + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
+    launch_k(pdl, k_rbp_pivots<R, true>, dim3(ptiles * ((max_nj + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
     const dim3 gv((unsigned)((max_np + 1) / 2), nsys);
     for (int ns = 0; ns < nim; ++ns)
         for (int half = 0; half < 2; ++half)
             for (int colour = 0; colour < 2; ++colour)
                 launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
     launch_k(pdl, k_rbp_copy<R, false>, dim3(tiles_out, max_nj, nsys), dim3(32, 8), 0, st, g, b);
-    return 4 + 4 * nim;
+    return 6 + 4 * nim;
 }
 
 int prepare_rbp() {
