@@ -370,8 +370,20 @@ __device__ __forceinline__ void rbp_pass(const RbpBatch<R>& b, int e, const Plan
     sA[threadIdx.x] = cnt > 0 ? Pc : R(1);
     sB[threadIdx.x] = cnt > 0 ? qc : R(0);
     __syncthreads();
+    // carry into the segment: the maps of the segments before it, in order
+    // (their loads taken four at a time ahead of the chain)
     R qin = xlo;
-    for (int k = 0; k < seg && k < S; ++k) qin = sA[(k * G + grp) * 32 + lane] * qin + sB[(k * G + grp) * 32 + lane];
+    for (int k0 = 0; k0 < seg; k0 += 4) {
+        R a4[4], b4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = k0 + u;
+            if (k < seg) { a4[u] = sA[(k * G + grp) * 32 + lane]; b4[u] = sB[(k * G + grp) * 32 + lane]; }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k0 + u < seg) qin = a4[u] * qin + b4[u];
+    }
 #pragma unroll
     for (int i = 0; i < M; ++i)
         if (i < cnt) q[i] = q[i] + P[i] * qin;
@@ -391,7 +403,17 @@ __device__ __forceinline__ void rbp_pass(const RbpBatch<R>& b, int e, const Plan
     sB[threadIdx.x] = cnt > 0 ? xc : R(0);
     __syncthreads();
     R xin = xhi;
-    for (int k = S - 1; k > seg; --k) xin = sA[(k * G + grp) * 32 + lane] * xin + sB[(k * G + grp) * 32 + lane];
+    for (int k0 = S - 1; k0 > seg; k0 -= 4) {
+        R a4[4], b4[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int k = k0 - u;
+            if (k > seg) { a4[u] = sA[(k * G + grp) * 32 + lane]; b4[u] = sB[(k * G + grp) * 32 + lane]; }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (k0 - u > seg) xin = a4[u] * xin + b4[u];
+    }
 #pragma unroll
     for (int i = 0; i < M; ++i) {
         if (i < cnt) {
@@ -424,15 +446,11 @@ __device__ __forceinline__ void l2_prefetch(const void* ptr, size_t bytes) {
     }
 }
 
-constexpr int kLoadUnroll = 12;
-
 // One colour visit: every plane p = colour, colour + 2, .. of the call's
 // planes (I = IB + 2p), one CTA each.
 template <typename R, int NT, int M>
 __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, int sweep) {
     extern __shared__ __align__(16) unsigned char rbp_smem[];
-    pdl_wait();
-    pdl_trigger();
     const int e = blockIdx.y;
     const Sys<R>& s = b.sys[e];
     if (sweep >= s.nim) return;
@@ -440,6 +458,27 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
     const int npc = (d.npl - colour + 1) / 2;
     if ((int)blockIdx.x >= npc) return;
     const int p = colour + 2 * (int)blockIdx.x;
+    const int XJ = d.nK + 2, np = (d.nJ + 2) * XJ;
+    const int base = (p + 1) * np;
+    R* __restrict__ xp = b.xp[e];
+    if (threadIdx.x == 0) {
+        // everything the visit reads from global memory, on its way to L2:
+        // the records of the plane (fixed during the call, so this may run
+        // while the kernel before is finishing) and, after the wait, the
+        // plane and its two neighbours in XP
+        const size_t pc = (size_t)d.nJ * d.nK;
+        l2_prefetch(b.yc[e] + p * pc, pc * sizeof(Quad<R>));
+        l2_prefetch(b.yp[e] + p * pc, pc * sizeof(Pair<R>));
+        l2_prefetch(b.yx[e] + p * pc, pc * sizeof(Pair<R>));
+        l2_prefetch(b.zc[e] + p * pc, pc * sizeof(Quad<R>));
+        l2_prefetch(b.zp[e] + p * pc, pc * sizeof(Pair<R>));
+    }
+    pdl_wait();
+    pdl_trigger();
+    if (threadIdx.x == 0) {
+        l2_prefetch(xp + base - np, (size_t)np * sizeof(R));
+        l2_prefetch(xp + base + np, (size_t)np * sizeof(R));
+    }
     const int PS = rbp_pitch<R>(d.nK);
     const int PB = (d.nJ + 2) * PS;
     R* xa = reinterpret_cast<R*>(rbp_smem);
@@ -447,40 +486,32 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
     R* bxs = xb + PB;
     R* sA = bxs + d.nJ * PS;
     R* sB = sA + NT;
-    R* __restrict__ xp = b.xp[e];
-    const int XJ = d.nK + 2, np = (d.nJ + 2) * XJ;
-    const int base = (p + 1) * np;
-    if (threadIdx.x == 0) {
-        // everything the visit reads from global memory, on its way to L2
-        // while the plane is loaded: the records of the plane and the two
-        // neighbouring planes of XP
-        const size_t pc = (size_t)d.nJ * d.nK;
-        l2_prefetch(b.yc[e] + p * pc, pc * sizeof(Quad<R>));
-        l2_prefetch(b.yp[e] + p * pc, pc * sizeof(Pair<R>));
-        l2_prefetch(b.yx[e] + p * pc, pc * sizeof(Pair<R>));
-        l2_prefetch(xp + base - np, (size_t)np * sizeof(R));
-        l2_prefetch(xp + base + np, (size_t)np * sizeof(R));
-        l2_prefetch(b.zc[e] + p * pc, pc * sizeof(Quad<R>));
-        l2_prefetch(b.zp[e] + p * pc, pc * sizeof(Pair<R>));
-    }
-    // the plane with its border; the border also into xb (the line ends).
-    // kLoadUnroll points a thread, their loads issued together
-    for (int t0 = 0; t0 < np; t0 += kLoadUnroll * NT) {
-        R v[kLoadUnroll];
+    // the plane with its border, two J rows of 128 points a warp at a time
+    // (their loads issued together); the border also into xb (the line ends)
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        constexpr int NW = NT / 32;
+        for (int j0 = 2 * warp; j0 < d.nJ + 2; j0 += 2 * NW)
+            for (int k0 = 0; k0 < XJ; k0 += 128) {
+                R v[2][4];
 #pragma unroll
-        for (int u = 0; u < kLoadUnroll; ++u) {
-            const int t = t0 + u * NT + threadIdx.x;
-            if (t < np) v[u] = xp[base + t];
-        }
+                for (int a = 0; a < 2; ++a)
 #pragma unroll
-        for (int u = 0; u < kLoadUnroll; ++u) {
-            const int t = t0 + u * NT + threadIdx.x;
-            if (t < np) {
-                const int jr = t / XJ, kr = t - jr * XJ;
-                xa[jr * PS + kr] = v[u];
-                if (jr == 0 || jr == d.nJ + 1 || kr == 0 || kr == d.nK + 1) xb[jr * PS + kr] = v[u];
+                    for (int u = 0; u < 4; ++u) {
+                        const int jr = j0 + a, kr = k0 + lane + 32 * u;
+                        if (jr < d.nJ + 2 && kr < XJ) v[a][u] = xp[base + jr * XJ + kr];
+                    }
+#pragma unroll
+                for (int a = 0; a < 2; ++a)
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int jr = j0 + a, kr = k0 + lane + 32 * u;
+                        if (jr < d.nJ + 2 && kr < XJ) {
+                            xa[jr * PS + kr] = v[a][u];
+                            if (jr == 0 || jr == d.nJ + 1 || kr == 0 || kr == d.nK + 1) xb[jr * PS + kr] = v[a][u];
+                        }
+                    }
             }
-        }
     }
     __syncthreads();
     // pass L=1: y-lines into xb, then the z-lines averaged into it
@@ -494,10 +525,8 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
         rbp_pass<R, M, true, false>(b, e, d, p, PS, xb, xa, bxs, sA, sB);
     }
     const R* out = one_row ? xb : xa;
-    for (int t = threadIdx.x; t < d.nJ * d.nK; t += NT) {
-        const int jj = t / d.nK, kk = t - jj * d.nK;
-        xp[xp_index(d, p, jj, kk)] = out[(jj + 1) * PS + kk + 1];
-    }
+    for (int jj = threadIdx.x >> 5; jj < d.nJ; jj += NT / 32)
+        for (int kk = threadIdx.x & 31; kk < d.nK; kk += 32) xp[xp_index(d, p, jj, kk)] = out[(jj + 1) * PS + kk + 1];
 }
 
 constexpr int kRbpM = 8;            // rows of a segment held in registers
