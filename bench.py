@@ -207,40 +207,78 @@ def time_to_residual(case, adi, prec, thresh: float, max_iter: int, lp=None, fie
 
 
 TTR_THRESHOLD = 1.0e-3
+TTR_SEEDS = (20261203, 11, 12, 13)
 TTR_REASON = ("res_mass <= 1e-5 is not reached by the method on these cases: the mass residual plateaus near 1e-3 "
-              "on the 48x24x16 furnace and 2-7e-4 at 192x96x64 with the exit factor oscillating, as the reference's "
-              "own logs plateau (convg0041c.plt ends at 1.3e-4); the time to the plateau threshold 1e-3 is reported")
+              "with the exit factor oscillating, as the reference's own logs plateau (convg0041c.plt ends at "
+              "1.3e-4); the time to the plateau threshold 1e-3 is reported")
+TTR_NOTE = ("the iteration is chaotic at the plateau: a run can settle instead with the exit factor held at its "
+            "0.8 bound and res_mass near 1.4e-3, whatever the arithmetic (seen in FP64 and in both forms of the "
+            "mixed line solver); so the time is taken on four seeded furnaces (inlet-velocity jitter and initial "
+            "noise from the seed) and the median over the runs that reached the threshold is reported with the "
+            "count")
+
+
+def _median(v):
+    v = sorted(v)
+    return None if not v else (v[len(v) // 2] if len(v) % 2 else 0.5 * (v[len(v) // 2 - 1] + v[len(v) // 2]))
 
 
 def time_to_residual_leg(case, adi, args) -> tuple:
     """Time from the fresh start to res_mass < 1e-3 for the plain FP64 path,
     the mixed path and the mixed path with the learned p' guess (trained here
-    on seeded variants of the 48x24x16 furnace), each with the error of every
-    reported field at the state where it stopped, against the plain FP64
-    path's (the FP64 oracle's arithmetic, checked against it at 1e-9 per
-    iteration)."""
-    from gfm_gb300 import abi
+    on seeded variants of the 48x24x16 furnace), on four seeded 192x96x64
+    furnaces; each run carries the error of every reported field where it
+    stopped against the plain FP64 path's run of the same seed (the FP64
+    oracle's arithmetic, checked against it at 1e-9 per iteration)."""
+    from gfm_gb300 import Case, abi, configs
     thr = args.ttr or TTR_THRESHOLD
-    ttr = {"threshold": thr, "why_not_1e-5": TTR_REASON,
-           "field_error_reference": "the plain FP64 GPU path's fields where it stopped"}
-    f64, fmix, flp = [], [], []
-    ttr["fp64"] = time_to_residual(case, adi, abi.GFM_PREC_FP64, thr, args.ttr_max, fields_out=f64)
-    ttr["mixed"] = time_to_residual(case, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max, fields_out=fmix)
-    ttr["mixed"]["field_error"] = field_errors(case, fmix[0], f64[0])
-    ttr["mixed_vs_fp64_speedup"] = ttr["fp64"]["seconds"] / ttr["mixed"]["seconds"]
+    lp = None
     learned = None
     if not args.no_learned:
         from gfm_gb300.lp import train_default
         t0 = time.perf_counter()
         log = []
         lp = train_default((case.mp // 2 - 2, case.np // 2 - 2, case.lp // 2 - 2), log=log, steps=args.lp_steps)
-        train_s = time.perf_counter() - t0
-        run = time_to_residual(case, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max, lp=lp, fields_out=flp)
-        run["field_error"] = field_errors(case, flp[0], f64[0])
+        learned = {"threshold": thr, "train_seconds": time.perf_counter() - t0, "training": log, "runs": []}
+    runs = {"fp64": [], "mixed": []}
+    for seed in TTR_SEEDS:
+        c = Case(configs.large_furnace(seed=seed))
+        f64, fmix = [], []
+        r64 = time_to_residual(c, adi, abi.GFM_PREC_FP64, thr, args.ttr_max, fields_out=f64)
+        rmx = time_to_residual(c, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max, fields_out=fmix)
+        rmx["field_error_vs_fp64"] = field_errors(c, fmix[0], f64[0])
+        for r in (r64, rmx):
+            r["seed"] = seed
+        runs["fp64"].append(r64)
+        runs["mixed"].append(rmx)
+        if lp is not None:
+            flp = []
+            rlp = time_to_residual(c, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max, lp=lp, fields_out=flp)
+            rlp["field_error_vs_fp64"] = field_errors(c, flp[0], f64[0])
+            rlp["seed"] = seed
+            learned["runs"].append(rlp)
+    if lp is not None:
         lp.close()
-        learned = {"threshold": thr, "train_seconds": train_s, "training": log, "plain": ttr["mixed"],
-                   "learned": run, "speedup_vs_plain_mixed": ttr["mixed"]["seconds"] / run["seconds"],
-                   "speedup_vs_fp64": ttr["fp64"]["seconds"] / run["seconds"]}
+
+    def summary(rs):
+        ok = [r for r in rs if r["reached"]]
+        return {"reached": f"{len(ok)} of {len(rs)}", "median_seconds": _median([r["seconds"] for r in ok]),
+                "median_iterations": _median([r["iterations"] for r in ok])}
+
+    ttr = {"threshold": thr, "why_not_1e-5": TTR_REASON, "seeds": list(TTR_SEEDS), "note": TTR_NOTE,
+           "max_iterations": args.ttr_max, "fp64": summary(runs["fp64"]), "mixed": summary(runs["mixed"]),
+           "runs": runs}
+    if ttr["fp64"]["median_seconds"] and ttr["mixed"]["median_seconds"]:
+        ttr["mixed_vs_fp64_speedup"] = ttr["fp64"]["median_seconds"] / ttr["mixed"]["median_seconds"]
+    if learned is not None:
+        learned["learned"] = summary(learned["runs"])
+        learned["plain_mixed"] = ttr["mixed"]
+        lm = learned["learned"]["median_seconds"]
+        if lm:
+            if ttr["mixed"]["median_seconds"]:
+                learned["speedup_vs_plain_mixed"] = ttr["mixed"]["median_seconds"] / lm
+            if ttr["fp64"]["median_seconds"]:
+                learned["speedup_vs_fp64"] = ttr["fp64"]["median_seconds"] / lm
     return ttr, learned
 
 
@@ -698,7 +736,7 @@ def main():
     ap.add_argument("--no-ttr", action="store_true", help="skip the time-to-residual and learned p' legs")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned p' leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched furnace-variant leg")
-    ap.add_argument("--ttr-max", type=int, default=3000)
+    ap.add_argument("--ttr-max", type=int, default=1000)
     ap.add_argument("--batched", action="store_true",
                     help="run the batched furnace-variant workload instead of the 192x96x64 furnace")
     ap.add_argument("--batch", type=int, default=64)
