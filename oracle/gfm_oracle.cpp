@@ -2548,3 +2548,398 @@ double gfo_enth_to_t(const double* y, double h_norm, double t_guess_norm) {
 void gfo_conc(double* y) { conc(Y9{y, 1}); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Start-up of the synthetic furnace, restated for the oracle so that its runs
+// (the reference arm of the benchmark among them) need nothing from the
+// product library: GRID3's coordinate lines and cell map with the
+// 27-neighbour propagation (Grid3.f90:31-280), the SETUP constants
+// (Setup.f90:542-731), SBC's inlet states with the SBC1/SBC3 face values and
+// the outlet composition (Sbc.f90:57-388, 491-576), gen_initial_guess
+// (Initsv.f90:97-162), the wall patches of the convective sink
+// (Qwall.f90:395-513) and the kinetics table (Setup.f90:858-888).  The
+// furnace itself (a box, inlets on x=0 snapped to whole cells with the
+// velocity rescaled to keep the mass flow, a flue on x=lx, seeded jitter and
+// noise) is the benchmark's synthetic stand-in for a case directory; its
+// conventions are the generator's and are the same here.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct OCase {
+    int mp = 0, np = 0, lp = 0;
+    vec x, dx, r, dr, rs, z, dz;
+    std::vector<int16_t> ib;
+    std::vector<int16_t> b_typ, b_i, b_j, b_k, b_orient, b_direct;
+    vec b_t, rtim, delrt, hrt, delr, timed, hrd, wl, akl0;
+    vec p, t, dnst, theta, tmu, gama, crate, hrate, bs_hprev, ug, gf, qa, qe, t_surf_prev;
+    long at(int i, int j, int k) const { return (i - 1) + (long)mp * ((j - 1) + (long)np * (k - 1)); }
+    long n() const { return (long)mp * np * lp; }
+};
+
+uint64_t oc_mix64(uint64_t x) {   // splitmix64 finaliser: the generator's per-cell noise
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+double oc_noise(uint64_t seed, uint64_t idx, uint64_t comp) {   // uniform on [-1, 1)
+    uint64_t h = oc_mix64(seed ^ oc_mix64(idx * 16 + comp));
+    return ((double)(h >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;
+}
+
+// GRID3 coordinate line (Grid3.f90:79-109) of a uniform grid file: X(1..3) =
+// 0, then DEL added I2-I1 times up to X(N-1) = length, X(N) = X(N-1),
+// DX(I) = X(I+1) - X(I-1) inside, 0 at both ends.
+void oc_line(int n, double len, vec& x, vec& dx) {
+    x.assign(n, 0.0);
+    dx.assign(n, 0.0);
+    const int i1 = 3, i2 = n - 1;
+    const double del = (len - x[i1 - 1]) / (i2 - i1);
+    for (int i = i1 + 1; i <= i2; ++i) x[i - 1] = x[i - 2] + del;
+    x[n - 1] = x[n - 2];
+    for (int i = 2; i <= n - 1; ++i) dx[i - 1] = x[i] - x[i - 2];
+}
+
+// the generator's opening on a line of ncell cells of width h: a run of whole
+// cells, count = round((b-a)/h) at least 1, centred on the opening
+void oc_snap(double a, double b, double h, int ncell, int& first, int& count) {
+    count = (int)std::lround((b - a) / h);
+    if (count < 1) count = 1;
+    if (count > ncell) count = ncell;
+    first = (int)std::lround(0.5 * (a + b) / h - 0.5 * count) + 1;
+    if (first < 1) first = 1;
+    if (first + count - 1 > ncell) first = ncell - count + 1;
+}
+
+struct OInlet { int j1, j2, k1, k2; double u, t_k, yf, yox, yn2, yco2, yh2o; };
+
+}  // namespace
+
+extern "C" {
+
+int gfo_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* out) {
+    if (!sp || !kinetic_path || !out) return GFM_E_ARG;
+    std::memset(out, 0, sizeof *out);
+    if (sp->nx < 4 || sp->ny < 4 || sp->nz < 4 || sp->n_inlets < 1 || sp->n_inlets > 8 || sp->nwl < 1 || sp->nwl > 16)
+        return GFM_E_ARG;
+    OCase* c = new OCase;
+    OCase& s = *c;
+    const int mp = 2 * sp->nx + 4, np = 2 * sp->ny + 4, lp = 2 * sp->nz + 4;
+    s.mp = mp; s.np = np; s.lp = lp;
+    const long N = s.n();
+    oc_line(mp, sp->lx, s.x, s.dx);
+    oc_line(np, sp->ly, s.r, s.dr);
+    oc_line(lp, sp->lz, s.z, s.dz);
+    s.rs.assign(np, 1.0);   // cartesian (Grid3.f90:166)
+    auto IB = [&](int i, int j, int k) -> int16_t& { return s.ib[s.at(i, j, k)]; };
+
+    // cell map: walls (IBCELL 1) on the six faces of the box, inlets (2) on
+    // x=0, the flue (3) on x=lx, open cells (0) inside
+    s.ib.assign(N, 0);
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 2; i <= mp; i += 2)
+                if (i == 2 || i == mp || j == 2 || j == np || k == 2 || k == lp) IB(i, j, k) = 1;
+    const double hy = sp->ly / sp->ny, hz = sp->lz / sp->nz;
+    std::vector<OInlet> inl(sp->n_inlets);
+    for (int n = 0; n < sp->n_inlets; ++n) {
+        const gfm_inlet_spec& is = sp->inlets[n];
+        int fy, cy, fz, cz;
+        oc_snap(is.y0, is.y1, hy, sp->ny, fy, cy);
+        oc_snap(is.z0, is.z1, hz, sp->nz, fz, cz);
+        OInlet& b = inl[n];
+        b.j1 = 2 * fy + 2; b.j2 = 2 * (fy + cy - 1) + 2;
+        b.k1 = 2 * fz + 2; b.k2 = 2 * (fz + cz - 1) + 2;
+        const double jit = sp->inlet_jitter > 0 ? 1.0 + sp->inlet_jitter * oc_noise(sp->seed, 1000003ull + n, 7) : 1.0;
+        b.u = is.u_ms * ((is.y1 - is.y0) * (is.z1 - is.z0)) / (cy * hy * cz * hz) * jit;
+        b.t_k = is.t_k; b.yf = is.yf; b.yox = is.yo2; b.yn2 = is.yn2; b.yco2 = is.yco2; b.yh2o = is.yh2o;
+        for (int k = b.k1; k <= b.k2; k += 2)
+            for (int j = b.j1; j <= b.j2; j += 2) IB(2, j, k) = 2;
+    }
+    {
+        int fy, cy, fz, cz;
+        oc_snap(sp->exit_y0, sp->exit_y1, hy, sp->ny, fy, cy);
+        oc_snap(sp->exit_z0, sp->exit_z1, hz, sp->nz, fz, cz);
+        for (int k = 2 * fz + 2; k <= 2 * (fz + cz - 1) + 2; k += 2)
+            for (int j = 2 * fy + 2; j <= 2 * (fy + cy - 1) + 2; j += 2) IB(mp, j, k) = 3;
+    }
+    // NCELLS and the propagation of each closed cell's code onto its faces,
+    // edges and corners that are not walls (Grid3.f90:259-275)
+    int ncells = 0;
+    for (int i = 2; i <= mp; i += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int k = 2; k <= lp; k += 2) {
+                const int ibc1 = IB(i, j, k);
+                if (ibc1 <= 0) { ++ncells; continue; }
+                for (int i1 = i - 1; i1 <= i + 1; ++i1)
+                    for (int j1 = j - 1; j1 <= j + 1; ++j1)
+                        for (int k1 = k - 1; k1 <= k + 1; ++k1) {
+                            if (i1 > mp || j1 > np || k1 > lp) continue;
+                            if (IB(i1, j1, k1) != 1) IB(i1, j1, k1) = (int16_t)ibc1;
+                        }
+            }
+
+    // SETUP (Setup.f90:542-731); GMFR is the inlets' total mass flow, as the
+    // case-writing front end puts it in the &INPUT group
+    const double pg0 = sp->pg0 > 0 ? sp->pg0 : 1.01325e5;
+    const double RU = 8.3143e+3;
+    double gmfr = 0.0;
+    for (int n = 0; n < sp->n_inlets; ++n) {
+        const gfm_inlet_spec& is = sp->inlets[n];
+        const double w_in = ONE / (is.yf / WF + is.yco2 / WCO2 + is.yh2o / WH2O + is.yo2 / WO2 + is.yn2 / WN2);
+        const double rho = pg0 * w_in / (RU * is.t_k);
+        const int cy = (inl[n].j2 - inl[n].j1) / 2 + 1, cz = (inl[n].k2 - inl[n].k1) / 2 + 1;
+        gmfr += rho * std::fabs(inl[n].u) * (cy * hy) * (cz * hz);
+    }
+    gfm_params& P = out->params;
+    const double t0 = T0C, h_0 = H0C, area0 = 1.0, r0 = 1.0;
+    const double wt0 = 1.0 / (0.5 / 16.0426 + 0.0 / 44.0098 + 0.0 / 18.0152 + 0.49 / 31.9988 + 0.01 / 28.0134);
+    const double dnst0 = pg0 * wt0 / RU / t0;
+    const double ug0 = gmfr / dnst0 / area0;
+    const double gmu_ref = 2.6e-5 * std::pow(5.33e+2 / 2.98e+2, 0.0);
+    const double tk0 = 5.0e-2 * (ug0 * ug0), epsi0 = 1.0 * (tk0 * tk0);
+    const double reyg = 2.0 * dnst0 * ug0 * r0 / gmu_ref;
+    P.t0 = t0; P.h_0 = h_0; P.dnst0 = dnst0; P.ug0 = ug0; P.gmfr = gmfr; P.pg0 = pg0; P.r0 = r0;
+    P.reyg = reyg; P.reyg2 = reyg / 2.0;
+    P.epsr = tk0 / (ug0 * ug0);
+    P.taur = epsi0 * r0 / (tk0 * ug0);
+    P.eun = pg0 / (dnst0 * (ug0 * ug0));
+    P.qr0 = h_0 * dnst0 * ug0 / r0;
+    P.q0 = (sp->q0_jkg > 0 ? sp->q0_jkg : 2.42e6) / h_0;
+    P.tk0 = tk0;
+    P.gra[0] = 0.0 / ug0 / ug0 * r0; P.gra[1] = 0.0 / ug0 / ug0 * r0; P.gra[2] = -9.80621 / ug0 / ug0 * r0;
+    P.amu = 0.0; P.trdg = 298.15 / 5.0e+2; P.wt0 = wt0; P.stoich = 2.0 * 31.9988 / 16.0426;
+    P.cmu = 9.0e-2; P.ct1 = 1.44; P.ct2 = 1.92;
+    P.p_mx = 0.2; P.p_mn = -0.6; P.t_mx = 3.0e+3 / t0; P.t_mn = 2.0e+2 / 5.0e+2;
+    P.u_mx = 1.0e+3 / ug0; P.u_mn = -P.u_mx; P.f_mx = 1.5; P.f_mn = 0.8;
+    for (int i = 0; i < 21; ++i) { P.rf[i] = 0.7; P.rfl[i] = 0.6; }
+    P.rf[0] = P.rf[1] = P.rf[2] = sp->rf_uvw;
+    P.rf[17] = 0.6; P.rf[20] = 0.6;
+    P.rfl[0] = sp->rfl_species; P.rfl[1] = sp->rfl_species; P.rfl[2] = sp->rfl_h; P.rfl[3] = sp->rfl_k;
+    P.rfl[4] = sp->rfl_eps; P.rfl[5] = sp->rfl_species; P.rfl[6] = sp->rfl_species;
+    const double sig0[12] = {0.7, 0.7, 0.7, 1.0, 1.0, 0.7, 0.7, 0.7, 0.7, 0.7, 0.7, 0.7};
+    for (int i = 0; i < 12; ++i) P.sigma[i] = sig0[i];
+    P.sigma[3] = sp->sigma_k; P.sigma[4] = sp->sigma_eps;
+    for (int i = 0; i < 20; ++i) P.ntimesg[i] = i < 12 ? sp->ntimesg[i] : 2;
+    P.rf_hsource = sp->rf_hsource;
+    P.react = sp->react; P.turb = 1;
+    P.wall_sink = sp->wall_sink; P.h_g = sp->h_g;
+    P.rad_emission = sp->rad_emission; P.rad_qe_frequency = 10;
+    P.sig = 5.668e-8; P.ri = 1.0; P.hck = 1.439e-2;
+    P.bgcon = sp->bgcon; P.maxgi = sp->maxgi; P.adi_mode = sp->adi_mode; P.precision = sp->precision;
+
+    // fields at allocation (Setup.f90:747-779)
+    s.p.assign(N, 0.0); s.t.assign(N, 1.0); s.dnst.assign(N, 1.0); s.theta.assign(N, 1.0);
+    s.tmu.assign(N, 0.0); s.gama.assign(N, 0.0); s.crate.assign(N, 0.0); s.hrate.assign(N, 0.0);
+    s.bs_hprev.assign(N, 0.0); s.ug.assign(3 * N, 0.0); s.gf.assign(9 * N, 0.0);
+    const long ncell_arr = (long)(mp / 2) * (np / 2) * (lp / 2);
+    s.qa.assign(ncell_arr, 0.0); s.qe.assign(ncell_arr, 0.0);
+    s.t_surf_prev.assign((size_t)(mp / 2) * (np / 2), 0.0);
+    auto Y = [&](long a) { return Y9{&s.gf[a], N}; };
+    auto GF = [&](long a, int l) -> double& { return s.gf[a + (long)(l - 1) * N]; };
+    auto dnst_at = [&](long a) {   // dnst_calc (Prop.f90:187-198)
+        conc(Y(a));
+        const double temp = (ONE + s.p[a]) / s.t[a] * wmix(Y(a)) / P.wt0;
+        s.dnst[a] = fmax2(temp, small20);
+    };
+    auto ther_at = [&](long a) {   // THER (Prop.f90:130-154)
+        GF(a, IEPS) = fmax2(GF(a, IEPS), 1.0e-12);
+        s.tmu[a] = P.cmu * P.reyg * P.epsr / (TWO * P.taur) * (GF(a, IK) * GF(a, IK)) / GF(a, IEPS) * s.dnst[a];
+        s.gama[a] = TWO / P.reyg * (s.tmu[a] + std::pow(s.t[a] / P.trdg, P.amu));
+    };
+    auto tke_at = [&](long a) {    // TKE (Prop.f90:162-176)
+        const double g = s.ug[a] * s.ug[a] + s.ug[a + N] * s.ug[a + N] + s.ug[a + 2 * N] * s.ug[a + 2 * N];
+        GF(a, IK) = fmax2(g, 1.0e-6);
+        GF(a, IEPS) = GF(a, IK) * GF(a, IK);
+    };
+    auto t2h_at = [&](long a) { GF(a, IH) = T_to_enth(Y(a), s.t[a]); };
+
+    // SBC (Sbc.f90:57-269): inlet cells of each block, IU = 1 (x faces)
+    const double p_ref = 0.0 / pg0;
+    double fr_f = 0, fr_ox = 0, fr_n2 = 0, q_h_in = 0;
+    std::vector<char> done(N, 0);
+    for (const OInlet& b : inl) {
+        const double T_0 = b.t_k / t0, U_0 = b.u / ug0;
+        for (int j = b.j1; j <= b.j2; j += 2)
+            for (int k = b.k1; k <= b.k2; k += 2) {
+                const long a = s.at(2, j, k);
+                if (IB(2, j, k) != 2 || done[a]) continue;
+                done[a] = 1;
+                s.p[a] = p_ref;
+                s.t[a] = T_0;
+                GF(a, IYF) = b.yf; GF(a, IYCO2) = b.yco2; GF(a, IYH2O) = b.yh2o; GF(a, IYO2) = b.yox; GF(a, IYN2) = b.yn2;
+                dnst_at(a);
+                s.ug[a] = U_0; s.ug[a + N] = 0.0; s.ug[a + 2 * N] = 0.0;
+                tke_at(a);
+                ther_at(a);
+                t2h_at(a);
+                double g0 = s.theta[a] * s.dnst[a] * dnst0;
+                const double area = s.dr[j - 1] * s.rs[j - 1] * s.dz[k - 1] * area0;   // AREA_C(.,.,.,1)
+                g0 = g0 * std::fabs(U_0) * ug0 * area;
+                fr_f += g0 * GF(a, IYF);
+                fr_ox += g0 * GF(a, IYO2);
+                fr_n2 += g0 * GF(a, IYN2);
+                q_h_in += GF(a, IH) * h_0 * g0;
+            }
+        // SBC1 (Sbc.f90:391-486): the faces between a block's inlet cells
+        auto sbc1 = [&](long A, long B, long C, double f1) {
+            const double f2 = 1.0 - f1;
+            s.p[C] = f1 * s.p[A] + f2 * s.p[B];
+            s.t[C] = f1 * s.t[A] + f2 * s.t[B];
+            for (int l = 0; l < 9; ++l) {
+                if (l < 3) s.ug[C + l * N] = f1 * s.ug[A + l * N] + f2 * s.ug[B + l * N];
+                s.gf[C + l * N] = f1 * s.gf[A + l * N] + f2 * s.gf[B + l * N];
+            }
+            dnst_at(C);
+            s.theta[C] = f1 * s.theta[A] + f2 * s.theta[B];
+            s.tmu[C] = f1 * s.tmu[A] + f2 * s.tmu[B];
+            s.gama[C] = f1 * s.gama[A] + f2 * s.gama[B];
+        };
+        // SBC3 (Sbc.f90:491-522): copy onto the inlet's neighbouring face planes
+        auto sbc3 = [&](long A, long B) {
+            for (int l = 0; l < 3; ++l) s.ug[B + l * N] = s.ug[A + l * N];
+            s.p[B] = s.p[A]; s.t[B] = s.t[A];
+            for (int l = 0; l < 9; ++l) s.gf[B + l * N] = s.gf[A + l * N];
+            s.dnst[B] = s.dnst[A]; s.theta[B] = s.theta[A]; s.tmu[B] = s.tmu[A]; s.gama[B] = s.gama[A];
+        };
+        const int i = 2;   // IU = 1 block on the x=0 wall (Sbc.f90:179-206)
+        if (b.k2 > b.k1)
+            for (int k = b.k1 + 1; k <= b.k2 - 1; k += 2)
+                for (int j = b.j1; j <= b.j2; j += 2)
+                    sbc1(s.at(i, j, k + 1), s.at(i, j, k - 1), s.at(i, j, k), (s.z[k - 1] - s.z[k - 2]) / s.dz[k - 1]);
+        if (b.j2 > b.j1)
+            for (int j = b.j1 + 1; j <= b.j2 - 1; j += 2)
+                for (int k = b.k1; k <= b.k2; ++k)
+                    sbc1(s.at(i, j + 1, k), s.at(i, j - 1, k), s.at(i, j, k), (s.r[j - 1] - s.r[j - 2]) / s.dr[j - 1]);
+        for (int j = b.j1; j <= b.j2; ++j)
+            for (int k = b.k1; k <= b.k2; ++k) {
+                if (i < mp && IB(i + 1, j, k) == 2) sbc3(s.at(i, j, k), s.at(i + 1, j, k));
+                if (i > 2 && IB(i - 1, j, k) == 2) sbc3(s.at(i, j, k), s.at(i - 1, j, k));
+            }
+    }
+    const double gfin = fr_f + fr_ox + fr_n2;
+    if (!(gfin > 0.0)) { delete c; std::memset(out, 0, sizeof *out); return GFM_E_ARG; }
+    // est_out_mass_frac (Sbc.f90:566-576)
+    const double yn2_out = fr_n2 / gfin;
+    const double yh2o_out = (2 * fr_f * WH2O / WF) / gfin;
+    const double yco2_out = (fr_f * WCO2 / WF) / gfin;
+    const double yo2_out = (fr_ox - 2 * fr_f * WO2 / WF) / gfin;
+
+    // gen_initial_guess (Initsv.f90:97-162), with the generator's seeded
+    // perturbation of T and the species in the open cells
+    gfm_fields& F = out->fields;
+    F.factor = 1.0; F.fadj = 0.0;
+    const double T_init = sp->t_init_k / t0, amp = sp->noise_amp;
+    for (int i = 2; i <= mp; i += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int k = 2; k <= lp; k += 2) {
+                const int ibc = IB(i, j, k);
+                if (ibc == 2) continue;
+                const long a = s.at(i, j, k);
+                double nz5[5] = {0, 0, 0, 0, 0};
+                if (ibc == 0 && amp != 0.0)
+                    for (int q = 0; q < 5; ++q) nz5[q] = amp * oc_noise(sp->seed, (uint64_t)a, (uint64_t)q);
+                GF(a, IYF) = 0;
+                GF(a, IYO2) = yo2_out * (1.0 + nz5[1]);
+                GF(a, IYCO2) = yco2_out * (1.0 + nz5[2]);
+                GF(a, IYH2O) = yh2o_out * (1.0 + nz5[3]);
+                GF(a, IYN2) = yn2_out * (1.0 + nz5[4]);
+                if (ibc == 1) {
+                    s.t[a] = T_init;
+                    t2h_at(a);
+                    continue;
+                }
+                s.ug[a] = 0; s.ug[a + N] = 0; s.ug[a + 2 * N] = 0;
+                s.theta[a] = 1.0;
+                if (ibc != 4) s.t[a] = T_init * (1.0 + nz5[0]);
+                t2h_at(a);
+                tke_at(a);
+                dnst_at(a);
+                ther_at(a);
+            }
+
+    // wall patches (Qwall.f90:395-513): faces of closed cells next to an
+    // open one, x then y then z faces, b_T the fixed wall temperature
+    auto add_patch = [&](int typ, int ori, int dir, int i, int j, int k) {
+        s.b_typ.push_back((int16_t)typ); s.b_orient.push_back((int16_t)ori); s.b_direct.push_back((int16_t)dir);
+        s.b_i.push_back((int16_t)i); s.b_j.push_back((int16_t)j); s.b_k.push_back((int16_t)k);
+        s.b_t.push_back(sp->t_wall_k);
+    };
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 3; i <= mp - 1; i += 2) {
+                const int m = IB(i, j, k);
+                if (m < 1 || (IB(i - 1, j, k) > 0 && IB(i + 1, j, k) > 0)) continue;
+                add_patch(m, 1, IB(i + 1, j, k) == 0 ? 0 : 1, i, j, k);
+            }
+    for (int k = 2; k <= lp; k += 2)
+        for (int j = 3; j <= np - 1; j += 2)
+            for (int i = 2; i <= mp; i += 2) {
+                const int m = IB(i, j, k);
+                if (m < 1 || (IB(i, j - 1, k) > 0 && IB(i, j + 1, k) > 0)) continue;
+                add_patch(m, 2, IB(i, j + 1, k) == 0 ? 0 : 1, i, j, k);
+            }
+    for (int k = 3; k <= lp - 1; k += 2)
+        for (int j = 2; j <= np; j += 2)
+            for (int i = 2; i <= mp; i += 2) {
+                const int m = IB(i, j, k);
+                if (m < 1 || (IB(i, j, k - 1) > 0 && IB(i, j, k + 1) > 0)) continue;
+                add_patch(m, 3, IB(i, j, k + 1) == 0 ? 0 : 1, i, j, k);
+            }
+
+    // kinetics table (Setup.f90:858-888): two blocks of NR0 rows after a
+    // header line each; times scaled by 0.7, heat by CHRD/H_0/WF
+    const int nr0 = 100;
+    {
+        FILE* fp = std::fopen(kinetic_path, "r");
+        if (!fp) { delete c; std::memset(out, 0, sizeof *out); return GFM_E_IO; }
+        char line[512];
+        bool ok = std::fgets(line, sizeof line, fp) != nullptr;
+        const double chrd = 0.166;
+        s.rtim.resize(nr0); s.delrt.resize(nr0); s.hrt.resize(nr0);
+        s.delr.resize(nr0); s.timed.resize(nr0); s.hrd.resize(nr0);
+        for (int i = 0; ok && i < nr0; ++i) {
+            ok = std::fgets(line, sizeof line, fp) && std::sscanf(line, "%lf %lf %lf", &s.rtim[i], &s.delrt[i], &s.hrt[i]) == 3;
+            s.rtim[i] = s.rtim[i] * 0.7;
+            s.hrt[i] = chrd * s.hrt[i] / h_0 / WF;
+        }
+        ok = ok && std::fgets(line, sizeof line, fp) != nullptr;
+        for (int i = 0; ok && i < nr0; ++i) {
+            ok = std::fgets(line, sizeof line, fp) && std::sscanf(line, "%lf %lf %lf", &s.delr[i], &s.timed[i], &s.hrd[i]) == 3;
+            s.timed[i] = s.timed[i] * 0.7;
+            s.hrd[i] = chrd * s.hrd[i] / h_0 / WF;
+        }
+        std::fclose(fp);
+        if (!ok) { delete c; std::memset(out, 0, sizeof *out); return GFM_E_IO; }
+    }
+    for (int l = 0; l < sp->nwl; ++l) { s.wl.push_back(sp->wl_um[l] * 1.0e-6); s.akl0.push_back(sp->kappa[l]); }
+
+    gfm_grid& G = out->grid;
+    G.mp = mp; G.np = np; G.lp = lp;
+    G.x = s.x.data(); G.dx = s.dx.data(); G.r = s.r.data(); G.dr = s.dr.data(); G.rs = s.rs.data();
+    G.z = s.z.data(); G.dz = s.dz.data(); G.ibcell = s.ib.data(); G.ncells = ncells;
+    G.i_ref = 2; G.j_ref = inl[0].j1; G.k_ref = inl[0].k1; G.p_ref = p_ref;
+    G.b_cnt = (int)s.b_typ.size();
+    G.b_typ = s.b_typ.data(); G.b_i = s.b_i.data(); G.b_j = s.b_j.data(); G.b_k = s.b_k.data();
+    G.b_orient = s.b_orient.data(); G.b_direct = s.b_direct.data(); G.b_t = s.b_t.data();
+    G.nr0 = nr0;
+    G.rtim = s.rtim.data(); G.delrt = s.delrt.data(); G.hrt = s.hrt.data();
+    G.delr = s.delr.data(); G.timed = s.timed.data(); G.hrd = s.hrd.data();
+    G.nwl = sp->nwl; G.wl = s.wl.data(); G.akl0 = s.akl0.data();
+    F.p = s.p.data(); F.t = s.t.data(); F.dnst = s.dnst.data(); F.theta = s.theta.data();
+    F.tmu = s.tmu.data(); F.gama = s.gama.data(); F.crate = s.crate.data(); F.hrate = s.hrate.data();
+    F.bs_hprev = s.bs_hprev.data(); F.ug = s.ug.data(); F.gf = s.gf.data(); F.qa = s.qa.data(); F.qe = s.qe.data();
+    F.gfin0 = gfin / gmfr; F.q_h_in = q_h_in;
+    out->tail.mz = mp / 2; out->tail.nz = np / 2; out->tail.t_surf_prev = s.t_surf_prev.data();
+    out->tail.interval_rad = 100;
+    out->priv = c;
+    return GFM_OK;
+}
+
+void gfo_case_free(gfm_case* c) {
+    if (!c) return;
+    delete static_cast<OCase*>(c->priv);
+    std::memset(c, 0, sizeof *c);
+}
+
+}  // extern "C"

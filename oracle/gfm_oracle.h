@@ -52,6 +52,13 @@ double gfo_t_to_enth(const double *y, double t_norm);
 double gfo_enth_to_t(const double *y, double h_norm, double t_guess_norm);
 void   gfo_conc(double *y);
 
+/* The synthetic furnace of a case spec, built by the oracle's own start-up
+ * (GRID3, SETUP, SBC, gen_initial_guess, wall patches, kinetics table) into
+ * storage owned by *out; gfo_case_free releases it.  Same inputs and result
+ * as the product's gfm_case_build, made without it. */
+int   gfo_case_build(const gfm_case_spec *spec, const char *kinetic_path, gfm_case *out);
+void  gfo_case_free(gfm_case *c);
+
 #define GFO_STEP_WALLFN      1
 #define GFO_STEP_MOMASM      2
 #define GFO_STEP_PSOLVE      3

@@ -55,9 +55,34 @@ def load(check_bounds: bool = False) -> C.CDLL:
     lib.gfo_t_to_enth.argtypes = [dp, C.c_double]
     lib.gfo_enth_to_t.argtypes = [dp, C.c_double, C.c_double]
     lib.gfo_conc.argtypes = [dp]
+    lib.gfo_case_build.argtypes = [C.POINTER(abi.GfmCaseSpec), C.c_char_p, C.POINTER(abi.GfmCase)]
+    lib.gfo_case_free.argtypes = [C.POINTER(abi.GfmCase)]
     if not check_bounds:
         _lib = lib
     return lib
+
+
+class OracleCase(Case):
+    """A synthetic furnace built by the oracle's own start-up (gfo_case_build:
+    GRID3, SETUP, SBC, gen_initial_guess, wall patches, kinetics table) in
+    place of the product's gfm_case_build; the same interface as Case, and
+    nothing of the product library is loaded."""
+
+    def __init__(self, cfg, check_bounds: bool = False):
+        self.cfg = cfg
+        self.lib = load(check_bounds)
+        self.c = abi.GfmCase()
+        self.summary = None
+        self.name = cfg.name
+        self.spec = cfg.to_spec()
+        rc = self.lib.gfo_case_build(C.byref(self.spec), str(abi.KINETIC_PATH).encode(), C.byref(self.c))
+        if rc != 0:
+            raise RuntimeError(f"gfo_case_build: {rc}")
+        self._dims()
+
+    def close(self) -> None:
+        if self.c.priv:
+            self.lib.gfo_case_free(C.byref(self.c))
 
 
 class Oracle:
