@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -464,6 +465,10 @@ int Net::create(int nx, int ny, int nz, uint64_t seed) {
     }
     if (cudaMemcpy(p32, h.data(), sizeof(float) * np, cudaMemcpyHostToDevice) != cudaSuccess) return GFM_E_CUDA;
     cudaMemset(tc_err, 0, sizeof(int));
+    {
+        const char* w = std::getenv("GFM_LP_WAIT1");
+        tc_wait1 = w ? std::atoi(w) : 0;
+    }
     if (prepare_tc() != GFM_OK) { err = "cannot raise the shared-memory limit of the tcgen05 convolutions"; return GFM_E_CUDA; }
     cudaMemset(g32, 0, sizeof(float) * np);
     cudaMemset(m32, 0, sizeof(float) * np);
@@ -502,24 +507,24 @@ void Net::forward(const bf16* X, int nx, int ny, int nz, cudaStream_t st) {
     const float* b = p32;
     auto bias = [&](int l) { return b + weight_offset(l) + 27 * kLayers[l].cin * kLayers[l].cout; };
     if (use_tc) {
-        conv_tc<16, 16>(f, X, 16, 0, wtc[0], bias(0), A1, nullptr, 16, 0, true, tc_err, st);
-        conv_tc<16, 16>(f, A1, 16, 0, wtc[1], bias(1), CAT, nullptr, 48, 0, true, tc_err, st);
+        conv_tc<16, 16>(f, X, 16, 0, wtc[0], bias(0), A1, nullptr, 16, 0, true, tc_err, tc_wait1, st);
+        conv_tc<16, 16>(f, A1, 16, 0, wtc[1], bias(1), CAT, nullptr, 48, 0, true, tc_err, tc_wait1, st);
     } else {
         conv<16, 16>(f, X, 16, 0, w16[0], bias(0), A1, nullptr, 16, 0, true, st);
         conv<16, 16>(f, A1, 16, 0, w16[1], bias(1), CAT, nullptr, 48, 0, true, st);
     }
     k_pool<<<nblk((long long)c.nx * c.ny * c.nz * 16), 256, 0, st>>>(f, CAT, 48, 0, P0, 16);
     if (use_tc) {
-        conv_tc<16, 32>(c, P0, 16, 0, wtc[2], bias(2), A2, nullptr, 32, 0, true, tc_err, st);
-        conv_tc<32, 32>(c, A2, 32, 0, wtc[3], bias(3), E1, nullptr, 32, 0, true, tc_err, st);
+        conv_tc<16, 32>(c, P0, 16, 0, wtc[2], bias(2), A2, nullptr, 32, 0, true, tc_err, tc_wait1, st);
+        conv_tc<32, 32>(c, A2, 32, 0, wtc[3], bias(3), E1, nullptr, 32, 0, true, tc_err, tc_wait1, st);
     } else {
         conv<16, 32>(c, P0, 16, 0, w16[2], bias(2), A2, nullptr, 32, 0, true, st);
         conv<32, 32>(c, A2, 32, 0, w16[3], bias(3), E1, nullptr, 32, 0, true, st);
     }
     k_up<<<nblk((long long)nx * ny * nz), 256, 0, st>>>(f, E1, CAT, 48, 16, 32);
     if (use_tc) {
-        conv_tc<48, 16>(f, CAT, 48, 0, wtc[4], bias(4), A3, nullptr, 16, 0, true, tc_err, st);
-        conv_tc<16, 16>(f, A3, 16, 0, wtc[5], bias(5), nullptr, OUT, 16, 0, false, tc_err, st);
+        conv_tc<48, 16>(f, CAT, 48, 0, wtc[4], bias(4), A3, nullptr, 16, 0, true, tc_err, tc_wait1, st);
+        conv_tc<16, 16>(f, A3, 16, 0, wtc[5], bias(5), nullptr, OUT, 16, 0, false, tc_err, tc_wait1, st);
     } else {
         conv<48, 16>(f, CAT, 48, 0, w16[4], bias(4), A3, nullptr, 16, 0, true, st);
         conv<16, 16>(f, A3, 16, 0, w16[5], bias(5), nullptr, OUT, 16, 0, false, st);
@@ -669,7 +674,9 @@ extern "C" int gfm_lp_set_tensor_path(gfm_lp* lp, int tcgen05) {
     reinterpret_cast<Net*>(lp)->use_tc = tcgen05 != 0;
     return GFM_OK;
 }
-// 1 when a tcgen05 convolution tile gave up waiting for its MMAs (its output is then invalid)
+// 0: every tcgen05 tile's first bounded wait for its MMAs succeeded; 1: a
+// first wait ran out (the second one saw the MMAs end, output written); 2: a
+// tile gave up (output not written, the pass's result invalid)
 extern "C" int gfm_lp_tensor_status(gfm_lp* lp) {
     if (!lp) return GFM_E_ARG;
     Net* n = reinterpret_cast<Net*>(lp);

@@ -40,6 +40,8 @@ struct Net {
     // forward convolutions on tcgen05 (lp_tc.cu): weights in the operand order, expiry flag
     __nv_bfloat16* wtc[kNumLayers] = {};
     int* tc_err = nullptr;
+    int tc_wait1 = 0;                        // polls of the first bounded MMA wait (0: the default limit);
+                                             // GFM_LP_WAIT1 at create, for tests of the expiry path
     float* wg_part = nullptr;                // per-chunk weight-gradient partials (fixed-order sums)
     bool use_tc = true;
     std::string err;
@@ -58,7 +60,8 @@ int prepare_tc();
 void stage_tc(int cin, int cout, const float* wf, __nv_bfloat16* wtc, cudaStream_t st);
 template <int CIN, int COUT>
 void conv_tc(const Grid3& gd, const __nv_bfloat16* in, int in_cs, int in_co, const __nv_bfloat16* wtc, const float* bias,
-             __nv_bfloat16* out, float* out_f, int out_cs, int out_co, bool relu, int* err, cudaStream_t st);
+             __nv_bfloat16* out, float* out_f, int out_cs, int out_co, bool relu, int* err, int wait1,
+             cudaStream_t st);
 
 }  // namespace lp
 }  // namespace gfm

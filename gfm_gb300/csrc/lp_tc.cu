@@ -81,7 +81,7 @@ template <int CIN, int COUT>
 __global__ void __launch_bounds__(kTcThreads) k_conv_tc(Grid3 gd, const bf16* __restrict__ in, int in_cs, int in_co,
                                                        const bf16* __restrict__ wtc, const float* __restrict__ bias,
                                                        bf16* __restrict__ out, float* __restrict__ out_f, int out_cs,
-                                                       int out_co, int relu, int* err) {
+                                                       int out_co, int relu, int* err, int wait1) {
     using S = TcShape<CIN, COUT>;
     constexpr int C8 = S::C8;
     extern __shared__ __align__(128) unsigned char sm[];
@@ -150,12 +150,18 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(Grid3 gd, const bf16* __
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mb) : "memory");
     }
-    // the wait is bounded; the outcome is made uniform over the block so the
-    // warp-collective TMEM reads below run in all warps or in none
-    bool done = __syncthreads_and(mbar_wait(mb, 0, kTcWaitLimit));
+    // the wait is bounded (wait1 polls); the outcome is made uniform over the
+    // block so the warp-collective TMEM reads below run in all warps or in
+    // none.  On expiry the flag is raised (1) and the MMAs are waited for
+    // again; the tile's output is written only when they ended.
+    bool done = __syncthreads_and(mbar_wait(mb, 0, wait1));
     if (!done) {
-        if (tid == 0) atomicExch(err, 1);
-        done = __syncthreads_and(mbar_wait(mb, 0, kTcWaitLimit));   // the MMAs must end before TMEM is freed
+        if (tid == 0) atomicMax(err, 1);
+        done = __syncthreads_and(mbar_wait(mb, 0, kTcWaitLimit));
+        // a second expiry (2): the tile is abandoned and its tensor memory
+        // released below all the same, so that no later CTA on this SM waits
+        // for it; the launch's output is invalid either way
+        if (!done && tid == 0) atomicMax(err, 2);
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (done) {
@@ -200,8 +206,7 @@ __global__ void __launch_bounds__(kTcThreads) k_conv_tc(Grid3 gd, const bf16* __
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0 && done)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TCOLS));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(S::TCOLS));
 }
 
 // weights of one layer in the B operand order [t][c8][co][8], from the FP32 master W[t][co][ci]
@@ -228,19 +233,19 @@ void stage_tc(int cin, int cout, const float* wf, bf16* wtc, cudaStream_t st) {
 }
 template <int CIN, int COUT>
 void conv_tc(const Grid3& gd, const bf16* in, int in_cs, int in_co, const bf16* wtc, const float* bias, bf16* out,
-             float* out_f, int out_cs, int out_co, bool relu, int* err, cudaStream_t st) {
+             float* out_f, int out_cs, int out_co, bool relu, int* err, int wait1, cudaStream_t st) {
     const dim3 grid((unsigned)(((gd.nx + kTcX - 1) / kTcX) * ((gd.ny + kTcY - 1) / kTcY)), (unsigned)gd.nz);
-    k_conv_tc<CIN, COUT><<<grid, kTcThreads, TcShape<CIN, COUT>::SMEM, st>>>(gd, in, in_cs, in_co, wtc, bias, out, out_f,
-                                                                              out_cs, out_co, relu ? 1 : 0, err);
+    k_conv_tc<CIN, COUT><<<grid, kTcThreads, TcShape<CIN, COUT>::SMEM, st>>>(
+        gd, in, in_cs, in_co, wtc, bias, out, out_f, out_cs, out_co, relu ? 1 : 0, err, wait1 > 0 ? wait1 : kTcWaitLimit);
 }
 template void conv_tc<16, 16>(const Grid3&, const bf16*, int, int, const bf16*, const float*, bf16*, float*, int, int, bool,
-                              int*, cudaStream_t);
+                              int*, int, cudaStream_t);
 template void conv_tc<16, 32>(const Grid3&, const bf16*, int, int, const bf16*, const float*, bf16*, float*, int, int, bool,
-                              int*, cudaStream_t);
+                              int*, int, cudaStream_t);
 template void conv_tc<32, 32>(const Grid3&, const bf16*, int, int, const bf16*, const float*, bf16*, float*, int, int, bool,
-                              int*, cudaStream_t);
+                              int*, int, cudaStream_t);
 template void conv_tc<48, 16>(const Grid3&, const bf16*, int, int, const bf16*, const float*, bf16*, float*, int, int, bool,
-                              int*, cudaStream_t);
+                              int*, int, cudaStream_t);
 
 }  // namespace lp
 }  // namespace gfm

@@ -60,7 +60,9 @@ class LearnedPressure:
         self._check(self.lib.gfm_lp_set_tensor_path(self.h, 1 if tcgen05 else 0))
 
     def tensor_status(self) -> int:
-        """1 if a tcgen05 tile gave up waiting for its MMAs (output invalid)."""
+        """0: every tcgen05 tile's first bounded wait for its MMAs succeeded;
+        1: a first wait ran out and the second saw the MMAs end (output
+        written); 2: a tile gave up (the forward pass's output invalid)."""
         return self.lib.gfm_lp_tensor_status(self.h)
 
     def forward(self, feats, dims) -> "torch.Tensor":

@@ -379,9 +379,12 @@ int  gfm_lp_train_step(gfm_lp *lp, const void *feats, const float *target,
                        int nx, int ny, int nz, float lr, int update,
                        double *loss, void *stream);
 /* Forward convolutions on the tcgen05 tensor cores (1, the default) or on
- * warp-level mma.sync (0); gradients always use mma.sync.  Status: 1 when
- * a tcgen05 tile gave up its bounded wait for its MMAs since creation (its
- * output is then invalid), 0 otherwise; waits for the device. */
+ * warp-level mma.sync (0); gradients always use mma.sync.  Status since
+ * creation (waits for the device): 0 when every tcgen05 tile's bounded wait
+ * for its MMAs succeeded; 1 when a tile's first wait ran out, after which it
+ * waited again, saw its MMAs end and wrote its output; 2 when a tile's second
+ * wait ran out too: the tile released its tensor memory without writing its
+ * output, so the forward pass's result is invalid. */
 int  gfm_lp_set_tensor_path(gfm_lp *lp, int tcgen05);
 int  gfm_lp_tensor_status(gfm_lp *lp);
 const char *gfm_lp_last_error(void);
