@@ -35,11 +35,7 @@
 // the affine recurrences of the forward elimination and the back substitution
 // are joined across segments by a scan of the segment maps in shared memory.
 // Each visit thus reads the records of its plane once from DRAM (pass L=2
-// finds them in L2) and the intermediate results never leave the SM.  Where
-// the planes allow it, a visit runs on a cluster of two CTAs, half a plane
-// each (k_rbc_visit, below).
-#include <cooperative_groups.h>
-
+// finds them in L2) and the intermediate results never leave the SM.
 #include <algorithm>
 
 #include "state.cuh"
@@ -533,304 +529,6 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
         for (int kk = threadIdx.x & 31; kk < d.nK; kk += 32) xp[xp_index(d, p, jj, kk)] = out[(jj + 1) * PS + kk + 1];
 }
 
-// ---------------------------------------------------------------------------
-// The same visit by a cluster of two CTAs: rank r holds the K-columns
-// [k_lo, k_lo + W) of the plane (rank 0 the first ceil(nK/2), rank 1 the
-// rest) with a one-column halo on either side, so a plane's work runs on two
-// SMs and each CTA's half-plane fits beside another CTA on its SM.  A y-line
-// lies within one half.  A z-line crosses both: each rank runs its rows as
-// segments, and the two halves are joined through distributed shared memory
-// -- rank 0 hands its line's last forward value to rank 1 (the carry of its
-// first segment), rank 1 hands its line's first back-substituted value to
-// rank 0 (the carry of its last segment), one cluster barrier each.  After
-// pass L=1 the ranks exchange their edge columns of the average, which the
-// y-lines of pass L=2 read across the split.  The arithmetic is that of
-// rbp_pass, with each CTA's segment carries formed as the composed map of the
-// segments before (or after) it applied to the line's start (or end) value.
-// ---------------------------------------------------------------------------
-namespace cg = cooperative_groups;
-
-struct HalfPlane {
-    int k_lo, W, PS;   // first K column, columns, shared-memory row pitch (same in both ranks)
-};
-
-template <typename R, int M, bool ZL, bool FIRST>
-__device__ __forceinline__ void rbc_pass(const RbpBatch<R>& b, int e, const PlaneDims& d, int p, const HalfPlane& h,
-                                         int rank, const R* __restrict__ src, R* __restrict__ dst, R* __restrict__ bxs,
-                                         R* __restrict__ sA, R* __restrict__ sB, R* __restrict__ ex_fwd,
-                                         R* __restrict__ ex_bwd, cg::cluster_group& cl) {
-    const int PS = h.PS;
-    const int nlines = ZL ? d.nJ : h.W, n = ZL ? h.W : d.nJ;
-    const int G = (nlines + 31) >> 5;
-    int S = ((int)(blockDim.x >> 5)) / G;
-    S = S < 1 ? 1 : (S > n ? n : S);
-    const int m = (n + S - 1) / S;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int grp = warp % G, seg = warp / G;
-    const int line = grp * 32 + lane;
-    const bool active = seg < S && line < nlines;
-    const int e0 = seg * m;
-    int cnt = active ? n - e0 : 0;
-    cnt = cnt < 0 ? 0 : (cnt > m ? m : cnt);
-    // bordered half-plane: (jj, local column c) at (jj+1)*PS + c+1; bxs at jj*PS + c
-    const int rstep = ZL ? 1 : PS, across = ZL ? PS : 1;
-    const int c0 = ZL ? (line + 1) * PS + 1 : PS + line + 1;
-    const int bx0 = ZL ? line * PS : line;
-    const int bstep = ZL ? 1 : PS;
-    R xlo = R(0), xhi = R(0);
-    if (active) {
-        xlo = src[c0 - rstep];
-        xhi = src[c0 + n * rstep];
-    }
-    R rr[M], al[M], pv[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        if (i < cnt) {
-            const int row = e0 + i;
-            const int c = c0 + row * rstep;
-            R bx;
-            Quad<R> A;
-            Pair<R> Wp;
-            if (ZL) {
-                const int q = (p * d.nK + h.k_lo + row) * d.nJ + line;
-                A = b.zc[e][q];
-                Wp = b.zp[e][q];
-                bx = bxs[bx0 + row * bstep];
-            } else {
-                const int kk = h.k_lo + line;
-                const int q = (p * d.nJ + row) * d.nK + kk;
-                A = b.yc[e][q];
-                Wp = b.yp[e][q];
-                if (FIRST) {
-                    const Pair<R> X = b.yx[e][q];
-                    const R* __restrict__ xp = b.xp[e];
-                    const R xm = xp[xp_index(d, p - 1, row, kk)];
-                    const R xq = xp[xp_index(d, p + 1, row, kk)];
-                    bx = (A.w + X.y * xq) + X.x * xm;   // BS + AS12 XT(I+2) + AS11 XT(I-2)
-                    bxs[bx0 + row * bstep] = bx;
-                } else {
-                    bx = bxs[bx0 + row * bstep];
-                }
-            }
-            const R v = Wp.x * ((bx + A.z * src[c + across]) + A.y * src[c - across]);
-            const bool cp = rbp_copy(Wp.y);
-            rr[i] = cp ? src[c] : v;
-            al[i] = A.x * Wp.x;
-            pv[i] = Wp.y;
-        }
-    }
-    R q[M], P[M];
-    R qc = R(0), Pc = R(1);
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        if (i < cnt) {
-            qc = rr[i] + al[i] * qc;
-            Pc = al[i] * Pc;
-            q[i] = qc;
-            P[i] = Pc;
-        }
-    }
-    sA[threadIdx.x] = cnt > 0 ? Pc : R(1);
-    sB[threadIdx.x] = cnt > 0 ? qc : R(0);
-    __syncthreads();
-    // the composed map of this CTA's segments before this one
-    R Ppre = R(1), qpre = R(0);
-    for (int k = 0; k < seg; ++k) {
-        const R a = sA[(k * G + grp) * 32 + lane], bb = sB[(k * G + grp) * 32 + lane];
-        qpre = a * qpre + bb;
-        Ppre = a * Ppre;
-    }
-    // carry in: the line's start, or across the split the last forward value of rank 0
-    const bool joined = ZL && rank == 1;
-    if (!joined) {
-        const R qin = Ppre * xlo + qpre;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            if (i < cnt) {
-                q[i] = q[i] + P[i] * qin;
-                if (ZL && e0 + i == n - 1) ex_fwd[line] = q[i];
-            }
-        }
-    }
-    if (ZL) cl.sync();
-    if (joined && active) {
-        const R* rem = cl.map_shared_rank(ex_fwd, 0);
-        const R qin = Ppre * rem[line] + qpre;
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-            if (i < cnt) q[i] = q[i] + P[i] * qin;
-    }
-    __syncthreads();
-    R xc = R(0), Rc = R(1);
-#pragma unroll
-    for (int i = M - 1; i >= 0; --i) {
-        if (i < cnt) {
-            xc = pv[i] * xc + q[i];
-            Rc = pv[i] * Rc;
-            q[i] = xc;
-            P[i] = Rc;
-        }
-    }
-    sA[threadIdx.x] = cnt > 0 ? Rc : R(1);
-    sB[threadIdx.x] = cnt > 0 ? xc : R(0);
-    __syncthreads();
-    R Rpost = R(1), xpost = R(0);
-    for (int k = S - 1; k > seg; --k) {
-        const R a = sA[(k * G + grp) * 32 + lane], bb = sB[(k * G + grp) * 32 + lane];
-        xpost = a * xpost + bb;
-        Rpost = a * Rpost;
-    }
-    // carry in from the end: the line's end value, or across the split the
-    // first back-substituted value of rank 1
-    const bool joined_b = ZL && rank == 0;
-    if (!joined_b) {
-        const R xin = Rpost * xhi + xpost;
-#pragma unroll
-        for (int i = 0; i < M; ++i) {
-            if (i < cnt) {
-                q[i] = q[i] + P[i] * xin;
-                if (ZL && e0 + i == 0) ex_bwd[line] = q[i];
-            }
-        }
-    }
-    if (ZL) cl.sync();
-    if (joined_b && active) {
-        const R* rem = cl.map_shared_rank(ex_bwd, 1);
-        const R xin = Rpost * rem[line] + xpost;
-#pragma unroll
-        for (int i = 0; i < M; ++i)
-            if (i < cnt) q[i] = q[i] + P[i] * xin;
-    }
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        if (i < cnt) {
-            const int c = c0 + (e0 + i) * rstep;
-            dst[c] = ZL ? (dst[c] + q[i]) / R(2) : q[i];
-        }
-    }
-    __syncthreads();
-}
-
-template <typename R>
-__host__ __device__ __forceinline__ HalfPlane half_plane(const PlaneDims& d, int rank) {
-    const int h0 = (d.nK + 1) / 2;
-    return HalfPlane{rank == 0 ? 0 : h0, rank == 0 ? h0 : d.nK - h0, (h0 + 2) | 1};
-}
-template <typename R>
-__host__ __device__ __forceinline__ size_t rbc_smem_bytes(const PlaneDims& d, int nt) {
-    const HalfPlane h = half_plane<R>(d, 0);
-    return (size_t)(2 * (d.nJ + 2) * h.PS + d.nJ * h.PS + 2 * nt + 2 * d.nJ) * sizeof(R);
-}
-
-template <typename R, int NT, int M>
-__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(NT, 2) k_rbc_visit(RbpBatch<R> b, int colour, int sweep) {
-    extern __shared__ __align__(16) unsigned char rbc_smem[];
-    cg::cluster_group cl = cg::this_cluster();
-    const int rank = (int)cl.block_rank();
-    const int e = blockIdx.y;
-    const Sys<R>& s = b.sys[e];
-    if (sweep >= s.nim) return;   // both ranks of a cluster leave together
-    const PlaneDims d = dims_of(s);
-    const int npc = (d.npl - colour + 1) / 2;
-    if ((int)(blockIdx.x >> 1) >= npc) return;
-    const int p = colour + 2 * (int)(blockIdx.x >> 1);
-    const HalfPlane h = half_plane<R>(d, rank);
-    const int XJ = d.nK + 2, np = (d.nJ + 2) * XJ;
-    const int base = (p + 1) * np;
-    R* __restrict__ xp = b.xp[e];
-    if (threadIdx.x == 0) {
-        // the records of the plane, one half of them per rank (fixed during
-        // the call, so this may run while the kernel before is finishing)
-        const size_t pc = (size_t)d.nJ * d.nK;
-        if (rank == 0) {
-            l2_prefetch(b.yc[e] + p * pc, pc * sizeof(Quad<R>));
-            l2_prefetch(b.yp[e] + p * pc, pc * sizeof(Pair<R>));
-            l2_prefetch(b.yx[e] + p * pc, pc * sizeof(Pair<R>));
-        } else {
-            l2_prefetch(b.zc[e] + p * pc, pc * sizeof(Quad<R>));
-            l2_prefetch(b.zp[e] + p * pc, pc * sizeof(Pair<R>));
-        }
-    }
-    pdl_wait();
-    pdl_trigger();
-    if (threadIdx.x == 0) l2_prefetch(xp + base + (rank == 0 ? -np : np), (size_t)np * sizeof(R));
-    const int PS = h.PS, PB = (d.nJ + 2) * PS;
-    R* xa = reinterpret_cast<R*>(rbc_smem);
-    R* xb = xa + PB;
-    R* bxs = xb + PB;
-    R* sA = bxs + d.nJ * PS;
-    R* sB = sA + NT;
-    R* ex_fwd = sB + NT;
-    R* ex_bwd = ex_fwd + d.nJ;
-    // the half-plane with its halo columns and border rows; into xb the
-    // border rows and the plane's own border column (the line ends)
-    {
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        constexpr int NW = NT / 32;
-        const int wc = h.W + 2;
-        for (int j0 = 2 * warp; j0 < d.nJ + 2; j0 += 2 * NW)
-            for (int k0 = 0; k0 < wc; k0 += 64) {
-                R v[2][2];
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int jr = j0 + a, cr = k0 + lane + 32 * u;
-                        if (jr < d.nJ + 2 && cr < wc) v[a][u] = xp[base + jr * XJ + h.k_lo + cr];
-                    }
-#pragma unroll
-                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                    for (int u = 0; u < 2; ++u) {
-                        const int jr = j0 + a, cr = k0 + lane + 32 * u;
-                        if (jr < d.nJ + 2 && cr < wc) {
-                            xa[jr * PS + cr] = v[a][u];
-                            const bool edge = jr == 0 || jr == d.nJ + 1 || (rank == 0 && cr == 0) ||
-                                              (rank == 1 && cr == h.W + 1);
-                            if (edge) xb[jr * PS + cr] = v[a][u];
-                        }
-                    }
-            }
-    }
-    __syncthreads();
-    rbc_pass<R, M, false, true>(b, e, d, p, h, rank, xa, xb, bxs, sA, sB, ex_fwd, ex_bwd, cl);
-    rbc_pass<R, M, true, false>(b, e, d, p, h, rank, xa, xb, bxs, sA, sB, ex_fwd, ex_bwd, cl);
-    // the average's columns at the split, for the y-lines of pass L=2
-    cl.sync();
-    {
-        const R* rem = cl.map_shared_rank(xb, rank ^ 1);
-        const int W0 = (d.nK + 1) / 2;
-        for (int jj = threadIdx.x; jj < d.nJ; jj += NT) {
-            if (rank == 0) xb[(jj + 1) * PS + h.W + 1] = rem[(jj + 1) * PS + 1];
-            else xb[(jj + 1) * PS] = rem[(jj + 1) * PS + W0];
-        }
-    }
-    __syncthreads();
-    rbc_pass<R, M, false, false>(b, e, d, p, h, rank, xb, xa, bxs, sA, sB, ex_fwd, ex_bwd, cl);
-    rbc_pass<R, M, true, false>(b, e, d, p, h, rank, xb, xa, bxs, sA, sB, ex_fwd, ex_bwd, cl);
-    for (int jj = threadIdx.x >> 5; jj < d.nJ; jj += NT / 32)
-        for (int c = threadIdx.x & 31; c < h.W; c += 32) xp[xp_index(d, p, jj, h.k_lo + c)] = xa[(jj + 1) * PS + c + 1];
-    cl.sync();   // neither rank leaves while the other may still read its shared memory
-}
-
-constexpr int kRbcThreads = 384;   // threads of a cluster-visit CTA (two CTAs a plane, two CTAs an SM)
-constexpr int kRbcMaxSmem = 110 * 1024;
-
-// the cluster form fits when both halves' passes keep within M rows a
-// segment (the formula of rbc_pass) and two CTAs fit an SM
-template <typename R>
-bool rbc_fits(const PlaneDims& d) {
-    if (d.nK < 4) return false;
-    auto fits = [](int nlines, int n) {
-        const int G = (nlines + 31) / 32;
-        int S = (kRbcThreads / 32) / G;
-        S = S < 1 ? 1 : (S > n ? n : S);
-        return (n + S - 1) / S <= 8;
-    };
-    const int W0 = (d.nK + 1) / 2;
-    return fits(W0, d.nJ) && fits(d.nJ, W0) && rbc_smem_bytes<R>(d, kRbcThreads) <= (size_t)kRbcMaxSmem;
-}
-
 constexpr int kRbpM = 8;            // rows of a segment held in registers
 constexpr int kRbpThreads = 768;    // threads of a visit CTA (80 registers a thread, one CTA per SM)
 constexpr size_t kRbpMaxSmem = 227 * 1024;
@@ -847,8 +545,7 @@ inline bool rbp_pass_fits(int nlines, int n) {
 }  // namespace
 
 template <typename R>
-int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, cudaStream_t st, int rb_flags) {
-    const bool pdl = (rb_flags & kRbPdl) != 0;
+int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, cudaStream_t st, bool pdl) {
     RbpBatch<R> b;
     b.nsys = nsys;
     size_t smem = 0;
@@ -872,13 +569,6 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
         nim = std::max(nim, sys[e].nim);
     }
     if (smem > kRbpMaxSmem) return 0;
-    bool cluster = (rb_flags & kRbCluster) != 0;
-    size_t csmem = 0;
-    for (int e = 0; e < nsys; ++e) {
-        const PlaneDims d = dims_of(sys[e]);
-        cluster = cluster && rbc_fits<R>(d) && sys[e].kb < sys[e].ke;
-        csmem = std::max(csmem, rbc_smem_bytes<R>(d, kRbcThreads));
-    }
     const unsigned tiles_in = (unsigned)(((max_np + 2 + 31) / 32) * ((max_nk + 2 + 31) / 32));
     const unsigned tiles_out = (unsigned)(((max_np + 31) / 32) * ((max_nk + 31) / 32));
     const unsigned ptiles = (unsigned)((max_np + 31) / 32);
@@ -888,15 +578,10 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     launch_k(pdl, k_rbp_pivots<R, false>, dim3(ptiles * ((max_nk + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
     launch_k(pdl, k_rbp_pivots<R, true>, dim3(ptiles * ((max_nj + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
     const dim3 gv((unsigned)((max_np + 1) / 2), nsys);
-    const dim3 gc((unsigned)(2 * ((max_np + 1) / 2)), nsys);
     for (int ns = 0; ns < nim; ++ns)
         for (int half = 0; half < 2; ++half)
-            for (int colour = 0; colour < 2; ++colour) {
-                if (cluster)
-                    launch_k(pdl, k_rbc_visit<R, kRbcThreads, kRbpM>, gc, dim3(kRbcThreads), csmem, st, b, colour, ns);
-                else
-                    launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
-            }
+            for (int colour = 0; colour < 2; ++colour)
+                launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
     launch_k(pdl, k_rbp_copy<R, false>, dim3(tiles_out, max_nj, nsys), dim3(32, 8), 0, st, g, b);
     return 6 + 4 * nim;
 }
@@ -905,16 +590,12 @@ int prepare_rbp() {
     const bool ok = cudaFuncSetAttribute(k_rbp_visit<float, kRbpThreads, kRbpM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess &&
                     cudaFuncSetAttribute(k_rbp_visit<double, kRbpThreads, kRbpM>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_rbc_visit<float, kRbcThreads, kRbpM>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kRbcMaxSmem) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_rbc_visit<double, kRbcThreads, kRbpM>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kRbcMaxSmem) == cudaSuccess;
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess;
     return ok ? GFM_OK : GFM_E_CUDA;
 }
 
-template int launch_rbp<float>(const GeoT<float>&, const Sys<float>*, const AdiScratch<float>*, int, cudaStream_t, int);
+template int launch_rbp<float>(const GeoT<float>&, const Sys<float>*, const AdiScratch<float>*, int, cudaStream_t, bool);
 template int launch_rbp<double>(const GeoT<double>&, const Sys<double>*, const AdiScratch<double>*, int, cudaStream_t,
-                                int);
+                                bool);
 
 }  // namespace gfm

@@ -102,10 +102,9 @@ struct gfm_handle {
     bool rad_ready = false;
     cudaStream_t rad_stream[2]{};       // the y- and z-direction traces run beside the x-direction
     cudaEvent_t rad_ev[3]{};
-    int rb_flags = kRbPlane | kRbCluster | kRbPdl | kRbAvgInPass;   // red-black options (environment at create):
-                                                                    // GFM_RB_PLANE=0 drops kRbPlane, GFM_RB_CLUSTER=0
-                                                                    // kRbCluster, GFM_PDL=0 kRbPdl,
-                                                                    // GFM_RB_AVG_IN_PASS=0 kRbAvgInPass
+    int rb_flags = kRbPlane | kRbPdl | kRbAvgInPass;   // red-black options (environment at create): GFM_RB_PLANE=0
+                                                       // drops kRbPlane, GFM_PDL=0 kRbPdl, GFM_RB_AVG_IN_PASS=0
+                                                       // kRbAvgInPass
 };
 
 namespace {
@@ -828,11 +827,10 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     if (prepare_line_solver() != GFM_OK) { h->err = "cannot raise the line solver's shared-memory limit"; return GFM_E_CUDA; }
     {
         const char* pl = std::getenv("GFM_RB_PLANE");
-        const char* cl = std::getenv("GFM_RB_CLUSTER");
         const char* pd = std::getenv("GFM_PDL");
         const char* ap = std::getenv("GFM_RB_AVG_IN_PASS");
-        h->rb_flags = (pl && pl[0] == '0' ? 0 : kRbPlane) | (cl && cl[0] == '0' ? 0 : kRbCluster) |
-                      (pd && pd[0] == '0' ? 0 : kRbPdl) | (ap && ap[0] == '0' ? 0 : kRbAvgInPass);
+        h->rb_flags = (pl && pl[0] == '0' ? 0 : kRbPlane) | (pd && pd[0] == '0' ? 0 : kRbPdl) |
+                      (ap && ap[0] == '0' ? 0 : kRbAvgInPass);
     }
     cudaEventCreate(&h->ev_adi0);
     cudaEventCreate(&h->ev_adi1);

@@ -169,19 +169,17 @@ template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
 template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
 template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);
-// red-black line-solver options: kRbPlane runs each plane visit in shared memory
+// red-black line-solver options: kRbPlane runs each plane visit in one CTA
 // (adi_plane.cu) wherever every plane of the batch fits, else the segmented
 // colour passes below run; kRbPdl launches the line-solver kernels with
 // programmatic dependent launch; kRbAvgInPass lets pass L=2 of the segmented
 // form average the pass L=1 results where it reads them, in place of the
 // averaging launch between the passes
-// kRbCluster lets a plane visit run on a cluster of two CTAs (half a plane
-// each) wherever the batch's planes fit that form
-constexpr int kRbPlane = 1, kRbPdl = 2, kRbAvgInPass = 4, kRbCluster = 8;
+constexpr int kRbPlane = 1, kRbPdl = 2, kRbAvgInPass = 4;
 // the plane-visit form of one ADLBL3 call on a batch; returns the kernels it
 // launched, or 0 (nothing launched) when a plane of the batch does not fit
 template <typename R> int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
-                                     cudaStream_t s, int rb_flags);
+                                     cudaStream_t s, bool pdl);
 int prepare_rbp();
 // returns the number of kernels it launched
 template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,

@@ -51,21 +51,16 @@ def _oracle_adlbl3(case, adi, ap, as6, bs, x0, rng, nim):
     return xo
 
 
-FORMS = {"cluster": {}, "plane": {"GFM_RB_CLUSTER": "0"}, "segmented": {"GFM_RB_PLANE": "0"}}
-
-
-@pytest.mark.parametrize("form", list(FORMS))
+@pytest.mark.parametrize("plane", ["1", "0"])
 @pytest.mark.parametrize("cls", [(0, 0, 0), (1, 0, 0), (0, 1, 0), (0, 0, 1)])
 @pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-13), (abi.GFM_PREC_MIXED, 1e-5)])
-def test_redblack_matches_the_redblack_oracle(cls, prec, tol, form, monkeypatch):
+def test_redblack_matches_the_redblack_oracle(cls, prec, tol, plane, monkeypatch):
     """Two sweeps in the red-black plane order against the oracle's ADLBL3 in
     the same order, on each face class: the same iterate up to rounding
-    (FP64) or to FP32 rounding (mixed).  All three forms of the order (read
-    when the handle is created): a plane visit by a cluster of two CTAs (the
-    default), by one CTA (GFM_RB_CLUSTER=0), and the segmented colour passes
-    (GFM_RB_PLANE=0)."""
-    for k, v in FORMS[form].items():
-        monkeypatch.setenv(k, v)
+    (FP64) or to FP32 rounding (mixed).  Both forms of the order: one CTA per
+    plane visit (default), and the segmented colour passes (GFM_RB_PLANE=0,
+    read when the handle is created)."""
+    monkeypatch.setenv("GFM_RB_PLANE", plane)
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case, cls)
     g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
@@ -76,13 +71,12 @@ def test_redblack_matches_the_redblack_oracle(cls, prec, tol, form, monkeypatch)
     assert err < tol, err
 
 
-@pytest.mark.parametrize("adi,form", [(abi.GFM_ADI_MARCH, "cluster"), (abi.GFM_ADI_REDBLACK, "cluster"),
-                                      (abi.GFM_ADI_REDBLACK, "plane"), (abi.GFM_ADI_REDBLACK, "segmented")])
-def test_single_z_row_takes_the_y_pass_alone(adi, form, monkeypatch):
+@pytest.mark.parametrize("adi,plane", [(abi.GFM_ADI_MARCH, "1"), (abi.GFM_ADI_REDBLACK, "1"),
+                                       (abi.GFM_ADI_REDBLACK, "0")])
+def test_single_z_row_takes_the_y_pass_alone(adi, plane, monkeypatch):
     """A solve range with one z-row (kb == ke): the reference's ADLZ copies the
     first y-line pass into XT and leaves the plane (Adlbl3.f90:124-130)."""
-    for k, v in FORMS[form].items():
-        monkeypatch.setenv(k, v)
+    monkeypatch.setenv("GFM_RB_PLANE", plane)
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case)
     ib0, ie, jb, je, kb, ke = rng
@@ -120,12 +114,10 @@ def test_redblack_launch_forms_agree_bit_for_bit(prec, cls, monkeypatch):
 
 
 @pytest.mark.parametrize("prec", [abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED])
-@pytest.mark.parametrize("form", ["cluster", "plane"])
-def test_plane_visit_with_and_without_dependent_launch(prec, form, monkeypatch):
-    """Both plane-visit forms give identical iterates with and without
-    programmatic dependent launch of their kernels."""
-    for k, v in FORMS[form].items():
-        monkeypatch.setenv(k, v)
+def test_plane_visit_with_and_without_dependent_launch(prec, monkeypatch):
+    """The plane-visit form gives identical iterates with and without
+    programmatic dependent launch of its kernels."""
+    monkeypatch.setenv("GFM_RB_PLANE", "1")
     case = Case(configs.small_furnace())
     ap, as6, bs, x0, sol, rng, open_ = manufactured(case, (0, 1, 1))
     out = []
