@@ -531,13 +531,14 @@ __global__ void __launch_bounds__(NT, 1) k_rbp_visit(RbpBatch<R> b, int colour, 
 
 constexpr int kRbpM = 8;            // rows of a segment held in registers
 constexpr int kRbpThreads = 768;    // threads of a visit CTA (80 registers a thread, one CTA per SM)
+constexpr int kRbpSmall = 256;      // threads of a visit CTA for planes whose passes fit 8 warps
 constexpr size_t kRbpMaxSmem = 227 * 1024;
 
 // segments a pass of n-row lines, nlines of them, gets from the CTA (the
 // formula of rbp_pass); the pass fits when no segment exceeds M rows
-inline bool rbp_pass_fits(int nlines, int n) {
+inline bool rbp_pass_fits(int nlines, int n, int nt = kRbpThreads) {
     const int G = (nlines + 31) / 32;
-    int S = (kRbpThreads / 32) / G;
+    int S = (nt / 32) / G;
     S = S < 1 ? 1 : (S > n ? n : S);
     return (n + S - 1) / S <= kRbpM;
 }
@@ -550,9 +551,13 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     b.nsys = nsys;
     size_t smem = 0;
     int max_np = 0, max_nj = 0, max_nk = 0, nim = 0;
+    // planes small enough for 8 warps run on CTAs of that size: a few
+    // hundred points a plane leave most of a larger CTA idle at its barriers
+    bool small = true;
     for (int e = 0; e < nsys; ++e) {
         const PlaneDims d = dims_of(sys[e]);
         if (!rbp_pass_fits(d.nK, d.nJ) || !rbp_pass_fits(d.nJ, d.nK)) return 0;
+        small = small && rbp_pass_fits(d.nK, d.nJ, kRbpSmall) && rbp_pass_fits(d.nJ, d.nK, kRbpSmall);
         smem = std::max(smem, rbp_smem_bytes<R>(d, kRbpThreads));
         b.sys[e] = sys[e];
         // the records in the scratch of the segmented form (2*CBH elements each)
@@ -569,6 +574,10 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
         nim = std::max(nim, sys[e].nim);
     }
     if (smem > kRbpMaxSmem) return 0;
+    // in FP64 the small planes go to the segmented colour passes, which keep
+    // more lines in flight per SM for the FP64 pipe (TC21: 2.6 against 3.5 ms
+    // an iteration)
+    if (small && sizeof(R) == 8) return 0;
     const unsigned tiles_in = (unsigned)(((max_np + 2 + 31) / 32) * ((max_nk + 2 + 31) / 32));
     const unsigned tiles_out = (unsigned)(((max_np + 31) / 32) * ((max_nk + 31) / 32));
     const unsigned ptiles = (unsigned)((max_np + 31) / 32);
@@ -581,7 +590,10 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     for (int ns = 0; ns < nim; ++ns)
         for (int half = 0; half < 2; ++half)
             for (int colour = 0; colour < 2; ++colour)
-                launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
+                if (small)
+                    launch_k(pdl, k_rbp_visit<R, kRbpSmall, kRbpM>, gv, dim3(kRbpSmall), smem, st, b, colour, ns);
+                else
+                    launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
     launch_k(pdl, k_rbp_copy<R, false>, dim3(tiles_out, max_nj, nsys), dim3(32, 8), 0, st, g, b);
     return 6 + 4 * nim;
 }
@@ -590,6 +602,10 @@ int prepare_rbp() {
     const bool ok = cudaFuncSetAttribute(k_rbp_visit<float, kRbpThreads, kRbpM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess &&
                     cudaFuncSetAttribute(k_rbp_visit<double, kRbpThreads, kRbpM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_rbp_visit<float, kRbpSmall, kRbpM>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_rbp_visit<double, kRbpSmall, kRbpM>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbpMaxSmem) == cudaSuccess;
     return ok ? GFM_OK : GFM_E_CUDA;
 }

@@ -71,6 +71,21 @@ def test_redblack_matches_the_redblack_oracle(cls, prec, tol, plane, monkeypatch
     assert err < tol, err
 
 
+@pytest.mark.parametrize("prec,tol", [(abi.GFM_PREC_FP64, 1e-13), (abi.GFM_PREC_MIXED, 1e-5)])
+def test_redblack_large_planes_match_the_redblack_oracle(prec, tol):
+    """The 192x96x64 furnace's planes (96 x 64 points) take the plane visit on
+    CTAs of 768 threads (the smaller cases above fit the 256-thread form):
+    one sweep against the oracle in the same plane order."""
+    case = Case(configs.large_furnace())
+    ap, as6, bs, x0, sol, rng, open_ = manufactured(case, (0, 0, 1))
+    g = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK, precision=prec)
+    xg = g.adlbl3(x0, ap, as6, bs, *rng, 1)
+    g.close()
+    xo = _oracle_adlbl3(case, abi.GFM_ADI_REDBLACK, ap, as6, bs, x0, rng, 1)
+    err = np.abs(xg - xo)[open_].max() / np.abs(xo[open_]).max()
+    assert err < tol, err
+
+
 @pytest.mark.parametrize("adi,plane", [(abi.GFM_ADI_MARCH, "1"), (abi.GFM_ADI_REDBLACK, "1"),
                                        (abi.GFM_ADI_REDBLACK, "0")])
 def test_single_z_row_takes_the_y_pass_alone(adi, plane, monkeypatch):
