@@ -135,11 +135,8 @@ __global__ void k_rbp_copy(GeoT<R> g, RbpBatch<R> b) {
 // record), z = system.
 // ---------------------------------------------------------------------------
 template <typename R, bool ZL>
-__global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b) {
+__device__ __forceinline__ void rbp_fill(const GeoT<R>& g, const RbpBatch<R>& b, int bx, R (*tile)[16][33]) {
     constexpr int NF = ZL ? 3 : 6;
-    __shared__ R tile[NF][16][33];
-    pdl_wait();
-    pdl_trigger();
     const int e = blockIdx.z;
     const Sys<R>& s = b.sys[e];
     const PlaneDims d = dims_of(s);
@@ -147,7 +144,7 @@ __global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b) {
     const int row = blockIdx.y;
     if (row >= nrows) return;
     const int ntp = (d.npl + 31) / 32;
-    const int p0 = (blockIdx.x % ntp) * 32, l0 = (blockIdx.x / ntp) * 16;
+    const int p0 = (bx % ntp) * 32, l0 = (bx / ntp) * 16;
     if (l0 >= nlines) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     // y-line record: AS21, AS31, AS32, BS, AS11, AS12; z-line record: AS31, AS21, AS22
@@ -187,6 +184,17 @@ __global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b) {
     }
 }
 
+// the y-line records in blocks [0, nyb) of grid x, the z-line records in
+// the rest: both directions in one launch
+template <typename R>
+__global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b, int nyb) {
+    __shared__ R tile[6][16][33];
+    pdl_wait();
+    pdl_trigger();
+    if ((int)blockIdx.x < nyb) rbp_fill<R, false>(g, b, blockIdx.x, tile);
+    else rbp_fill<R, true>(g, b, blockIdx.x - nyb, tile);
+}
+
 // ---------------------------------------------------------------------------
 // Pivots of every line, once per call: a thread walks one line (plane p, a
 // fixed cross index) row by row through the pivot chain of ADLZY/ADLYZ.
@@ -200,17 +208,15 @@ __global__ void __launch_bounds__(256) k_rbp_fill(GeoT<R> g, RbpBatch<R> b) {
 // ---------------------------------------------------------------------------
 constexpr int kPivRows = 8;
 template <typename R, bool ZL>
-__global__ void __launch_bounds__(256) k_rbp_pivots(GeoT<R> g, RbpBatch<R> b) {
+__device__ __forceinline__ void rbp_pivots(const GeoT<R>& g, const RbpBatch<R>& b, int bx,
+                                           Pair<R> (*tile)[8][33]) {
     constexpr int C = kPivRows;
-    __shared__ Pair<R> tile[C][8][33];
-    pdl_wait();
-    pdl_trigger();
     const int e = blockIdx.y;
     const Sys<R>& s = b.sys[e];
     const PlaneDims d = dims_of(s);
     const int nlines = ZL ? d.nJ : d.nK, nrows = ZL ? d.nK : d.nJ;
     const int ntp = (d.npl + 31) / 32;
-    const int p0 = (blockIdx.x % ntp) * 32, l0 = (blockIdx.x / ntp) * 8;
+    const int p0 = (bx % ntp) * 32, l0 = (bx / ntp) * 8;
     if (l0 >= nlines) return;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int p = p0 + tx, l = l0 + ty;
@@ -280,6 +286,17 @@ __global__ void __launch_bounds__(256) k_rbp_pivots(GeoT<R> g, RbpBatch<R> b) {
             cap[c] = nap[c]; csub[c] = nsub[c]; cnxt[c] = nnxt[c]; cblk[c] = nblk[c];
         }
     }
+}
+
+// the y-line pivots in blocks [0, nyb) of grid x, the z-line pivots in the
+// rest: both directions in one launch
+template <typename R>
+__global__ void __launch_bounds__(256) k_rbp_pivots(GeoT<R> g, RbpBatch<R> b, int nyb) {
+    __shared__ Pair<R> tile[kPivRows][8][33];
+    pdl_wait();
+    pdl_trigger();
+    if ((int)blockIdx.x < nyb) rbp_pivots<R, false>(g, b, blockIdx.x, tile);
+    else rbp_pivots<R, true>(g, b, blockIdx.x - nyb, tile);
 }
 
 // ---------------------------------------------------------------------------
@@ -582,10 +599,10 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     const unsigned tiles_out = (unsigned)(((max_np + 31) / 32) * ((max_nk + 31) / 32));
     const unsigned ptiles = (unsigned)((max_np + 31) / 32);
     launch_k(pdl, k_rbp_copy<R, true>, dim3(tiles_in, max_nj + 2, nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_fill<R, false>, dim3(ptiles * ((max_nk + 15) / 16), max_nj, nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_fill<R, true>, dim3(ptiles * ((max_nj + 15) / 16), max_nk, nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_pivots<R, false>, dim3(ptiles * ((max_nk + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
-    launch_k(pdl, k_rbp_pivots<R, true>, dim3(ptiles * ((max_nj + 7) / 8), nsys), dim3(32, 8), 0, st, g, b);
+    const int fy = (int)(ptiles * ((max_nk + 15) / 16)), fz = (int)(ptiles * ((max_nj + 15) / 16));
+    launch_k(pdl, k_rbp_fill<R>, dim3((unsigned)(fy + fz), std::max(max_nj, max_nk), nsys), dim3(32, 8), 0, st, g, b, fy);
+    const int py = (int)(ptiles * ((max_nk + 7) / 8)), pz = (int)(ptiles * ((max_nj + 7) / 8));
+    launch_k(pdl, k_rbp_pivots<R>, dim3((unsigned)(py + pz), nsys), dim3(32, 8), 0, st, g, b, py);
     const dim3 gv((unsigned)((max_np + 1) / 2), nsys);
     for (int ns = 0; ns < nim; ++ns)
         for (int half = 0; half < 2; ++half)
@@ -595,7 +612,7 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
                 else
                     launch_k(pdl, k_rbp_visit<R, kRbpThreads, kRbpM>, gv, dim3(kRbpThreads), smem, st, b, colour, ns);
     launch_k(pdl, k_rbp_copy<R, false>, dim3(tiles_out, max_nj, nsys), dim3(32, 8), 0, st, g, b);
-    return 6 + 4 * nim;
+    return 4 + 4 * nim;
 }
 
 int prepare_rbp() {
