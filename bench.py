@@ -134,8 +134,8 @@ class ClockSampler:
 
 
 def load_traffic(prec: str):
-    """DRAM traffic of one colour visit of the line solver (pass L=1, average,
-    pass L=2, average) from the committed ncu summary of the same workload."""
+    """DRAM traffic of one colour visit of the line solver (one plane-visit
+    launch) from the committed ncu summary of the same workload."""
     p = ROOT / "profiles" / f"ncu_adi_{prec}_192x96x64.json"
     if p.exists():
         try:
@@ -549,7 +549,7 @@ def run_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None,
                          "traffic": traffic.get("dram_bytes_per_colour_visit") if traffic else None,
-                         "traffic_unit": "DRAM bytes per colour visit (4 launches) of the 192x96x64 P equation, ncu",
+                         "traffic_unit": "DRAM bytes per colour visit (one launch) of the 192x96x64 P equation, ncu",
                          "traffic_algorithmic": traffic.get("algorithmic_bytes_per_colour_visit") if traffic else None,
                          "peak_kind": peak_kind, "kernel": "ADLBL3 line solver (plane updates)",
                          "algorithmic_bytes": f"{BYTES_PER_CELL_VISIT} x {w} B per cell per plane visit",

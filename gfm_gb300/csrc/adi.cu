@@ -909,7 +909,7 @@ int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* 
         auto blocks = [](long long n, int t) { long long b = (n + t - 1) / t; return (unsigned)(b < 1 ? 1 : (b > 4096 ? 4096 : b)); };
         const bool pdl = (rb_flags & kRbPdl) != 0;
         if (rb_flags & kRbPlane) {
-            const int n = launch_rbp(g, sys, scr, nsys, st, pdl);
+            const int n = launch_rbp(g, sys, scr, nsys, st, rb_flags);
             if (n > 0) return n;
         }
         const int S = rb_segments<R>(max_n);

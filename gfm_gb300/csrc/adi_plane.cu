@@ -563,7 +563,8 @@ inline bool rbp_pass_fits(int nlines, int n, int nt = kRbpThreads) {
 }  // namespace
 
 template <typename R>
-int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, cudaStream_t st, bool pdl) {
+int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys, cudaStream_t st, int rb_flags) {
+    const bool pdl = (rb_flags & kRbPdl) != 0;
     RbpBatch<R> b;
     b.nsys = nsys;
     size_t smem = 0;
@@ -594,7 +595,8 @@ int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, in
     // in FP64 the small planes go to the segmented colour passes, which keep
     // more lines in flight per SM for the FP64 pipe (TC21: 2.6 against 3.5 ms
     // an iteration)
-    if (small && sizeof(R) == 8) return 0;
+    if (rb_flags & kRbNoSmall) small = false;
+    if (small && sizeof(R) == 8 && !(rb_flags & kRbSmallF64)) return 0;
     const unsigned tiles_in = (unsigned)(((max_np + 2 + 31) / 32) * ((max_nk + 2 + 31) / 32));
     const unsigned tiles_out = (unsigned)(((max_np + 31) / 32) * ((max_nk + 31) / 32));
     const unsigned ptiles = (unsigned)((max_np + 31) / 32);
@@ -627,8 +629,8 @@ int prepare_rbp() {
     return ok ? GFM_OK : GFM_E_CUDA;
 }
 
-template int launch_rbp<float>(const GeoT<float>&, const Sys<float>*, const AdiScratch<float>*, int, cudaStream_t, bool);
+template int launch_rbp<float>(const GeoT<float>&, const Sys<float>*, const AdiScratch<float>*, int, cudaStream_t, int);
 template int launch_rbp<double>(const GeoT<double>&, const Sys<double>*, const AdiScratch<double>*, int, cudaStream_t,
-                                bool);
+                                int);
 
 }  // namespace gfm

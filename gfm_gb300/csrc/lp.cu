@@ -467,7 +467,7 @@ int Net::create(int nx, int ny, int nz, uint64_t seed) {
     cudaMemset(tc_err, 0, sizeof(int));
     {
         const char* w = std::getenv("GFM_LP_WAIT1");
-        tc_wait1 = w ? std::atoi(w) : 0;
+        tc_wait1 = w ? std::atoi(w) : -1;
     }
     if (prepare_tc() != GFM_OK) { err = "cannot raise the shared-memory limit of the tcgen05 convolutions"; return GFM_E_CUDA; }
     cudaMemset(g32, 0, sizeof(float) * np);

@@ -40,7 +40,7 @@ struct Net {
     // forward convolutions on tcgen05 (lp_tc.cu): weights in the operand order, expiry flag
     __nv_bfloat16* wtc[kNumLayers] = {};
     int* tc_err = nullptr;
-    int tc_wait1 = 0;                        // polls of the first bounded MMA wait (0: the default limit);
+    int tc_wait1 = -1;                       // polls of the first bounded MMA wait (<0: the default limit);
                                              // GFM_LP_WAIT1 at create, for tests of the expiry path
     float* wg_part = nullptr;                // per-chunk weight-gradient partials (fixed-order sums)
     bool use_tc = true;

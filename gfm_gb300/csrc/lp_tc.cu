@@ -236,7 +236,7 @@ void conv_tc(const Grid3& gd, const bf16* in, int in_cs, int in_co, const bf16* 
              float* out_f, int out_cs, int out_co, bool relu, int* err, int wait1, cudaStream_t st) {
     const dim3 grid((unsigned)(((gd.nx + kTcX - 1) / kTcX) * ((gd.ny + kTcY - 1) / kTcY)), (unsigned)gd.nz);
     k_conv_tc<CIN, COUT><<<grid, kTcThreads, TcShape<CIN, COUT>::SMEM, st>>>(
-        gd, in, in_cs, in_co, wtc, bias, out, out_f, out_cs, out_co, relu ? 1 : 0, err, wait1 > 0 ? wait1 : kTcWaitLimit);
+        gd, in, in_cs, in_co, wtc, bias, out, out_f, out_cs, out_co, relu ? 1 : 0, err, wait1 >= 0 ? wait1 : kTcWaitLimit);
 }
 template void conv_tc<16, 16>(const Grid3&, const bf16*, int, int, const bf16*, const float*, bf16*, float*, int, int, bool,
                               int*, int, cudaStream_t);

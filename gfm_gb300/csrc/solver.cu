@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <map>
+#include <mutex>
 #include <type_traits>
 
 #include <cuda_bf16.h>
@@ -105,6 +107,19 @@ struct gfm_handle {
     int rb_flags = kRbPlane | kRbPdl | kRbAvgInPass;   // red-black options (environment at create): GFM_RB_PLANE=0
                                                        // drops kRbPlane, GFM_PDL=0 kRbPdl, GFM_RB_AVG_IN_PASS=0
                                                        // kRbAvgInPass
+    // line-solver autotuning (red-black order): the line-solver calls of one
+    // iteration are recorded while it is captured; before the first
+    // iteration each is timed in every form on stand-in systems of its shape
+    // and the fastest form's flags are kept for it (GFM_RB_TUNE=0: no tuning)
+    struct AdiSite {
+        int nsys;
+        int rng[8][7];                  // ib, ie, jb, je, kb, ke, nim of each system
+    };
+    std::vector<AdiSite> sites;
+    bool record_sites = false, tune = true, tuned = false;
+    int adi_site = 0;                   // call index inside the iteration being issued
+    std::vector<int> site_flags;        // chosen flags per call site (empty: rb_flags)
+    std::vector<std::array<float, 3>> site_ms;   // measured ms of the three forms per call site
 };
 
 namespace {
@@ -491,8 +506,19 @@ void finish(gfm_handle* h, Ctx<R>& c, std::initializer_list<std::array<int, 3>> 
 template <typename R>
 void adi_call(gfm_handle* h, const GeoT<R>& g, const Sys<R>* sys, AdiScratch<R>* scr, int nsys, cudaStream_t st) {
     // external records: inside a captured graph these become real event nodes
+    const int site = h->adi_site++;
+    if (h->record_sites) {
+        gfm_handle::AdiSite rec{};
+        rec.nsys = nsys;
+        for (int e = 0; e < nsys; ++e) {
+            const int v[7] = {sys[e].ib, sys[e].ie, sys[e].jb, sys[e].je, sys[e].kb, sys[e].ke, sys[e].nim};
+            for (int q = 0; q < 7; ++q) rec.rng[e][q] = v[q];
+        }
+        h->sites.push_back(rec);
+    }
+    const int flags = site < (int)h->site_flags.size() ? h->site_flags[site] : h->rb_flags;
     if (h->n_ev + 2 <= 16) cudaEventRecordWithFlags(h->ev[h->n_ev], st, cudaEventRecordExternal);
-    const int launched = launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st, h->rb_flags);
+    const int launched = launch_adlbl3_scr(g, sys, scr, nsys, h->adi_mode, st, flags);
     if (h->n_ev + 2 <= 16) { cudaEventRecordWithFlags(h->ev[h->n_ev + 1], st, cudaEventRecordExternal); h->n_ev += 2; }
     int nim = 0;
     for (int e = 0; e < nsys; ++e) {
@@ -509,6 +535,7 @@ int gflow_once(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
     const GeoT<R>& g = c.g;
     const gfm_params& P = h->params;
     h->n_ev = 0;
+    h->adi_site = 0;
     h->adi_kernels_per_iter = 0;
     h->adi_cells_visits = 0;
     // iteration flags read by the kernels (device scalars, so one captured graph serves every iteration)
@@ -826,6 +853,8 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     if (ce != cudaSuccess) { h->err = cudaGetErrorString(ce); return GFM_E_CUDA; }
     if (prepare_line_solver() != GFM_OK) { h->err = "cannot raise the line solver's shared-memory limit"; return GFM_E_CUDA; }
     {
+        const char* tn = std::getenv("GFM_RB_TUNE");
+        h->tune = !(tn && tn[0] == '0');
         const char* pl = std::getenv("GFM_RB_PLANE");
         const char* pd = std::getenv("GFM_PDL");
         const char* ap = std::getenv("GFM_RB_AVG_IN_PASS");
@@ -1054,9 +1083,120 @@ int iter_finish(gfm_handle* h, int* conv) {
     }
     return GFM_OK;
 }
-int ensure_graph(gfm_handle* h) {
-    if (h->use_graph && !h->graph_exec) return capture_iteration(h);
+__global__ void k_tune_fill(float* p, long long n, float v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+__global__ void k_tune_fill(double* p, long long n, double v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        p[i] = v;
+}
+
+// Times every call site of the iteration in the three red-black forms --
+// segmented colour passes, plane visits (small planes on 256-thread CTAs),
+// plane visits on 768-thread CTAs only -- on stand-in systems with the
+// site's ranges and sweep counts (diagonally dominant, AP = 1, AS = 0.1,
+// BS = 0.1), three timed calls after one untimed, and keeps the fastest
+// form's flags for the site.  The stand-in arrays live only for the tuning.
+// Choices already made in this process, by call shape (precision, systems,
+// ranges, sweeps): a shape is timed once, so every handle of the process
+// that meets it runs the same form and gives the same bits.
+std::mutex g_tune_mu;
+std::map<std::vector<int>, std::pair<int, std::array<float, 3>>> g_tune_cache;
+
+template <typename R>
+int tune_sites(gfm_handle* h, Ctx<R>& c, AdiScratch<R>* scr) {
+    const GeoT<R>& g = c.g;
+    cudaStream_t st = h->stream;
+    int max_sys = 1;
+    for (const auto& s : h->sites) max_sys = std::max(max_sys, s.nsys);
+    const long long NS = 8LL * g.CB;
+    const int narr = 8 + max_sys;   // AP, AS x6, BS shared; one XT per system
+    R* pool = nullptr;
+    if (cudaMalloc(&pool, sizeof(R) * NS * narr) != cudaSuccess) {
+        cudaGetLastError();
+        return GFM_OK;   // no room to tune: the default forms stay
+    }
+    R* ap = pool;
+    R* as6[6];
+    for (int q = 0; q < 6; ++q) as6[q] = pool + NS * (1 + q);
+    R* bs = pool + NS * 7;
+    k_tune_fill<<<1024, 256, 0, st>>>(ap, NS, R(1));
+    k_tune_fill<<<1024, 256, 0, st>>>(as6[0], 6 * NS, R(0.1));
+    k_tune_fill<<<1024, 256, 0, st>>>(bs, NS, R(0.1));
+    k_tune_fill<<<1024, 256, 0, st>>>(pool + NS * 8, NS * max_sys, R(0));
+    const int forms[3] = {h->rb_flags & ~kRbPlane, h->rb_flags | kRbPlane | kRbSmallF64,
+                          h->rb_flags | kRbPlane | kRbNoSmall};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    h->site_flags.assign(h->sites.size(), h->rb_flags);
+    h->site_ms.assign(h->sites.size(), {0.f, 0.f, 0.f});
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (size_t k = 0; k < h->sites.size(); ++k) {
+        const auto& site = h->sites[k];
+        std::vector<int> key = {(int)sizeof(R), h->rb_flags, site.nsys};
+        for (int e = 0; e < site.nsys; ++e) key.insert(key.end(), site.rng[e], site.rng[e] + 7);
+        const auto hit = g_tune_cache.find(key);
+        if (hit != g_tune_cache.end()) {
+            h->site_flags[k] = hit->second.first;
+            h->site_ms[k] = hit->second.second;
+            continue;
+        }
+        Sys<R> sys[8];
+        for (int e = 0; e < site.nsys; ++e) {
+            const int* r = site.rng[e];
+            sys[e] = sys_of<R>(pool + NS * (8 + e), ap, as6, bs, r[0], r[1], r[2], r[3], r[4], r[5], r[6]);
+        }
+        float best = 0.f;
+        for (int f = 0; f < 3; ++f) {
+            launch_adlbl3_scr(g, sys, scr, site.nsys, h->adi_mode, st, forms[f]);
+            float ms = 1e30f;
+            for (int rep = 0; rep < 3; ++rep) {
+                cudaEventRecord(e0, st);
+                launch_adlbl3_scr(g, sys, scr, site.nsys, h->adi_mode, st, forms[f]);
+                cudaEventRecord(e1, st);
+                float t = 0.f;
+                if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess)
+                    ms = std::min(ms, t);
+            }
+            h->site_ms[k][f] = ms;
+            if (f == 0 || ms < best) {
+                best = ms;
+                h->site_flags[k] = forms[f];
+            }
+        }
+        g_tune_cache[key] = {h->site_flags[k], h->site_ms[k]};
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(pool);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    if (const char* lg = std::getenv("GFM_TUNE_LOG"); lg && lg[0] == '1')
+        for (size_t k = 0; k < h->sites.size(); ++k)
+            std::fprintf(stderr, "gfm line-solver site %zu: %d system(s), %dx%dx%d, nim %d: segmented %.3f ms, plane %.3f ms, "
+                         "plane-768 %.3f ms -> flags %d\n", k, h->sites[k].nsys,
+                         (h->sites[k].rng[0][1] - h->sites[k].rng[0][0]) / 2 + 1,
+                         (h->sites[k].rng[0][3] - h->sites[k].rng[0][2]) / 2 + 1,
+                         (h->sites[k].rng[0][5] - h->sites[k].rng[0][4]) / 2 + 1, h->sites[k].rng[0][6],
+                         h->site_ms[k][0], h->site_ms[k][1], h->site_ms[k][2], h->site_flags[k]);
     return GFM_OK;
+}
+
+int ensure_graph(gfm_handle* h) {
+    if (!h->use_graph || h->graph_exec) return GFM_OK;
+    // (GFM_RB_PLANE=0 forces the segmented passes: nothing to choose then)
+    const bool tune = h->tune && !h->tuned && h->adi_mode == GFM_ADI_REDBLACK && (h->rb_flags & kRbPlane);
+    h->record_sites = tune;
+    h->sites.clear();
+    int rc = capture_iteration(h);
+    h->record_sites = false;
+    if (rc || !tune) return rc;
+    rc = h->prec == GFM_PREC_FP64 ? tune_sites(h, h->cd, h->scr_d) : tune_sites(h, h->cf, h->scr_f);
+    if (rc) return rc;
+    h->tuned = true;
+    return capture_iteration(h);
 }
 void close_timing(gfm_handle* h) {
     cudaEventRecord(h->ev_g1, h->stream);

@@ -175,11 +175,14 @@ template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys
 // programmatic dependent launch; kRbAvgInPass lets pass L=2 of the segmented
 // form average the pass L=1 results where it reads them, in place of the
 // averaging launch between the passes
-constexpr int kRbPlane = 1, kRbPdl = 2, kRbAvgInPass = 4;
+// kRbNoSmall keeps planes that fit 8 warps on the 768-thread visit CTAs;
+// kRbSmallF64 lets small FP64 planes take the plane visit (by default they
+// take the segmented passes)
+constexpr int kRbPlane = 1, kRbPdl = 2, kRbAvgInPass = 4, kRbNoSmall = 16, kRbSmallF64 = 32;
 // the plane-visit form of one ADLBL3 call on a batch; returns the kernels it
 // launched, or 0 (nothing launched) when a plane of the batch does not fit
 template <typename R> int launch_rbp(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
-                                     cudaStream_t s, bool pdl);
+                                     cudaStream_t s, int rb_flags);
 int prepare_rbp();
 // returns the number of kernels it launched
 template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,

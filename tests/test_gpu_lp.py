@@ -65,10 +65,10 @@ def test_tcgen05_forward_matches_mma_sync_and_reference(torch, dims):
 
 def test_tcgen05_wait_expiry_is_reported_and_the_pass_completes(torch, monkeypatch):
     """The bounded wait of a tcgen05 tile for its MMAs: with the first wait cut
-    to one poll (GFM_LP_WAIT1, read at creation) it runs out, the status says
-    so (1), the tile waits again with the normal limit, and the output is the
-    same as without the cut; the launch completes and frees its tensor
-    memory (later launches still run)."""
+    to no poll at all (GFM_LP_WAIT1=0, read at creation) it runs out, the
+    status says so (1), the tile waits again with the normal limit, and the
+    output is the same as without the cut; the launch completes and frees its
+    tensor memory (later launches still run)."""
     from gfm_gb300.lp import LearnedPressure
     dims = (24, 20, 6)
     rng = np.random.default_rng(4)
@@ -79,7 +79,7 @@ def test_tcgen05_wait_expiry_is_reported_and_the_pass_completes(torch, monkeypat
     want = ref.forward(xb, dims).cpu().numpy()
     assert ref.tensor_status() == 0
     ref.close()
-    monkeypatch.setenv("GFM_LP_WAIT1", "1")
+    monkeypatch.setenv("GFM_LP_WAIT1", "0")
     lp = LearnedPressure(dims, seed=1)
     lp.set_params(p)
     got = lp.forward(xb, dims).cpu().numpy()

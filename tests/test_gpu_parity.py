@@ -108,9 +108,14 @@ def test_fp64_redblack_small_furnace_one_iteration():
         assert sg[k] == pytest.approx(so[k], rel=1e-9, abs=1e-300), k
 
 
+# With the line-solver forms timed per call site at graph capture (default)
+# and with the fixed forms (GFM_RB_TUNE=0): either choice is the same plane
+# update in the same order.
+@pytest.mark.parametrize("tune", ["1", "0"], ids=["tuned", "fixed"])
 @pytest.mark.parametrize("cfg,n", [(configs.tiny_furnace(), 10), (configs.small_furnace(), 1)],
                          ids=["tiny_10", "small_1"])
-def test_mixed_redblack_matches_the_redblack_oracle(cfg, n):
+def test_mixed_redblack_matches_the_redblack_oracle(cfg, n, tune, monkeypatch):
+    monkeypatch.setenv("GFM_RB_TUNE", tune)
     sg, so, fg, fo, mask = run_pair(cfg, n, adi=abi.GFM_ADI_REDBLACK, prec=abi.GFM_PREC_MIXED)
     err = field_errors(fg, fo, mask)
     assert max(err.values()) < MIXED_TOL, err
