@@ -51,6 +51,7 @@ class GfmGrid(C.Structure):
         ("rtim", _dp), ("delrt", _dp), ("hrt", _dp), ("delr", _dp), ("timed", _dp), ("hrd", _dp),
         ("nwl", C.c_int),
         ("wl", _dp), ("akl0", _dp),
+        ("bv_f", C.c_double * 2), ("ba_f", C.c_double * 6),
     ]
 
 

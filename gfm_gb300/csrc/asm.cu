@@ -33,10 +33,8 @@ template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return a > b
 template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return a < b ? a : b; }
 
 // ---------------------------------------------------------------------------
-// Metric functions (Grid3.f90:310-471, BV_F = BA_F = 1)
+// Metric functions (Grid3.f90:310-392; VOL_C0 and AREA_C in device.cuh)
 // ---------------------------------------------------------------------------
-template <typename R>
-__device__ __forceinline__ R vol_c0(const GeoT<R>& g, int I, int J, int K) { return g.DX[I] * g.DR[J] * g.RS[J] * g.DZ[K]; }
 
 template <typename R>
 __device__ R vol_c(const GeoT<R>& g, int I, int J, int K) {
@@ -54,13 +52,6 @@ __device__ R vol_c(const GeoT<R>& g, int I, int J, int K) {
         return vp + vm;
     }
     return vol_c0(g, I, J, K);
-}
-template <typename R>
-__device__ __forceinline__ R area_c(const GeoT<R>& g, int I, int J, int K, int ix) {
-    if (IBC(g, I, J, K) == 1) return R(0);
-    if (ix == 1) return g.DR[J] * g.RS[J] * g.DZ[K];
-    if (ix == 2) return g.DX[I] * g.DZ[K];
-    return g.DX[I] * g.DR[J] * g.RS[J];
 }
 template <typename R>
 __device__ R dxav(const GeoT<R>& g, int I, int J, int K) {

@@ -18,13 +18,6 @@ inline int gridn(long long n) {
 template <typename R> __device__ __forceinline__ R rmax2(R a, R b) { return a > b ? a : b; }
 template <typename R> __device__ __forceinline__ R rmin2(R a, R b) { return a < b ? a : b; }
 
-template <typename R>
-__device__ __forceinline__ R area_cc(const GeoT<R>& g, int I, int J, int K, int ix) {
-    if (IBC(g, I, J, K) == 1) return R(0);
-    if (ix == 1) return g.DR[J] * g.RS[J] * g.DZ[K];
-    if (ix == 2) return g.DX[I] * g.DZ[K];
-    return g.DX[I] * g.DR[J] * g.RS[J];
-}
 
 // dnst_calc at one position of the split arrays (calls CONC, Prop.f90:187-198)
 template <typename R>
@@ -55,7 +48,7 @@ __global__ void k_extr_io(Ctx<R> c) {
             // THER at the inlet keeps TMU and is overwritten in GAMA: only its eps clip survives
             c.GF[kEps][o] = rmax2(c.GF[kEps][o], R(1.0e-12));
             c.GAMA[o] = c.GAMA[o1];
-            R area = area_cc(g, e.I, e.J, e.K, e.IX);
+            R area = area_c(g, e.I, e.J, e.K, e.IX);
             R g0 = c.THETA[o] * c.DNST[o] * c.UG[e.IX - 1][o] * area;
             gfin0 += fabs((double)g0);
             continue;
@@ -75,7 +68,7 @@ __global__ void k_extr_io(Ctx<R> c) {
             c.T[o] = enth_to_t<R>(*c.nist, y, 1, y[kH], c.T[o], R(c.p.t0), R(c.p.h_0));
         }
         dnst_at(c, o);
-        R area = area_cc(g, e.I, e.J, e.K, e.IX);
+        R area = area_c(g, e.I, e.J, e.K, e.IX);
         double g0 = fabs((double)c.UG[e.IX - 1][o]) * c.p.ug0 * (double)area;
         g0 = g0 * (double)c.THETA[o] * (double)c.DNST[o] * c.p.dnst0;
         qex += (double)c.GF[kH][o] * c.p.h_0 * g0;
@@ -174,7 +167,7 @@ __global__ void k_extrv(Ctx<R> c, int mex, int first, int count) {
         else { K1 = e.K + 2 * M; K0 = e.K - M; }
         const long long o1 = pidx(g, I1, J1, K1);
         if (u[o1] * R(M) > R(0)) u[o1] = R(0);
-        R area = area_cc(g, e.I, e.J, e.K, IU);
+        R area = area_c(g, e.I, e.J, e.K, IU);
         R g0 = c.THETA[o1] * c.DNST[o1] * u[o1] * area;
         if (mex == 0) {
             gfex += fabs((double)g0);
@@ -343,7 +336,8 @@ __global__ void k_rad_emission(Ctx<R> c) {
         double T_rad = (double)c.T[o] * c.p.t0;
         if (g.ib[o] <= 0 && T_rad >= 300.0) {
             double dx = g.DX[I], dr = g.DR[J], dz = g.DZ[K];
-            double vol = dx * dr * (double)g.RS[J] * dz;
+            double vol = dx * dr * (double)g.RS[J] * dz;   // VOL_C0
+            if (g.HALF && g.ib[o] <= -1) vol = vol * (double)g.BVF[-g.ib[o] - 1];
             double sa = ((dx * dr) + (dr * dz) + (dx * dz)) * 2.0;
             double opl = sa > 1.0e-16 ? 6.0 * vol / sa : 0.0;
             if (sa > 1.0e-16 && opl > 1.0e-10) {

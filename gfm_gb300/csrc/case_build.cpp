@@ -59,6 +59,31 @@ double unit_noise(uint64_t seed, uint64_t idx, uint64_t comp) {
     return ((double)(h >> 11) * (1.0 / 9007199254740992.0)) * 2.0 - 1.0;  // [-1,1)
 }
 
+// AREA_C (Grid3.f90:411-471) on the host arrays (1-based indices): 0 on a
+// wall, times BA_F on a half-blocked cell, and on a cell with IBCELL >= 2
+// times BA_F of a half-blocked neighbour two positions away along ix
+double area_c(const CaseStore& s, int i, int j, int k, int ix) {
+    auto IB = [&](int a, int b, int c) { return (int)s.ibcell[s.at(a, b, c)]; };
+    const int ib = IB(i, j, k);
+    if (ib == 1) return 0.0;
+    double a = ix == 1 ? s.dr[j - 1] * s.rs[j - 1] * s.dz[k - 1]
+                       : ix == 2 ? s.dx[i - 1] * s.dz[k - 1] : s.dx[i - 1] * s.dr[j - 1] * s.rs[j - 1];
+    if (ib == 0) return a;
+    if (ib <= -1) return a * s.ba_f[3 * (-ib - 1) + ix - 1];
+    int nb = 0;
+    if (ix == 1) {
+        if (i <= s.mp - 2 && IB(i + 2, j, k) <= -1) nb = IB(i + 2, j, k);
+        else if (i >= 4 && IB(i - 2, j, k) <= -1) nb = IB(i - 2, j, k);
+    } else if (ix == 2) {
+        if (j <= s.np - 2 && IB(i, j + 2, k) <= -1) nb = IB(i, j + 2, k);
+        else if (j >= 4 && IB(i, j - 2, k) <= -1) nb = IB(i, j - 2, k);
+    } else {
+        if (k <= s.lp - 2 && IB(i, j, k + 2) <= -1) nb = IB(i, j, k + 2);
+        else if (k >= 4 && IB(i, j, k - 2) <= -1) nb = IB(i, j, k - 2);
+    }
+    return nb <= -1 ? a * s.ba_f[3 * (-nb - 1) + ix - 1] : a;
+}
+
 // GRID3 coordinate line (Grid3.f90:79-109): X(1..i1)=x0, then linear to
 // X(n-1)=x1 by repeated addition of DEL, X(n)=X(n-1), DX(I)=X(I+1)-X(I-1).
 void coord_line(int n, double len, std::vector<double>& x, std::vector<double>& dx) {
@@ -283,12 +308,9 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
                     prop_ther(s, P, a);
                     prop_t2h(s, P, a);
                     double g0 = s.theta[a] * s.dnst[a] * dnst0;
-                    // AREA_C(I,J,K,IU) of an open cell (Grid3.f90:412-432)
-                    double area, un;
-                    if (b.iu == 2) { area = s.dx[i - 1] * s.dz[k - 1] * area0; un = V_0; }
-                    else if (b.iu == 3) { area = s.dx[i - 1] * s.dr[j - 1] * s.rs[j - 1] * area0; un = W_0; }
-                    else { area = s.dr[j - 1] * s.rs[j - 1] * s.dz[k - 1] * area0; un = U_0; }
-                    g0 = g0 * std::fabs(un) * ug0 * area;
+                    // AREA_C(I,J,K,IU)*AREA0 of the inlet cell (Sbc.f90:138)
+                    const double un = b.iu == 2 ? V_0 : b.iu == 3 ? W_0 : U_0;
+                    g0 = g0 * std::fabs(un) * ug0 * (area_c(s, i, j, k, b.iu) * area0);
                     fr_f += g0 * GF(i, j, k, gfm::kYF);
                     fr_ox += g0 * GF(i, j, k, gfm::kYO2);
                     fr_n2 += g0 * GF(i, j, k, gfm::kYN2);
@@ -486,6 +508,8 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
     G.rtim = s.rtim.data(); G.delrt = s.delrt.data(); G.hrt = s.hrt.data();
     G.delr = s.delr.data(); G.timed = s.timed.data(); G.hrd = s.hrd.data();
     G.nwl = nwl; G.wl = s.wl.data(); G.akl0 = s.akl0.data();
+    for (int q = 0; q < 2; ++q) G.bv_f[q] = s.bv_f[q];
+    for (int q = 0; q < 6; ++q) G.ba_f[q] = s.ba_f[q];
 
     F.p = s.p.data(); F.t = s.t.data(); F.dnst = s.dnst.data(); F.theta = s.theta.data();
     F.tmu = s.tmu.data(); F.gama = s.gama.data(); F.crate = s.crate.data(); F.hrate = s.hrate.data();

@@ -176,9 +176,15 @@ bool read_namelist(TextFile& f, const char* group, Namelist& kv) {
         if (!l) return false;
         text += " " + *l;
     }
+    // element designators keep their subscripts in one token: "ba_f(1,2)"
+    // becomes "ba_f(1:2)"
     std::string spaced;
+    int depth = 0;
     for (char c : text) {
+        if (c == '(') ++depth;
+        if (c == ')' && depth > 0) --depth;
         if (c == '=') spaced += " = ";
+        else if (c == ',' && depth > 0) spaced.push_back(':');
         else spaced.push_back(c);
     }
     std::vector<std::string> tok;
@@ -293,7 +299,9 @@ int read_gd(const char* path, CaseStore& s, int& nr0) {
                     d = c - '0';
                 }
                 if (d > 5) d -= 10;   // Grid3.f90:242
-                if (d < 0) return GFM_E_UNSUPPORTED;   // half-blocked cells
+                // half-blocked cells: -1 and -2 index BV_F(2) and BA_F(3,2)
+                // (Grid3.f90:12); digits 6 and 7 would index past them
+                if (d < -2) return GFM_E_UNSUPPORTED;
                 ibc[j] = d;
             }
             for (int k = k1 + 2; k <= k2; k += 2)
@@ -303,7 +311,51 @@ int read_gd(const char* path, CaseStore& s, int& nr0) {
         }
         k1 = k2;
     }
-    // &GRD carries the half-block factors, which need no reading here
+    // &GRD: the half-block factors (Grid3.f90:252-255); absent, they stay 1
+    Namelist kv;
+    if (read_namelist(f, "GRD", kv)) {
+        for (const auto& it : kv) {
+            const std::string& key = it.first;
+            const size_t par = key.find('(');
+            const std::string name = key.substr(0, par);
+            int dims[2];
+            double* dst;
+            double bd[6];
+            if (name == "bv_f") { dims[0] = 2; dims[1] = 1; dst = s.bv_f; }
+            else if (name == "ba_f") { dims[0] = 3; dims[1] = 2; dst = s.ba_f; }
+            else if (name == "bd_f") { dims[0] = 3; dims[1] = 2; dst = bd; }   // declared, used nowhere
+            else return GFM_E_IO;
+            // first element: the subscripts of an element designator, else (1,1)
+            int sub[2] = {1, 1};
+            if (par != std::string::npos) {
+                const size_t end = key.find(')', par);
+                if (end == std::string::npos) return GFM_E_IO;
+                std::string inner = key.substr(par + 1, end - par - 1);
+                int ns = 0;
+                size_t b = 0;
+                while (b <= inner.size() && ns < 2) {
+                    size_t e = inner.find(':', b);
+                    if (e == std::string::npos) e = inner.size();
+                    int v;
+                    if (!to_int(inner.substr(b, e - b), v)) return GFM_E_IO;
+                    sub[ns++] = v;
+                    b = e + 1;
+                }
+                if (sub[0] < 1 || sub[0] > dims[0] || sub[1] < 1 || sub[1] > dims[1]) return GFM_E_IO;
+            }
+            int pos = (sub[0] - 1) + dims[0] * (sub[1] - 1);   // column-major, as Fortran stores them
+            for (const std::string& v : it.second) {
+                if (pos >= dims[0] * dims[1]) return GFM_E_IO;
+                double x;
+                if (!to_double(v, x)) return GFM_E_IO;
+                dst[pos++] = x;
+            }
+        }
+        for (int q = 0; q < 8; ++q) {
+            const double v = q < 2 ? s.bv_f[q] : s.ba_f[q - 2];
+            if (!(v > 0.0 && v < 1.0e30)) return GFM_E_IO;
+        }
+    }
     return GFM_OK;
 }
 
@@ -684,7 +736,10 @@ extern "C" int gfm_case_write_files(const gfm_case_spec* sp, const char* dir, co
         f.line("Computational and blocked cells");
         auto row = [&](int i, int k) {
             std::string t;
-            for (int j = 2; j <= np; j += 2) t.push_back((char)('0' + IB(i, j, k)));
+            for (int j = 2; j <= np; j += 2) {
+                const int v = IB(i, j, k);
+                t.push_back((char)('0' + (v < 0 ? v + 10 : v)));   // half-blocked -1, -2 as 9, 8
+            }
             return t;
         };
         auto layer = [&](int k) {

@@ -23,6 +23,10 @@ struct CaseStore {
     std::vector<double> wl, akl0;
     std::vector<double> p, t, dnst, theta, tmu, gama, crate, hrate, bs_hprev, ug, gf, qa, qe;
     std::vector<double> t_surf_prev;   // T_surf_prev(MZ,NZ) (K)
+    // half-block factors of &GRD (Grid3.f90:12-13, 252-255): BV_F(IBC) and
+    // BA_F(IX,IBC) at ba_f[3*(IBC-1) + IX-1]
+    double bv_f[2] = {1.0, 1.0};
+    double ba_f[6] = {1.0, 1.0, 1.0, 1.0, 1.0, 1.0};
     long at(int i, int j, int k) const { return (i - 1) + (long)mp * ((j - 1) + (long)np * (k - 1)); }
     long n() const { return (long)mp * np * lp; }
 };

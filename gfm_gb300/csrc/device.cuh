@@ -33,6 +33,10 @@ struct GeoT {
     int NCELLS;
     const R *X, *DX, *Rr, *DR, *RS, *Z, *DZ;
     const int8_t* ib;          // IBCELL, parity split
+    // half-blocked cells (IBCELL -1, -2): BV_F(IBC), BA_F(IX,IBC) at
+    // BAF[3*(IBC-1) + IX-1]; HALF is 0 when the grid has none
+    R BVF[2], BAF[6];
+    int HALF;
 };
 using Geo = GeoT<double>;
 
@@ -49,6 +53,42 @@ __host__ __device__ __forceinline__ long long pidx(const GeoT<R>& g, int I, int 
     for (int t = blockIdx.x * blockDim.x + threadIdx.x, t##_end = (int)(n); t < t##_end; t += gridDim.x * blockDim.x)
 template <typename R>
 __device__ __forceinline__ int IBC(const GeoT<R>& g, int I, int J, int K) { return g.ib[pidx(g, I, J, K)]; }
+
+// VOL_C0 (Grid3.f90:395-405): the cell's volume, times BV_F on a
+// half-blocked cell
+template <typename R>
+__device__ __forceinline__ R vol_c0(const GeoT<R>& g, int I, int J, int K) {
+    const R v = g.DX[I] * g.DR[J] * g.RS[J] * g.DZ[K];
+    if (g.HALF) {
+        const int ib = IBC(g, I, J, K);
+        if (ib <= -1) return v * g.BVF[-ib - 1];
+    }
+    return v;
+}
+// AREA_C (Grid3.f90:411-471): the face area normal to direction ix of the
+// cell; 0 on a wall, times BA_F on a half-blocked cell, and on a cell with
+// IBCELL >= 2 times BA_F of a half-blocked neighbour two positions away
+// along ix (the + side first)
+template <typename R>
+__device__ __forceinline__ R area_c(const GeoT<R>& g, int I, int J, int K, int ix) {
+    const int ib = IBC(g, I, J, K);
+    if (ib == 1) return R(0);
+    const R a = ix == 1 ? g.DR[J] * g.RS[J] * g.DZ[K] : ix == 2 ? g.DX[I] * g.DZ[K] : g.DX[I] * g.DR[J] * g.RS[J];
+    if (!g.HALF || ib == 0) return a;
+    if (ib <= -1) return a * g.BAF[3 * (-ib - 1) + ix - 1];
+    int nb = 0;
+    if (ix == 1) {
+        if (I <= g.MPM2 && IBC(g, I + 2, J, K) <= -1) nb = IBC(g, I + 2, J, K);
+        else if (I >= 4 && IBC(g, I - 2, J, K) <= -1) nb = IBC(g, I - 2, J, K);
+    } else if (ix == 2) {
+        if (J <= g.NPM2 && IBC(g, I, J + 2, K) <= -1) nb = IBC(g, I, J + 2, K);
+        else if (J >= 4 && IBC(g, I, J - 2, K) <= -1) nb = IBC(g, I, J - 2, K);
+    } else {
+        if (K <= g.LPM2 && IBC(g, I, J, K + 2) <= -1) nb = IBC(g, I, J, K + 2);
+        else if (K >= 4 && IBC(g, I, J, K - 2) <= -1) nb = IBC(g, I, J, K - 2);
+    }
+    return nb <= -1 ? a * g.BAF[3 * (-nb - 1) + ix - 1] : a;
+}
 
 // Programmatic dependent launch.  A kernel launched by launch_k with pdl set
 // may begin (block scheduling, prologue) while the kernel before it in the

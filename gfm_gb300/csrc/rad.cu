@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict_
         for (int l = 0; l < a.NWL; ++l) { a.akl[c + (long long)l * n] = 0.0; a.qel0[c + (long long)l * n] = 0.0; }
         if (!(a.ibr[c] <= 0 && t >= kTgMn)) continue;
         const double dx = a.g.DX[I], dr = a.g.DR[J], dz = a.g.DZ[K];
-        const double vol = dx * dr * a.g.RS[J] * dz;                  // VOL_C at a cell centre (VOL_C0)
+        double vol = dx * dr * a.g.RS[J] * dz;                        // VOL_C at a cell centre (VOL_C0)
+        if (a.g.HALF && a.ibr[c] <= -1) vol = vol * a.g.BVF[-a.ibr[c] - 1];
         const double sa = ((dx * dr) + (dr * dz) + (dx * dz)) * 2.0;
         if (sa <= kSmall16) continue;
         const double opl = 6.0 * vol / sa;

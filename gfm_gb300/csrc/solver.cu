@@ -38,6 +38,8 @@ struct HostGrid {
     int MP, NP, LP;
     std::vector<int16_t> ib;   // doubled layout
     std::vector<double> X, DX, R, DR, RS, Z, DZ;   // 1-based
+    double bvf[2], baf[6];     // half-block factors BV_F, BA_F
+    int half;                  // the grid has half-blocked cells
     int at(int i, int j, int k) const { return ib[(i - 1) + (long)MP * ((j - 1) + (long)NP * (k - 1))]; }
 };
 
@@ -421,6 +423,9 @@ int setup_ctx(gfm_handle* h, Ctx<R>& c, GeoT<R>& g, AdiScratch<R>* scr, const gf
     g.NJY1V[1] = 4; g.NJY2V[1] = g.NPM2; g.NJY1V[2] = 5; g.NJY2V[2] = hg.NP - 3; g.NJY1V[3] = 4; g.NJY2V[3] = g.NPM2;
     g.LKZ1V[1] = 4; g.LKZ2V[1] = g.LPM2; g.LKZ1V[2] = 4; g.LKZ2V[2] = g.LPM2; g.LKZ1V[3] = 5; g.LKZ2V[3] = hg.LP - 3;
     g.NCELLS = h->ncells;
+    for (int q = 0; q < 2; ++q) g.BVF[q] = R(hg.bvf[q]);
+    for (int q = 0; q < 6; ++q) g.BAF[q] = R(hg.baf[q]);
+    g.HALF = hg.half;
     int rc;
     if ((rc = up1(hg.X, &g.X)) || (rc = up1(hg.DX, &g.DX)) || (rc = up1(hg.R, &g.Rr)) || (rc = up1(hg.DR, &g.DR)) ||
         (rc = up1(hg.RS, &g.RS)) || (rc = up1(hg.Z, &g.Z)) || (rc = up1(hg.DZ, &g.DZ)))
@@ -842,8 +847,19 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     hg.MP = gr->mp; hg.NP = gr->np; hg.LP = gr->lp;
     h->N = (long long)hg.MP * hg.NP * hg.LP;
     hg.ib.assign(gr->ibcell, gr->ibcell + h->N);
-    for (long long i = 0; i < h->N; ++i)
-        if (hg.ib[i] < 0 || hg.ib[i] > 20) { h->err = "IBCELL: half-blocked cells are not supported"; return GFM_E_UNSUPPORTED; }
+    // half-blocked cells carry IBCELL -1 or -2, the two entries of BV_F and
+    // BA_F (Grid3.f90:12); lower values would index past them
+    hg.half = 0;
+    for (long long i = 0; i < h->N; ++i) {
+        if (hg.ib[i] < -2 || hg.ib[i] > 20) { h->err = "IBCELL outside -2..20"; return GFM_E_UNSUPPORTED; }
+        if (hg.ib[i] < 0) hg.half = 1;
+    }
+    for (int q = 0; q < 2; ++q) hg.bvf[q] = gr->bv_f[q];
+    for (int q = 0; q < 6; ++q) hg.baf[q] = gr->ba_f[q];
+    for (int q = 0; q < 8; ++q) {
+        const double v = q < 2 ? hg.bvf[q] : hg.baf[q - 2];
+        if (!(v > 0.0 && v < 1.0e30)) { h->err = "half-block factors BV_F, BA_F must be positive"; return GFM_E_ARG; }
+    }
     auto one_based = [](const double* s, int n) { std::vector<double> v(n + 3, 0.0); for (int i = 0; i < n; ++i) v[i + 1] = s[i]; return v; };
     hg.X = one_based(gr->x, hg.MP); hg.DX = one_based(gr->dx, hg.MP);
     hg.R = one_based(gr->r, hg.NP); hg.DR = one_based(gr->dr, hg.NP); hg.RS = one_based(gr->rs, hg.NP);
@@ -866,6 +882,9 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     // double geometry first: its int8 map is shared by the float copy
     GeoT<double>& g = h->gd;
     g.MP = hg.MP; g.NP = hg.NP; g.LP = hg.LP;
+    for (int q = 0; q < 2; ++q) g.BVF[q] = hg.bvf[q];
+    for (int q = 0; q < 6; ++q) g.BAF[q] = hg.baf[q];
+    g.HALF = hg.half;
     g.HX = hg.MP / 2 + 1; g.HY = hg.NP / 2 + 1; g.HZ = hg.LP / 2 + 1;
     g.PX = ((g.HX + 15) / 16) * 16;
     g.CB = (long long)g.PX * g.HY * g.HZ;

@@ -78,6 +78,12 @@ typedef struct gfm_grid {
     /* gray radiation bands: edges WL (m) and absorption coefficients (1/m) */
     int nwl;
     const double *wl, *akl0;
+    /* half-blocked cells, IBCELL = -1 or -2 (gd digits 9 and 8): the volume
+     * factor BV_F(IBC) and the face-area factors BA_F(IX,IBC), stored at
+     * ba_f[3*(IBC-1) + IX-1], read from &GRD (Grid3.f90:12-13,252-255) and
+     * applied by VOL_C0 and AREA_C (Grid3.f90:395-471); 1 when absent */
+    double bv_f[2];
+    double ba_f[6];
 } gfm_grid;
 
 /* ---- scalar constants of module GBL_VAR after SETUP ---------------------- */
@@ -249,8 +255,10 @@ typedef struct gfm_case_summary {
 
 /* GRID3 + SETUP + SBC + INITSV (fresh start or restart) from the case files:
  * the start-up a Fortran host does before the first GFLOW
- * (A0main.f90:158-190).  Parse errors return GFM_E_IO; cell maps with
- * half-blocked cells (IBCELL<0, Grid3.f90:236) and two-phase cases return
+ * (A0main.f90:158-190).  Parse errors return GFM_E_IO.  Half-blocked cells
+ * (digits 9 and 8, IBCELL -1 and -2) are read with the &GRD factors BV_F
+ * and BA_F into the grid; digits 7 and 6 (IBCELL -3, -4, past the two
+ * entries of BV_F, Grid3.f90:12) and two-phase cases return
  * GFM_E_UNSUPPORTED.  summary may be NULL. */
 int  gfm_case_read(const gfm_case_files *files, const gfm_case_options *opt,
                    gfm_case *out, gfm_case_summary *summary);

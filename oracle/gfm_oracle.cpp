@@ -208,6 +208,7 @@ struct Oracle {
     double P_REF;
     vec X, DX, R, DR, RS, Z, DZ;   // 1-based (index 0 unused)
     std::vector<int16_t> IBC;
+    double BV_F[3], BA_F[4][3];    // COMMON /GRD1/ (Grid3.f90:12), 1-based: BV_F(IBC), BA_F(IX,IBC)
     vec P, T, DNST, THETA, TMU, GAMA, CRATE, HRATE, GTE, FZ, BS, SFP, AP, bs_hprev, UG, GF, AS, QA, QE;
     gfm_params pr;
     double RFC[21], RFLC[21];
@@ -258,7 +259,15 @@ struct Oracle {
         if (ibcell(I, J, K + 2) >= 1) return Z[K + 2] - Z[K - 1];
         return DZ[K];
     }
-    double VOL_C0(int I, int J, int K) { return DX[I] * DR[J] * RS[J] * DZ[K]; }   // BV_F=1
+    // VOL_C0 (Grid3.f90:395-405)
+    double VOL_C0(int I, int J, int K) {
+        double VOL = DX[I] * DR[J] * RS[J] * DZ[K];
+        if (ibcell(I, J, K) <= -1) {
+            int IBCX = -ibcell(I, J, K);
+            VOL = VOL * BV_F[IBCX];
+        }
+        return VOL;
+    }
     double VOL_C(int I, int J, int K) {
         double VOL;
         if ((I / 2) * 2 != I) {
@@ -278,11 +287,30 @@ struct Oracle {
         }
         return VOL;
     }
-    double AREA_C(int I, int J, int K, int IXD) {   // BA_F=1
+    // AREA_C (Grid3.f90:411-471)
+    double AREA_C(int I, int J, int K, int IXD) {
         if (ibcell(I, J, K) == 1) return ZERO;
-        if (IXD == 1) return DR[J] * RS[J] * DZ[K];
-        if (IXD == 2) return DX[I] * DZ[K];
-        return DX[I] * DR[J] * RS[J];
+        double AREA;
+        if (IXD == 1) AREA = DR[J] * RS[J] * DZ[K];
+        else if (IXD == 2) AREA = DX[I] * DZ[K];
+        else AREA = DX[I] * DR[J] * RS[J];
+        if (ibcell(I, J, K) == 0) return AREA;
+        if (ibcell(I, J, K) <= -1) return AREA * BA_F[IXD][-ibcell(I, J, K)];
+        int IBCX;
+        if (IXD == 1) {
+            if (I <= MPM2 && ibcell(I + 2, J, K) <= -1) IBCX = -ibcell(I + 2, J, K);
+            else if (I >= 4 && ibcell(I - 2, J, K) <= -1) IBCX = -ibcell(I - 2, J, K);
+            else return AREA;
+        } else if (IXD == 2) {
+            if (J <= NPM2 && ibcell(I, J + 2, K) <= -1) IBCX = -ibcell(I, J + 2, K);
+            else if (J >= 4 && ibcell(I, J - 2, K) <= -1) IBCX = -ibcell(I, J - 2, K);
+            else return AREA;
+        } else {
+            if (K <= LPM2 && ibcell(I, J, K + 2) <= -1) IBCX = -ibcell(I, J, K + 2);
+            else if (K >= 4 && ibcell(I, J, K - 2) <= -1) IBCX = -ibcell(I, J, K - 2);
+            else return AREA;
+        }
+        return AREA * BA_F[IXD][IBCX];
     }
 
     // ---- Prop.f90 per-position wrappers --------------------------------------
@@ -2380,6 +2408,10 @@ void* gfo_create(const gfm_grid* g, const gfm_params* p, const gfm_fields* f) {
     o->R = one_based(g->r, o->NP); o->DR = one_based(g->dr, o->NP); o->RS = one_based(g->rs, o->NP);
     o->Z = one_based(g->z, o->LP); o->DZ = one_based(g->dz, o->LP);
     o->IBC.assign(g->ibcell, g->ibcell + o->N);
+    for (int b = 1; b <= 2; ++b) {
+        o->BV_F[b] = g->bv_f[b - 1];
+        for (int ixd = 1; ixd <= 3; ++ixd) o->BA_F[ixd][b] = g->ba_f[3 * (b - 1) + ixd - 1];
+    }
     for (int i = 0; i < g->b_cnt; ++i) {
         o->b_typ.push_back(g->b_typ[i]); o->b_i.push_back(g->b_i[i]); o->b_j.push_back(g->b_j[i]); o->b_k.push_back(g->b_k[i]);
         o->b_orient.push_back(g->b_orient[i]); o->b_direct.push_back(g->b_direct[i]); o->b_T.push_back(g->b_t[i]);
@@ -2926,6 +2958,8 @@ int gfo_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* 
     G.rtim = s.rtim.data(); G.delrt = s.delrt.data(); G.hrt = s.hrt.data();
     G.delr = s.delr.data(); G.timed = s.timed.data(); G.hrd = s.hrd.data();
     G.nwl = sp->nwl; G.wl = s.wl.data(); G.akl0 = s.akl0.data();
+    for (int q = 0; q < 2; ++q) G.bv_f[q] = 1.0;   // GRID3 defaults (Grid3.f90:252-254)
+    for (int q = 0; q < 6; ++q) G.ba_f[q] = 1.0;
     F.p = s.p.data(); F.t = s.t.data(); F.dnst = s.dnst.data(); F.theta = s.theta.data();
     F.tmu = s.tmu.data(); F.gama = s.gama.data(); F.crate = s.crate.data(); F.hrate = s.hrate.data();
     F.bs_hprev = s.bs_hprev.data(); F.ug = s.ug.data(); F.gf = s.gf.data(); F.qa = s.qa.data(); F.qe = s.qe.data();

@@ -310,12 +310,18 @@ def test_bad_inputs_fail_loudly(case_dir, tmp_path):
     with pytest.raises(GfmError) as e:
         Case.from_files(d, "0041", restart=True)              # no rg file in this directory
     assert e.value.rc == abi.GFM_E_IO
-    # a half-blocked cell (digit 9 -> IBCELL=-1) is outside the supported set
+    # digit 7 (IBCELL=-3) would index past BV_F(2) and BA_F(3,2)
     gd = (d / "gd0041c.dat").read_text()
-    (d / "gd0041c.dat").write_text(gd.replace("  36  110000000000000000000011", "  36  110000000009000000000011", 1))
+    (d / "gd0041c.dat").write_text(gd.replace("  36  110000000000000000000011", "  36  110000000007000000000011", 1))
     with pytest.raises(GfmError) as e:
         Case.from_files(d, "0041")
     assert e.value.rc == abi.GFM_E_UNSUPPORTED
+    # an unknown name in &GRD, and a subscript outside BA_F(3,2)
+    for grd in ("&GRD\n BX_F=1.0\n/", "&GRD\n BA_F(4,1)=0.5\n/"):
+        (d / "gd0041c.dat").write_text(gd.replace("&GRD\n/", grd))
+        with pytest.raises(GfmError) as e:
+            Case.from_files(d, "0041")
+        assert e.value.rc == abi.GFM_E_IO
     # the pressure reference must be an inlet cell
     (d / "gd0041c.dat").write_text(gd)
     sbc = (d / "sbc0041c.dat").read_text()
@@ -479,3 +485,47 @@ def test_fortran_input_spellings_read_the_same(tmp_path):
         with pytest.raises(GfmError) as err:
             Case.from_files(e, "0041")
         assert err.value.rc == abi.GFM_E_IO, name
+
+
+HALF_ROW = ("  36  110000000000000000000011", "  36  119800000000000000000011")
+HALF_GRD = "&GRD\n BV_F=0.5, 0.75\n BA_F(1,1)=0.5,0.625, 0.75 BA_F(1,2)=2*0.875,\n 0.9375\n BD_F=6*1.0\n/"
+
+
+def half_blocked_dir(case_dir, d):
+    """TC21 case 0041 with half-blocked cells: on the first layer that row
+    describes, J=6 becomes IBCELL -1 (digit 9) and J=8 IBCELL -2 (digit 8),
+    next to the J=4 wall, with &GRD factors BV_F = (0.5, 0.75) and
+    BA_F = ((0.5, 0.625, 0.75), (0.875, 0.875, 0.9375)) given in the
+    namelist's element, list and repeat forms."""
+    d.mkdir(exist_ok=True)
+    for n in INPUTS:
+        shutil.copyfile(case_dir / n, d / n)
+    gd = (d / "gd0041c.dat").read_text()
+    assert HALF_ROW[0] in gd and "&GRD\n/" in gd
+    (d / "gd0041c.dat").write_text(gd.replace(HALF_ROW[0], HALF_ROW[1], 1).replace("&GRD\n/", HALF_GRD))
+    return d
+
+
+def test_half_blocked_cells_and_grd_factors_are_read(case_dir, tmp_path):
+    """Digits 9 and 8 of the cell map are IBCELL -1 and -2 (Grid3.f90:242);
+    &GRD sets BV_F and BA_F (Grid3.f90:252-255).  A half-blocked cell counts
+    as a computational cell (Grid3.f90:259-268) and spreads nothing to its
+    faces."""
+    plain = Case.from_files(case_dir, "0041")
+    case = Case.from_files(half_blocked_dir(case_dir, tmp_path / "half"), "0041")
+    ib0, ib = plain.ibcell(), case.ibcell()
+    diff = np.argwhere(ib != ib0)
+    assert len(diff) > 0
+    assert set(np.unique(ib[ib != ib0])) == {-1, -2}
+    assert set(np.unique(ib0[ib != ib0])) == {0}
+    # the changed positions are cell centres (even doubled indices), J = 6 or 8
+    k, j, i = diff.T + 1
+    assert np.all(i % 2 == 0) and np.all(j % 2 == 0) and np.all(k % 2 == 0)
+    assert set(j) == {6, 8}
+    assert np.all(ib[k - 1, j - 1, i - 1] == np.where(j == 6, -1, -2))
+    assert case.grid.ncells == plain.grid.ncells
+    g = case.grid
+    assert list(g.bv_f) == [0.5, 0.75]
+    assert list(g.ba_f) == [0.5, 0.625, 0.75, 0.875, 0.875, 0.9375]
+    assert list(plain.grid.bv_f) == [1.0, 1.0] and list(plain.grid.ba_f) == [1.0] * 6
+

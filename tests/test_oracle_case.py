@@ -67,3 +67,35 @@ def test_oracle_runs_from_its_own_start_up():
     assert sa["res_mass"] == pytest.approx(sb["res_mass"], rel=1e-12)
     for k in ("p", "t", "ug"):
         assert np.allclose(fa.arrays[k], fb.arrays[k], rtol=1e-11, atol=1e-14), k
+
+
+def test_oracle_half_blocked_factors_take_effect(tmp_path):
+    """The oracle's VOL_C0 and AREA_C scale by BV_F and BA_F: one iteration
+    of TC21 case 0041 with half-blocked cells moves with the factors, and
+    stays finite."""
+    import shutil
+    from gfm_gb300 import Case
+    from .test_case_files import GOLD, INPUTS, half_blocked_dir
+    src = tmp_path / "src"
+    src.mkdir()
+    for n in INPUTS:
+        shutil.copyfile(GOLD / n, src / n)
+    d = half_blocked_dir(src, tmp_path / "half")
+    ones = tmp_path / "ones"
+    ones.mkdir()
+    for n in INPUTS:
+        shutil.copyfile(d / n, ones / n)
+    gd = (ones / "gd0041c.dat").read_text()
+    start = gd.index("&GRD")
+    (ones / "gd0041c.dat").write_text(gd[:start] + "&GRD\n/\n")
+    res = []
+    for dd in (d, ones):
+        o = Oracle(Case.from_files(dd, "0041"))
+        o.initsv()
+        st = o.gflow(1)[0]
+        f = o.download()
+        o.close()
+        assert np.all(np.isfinite(f.arrays["p"])) and np.all(np.isfinite(f.arrays["t"]))
+        res.append((st["res_mass"], f.arrays["p"].copy()))
+    assert res[0][0] != res[1][0]
+    assert not np.array_equal(res[0][1], res[1][1])
