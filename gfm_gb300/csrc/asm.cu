@@ -620,7 +620,7 @@ __global__ void k_qconv(Ctx<R> c) {
 // radiation term, the wall sink gathered per cell in patch order and the
 // source relaxation with bs_hprev (Source.f90:269-522).
 template <typename R, int L>
-__global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
+__global__ void k_scalar_assemble(Ctx<R> c, Range rg) {
     __shared__ double sh[32];
     const GeoT<R>& g = c.g;
     const R zero = R(0);
@@ -629,7 +629,6 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
     R* bs_out = c.BSs[L - 1];
     R* as_set[6];
     for (int q = 0; q < 6; ++q) as_set[q] = c.ASs[c.as_set[L - 1]][q];
-    const R sgm = R(c.p.sigma[L - 1]);
     const R* fz = c.GF[L - 1];
     long long n = rg.count();
     double qreact = 0.0;
@@ -724,30 +723,12 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
             // blocked cells keep AP=1, AS=0 and BS=FZ (GSLV3V reset / SOURCE)
             ap_out[o] = R(1);
             bs_out[o] = bs;
-            if (new_as) for (int q = 0; q < 6; ++q) as_set[q][o] = zero;
             continue;
         }
         if (NELG == 8) c.BSH[o] = bs;   // bs_hprev = bs (Source.f90:520)
-        // ---- GSLV3G0 --------------------------------------------------------------
+        // ---- GSLV3G0: AP from the six coefficients (k_scalar_faces) ----------------
         R ap = zero;
-        for (int IU = 1; IU <= 3; ++IU)
-            for (int M = -1; M <= 1; M += 2) {
-                int M1 = (M + 3) / 2;
-                int q = (IU - 1) * 2 + (M1 - 1);
-                R a;
-                if (new_as) {
-                    int I1 = I + (IU == 1 ? M : 0), J1 = J + (IU == 2 ? M : 0), K1 = K + (IU == 3 ? M : 0);
-                    int I2 = I1 + (IU == 1 ? M : 0), J2 = J1 + (IU == 2 ? M : 0), K2 = K1 + (IU == 3 ? M : 0);
-                    int ibc0 = IBC(g, I2, J2, K2);
-                    if (ibc0 <= 0) a = flwd(c, I1, J1, K1, IU, M1, sgm);
-                    else if (ibc0 == 2) a = flw(c, I2, J2, K2, IU, M1);
-                    else a = zero;
-                    as_set[q][o] = a;
-                } else {
-                    a = as_set[q][o];
-                }
-                ap = ap + a;
-            }
+        for (int q = 0; q < 6; ++q) ap = ap + as_set[q][o];
         // ---- relaxation (Gslv3g.f90:64-87) -----------------------------------------
         if (fabs(ap) <= R(1.0e-20)) { ap_out[o] = R(1); bs_out[o] = fz[o]; continue; }
         R vol = vol_c(g, I, J, K);
@@ -761,6 +742,67 @@ __global__ void k_scalar_assemble(Ctx<R> c, Range rg, int new_as) {
     if (NELG == 8) {
         double s = block_sum(qreact, sh);
         if (threadIdx.x == 0) c.partials[5 * kRedBlocks + blockIdx.x] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// GSLV3G0's six neighbour coefficients of the scalar equations (Gslv3g.f90:
+// 30-47 with FLWD/FLW, Gslv3x.f90:292-329), evaluated once per face.  The
+// reference forms them per cell, so every interior face's flux f and
+// diffusion conductance, and the DA weight of the pair, are evaluated by
+// both cells that share it; here one thread per face (blockIdx.y = direction
+// IU) evaluates them once and writes the coefficient of the cell on each
+// side: AS(C-, IU, +) = DA + max(0,-f), AS(C+, IU, -) = DA + max(0,f), or
+// FLW at an inlet neighbour, or 0 at a blocked one, as each cell would.  The
+// values are the cell-wise ones bit for bit.  Cells outside the solved range
+// are not written; blocked cells in it get 0.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_scalar_faces(Ctx<R> c, Range cr, int set, R sgm) {
+    const GeoT<R>& g = c.g;
+    const int IU = (int)blockIdx.y + 1;
+    R* const* as_set = c.ASs[set];
+    // faces of direction IU: the cell range widened by one face on each end
+    const int fi0 = IU == 1 ? cr.i0 - 1 : cr.i0, fi1 = IU == 1 ? cr.i1 + 1 : cr.i1;
+    const int fj0 = IU == 2 ? cr.j0 - 1 : cr.j0, fj1 = IU == 2 ? cr.j1 + 1 : cr.j1;
+    const int fk0 = IU == 3 ? cr.k0 - 1 : cr.k0, fk1 = IU == 3 ? cr.k1 + 1 : cr.k1;
+    const Range fr{fi0, fi1, fj0, fj1, fk0, fk1};
+    const int ex = IU == 1, ey = IU == 2, ez = IU == 3;
+    const long long n = fr.count();
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        int I, J, K;
+        fr.at((int)t, I, J, K);
+        const int Im = I - ex, Jm = J - ey, Km = K - ez, Ip = I + ex, Jp = J + ey, Kp = K + ez;
+        const bool in_m = IU == 1 ? Im >= cr.i0 : IU == 2 ? Jm >= cr.j0 : Km >= cr.k0;
+        const bool in_p = IU == 1 ? Ip <= cr.i1 : IU == 2 ? Jp <= cr.j1 : Kp <= cr.k1;
+        const int ib_m = IBC(g, Im, Jm, Km), ib_p = IBC(g, Ip, Jp, Kp);
+        const bool want_m = in_m && ib_m < 1, want_p = in_p && ib_p < 1;
+        R dsum = R(0), f = R(0);
+        if ((want_m && ib_p <= 0) || (want_p && ib_m <= 0)) {
+            // FLWD's flux and conductance at the face, DA once
+            const R area = area_c(g, I, J, K, IU);
+            const R ddl = IU == 1 ? g.DX[I] : (IU == 2 ? g.DR[J] : g.DZ[K]);
+            f = A(c.THETA, I, J, K) * A(c.DNST, I, J, K) * A(c.UG[IU - 1], I, J, K) * area;
+            const R diff = A(c.THETA, I, J, K) * A(c.GAMA, I, J, K) / sgm * area / ddl;
+            dsum = da<R>(diff, f);
+        }
+        // the cell on the - side: its + neighbour is the cell on the + side
+        if (in_m) {
+            R a = R(0);
+            if (want_m) {
+                if (ib_p <= 0) a = dsum + rmax(R(0), -f);
+                else if (ib_p == 2) a = flw(c, Ip, Jp, Kp, IU, 2);
+            }
+            as_set[(IU - 1) * 2 + 1][pidx(g, Im, Jm, Km)] = a;
+        }
+        if (in_p) {
+            R a = R(0);
+            if (want_p) {
+                if (ib_m <= 0) a = dsum + rmax(R(0), f);
+                else if (ib_m == 2) a = flw(c, Im, Jm, Km, IU, 1);
+            }
+            as_set[(IU - 1) * 2][pidx(g, Ip, Jp, Kp)] = a;
+        }
     }
 }
 
@@ -932,15 +974,16 @@ template <typename R> void launch_scalar_sources_first(const Ctx<R>& c, cudaStre
 template <typename R> void launch_scalar_assemble(const Ctx<R>& c, int L, bool new_as, cudaStream_t s) {
     Range r = cell_range(c);
     int nb = grid_for(r.count());
-    int na = new_as ? 1 : 0;
+    // the coefficient set of equal sigma, face by face, before its first equation
+    if (new_as) k_scalar_faces<R><<<dim3(nb, 3), kBlock, 0, s>>>(c, r, c.as_set[L - 1], R(c.p.sigma[L - 1]));
     switch (L) {
-        case 1: k_scalar_assemble<R, 1><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 2: k_scalar_assemble<R, 2><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 3: k_scalar_assemble<R, 3><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 4: k_scalar_assemble<R, 4><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 5: k_scalar_assemble<R, 5><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 6: k_scalar_assemble<R, 6><<<nb, kBlock, 0, s>>>(c, r, na); break;
-        case 7: k_scalar_assemble<R, 7><<<nb, kBlock, 0, s>>>(c, r, na); break;
+        case 1: k_scalar_assemble<R, 1><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 2: k_scalar_assemble<R, 2><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 3: k_scalar_assemble<R, 3><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 4: k_scalar_assemble<R, 4><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 5: k_scalar_assemble<R, 5><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 6: k_scalar_assemble<R, 6><<<nb, kBlock, 0, s>>>(c, r); break;
+        case 7: k_scalar_assemble<R, 7><<<nb, kBlock, 0, s>>>(c, r); break;
     }
     // FZ(L) <- GF(L) for the solve: class 0 block
     k_copy_centres<R><<<grid_for(c.g.CB), kBlock, 0, s>>>(c.GF[L - 1], c.FZs[L - 1], c.g.CB);
