@@ -166,9 +166,37 @@ class GfmRestartTail(C.Structure):
     ]
 
 
+MAX_EXHAUSTS = 16
+
+
+class GfmWallSpec(C.Structure):
+    _fields_ = [
+        ("eps_w", C.c_double), ("eps_c", C.c_double), ("eps_m", C.c_double),
+        ("have_crown", C.c_int), ("height_to_ceiling", C.c_double),
+        ("maxri1", C.c_int), ("maxri2", C.c_int), ("minri2", C.c_int),
+        ("t_a", C.c_double), ("h_a", C.c_double), ("w_k", C.c_double), ("w_d", C.c_double),
+        ("t_mnk", C.c_double),
+        ("nex", C.c_int),
+    ] + [(n, C.c_int * MAX_EXHAUSTS) for n in ("exh_i1", "exh_j1", "exh_k1", "exh_i2", "exh_j2", "exh_k2",
+                                                "exh_orient", "exh_direct", "exh_type")] + [
+        ("exh_frac", C.c_double * MAX_EXHAUSTS), ("exh_fixed", C.c_double * MAX_EXHAUSTS),
+    ]
+
+
+class GfmWallTotals(C.Structure):
+    _fields_ = [("b_cnt", C.c_int), ("sweeps", C.c_int), ("outer", C.c_int), ("reserved", C.c_int)] + [
+        (n, C.c_double) for n in ("avg_wall_T", "q_melt", "q_wall_loss", "q_incident_total", "q_incident_wall",
+                                  "q_incident_inlet", "q_incident_exit", "q_incident_melt", "qconv_total",
+                                  "q_rad_inlet", "q_rad_outlet", "qm_flame", "qm_bnds", "qm_conv",
+                                  "rel_rad_chg_mean")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_ if n != "reserved"}
+
+
 class GfmCase(C.Structure):
     _fields_ = [("grid", GfmGrid), ("params", GfmParams), ("fields", GfmFields), ("priv", C.c_void_p),
-                ("tail", GfmRestartTail)]
+                ("tail", GfmRestartTail), ("wall", GfmWallSpec)]
 
 
 class GfmCaseFiles(C.Structure):
@@ -217,6 +245,9 @@ SIGNATURES = [
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("gfm_gpu_rad_emission", C.c_int, [C.c_void_p]),
     ("gfm_gpu_rad_transfer", C.c_int, [C.c_void_p, C.POINTER(GfmRadTotals)]),
+    ("gfm_gpu_wall_setup", C.c_int, [C.c_void_p, C.POINTER(GfmWallSpec)]),
+    ("gfm_gpu_wall_totals", C.c_int, [C.c_void_p, C.POINTER(GfmWallTotals)]),
+    ("gfm_gpu_wall_get", C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_int]),
     ("gfm_gpu_kernel_times", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     ("gfm_gpu_reset_kernel_times", C.c_int, [C.c_void_p]),
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),

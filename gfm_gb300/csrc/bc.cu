@@ -91,8 +91,11 @@ __device__ void extr_wall_one(const Ctx<R>& c, const ExtrRec& e) {
     c.P[o] = c.P[o1] * R(e.F1) + c.P[o2] * R(e.F2);
     c.TMU[o] = c.TMU[o2];
     c.GAMA[o] = c.GAMA[o2];
-    for (int L = 1; L <= 7; ++L) c.GF[L - 1][o] = c.GF[L - 1][o1];
-    c.T[o] = c.T[o1];   // walls adiabatic until a first full radiation call
+    // walls adiabatic until a first full radiation call (Extr.f90:194-197)
+    const bool adiabatic = c.scal[S_RAD_DONE] == 0.0;
+    for (int L = 1; L <= 7; ++L)
+        if (L - 1 != kH || adiabatic) c.GF[L - 1][o] = c.GF[L - 1][o1];
+    if (adiabatic) c.T[o] = c.T[o1];
     dnst_at(c, o);
 }
 
@@ -125,8 +128,11 @@ __global__ void k_extr_ft_apply(Ctx<R> c) {
         c.P[o] = v[0];
         c.TMU[o] = v[1];
         c.GAMA[o] = v[2];
-        for (int L = 1; L <= 7; ++L) c.GF[L - 1][o] = v[2 + L];
-        c.T[o] = v[10];   // walls adiabatic until a first full radiation call
+        // walls adiabatic until a first full radiation call (Extr.f90:194-197)
+        const bool adiabatic = c.scal[S_RAD_DONE] == 0.0;
+        for (int L = 1; L <= 7; ++L)
+            if (L - 1 != kH || adiabatic) c.GF[L - 1][o] = v[2 + L];
+        if (adiabatic) c.T[o] = v[10];
         dnst_at(c, o);
     }
 }

@@ -445,9 +445,78 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
                 }
     }
 
-    // ---- wall patches (Qwall.f90:395-513); b_T is the fixed wall temperature
-    // for wall patches and the melt-cell temperature for melt-surface patches
-    // (Rad_emis.f90:196-210); the sink reads no other patch temperature
+    // ---- boundary patches (prepare_for_wall_radiation_calculation,
+    // Qwall.f90:54-520).  The cell map is copied to MAPB and each exit's
+    // tunnel through the wall is closed: the exit moves to the tunnel's inner
+    // end and the rest of the tunnel becomes wall (steps 1-2, Qwall.f90:72-
+    // 346).  Patches are the faces with MAPB >= 1 next to an open position
+    // (steps 3-5, Qwall.f90:395-513).  b_T is the fixed wall temperature for
+    // wall patches and the melt-cell temperature for melt-surface patches
+    // (Rad_emis.f90:196-210); the wall sink reads no other patch temperature.
+    std::vector<int16_t> mapb(s.ibcell);
+    auto MB = [&](int i, int j, int k) -> int16_t& { return mapb[s.at(i, j, k)]; };
+    auto fill = [&](int ia, int ib, int ja, int jb, int ka, int kb, int16_t v) {
+        for (int i = ia; i <= ib; ++i)
+            for (int j = ja; j <= jb; ++j)
+                for (int k = ka; k <= kb; ++k) MB(i, j, k) = v;
+    };
+    // extent of an exit from one corner: the last position of the run of 3s
+    // along one axis (the reference leaves the end unset when the run reaches
+    // the grid's edge; it then ends there)
+    auto run_end = [&](int i, int j, int k, int di, int dj, int dk, int lim) {
+        int a = i, b = j, c = k;
+        for (;;) {
+            const int n = (di ? a : dj ? b : c) + 2;
+            if (n > lim) return n - 2;
+            if (MB(a + 2 * di, b + 2 * dj, c + 2 * dk) != 3) return n - 2;
+            a += 2 * di; b += 2 * dj; c += 2 * dk;
+        }
+    };
+    for (int face = 0; face < 5; ++face) {
+        // back (i=2), front (i=MP), sides (j=2, j=NP) and top (k=LP) walls
+        const int ax = face < 2 ? 0 : face < 4 ? 1 : 2;
+        const bool lo = face == 0 || face == 2;
+        const int fixed = ax == 0 ? (lo ? 2 : mp) : ax == 1 ? (lo ? 2 : np) : lp;
+        const int na = ax == 0 ? np : mp, nb = ax == 2 ? np : lp;   // the two other axes
+        for (int u = 2; u <= na; u += 2)
+            for (int v = 2; v <= nb; v += 2) {
+                int i, j, k;
+                if (ax == 0) { i = fixed; j = u; k = v; } else if (ax == 1) { i = u; j = fixed; k = v; } else { i = u; j = v; k = fixed; }
+                if (MB(i, j, k) != 3) continue;
+                // the exit's rectangle in the wall plane
+                int a0, a1, b0, b1;
+                if (ax == 0) { a0 = j; a1 = run_end(i, j, k, 0, 1, 0, np); b0 = k; b1 = run_end(i, j, k, 0, 0, 1, lp); }
+                else if (ax == 1) { a0 = i; a1 = run_end(i, j, k, 1, 0, 0, mp); b0 = k; b1 = run_end(i, j, k, 0, 0, 1, lp); }
+                else { a0 = i; a1 = run_end(i, j, k, 1, 0, 0, mp); b0 = j; b1 = run_end(i, j, k, 0, 1, 0, np); }
+                // the interior end: the first layer in from the wall where a
+                // position diagonally outside a corner of the rectangle is open
+                const int n = ax == 0 ? mp : ax == 1 ? np : lp;
+                auto open_at = [&](int w) {
+                    // positions past the grid's edge count as closed
+                    auto at = [&](int p, int q) -> int {
+                        int i = w, j = p, k = q;
+                        if (ax == 1) { i = p; j = w; k = q; } else if (ax == 2) { i = p; j = q; k = w; }
+                        if (i < 1 || i > mp || j < 1 || j > np || k < 1 || k > lp) return 1;
+                        return MB(i, j, k);
+                    };
+                    return at(a0 - 2, b0 - 2) == 0 || at(a1 + 2, b1 + 2) == 0 || at(a0 - 2, b1 + 2) == 0 ||
+                           at(a1 + 2, b0 - 2) == 0;
+                };
+                int wnew = -1;
+                if (lo) {
+                    for (int w = 4; w <= n; w += 2) if (open_at(w)) { wnew = w - 2; break; }
+                } else {
+                    for (int w = n - 2; w >= 2; w -= 2) if (open_at(w)) { wnew = w + 2; break; }
+                }
+                if (wnew < 0) continue;   // no inner end: the map stays as read
+                // exit at the inner end (two positions), wall in the rest of the tunnel
+                int e0 = lo ? wnew : wnew - 1, e1 = lo ? wnew + 1 : wnew;
+                int w0 = lo ? 2 : wnew + 1, w1 = lo ? wnew - 1 : n;
+                if (ax == 0) { fill(e0, e1, a0, a1, b0, b1, 3); fill(w0, w1, a0, a1, b0, b1, 1); }
+                else if (ax == 1) { fill(a0, a1, e0, e1, b0, b1, 3); fill(a0, a1, w0, w1, b0, b1, 1); }
+                else { fill(a0, a1, b0, b1, e0, e1, 3); fill(a0, a1, b0, b1, w0, w1, 1); }
+            }
+    }
     auto add_patch = [&](int typ, int ori, int dir, int i, int j, int k) {
         s.b_typ.push_back((int16_t)typ); s.b_orient.push_back((int16_t)ori); s.b_direct.push_back((int16_t)dir);
         s.b_i.push_back((int16_t)i); s.b_j.push_back((int16_t)j); s.b_k.push_back((int16_t)k);
@@ -463,26 +532,26 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
     for (int k = 2; k <= lp; k += 2)
         for (int j = 2; j <= np; j += 2)
             for (int i = 3; i <= mp - 1; i += 2) {
-                int m = IB(i, j, k);
+                int m = MB(i, j, k);
                 if (m < 1) continue;
-                if (IB(i - 1, j, k) > 0 && IB(i + 1, j, k) > 0) continue;
-                add_patch(m, 1, IB(i + 1, j, k) == 0 ? 0 : 1, i, j, k);
+                if (MB(i - 1, j, k) > 0 && MB(i + 1, j, k) > 0) continue;
+                add_patch(m, 1, MB(i + 1, j, k) == 0 ? 0 : 1, i, j, k);
             }
     for (int k = 2; k <= lp; k += 2)
         for (int j = 3; j <= np - 1; j += 2)
             for (int i = 2; i <= mp; i += 2) {
-                int m = IB(i, j, k);
+                int m = MB(i, j, k);
                 if (m < 1) continue;
-                if (IB(i, j - 1, k) > 0 && IB(i, j + 1, k) > 0) continue;
-                add_patch(m, 2, IB(i, j + 1, k) == 0 ? 0 : 1, i, j, k);
+                if (MB(i, j - 1, k) > 0 && MB(i, j + 1, k) > 0) continue;
+                add_patch(m, 2, MB(i, j + 1, k) == 0 ? 0 : 1, i, j, k);
             }
     for (int k = 3; k <= lp - 1; k += 2)
         for (int j = 2; j <= np; j += 2)
             for (int i = 2; i <= mp; i += 2) {
-                int m = IB(i, j, k);
+                int m = MB(i, j, k);
                 if (m < 1) continue;
-                if (IB(i, j, k - 1) > 0 && IB(i, j, k + 1) > 0) continue;
-                add_patch(m, 3, IB(i, j, k + 1) == 0 ? 0 : 1, i, j, k);
+                if (MB(i, j, k - 1) > 0 && MB(i, j, k + 1) > 0) continue;
+                add_patch(m, 3, MB(i, j, k + 1) == 0 ? 0 : 1, i, j, k);
             }
 
     // ---- kinetics table and radiation bands -----------------------------------
@@ -510,6 +579,7 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
     G.nwl = nwl; G.wl = s.wl.data(); G.akl0 = s.akl0.data();
     for (int q = 0; q < 2; ++q) G.bv_f[q] = s.bv_f[q];
     for (int q = 0; q < 6; ++q) G.ba_f[q] = s.ba_f[q];
+    out->wall = in.wall;
 
     F.p = s.p.data(); F.t = s.t.data(); F.dnst = s.dnst.data(); F.theta = s.theta.data();
     F.tmu = s.tmu.data(); F.gama = s.gama.data(); F.crate = s.crate.data(); F.hrate = s.hrate.data();
@@ -597,6 +667,16 @@ int synth_inputs(const gfm_case_spec* sp, CaseStore& s, CaseInputs& in) {
         snap(sp->exit_z0, sp->exit_z1, hz, sp->nz, fz, cz);
         for (int k = 2 * fz + 2; k <= 2 * (fz + cz - 1) + 2; k += 2)
             for (int j = 2 * fy + 2; j <= 2 * (fy + cy - 1) + 2; j += 2) IB(mp, j, k) = 3;
+        // the flue's exhaust entry: x-normal patches facing -x, at a fixed
+        // 1473 K (the flue temperature of the shipped TC21 case 0041)
+        gfm_wall_spec& w = in.wall;
+        w.nex = 1;
+        w.exh_i1[0] = mp; w.exh_j1[0] = 2 * fy + 2; w.exh_k1[0] = 2 * fz + 2;
+        w.exh_i2[0] = mp; w.exh_j2[0] = 2 * (fy + cy - 1) + 2; w.exh_k2[0] = 2 * (fz + cz - 1) + 2;
+        w.exh_orient[0] = 1; w.exh_direct[0] = 1; w.exh_type[0] = 1;
+        w.exh_frac[0] = 0.9; w.exh_fixed[0] = 1473.0;
+        w.eps_c = 0.9;   // crown emissivity of the synthetic furnace
+        w.have_crown = 0;
     }
 
     // ---- SETUP inputs --------------------------------------------------------

@@ -398,13 +398,23 @@ int read_sbc(const char* path, CaseInputs& in, SbcExtra& ex) {
         b.u = st[7]; b.v = st[8]; b.w = st[9];
         in.inlets.push_back(b);
     }
-    // exhausts (Sbc.f90:273-284): read for the record; the sink does not use them
+    // exhausts (Sbc.f90:273-284): box, then orientation, direction, type
+    // (0: a fraction of the mean wall T, else fixed), fraction, fixed T
     if (!f.next()) return GFM_E_IO;   // "Exhausts:"
     if (!read_ints(f, 1, &ex.n_exh) || ex.n_exh < 0 || ex.n_exh > 100000) return GFM_E_IO;
+    if (ex.n_exh > GFM_MAX_EXHAUSTS) return GFM_E_UNSUPPORTED;
+    in.wall.nex = ex.n_exh;
     for (int n = 0; n < ex.n_exh; ++n) {
         int e6[6];
-        double e5[5];
-        if (!read_ints(f, 6, e6) || !read_doubles(f, 5, e5)) return GFM_E_IO;
+        if (!read_ints(f, 6, e6)) return GFM_E_IO;
+        std::vector<std::string> v;
+        if (!read_list(f, 5, v)) return GFM_E_IO;
+        gfm_wall_spec& w = in.wall;
+        w.exh_i1[n] = e6[0]; w.exh_j1[n] = e6[1]; w.exh_k1[n] = e6[2];
+        w.exh_i2[n] = e6[3]; w.exh_j2[n] = e6[4]; w.exh_k2[n] = e6[5];
+        if (!to_int(v[0], w.exh_orient[n]) || !to_int(v[1], w.exh_direct[n]) || !to_int(v[2], w.exh_type[n]) ||
+            !to_double(v[3], w.exh_frac[n]) || !to_double(v[4], w.exh_fixed[n]))
+            return GFM_E_IO;
     }
     // wall properties up to a row of zeros (Sbc.f90:290-313)
     if (!f.next()) return GFM_E_IO;   // "Wall Properties:"
@@ -422,6 +432,15 @@ int read_sbc(const char* path, CaseInputs& in, SbcExtra& ex) {
     ex.nwl = 1;
     in.ri = 1.0; in.h_g = 10.0;
     if (!nl_int(rk, "nwl", ex.nwl) || !nl_double(rk, "ri", in.ri) || !nl_double(rk, "h_g", in.h_g)) return GFM_E_IO;
+    {
+        gfm_wall_spec& w = in.wall;
+        if (!nl_double(rk, "t_a", w.t_a) || !nl_double(rk, "h_a", w.h_a) || !nl_double(rk, "w_k", w.w_k) ||
+            !nl_double(rk, "w_d", w.w_d) || !nl_double(rk, "eps_w", w.eps_w) || !nl_double(rk, "eps_m", w.eps_m) ||
+            !nl_double(rk, "eps_c", w.eps_c) || !nl_int(rk, "have_crown", w.have_crown) ||
+            !nl_double(rk, "height_to_ceiling", w.height_to_ceiling) || !nl_int(rk, "maxri1", w.maxri1) ||
+            !nl_int(rk, "maxri2", w.maxri2) || !nl_int(rk, "minri2", w.minri2))
+            return GFM_E_IO;
+    }
     if (ex.nwl < 1 || ex.nwl > 16) return GFM_E_UNSUPPORTED;
     in.wl_m.resize(ex.nwl);
     if (!read_doubles(f, ex.nwl, in.wl_m.data())) return GFM_E_IO;

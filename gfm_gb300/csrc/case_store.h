@@ -69,6 +69,17 @@ struct CaseInputs {
     // restart file, NULL for a fresh start
     const char* rg_path = nullptr;
     int interval_rad = 100, initial_gitr = 100;
+    // wall radiation inputs: &RADIN and the exhaust table of the SBC file
+    gfm_wall_spec wall = wall_defaults();
+    static gfm_wall_spec wall_defaults() {   // Sbc.f90:317-331, T_mnK (Var_mod.f90:45)
+        gfm_wall_spec w{};
+        w.eps_w = 0.8; w.eps_c = 0.8; w.eps_m = 0.95;
+        w.have_crown = 0; w.height_to_ceiling = 0.0;
+        w.maxri1 = 100; w.maxri2 = 1000; w.minri2 = 4;
+        w.t_a = 350.0; w.h_a = 5.0; w.w_k = 2.0; w.w_d = 0.31;
+        w.t_mnk = 200.0;
+        return w;
+    }
 };
 
 // The synthetic furnace of a gfm_case_spec as the inputs a case directory

@@ -122,6 +122,20 @@ struct gfm_handle {
     int adi_site = 0;                   // call index inside the iteration being issued
     std::vector<int> site_flags;        // chosen flags per call site (empty: rb_flags)
     std::vector<std::array<float, 3>> site_ms;   // measured ms of the three forms per call site
+    // wall radiosity exchange (gfm_gpu_wall_setup): the case's patch list,
+    // the device data, and the state that carries from one exchange to the next
+    std::vector<int16_t> bp_typ, bp_i, bp_j, bp_k, bp_ori, bp_dir;
+    Patch* d_patches = nullptr;         // the wall-sink patches (b_T written by the exchange)
+    bool wall_on = false;
+    gfm_wall_spec wspec{};
+    WallArgs wall{};
+    std::vector<int> wall_typ;
+    double wall_area_total = 0;
+    int wall_first = 1, iterw = 0, wall_frac_exits = 0;
+    int* d_frac_exit = nullptr;
+    double* d_frac = nullptr;
+    double avg_wall_T = 1600.0, q_melt = 0.0;   // Qwall.f90:68; q_melt starts at zero
+    gfm_wall_totals wall_last{};        // results of the last exchange
 };
 
 namespace {
@@ -937,6 +951,10 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     c.extrv = e4;
     for (int d = 0; d < 3; ++d) c.n_extrv[d] = nev[d];
     c.patch = pp; c.cell_patch_start = i2; c.cell_patch_list = i3; c.n_patch = (int)patches.size();
+    h->d_patches = pp;
+    h->bp_typ.assign(gr->b_typ, gr->b_typ + gr->b_cnt); h->bp_i.assign(gr->b_i, gr->b_i + gr->b_cnt);
+    h->bp_j.assign(gr->b_j, gr->b_j + gr->b_cnt); h->bp_k.assign(gr->b_k, gr->b_k + gr->b_cnt);
+    h->bp_ori.assign(gr->b_orient, gr->b_orient + gr->b_cnt); h->bp_dir.assign(gr->b_direct, gr->b_direct + gr->b_cnt);
     c.intp_mode = im;
     if ((rc = dalloc(h, &c.scal, S_NUM + 128)) || (rc = dalloc(h, &c.partials, (long long)kRedSlots * kRedBlocks)) ||
         (rc = dalloc(h, &h->d_stage, h->N)) || (rc = dalloc(h, &h->d_bad, 1)))
@@ -1347,6 +1365,251 @@ int rad_prepare(gfm_handle* h, const RadArgs& in) {
 }
 }  // namespace
 
+namespace {
+
+// the sum of one slot of the exchange's block partials, in block order
+double wall_slot(const std::vector<double>& part, int slot) {
+    double s = 0.0;
+    for (int b = 0; b < kWallBlocks; ++b) s += part[(size_t)slot * kWallBlocks + b];
+    return s;
+}
+int wall_read(gfm_handle* h, std::vector<double>& part) {
+    part.resize((size_t)kWallSlots * kWallBlocks);
+    CK(cudaMemcpyAsync(part.data(), h->wall.part, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return GFM_OK;
+}
+
+// The exchange after a volume transfer: RAD_EMIS's patch temperatures
+// (Rad_emis.f90:186-273), wall_q_amb, then wallq's loops (Qwall.f90:990-
+// 1245), with T normalised throughout (T*T0 is formed where the reference
+// reads T in K).  The loop control runs on the host from sums read back after
+// each sweep.
+template <typename R>
+int wall_exchange(gfm_handle* h, Ctx<R>& c, gfm_wall_totals* tot) {
+    WallArgs& a = h->wall;
+    const gfm_wall_spec& w = h->wspec;
+    cudaStream_t st = h->stream;
+    std::vector<double> part;
+    int rc;
+    launch_wall_start<R>(a, c.T, h->wall_first, st);
+    launch_wall_init<R>(a, c.QA, c.QE, st);
+    launch_wall_qamb(a, st);
+    if ((rc = wall_read(h, part))) return rc;
+    gfm_wall_totals t{};
+    t.q_incident_total = wall_slot(part, W_INC_TOTAL); t.q_incident_wall = wall_slot(part, W_INC_WALL);
+    t.q_incident_inlet = wall_slot(part, W_INC_INLET); t.q_incident_exit = wall_slot(part, W_INC_EXIT);
+    t.q_incident_melt = wall_slot(part, W_INC_MELT);
+    const double tol = 1.0e-10;   // wall_radiosity_tolerance, radiation_boundary_tolerance
+    int nn = 1, nnextra = w.maxri1, outer = 0;
+    double rel_mean = 0.0;
+    while (nn <= w.maxri1 && nn <= nnextra) {
+        const int minradi = w.minri2;
+        // calc_q_conv_wall: the wall sink's kernel on the exchange's temperatures
+        launch_wall_to_sink(a, h->d_patches, st);
+        launch_qconv(c, st);
+        launch_wall_from_sink<R>(a, c.qconv, st);
+        int n = 1, nextra = w.maxri2;
+        while (n <= w.maxri2 && n <= nextra) {
+            launch_wall_sweep(a, st);
+            std::swap(a.J, a.Jn);
+            ++h->iterw;
+            double rel = 0.0;
+            CK(cudaMemcpyAsync(part.data() + (size_t)W_REL * kWallBlocks, a.part + (size_t)W_REL * kWallBlocks,
+                               kWallBlocks * sizeof(double), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            rel = wall_slot(part, W_REL);
+            rel_mean = rel / a.nb;
+            if (rel_mean < tol && n > minradi && nextra == w.maxri2) nextra = n + 3;
+            ++n;
+        }
+        const double prev_q_melt = h->q_melt;
+        launch_wall_rad(a, 1 << 4, st);
+        launch_wall_temps(a, st);
+        launch_wall_qamb(a, st);
+        if ((rc = wall_read(h, part))) return rc;
+        h->q_melt = wall_slot(part, W_Q_MELT);
+        t.q_wall_loss = wall_slot(part, W_Q_LOSS);
+        t.qconv_total = wall_slot(part, W_QCONV);
+        const double chg = std::fabs((prev_q_melt - h->q_melt) / (h->q_melt + 1.0e-16));
+        if (chg < tol && nnextra == w.maxri1) nnextra = nn + 1;
+        ++outer;
+        ++nn;
+    }
+    // after the loops: wall T into the field, inlet, outlet and melt totals
+    launch_wall_rad(a, (1 << 2) | (1 << 3) | (1 << 4), st);
+    launch_wall_post<R>(a, c.T, st);
+    if ((rc = wall_read(h, part))) return rc;
+    h->avg_wall_T = wall_slot(part, W_T_AREA) / h->wall_area_total;
+    if (h->wall_frac_exits) launch_wall_exits(a, h->d_frac_exit, h->d_frac, h->avg_wall_T, st);
+    launch_wall_to_sink(a, h->d_patches, st);   // the gas solve's wall sink reads the new b_T
+    const double one = 1.0;
+    CK(cudaMemcpyAsync(c.scal + S_RAD_DONE, &one, sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+    h->wall_first = 0;
+    t.b_cnt = a.nb;
+    t.sweeps = h->iterw;
+    t.outer = outer;
+    t.avg_wall_T = h->avg_wall_T;
+    t.q_melt = h->q_melt;
+    t.q_rad_inlet = wall_slot(part, W_Q_RAD_IN);
+    t.q_rad_outlet = wall_slot(part, W_Q_RAD_OUT);
+    t.qm_flame = wall_slot(part, W_QM_FLAME);
+    t.qm_bnds = wall_slot(part, W_QM_BNDS);
+    t.qm_conv = wall_slot(part, W_QM_CONV);
+    t.rel_rad_chg_mean = rel_mean;
+    if (tot) *tot = t;
+    return GFM_OK;
+}
+
+}  // namespace
+
+// Boundary-patch data of the exchange (prepare_for_wall_radiation_calculation
+// steps 5-8, Qwall.f90:395-736) from the case's patch list, and the view
+// factors on the device.
+extern "C" int gfm_gpu_wall_setup(gfm_handle* h, const gfm_wall_spec* spec) {
+    if (!h || !spec) return GFM_E_ARG;
+    if (h->wall_on) { h->err = "wall exchange: already set up"; return GFM_E_ARG; }
+    if (spec->nex < 0 || spec->nex > GFM_MAX_EXHAUSTS || spec->maxri1 < 1 || spec->maxri2 < 1 || spec->eps_w <= 0.0 ||
+        spec->eps_c <= 0.0 || spec->eps_m <= 0.0) {
+        h->err = "wall exchange: inputs out of range";
+        return GFM_E_ARG;
+    }
+    const int nb = (int)h->bp_typ.size();
+    if (nb < 2) { h->err = "wall exchange: fewer than two boundary patches"; return GFM_E_ARG; }
+    const HostGrid& g = h->hg;
+    std::vector<int> typ(nb), bi(nb), bj(nb), bk(nb), ori(nb), dir(nb), o_bc(nb), o_b(nb), sink(nb), exh(nb, 0),
+        frac_exit(nb, 0);
+    std::vector<int> bci(nb), bcj(nb), bck(nb);
+    std::vector<double> px(nb), py(nb), pz(nb), emis(nb), area(nb), face(nb), bt_exit(nb, 0.0), frac(nb, 0.0);
+    int ns = 0;
+    h->wall_area_total = 0.0;
+    for (int n = 0; n < nb; ++n) {
+        typ[n] = h->bp_typ[n]; bi[n] = h->bp_i[n]; bj[n] = h->bp_j[n]; bk[n] = h->bp_k[n];
+        ori[n] = h->bp_ori[n]; dir[n] = h->bp_dir[n];
+        const int s = dir[n] == 0 ? -1 : 1;   // the closed cell is behind the face
+        bci[n] = bi[n] + (ori[n] == 1 ? s : 0);
+        bcj[n] = bj[n] + (ori[n] == 2 ? s : 0);
+        bck[n] = bk[n] + (ori[n] == 3 ? s : 0);
+        o_bc[n] = (int)pidx(h->gd, bci[n], bcj[n], bck[n]);
+        o_b[n] = (int)pidx(h->gd, bi[n], bj[n], bk[n]);
+        px[n] = g.X[bi[n]]; py[n] = g.R[bj[n]]; pz[n] = g.Z[bk[n]];
+        area[n] = ori[n] == 1 ? g.DR[bj[n]] * g.DZ[bk[n]] : ori[n] == 2 ? g.DX[bi[n]] * g.DZ[bk[n]] : g.DX[bi[n]] * g.DR[bj[n]];
+        if (typ[n] == 1) {
+            const int ktop = ori[n] == 3 ? g.LP - 1 : g.LP;
+            emis[n] = (g.Z[bk[n]] >= spec->height_to_ceiling || (bk[n] == ktop && spec->have_crown == 0)) ? spec->eps_c
+                                                                                                              : spec->eps_w;
+            h->wall_area_total += area[n];
+        } else {
+            emis[n] = typ[n] == 4 && ori[n] == 3 ? spec->eps_m : 1.0;
+        }
+        sink[n] = (typ[n] == 1 || typ[n] == 4) ? ns++ : -1;
+        if (typ[n] == 3) {
+            // the exhaust the patch belongs to (step 6, Qwall.f90:534-557)
+            for (int m = 0; m < spec->nex && !exh[n]; ++m) {
+                if (ori[n] != spec->exh_orient[m] || dir[n] != spec->exh_direct[m]) continue;
+                const bool in = ori[n] == 1 ? (bcj[n] >= spec->exh_j1[m] && bcj[n] <= spec->exh_j2[m] && bck[n] >= spec->exh_k1[m] && bck[n] <= spec->exh_k2[m])
+                              : ori[n] == 2 ? (bci[n] >= spec->exh_i1[m] && bci[n] <= spec->exh_i2[m] && bck[n] >= spec->exh_k1[m] && bck[n] <= spec->exh_k2[m])
+                                            : (bci[n] >= spec->exh_i1[m] && bci[n] <= spec->exh_i2[m] && bcj[n] >= spec->exh_j1[m] && bcj[n] <= spec->exh_j2[m]);
+                if (in) exh[n] = m + 1;
+            }
+            if (!exh[n]) { h->err = "wall exchange: an exit patch outside every exhaust"; return GFM_E_ARG; }
+            const int m = exh[n] - 1;
+            bt_exit[n] = spec->exh_type[m] == 0 ? spec->exh_frac[m] * h->avg_wall_T : spec->exh_fixed[m];
+            frac_exit[n] = spec->exh_type[m] == 0;
+            frac[n] = spec->exh_frac[m];
+            if (frac_exit[n]) h->wall_frac_exits = 1;
+        }
+    }
+    if (ns != h->cd.n_patch) { h->err = "wall exchange: patch list differs from the wall sink's"; return GFM_E_ARG; }
+    if (h->wall_area_total <= 0.0) { h->err = "wall exchange: no wall patches"; return GFM_E_ARG; }
+    // step 8: the face area of the patches on one cell, with the reference's
+    // chain of same-cell links as it is written (Qwall.f90:684-736)
+    {
+        std::vector<int> c1(nb + 1, 0), c2(nb + 1, 0), c3(nb + 1, 0), c4(nb + 1, 0);   // 1-based, 0 = none
+        auto same = [&](int n, int m) { return bci[n - 1] == bci[m - 1] && bcj[n - 1] == bcj[m - 1] && bck[n - 1] == bck[m - 1]; };
+        for (int n = 1; n <= nb; ++n)
+            for (int m = n + 1; m <= nb; ++m) {
+                if (!same(n, m)) continue;
+                if (c1[n] == 0) { c1[n] = m; c1[m] = n; }
+                else if (c2[n] == 0) {
+                    if (c1[n] == m) continue;
+                    c2[n] = m; c1[m] = n; c2[m] = c1[n]; c2[c1[n]] = m;
+                } else if (c3[n] == 0) {
+                    if (c1[n] == m || c2[n] == m) continue;
+                    c3[n] = m; c1[m] = n; c2[m] = c1[n]; c3[c2[n]] = m; c3[m] = c2[n];
+                } else if (c4[n] == 0) {
+                    if (c1[n] == m || c2[n] == m || c3[n] == m) continue;
+                    c4[n] = m; c1[m] = n; c2[m] = c1[n]; c4[c2[n]] = m; c3[m] = c2[n]; c4[c3[n]] = m; c4[m] = c3[n];
+                }
+            }
+        for (int n = 1; n <= nb; ++n) {
+            double f = area[n - 1];
+            const int links[4] = {c1[n], c2[n], c3[n], c4[n]};
+            for (int q = 0; q < 4 && links[q]; ++q) f = f + area[links[q] - 1];
+            face[n - 1] = f;
+        }
+    }
+    WallArgs a{};
+    a.nb = nb;
+    int* ip[10];
+    const std::vector<int>* iv[10] = {&typ, &bi, &bj, &bk, &ori, &dir, &o_bc, &o_b, &sink, &frac_exit};
+    double* dp[7];
+    const std::vector<double>* dv[7] = {&px, &py, &pz, &emis, &area, &face, &bt_exit};
+    int rc;
+    for (int q = 0; q < 10; ++q) if ((rc = dupload(h, &ip[q], *iv[q]))) return rc;
+    for (int q = 0; q < 7; ++q) if ((rc = dupload(h, &dp[q], *dv[q]))) return rc;
+    a.typ = ip[0]; a.bi = ip[1]; a.bj = ip[2]; a.bk = ip[3]; a.ori = ip[4]; a.dir = ip[5];
+    a.o_bc = ip[6]; a.o_b = ip[7]; a.sink = ip[8]; h->d_frac_exit = ip[9];
+    a.px = dp[0]; a.py = dp[1]; a.pz = dp[2]; a.emis = dp[3]; a.area = dp[4]; a.face_area = dp[5]; a.bT_exit = dp[6];
+    if ((rc = dupload(h, &h->d_frac, frac))) return rc;
+    double* work[9];
+    for (int q = 0; q < 9; ++q) if ((rc = dalloc(h, &work[q], nb))) return rc;
+    a.bT = work[0]; a.J = work[1]; a.Jn = work[2]; a.qc = work[3]; a.qeb = work[4]; a.qconv = work[5];
+    a.qamb = work[6]; a.rad = work[7]; a.rel = work[8];
+    if ((rc = dalloc(h, &a.part, (long long)kWallSlots * kWallBlocks))) return rc;
+    // the view factors: FP64 on the FP64 path, FP32 on the mixed one
+    const size_t vf_bytes = (size_t)nb * nb * (h->prec == GFM_PREC_FP64 ? 8 : 4);
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    if (vf_bytes + ((size_t)1 << 30) > free_b) { h->err = "wall exchange: view factors exceed device memory"; return GFM_E_NOMEM; }
+    if (h->prec == GFM_PREC_FP64) { if ((rc = dalloc(h, &a.vf64, (long long)nb * nb))) return rc; }
+    else if ((rc = dalloc(h, &a.vf32, (long long)nb * nb))) return rc;
+    a.sig = h->params.sig;
+    const double t2 = spec->t_mnk * spec->t_mnk;
+    a.radi_min = h->params.sig * (t2 * t2);   // Setup.f90:214
+    a.t0 = h->params.t0;
+    a.u_a0 = (spec->w_k < 1.0e-20 || spec->h_a < 1.0e-20) ? 0.0 : 1.0 / (spec->w_d / spec->w_k + 1.0 / spec->h_a);
+    a.t_a = spec->t_a;
+    a.t_mnk = spec->t_mnk;
+    if ((rc = launch_wall_vf(a, h->stream))) { h->err = "wall exchange: view-factor launch"; return rc; }
+    CK(cudaStreamSynchronize(h->stream));
+    h->wall = a;
+    h->wspec = *spec;
+    h->wall_typ = typ;
+    h->wall_on = true;
+    return GFM_OK;
+}
+
+extern "C" int gfm_gpu_wall_totals(gfm_handle* h, gfm_wall_totals* out) {
+    if (!h || !out || !h->wall_on) return GFM_E_ARG;
+    *out = h->wall_last;
+    return GFM_OK;
+}
+
+extern "C" int gfm_gpu_wall_get(gfm_handle* h, const char* name, double* out, int cap) {
+    if (!h || !name || !out || !h->wall_on) return GFM_E_ARG;
+    const WallArgs& a = h->wall;
+    if (cap < a.nb) return GFM_E_ARG;
+    const std::string s(name);
+    const double* src = s == "b_t" ? a.bT : s == "radiosity" ? a.J : s == "q_amb" ? a.qamb : s == "q_conv" ? a.qconv
+                      : s == "qc" ? a.qc : s == "qeb" ? a.qeb : s == "emis" ? a.emis : s == "b_face_area" ? a.face_area
+                      : s == "patch_area" ? a.area : nullptr;
+    if (!src) return GFM_E_ARG;
+    CK(cudaMemcpy(out, src, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
+    return a.nb;
+}
+
 extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
     if (!h) return GFM_E_ARG;
     const Ctx<double>& cdb = h->cd;
@@ -1394,6 +1657,12 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
         return GFM_E_UNSUPPORTED;
     }
     h->rad_active = 1;
+    if (h->wall_on) {
+        // the wall exchange of QRNF (Qrn.f90:209-211)
+        rc = h->prec == GFM_PREC_FP64 ? wall_exchange<double>(h, h->cd, &h->wall_last)
+                                      : wall_exchange<float>(h, h->cf, &h->wall_last);
+        if (rc) return rc;
+    }
     if (out) {
         std::memset(out, 0, sizeof *out);
         for (int b = 0; b < parts; ++b) {   // x-, y-, z-direction CTAs, each in CTA order

@@ -36,7 +36,9 @@ enum Scal {
     S_Q_REACT, S_Q_EXHAUST, S_QCONV, S_TAVE, S_P_RESID_PRE, S_P_RESID, S_PCORR_RESID,
     S_U_RESID_PRE, S_U_RESID = S_U_RESID_PRE + 3, S_GF_RESID_PRE = S_U_RESID + 3, S_GF_RESID = S_GF_RESID_PRE + 10,
     S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_RAD_ACTIVE,
-    S_LP_SCALE, S_LP_USED, S_LP_RATIO, S_LP_ALPHA, S_LP_TSCALE, S_NUM
+    S_LP_SCALE, S_LP_USED, S_LP_RATIO, S_LP_ALPHA, S_LP_TSCALE,
+    S_RAD_DONE,   // i1st_rad_done: a wall exchange has run, EXTR keeps wall h and T (Extr.f90:194-197)
+    S_NUM
 };
 
 template <typename R>
@@ -106,6 +108,40 @@ struct AdiScratch {
     R *xs, *x2, *x3, *sby, *sbz, *x2b, *x3b;
     Quad<R> *ya, *yb, *za, *zb;
 };
+
+// ---- wall radiosity exchange (wall.cu) -----------------------------------------
+constexpr int kWallBlocks = 128;   // blocks of the per-patch kernels (fixed: their partial sums add in block order)
+constexpr int kWallSlots = 16;
+enum WallSlot {
+    W_INC_TOTAL = 0, W_INC_WALL, W_INC_INLET, W_INC_EXIT, W_INC_MELT, W_REL, W_Q_MELT, W_Q_LOSS,
+    W_T_AREA, W_Q_RAD_IN, W_Q_RAD_OUT, W_QM_FLAME, W_QM_BNDS, W_QM_CONV, W_QCONV
+};
+struct WallArgs {
+    int nb;                        // boundary patches
+    float* vf32;                   // nb x nb normalised view factors, row = near patch (mixed precision)
+    double* vf64;                  //   the same in FP64 (FP64 path)
+    const int *typ, *bi, *bj, *bk, *ori, *dir;
+    const int *o_bc;               // split index of each patch's closed cell centre
+    const int *o_b;                // split index of the patch position
+    const int *sink;               // index in the wall-sink patch list, -1 for inlets and exits
+    const double *px, *py, *pz;    // X(b_i), R(b_j), Z(b_k)
+    const double *emis, *area, *face_area, *bT_exit;   // bT_exit: exits' temperature at the first exchange
+    double *bT, *J, *Jn, *qc, *qeb, *qconv, *qamb, *rad, *rel;
+    double* part;                  // kWallSlots x kWallBlocks partial sums
+    double sig, radi_min, t0, u_a0, t_a, t_mnk;
+};
+
+int launch_wall_vf(const WallArgs& a, cudaStream_t st);
+template <typename R> void launch_wall_start(const WallArgs& a, const R* T, int first, cudaStream_t st);
+template <typename R> void launch_wall_init(const WallArgs& a, const R* QA, R* QE, cudaStream_t st);
+void launch_wall_to_sink(const WallArgs& a, Patch* sink_patches, cudaStream_t st);
+template <typename R> void launch_wall_from_sink(const WallArgs& a, const R* qconv_sink, cudaStream_t st);
+void launch_wall_sweep(const WallArgs& a, cudaStream_t st);
+void launch_wall_rad(const WallArgs& a, int mask, cudaStream_t st);
+void launch_wall_temps(const WallArgs& a, cudaStream_t st);
+void launch_wall_qamb(const WallArgs& a, cudaStream_t st);
+template <typename R> void launch_wall_post(const WallArgs& a, R* T, cudaStream_t st);
+void launch_wall_exits(const WallArgs& a, const int* frac_exit, const double* frac, double avg_wall_T, cudaStream_t st);
 
 // ---- volume radiation transfer (rad.cu) ---------------------------------------
 constexpr int kRadMaxBands = 16;

@@ -283,6 +283,24 @@ class GpuSolver:
         self._check(self.lib.gfm_gpu_rad_transfer(self.h, C.byref(t)))
         return t.as_dict()
 
+    def wall_setup(self, spec=None) -> None:
+        """Ends every later rad_transfer with the wall radiosity exchange, with
+        the case's wall inputs unless `spec` is given."""
+        spec = spec if spec is not None else self.case.c.wall
+        self._check(self.lib.gfm_gpu_wall_setup(self.h, C.byref(spec)))
+
+    def wall_totals(self) -> dict:
+        t = abi.GfmWallTotals()
+        self._check(self.lib.gfm_gpu_wall_totals(self.h, C.byref(t)))
+        return t.as_dict()
+
+    def wall_array(self, name: str) -> np.ndarray:
+        out = np.zeros(self.case.grid.b_cnt)
+        n = self.lib.gfm_gpu_wall_get(self.h, name.encode(), abi.dptr(out), out.size)
+        if n != out.size:
+            self._check(n if n < 0 else abi.GFM_E_ARG)
+        return out
+
     def adlbl3(self, xt, ap, as6, bs, ib, ie, jb, je, kb, ke, nim) -> np.ndarray:
         x = np.ascontiguousarray(xt, dtype=np.float64).copy()
         arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in as6]

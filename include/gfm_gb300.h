@@ -183,6 +183,25 @@ typedef struct gfm_restart_tail {
     int     interval_rad;        /* gas iterations between radiation calls      */
 } gfm_restart_tail;
 
+/* Wall radiation inputs: the &RADIN wall entries (Sbc.f90:25-35, defaults
+ * Sbc.f90:317-331) and the exhaust table of the sbc file (Sbc.f90:273-284).
+ * Wall-property blocks (NRADWALL > 0, IWALL) are not supported. */
+#define GFM_MAX_EXHAUSTS 16
+typedef struct gfm_wall_spec {
+    double eps_w, eps_c, eps_m;  /* wall, crown and melt-surface emissivity     */
+    int    have_crown;           /* 1: walls at z >= height_to_ceiling are crown */
+    double height_to_ceiling;    /* m                                          */
+    int    maxri1, maxri2, minri2;   /* radiosity solver loop limits (wallq)   */
+    double t_a, h_a, w_k, w_d;   /* ambient T (K), outside h (W/m2/K), wall
+                                    conductivity (W/m/K) and thickness (m)    */
+    double t_mnk;                /* lower bound of a wall T (K), T_mnK         */
+    int    nex;                  /* exhausts                                   */
+    int    exh_i1[GFM_MAX_EXHAUSTS], exh_j1[GFM_MAX_EXHAUSTS], exh_k1[GFM_MAX_EXHAUSTS];
+    int    exh_i2[GFM_MAX_EXHAUSTS], exh_j2[GFM_MAX_EXHAUSTS], exh_k2[GFM_MAX_EXHAUSTS];
+    int    exh_orient[GFM_MAX_EXHAUSTS], exh_direct[GFM_MAX_EXHAUSTS], exh_type[GFM_MAX_EXHAUSTS];
+    double exh_frac[GFM_MAX_EXHAUSTS], exh_fixed[GFM_MAX_EXHAUSTS];
+} gfm_wall_spec;
+
 /* A built case: host-owned arrays allocated by gfm_case_build or
  * gfm_case_read. */
 typedef struct gfm_case {
@@ -191,6 +210,8 @@ typedef struct gfm_case {
     gfm_fields fields;
     void      *priv;             /* owns the storage behind the pointers       */
     gfm_restart_tail tail;       /* restart records beyond the fields           */
+    gfm_wall_spec wall;          /* wall radiation inputs (sbc file, or the
+                                    synthetic furnace's defaults)             */
 } gfm_case;
 
 /* Opaque GPU solver handle. */
@@ -320,6 +341,23 @@ int  gfm_gpu_adlbl3(gfm_handle *h, double *xt, const double *ap,
  * (rad_qe_only, Rad_emis.f90:411-466 with RAD0 Rad0.f90:112-157). */
 int  gfm_gpu_rad_emission(gfm_handle *h);
 
+/* Results of one wall radiosity exchange (wallq, Qwall.f90:990-1365;
+ * wall_q_amb, Qwall.f90:1585-1660), W unless stated. */
+typedef struct gfm_wall_totals {
+    int    b_cnt;                /* boundary patches                           */
+    int    sweeps;               /* radiosity sweeps done (iterw increments)   */
+    int    outer;                /* outer passes (q_conv, T update, q_amb)     */
+    int    reserved;
+    double avg_wall_T;           /* area-weighted mean wall T (K)              */
+    double q_melt;               /* net flux into the melt surface             */
+    double q_wall_loss;          /* loss through the walls to ambient          */
+    double q_incident_total, q_incident_wall, q_incident_inlet, q_incident_exit, q_incident_melt;
+    double qconv_total;          /* convection from the gas to the boundaries  */
+    double q_rad_inlet, q_rad_outlet;
+    double qm_flame, qm_bnds, qm_conv;
+    double rel_rad_chg_mean;     /* last sweep's mean relative radiosity change */
+} gfm_wall_totals;
+
 /* Totals of one volume radiation transfer, W (Qrn.f90:73-87, Qre.f90:511-514,
  * Rad0.f90:137-148). */
 typedef struct gfm_rad_totals {
@@ -344,6 +382,25 @@ typedef struct gfm_rad_totals {
  * undefined corner case (a wall-corner split on the emitter's own column),
  * return GFM_E_UNSUPPORTED / GFM_E_LIMIT. */
 int  gfm_gpu_rad_transfer(gfm_handle *h, gfm_rad_totals *out);
+/* The wall radiosity exchange that follows the volume transfer in QRNF
+ * (Qrn.f90:209-211: wall_q_amb, wallq; Qwall.f90:990-1245, 1585-1655).
+ * gfm_gpu_wall_setup forms the patch data of the case's boundary patches
+ * (prepare_for_wall_radiation_calculation steps 5-8, Qwall.f90:395-736) and
+ * the normalised view factors on the device (nb x nb, FP64 on the FP64 path,
+ * FP32 on the mixed one; GFM_E_NOMEM when they do not fit); from then on every
+ * gfm_gpu_rad_transfer ends with the exchange: patch temperatures at the
+ * first call (Rad_emis.f90:186-273), radiosity sweeps with the reference's
+ * stopping rules, wall temperatures written into T, and the wall sink and EXTR
+ * of the following iterations use them (Extr.f90:194-197).  The sweeps read
+ * the previous sweep's radiosities (Jacobi) where the reference updates in
+ * patch order; both reach the same fixed point.  Every exit patch must lie in
+ * an exhaust of `spec`.  gfm_gpu_wall_totals returns the last exchange's
+ * results; gfm_gpu_wall_get copies one per-patch array ("b_t", "radiosity",
+ * "q_amb", "q_conv", "qc", "qeb", "emis", "b_face_area", "patch_area") and
+ * returns the patch count. */
+int  gfm_gpu_wall_setup(gfm_handle *h, const gfm_wall_spec *spec);
+int  gfm_gpu_wall_totals(gfm_handle *h, gfm_wall_totals *out);
+int  gfm_gpu_wall_get(gfm_handle *h, const char *name, double *out, int cap);
 /* Device times (CUDA events on the handle's stream) accumulated since the
  * last reset: adi_ms = line-solver batches, gflow_ms = whole GFLOW calls
  * (first to last iteration of each gfm_gpu_gflow), other_ms reserved;

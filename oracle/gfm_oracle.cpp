@@ -215,6 +215,18 @@ struct Oracle {
     // wall patches, kinetics, bands
     std::vector<int> b_typ, b_i, b_j, b_k, b_orient, b_direct;
     vec b_T, q_conv;
+    // wall radiation exchange (Qwall.f90), set up by gfo_wall_setup
+    bool wall_on = false;
+    int i1st_rad_done = 0;
+    gfm_wall_spec ws{};
+    std::vector<int> bc_i, bc_j, bc_k, b_exh;
+    vec emis, patch_area, b_face_area, vf, radiosity, q_amb, qc, qeb, qrs;
+    double avg_wall_T = 1600.0, radi_min = 0, rad_from_bnds = 0;
+    double wall_area_total = 0, melt_area_total = 0, inlet_area_total = 0, exit_area_total = 0, boundary_area_total = 0;
+    double q_melt = 0, q_wall_loss = 0, q_incident_total = 0, q_incident_wall = 0, q_incident_inlet = 0;
+    double q_incident_exit = 0, q_incident_melt = 0, q_rad_inlet = 0, q_rad_outlet = 0, qm_flame = 0, qm_bnds = 0, qm_conv = 0;
+    double last_rel_rad_chg_mean = 0;
+    int iterw = 0, wall_outer = 0, have_frac_exh_T = 0;
     int NR0;
     vec RTIM, DELRT, HRT, DELR, TIMED, HRD;
     int NWL;
@@ -540,7 +552,10 @@ struct Oracle {
         a3(SFP, I, J, K) = -GDZ;
     }
 
-    void calc_q_conv_wall() {   // Qwall.f90:1370-1475 (T in K: T*T0)
+    // Qwall.f90:1370-1475 with T in K: T*T0 in the gas solve (tscale = T0),
+    // T itself inside RAD_EMIS, which has already multiplied T by T0
+    void calc_q_conv_wall(double tscale = -1.0) {
+        if (tscale < 0) tscale = pr.t0;
         const double pi = 3.141592653589793;
         const double kappa_cmu = 0.4 * std::pow(9.0e-2, 0.25), E_cmu = 9.0 * std::pow(9.0e-2, 0.25);
         const double c_htw = 0.4 * ((pi / 4) / std::sin(pi / 4)) * std::sqrt(26.0) * (0.7 - ONE) / std::pow(0.7, 0.25);
@@ -562,7 +577,7 @@ struct Oracle {
             double cpmix = CP0 * (CPF1 * gf(inc, jnc, knc, IYF) + CPCO21 * gf(inc, jnc, knc, IYCO2) +
                                   CPH2O1 * gf(inc, jnc, knc, IYH2O) + CPO21 * gf(inc, jnc, knc, IYO2) +
                                   CPN21 * gf(inc, jnc, knc, IYN2));
-            double Tgas = a3(T, inc, jnc, knc) * pr.t0;
+            double Tgas = a3(T, inc, jnc, knc) * tscale;
             double gmu_T = ((2.0e-15 * Tgas + -1.1e-11) * Tgas + 4.5e-8) * Tgas + 7.0e-6;
             double h_t;
             if (pr.tk0 * gf(inc, jnc, knc, IK) < 0.1) {
@@ -579,6 +594,404 @@ struct Oracle {
                                 : (b_orient[n] == 2 ? DX[b_i[n]] * DZ[b_k[n]] : DX[b_i[n]] * DR[b_j[n]]);
             qconv_total = qconv_total + (q_conv[n] * patch_area);
         }
+    }
+
+    // ---- wall radiation exchange (Qwall.f90) ---------------------------------
+    // X**4 with an integer exponent: (X*X)*(X*X)
+    static double pow4(double x) { const double x2 = x * x; return x2 * x2; }
+    // prepare_for_wall_radiation_calculation steps 1-5 (Qwall.f90:72-513):
+    // MAPB = IBCELL with each exit tunnel closed, then the boundary patches.
+    // Each patch: type, i, j, k, orientation, direction.
+    void wall_patch_list(std::vector<int>& out) const {
+        std::vector<int> mapb(IBC.begin(), IBC.end());
+        auto mb = [&](int i, int j, int k) -> int& { return mapb[ix(i, j, k)]; };
+        auto mbs = [&](int i, int j, int k) -> int {   // outside the grid: closed
+            if (i < 1 || i > MP || j < 1 || j > NP || k < 1 || k > LP) return 1;
+            return mapb[ix(i, j, k)];
+        };
+        auto set = [&](int i0, int i1, int j0, int j1, int k0, int k1, int v) {
+            for (int ii = i0; ii <= i1; ++ii)
+                for (int jj = j0; jj <= j1; ++jj)
+                    for (int kk = k0; kk <= k1; ++kk) mb(ii, jj, kk) = v;
+        };
+        // the end of a run of exit positions; a run reaching the grid's edge ends there
+        auto endrun = [&](int start, int lim, auto at) {
+            int e = start;
+            for (int q = start + 2; q <= lim; q += 2) { if (at(q) != 3) return q - 2; e = q; }
+            return e;
+        };
+        // back wall, I = 2
+        for (int J = 2; J <= NP; J += 2)
+            for (int K = 2; K <= LP; K += 2) {
+                const int I = 2;
+                if (mb(I, J, K) != 3) continue;
+                int ks = K, ke = endrun(K, LP, [&](int q) { return mb(I, J, q); });
+                int js = J, je = endrun(J, NP, [&](int q) { return mb(I, q, K); });
+                int inew = -1;
+                for (int ii = 4; ii <= MP; ii += 2)
+                    if (mbs(ii, js - 2, ks - 2) == 0 || mbs(ii, je + 2, ke + 2) == 0 || mbs(ii, js - 2, ke + 2) == 0 ||
+                        mbs(ii, je + 2, ks - 2) == 0) { inew = ii - 2; break; }
+                if (inew < 0) continue;
+                set(inew, inew + 1, js, je, ks, ke, 3);
+                set(2, inew - 1, js, je, ks, ke, 1);
+            }
+        // front wall, I = MP
+        for (int J = 2; J <= NP; J += 2)
+            for (int K = 2; K <= LP; K += 2) {
+                const int I = MP;
+                if (mb(I, J, K) != 3) continue;
+                int ks = K, ke = endrun(K, LP, [&](int q) { return mb(I, J, q); });
+                int js = J, je = endrun(J, NP, [&](int q) { return mb(I, q, K); });
+                int inew = -1;
+                for (int ii = MP - 2; ii >= 2; ii -= 2)
+                    if (mbs(ii, js - 2, ks - 2) == 0 || mbs(ii, je + 2, ke + 2) == 0 || mbs(ii, js - 2, ke + 2) == 0 ||
+                        mbs(ii, je + 2, ks - 2) == 0) { inew = ii + 2; break; }
+                if (inew < 0) continue;
+                set(inew - 1, inew, js, je, ks, ke, 3);
+                set(inew + 1, MP, js, je, ks, ke, 1);
+            }
+        // side walls, J = 2 and J = NP
+        for (int side = 0; side < 2; ++side)
+            for (int I = 2; I <= MP; I += 2)
+                for (int K = 2; K <= LP; K += 2) {
+                    const int J = side == 0 ? 2 : NP;
+                    if (mb(I, J, K) != 3) continue;
+                    int ks = K, ke = endrun(K, LP, [&](int q) { return mb(I, J, q); });
+                    int is = I, ie = endrun(I, MP, [&](int q) { return mb(q, J, K); });
+                    int jnew = -1;
+                    if (side == 0) {
+                        for (int jj = 4; jj <= NP; jj += 2)
+                            if (mbs(is - 2, jj, ks - 2) == 0 || mbs(ie + 2, jj, ke + 2) == 0 || mbs(is - 2, jj, ke + 2) == 0 ||
+                                mbs(ie + 2, jj, ks - 2) == 0) { jnew = jj - 2; break; }
+                        if (jnew < 0) continue;
+                        set(is, ie, jnew, jnew + 1, ks, ke, 3);
+                        set(is, ie, 2, jnew - 1, ks, ke, 1);
+                    } else {
+                        for (int jj = NP - 2; jj >= 2; jj -= 2)
+                            if (mbs(is - 2, jj, ks - 2) == 0 || mbs(ie + 2, jj, ke + 2) == 0 || mbs(is - 2, jj, ke + 2) == 0 ||
+                                mbs(ie + 2, jj, ks - 2) == 0) { jnew = jj + 2; break; }
+                        if (jnew < 0) continue;
+                        set(is, ie, jnew - 1, jnew, ks, ke, 3);
+                        set(is, ie, jnew + 1, NP, ks, ke, 1);
+                    }
+                }
+        // top, K = LP
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2) {
+                const int K = LP;
+                if (mb(I, J, K) != 3) continue;
+                int is = I, ie = endrun(I, MP, [&](int q) { return mb(q, J, K); });
+                int js = J, je = endrun(J, NP, [&](int q) { return mb(I, q, K); });
+                int knew = -1;
+                for (int kk = LP - 2; kk >= 2; kk -= 2)
+                    if (mbs(is - 2, js - 2, kk) == 0 || mbs(ie + 2, je + 2, kk) == 0 || mbs(is - 2, je + 2, kk) == 0 ||
+                        mbs(ie + 2, js - 2, kk) == 0) { knew = kk + 2; break; }
+                if (knew < 0) continue;
+                set(is, ie, js, je, knew - 1, knew, 3);
+                set(is, ie, js, je, knew + 1, LP, 1);
+            }
+        out.clear();
+        auto add = [&](int t, int i, int j, int k, int o, int d) {
+            const int v[6] = {t, i, j, k, o, d};
+            out.insert(out.end(), v, v + 6);
+        };
+        for (int k = 2; k <= LP; k += 2)
+            for (int j = 2; j <= NP; j += 2)
+                for (int i = 3; i <= MP - 1; i += 2) {
+                    if (mb(i, j, k) < 1) continue;
+                    if (mb(i - 1, j, k) > 0 && mb(i + 1, j, k) > 0) continue;
+                    add(mb(i, j, k), i, j, k, 1, mb(i + 1, j, k) == 0 ? 0 : 1);
+                }
+        for (int k = 2; k <= LP; k += 2)
+            for (int j = 3; j <= NP - 1; j += 2)
+                for (int i = 2; i <= MP; i += 2) {
+                    if (mb(i, j, k) < 1) continue;
+                    if (mb(i, j - 1, k) > 0 && mb(i, j + 1, k) > 0) continue;
+                    add(mb(i, j, k), i, j, k, 2, mb(i, j + 1, k) == 0 ? 0 : 1);
+                }
+        for (int k = 3; k <= LP - 1; k += 2)
+            for (int j = 2; j <= NP; j += 2)
+                for (int i = 2; i <= MP; i += 2) {
+                    if (mb(i, j, k) < 1) continue;
+                    if (mb(i, j, k - 1) > 0 && mb(i, j, k + 1) > 0) continue;
+                    add(mb(i, j, k), i, j, k, 3, mb(i, j, k + 1) == 0 ? 0 : 1);
+                }
+    }
+
+    // prepare_for_wall_radiation_calculation steps 5-8 (Qwall.f90:395-760) on
+    // the patch list: cell centres, emissivities, areas, exhaust numbers,
+    // normalised view factors and the face area of each patch's cell
+    void wall_setup(const gfm_wall_spec& spec) {
+        ws = spec;
+        const int nb = (int)b_typ.size();
+        bc_i.assign(nb, 0); bc_j.assign(nb, 0); bc_k.assign(nb, 0); b_exh.assign(nb, 0);
+        emis.assign(nb, 0.0); patch_area.assign(nb, 0.0); b_face_area.assign(nb, 0.0);
+        for (int n = 0; n < nb; ++n) {
+            const int i = b_i[n], j = b_j[n], k = b_k[n], t = b_typ[n];
+            bc_i[n] = i; bc_j[n] = j; bc_k[n] = k;
+            const int s = b_direct[n] == 0 ? -1 : 1;
+            if (b_orient[n] == 1) { bc_i[n] = i + s; patch_area[n] = DR[j] * DZ[k]; }
+            else if (b_orient[n] == 2) { bc_j[n] = j + s; patch_area[n] = DX[i] * DZ[k]; }
+            else { bc_k[n] = k + s; patch_area[n] = DX[i] * DR[j]; }
+            if (t == 1) {
+                const int ktop = b_orient[n] == 3 ? LP - 1 : LP;
+                emis[n] = (Z[k] >= ws.height_to_ceiling || (k == ktop && ws.have_crown == 0)) ? ws.eps_c : ws.eps_w;
+            } else if (t == 4 && b_orient[n] == 3) {
+                emis[n] = ws.eps_m;
+            } else {
+                emis[n] = ONE;
+            }
+        }
+        // step 6: exhaust numbers (Qwall.f90:534-557)
+        have_frac_exh_T = 0;
+        for (int m = 0; m < ws.nex; ++m) if (ws.exh_type[m] == 0) have_frac_exh_T = 1;
+        for (int n = 0; n < nb; ++n) {
+            if (b_typ[n] != 3) continue;
+            for (int m = 0; m < ws.nex; ++m) {
+                if (b_orient[n] != ws.exh_orient[m] || b_direct[n] != ws.exh_direct[m]) continue;
+                bool in;
+                if (b_orient[n] == 1) in = bc_j[n] >= ws.exh_j1[m] && bc_j[n] <= ws.exh_j2[m] && bc_k[n] >= ws.exh_k1[m] && bc_k[n] <= ws.exh_k2[m];
+                else if (b_orient[n] == 2) in = bc_i[n] >= ws.exh_i1[m] && bc_i[n] <= ws.exh_i2[m] && bc_k[n] >= ws.exh_k1[m] && bc_k[n] <= ws.exh_k2[m];
+                else in = bc_i[n] >= ws.exh_i1[m] && bc_i[n] <= ws.exh_i2[m] && bc_j[n] >= ws.exh_j1[m] && bc_j[n] <= ws.exh_j2[m];
+                if (in) { b_exh[n] = m + 1; break; }
+            }
+        }
+        // step 7: view factors, normalised per row (Qwall.f90:562-666)
+        const double pi = 3.141592653589793;
+        vf.assign((size_t)nb * nb, 0.0);
+        for (int n = 0; n < nb; ++n) {
+            double vf_sum = ZERO;
+            for (int m = 0; m < nb; ++m) {
+                if (n == m) continue;
+                const double dx = X[b_i[n]] - X[b_i[m]], dy = R[b_j[n]] - R[b_j[m]], dz = Z[b_k[n]] - Z[b_k[m]];
+                const double dd = dx * dx + dy * dy + dz * dz;
+                const double denominator = pi * (dd * dd);
+                // the near patch's normal offset, and the far patch's
+                auto off = [&](int o, int a, int b) {
+                    return o == 1 ? X[b_i[a]] - X[b_i[b]] : o == 2 ? R[b_j[a]] - R[b_j[b]] : Z[b_k[a]] - Z[b_k[b]];
+                };
+                const int on = b_orient[n], om = b_orient[m];
+                const int cn = on == 1 ? b_i[n] : on == 2 ? b_j[n] : b_k[n];
+                const int cm = on == 1 ? b_i[m] : on == 2 ? b_j[m] : b_k[m];
+                if (b_direct[n] == 0 && cm <= cn) continue;
+                if (b_direct[n] == 1 && cm >= cn) continue;
+                double v;
+                if (om == on) {
+                    const double d = off(on, m, n);
+                    v = d * d * patch_area[m] / denominator;
+                } else {
+                    v = std::fabs(off(on, m, n) * off(om, m, n)) * patch_area[m] / denominator;
+                }
+                vf[(size_t)n * nb + m] = v;
+                vf_sum = vf_sum + v;
+            }
+            for (int m = 0; m < nb; ++m) {
+                if (vf_sum == ZERO) continue;
+                vf[(size_t)n * nb + m] = vf[(size_t)n * nb + m] / vf_sum;
+            }
+        }
+        // step 8: the face area of the patches on one cell (Qwall.f90:684-736),
+        // with the reference's chain of same-cell links as written
+        std::vector<int> s1(nb, 0), s2(nb, 0), s3(nb, 0), s4(nb, 0);   // 1-based patch numbers, 0 = none
+        for (int n = 1; n <= nb; ++n)
+            for (int m = n + 1; m <= nb; ++m) {
+                if (!(bc_i[n - 1] == bc_i[m - 1] && bc_j[n - 1] == bc_j[m - 1] && bc_k[n - 1] == bc_k[m - 1])) continue;
+                if (s1[n - 1] == 0) {
+                    s1[n - 1] = m; s1[m - 1] = n;
+                } else if (s2[n - 1] == 0) {
+                    if (s1[n - 1] == m) continue;
+                    s2[n - 1] = m; s1[m - 1] = n;
+                    s2[m - 1] = s1[n - 1]; s2[s1[n - 1] - 1] = m;
+                } else if (s3[n - 1] == 0) {
+                    if (s1[n - 1] == m || s2[n - 1] == m) continue;
+                    s3[n - 1] = m; s1[m - 1] = n;
+                    s2[m - 1] = s1[n - 1]; s3[s2[n - 1] - 1] = m;
+                    s3[m - 1] = s2[n - 1];
+                } else if (s4[n - 1] == 0) {
+                    if (s1[n - 1] == m || s2[n - 1] == m || s3[n - 1] == m) continue;
+                    s4[n - 1] = m; s1[m - 1] = n;
+                    s2[m - 1] = s1[n - 1]; s4[s2[n - 1] - 1] = m;
+                    s3[m - 1] = s2[n - 1]; s4[s3[n - 1] - 1] = m;
+                    s4[m - 1] = s3[n - 1];
+                }
+            }
+        wall_area_total = melt_area_total = inlet_area_total = exit_area_total = ZERO;
+        for (int n = 0; n < nb; ++n) {
+            auto pa = [&](int q) { return patch_area[q - 1]; };
+            if (s1[n] == 0) b_face_area[n] = patch_area[n];
+            else if (s2[n] == 0) b_face_area[n] = patch_area[n] + pa(s1[n]);
+            else if (s3[n] == 0) b_face_area[n] = patch_area[n] + pa(s1[n]) + pa(s2[n]);
+            else if (s4[n] == 0) b_face_area[n] = patch_area[n] + pa(s1[n]) + pa(s2[n]) + pa(s3[n]);
+            else b_face_area[n] = patch_area[n] + pa(s1[n]) + pa(s2[n]) + pa(s3[n]) + pa(s4[n]);
+            if (b_typ[n] == 1) wall_area_total = wall_area_total + patch_area[n];
+            else if (b_typ[n] == 4) melt_area_total = melt_area_total + patch_area[n];
+            else if (b_typ[n] == 2) inlet_area_total = inlet_area_total + patch_area[n];
+            else exit_area_total = exit_area_total + patch_area[n];
+        }
+        boundary_area_total = wall_area_total + melt_area_total + inlet_area_total + exit_area_total;
+        radiosity.assign(nb, 0.0); q_amb.assign(nb, 0.0); qc.assign(nb, 0.0); qeb.assign(nb, 0.0);
+        qrs.assign((size_t)MP * NP, 0.0);
+        radi_min = pr.sig * pow4(ws.t_mnk);   // Setup.f90:214
+        avg_wall_T = 1600.0;                            // Qwall.f90:68
+        wall_on = true;
+    }
+
+    // RAD_EMIS's patch temperatures and first radiosities (Rad_emis.f90:186-273),
+    // with T in K
+    void wall_start() {
+        const int nb = (int)b_typ.size();
+        if (i1st_rad_done == 0) {
+            for (int n = 0; n < nb; ++n) {
+                if (b_typ[n] == 1 || b_typ[n] == 2) b_T[n] = a3(T, bc_i[n], bc_j[n], bc_k[n]);
+                else if (b_typ[n] == 3) {
+                    const int m = b_exh[n] - 1;
+                    b_T[n] = ws.exh_type[m] == 0 ? ws.exh_frac[m] * avg_wall_T : ws.exh_fixed[m];
+                } else b_T[n] = a3(T, b_i[n], b_j[n], b_k[n]);
+                radiosity[n] = pr.sig * pow4(b_T[n]);
+            }
+        } else {
+            for (int n = 0; n < nb; ++n)
+                if (b_typ[n] == 4) {
+                    b_T[n] = a3(T, b_i[n], b_j[n], b_k[n]);
+                    radiosity[n] = pr.sig * pow4(b_T[n]);
+                }
+        }
+    }
+
+    // get_radiation_from_boundaries (Qwall.f90:1489-1577), the preset form
+    void radiation_from_boundaries(int i) {
+        const int nb = (int)b_typ.size();
+        rad_from_bnds = ZERO;
+        const double* row = &vf[(size_t)i * nb];
+        for (int j = 0; j < nb; ++j) rad_from_bnds = rad_from_bnds + radiosity[j] * row[j];
+    }
+
+    // wall_q_amb (Qwall.f90:1585-1655): one wall material (IWALL all zero)
+    void wall_q_amb() {
+        q_wall_loss = ZERO;
+        double u_a0;
+        if (ws.w_k < 1.0e-20 || ws.h_a < 1.0e-20) u_a0 = ZERO;
+        else u_a0 = ONE / (ws.w_d / ws.w_k + ONE / ws.h_a);
+        for (size_t n = 0; n < b_typ.size(); ++n) {
+            if (b_typ[n] != 1) { q_amb[n] = ZERO; continue; }
+            q_amb[n] = u_a0 * (b_T[n] - ws.t_a);
+            q_wall_loss = q_wall_loss + (q_amb[n] * patch_area[n]);
+        }
+    }
+
+    // wallq (Qwall.f90:990-1245), T in K; the GUI, timer and print branches
+    // are left out (qrn2, which the 20-second timer calls, only rebuilds QA)
+    void wallq() {
+        const int nb = (int)b_typ.size();
+        q_incident_total = q_incident_wall = q_incident_inlet = q_incident_exit = q_incident_melt = ZERO;
+        for (int n = 0; n < nb; ++n) {
+            qc[n] = QA[cix(bc_i[n] / 2, bc_j[n] / 2, bc_k[n] / 2)] / b_face_area[n];
+            q_incident_total = q_incident_total + (qc[n] * patch_area[n]);
+            switch (b_typ[n]) {
+            case 1: q_incident_wall = q_incident_wall + (qc[n] * patch_area[n]); break;
+            case 2:
+                q_incident_inlet = q_incident_inlet + (qc[n] * patch_area[n]);
+                qeb[n] = pr.sig * pow4(b_T[n]);
+                break;
+            case 3:
+                q_incident_exit = q_incident_exit + (qc[n] * patch_area[n]);
+                qeb[n] = pr.sig * pow4(b_T[n]);
+                break;
+            case 4:
+                q_incident_melt = q_incident_melt + (qc[n] * patch_area[n]);
+                qeb[n] = emis[n] * pr.sig * pow4(b_T[n]);
+                QE[cix(bc_i[n] / 2, bc_j[n] / 2, bc_k[n] / 2)] = qeb[n];
+                break;
+            }
+        }
+        const double wall_radiosity_tolerance = 1.0e-10, radiation_boundary_tolerance = 1.0e-10;
+        double prev_q_melt_chg = 1.0e6;
+        int nn = 1, nnextra = ws.maxri1;
+        wall_outer = 0;
+        while (nn <= ws.maxri1 && nn <= nnextra) {
+            const int minradi = ws.minri2;
+            calc_q_conv_wall(1.0);
+            int n = 1, nextra = ws.maxri2;
+            while (n <= ws.maxri2 && n <= nextra) {
+                double rel_rad_chg_mean = ZERO;
+                ++iterw;
+                for (int i = 0; i < nb; ++i) {
+                    rad_from_bnds = ZERO;
+                    if (b_typ[i] == 1 || emis[i] < ONE) radiation_from_boundaries(i);
+                    double rel_change = radiosity[i];
+                    if (b_typ[i] == 1) radiosity[i] = fmax2(qc[i] + q_conv[i] - q_amb[i] + rad_from_bnds, emis[i] * radi_min);
+                    else radiosity[i] = qeb[i] + (ONE - emis[i]) * (rad_from_bnds + qc[i]);
+                    if (rel_change < wall_radiosity_tolerance) {
+                        rel_change = ZERO;
+                    } else {
+                        rel_change = std::fabs((rel_change - radiosity[i]) / rel_change);
+                        rel_rad_chg_mean = rel_rad_chg_mean + rel_change;
+                    }
+                }
+                rel_rad_chg_mean = rel_rad_chg_mean / nb;
+                last_rel_rad_chg_mean = rel_rad_chg_mean;
+                if (rel_rad_chg_mean < wall_radiosity_tolerance && n > minradi)
+                    if (nextra == ws.maxri2) nextra = n + 3;
+                ++n;
+            }
+            // wall temperatures and the melt-surface flux (Qwall.f90:1134-1184)
+            const double prev_q_melt = q_melt;
+            q_melt = ZERO;
+            for (int i = 0; i < nb; ++i) {
+                if (b_typ[i] == 1) {
+                    b_T[i] = std::pow(fmax2(ZERO, (radiosity[i] - (q_amb[i] - q_conv[i]) * (ONE - emis[i]) / emis[i]) / pr.sig), 0.25);
+                    b_T[i] = fmax2(ws.t_mnk, b_T[i]);
+                } else if (b_typ[i] == 4) {
+                    radiation_from_boundaries(i);
+                    double& q = qrs[(size_t)(b_i[i] - 1) + (size_t)MP * (b_j[i] - 1)];
+                    q = qc[i] + q_conv[i] + rad_from_bnds - radiosity[i];
+                    q_melt = q_melt + (q * patch_area[i]);
+                }
+            }
+            wall_q_amb();
+            const double q_melt_chg = std::fabs((prev_q_melt - q_melt) / (q_melt + small16));
+            if (q_melt_chg < radiation_boundary_tolerance)
+                if (nnextra == ws.maxri1) nnextra = nn + 1;
+            prev_q_melt_chg = q_melt_chg;
+            ++wall_outer;
+            ++nn;
+        }
+        (void)prev_q_melt_chg;
+        // after the loop (Qwall.f90:1192-1245)
+        q_rad_outlet = q_rad_inlet = ZERO;
+        double wall_TxArea_total = ZERO;
+        qm_flame = qm_bnds = qm_conv = ZERO;
+        for (int i = 0; i < nb; ++i) {
+            switch (b_typ[i]) {
+            case 1:
+                a3(T, b_i[i], b_j[i], b_k[i]) = b_T[i];
+                wall_TxArea_total = wall_TxArea_total + (b_T[i] * patch_area[i]);
+                break;
+            case 2:
+                radiation_from_boundaries(i);
+                q_rad_inlet = q_rad_inlet + (qc[i] + rad_from_bnds - qeb[i]) * patch_area[i];
+                break;
+            case 3:
+                radiation_from_boundaries(i);
+                q_rad_outlet = q_rad_outlet + (qc[i] + rad_from_bnds - qeb[i]) * patch_area[i];
+                break;
+            case 4: {
+                radiation_from_boundaries(i);
+                const double f_melt = 1.0 - qeb[i] / (emis[i] * (qc[i] + rad_from_bnds) + q_conv[i]);
+                qm_flame = qm_flame + f_melt * emis[i] * qc[i] * patch_area[i];
+                qm_bnds = qm_bnds + f_melt * emis[i] * rad_from_bnds * patch_area[i];
+                qm_conv = qm_conv + f_melt * q_conv[i] * patch_area[i];
+                break;
+            }
+            }
+        }
+        avg_wall_T = wall_TxArea_total / wall_area_total;
+        if (have_frac_exh_T == 1)
+            for (int i = 0; i < nb; ++i) {
+                if (b_typ[i] != 3) continue;
+                const int m = b_exh[i] - 1;
+                b_T[i] = ws.exh_type[m] == 0 ? ws.exh_frac[m] * avg_wall_T : ws.exh_fixed[m];
+            }
     }
 
     void SOURCE(int MI1, int MI3, int NJ1, int NJ3, int LK1, int LK3) {
@@ -1173,9 +1586,11 @@ struct Oracle {
                     a3(GAMA, I, J, K) = a3(GAMA, I2, J2, K2);
                     for (int L = LSTAR; L <= LEND; ++L)
                         if (L != IH) gf(I, J, K, L) = gf(I1, J1, K1, L);
-                    // walls adiabatic until the first full radiation call (i1st_rad_done=0)
-                    gf(I, J, K, IH) = gf(I1, J1, K1, IH);
-                    a3(T, I, J, K) = a3(T, I1, J1, K1);
+                    // walls adiabatic until the first full radiation call (Extr.f90:194-197)
+                    if (i1st_rad_done == 0) {
+                        gf(I, J, K, IH) = gf(I1, J1, K1, IH);
+                        a3(T, I, J, K) = a3(T, I1, J1, K1);
+                    }
                     dnst_calc(I, J, K);
                 }
     }
@@ -2323,6 +2738,7 @@ struct RadVolume {
                     else if (ibr(IP2, J, K) <= 0) m = 111;
                 }
         for (auto& t : o.T) t = t * o.pr.t0;
+        if (o.wall_on) o.wall_start();
         // RAD0 (Rad0.f90:22-42, 112-166) with gray bands: AKLG = AKL0, AKLS = 0
         SGN = o.pr.sig * o.pr.ri * o.pr.ri;
         for (int L = 1; L <= NWL; ++L) DEB0[L] = o.pr.hck / o.pr.ri / o.WL[L - 1];
@@ -2376,8 +2792,14 @@ struct RadVolume {
                     for (int L = 1; L <= NWL; ++L) G0 = G0 + qal(I / 2, J / 2, K / 2, L);
                     o.QA[o.cix(I / 2, J / 2, K / 2)] = G0;
                 }
+        // the wall exchange of QRNF (Qrn.f90:209-211); qrn2 rebuilds QA as above
+        if (o.wall_on) {
+            o.wall_q_amb();
+            o.wallq();
+        }
         for (auto& t : o.T) t = t / o.pr.t0;
         o.i1st_rad_qe_done = 1;
+        if (o.wall_on) o.i1st_rad_done = 1;
     }
 };
 
@@ -2505,6 +2927,16 @@ long gfo_get_array(void* vo, const char* name, double* out, long cap) {
     const vec* src = nullptr;
     long off = 0, n = o->N;
     std::string s(name);
+    // per-patch arrays of the wall exchange
+    const vec* patch_arr = s == "b_t" ? &o->b_T : s == "radiosity" ? &o->radiosity : s == "q_amb" ? &o->q_amb
+                         : s == "q_conv" ? &o->q_conv : s == "qc" ? &o->qc : s == "qeb" ? &o->qeb : s == "emis" ? &o->emis
+                         : s == "b_face_area" ? &o->b_face_area : s == "patch_area" ? &o->patch_area : nullptr;
+    if (patch_arr) {
+        const long nb = (long)patch_arr->size();
+        if (cap < nb) return GFM_E_ARG;
+        std::memcpy(out, patch_arr->data(), nb * sizeof(double));
+        return nb;
+    }
     if (s == "ap") src = &o->AP; else if (s == "bs") src = &o->BS; else if (s == "sfp") src = &o->SFP;
     else if (s == "fz") src = &o->FZ; else if (s == "gte") src = &o->GTE; else if (s == "bs_hprev") src = &o->bs_hprev;
     else if (s.size() == 4 && s[0] == 'a' && s[1] == 's') {
@@ -2564,6 +2996,56 @@ int gfo_rad_transfer(void* vo, gfm_rad_totals* out) {
         out->tot_qe_soot = rv.tot_qe_soot;
         out->n_emitters = rv.n_emit;
     }
+    return GFM_OK;
+}
+int gfo_wall_patch_list(void* vo, int* out, int cap) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o) return GFM_E_ARG;
+    std::vector<int> pl;
+    o->wall_patch_list(pl);
+    const int n = (int)pl.size() / 6;
+    if (out) {
+        if (cap < n) return GFM_E_ARG;
+        std::memcpy(out, pl.data(), pl.size() * sizeof(int));
+    }
+    return n;
+}
+int gfo_wall_setup(void* vo, const gfm_wall_spec* spec) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || !spec) return GFM_E_ARG;
+    if (spec->nex < 0 || spec->nex > GFM_MAX_EXHAUSTS) return GFM_E_ARG;
+    // the patch list the case carries must be the one MAPB gives
+    std::vector<int> pl;
+    o->wall_patch_list(pl);
+    if (pl.size() != 6 * o->b_typ.size()) return GFM_E_ARG;
+    for (size_t n = 0; n < o->b_typ.size(); ++n) {
+        const int v[6] = {o->b_typ[n], o->b_i[n], o->b_j[n], o->b_k[n], o->b_orient[n], o->b_direct[n]};
+        for (int q = 0; q < 6; ++q) if (pl[6 * n + q] != v[q]) return GFM_E_ARG;
+    }
+    for (size_t n = 0; n < o->b_typ.size(); ++n)
+        if (o->b_typ[n] == 3) {
+            // every exit patch needs an exhaust entry (exh_type(b_exh) is read)
+            o->wall_setup(*spec);
+            for (size_t q = 0; q < o->b_typ.size(); ++q) if (o->b_typ[q] == 3 && o->b_exh[q] == 0) { o->wall_on = false; return GFM_E_ARG; }
+            return GFM_OK;
+        }
+    o->wall_setup(*spec);
+    return GFM_OK;
+}
+int gfo_wall_totals(void* vo, gfm_wall_totals* t) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || !t || !o->wall_on) return GFM_E_ARG;
+    std::memset(t, 0, sizeof *t);
+    t->b_cnt = (int)o->b_typ.size();
+    t->sweeps = o->iterw;
+    t->outer = o->wall_outer;
+    t->avg_wall_T = o->avg_wall_T; t->q_melt = o->q_melt; t->q_wall_loss = o->q_wall_loss;
+    t->q_incident_total = o->q_incident_total; t->q_incident_wall = o->q_incident_wall;
+    t->q_incident_inlet = o->q_incident_inlet; t->q_incident_exit = o->q_incident_exit;
+    t->q_incident_melt = o->q_incident_melt; t->qconv_total = o->qconv_total;
+    t->q_rad_inlet = o->q_rad_inlet; t->q_rad_outlet = o->q_rad_outlet;
+    t->qm_flame = o->qm_flame; t->qm_bnds = o->qm_bnds; t->qm_conv = o->qm_conv;
+    t->rel_rad_chg_mean = o->last_rel_rad_chg_mean;
     return GFM_OK;
 }
 double gfo_rif3(double x) { return RIF3(x); }

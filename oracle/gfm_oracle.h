@@ -45,6 +45,16 @@ double gfo_atand(double x);
 /* Volume radiation transfer (RAD0 + QRNF/QREF/QRTX/Y/Z + QRN1): sets QE and
  * QA of the state from its T and switches the radiation source term on. */
 int   gfo_rad_transfer(void *o, gfm_rad_totals *out);
+/* The wall radiosity exchange (Qwall.f90): gfo_wall_setup checks the case's
+ * patch list against the one MAPB gives (prepare_for_wall_radiation_
+ * calculation steps 1-5), then forms the patch data and view factors (steps
+ * 5-8); from then on gfo_rad_transfer ends with wall_q_amb and wallq, and
+ * EXTR keeps the wall temperatures.  gfo_wall_patch_list writes six ints per
+ * patch (type, i, j, k, orientation, direction) and returns the count;
+ * gfo_wall_totals gives the last exchange's results. */
+int   gfo_wall_setup(void *o, const gfm_wall_spec *spec);
+int   gfo_wall_patch_list(void *o, int *out, int cap);
+int   gfo_wall_totals(void *o, gfm_wall_totals *t);
 double gfo_rif3(double x);
 double gfo_zy1(const double *x, const double *y, double x1, int n);
 /* y: 9 GF components; returns normalised enthalpy / temperature */

@@ -44,6 +44,9 @@ def load(check_bounds: bool = False) -> C.CDLL:
     lib.gfo_calc_residual.restype = C.c_double
     lib.gfo_calc_residual.argtypes = [C.c_void_p, dp, dp, C.POINTER(dp), dp] + [C.c_int] * 6
     lib.gfo_rad_transfer.argtypes = [C.c_void_p, C.POINTER(abi.GfmRadTotals)]
+    lib.gfo_wall_setup.argtypes = [C.c_void_p, C.POINTER(abi.GfmWallSpec)]
+    lib.gfo_wall_patch_list.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int]
+    lib.gfo_wall_totals.argtypes = [C.c_void_p, C.POINTER(abi.GfmWallTotals)]
     for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1", "gfo_atand"):
         getattr(lib, n).restype = C.c_double
     lib.gfo_da.argtypes = [C.c_double, C.c_double]
@@ -124,6 +127,34 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"gfo_rad_transfer: {rc}")
         return t.as_dict()
+
+    def wall_setup(self, spec=None) -> None:
+        """Turns on the wall radiosity exchange at the end of rad_transfer,
+        with the case's wall inputs unless `spec` is given."""
+        spec = spec if spec is not None else self.case.c.wall
+        rc = self.lib.gfo_wall_setup(self.o, C.byref(spec))
+        if rc != 0:
+            raise RuntimeError(f"gfo_wall_setup: {rc}")
+
+    def wall_patch_list(self) -> np.ndarray:
+        n = self.lib.gfo_wall_patch_list(self.o, None, 0)
+        out = np.zeros(6 * n, dtype=np.int32)
+        self.lib.gfo_wall_patch_list(self.o, out.ctypes.data_as(C.POINTER(C.c_int)), n)
+        return out.reshape(n, 6)
+
+    def wall_totals(self) -> dict:
+        t = abi.GfmWallTotals()
+        rc = self.lib.gfo_wall_totals(self.o, C.byref(t))
+        if rc != 0:
+            raise RuntimeError(f"gfo_wall_totals: {rc}")
+        return t.as_dict()
+
+    def patch_array(self, name: str) -> np.ndarray:
+        out = np.zeros(self.case.grid.b_cnt)
+        got = self.lib.gfo_get_array(self.o, name.encode(), abi.dptr(out), out.size)
+        if got != out.size:
+            raise KeyError(name)
+        return out
 
     def download(self) -> Fields:
         out = Fields.empty(self.case.mp, self.case.np, self.case.lp)
