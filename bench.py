@@ -521,6 +521,13 @@ def run_ours(args):
         except Exception as e:   # reported, never required
             tc21 = {"failed": str(e)}
 
+    wall = None
+    if rank == 0 and not args.no_wall:
+        try:
+            wall = wall_exchange_leg(not args.no_cpu_baseline)
+        except Exception as e:   # reported, never required
+            wall = {"failed": str(e)}
+
     batched = None
     if rank == 0 and not args.no_batched:
         try:
@@ -565,6 +572,7 @@ def run_ours(args):
             "learned_p_prime": learned,
             "rad_transfer": rad,
             "tc21_case0041": tc21,
+            "wall_exchange": wall,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -701,6 +709,89 @@ def rad_transfer_leg(with_cpu: bool) -> dict:
     return out
 
 
+def wall_exchange_leg(with_cpu: bool) -> dict:
+    """The wall radiosity exchange (wall_q_amb and wallq after the volume
+    transfer, Qwall.f90:990-1245) on TC21 case 0041 read from its files, gray
+    kappa 0.5 1/m in its 10 bands, the wall sink on, from the state after 3
+    FP64 iterations of the oracle: gfm_gpu_rad_transfer with the exchange set
+    up, against the same call without it (the exchange's share is the
+    difference of the medians), next to the oracle's Gauss-Seidel restatement
+    on one host core, with the largest patch-temperature difference."""
+    import numpy as np
+    import shutil
+    import tempfile
+    from gfm_gb300 import Case, GpuSolver, abi
+    from oracle.pyoracle import Oracle
+    gold = pathlib.Path(__file__).resolve().parent / "tests" / "golden" / "case0041"
+    with tempfile.TemporaryDirectory() as d:
+        for n in ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt"):
+            shutil.copyfile(gold / n, pathlib.Path(d) / n)
+        case = Case.from_files(d, "0041", kappa=[0.5] * 16, wall_sink=True)
+    o = Oracle(case)
+    o.initsv()
+    o.gflow(3)
+    state = o.download()
+
+    def timed(with_wall: bool):
+        g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+        g.upload(state)
+        g.rad_transfer()   # first call: buffers, kernel attributes
+        setup = None
+        if with_wall:
+            t0 = time.perf_counter()
+            g.wall_setup()
+            setup = time.perf_counter() - t0
+        ts, tot = [], None
+        for _ in range(3):
+            g.close()
+            g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+            g.upload(state)
+            g.rad_transfer()
+            if with_wall:
+                g.wall_setup()
+            g.upload(state)
+            t0 = time.perf_counter()
+            g.rad_transfer()
+            ts.append(time.perf_counter() - t0)
+            if with_wall:
+                tot = g.wall_totals()
+                bt = g.wall_array("b_t")
+        g.close()
+        return sorted(ts)[1], setup, (tot, bt) if with_wall else None
+
+    t_rad, _, _ = timed(False)
+    t_all, t_setup, (tot, bt) = timed(True)
+    nb = tot["b_cnt"]
+    out = {"workload": f"wall radiosity exchange, TC21 case 0041 ({nb:,} boundary patches, {case.ncells:,} open "
+                       "cells), gray kappa 0.5 1/m in 10 bands, the wall sink on, state after 3 FP64 iterations",
+           "patches": nb, "sweeps": tot["sweeps"], "outer_passes": tot["outer"],
+           "seconds": t_all - t_rad, "seconds_with_volume_transfer": t_all, "setup_seconds": t_setup,
+           "view_factor_bytes": nb * nb * 8,
+           "timing": "host wall clock around the synchronous gfm_gpu_rad_transfer with the exchange set up, "
+                     "less the same call without it (medians of 3)",
+           "avg_wall_T": tot["avg_wall_T"], "q_melt": tot["q_melt"]}
+    if with_cpu:
+        o.wall_setup()
+        t0 = time.perf_counter()
+        o.rad_transfer()
+        t_o = time.perf_counter() - t0
+        o2 = Oracle(case, fields=state)
+        t0 = time.perf_counter()
+        o2.rad_transfer()
+        t_o_rad = time.perf_counter() - t0
+        o2.close()
+        to = o.wall_totals()
+        bt_o = o.patch_array("b_t")
+        out["cpu_baseline"] = {"seconds": t_o - t_o_rad, "cores": 1, "kind": "port",
+                               "sample": "the oracle's Gauss-Seidel exchange from the same state (its whole "
+                                         "radiation call less its volume transfer alone)",
+                               "sweeps": to["sweeps"], "avg_wall_T": to["avg_wall_T"], "q_melt": to["q_melt"]}
+        out["max_rel_err_b_T"] = float(np.max(np.abs(bt - bt_o) / bt_o))
+        out["vs_cpu_oracle"] = out["cpu_baseline"]["seconds"] / out["seconds"]
+    o.close()
+    return out
+
+
 def run_batched(args):
     """The batched workload alone (`--batched`): its own JSON line."""
     rank, world, local = dist_env()
@@ -730,6 +821,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-rad", action="store_true", help="skip the volume radiation transfer leg")
     ap.add_argument("--no-tc21", action="store_true", help="skip the TC21 case 0041 leg")
+    ap.add_argument("--no-wall", action="store_true", help="skip the wall radiosity exchange leg")
     ap.add_argument("--case", choices=["large", "medium", "xl"], default="large",
                     help="medium: the same furnace at 96x48x32, for kernel captures; xl: 384x160x96 with 10 bands "
                          "(neither is the benchmark workload)")
