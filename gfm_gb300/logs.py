@@ -23,6 +23,17 @@ descriptors of the reference's WRITE statements:
 
 List-directed header lines start with a blank, as the reference's compiler
 writes them, and lines end in CR-LF as in the shipped case directories.
+
+The run files of the GUI's energy-balance views are written here too:
+
+  summary####c.txt   the inflow header (summary_file_init, Utility.f90:95-
+                     108), then at the end of a run a "Run End" line and the
+                     energy balance (A0main.f90:315-320,
+                     sum_info_file_end_conditions, Utility.f90:124-220)
+  Info####c.plt      the same header (Info_file_init, Utility.f90:47-67),
+                     one energy record per iteration ((1x,i5,8e22.14),
+                     track_energy, A0main.f90:371-399) and the energy balance
+                     at the end of the run (A0main.f90:300-312)
 """
 from __future__ import annotations
 
@@ -129,3 +140,152 @@ class PlotLogs:
 
     def __exit__(self, *a):
         self.close()
+
+
+# ---- summary and Info files ---------------------------------------------------
+
+def tabbed(*fields) -> str:
+    """One record of T-positioned fields: (column, text) pairs, the column
+    1-based as in a Tn edit descriptor, text placed from that column."""
+    line: list = []
+    for col, text in fields:
+        pos = col - 1
+        if len(line) < pos:
+            line.extend(" " * (pos - len(line)))
+        line[pos:pos + len(text)] = list(text)
+    return "".join(line)
+
+
+def run_header(runum: str, kind: str, ncells: int, area_melt_surf: float, fr_f: float, fr_ox: float,
+               fr_n2: float, heat_in_fuel: float) -> list:
+    """The lines summary_file_init ("Summary Data") or Info_file_init
+    ("Information") writes on a fresh start (Utility.f90:61-67, 99-108)."""
+    title = {"summary": "Summary Data", "info": "Information"}[kind]
+    e = lambda v: fortran_e(v, 25, 14)
+    lines = [f"# Case {runum} {title} for Simulation and Evolving Global Energy Distribution", "",
+             tabbed((1, "# "), (5, "Number of cells in combustion grid:"), (40, fortran_i(ncells, 7))),
+             tabbed((1, "# "), (5, "Melt surface area: "), (38, e(area_melt_surf) + " m^2")), "",
+             tabbed((1, "# "), (5, "Fuel in flow rate: "), (38, e(fr_f) + " kg/s")),
+             tabbed((1, "# "), (5, "Oxygen in flow rate: "), (38, e(fr_ox) + " kg/s")),
+             tabbed((1, "# "), (5, "Nitrogen in flow rate: "), (38, e(fr_n2) + " kg/s")),
+             tabbed((1, "# "), (5, "Total in flow rate: "), (38, e(fr_n2 + fr_ox + fr_f) + " kg/s")), "",
+             tabbed((1, "# "), (5, "Heat value in with fuel: "), (38, e(heat_in_fuel) + " W")),
+             "  "]
+    if kind == "info":
+        lines.append("# PlotData")
+    return lines
+
+
+INFO_COLUMNS = ("# iter      " + "h flow in             " + "q reaction            " + "q melt                "
+                + "q exhaust             " + "q wall loss         " + "q rad opening loss      "
+                + "q from media          " + "q gas to wall")
+
+
+def info_record(itr_gas: int, q_h_in: float, q_react: float, q_melt: float, q_exhaust: float,
+                q_wall_loss: float, q_rad_openings: float, q_incident_total: float, qconv_total: float) -> str:
+    """One iteration's record of the Info file (track_energy, A0main.f90:392-399)."""
+    vals = (q_h_in, q_react, q_melt, q_exhaust, q_wall_loss, q_rad_openings, q_incident_total, qconv_total)
+    return " " + fortran_i(itr_gas, 5) + "".join(fortran_e(v, 22, 14) for v in vals)
+
+
+def end_conditions(v: dict, cycle_count=None, soot=None) -> list:
+    """sum_info_file_end_conditions (Utility.f90:124-220) from the run's end
+    values: q_react, q_h_in, q_exhaust, q_melt, q_wall_loss, q_rad_inlet,
+    q_rad_outlet, qm_flame, qm_bnds, qm_conv, qconv_total, qa_sum_to_melt,
+    qa_sum_to_wall, qa_sum_to_inlet, qa_sum_to_exit, gfin, gfex, fuel_out,
+    q0_h0 (Q0*H_0, the fuel heat per unit fuel mass), tave, tmean_ex,
+    avg_wall_T.  `soot` = (smf_max, smf_max_noclip, clipped count) and
+    `cycle_count` add the lines the reference writes when they apply."""
+    e = lambda x: fortran_e(x, 25, 14)
+
+    def row(ind, label, col, x, unit):
+        return tabbed((1, "# "), (ind, label), (col, e(x) + unit))
+
+    q_in = v["q_react"] + v["q_h_in"]
+    out = v["q_exhaust"] + v["q_melt"] + v["q_wall_loss"] + v["q_rad_inlet"] + v["q_rad_outlet"]
+    gas_out = (v["q_exhaust"] + v["qconv_total"] + v["qm_conv"] + v["qa_sum_to_melt"] + v["qa_sum_to_wall"]
+               + v["qa_sum_to_inlet"] + v["qa_sum_to_exit"])
+    L = ["", "# Energy Balance on Exterior Walls", "# --------------------------------", "",
+         row(5, "Total energy in:", 36, q_in, " W"),
+         row(9, "Energy in with flow:", 40, v["q_h_in"], " W"),
+         row(9, "Energy in via combustion:", 40, v["q_react"], " W"), "",
+         row(5, "Total energy leaving furnace:", 36, out, " W"),
+         row(9, "Energy out with flow:", 40, v["q_exhaust"], " W"),
+         row(9, "Energy out through walls:", 40, v["q_wall_loss"], " W"),
+         row(9, "Net radiation out inlets:", 40, v["q_rad_inlet"], " W"),
+         row(9, "Net radiation out outlets:", 40, v["q_rad_outlet"], " W"),
+         row(9, "Energy out to melt:", 40, v["q_melt"], " W"),
+         row(13, "from flame:", 44, v["qm_flame"], " W"),
+         row(13, "from surfaces:", 44, v["qm_bnds"], " W"),
+         row(13, "from convection:", 44, v["qm_conv"], " W"),
+         row(13, "(sum of froms):", 44, v["qm_flame"] + v["qm_bnds"] + v["qm_conv"], " W"),
+         "", "# Gas Energy Balance", "# --------------------------------", "",
+         row(5, "Total energy in:", 36, q_in, " W"),
+         row(9, "Energy in with flow:", 40, v["q_h_in"], " W"),
+         row(9, "Energy in via combustion:", 40, v["q_react"], " W"), "",
+         row(5, "Energy out with or from the gas:", 36, gas_out, " W"),
+         row(9, "Energy out with flow", 40, v["q_exhaust"], " W"),
+         row(9, "Convection to walls", 40, v["qconv_total"], " W"),
+         row(9, "Convection to melt surface", 40, v["qm_conv"], " W"),
+         row(9, "Radiation from flame to melt:", 40, v["qa_sum_to_melt"], " W"),
+         row(9, "Radiation from flame to walls:", 40, v["qa_sum_to_wall"], " W"),
+         row(9, "Radiation from flame to inlets:", 40, v["qa_sum_to_inlet"], " W"),
+         row(9, "Radiation from flame to exits:", 40, v["qa_sum_to_exit"], " W"),
+         "", "# --------------------------------",
+         "", row(5, "Mass in:", 36, v["gfin"], " kg/s"),
+         row(5, "Mass out:", 36, v["gfex"], " kg/s"),
+         "", row(5, "Fuel mass out:", 36, v["fuel_out"], " kg/s"),
+         row(5, "Fuel energy out:", 36, v["fuel_out"] * v["q0_h0"], " W"),
+         "", row(5, "Mean temperature:", 36, v["tave"], " K"),
+         row(5, "Mean exit temperature:", 36, v["tmean_ex"], " K"),
+         row(5, "Mean wall temperature:", 36, v["avg_wall_T"], " K")]
+    if soot is not None:
+        L += [tabbed((1, "# "), (5, "Maximum soot mass fraction:"), (36, e(soot[0]))),
+              tabbed((1, "# "), (5, "Not clipped soot mass fraction:"), (36, e(soot[1]))),
+              tabbed((1, "# "), (5, "Number of cells clipped:"), (36, fortran_i(soot[2], 9)))]
+    if cycle_count is not None:
+        L += ["", tabbed((1, "# "), (5, "Cycle count:"), (36, fortran_i(cycle_count, 5)))]
+    return L
+
+
+RUN_END = ["", "", "", "# #################   Run End   #################", ""]
+
+
+class RunFiles:
+    """summary####c.txt and Info####c.plt of one run in a case directory:
+    the inflow header at the start (appended to on a restart, as the
+    reference does when the file exists and IRSTYP > 0), `iteration(...)`
+    after every iteration, `end(values)` at the end of the run."""
+
+    def __init__(self, case_dir, runum: str, header: dict, restart: bool = False, newline: str = "\r\n"):
+        self.nl = newline
+        self.fh = {}
+        self.info_started = False
+        for kind, name in (("summary", f"summary{runum}c.txt"), ("info", f"Info{runum}c.plt")):
+            path = pathlib.Path(case_dir) / name
+            if restart and path.exists():
+                self.fh[kind] = open(path, "a", newline="")
+            else:
+                self.fh[kind] = open(path, "w", newline="")
+                self._lines(kind, run_header(runum, kind, **header))
+
+    def _lines(self, kind: str, lines) -> None:
+        self.fh[kind].write("".join(l + self.nl for l in lines))
+
+    def iteration(self, itr_gas: int, **q) -> None:
+        """One Info record (track_energy); the column headings before the first."""
+        if not self.info_started:
+            self._lines("info", ["", INFO_COLUMNS, ""])
+            self.info_started = True
+        self._lines("info", [info_record(itr_gas, **q)])
+
+    def end(self, values: dict) -> None:
+        self._lines("info", [INFO_COLUMNS] + end_conditions(values))
+        self._lines("summary", RUN_END + end_conditions(values))
+        self.close()
+
+    def close(self) -> None:
+        for f in self.fh.values():
+            f.close()
+        self.fh = {}
+

@@ -24,9 +24,9 @@ reference's own run of the case printed:
                             the mean gas temperature of the last iteration
 
 The first 48 lines of each per-iteration log (convg, gresid, gresid_xtra,
-Tave and, where the run wrote them, the pre-solve gresidp and gresid_xtrap)
-are copied unchanged into logs/, as the byte-level reference of their
-format.  For case0041 the converged restart file rg0041c.d is stored
+Tave, Info and, where the run wrote them, the pre-solve gresidp and
+gresid_xtrap) and the first 80 lines of summary####c.txt are copied unchanged
+into logs/, as the byte-level reference of their format.  For case0041 the converged restart file rg0041c.d is stored
 xz-compressed.
 
 Run from the repository root with the reference package root as argument:
@@ -69,11 +69,13 @@ def main(pkg_root: str) -> None:
             shutil.copyfile(case / name, out / name)
         shutil.copyfile(src / "relaxfactorc.txt", out / "relaxfactorc.txt")
         (out / "logs").mkdir(exist_ok=True)
-        for log in ("convg", "gresid", "gresidp", "gresid_xtra", "gresid_xtrap", "Tave"):
+        for log in ("convg", "gresid", "gresidp", "gresid_xtra", "gresid_xtrap", "Tave", "Info"):
             f = case / f"{log}{num}c.plt"
             if f.exists():
                 head = f.read_bytes().split(b"\r\n")[:48]
                 (out / "logs" / f.name).write_bytes(b"\r\n".join(head) + b"\r\n")
+        head = (case / f"summary{num}c.txt").read_bytes().split(b"\r\n")[:80]
+        (out / "logs" / f"summary{num}c.txt").write_bytes(b"\r\n".join(head) + b"\r\n")
         summ = (case / f"summary{num}c.txt").read_text()
         ref = {
             "source": f"combustion/{dirname} of the reference package",
