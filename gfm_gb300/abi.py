@@ -78,6 +78,11 @@ class GfmParams(C.Structure):
         ("maxgi", C.c_int),
         ("adi_mode", C.c_int),
         ("precision", C.c_int),
+        ("gas_model", C.c_int), ("maxms", C.c_int), ("ntimesm", C.c_int), ("irstypm", C.c_int),
+        ("bmcon", C.c_double), ("ssigma", C.c_double), ("rfm", C.c_double), ("rfm_soot", C.c_double),
+        ("rf_soot_form", C.c_double), ("rf_soot_oxid", C.c_double),
+        ("soot_cap", C.c_double), ("t0_sf", C.c_double), ("t0_so", C.c_double),
+        ("aform", C.c_double), ("aoxid", C.c_double), ("esf_r", C.c_double), ("eso_r", C.c_double),
     ]
 
 
@@ -89,6 +94,31 @@ class GfmFields(C.Structure):
         ("itr_gas", C.c_int), ("do_rad_qe_only_cnt", C.c_int), ("i1st_rad_qe_done", C.c_int),
         ("factor", C.c_double), ("fadj", C.c_double), ("gfin0", C.c_double), ("q_h_in", C.c_double),
     ]
+
+
+NSP_MINOR = 7
+
+
+class GfmMinor(C.Structure):
+    _fields_ = [
+        ("gfm", _dp), ("smf", _dp), ("bs_soot_prev", _dp), ("sfp_soot_prev", _dp), ("rrms", _dp),
+        ("itr_ms", C.c_int), ("imscon", C.c_int),
+    ]
+
+
+class GfmMsflowStats(C.Structure):
+    _fields_ = [
+        ("itr_ms", C.c_int), ("iterations", C.c_int), ("converged", C.c_int), ("reserved", C.c_int),
+        ("resid_ms_pre", C.c_double * 8), ("resid_ms", C.c_double * 8),
+        ("bal_ms", C.c_double), ("soot_tot", C.c_double), ("smf_max", C.c_double), ("smf_max_noclip", C.c_double),
+        ("gfm_out", C.c_double * 7), ("svf_r", C.c_double),
+    ]
+
+    def as_dict(self) -> dict:
+        return {"itr_ms": self.itr_ms, "iterations": self.iterations, "converged": self.converged,
+                "resid_ms_pre": list(self.resid_ms_pre), "resid_ms": list(self.resid_ms), "bal_ms": self.bal_ms,
+                "soot_tot": self.soot_tot, "smf_max": self.smf_max, "smf_max_noclip": self.smf_max_noclip,
+                "gfm_out": list(self.gfm_out), "svf_r": self.svf_r}
 
 
 class GfmIterStats(C.Structure):
@@ -208,6 +238,7 @@ class GfmCaseOptions(C.Structure):
     _fields_ = [
         ("sigma_eps", C.c_double), ("wall_sink", C.c_int), ("t_wall_k", C.c_double), ("rad_emission", C.c_int),
         ("kappa", C.c_double * 16), ("maxgi", C.c_int), ("adi_mode", C.c_int), ("precision", C.c_int),
+        ("gas_model", C.c_int),
     ]
 
 
@@ -248,6 +279,10 @@ SIGNATURES = [
     ("gfm_gpu_wall_setup", C.c_int, [C.c_void_p, C.POINTER(GfmWallSpec)]),
     ("gfm_gpu_wall_totals", C.c_int, [C.c_void_p, C.POINTER(GfmWallTotals)]),
     ("gfm_gpu_wall_get", C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_int]),
+    ("gfm_minor_read", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmMinor)]),
+    ("gfm_minor_write", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmMinor)]),
+    ("gfm_gpu_minor_upload", C.c_int, [C.c_void_p, C.POINTER(GfmMinor)]),
+    ("gfm_gpu_minor_download", C.c_int, [C.c_void_p, C.POINTER(GfmMinor)]),
     ("gfm_gpu_kernel_times", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     ("gfm_gpu_reset_kernel_times", C.c_int, [C.c_void_p]),
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),

@@ -326,7 +326,7 @@ __global__ void k_pref(Ctx<R> c, int I1, int J1, int K1, int I2, int J2, int K2,
 // whole-array round trip does.
 // ---------------------------------------------------------------------------
 template <typename R>
-__global__ void k_rad_emission(Ctx<R> c) {
+__global__ void k_rad_emission(Ctx<R> c, const double* __restrict__ gas_aklg, const double* __restrict__ gas_akls) {
     const GeoT<R>& g = c.g;
     const int hx = g.HX, hy = g.HY, hz = g.HZ;
     const long long tot = (long long)hx * hy * hz;
@@ -357,7 +357,14 @@ __global__ void k_rad_emission(Ctx<R> c) {
                 deb[c.nwl - 1] = 1.0 - eb0;
                 double t2 = T_rad * T_rad;
                 double s = 0.0;
-                for (int l = 0; l < c.nwl; ++l) s = s + deb[l] * emf(c.akl0[l], opl);
+                if (gas_aklg) {   // AKL0 = AKLG + AKLS of the band model, per cell (I fastest)
+                    const int mz = g.MP / 2, ncl = mz * (g.NP / 2) * (g.LP / 2);
+                    const int cc = (ia - 1) + mz * ((ja - 1) + (g.NP / 2) * (ka - 1));
+                    for (int l = 0; l < c.nwl; ++l)
+                        s = s + deb[l] * emf(gas_aklg[cc + (long long)l * ncl] + gas_akls[cc + (long long)l * ncl], opl);
+                } else {
+                    for (int l = 0; l < c.nwl; ++l) s = s + deb[l] * emf(c.akl0[l], opl);
+                }
                 qe = sa * sgn * (t2 * t2) * s;
             }
         }
@@ -491,9 +498,10 @@ template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s) {
     long long n = (long long)c.g.MP * c.g.NP * c.g.LP / 4;
     for (int st = 1; st <= 3; ++st) k_intp<R><<<gridn(n), kBlk, 0, s>>>(c, st);
 }
-template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s) {
+template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s, const double* gas_aklg,
+                                               const double* gas_akls) {
     long long n = (long long)c.g.HX * c.g.HY * c.g.HZ;
-    k_rad_emission<R><<<gridn(n), kBlk, 0, s>>>(c);
+    k_rad_emission<R><<<gridn(n), kBlk, 0, s>>>(c, gas_aklg, gas_akls);
     k_t_roundtrip<R><<<gridn(8 * c.g.CB), kBlk, 0, s>>>(c.T, 8 * c.g.CB, c.p.t0);
 }
 template <typename R> void launch_factor(const Ctx<R>& c, cudaStream_t s) {
@@ -527,7 +535,7 @@ template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* sr
     template void launch_extrv<R>(const Ctx<R>&, int, cudaStream_t);                                               \
     template void launch_intpv<R>(const Ctx<R>&, cudaStream_t);                                                    \
     template void launch_intp<R>(const Ctx<R>&, cudaStream_t);                                                     \
-    template void launch_rad_emission<R>(const Ctx<R>&, cudaStream_t);                                             \
+    template void launch_rad_emission<R>(const Ctx<R>&, cudaStream_t, const double*, const double*);                                             \
     template void launch_factor<R>(const Ctx<R>&, cudaStream_t);                                                   \
     template void launch_pref_idx<R>(const Ctx<R>&, int, int, int, int, int, int, double, double, cudaStream_t);  \
     template void launch_to_split<R>(const GeoT<R>&, const double*, R*, cudaStream_t);                             \

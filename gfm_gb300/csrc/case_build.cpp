@@ -267,6 +267,12 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
     P.sig = gfm::kSig; P.ri = in.ri; P.hck = gfm::kHck;
     P.bgcon = in.bgcon; P.maxgi = in.maxgi;
     P.adi_mode = in.adi_mode; P.precision = in.precision;
+    P.gas_model = in.gas_model; P.maxms = in.maxms; P.ntimesm = in.ntimesm; P.irstypm = in.irstypm;
+    P.bmcon = in.bmcon; P.ssigma = in.ssigma; P.rfm = in.rfm; P.rfm_soot = in.rfm_soot;
+    P.rf_soot_form = in.rf_soot_form; P.rf_soot_oxid = in.rf_soot_oxid;
+    P.soot_cap = in.soot_cap; P.t0_sf = in.t0_sf; P.t0_so = in.t0_so;
+    P.aform = in.aform; P.aoxid = in.aoxid;
+    P.esf_r = in.esf / gfm::kRu; P.eso_r = in.eso / gfm::kRu;   // Setup.f90:416-417
 
     // ---- fields at allocation (Setup.f90:747-779) -----------------------------
     s.p.assign(N, 0.0); s.t.assign(N, 1.0); s.dnst.assign(N, 1.0); s.theta.assign(N, 1.0);

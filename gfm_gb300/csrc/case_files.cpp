@@ -374,7 +374,10 @@ int read_sbc(const char* path, CaseInputs& in, SbcExtra& ex) {
               nl_double(kv, "gmu_ref", in.gmu_ref) && nl_int(kv, "maxgi", in.maxgi) &&
               nl_logical(kv, "react", in.react) && nl_int(kv, "irstyp", ex.irstyp) &&
               nl_int(kv, "id_rad", ex.id_rad) && nl_int(kv, "interval_rad", in.interval_rad) &&
-              nl_int(kv, "initial_gitr", in.initial_gitr);
+              nl_int(kv, "initial_gitr", in.initial_gitr) && nl_int(kv, "ms", in.ms) &&
+              nl_int(kv, "irstypm", in.irstypm) && nl_int(kv, "maxms", in.maxms) && nl_double(kv, "bmcon", in.bmcon) &&
+              nl_double(kv, "aform", in.aform) && nl_double(kv, "aoxid", in.aoxid) && nl_double(kv, "esf", in.esf) &&
+              nl_double(kv, "eso", in.eso);
     if (!ok) return GFM_E_IO;
     // pressure reference (Sbc.f90:57)
     {
@@ -464,17 +467,18 @@ int read_relax(const char* path, CaseInputs& in) {
     for (double& r : in.rf) r = v;
     if (!one(in.rf[0]) || !one(in.rf[1]) || !one(in.rf[2]) || !one(in.rf[17]) || !one(in.rf[20])) return GFM_E_IO;
     if (!one(in.rf_tsurf)) return GFM_E_IO;
-    if (!one(v) || !one(v)) return GFM_E_IO;   // minor species and soot
+    if (!one(in.rfm) || !one(in.rfm_soot)) return GFM_E_IO;   // minor species and soot
     if (!f.next()) return GFM_E_IO;
-    if (!one(in.rf_hsource)) return GFM_E_IO;
-    for (int n = 0; n < 7; ++n)
-        if (!one(v)) return GFM_E_IO;            // soot source terms and bounds
+    if (!one(in.rf_hsource) || !one(in.rf_soot_form) || !one(in.rf_soot_oxid)) return GFM_E_IO;
+    if (!one(v) || !one(v)) return GFM_E_IO;   // soot calibration (rf_aform, rf_afover)
+    if (!one(in.soot_cap) || !one(in.t0_sf) || !one(in.t0_so)) return GFM_E_IO;
     if (!f.next()) return GFM_E_IO;
     int g;
     if (!read_ints(f, 1, &g)) return GFM_E_IO;
     for (int& n : in.ntimesg) n = g;
     for (int n = 0; n < 12; ++n)
         if (!read_ints(f, 1, &in.ntimesg[n])) return GFM_E_IO;
+    if (!read_ints(f, 1, &in.ntimesm)) return GFM_E_IO;   // minor species (Setup.f90:510-511)
     return GFM_OK;
 }
 
@@ -641,6 +645,8 @@ extern "C" int gfm_case_read(const gfm_case_files* files, const gfm_case_options
         if (opt->maxgi > 0) in.maxgi = opt->maxgi;
         in.adi_mode = opt->adi_mode;
         in.precision = opt->precision;
+        if (opt->gas_model && !in.ms) { delete S; return GFM_E_ARG; }
+        in.gas_model = opt->gas_model;
     }
     in.rg_path = files->rg;
     rc = gfm::host::finish_case(S, in, files->kinetic, out, summary);
@@ -687,6 +693,69 @@ extern "C" int gfm_restart_write(const char* path, const gfm_grid* grid, const g
     ok = ok && w.rec(f->bs_hprev, sizeof(double) * N) &&
          w.rec(tail->t_surf_prev, sizeof(double) * (size_t)tail->mz * tail->nz) && w.rec(ff, sizeof ff) &&
          w.rec(&q1, 4) && w.rec(&rd, 4) && w.rec(&itr, 4) && w.rec(ir2, 8) && w.rec(&ivr, 4);
+    if (std::fclose(w.fp) != 0) ok = false;
+    return ok ? GFM_OK : GFM_E_IO;
+}
+
+// ---- the minor species restart rs####c.d (Sav3f.f90:96-117, Initsv.f90:350-372) ----
+namespace {
+bool minor_arrays(const gfm_minor* m) {
+    return m && m->gfm && m->smf && m->bs_soot_prev && m->sfp_soot_prev && m->rrms;
+}
+}  // namespace
+
+extern "C" int gfm_minor_read(const char* path, const gfm_grid* grid, gfm_minor* out) {
+    if (!path || !grid || !minor_arrays(out)) return GFM_E_ARG;
+    const int mp = grid->mp, np = grid->np, lp = grid->lp;
+    if (mp < 4 || np < 4 || lp < 4) return GFM_E_ARG;
+    const long N = (long)mp * np * lp, NCA = (long)(mp / 2) * (np / 2) * (lp / 2);
+    auto at = [&](int i, int j, int k) { return (i - 1) + (long)mp * ((j - 1) + (long)np * (k - 1)); };
+    gfm::host::RecReader r;
+    r.fp = std::fopen(path, "rb");
+    if (!r.fp) return GFM_E_IO;
+    bool ok = true;
+    for (int i = 2; i <= mp && ok; i += 2)
+        for (int j = 2; j <= np && ok; j += 2)
+            for (int k = 2; k <= lp && ok; k += 2) {
+                double g[GFM_NSP_MINOR + 1];
+                ok = r.rec(g, sizeof g);
+                if (!ok) break;
+                const long a = at(i, j, k);
+                for (int l = 0; l < GFM_NSP_MINOR; ++l) out->gfm[a + (long)l * N] = g[l];
+                out->smf[a] = g[GFM_NSP_MINOR];
+            }
+    int32_t itr = 0;
+    ok = ok && r.rec(out->bs_soot_prev, sizeof(double) * N) && r.rec(out->sfp_soot_prev, sizeof(double) * N) &&
+         r.rec(out->rrms, sizeof(double) * 5 * NCA) && r.rec(&itr, 4);
+    std::fclose(r.fp);
+    if (!ok) return GFM_E_IO;
+    out->itr_ms = itr;
+    out->imscon = 0;
+    return GFM_OK;
+}
+
+extern "C" int gfm_minor_write(const char* path, const gfm_grid* grid, const gfm_minor* m) {
+    if (!path || !grid || !minor_arrays(m)) return GFM_E_ARG;
+    const int mp = grid->mp, np = grid->np, lp = grid->lp;
+    if (mp < 4 || np < 4 || lp < 4) return GFM_E_ARG;
+    const long N = (long)mp * np * lp, NCA = (long)(mp / 2) * (np / 2) * (lp / 2);
+    auto at = [&](int i, int j, int k) { return (i - 1) + (long)mp * ((j - 1) + (long)np * (k - 1)); };
+    gfm::host::RecWriter w;
+    w.fp = std::fopen(path, "wb");
+    if (!w.fp) return GFM_E_IO;
+    bool ok = true;
+    for (int i = 2; i <= mp && ok; i += 2)
+        for (int j = 2; j <= np && ok; j += 2)
+            for (int k = 2; k <= lp && ok; k += 2) {
+                const long a = at(i, j, k);
+                double g[GFM_NSP_MINOR + 1];
+                for (int l = 0; l < GFM_NSP_MINOR; ++l) g[l] = m->gfm[a + (long)l * N];
+                g[GFM_NSP_MINOR] = m->smf[a];
+                ok = w.rec(g, sizeof g);
+            }
+    const int32_t itr = m->itr_ms;
+    ok = ok && w.rec(m->bs_soot_prev, sizeof(double) * N) && w.rec(m->sfp_soot_prev, sizeof(double) * N) &&
+         w.rec(m->rrms, sizeof(double) * 5 * NCA) && w.rec(&itr, 4);
     if (std::fclose(w.fp) != 0) ok = false;
     return ok ? GFM_OK : GFM_E_IO;
 }

@@ -69,6 +69,13 @@ struct CaseInputs {
     // restart file, NULL for a fresh start
     const char* rg_path = nullptr;
     int interval_rad = 100, initial_gitr = 100;
+    // minor species and soot (Var_mod.f90:215, 465-492; Setup.f90:161-185),
+    // relaxfactorc.txt's minor-species lines (Setup.f90:476-511)
+    int ms = 0, irstypm = 0, maxms = 300, ntimesm = 4;
+    double bmcon = 1.0e-7, ssigma = 0.7, rfm = 0.5, rfm_soot = 0.2;
+    double rf_soot_form = 0.3, rf_soot_oxid = 0.3, soot_cap = 4.0e-3, t0_sf = 0.0, t0_so = 0.0;
+    double aform = 400.0, aoxid = 26.0, esf = 5.0e7, eso = 5.0e7;
+    int gas_model = 0;
     // wall radiation inputs: &RADIN and the exhaust table of the SBC file
     gfm_wall_spec wall = wall_defaults();
     static gfm_wall_spec wall_defaults() {   // Sbc.f90:317-331, T_mnK (Var_mod.f90:45)

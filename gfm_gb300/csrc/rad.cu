@@ -121,7 +121,8 @@ __device__ void rad_debx(const RadArgs& a, double t, double* deb) {   // DEBX, R
     deb[a.NWL - 1] = 1.0 - eb0;
 }
 
-// RAD0 (ID_RAD=10), gray bands: AKLG = AKL0, AKLS = 0.  Also the cell
+// RAD0 (ID_RAD=10): AKL = EMF(AKLG + AKLS) from the band model (gas.cu), or
+// from the gray bands (AKLG = AKL0, AKLS = 0).  Also the cell
 // temperature in kelvin (T*T0), the one the transfer reads, and for every
 // emitter (open, T > TG_MN) QREF's emission per unit area of each band,
 // QEL0 = DEB*AKL*SGN*T^4 (Qre.f90:80-86), with the same DEB.  Block partials
@@ -152,11 +153,14 @@ __global__ void __launch_bounds__(256) k_rad_akl(RadArgs a, const R* __restrict_
         const bool emitter = t > kTgMn;
         const double g0 = a.sgn * (t2 * t2);
         for (int l = 0; l < a.NWL; ++l) {
-            const double akl = emf(a.akl0[l], opl);
-            a.akl[c + (long long)l * n] = akl;
-            if (emitter) a.qel0[c + (long long)l * n] = deb[l] * akl * g0;
-            sg = sg + deb[l] * emf(a.akl0[l], opl);
-            ss = ss + deb[l] * emf(0.0, opl);
+            const long long cl = c + (long long)l * n;
+            const double ag = a.gas_aklg ? a.gas_aklg[cl] : a.akl0[l];
+            const double as = a.gas_aklg ? a.gas_akls[cl] : 0.0;
+            const double akl = emf(a.gas_aklg ? ag + as : a.akl0[l], opl);
+            a.akl[cl] = akl;
+            if (emitter) a.qel0[cl] = deb[l] * akl * g0;
+            sg = sg + deb[l] * emf(ag, opl);
+            ss = ss + deb[l] * emf(as, opl);
         }
         sg_tot += area_sgn_t4 * sg;
         ss_tot += area_sgn_t4 * ss;

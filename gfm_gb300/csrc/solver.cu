@@ -136,6 +136,12 @@ struct gfm_handle {
     double* d_frac = nullptr;
     double avg_wall_T = 1600.0, q_melt = 0.0;   // Qwall.f90:68; q_melt starts at zero
     gfm_wall_totals wall_last{};        // results of the last exchange
+    // minor species and soot (gfm_gpu_minor_upload), the band model's buffers
+    MinorDev<double> mnd{};
+    MinorDev<float> mnf{};
+    bool minor_on = false;
+    int itr_ms = 0, imscon = 0;
+    GasBuffers gas{};
 };
 
 namespace {
@@ -1077,6 +1083,23 @@ int capture_iteration(gfm_handle* h) {
 }  // namespace
 
 namespace {
+int gas_band(gfm_handle* h);
+int gas_check(gfm_handle* h);
+// the emission-only source (rad_qe_only, Rad_emis.f90:411-466) on the
+// handle's stream, on the band model's coefficients when the case asks for it
+int rad_emission_launch(gfm_handle* h) {
+    if (h->params.gas_model) {
+        if (h->gas.err) CK(cudaMemsetAsync(h->gas.err, 0, sizeof(int), h->stream));
+        int rc = gas_band(h);
+        if (rc) return rc;
+    }
+    const double* ag = h->params.gas_model ? h->gas.aklg : nullptr;
+    const double* as = h->params.gas_model ? h->gas.akls : nullptr;
+    if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream, ag, as);
+    else launch_rad_emission(h->cf, h->stream, ag, as);
+    return GFM_OK;
+}
+
 // One SPHASE pass split in two, so that several handles can have an
 // iteration in flight at once: iter_launch queues GFLOW and the read-back of
 // the statistics on the handle's stream; iter_finish waits for them and
@@ -1103,6 +1126,7 @@ int iter_finish(gfm_handle* h, int* conv) {
     *conv = 0;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
+    if (int rc = gas_check(h)) return rc;   // the band model of the last emission update
     for (int q = 0; q + 1 < h->n_ev; q += 2) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, h->ev[q], h->ev[q + 1]) == cudaSuccess) h->adi_ms += ms;
@@ -1112,8 +1136,8 @@ int iter_finish(gfm_handle* h, int* conv) {
     if (h->params.rad_emission) {
         h->cnt_qe += 1;
         if (h->cnt_qe >= h->params.rad_qe_frequency && h->itr_gas > 50) {
-            if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
-            else launch_rad_emission(h->cf, h->stream);
+            int rc = rad_emission_launch(h);
+            if (rc) return rc;
             h->rad_active = 1;
             h->cnt_qe = 0;
         }
@@ -1303,23 +1327,29 @@ extern "C" int gfm_gpu_download(gfm_handle* h, gfm_fields* f) {
 }
 
 namespace {
+// The radiation code works in FP64: in mixed mode the handle's FP64 geometry
+// holds only IBCELL until this uploads its coordinates (once per handle)
+int ensure_double_coords(gfm_handle* h) {
+    if (h->gd.X) return GFM_OK;
+    const HostGrid& hg = h->hg;
+    double *x, *dx, *r, *dr, *rs, *z, *dz;
+    int rc;
+    if ((rc = dupload(h, &x, hg.X)) || (rc = dupload(h, &dx, hg.DX)) || (rc = dupload(h, &r, hg.R)) ||
+        (rc = dupload(h, &dr, hg.DR)) || (rc = dupload(h, &rs, hg.RS)) || (rc = dupload(h, &z, hg.Z)) ||
+        (rc = dupload(h, &dz, hg.DZ)))
+        return rc;
+    h->gd.X = x; h->gd.DX = dx; h->gd.Rr = r; h->gd.DR = dr; h->gd.RS = rs; h->gd.Z = z; h->gd.DZ = dz;
+    return GFM_OK;
+}
+
 // buffers, streams and the launch plan of the volume transfer, once per handle
 int rad_prepare(gfm_handle* h, const RadArgs& in) {
     if (h->rad_ready) return GFM_OK;
     RadArgs a = in;
     const long long nc = (long long)a.MZ * a.NZ * a.LZ;
-    // the transfer works in FP64: in mixed mode the handle's FP64 geometry
-    // holds only IBCELL, so the coordinates are uploaded for it here
-    if (!a.g.X) {
-        const HostGrid& hg = h->hg;
-        double *x, *dx, *r, *dr, *rs, *z, *dz;
-        int rc;
-        if ((rc = dupload(h, &x, hg.X)) || (rc = dupload(h, &dx, hg.DX)) || (rc = dupload(h, &r, hg.R)) ||
-            (rc = dupload(h, &dr, hg.DR)) || (rc = dupload(h, &rs, hg.RS)) || (rc = dupload(h, &z, hg.Z)) ||
-            (rc = dupload(h, &dz, hg.DZ)))
-            return rc;
-        a.g.X = x; a.g.DX = dx; a.g.Rr = r; a.g.DR = dr; a.g.RS = rs; a.g.Z = z; a.g.DZ = dz;
-    }
+    if (int rc = ensure_double_coords(h)) return rc;
+    a.g.X = h->gd.X; a.g.DX = h->gd.DX; a.g.Rr = h->gd.Rr; a.g.DR = h->gd.DR; a.g.RS = h->gd.RS;
+    a.g.Z = h->gd.Z; a.g.DZ = h->gd.DZ;
     int dev = 0, sms = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1610,6 +1640,145 @@ extern "C" int gfm_gpu_wall_get(gfm_handle* h, const char* name, double* out, in
     return a.nb;
 }
 
+namespace {
+__global__ void k_cast_d2f(const double* __restrict__ s, float* __restrict__ d, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = (float)s[i];
+}
+__global__ void k_cast_f2d(const float* __restrict__ s, double* __restrict__ d, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = (double)s[i];
+}
+int cast_grid(long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); }
+
+template <typename R>
+int minor_alloc(gfm_handle* h, MinorDev<R>& m) {
+    if (m.smf) return GFM_OK;
+    const long long ncl = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    int rc;
+    for (int l = 0; l < 7; ++l)
+        if ((rc = dalloc(h, &m.gfm[l], h->NS))) return rc;
+    if ((rc = dalloc(h, &m.smf, h->NS)) || (rc = dalloc(h, &m.bsp, h->NS)) || (rc = dalloc(h, &m.sfpp, h->NS)) ||
+        (rc = dalloc(h, &m.rrms, 5 * ncl)))
+        return rc;
+    return GFM_OK;
+}
+
+template <typename R>
+int minor_put(gfm_handle* h, const GeoT<R>& g, MinorDev<R>& m, const gfm_minor* src) {
+    int rc;
+    if ((rc = minor_alloc(h, m))) return rc;
+    cudaStream_t st = h->stream;
+    const long long N = h->N;
+    const long long ncl = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    auto put = [&](const double* a, R* dst) -> int {
+        CK(cudaMemcpyAsync(h->d_stage, a, N * sizeof(double), cudaMemcpyHostToDevice, st));
+        launch_to_split(g, h->d_stage, dst, st);
+        return GFM_OK;
+    };
+    for (int l = 0; l < 7; ++l)
+        if ((rc = put(src->gfm + (long long)l * N, m.gfm[l]))) return rc;
+    if ((rc = put(src->smf, m.smf)) || (rc = put(src->bs_soot_prev, m.bsp)) || (rc = put(src->sfp_soot_prev, m.sfpp)))
+        return rc;
+    // RRMS keeps the cell layout; 5 x ncell <= N, so it fits the staging buffer
+    CK(cudaMemcpyAsync(h->d_stage, src->rrms, 5 * ncl * sizeof(double), cudaMemcpyHostToDevice, st));
+    if constexpr (std::is_same<R, double>::value) {
+        CK(cudaMemcpyAsync(m.rrms, h->d_stage, 5 * ncl * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    } else {
+        k_cast_d2f<<<cast_grid(5 * ncl), 256, 0, st>>>(h->d_stage, m.rrms, 5 * ncl);
+    }
+    CK(cudaStreamSynchronize(st));
+    return GFM_OK;
+}
+
+template <typename R>
+int minor_get(gfm_handle* h, const GeoT<R>& g, const MinorDev<R>& m, gfm_minor* out) {
+    cudaStream_t st = h->stream;
+    const long long N = h->N;
+    const long long ncl = (long long)(h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    auto get = [&](const R* src, double* a) -> int {
+        launch_from_split(g, src, h->d_stage, st);
+        CK(cudaMemcpyAsync(a, h->d_stage, N * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        return GFM_OK;
+    };
+    int rc;
+    for (int l = 0; l < 7; ++l)
+        if ((rc = get(m.gfm[l], out->gfm + (long long)l * N))) return rc;
+    if ((rc = get(m.smf, out->smf)) || (rc = get(m.bsp, out->bs_soot_prev)) || (rc = get(m.sfpp, out->sfp_soot_prev)))
+        return rc;
+    if constexpr (std::is_same<R, double>::value) {
+        CK(cudaMemcpyAsync(h->d_stage, m.rrms, 5 * ncl * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    } else {
+        k_cast_f2d<<<cast_grid(5 * ncl), 256, 0, st>>>(m.rrms, h->d_stage, 5 * ncl);
+    }
+    CK(cudaMemcpyAsync(out->rrms, h->d_stage, 5 * ncl * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return GFM_OK;
+}
+
+// the band model's AKLG and AKLS on the current state (gas.cu), when the
+// case asks for it; a no-op for the gray bands
+int gas_band(gfm_handle* h) {
+    if (!h->params.gas_model) return GFM_OK;
+    if (!h->minor_on) { h->err = "band model: no minor species state (gfm_gpu_minor_upload)"; return GFM_E_ARG; }
+    const int ncl = (h->hg.MP / 2) * (h->hg.NP / 2) * (h->hg.LP / 2);
+    const int nwl = h->cd.nwl;
+    int rc;
+    if (!h->gas.aklg) {
+        if ((rc = dalloc(h, &h->gas.aklg, (long long)ncl * nwl)) || (rc = dalloc(h, &h->gas.akls, (long long)ncl * nwl)) ||
+            (rc = dalloc(h, &h->gas.fvs, ncl)) || (rc = dalloc(h, &h->gas.setter, ncl)) ||
+            (rc = dalloc(h, &h->gas.blockmax, gas_scan_blocks(ncl))) || (rc = dalloc(h, &h->gas.err, 1)))
+            return rc;
+    }
+    if ((rc = ensure_double_coords(h))) return rc;
+    const gfm_params& P = h->params;
+    if (h->prec == GFM_PREC_FP64) {
+        const Ctx<double>& c = h->cd;
+        rc = launch_gas_band<double>(h->gas, h->gd, c.T, c.P, c.DNST, h->mnd.gfm, h->mnd.smf, P.t0, P.pg0, P.dnst0, nwl,
+                                     c.wl, h->stream);
+    } else {
+        const Ctx<float>& c = h->cf;
+        rc = launch_gas_band<float>(h->gas, h->gd, c.T, c.P, c.DNST, h->mnf.gfm, h->mnf.smf, P.t0, P.pg0, P.dnst0, nwl,
+                                    h->cd.wl, h->stream);
+    }
+    if (rc) h->err = "band model launch";
+    return rc;
+}
+// the band model's error bits, read after the stream has finished
+int gas_check(gfm_handle* h) {
+    if (!h->params.gas_model || !h->gas.err) return GFM_OK;
+    int e = 0;
+    CK(cudaMemcpy(&e, h->gas.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        h->err = (e & 2) ? "band model: BANDA argument < 0 (Rad_gas.f90:368-371)"
+                         : "band model: W_R <= 0 with CO2 present (Rad_gas.f90:233)";
+        return GFM_E_NAN;
+    }
+    return GFM_OK;
+}
+}  // namespace
+
+extern "C" int gfm_gpu_minor_upload(gfm_handle* h, const gfm_minor* m) {
+    if (!h || !m || !m->gfm || !m->smf || !m->bs_soot_prev || !m->sfp_soot_prev || !m->rrms) return GFM_E_ARG;
+    int rc = h->prec == GFM_PREC_FP64 ? minor_put(h, h->gd, h->mnd, m) : minor_put(h, h->gfl, h->mnf, m);
+    if (rc) return rc;
+    h->minor_on = true;
+    h->itr_ms = m->itr_ms;
+    h->imscon = m->imscon;
+    return GFM_OK;
+}
+
+extern "C" int gfm_gpu_minor_download(gfm_handle* h, gfm_minor* m) {
+    if (!h || !m || !m->gfm || !m->smf || !m->bs_soot_prev || !m->sfp_soot_prev || !m->rrms) return GFM_E_ARG;
+    if (!h->minor_on) { h->err = "no minor species state"; return GFM_E_ARG; }
+    int rc = h->prec == GFM_PREC_FP64 ? minor_get(h, h->gd, h->mnd, m) : minor_get(h, h->gfl, h->mnf, m);
+    if (rc) return rc;
+    m->itr_ms = h->itr_ms;
+    m->imscon = h->imscon;
+    return GFM_OK;
+}
+
 extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
     if (!h) return GFM_E_ARG;
     const Ctx<double>& cdb = h->cd;
@@ -1629,12 +1798,20 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
         int rc = rad_prepare(h, a);
         if (rc) return rc;
     }
-    const RadArgs& a = h->rad;
     cudaStream_t st = h->stream;
+    int rc;
+    if (h->params.gas_model) {
+        if (h->gas.err) CK(cudaMemsetAsync(h->gas.err, 0, sizeof(int), st));
+        if ((rc = gas_band(h))) return rc;
+        h->rad.gas_aklg = h->gas.aklg;
+        h->rad.gas_akls = h->gas.akls;
+    } else {
+        h->rad.gas_aklg = h->rad.gas_akls = nullptr;
+    }
+    const RadArgs& a = h->rad;
     const cudaStream_t streams[3] = {st, h->rad_stream[0], h->rad_stream[1]};
     CK(cudaMemsetAsync(a.err, 0, sizeof(int), st));
     const long long nT = 8 * h->gd.CB;
-    int rc;
     if (h->prec == GFM_PREC_FP64) {
         if ((rc = launch_rad_transfer<double>(a, h->cd.T, nT, streams, h->rad_ev))) { h->err = "radiation transfer launch"; return rc; }
         launch_cells_to_split(h->gd, a.qe, h->cd.QE, st);
@@ -1656,6 +1833,7 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
         h->err = "radiation transfer: a wall-corner split inside the box (geometry outside the supported set)";
         return GFM_E_UNSUPPORTED;
     }
+    if ((rc = gas_check(h))) return rc;
     h->rad_active = 1;
     if (h->wall_on) {
         // the wall exchange of QRNF (Qrn.f90:209-211)
@@ -1686,12 +1864,12 @@ extern "C" int gfm_gpu_rad_transfer(gfm_handle* h, gfm_rad_totals* out) {
 
 extern "C" int gfm_gpu_rad_emission(gfm_handle* h) {
     if (!h) return GFM_E_ARG;
-    if (h->prec == GFM_PREC_FP64) launch_rad_emission(h->cd, h->stream);
-    else launch_rad_emission(h->cf, h->stream);
+    int rc = rad_emission_launch(h);
+    if (rc) return rc;
     h->rad_active = 1;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return GFM_E_CUDA; }
-    return GFM_OK;
+    return gas_check(h);
 }
 
 namespace {

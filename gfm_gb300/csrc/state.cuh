@@ -168,6 +168,9 @@ struct RadArgs {
     double* scratch[3];          // slab arrays when they do not fit in shared memory
     unsigned char* fscratch[3];
     int* err;                    // bit 0: geometry outside the supported set
+    // band model (gas.cu): AKLG and AKLS per cell and band (cell + l*ncell);
+    // null for the gray bands akl0
+    const double *gas_aklg, *gas_akls;
     // per direction and CTA: the corner-split additions of the interior
     // columns of one slab, split_capc entries per column (rad.cu)
     int split_capc[3];
@@ -175,6 +178,29 @@ struct RadArgs {
     int* split_meta[3];          // [cta][column][entry][row, target column, band mask]
     double* split_q[3];          // [cta][column][entry][band]
 };
+// ---- minor species and soot (ms=1): MSFLOW's state -----------------------------
+template <typename R>
+struct MinorDev {
+    R* gfm[7];                   // GFM(.,L), parity split
+    R *smf, *bsp, *sfpp;         // soot mass fraction, bs_soot_prev, sfp_soot_prev, parity split
+    R* rrms;                     // RRMS(MZ,NZ,LZ,5), cell layout (I fastest)
+};
+
+// ---- gas and soot band model (gas.cu) ------------------------------------------
+struct GasBuffers {
+    double *aklg, *akls;         // per cell (I fastest) and band: cell + l*ncell
+    double* fvs;                 // soot volume fraction, by loop order (K fastest)
+    int *setter, *blockmax;      // the cells that set AKLS, and the prefix maxima
+    int* err;                    // bit 1: BANDA argument < 0, bit 2: W_R <= 0 with CO2
+};
+int gas_scan_blocks(int ncell);
+// RAD_GAS and SOOTA of RAD0 (Rad0.f90:116-132) on the current T, P, DNST
+// and minor species: AKLG and AKLS of every open cell with T >= TG_MN
+template <typename R>
+int launch_gas_band(const GasBuffers& b, const GeoT<double>& g, const R* T, const R* P, const R* DNST,
+                    const R* const* gfm, const R* smf, double t0, double pg0, double dnst0, int nwl, const double* wl,
+                    cudaStream_t st);
+
 // fills slab_in_smem, smem, grid and part_base from the grid, the band count
 // and the SM count
 int rad_plan(RadArgs& a, int sms);
@@ -201,7 +227,8 @@ template <typename R> void launch_props(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_tave(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s);
-template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s, const double* gas_aklg = nullptr,
+                                               const double* gas_akls = nullptr);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);
 template <typename R> void launch_refine_rhs(const GeoT<R>& g, const Sys<R>& sys, R* rhs, cudaStream_t s);
 template <typename R> void launch_refine_add(const GeoT<R>& g, const Sys<R>& sys, const R* dx, cudaStream_t s);

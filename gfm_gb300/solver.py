@@ -69,6 +69,38 @@ class Fields:
                       self.i1st_rad_qe_done, self.factor, self.fadj, self.gfin0, self.q_h_in)
 
 
+class Minor:
+    """The minor species state of MSFLOW in the reference layout: gfm
+    (7, LP, NP, MP) C-order views of GFM(MP,NP,LP,7), smf and the soot
+    sources (LP, NP, MP), rrms (5, LZ, NZ, MZ)."""
+
+    def __init__(self, gfm, smf, bs_soot_prev, sfp_soot_prev, rrms, itr_ms: int = 0, imscon: int = 0):
+        self.gfm, self.smf, self.bs_soot_prev, self.sfp_soot_prev, self.rrms = gfm, smf, bs_soot_prev, sfp_soot_prev, rrms
+        self.itr_ms, self.imscon = itr_ms, imscon
+        self._c = None
+
+    @staticmethod
+    def empty(mp: int, np_: int, lp: int) -> "Minor":
+        z = lambda *sh: np.zeros(sh, dtype=np.float64)
+        return Minor(z(abi.NSP_MINOR, lp, np_, mp), z(lp, np_, mp), z(lp, np_, mp), z(lp, np_, mp),
+                     z(5, lp // 2, np_ // 2, mp // 2))
+
+    def to_c(self) -> abi.GfmMinor:
+        for a in (self.gfm, self.smf, self.bs_soot_prev, self.sfp_soot_prev, self.rrms):
+            assert a.flags.c_contiguous and a.dtype == np.float64
+        p = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._c = abi.GfmMinor(p(self.gfm), p(self.smf), p(self.bs_soot_prev), p(self.sfp_soot_prev), p(self.rrms),
+                               int(self.itr_ms), int(self.imscon))
+        return self._c
+
+    def update_scalars(self, m: abi.GfmMinor) -> None:
+        self.itr_ms, self.imscon = m.itr_ms, m.imscon
+
+    def copy(self) -> "Minor":
+        return Minor(self.gfm.copy(), self.smf.copy(), self.bs_soot_prev.copy(), self.sfp_soot_prev.copy(),
+                     self.rrms.copy(), self.itr_ms, self.imscon)
+
+
 class Case:
     """A built case (host arrays owned by the native library): a synthetic
     furnace (``Case(cfg)``) or a GFM case directory (``Case.from_files``)."""
@@ -97,12 +129,14 @@ class Case:
                    sigma_eps: float = 1.0, wall_sink: bool = False, t_wall_k: float = 1700.0,
                    rad_emission: bool = False, kappa=None, maxgi: int = 0,
                    adi_mode: int = abi.GFM_ADI_MARCH, precision: int = abi.GFM_PREC_FP64,
-                   lib: C.CDLL | None = None) -> "Case":
+                   gas_model: bool = False, lib: C.CDLL | None = None) -> "Case":
         """The start-up the Fortran host does from a case directory: reads
         gd<runum>c.dat, sbc<runum>c.dat, it<runum>t.dat (when present),
         relaxfactorc.txt (``relax``, default: in the case directory) and the
         kinetics table, and with ``restart`` the restart file rg<runum>c.d
-        (A0main.f90:158-190).  ``summary`` holds what GRID3/SBC derived."""
+        (A0main.f90:158-190).  ``summary`` holds what GRID3/SBC derived.
+        ``gas_model`` takes the absorption coefficients from RAD_GAS and
+        SOOTA on the minor species instead of ``kappa``."""
         import pathlib
         d = pathlib.Path(case_dir)
         it = d / f"it{runum}t.dat"
@@ -122,6 +156,7 @@ class Case:
         for l, k in enumerate(kappa or []):
             opt.kappa[l] = k
         opt.maxgi, opt.adi_mode, opt.precision = maxgi, adi_mode, precision
+        opt.gas_model = int(gas_model)
         summ = abi.GfmCaseSummary()
         rc = self.lib.gfm_case_read(C.byref(files), C.byref(opt), C.byref(self.c), C.byref(summ))
         if rc != abi.GFM_OK:
@@ -129,6 +164,20 @@ class Case:
         self.summary = summ.as_dict()
         self._dims()
         return self
+
+    def read_minor(self, path) -> "Minor":
+        """The minor species restart rs<runum>c.d (SAV3FM's records)."""
+        m = Minor.empty(self.mp, self.np, self.lp)
+        rc = self.lib.gfm_minor_read(str(path).encode(), C.byref(self.c.grid), C.byref(m.to_c()))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, f"gfm_minor_read failed for {path}")
+        m.itr_ms = m._c.itr_ms
+        return m
+
+    def write_minor(self, path, m: "Minor") -> None:
+        rc = self.lib.gfm_minor_write(str(path).encode(), C.byref(self.c.grid), C.byref(m.to_c()))
+        if rc != abi.GFM_OK:
+            raise GfmError(rc, f"gfm_minor_write failed for {path}")
 
     def t_surf_prev(self) -> np.ndarray:
         """T_surf_prev(MZ,NZ) (K) as an (NZ, MZ) C-order array."""
@@ -276,6 +325,17 @@ class GpuSolver:
 
     def rad_emission(self) -> None:
         self._check(self.lib.gfm_gpu_rad_emission(self.h))
+
+    def minor_upload(self, m: "Minor") -> None:
+        """The minor species state the band model (and MSFLOW) work on."""
+        self._check(self.lib.gfm_gpu_minor_upload(self.h, C.byref(m.to_c())))
+
+    def minor_download(self) -> "Minor":
+        out = Minor.empty(self.case.mp, self.case.np, self.case.lp)
+        c = out.to_c()
+        self._check(self.lib.gfm_gpu_minor_download(self.h, C.byref(c)))
+        out.update_scalars(c)
+        return out
 
     def rad_transfer(self) -> dict:
         """Volume radiation transfer from the current T (QE and QA replaced); the totals in W."""

@@ -109,6 +109,20 @@ typedef struct gfm_params {
     int    maxgi;
     int    adi_mode;             /* GFM_ADI_*                                  */
     int    precision;            /* GFM_PREC_*                                 */
+    /* minor species, soot and the gas band model (Var_mod.f90:134-137,
+     * 215-235, 465-509; &INPUT and relaxfactorc.txt, Setup.f90:476-511) */
+    int    gas_model;            /* 0: gray bands akl0; 1: RAD_GAS and SOOTA
+                                    from the minor species (Rad0.f90:116-132) */
+    int    maxms;                /* MSFLOW iterations, MAXMS (300)             */
+    int    ntimesm;              /* line-solver sweeps of the minor species    */
+    int    irstypm;              /* 1: minor species restart (IRSTYPM)         */
+    double bmcon;                /* MSFLOW convergence on resid_ms (BMCON)     */
+    double ssigma;               /* Schmidt number of the minor species (0.7) */
+    double rfm, rfm_soot;        /* relaxation of the species and of soot      */
+    double rf_soot_form, rf_soot_oxid;   /* soot source relaxation             */
+    double soot_cap, t0_sf, t0_so;       /* soot bound, cut-off T (K)          */
+    double aform, aoxid;         /* soot formation and oxidation constants     */
+    double esf_r, eso_r;         /* their activation energies over Ru (K)      */
 } gfm_params;
 
 /* ---- fields in the reference layout -------------------------------------- */
@@ -123,6 +137,32 @@ typedef struct gfm_fields {
     int    itr_gas, do_rad_qe_only_cnt, i1st_rad_qe_done;
     double factor, fadj, gfin0, q_h_in;
 } gfm_fields;
+
+/* ---- minor species and soot: the state of MSFLOW ------------------------- */
+#define GFM_NSP_MINOR 7
+typedef struct gfm_minor {
+    double *gfm;                 /* GFM(MP,NP,LP,7): CH4 O2 CO H2O CO2 N2 NO
+                                    mass fractions (Gslv3m.f90:122-129)        */
+    double *smf;                 /* soot mass fraction (MP,NP,LP)              */
+    double *bs_soot_prev, *sfp_soot_prev;   /* the last soot sources (MP,NP,LP) */
+    double *rrms;                /* RRMS(MZ,NZ,LZ,5) reaction rates            */
+    int    itr_ms;               /* MSFLOW iterations so far                   */
+    int    imscon;               /* the last MSFLOW met BMCON                  */
+} gfm_minor;
+
+/* What one MSFLOW call did (Msflow.f90:48-162, Gslv3m.f90:171-284). */
+typedef struct gfm_msflow_stats {
+    int    itr_ms;               /* cumulative MSFLOW iteration count          */
+    int    iterations;           /* iterations of this call                    */
+    int    converged;            /* imscon: every resid_ms <= BMCON            */
+    int    reserved;
+    double resid_ms_pre[8], resid_ms[8];    /* 7 species then soot             */
+    double bal_ms;               /* mean |1 - sum of GFM| (Gslv3m.f90:196-218) */
+    double soot_tot;             /* soot mass in the furnace (kg)              */
+    double smf_max, smf_max_noclip;
+    double gfm_out[7];           /* GFM_0(L,2): species flow out (kg/s)        */
+    double svf_r;                /* area-mean soot volume fraction at the exits */
+} gfm_msflow_stats;
 
 /* ---- per-iteration statistics (the reference's .plt log quantities) ------ */
 typedef struct gfm_iter_stats {
@@ -257,6 +297,8 @@ typedef struct gfm_case_options {
                              place of the band model of RAD_GAS                  */
     int    maxgi;         /* > 0: replaces &INPUT MAXGI                           */
     int    adi_mode, precision;
+    int    gas_model;     /* 1: RAD_GAS and SOOTA on the minor species in the
+                             place of kappa (needs MS=1 in &INPUT)               */
 } gfm_case_options;
 
 /* What GRID3 and SBC derived, as the reference prints it at the head of
@@ -304,6 +346,14 @@ int  gfm_case_write_files(const gfm_case_spec *spec, const char *dir,
  * i1st_rad_done, itr_gas, itr_rad/itr_gend and interval_rad. */
 int  gfm_restart_write(const char *path, const gfm_grid *grid,
                        const gfm_fields *f, const gfm_restart_tail *tail);
+
+/* Reads / writes the minor species restart rs####c.d in the record layout of
+ * SAV3FM (Sav3f.f90:96-117; read by INITSVM, Initsv.f90:350-372): one record
+ * GFM(1:7), smf per cell centre in I, J, K loop order, then bs_soot_prev,
+ * sfp_soot_prev, RRMS and itr_ms.  `out`'s arrays are the caller's, sized
+ * by the grid. */
+int  gfm_minor_read(const char *path, const gfm_grid *grid, gfm_minor *out);
+int  gfm_minor_write(const char *path, const gfm_grid *grid, const gfm_minor *m);
 
 /* ---- GPU solver ---------------------------------------------------------- */
 /* Query: number of CUDA devices usable (>=1) or a negative status. */
@@ -401,6 +451,14 @@ int  gfm_gpu_rad_transfer(gfm_handle *h, gfm_rad_totals *out);
 int  gfm_gpu_wall_setup(gfm_handle *h, const gfm_wall_spec *spec);
 int  gfm_gpu_wall_totals(gfm_handle *h, gfm_wall_totals *out);
 int  gfm_gpu_wall_get(gfm_handle *h, const char *name, double *out, int cap);
+/* Minor species and soot on the device (ms=1 of the reference).
+ * gfm_gpu_minor_upload / _download move the MSFLOW state.  With
+ * params.gas_model = 1 the emission and the volume transfer take their
+ * absorption coefficients from RAD_GAS and SOOTA on this state
+ * (Rad0.f90:116-132, Rad_gas.f90:16-395, Rad_soot.f90:26-69) instead of the
+ * gray akl0; they return GFM_E_ARG until a state has been uploaded. */
+int  gfm_gpu_minor_upload(gfm_handle *h, const gfm_minor *m);
+int  gfm_gpu_minor_download(gfm_handle *h, gfm_minor *m);
 /* Device times (CUDA events on the handle's stream) accumulated since the
  * last reset: adi_ms = line-solver batches, gflow_ms = whole GFLOW calls
  * (first to last iteration of each gfm_gpu_gflow), other_ms reserved;

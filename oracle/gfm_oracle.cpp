@@ -7,6 +7,7 @@
 // -ffp-contract=off so x86 and Arm hosts give the same bits.
 #include "gfm_oracle.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -187,6 +188,281 @@ double RIF3(double X) {   // RIF(3,0,X), Rad_fun.f90:45-91
     return rif > 1.0 ? 1.0 : rif;
 }
 
+// ---------------------------------------------------------------------------
+// Gas and soot band model of RAD0's open cells (Rad_gas.f90, Rad_soot.f90):
+// the module variables the routines share (T_RAD, TT0, P_RAD, YCO2, YH2O,
+// FVS, OPL, W_R, PE, AAH2O, AACO2, AKLG, AKLS) live in one object that is
+// reused from cell to cell as the reference's globals are.  Two of them carry
+// over between cells: AKLS when a cell's FVS < 1e-14 (SOOTA returns without
+// setting it, Rad_soot.f90:29) and AACO2 when W_R <= 0 (Rad_gas.f90:233).
+// ---------------------------------------------------------------------------
+const double HCK_R = 1.439e-2, T0_R = 1.0e2, P0_R = 1.01325e5;     // Var_mod.f90:134-136
+const double PI_R = 3.141592653589793;
+const double DNST_SOOT = 1.8e3;                                     // Var_mod.f90:137
+const double WMS[7] = {16.0426, 31.9988, 28.0104, 18.0152, 44.0098, 28.0134, 30.0061};   // Var_mod.f90:223-229
+
+double PER(int M, int N) {   // Rad_fun.f90:14-31 (M >= N always holds here)
+    double p = 1.0;
+    if (M == 0 || N == 0) return p;
+    for (int I = M - N + 1; I <= M; ++I) p = p * I;
+    return p;
+}
+
+struct RadGas {
+    int NWL = 0;
+    const double* WL = nullptr;        // band edges (m), 0-based
+    double T_RAD = 0, TT0 = 0, P_RAD = 0, YCO2 = 0, YH2O = 0, FVS = 0, OPL = 0, W_R = 0, PE = 0;
+    double AAH2O[6] = {0}, AACO2[7] = {0};           // 1-based
+    double WNH2O[6][4], WNCO2[7][4], WNG[12][3];     // 1-based
+    vec AKLG, AKLS, AKL0, E0;                        // 1-based, NWL
+    int error = 0;                                   // BANDA's stop_run condition (Rad_gas.f90:368-371)
+
+    void init(int nwl, const double* wl) {   // RAD0's ALLOCATE + zero (Rad0.f90:22-28)
+        NWL = nwl; WL = wl;
+        AKLG.assign(NWL + 1, 0.0); AKLS.assign(NWL + 1, 0.0); AKL0.assign(NWL + 1, 0.0); E0.assign(NWL + 1, 0.0);
+    }
+    double wl(int n) const { return WL[n - 1]; }
+
+    // CHIWHI (Rad_gas.f90:308-348): WHI divides by SQRT(TT0), the value of
+    // the current cell, also when TT is T0_R
+    void CHIWHI(double TT, const double V[4], const int NG[4], const int ND_R[4], double& CHI, double& WHI) {
+        if (ND_R[1] != 0 || ND_R[2] != 0 || ND_R[3] != 0) {
+            double U[4], UD = ZERO, XD = ZERO, XY = ZERO, YN = ZERO;
+            int NV[4];
+            for (int K = 1; K <= 3; ++K) {
+                U[K] = HCK_R * V[K] / TT;
+                NV[K] = 0;
+                if (ND_R[K] < 0) NV[K] = std::abs(ND_R[K]);
+                const int NDK = std::abs(ND_R[K]);
+                double Y1 = ZERO;
+                for (;;) {
+                    const double XGAS = std::exp(-U[K] * NV[K]) / PER(NG[K] - 1, NG[K] - 1);
+                    const double X1 = XGAS * PER(NV[K] + NG[K] + NDK - 1, NG[K] + NDK - 1);
+                    const double X2 = XGAS * PER(NV[K] + NG[K] - 1, NG[K] - 1);
+                    if (X1 < 1.0e-10) break;
+                    XY = XY + X1;
+                    XD = XD + X2;
+                    Y1 = Y1 + std::sqrt(X1);
+                    NV[K] = NV[K] + 1;
+                    if (NV[K] >= 100) break;
+                }
+                YN = YN + Y1 * Y1;
+                UD = UD - U[K] * ND_R[K];
+            }
+            CHI = (ONE - std::exp(UD)) * XY / XD;
+            WHI = YN / XY / std::sqrt(TT0);
+        } else {
+            CHI = ONE;
+            WHI = ONE / std::sqrt(TT0);
+        }
+    }
+    double BANDA(double ALP, double BTA, double A0) {   // Rad_gas.f90:360-395
+        if (A0 <= 0) return 0;
+        if (ALP < ZERO || BTA < ZERO || A0 < ZERO || W_R * PE < 0) { error = 1; return 0; }
+        if (W_R * PE == 0) return 0;
+        const double ETA = BTA * PE;
+        const double TAU = ALP * W_R / A0;
+        double A_S;
+        if (ETA >= ONE) {
+            A_S = TAU <= 1.0 ? TAU : 1.0 + std::log(TAU);
+        } else if (TAU <= ETA) {
+            A_S = TAU;
+        } else if (TAU <= 1 / ETA) {
+            A_S = 2.0 * std::sqrt(ETA * TAU) - ETA;
+        } else {
+            A_S = std::log(ETA * TAU) + 2.0 - ETA;
+        }
+        return A0 * A_S;
+    }
+    double A1(const double V[4], const int NG[4], const double B[4], const int ND_R[4]) {   // Rad_gas.f90:284-296
+        double CHI0, WHI0, CHI, WHI;
+        CHIWHI(T0_R, V, NG, ND_R, CHI0, WHI0);
+        CHIWHI(T_RAD, V, NG, ND_R, CHI, WHI);
+        const double C3 = B[3] * std::sqrt(T_RAD / T0_R);
+        const double C1 = B[1] * CHI / CHI0;
+        const double C2 = 2.0 * std::sqrt(C1 * C3 * B[2] * WHI / WHI0);
+        return BANDA(C1, C2, C3);
+    }
+    void AH2O() {   // Rad_gas.f90:149-212
+        const int NG[4] = {0, 1, 1, 1};
+        const double V[4] = {0, 3.652e+5, 1.595e+5, 3.756e+5};
+        double AA[6] = {0}, B[4] = {0};
+        int ND_R[4] = {0, 0, 0, 0};
+        for (int n = 1; n <= 5; ++n) AAH2O[n] = 0;
+        if (YH2O <= ZERO || T_RAD <= 3.0e+2) return;
+        PE = P_RAD + P_RAD * YH2O * (0.86e+1 / TT0 - 0.5);
+        W_R = P_RAD * YH2O * OPL / T_RAD / 8.208e-2 * WH2O;
+        B[1] = 0.52e+4 * std::exp(-0.176e+2 / TT0); B[2] = 0.14311; B[3] = 0.284e+2;
+        ND_R[1] = ND_R[2] = ND_R[3] = 0;
+        AA[1] = A1(V, NG, B, ND_R);
+        B[1] = 0.412e+2; B[2] = 0.9427e-1; B[3] = 0.564e+2;
+        ND_R[2] = 1;
+        AA[2] = A1(V, NG, B, ND_R);
+        B[1] = 0.19; B[2] = 0.13219; B[3] = 0.6e+2;
+        ND_R[2] = 2;
+        double CHI0, WHI0, CHI, WHI;
+        CHIWHI(T0_R, V, NG, ND_R, CHI0, WHI0);
+        CHIWHI(T_RAD, V, NG, ND_R, CHI, WHI);
+        const double T1 = B[1] * CHI / CHI0, T4 = B[2] * WHI / WHI0;
+        B[1] = 0.23e+1; ND_R[1] = 1; ND_R[2] = 0;
+        CHIWHI(T0_R, V, NG, ND_R, CHI0, WHI0);
+        CHIWHI(T_RAD, V, NG, ND_R, CHI, WHI);
+        const double T2 = B[1] * CHI / CHI0, T5 = B[2] * WHI / WHI0;
+        B[1] = 0.224e+2; ND_R[1] = 0; ND_R[3] = 1;
+        CHIWHI(T0_R, V, NG, ND_R, CHI0, WHI0);
+        CHIWHI(T_RAD, V, NG, ND_R, CHI, WHI);
+        const double T3 = B[1] * CHI / CHI0, T6 = B[2] * WHI / WHI0;
+        const double C1 = T1 + T2 + T3;
+        const double C3 = B[3] * TT0;
+        const double BTA = 2.0 * std::sqrt(C3) * (std::sqrt(T1 * T4) + std::sqrt(T2 * T5) + std::sqrt(T3 * T6));
+        AA[3] = BANDA(C1, BTA, C3);
+        B[1] = 3.0; B[2] = 0.8169e-1; B[3] = 0.431e2;
+        ND_R[2] = 1;
+        AA[4] = A1(V, NG, B, ND_R);
+        B[1] = 0.25e+1; B[2] = 0.11628; B[3] = 0.32e+2;
+        ND_R[1] = 1; ND_R[2] = 0;
+        AA[5] = A1(V, NG, B, ND_R);
+        for (int n = 1; n <= 5; ++n) AAH2O[n] = AA[n] * 1.0e+2;
+    }
+    void ACO2() {   // Rad_gas.f90:224-274
+        const int NG[4] = {0, 1, 2, 1};
+        const double V[4] = {0, 1.351e+5, 6.67e+4, 2.396e+5};
+        double AA[7] = {0}, B[4] = {0};
+        int ND_R[4] = {0, 0, 0, 0};
+        W_R = P_RAD * YCO2 * OPL / T_RAD / 8.208e-2 * WCO2;
+        if (W_R <= ZERO) return;
+        PE = std::pow(P_RAD + P_RAD * YCO2 * 0.3, 0.7);
+        B[1] = 0.19e+2; B[2] = 0.6157e-1; B[3] = 0.127e2;
+        ND_R[1] = 0; ND_R[2] = 1; ND_R[3] = 0;
+        AA[1] = A1(V, NG, B, ND_R);
+        PE = std::pow(P_RAD + P_RAD * YCO2 * 0.3, 0.8);
+        B[1] = 0.36; B[2] = 0.4017e-1; B[3] = 0.134e+2;
+        ND_R[1] = -1; ND_R[2] = 0; ND_R[3] = 1;
+        AA[2] = A1(V, NG, B, ND_R);
+        B[1] = 0.24; B[2] = 0.11888; B[3] = 0.101e+2;
+        AA[3] = A1(V, NG, B, ND_R);
+        B[1] = 0.11e+3; B[2] = 0.24723; B[3] = 0.112e+2;
+        ND_R[1] = 0;
+        AA[4] = A1(V, NG, B, ND_R);
+        PE = std::pow(P_RAD + P_RAD * YCO2 * 0.3, 0.65);
+        B[1] = 4.0; B[2] = 0.13341; B[3] = 23.5;
+        ND_R[1] = 1;
+        AA[5] = A1(V, NG, B, ND_R);
+        B[1] = 0.66e-1; B[2] = 0.39305; B[3] = 0.345e+2;
+        ND_R[1] = 2;
+        AA[6] = A1(V, NG, B, ND_R);
+        for (int n = 1; n <= 6; ++n) AACO2[n] = AA[n] * 1.0e+2;
+    }
+    static void SOC(double WL0, double& XN_K, double& X2NK) {   // Rad_soot.f90:49-69
+        const double SOCF[3] = {7.2e+26, 4.07e+27, 4.47e+28};
+        const double SOCH[3] = {1.2e+15, 5.90e+15, 5.60e+15};
+        const double SOCW[3] = {0.0, 1.25e+15, 7.25e+15};
+        const double C_0 = 2.9984e+8, E2ME0 = 3.185e+3;
+        XN_K = ONE;
+        X2NK = ZERO;
+        const double W = TWO * PI_R * C_0 / WL0;
+        for (int J = 0; J < 3; ++J) {
+            const double A = SOCW[J] * SOCW[J] - W * W;
+            const double B = A * A + W * W * SOCH[J] * SOCH[J];
+            if (B < 1.0e-20) return;
+            const double G0 = SOCF[J] * E2ME0;
+            XN_K = XN_K + G0 * A / B;
+            X2NK = X2NK + G0 * SOCH[J] * W / B;
+        }
+    }
+    void SOOTA() {   // Rad_soot.f90:26-37
+        if (FVS < 1.0e-14) return;
+        for (int N = 1; N <= NWL; ++N) {
+            const double WL0 = wl(N);
+            double XN_K, X2NK;
+            SOC(WL0, XN_K, X2NK);
+            const double G0 = 18.0 * PI_R * X2NK / ((XN_K + TWO) * (XN_K + TWO) + X2NK * X2NK);
+            AKLS[N] = G0 * FVS / WL0;
+        }
+    }
+    void RAD_GAS() {   // Rad_gas.f90:16-137
+        const double EPS1 = 1.0e-4;
+        for (int n = 0; n < 6; ++n) for (int m = 0; m < 4; ++m) WNH2O[n][m] = 0;
+        for (int n = 0; n < 7; ++n) for (int m = 0; m < 4; ++m) WNCO2[n][m] = 0;
+        for (int n = 0; n < 12; ++n) for (int m = 0; m < 3; ++m) WNG[n][m] = 0;
+        for (int n = 1; n <= NWL; ++n) AKLG[n] = ZERO;
+        if (YH2O > EPS1) {
+            WNH2O[1][1] = 0;
+            WNH2O[2][2] = 1.60e+5; WNH2O[3][2] = 3.76e+5; WNH2O[4][2] = 5.35e+5; WNH2O[5][2] = 7.25e+5;
+            AH2O();
+            WNH2O[1][2] = AAH2O[1] / 2;
+            WNH2O[1][3] = AAH2O[1];
+            for (int N = 2; N <= 5; ++N) {
+                const double G0 = AAH2O[N] / 2;
+                WNH2O[N][1] = WNH2O[N][2] - G0;
+                WNH2O[N][3] = WNH2O[N][2] + G0;
+                if (WNH2O[N - 1][3] > WNH2O[N][1]) WNH2O[N - 1][3] = WNH2O[N][1];
+            }
+        }
+        if (YCO2 > EPS1) {
+            WNCO2[1][2] = 6.67e+4; WNCO2[2][2] = 9.60e+4; WNCO2[3][2] = 1.06e+5;
+            WNCO2[4][3] = 2.41e+5; WNCO2[5][2] = 3.66e+5; WNCO2[6][2] = 5.20e+5;
+            ACO2();
+            for (int N = 1; N <= 6; ++N) {
+                const double G0 = AACO2[N] / 2;
+                if (N == 1 && G0 > WNCO2[1][2]) {
+                    WNCO2[1][1] = 0;
+                    WNCO2[1][3] = AACO2[1];
+                } else if (N == 4) {
+                    WNCO2[N][2] = WNCO2[N][3] - G0;
+                    WNCO2[N][1] = WNCO2[N][2] - G0;
+                } else {
+                    WNCO2[N][1] = WNCO2[N][2] - G0;
+                    WNCO2[N][3] = WNCO2[N][2] + G0;
+                }
+                if (N <= 1) continue;
+                if (WNCO2[N - 1][3] > WNCO2[N][1]) WNCO2[N - 1][3] = WNCO2[N][1];
+            }
+        }
+        SOOTA();
+        for (int n = 1; n <= 5; ++n) { WNG[n][1] = WNH2O[n][1]; WNG[n][2] = WNH2O[n][3]; }
+        for (int n = 1; n <= 6; ++n) { WNG[n + 5][1] = WNCO2[n][1]; WNG[n + 5][2] = WNCO2[n][3]; }
+        for (int N = 1; N <= 10; ++N) {
+            for (int N2 = N + 1; N2 <= 11; ++N2) {
+                if (WNG[N][1] < WNG[N2][1]) continue;
+                std::swap(WNG[N][1], WNG[N2][1]);
+                std::swap(WNG[N][2], WNG[N2][2]);
+            }
+            if (N <= 1) continue;
+            if (WNG[N - 1][2] > WNG[N][1]) WNG[N - 1][2] = WNG[N][1];
+        }
+        double WL2 = 10 / wl(1);
+        for (int n = 1; n <= NWL; ++n) E0[n] = ZERO;
+        int N0 = 11;
+        for (int N = 1; N <= NWL; ++N) {
+            const double WL1 = N == NWL ? 0 : 1 / wl(N);
+            if (WL2 <= WL1 || WNG[11][2] <= WL1) { WL2 = WL1; continue; }
+            for (int N1 = N0; N1 >= 1; --N1) {
+                if (WNG[N1][2] <= WL1) { N0 = N1; break; }
+                if (WNG[N1][2] >= WL1 && WNG[N1][2] <= WL2) {
+                    if (WNG[N1][1] < WL1) {
+                        E0[N] = E0[N] + WNG[N1][2] - WL1;
+                        WNG[N1][2] = WL1;
+                        N0 = N1;
+                        break;
+                    }
+                    E0[N] = E0[N] + WNG[N1][2] - WNG[N1][1];
+                }
+            }
+            if (E0[N] <= 0 || WL2 <= WL1) {
+                AKLG[N] = ZERO;
+            } else {
+                E0[N] = E0[N] / (WL2 - WL1);
+                double G0 = 1 - E0[N];
+                if (G0 <= 1.0e-20) G0 = 1.0e-20;
+                AKLG[N] = -std::log(G0) / OPL;
+            }
+            WL2 = WL1;
+        }
+        for (int n = 1; n <= NWL; ++n) AKL0[n] = AKLG[n] + AKLS[n];
+    }
+};
+
 double ZY1(const double* X, const double* Y, double X1, int N) {   // Source.f90:814-831
     if (X1 < X[0]) return Y[0] * X1 / X[0];
     for (int I = 2; I <= N; ++I)
@@ -231,6 +507,11 @@ struct Oracle {
     vec RTIM, DELRT, HRT, DELR, TIMED, HRD;
     int NWL;
     vec WL, AKL0;
+    // minor species and soot (ms=1, Setup.f90:904-929): GFM(MP,NP,LP,7), smf,
+    // the soot sources of the last MSFLOW iteration, RRMS(MZ,NZ,LZ,5)
+    vec GFMS, SMF, BS_SOOT_PREV, SFP_SOOT_PREV, RRMS, AP1;
+    int itr_ms = 0, imscon = 0, IGS0 = 0, minor_on = 0;
+    double resid_ms[9] = {0}, resid_ms_pre[9] = {0};
     // state scalars
     int itr_gas, do_rad_qe_only_cnt, i1st_rad_qe_done, NELG;
     double FACTOR, FADJ, GFIN0, GFIN, GFEX, SGM, q_h_in;
@@ -254,6 +535,21 @@ struct Oracle {
     double& as(int i, int j, int k, int l, int m) { return AS[ix(i, j, k) + (long)((l - 1) * 2 + (m - 1)) * N]; }
     Y9 y9(int i, int j, int k) { return Y9{&GF[ix(i, j, k)], N}; }
     long cix(int id2, int jd2, int kd2) const { return (long)(id2 - 1) + (long)MZ * ((long)(jd2 - 1) + (long)NZ * (long)(kd2 - 1)); }
+    double& gfm(int i, int j, int k, int l) { return GFMS[ix(i, j, k) + (long)(l - 1) * N]; }
+    double& rrms(int id2, int jd2, int kd2, int l) { return RRMS[cix(id2, jd2, kd2) + (long)(l - 1) * MZ * NZ * LZ]; }
+    // RAD0's inputs of RAD_GAS for one open cell, T_RAD in kelvin
+    // (Rad0.f90:118-123 with wmix_ms_calc, Prop.f90:207-218)
+    void rad_gas_inputs(RadGas& g, int I, int J, int K, double T_RAD) {
+        g.T_RAD = T_RAD;
+        g.TT0 = std::sqrt(T_RAD / T0_R);
+        g.P_RAD = (ONE + a3(P, I, J, K)) * pr.pg0 / P0_R;
+        double sum = ZERO;
+        for (int n = 1; n <= 7; ++n) sum = sum + gfm(I, J, K, n) / WMS[n - 1];
+        const double wmix_ms = ONE / sum;
+        g.YCO2 = gfm(I, J, K, 5) * wmix_ms / WCO2;
+        g.YH2O = gfm(I, J, K, 4) * wmix_ms / WH2O;
+        g.FVS = a3(SMF, I, J, K) * a3(DNST, I, J, K) * pr.dnst0 / DNST_SOOT;
+    }
 
     // ---- Grid3.f90 metric functions -----------------------------------------
     double DXAV(int I, int J, int K) {
@@ -1956,22 +2252,26 @@ struct Oracle {
                 }
         Tave = tave * pr.t0 / rho_vol_tot;
     }
-    void rad_qe_only() {   // Rad_emis.f90:411-466 with RAD0 (Rad0.f90:112-157), gray bands
+    void rad_qe_only() {   // Rad_emis.f90:411-466 with RAD0 (Rad0.f90:112-157); gray bands or RAD_GAS
         std::vector<double> qe2(QE.size(), 0.0);
         for (auto& t : T) t = t * pr.t0;
         double SGN = pr.sig * pr.ri * pr.ri;
         std::vector<double> DEB0(NWL), DEB(NWL);
         for (int l = 0; l < NWL; ++l) DEB0[l] = pr.hck / pr.ri / WL[l];
+        RadGas rg;
+        rg.init(NWL, WL.data());
         for (int I = 2; I <= MP; I += 2)
             for (int J = 2; J <= NP; J += 2)
                 for (int K = 2; K <= LP; K += 2) {
                     double T_RAD = a3(T, I, J, K);
                     if (!(ibcell(I, J, K) <= 0 && T_RAD >= 300.0)) continue;
+                    if (pr.gas_model) rad_gas_inputs(rg, I, J, K, T_RAD);
                     double VOL = VOL_C(I, J, K);
                     double SA = ((DX[I] * DR[J]) + (DR[J] * DZ[K]) + (DX[I] * DZ[K])) * TWO;
                     if (SA <= small16) continue;
                     double OPL = 6.0 * VOL / SA;
                     if (OPL <= 1.0e-10) continue;
+                    if (pr.gas_model) { rg.OPL = OPL; rg.RAD_GAS(); }
                     // DEBX (Rad_fun.f90:122-140)
                     double EB0 = 0;
                     for (int L = 1; L <= NWL - 1; ++L) {
@@ -1984,7 +2284,7 @@ struct Oracle {
                     double t2 = T_RAD * T_RAD;
                     double area_sgn_t4 = SA * SGN * (t2 * t2);
                     double sum = ZERO;
-                    for (int l = 0; l < NWL; ++l) sum = sum + DEB[l] * EMF(AKL0[l], OPL);
+                    for (int l = 0; l < NWL; ++l) sum = sum + DEB[l] * EMF(pr.gas_model ? rg.AKL0[l + 1] : AKL0[l], OPL);
                     qe2[cix(I / 2, J / 2, K / 2)] = area_sgn_t4 * sum;
                 }
         i1st_rad_qe_done = 1;
@@ -2739,28 +3039,36 @@ struct RadVolume {
                 }
         for (auto& t : o.T) t = t * o.pr.t0;
         if (o.wall_on) o.wall_start();
-        // RAD0 (Rad0.f90:22-42, 112-166) with gray bands: AKLG = AKL0, AKLS = 0
+        // RAD0 (Rad0.f90:22-42, 112-166): RAD_GAS and SOOTA on the minor
+        // species, or gray bands (AKLG = AKL0, AKLS = 0)
         SGN = o.pr.sig * o.pr.ri * o.pr.ri;
         for (int L = 1; L <= NWL; ++L) DEB0[L] = o.pr.hck / o.pr.ri / o.WL[L - 1];
         TG_MN = 300;
         AKL.assign(NC * NWL, 0.0);
+        RadGas rg;
+        rg.init(NWL, o.WL.data());
         for (int I = 2; I <= MP; I += 2)
             for (int J = 2; J <= NP; J += 2)
                 for (int K = 2; K <= LP; K += 2) {
                     const double T_RAD = o.a3(o.T, I, J, K);
                     if (!(ibr(I, J, K) <= 0 && T_RAD >= TG_MN)) continue;   // walls: emissivities, used only by the wall exchange
+                    if (o.pr.gas_model) o.rad_gas_inputs(rg, I, J, K, T_RAD);
                     const double VOL = o.VOL_C(I, J, K);
                     const double SA = ((o.DX[I] * o.DR[J]) + (o.DR[J] * o.DZ[K]) + (o.DX[I] * o.DZ[K])) * TWO;
                     if (SA <= small16) continue;
                     const double OPL = 6.0 * VOL / SA;
                     if (OPL <= 1.0e-10) continue;
+                    if (o.pr.gas_model) { rg.OPL = OPL; rg.RAD_GAS(); }
                     DEBX(T_RAD);
                     const double area_sgn_t4 = SA * SGN * T4(T_RAD);
                     double sg = ZERO, ss = ZERO;
                     for (int L = 1; L <= NWL; ++L) {
-                        akl(I / 2, J / 2, K / 2, L) = EMF(o.AKL0[L - 1], OPL);
-                        sg = sg + DEB[L] * EMF(o.AKL0[L - 1], OPL);
-                        ss = ss + DEB[L] * EMF(ZERO, OPL);
+                        const double a0 = o.pr.gas_model ? rg.AKL0[L] : o.AKL0[L - 1];
+                        const double ag = o.pr.gas_model ? rg.AKLG[L] : o.AKL0[L - 1];
+                        const double as = o.pr.gas_model ? rg.AKLS[L] : ZERO;
+                        akl(I / 2, J / 2, K / 2, L) = EMF(a0, OPL);
+                        sg = sg + DEB[L] * EMF(ag, OPL);
+                        ss = ss + DEB[L] * EMF(as, OPL);
                     }
                     tot_qe_h2o_co2 = tot_qe_h2o_co2 + (area_sgn_t4 * sg);
                     tot_qe_soot = tot_qe_soot + (area_sgn_t4 * ss);
@@ -2888,6 +3196,7 @@ int gfo_gflow_steps(void* vo, int stop_after) {
 int gfo_gflow(void* vo, int n_iter, gfm_iter_stats* out, int* n_done) {
     Oracle* o = static_cast<Oracle*>(vo);
     if (!o || n_iter < 0) return GFM_E_ARG;
+    if (o->pr.rad_emission && o->pr.gas_model && !o->minor_on) return GFM_E_ARG;
     int done = 0, conv = 0;
     for (int it = 0; it < n_iter; ++it) {
         o->itr_gas = o->itr_gas + 1;
@@ -2982,6 +3291,7 @@ double gfo_atand(double x) { return ATAND(x); }
 int gfo_rad_transfer(void* vo, gfm_rad_totals* out) {
     Oracle* o = static_cast<Oracle*>(vo);
     if (!o || o->NWL < 1) return GFM_E_ARG;
+    if (o->pr.gas_model && !o->minor_on) return GFM_E_ARG;
     RadVolume rv(*o);
     rv.run();
     if (out) {
@@ -3048,6 +3358,42 @@ int gfo_wall_totals(void* vo, gfm_wall_totals* t) {
     t->rel_rad_chg_mean = o->last_rel_rad_chg_mean;
     return GFM_OK;
 }
+int gfo_rad_emission(void* vo) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || o->NWL < 1) return GFM_E_ARG;
+    if (o->pr.gas_model && !o->minor_on) return GFM_E_ARG;
+    o->rad_qe_only();
+    return GFM_OK;
+}
+
+int gfo_minor_set(void* vo, const gfm_minor* m) {
+    if (!vo || !m || !m->gfm || !m->smf || !m->bs_soot_prev || !m->sfp_soot_prev || !m->rrms) return GFM_E_ARG;
+    Oracle* o = static_cast<Oracle*>(vo);
+    const long NCA = (long)o->MZ * o->NZ * o->LZ;
+    copy_in(o->GFMS, m->gfm, 7 * o->N);
+    copy_in(o->SMF, m->smf, o->N);
+    copy_in(o->BS_SOOT_PREV, m->bs_soot_prev, o->N);
+    copy_in(o->SFP_SOOT_PREV, m->sfp_soot_prev, o->N);
+    copy_in(o->RRMS, m->rrms, 5 * NCA);
+    o->itr_ms = m->itr_ms;
+    o->imscon = m->imscon;
+    o->minor_on = 1;
+    return GFM_OK;
+}
+int gfo_minor_get(void* vo, gfm_minor* m) {
+    if (!vo || !m || !m->gfm || !m->smf || !m->bs_soot_prev || !m->sfp_soot_prev || !m->rrms) return GFM_E_ARG;
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o->minor_on) return GFM_E_ARG;
+    std::copy(o->GFMS.begin(), o->GFMS.end(), m->gfm);
+    std::copy(o->SMF.begin(), o->SMF.end(), m->smf);
+    std::copy(o->BS_SOOT_PREV.begin(), o->BS_SOOT_PREV.end(), m->bs_soot_prev);
+    std::copy(o->SFP_SOOT_PREV.begin(), o->SFP_SOOT_PREV.end(), m->sfp_soot_prev);
+    std::copy(o->RRMS.begin(), o->RRMS.end(), m->rrms);
+    m->itr_ms = o->itr_ms;
+    m->imscon = o->imscon;
+    return GFM_OK;
+}
+
 double gfo_rif3(double x) { return RIF3(x); }
 double gfo_zy1(const double* x, const double* y, double x1, int n) { return ZY1(x, y, x1, n); }
 double gfo_t_to_enth(const double* y, double t_norm) {
@@ -3241,6 +3587,11 @@ int gfo_case_build(const gfm_case_spec* sp, const char* kinetic_path, gfm_case* 
     P.rad_emission = sp->rad_emission; P.rad_qe_frequency = 10;
     P.sig = 5.668e-8; P.ri = 1.0; P.hck = 1.439e-2;
     P.bgcon = sp->bgcon; P.maxgi = sp->maxgi; P.adi_mode = sp->adi_mode; P.precision = sp->precision;
+    // minor species defaults (Var_mod.f90:215, 474-492; relaxfactorc.txt)
+    P.gas_model = 0; P.maxms = 300; P.ntimesm = 4; P.irstypm = 0; P.bmcon = 1.0e-7; P.ssigma = 0.7;
+    P.rfm = 0.5; P.rfm_soot = 0.2; P.rf_soot_form = 0.3; P.rf_soot_oxid = 0.3;
+    P.soot_cap = 4.0e-3; P.t0_sf = 0.0; P.t0_so = 0.0; P.aform = 400.0; P.aoxid = 26.0;
+    P.esf_r = 5.0e7 / 8.3143e+3; P.eso_r = 5.0e7 / 8.3143e+3;
 
     // fields at allocation (Setup.f90:747-779)
     s.p.assign(N, 0.0); s.t.assign(N, 1.0); s.dnst.assign(N, 1.0); s.theta.assign(N, 1.0);

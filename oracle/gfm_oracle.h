@@ -55,6 +55,14 @@ int   gfo_rad_transfer(void *o, gfm_rad_totals *out);
 int   gfo_wall_setup(void *o, const gfm_wall_spec *spec);
 int   gfo_wall_patch_list(void *o, int *out, int cap);
 int   gfo_wall_totals(void *o, gfm_wall_totals *t);
+/* Minor species and soot (ms=1): the MSFLOW state, arrays sized by the grid
+ * as in gfm_minor.  With params.gas_model = 1, RAD0 runs RAD_GAS and SOOTA
+ * on this state in gfo_rad_transfer and in the emission updates. */
+int   gfo_minor_set(void *o, const gfm_minor *m);
+/* The emission-only source QE from the current state (rad_qe_only,
+ * Rad_emis.f90:411-466 with RAD0). */
+int   gfo_rad_emission(void *o);
+int   gfo_minor_get(void *o, gfm_minor *m);
 double gfo_rif3(double x);
 double gfo_zy1(const double *x, const double *y, double x1, int n);
 /* y: 9 GF components; returns normalised enthalpy / temperature */

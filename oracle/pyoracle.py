@@ -47,6 +47,9 @@ def load(check_bounds: bool = False) -> C.CDLL:
     lib.gfo_wall_setup.argtypes = [C.c_void_p, C.POINTER(abi.GfmWallSpec)]
     lib.gfo_wall_patch_list.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.c_int]
     lib.gfo_wall_totals.argtypes = [C.c_void_p, C.POINTER(abi.GfmWallTotals)]
+    lib.gfo_minor_set.argtypes = [C.c_void_p, C.POINTER(abi.GfmMinor)]
+    lib.gfo_minor_get.argtypes = [C.c_void_p, C.POINTER(abi.GfmMinor)]
+    lib.gfo_rad_emission.argtypes = [C.c_void_p]
     for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1", "gfo_atand"):
         getattr(lib, n).restype = C.c_double
     lib.gfo_da.argtypes = [C.c_double, C.c_double]
@@ -154,6 +157,29 @@ class Oracle:
         got = self.lib.gfo_get_array(self.o, name.encode(), abi.dptr(out), out.size)
         if got != out.size:
             raise KeyError(name)
+        return out
+
+    def rad_emission(self) -> None:
+        """The emission-only source QE from the current T (rad_qe_only)."""
+        rc = self.lib.gfo_rad_emission(self.o)
+        if rc != 0:
+            raise RuntimeError(f"gfo_rad_emission: {rc}")
+
+    def minor_set(self, m) -> None:
+        """The minor species state (a gfm_gb300.solver.Minor) the band model
+        and MSFLOW work on."""
+        rc = self.lib.gfo_minor_set(self.o, C.byref(m.to_c()))
+        if rc != 0:
+            raise RuntimeError(f"gfo_minor_set: {rc}")
+
+    def minor_get(self):
+        from gfm_gb300.solver import Minor
+        out = Minor.empty(self.case.mp, self.case.np, self.case.lp)
+        c = out.to_c()
+        rc = self.lib.gfo_minor_get(self.o, C.byref(c))
+        if rc != 0:
+            raise RuntimeError(f"gfo_minor_get: {rc}")
+        out.update_scalars(c)
         return out
 
     def download(self) -> Fields:

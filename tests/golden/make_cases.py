@@ -23,11 +23,17 @@ reference's own run of the case printed:
                             iterations (T_ave_calc, Utility.f90:1485-1509) and
                             the mean gas temperature of the last iteration
 
+  - rad_detail####c.plt      the last volume-radiation record of the run
+                            (Qrn.f90:181-197): its RAD0 band-emission totals
+                            and the QRNF emission and absorption totals
+
 The first 48 lines of each per-iteration log (convg, gresid, gresid_xtra,
 Tave, Info and, where the run wrote them, the pre-solve gresidp and
 gresid_xtrap) and the first 80 lines of summary####c.txt are copied unchanged
-into logs/, as the byte-level reference of their format.  For case0041 the converged restart file rg0041c.d is stored
-xz-compressed.
+into logs/, as the byte-level reference of their format.  For case0041 the
+converged restart file rg0041c.d and the minor species restart rs0041c.d
+(written after the run's last MSFLOW, read by the RAD_EMIS of that last
+rad_detail record) are stored xz-compressed.
 
 Run from the repository root with the reference package root as argument:
 
@@ -44,7 +50,7 @@ import sys
 HERE = pathlib.Path(__file__).resolve().parent
 # runum: (case directory in the package, keep the restart file); for 0020,
 # 0021, 0054 and 0055 the directory holding the run's fresh start
-CASES = {"0041": ("case0041", True), "0040": ("case0040", False), "1207": ("case1207", False),
+CASES = {"0041": ("case0041", True), "0040": ("case0040", False), "1207": ("case1207", True),
          "0020": ("case0020oldrun", False), "0021": ("case0021oldrun", False), "0054": ("case0054-start", False),
          "0055": ("case0055-start", False), "0056": ("case0056", False), "1206": ("case1206", False)}
 
@@ -97,11 +103,16 @@ def main(pkg_root: str) -> None:
         ref["tmean_ex"] = [float(r[2]) for r in tave[:3]]
         ref["tave_iteration_last"] = int(tave[-1][0])
         ref["tave_last"] = float(tave[-1][1])
+        rad = data_rows(case / f"rad_detail{num}c.plt")
+        keys = ("qe_h2o_co2", "qe_soot", "qe_sum", "qe_from_media", "qa_melt", "qa_wall", "qa_media", "qa_exit",
+                "qa_inlet", "qa_sum", "q_diff")
+        ref["rad_detail_last"] = {"itr_gas": int(rad[-1][0]), **{k: float(v) for k, v in zip(keys, rad[-1][1:])}}
         if keep_rg:
-            raw = (case / f"rg{num}c.d").read_bytes()
-            (out / f"rg{num}c.d.xz").write_bytes(lzma.compress(raw, preset=9))
-            ref["rg_sha256"] = hashlib.sha256(raw).hexdigest()
-            ref["rg_bytes"] = len(raw)
+            for kind in ("rg", "rs"):
+                raw = (case / f"{kind}{num}c.d").read_bytes()
+                (out / f"{kind}{num}c.d.xz").write_bytes(lzma.compress(raw, preset=9))
+                ref[f"{kind}_sha256"] = hashlib.sha256(raw).hexdigest()
+                ref[f"{kind}_bytes"] = len(raw)
         (out / f"case{num}_reference.json").write_text(json.dumps(ref, indent=1) + "\n")
         print(f"wrote {out}")
 
