@@ -283,6 +283,8 @@ SIGNATURES = [
     ("gfm_minor_write", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmMinor)]),
     ("gfm_gpu_minor_upload", C.c_int, [C.c_void_p, C.POINTER(GfmMinor)]),
     ("gfm_gpu_minor_download", C.c_int, [C.c_void_p, C.POINTER(GfmMinor)]),
+    ("gfm_gpu_initsvm", C.c_int, [C.c_void_p, C.c_int]),
+    ("gfm_gpu_msflow", C.c_int, [C.c_void_p, C.c_int, C.POINTER(GfmMsflowStats)]),
     ("gfm_gpu_kernel_times", C.c_int, [C.c_void_p, _dp, _dp, _dp, C.POINTER(C.c_longlong)]),
     ("gfm_gpu_reset_kernel_times", C.c_int, [C.c_void_p]),
     ("gfm_gpu_iteration_profile", C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), _dp]),

@@ -18,7 +18,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libgfm_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["asm.cu", "adi.cu", "adi_plane.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lp_tc.cu", "lpsolve.cu", "rad.cu", "wall.cu", "gas.cu"]
+CUDA_SOURCES = ["asm.cu", "adi.cu", "adi_plane.cu", "bc.cu", "solver.cu", "noalloc.cu", "lp.cu", "lp_tc.cu", "lpsolve.cu", "rad.cu", "wall.cu", "gas.cu", "minor.cu"]
 # per-file flags: the radiation transfer rounds every product and sum as the
 # reference does (angle ties and energy splits must break the same way)
 FILE_FLAGS = {"rad.cu": ["--fmad=false"], "gas.cu": ["--fmad=false"]}

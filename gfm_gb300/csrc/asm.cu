@@ -971,6 +971,15 @@ template <typename R> void launch_scalar_sources_first(const Ctx<R>& c, cudaStre
     Range r = cell_range(c);
     k_fuel_source<R><<<grid_for(r.count()), kBlock, 0, s>>>(c, r);
 }
+// GSLV3G0's coefficients of the scalar range with sigma sgm into six given
+// arrays (the minor species' set, SGM = SSIGMA, Gslv3m.f90:143-146)
+template <typename R> void launch_scalar_faces_into(const Ctx<R>& c, R* const* as_out, double sgm, cudaStream_t s) {
+    Ctx<R> cc = c;
+    for (int q = 0; q < 6; ++q) cc.ASs[0][q] = as_out[q];
+    Range r = cell_range(c);
+    int nb = grid_for(r.count());
+    k_scalar_faces<R><<<dim3(nb, 3), kBlock, 0, s>>>(cc, r, 0, R(sgm));
+}
 template <typename R> void launch_scalar_assemble(const Ctx<R>& c, int L, bool new_as, cudaStream_t s) {
     Range r = cell_range(c);
     int nb = grid_for(r.count());
@@ -1014,6 +1023,7 @@ template <typename R> void launch_tave(const Ctx<R>& c, cudaStream_t s) {
     template void launch_qconv<R>(const Ctx<R>&, cudaStream_t);                             \
     template void launch_scalar_sources_first<R>(const Ctx<R>&, cudaStream_t);              \
     template void launch_scalar_assemble<R>(const Ctx<R>&, int, bool, cudaStream_t);        \
+    template void launch_scalar_faces_into<R>(const Ctx<R>&, R* const*, double, cudaStream_t); \
     template void launch_scalar_finish<R>(const Ctx<R>&, int, cudaStream_t);                \
     template void launch_tave<R>(const Ctx<R>&, cudaStream_t);                              \
     template void launch_props<R>(const Ctx<R>&, cudaStream_t);

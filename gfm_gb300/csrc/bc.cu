@@ -310,6 +310,119 @@ __global__ void k_intp(Ctx<R> c, int stage) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Minor species (ms=1): INITSVM (Initsv.f90:329-378), EXTRM (Extr.f90:258-300)
+// and INTPM (Intp.f90:348-420) on the seven GFM arrays, with the record
+// tables and the carried-F1 codes of EXTR and INTP: the loops and the
+// neighbour choices are the same.
+// ---------------------------------------------------------------------------
+template <typename R>
+__global__ void k_initsvm(Ctx<R> c, MinorDev<R> m, int restart) {
+    const GeoT<R>& g = c.g;
+    const long long n = (long long)g.MP * g.NP * g.LP;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int I = (int)(t % g.MP) + 1, J = (int)((t / g.MP) % g.NP) + 1, K = (int)(t / ((long long)g.MP * g.NP)) + 1;
+        const long long o = pidx(g, I, J, K);
+        const bool centre = !(I & 1) && !(J & 1) && !(K & 1);
+        if (!restart) {   // smf = 0, GFM = 0, then the centres from the major species
+            m.smf[o] = R(0);
+            for (int l = 0; l < 7; ++l) m.gfm[l][o] = R(0);
+            if (!centre) continue;
+        } else if (!centre || g.ib[o] != 2) {
+            continue;   // the restart state stays, but at the inlet cells
+        }
+        m.gfm[0][o] = c.GF[0][o];   // CH4  <- fuel
+        m.gfm[1][o] = c.GF[1][o];   // O2
+        m.gfm[3][o] = c.GF[8][o];   // H2O
+        m.gfm[4][o] = c.GF[5][o];   // CO2
+        m.gfm[5][o] = c.GF[6][o];   // N2
+        if (restart) { m.gfm[2][o] = R(0); m.gfm[6][o] = R(0); }
+    }
+}
+// EXTRM's exit loop: the exit cell from EXT0/EXTR1's cells and weights
+// (the EXTR records of kind 3), copied onto the y-face toward J1
+template <typename R>
+__global__ void k_extrm_exit(Ctx<R> c, MinorDev<R> m) {
+    const GeoT<R>& g = c.g;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_io; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_io[t];
+        if (e.kind != 3) continue;
+        const long long o = pidx(g, e.I, e.J, e.K), o1 = pidx(g, e.I1, e.J1, e.K1), o2 = pidx(g, e.I2, e.J2, e.K2);
+        const long long oy = pidx(g, e.I, (e.J + e.J1) / 2, e.K);
+        const R F1 = R(e.F1), F2 = R(e.F2);
+        for (int l = 0; l < 7; ++l) {
+            const R g0 = m.gfm[l][o1] * F1 + m.gfm[l][o2] * F2;
+            m.gfm[l][o] = rmax2(g0, R(0));
+            m.gfm[l][oy] = m.gfm[l][o];
+        }
+        m.smf[o] = m.smf[o1];
+    }
+}
+// EXTRM's wall loop: the neighbour's value into the wall cell and onto the
+// face between them.  The fall-through cells read the cell above them before
+// this loop writes it (gather, then apply), as for EXTR.
+template <typename R>
+__device__ __forceinline__ void extrm_wall_put(const GeoT<R>& g, const MinorDev<R>& m, const ExtrRec& e, const R* v) {
+    const long long o = pidx(g, e.I, e.J, e.K);
+    long long of;
+    if (e.IX == 1) of = pidx(g, (e.I + e.I1) / 2, e.J, e.K);
+    else if (e.IX == 2) of = pidx(g, e.I, (e.J + e.J1) / 2, e.K);
+    else of = pidx(g, e.I, e.J, (e.K + e.K1) / 2);
+    for (int l = 0; l < 7; ++l) { m.gfm[l][o] = v[l]; m.gfm[l][of] = v[l]; }
+}
+template <typename R>
+__global__ void k_extrm_ft_gather(Ctx<R> c, MinorDev<R> m) {
+    const GeoT<R>& g = c.g;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_ft; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_ft[t];
+        const long long o1 = pidx(g, e.I1, e.J1, e.K1);
+        for (int l = 0; l < 7; ++l) c.ft_buf[(long long)t * kFtVals + l] = m.gfm[l][o1];
+    }
+}
+template <typename R>
+__global__ void k_extrm_ft_apply(Ctx<R> c, MinorDev<R> m) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_ft; t += gridDim.x * blockDim.x)
+        extrm_wall_put(c.g, m, c.extr_ft[t], c.ft_buf + (long long)t * kFtVals);
+}
+template <typename R>
+__global__ void k_extrm_wall(Ctx<R> c, MinorDev<R> m) {
+    const GeoT<R>& g = c.g;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < c.n_extr_wall; t += gridDim.x * blockDim.x) {
+        const ExtrRec& e = c.extr_wall[t];
+        const long long o1 = pidx(g, e.I1, e.J1, e.K1);
+        R v[7];
+        for (int l = 0; l < 7; ++l) v[l] = m.gfm[l][o1];
+        extrm_wall_put(g, m, e, v);
+    }
+}
+// INTPM: INTP's positions, stages and carried-F1 codes on the seven species
+template <typename R>
+__global__ void k_intpm(Ctx<R> c, MinorDev<R> m, int stage) {
+    const GeoT<R>& g = c.g;
+    int i0, i1, j0, j1, js, k0, k1, ks;
+    if (stage == 1) { i0 = 2; i1 = g.MP; j0 = 2; j1 = g.NP; js = 2; k0 = 3; k1 = g.LPM1; ks = 2; }
+    else if (stage == 2) { i0 = 2; i1 = g.MP; j0 = 3; j1 = g.NPM1; js = 2; k0 = 2; k1 = g.LP; ks = 1; }
+    else { i0 = 3; i1 = g.MPM1; j0 = 2; j1 = g.NP; js = 1; k0 = 2; k1 = g.LP; ks = 1; }
+    const int ni = (i1 - i0) / 2 + 1, nj = (j1 - j0) / js + 1, nk = (k1 - k0) / ks + 1;
+    const long long tot = (long long)ni * nj * nk;
+    GFM_FOR(t, tot) {
+        const int I = i0 + 2 * (t % ni);
+        const int r = t / ni;
+        const int J = j0 + js * (r % nj), K = k0 + ks * (r / nj);
+        const long long o = pidx(g, I, J, K);
+        const int mode = c.intp_mode[o];
+        if (mode == 0) continue;
+        int I1, J1, K1, I2, J2, K2, ix;
+        if (stage == 1) { I1 = I; J1 = J; K1 = K + 1; I2 = I; J2 = J; K2 = K - 1; ix = 3; }
+        else if (stage == 2) { I1 = I; J1 = J + 1; K1 = K; I2 = I; J2 = J - 1; K2 = K; ix = 2; }
+        else { I1 = I + 1; J1 = J; K1 = K; I2 = I - 1; J2 = J; K2 = K; ix = 1; }
+        const R f1 = mode == 1 ? intp1(g, I, J, K, ix) : (mode == 2 ? R(1) : R(0));
+        const R f2 = R(1) - f1;
+        const long long a = pidx(g, I1, J1, K1), b = pidx(g, I2, J2, K2);
+        for (int l = 0; l < 7; ++l) m.gfm[l][o] = f1 * m.gfm[l][a] + f2 * m.gfm[l][b];
+    }
+}
+
 // P at the reference inlet and the re-reference shift G0 (Gflow.f90:182-242)
 template <typename R>
 __global__ void k_pref(Ctx<R> c, int I1, int J1, int K1, int I2, int J2, int K2, double F1, double F2) {
@@ -494,6 +607,21 @@ template <typename R> void launch_intpv(const Ctx<R>& c, cudaStream_t s) {
         k_intpv<R><<<gridn(nc), kBlk, 0, s>>>(c, IU, 2, 4, M3, 2, 2, N3, 1, 2, L3, 1, IU);
     }
 }
+template <typename R> void launch_initsvm(const Ctx<R>& c, const MinorDev<R>& m, int restart, cudaStream_t s) {
+    k_initsvm<R><<<gridn((long long)c.g.MP * c.g.NP * c.g.LP), kBlk, 0, s>>>(c, m, restart);
+}
+template <typename R> void launch_extrm(const Ctx<R>& c, const MinorDev<R>& m, cudaStream_t s) {
+    if (c.n_extr_io > 0) k_extrm_exit<R><<<gridn(c.n_extr_io), kBlk, 0, s>>>(c, m);
+    if (c.n_extr_ft > 0) {
+        k_extrm_ft_gather<R><<<gridn(c.n_extr_ft), kBlk, 0, s>>>(c, m);
+        k_extrm_ft_apply<R><<<gridn(c.n_extr_ft), kBlk, 0, s>>>(c, m);
+    }
+    if (c.n_extr_wall > 0) k_extrm_wall<R><<<gridn(c.n_extr_wall), kBlk, 0, s>>>(c, m);
+}
+template <typename R> void launch_intpm(const Ctx<R>& c, const MinorDev<R>& m, cudaStream_t s) {
+    long long n = (long long)c.g.MP * c.g.NP * c.g.LP / 4;
+    for (int st = 1; st <= 3; ++st) k_intpm<R><<<gridn(n), kBlk, 0, s>>>(c, m, st);
+}
 template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s) {
     long long n = (long long)c.g.MP * c.g.NP * c.g.LP / 4;
     for (int st = 1; st <= 3; ++st) k_intp<R><<<gridn(n), kBlk, 0, s>>>(c, st);
@@ -535,6 +663,9 @@ template <typename R> void launch_cells_from_split(const GeoT<R>& g, const R* sr
     template void launch_extrv<R>(const Ctx<R>&, int, cudaStream_t);                                               \
     template void launch_intpv<R>(const Ctx<R>&, cudaStream_t);                                                    \
     template void launch_intp<R>(const Ctx<R>&, cudaStream_t);                                                     \
+    template void launch_initsvm<R>(const Ctx<R>&, const MinorDev<R>&, int, cudaStream_t);                         \
+    template void launch_extrm<R>(const Ctx<R>&, const MinorDev<R>&, cudaStream_t);                                \
+    template void launch_intpm<R>(const Ctx<R>&, const MinorDev<R>&, cudaStream_t);                                \
     template void launch_rad_emission<R>(const Ctx<R>&, cudaStream_t, const double*, const double*);                                             \
     template void launch_factor<R>(const Ctx<R>&, cudaStream_t);                                                   \
     template void launch_pref_idx<R>(const Ctx<R>&, int, int, int, int, int, int, double, double, cudaStream_t);  \

@@ -426,6 +426,12 @@ double soot_g0(double WL0) {
 
 int gas_scan_blocks(int ncell) { return (ncell + kScanBlock - 1) / kScanBlock; }
 
+void launch_prefix_max(int* a, int n, int* blockmax, cudaStream_t st) {
+    const int nb = gas_scan_blocks(n);
+    k_gas_scan_block<<<nb, kScanBlock, 0, st>>>(a, n, blockmax);
+    k_gas_scan_top<<<1, kScanBlock, 0, st>>>(blockmax, nb);
+}
+
 template <typename R>
 int launch_gas_band(const GasBuffers& b, const GeoT<double>& g, const R* T, const R* P, const R* DNST,
                     const R* const* gfm, const R* smf, double t0, double pg0, double dnst0, int nwl, const double* wl,
@@ -445,11 +451,9 @@ int launch_gas_band(const GasBuffers& b, const GeoT<double>& g, const R* T, cons
     }
     a.aklg = b.aklg; a.akls = b.akls; a.fvs = b.fvs; a.setter = b.setter; a.blockmax = b.blockmax; a.err = b.err;
     const int n = a.MZ * a.NZ * a.LZ;
-    const int nb = gas_scan_blocks(n);
     const int gb = (n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096;
     k_gas_band<R><<<gb, 128, 0, st>>>(a);
-    k_gas_scan_block<<<nb, kScanBlock, 0, st>>>(b.setter, n, b.blockmax);
-    k_gas_scan_top<<<1, kScanBlock, 0, st>>>(b.blockmax, nb);
+    launch_prefix_max(b.setter, n, b.blockmax, st);
     k_gas_soot<R><<<(n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096, 256, 0, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? GFM_OK : GFM_E_CUDA;
 }

@@ -139,9 +139,17 @@ struct gfm_handle {
     // minor species and soot (gfm_gpu_minor_upload), the band model's buffers
     MinorDev<double> mnd{};
     MinorDev<float> mnf{};
-    bool minor_on = false;
+    bool minor_on = false, minor_from_host = false;
     int itr_ms = 0, imscon = 0;
     GasBuffers gas{};
+    // MSFLOW's scratch; the coefficient array of the reference holds the
+    // minor species' set (true) or the last gas equation's (false)
+    MsScratch<double> msd{};
+    MsScratch<float> msf{};
+    bool as_minor_current = false;
+    int igs0 = 0;
+    double resid_ms_pre[8]{}, resid_ms[8]{};
+    double vol_tot = 0;                 // open volume (IBCELL = 0), Grid3.f90:286-294
 };
 
 namespace {
@@ -1085,6 +1093,8 @@ int capture_iteration(gfm_handle* h) {
 namespace {
 int gas_band(gfm_handle* h);
 int gas_check(gfm_handle* h);
+int minor_initsvm(gfm_handle* h, int restart);
+int msflow_run(gfm_handle* h, int maxms, gfm_msflow_stats* out);
 // the emission-only source (rad_qe_only, Rad_emis.f90:411-466) on the
 // handle's stream, on the band model's coefficients when the case asks for it
 int rad_emission_launch(gfm_handle* h) {
@@ -1106,6 +1116,7 @@ int rad_emission_launch(gfm_handle* h) {
 // applies the convergence test and the emission cadence (Sphase.f90:37-235).
 int iter_launch(gfm_handle* h) {
     h->itr_gas += 1;
+    h->as_minor_current = false;   // GSLV3G leaves the last gas equation's coefficients
     h->h_flags[0] = (double)h->itr_gas;
     h->h_flags[1] = (double)h->rad_active;
     if (h->use_graph) {
@@ -1136,7 +1147,13 @@ int iter_finish(gfm_handle* h, int* conv) {
     if (h->params.rad_emission) {
         h->cnt_qe += 1;
         if (h->cnt_qe >= h->params.rad_qe_frequency && h->itr_gas > 50) {
-            int rc = rad_emission_launch(h);
+            int rc;
+            if (h->params.gas_model && !h->rad_active) {
+                // the first emission update runs INITSVM and MSFLOW(300) before it (Sphase.f90:210-224)
+                if ((rc = minor_initsvm(h, h->params.irstypm != 0 && h->minor_from_host)) || (rc = msflow_run(h, 300, nullptr)))
+                    return rc;
+            }
+            rc = rad_emission_launch(h);
             if (rc) return rc;
             h->rad_active = 1;
             h->cnt_qe = 0;
@@ -1759,11 +1776,167 @@ int gas_check(gfm_handle* h) {
 }
 }  // namespace
 
+namespace {
+template <typename R>
+int ms_alloc(gfm_handle* h, MsScratch<R>& s) {
+    if (s.ap1) return GFM_OK;
+    const int ni = (h->hg.MP - 2 - 4) / 2 + 1, nj = (h->hg.NP - 2 - 4) / 2 + 1, nk = (h->hg.LP - 2 - 4) / 2 + 1;
+    s.nq = ni > 0 && nj > 0 && nk > 0 ? ni * nj * nk : 0;
+    int rc;
+    for (int q = 0; q < 6; ++q)
+        if ((rc = dalloc(h, &s.as[q], h->NS))) return rc;
+    for (int l = 0; l < 7; ++l)
+        if ((rc = dalloc(h, &s.fz[l], h->NS)) || (rc = dalloc(h, &s.bs[l], h->NS))) return rc;
+    if ((rc = dalloc(h, &s.ap1, h->NS)) || (rc = dalloc(h, &s.ap, h->NS)) ||
+        (rc = dalloc(h, &s.r4, std::max(s.nq, 1))) || (rc = dalloc(h, &s.setter, std::max(s.nq, 1))) ||
+        (rc = dalloc(h, &s.blockmax, std::max(gas_scan_blocks(s.nq), 1))) || (rc = dalloc(h, &s.carry, 1)) ||
+        (rc = dalloc(h, &s.stats, 8)))
+        return rc;
+    const gfm_params& P = h->params;
+    s.rfm = P.rfm; s.rfm_soot = P.rfm_soot; s.rf_sf = P.rf_soot_form; s.rf_so = P.rf_soot_oxid;
+    s.soot_cap = P.soot_cap; s.t0_sf = P.t0_sf; s.t0_so = P.t0_so; s.aform = P.aform; s.aoxid = P.aoxid;
+    s.esf_r = P.esf_r; s.eso_r = P.eso_r;
+    s.snorm = P.r0 / (P.dnst0 * P.ug0);   // Sourcem.f90:81
+    s.react = P.react;
+    // the open volume (Grid3.f90:286-294), in the reference's loop order
+    double v = 0.0;
+    const HostGrid& hg = h->hg;
+    for (int i = 2; i <= hg.MP; i += 2)
+        for (int j = 2; j <= hg.NP; j += 2)
+            for (int k = 2; k <= hg.LP; k += 2)
+                if (hg.at(i, j, k) == 0) v = v + hg.DX[i] * hg.DR[j] * hg.RS[j] * hg.DZ[k] * 1.0;
+    h->vol_tot = v;
+    return GFM_OK;
+}
+
+// INITSVM (Initsv.f90:329-378) on the device
+template <typename R>
+int initsvm_dev(gfm_handle* h, Ctx<R>& c, MinorDev<R>& m, int restart) {
+    int rc;
+    if ((rc = minor_alloc(h, m))) return rc;
+    launch_initsvm(c, m, restart, h->stream);
+    if (restart) launch_extrm(c, m, h->stream);
+    launch_intpm(c, m, h->stream);
+    h->igs0 = 0;
+    CK(cudaStreamSynchronize(h->stream));
+    return GFM_OK;
+}
+int minor_initsvm(gfm_handle* h, int restart) {
+    if (restart && !h->minor_on) { h->err = "INITSVM restart: no minor species state"; return GFM_E_ARG; }
+    int rc = h->prec == GFM_PREC_FP64 ? initsvm_dev(h, h->cd, h->mnd, restart) : initsvm_dev(h, h->cf, h->mnf, restart);
+    if (rc) return rc;
+    if (!h->minor_on) for (int l = 0; l < 8; ++l) { h->resid_ms[l] = 1.0e-16; h->resid_ms_pre[l] = 1.0e-16; }
+    h->minor_on = true;
+    return GFM_OK;
+}
+
+// MSFLOW (Msflow.f90:29-165): GSLV3M, the report sums, the convergence test
+// after iteration 10, EXTRM and INTPM, up to maxms iterations
+template <typename R>
+int msflow_dev(gfm_handle* h, Ctx<R>& c, MinorDev<R>& m, MsScratch<R>& s, AdiScratch<R>* scr, int maxms,
+               gfm_msflow_stats* out) {
+    int rc;
+    if ((rc = ms_alloc(h, s))) return rc;
+    cudaStream_t st = h->stream;
+    const GeoT<R>& g = c.g;
+    const gfm_params& P = h->params;
+    h->igs0 = 0;
+    int done = 0;
+    for (int it = 0; it < maxms; ++it) {
+        h->itr_ms += 1;
+        ++done;
+        CK(cudaMemsetAsync(c.partials, 0, sizeof(double) * kRedSlots * kRedBlocks, st));
+        // reaction rates, with the coefficients the reference's AS array holds now
+        R* const* as_spin = h->as_minor_current ? s.as : c.ASs[c.as_set[6]];
+        launch_ms_rates(c, m, s, as_spin, st);
+        if (h->igs0 == 0) {   // GSLV3G0(...,0) of the first species after INITSVM / MSFLOW's start
+            launch_scalar_faces_into(c, s.as, P.ssigma, st);
+            h->as_minor_current = true;
+            h->igs0 = 1;
+        }
+        launch_ms_ap(c, s, st);
+        for (int l = 0; l < 7; ++l) CK(cudaMemcpyAsync(s.fz[l], m.gfm[l], sizeof(R) * h->NS, cudaMemcpyDeviceToDevice, st));
+        launch_ms_species(c, m, s, st);
+        Sys<R> ss[7];
+        for (int l = 0; l < 7; ++l) {
+            ss[l] = sys_of<R>(s.fz[l], s.ap, s.as, s.bs[l], 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesm);
+            launch_residual(c, ss[l], kSlMsPre + l, st);
+        }
+        launch_adlbl3_scr(g, ss, scr, 7, h->adi_mode, st, h->rb_flags);   // returns the kernels it launched
+        for (int l = 0; l < 7; ++l) launch_residual(c, ss[l], kSlMsPost + l, st);
+        launch_ms_update(c, m, s, st);
+        if (P.react) {   // soot (Gslv3m.f90:225-284)
+            CK(cudaMemcpyAsync(s.fz[0], m.smf, sizeof(R) * h->NS, cudaMemcpyDeviceToDevice, st));
+            launch_soot_system(c, m, s, h->itr_ms, st);
+            Sys<R> so = sys_of<R>(s.fz[0], s.ap, s.as, s.bs[0], 4, g.MPM2, g.NJY1, g.NJY2, g.LKZ1, g.LKZ2, P.ntimesm);
+            launch_residual(c, so, kSlMsPre + 7, st);
+            launch_adlbl3_scr(g, &so, scr, 1, h->adi_mode, st, h->rb_flags);
+            launch_residual(c, so, kSlMsPost + 7, st);
+            launch_soot_update(c, m, s, st);
+        }
+        launch_ms_stats(c, m, s, st);
+        FinishSpec f{};
+        auto add = [&](int slot, int dst, int op) { f.slot[f.n] = slot; f.dst[f.n] = dst; f.op[f.n] = op; ++f.n; };
+        const int nsys = P.react ? 8 : 7;
+        for (int l = 0; l < nsys; ++l) { add(kSlMsPre + l, S_MS_RPRE + l, 2); add(kSlMsPost + l, S_MS_RES + l, 2); }
+        add(kSlMsBal, S_MS_BAL, 0);
+        if (P.react) { add(kSlMsSoot, S_MS_SOOT, 0); add(kSlMsSmfMax, S_MS_SMFMAX, 1); add(kSlMsSmfMaxNc, S_MS_SMFMAXNC, 1); }
+        launch_finish(c.partials, c.scal, f, (double)h->ncells, st);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h->h_scal, c.scal, sizeof(double) * (S_NUM + 128), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (int l = 0; l < nsys; ++l) { h->resid_ms_pre[l] = h->h_scal[S_MS_RPRE + l]; h->resid_ms[l] = h->h_scal[S_MS_RES + l]; }
+        h->imscon = 0;
+        if (h->itr_ms > 10) {
+            h->imscon = 1;
+            for (int l = 0; l < 8; ++l) if (h->resid_ms[l] > P.bmcon) h->imscon = 0;
+        }
+        if (h->imscon == 1) break;
+        launch_extrm(c, m, st);
+        launch_intpm(c, m, st);
+    }
+    double stats[8] = {0};
+    CK(cudaMemcpyAsync(stats, s.stats, sizeof stats, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (out) {
+        std::memset(out, 0, sizeof *out);
+        out->itr_ms = h->itr_ms;
+        out->iterations = done;
+        out->converged = h->imscon;
+        for (int l = 0; l < 8; ++l) { out->resid_ms_pre[l] = h->resid_ms_pre[l]; out->resid_ms[l] = h->resid_ms[l]; }
+        out->bal_ms = h->h_scal[S_MS_BAL] * 1.0 / h->vol_tot;
+        out->soot_tot = h->h_scal[S_MS_SOOT];
+        out->smf_max = h->h_scal[S_MS_SMFMAX];
+        out->smf_max_noclip = h->h_scal[S_MS_SMFMAXNC];
+        for (int l = 0; l < 7; ++l) out->gfm_out[l] = stats[l];
+        out->svf_r = stats[7];
+    }
+    return GFM_OK;
+}
+int msflow_run(gfm_handle* h, int maxms, gfm_msflow_stats* out) {
+    if (!h->minor_on) { h->err = "MSFLOW: no minor species state (gfm_gpu_initsvm or gfm_gpu_minor_upload)"; return GFM_E_ARG; }
+    return h->prec == GFM_PREC_FP64 ? msflow_dev(h, h->cd, h->mnd, h->msd, h->scr_d, maxms, out)
+                                    : msflow_dev(h, h->cf, h->mnf, h->msf, h->scr_f, maxms, out);
+}
+}  // namespace
+
+extern "C" int gfm_gpu_initsvm(gfm_handle* h, int restart) {
+    if (!h) return GFM_E_ARG;
+    return minor_initsvm(h, restart);
+}
+
+extern "C" int gfm_gpu_msflow(gfm_handle* h, int maxms, gfm_msflow_stats* out) {
+    if (!h || maxms < 0) return GFM_E_ARG;
+    return msflow_run(h, maxms, out);
+}
+
 extern "C" int gfm_gpu_minor_upload(gfm_handle* h, const gfm_minor* m) {
     if (!h || !m || !m->gfm || !m->smf || !m->bs_soot_prev || !m->sfp_soot_prev || !m->rrms) return GFM_E_ARG;
     int rc = h->prec == GFM_PREC_FP64 ? minor_put(h, h->gd, h->mnd, m) : minor_put(h, h->gfl, h->mnf, m);
     if (rc) return rc;
+    if (!h->minor_on) for (int l = 0; l < 8; ++l) { h->resid_ms[l] = 1.0e-16; h->resid_ms_pre[l] = 1.0e-16; }
     h->minor_on = true;
+    h->minor_from_host = true;
     h->itr_ms = m->itr_ms;
     h->imscon = m->imscon;
     return GFM_OK;

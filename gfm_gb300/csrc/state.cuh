@@ -38,6 +38,9 @@ enum Scal {
     S_TAREA_MEAN = S_GF_RESID + 10, S_AREA_EX, S_ITR_GAS, S_TAVE_DEN, S_RAD_ACTIVE,
     S_LP_SCALE, S_LP_USED, S_LP_RATIO, S_LP_ALPHA, S_LP_TSCALE,
     S_RAD_DONE,   // i1st_rad_done: a wall exchange has run, EXTR keeps wall h and T (Extr.f90:194-197)
+    // MSFLOW: resid_ms_pre and resid_ms of the seven species and soot, bal_MS,
+    // soot mass, largest soot mass fraction clipped and not
+    S_MS_RPRE, S_MS_RES = S_MS_RPRE + 8, S_MS_BAL = S_MS_RES + 8, S_MS_SOOT, S_MS_SMFMAX, S_MS_SMFMAXNC,
     S_NUM
 };
 
@@ -194,6 +197,37 @@ struct GasBuffers {
     int* err;                    // bit 1: BANDA argument < 0, bit 2: W_R <= 0 with CO2
 };
 int gas_scan_blocks(int ncell);
+// in-place prefix maximum of a[0..n): a[i] becomes the maximum within its
+// block of 1024 up to i, blockmax[b] the maximum of the blocks before b
+// (gas_scan_blocks(n) entries); the full prefix at i is the larger of the two
+void launch_prefix_max(int* a, int n, int* blockmax, cudaStream_t st);
+
+// ---- minor species transport and soot (minor.cu) ---------------------------------
+template <typename R>
+struct MsScratch {
+    R* as[6];                    // coefficient set of the minor species (SGM = SSIGMA)
+    R *ap1, *ap;                 // the sum of the six; AP of the system being solved
+    R *fz[7], *bs[7];            // unknowns and right-hand sides (soot in slot 0)
+    double* r4;                  // each reaction cell's last RR2, by loop order
+    int *setter, *blockmax;      // the reaction cells' loop-order prefix
+    double* carry;               // RR2 entering the next GSLV3M call
+    double* stats;               // GFM_0(L,2) of the seven species, SVF_R
+    int nq;                      // cells of the reaction range
+    // relaxation and soot constants (relaxfactorc.txt, &INPUT)
+    double rfm, rfm_soot, rf_sf, rf_so, soot_cap, t0_sf, t0_so, aform, aoxid, esf_r, eso_r, snorm;
+    int react;
+};
+// slots of the MSFLOW sums in the partials rows (after the gas iteration's)
+constexpr int kSlMsPre = 40, kSlMsPost = 48, kSlMsBal = 56, kSlMsSoot = 57, kSlMsSmfMax = 58, kSlMsSmfMaxNc = 59;
+template <typename R>
+void launch_ms_rates(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, R* const* as_spin, cudaStream_t st);
+template <typename R> void launch_ms_ap(const Ctx<R>& c, const MsScratch<R>& s, cudaStream_t st);
+template <typename R> void launch_ms_species(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, cudaStream_t st);
+template <typename R> void launch_ms_update(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, cudaStream_t st);
+template <typename R>
+void launch_soot_system(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, int itr_ms, cudaStream_t st);
+template <typename R> void launch_soot_update(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, cudaStream_t st);
+template <typename R> void launch_ms_stats(const Ctx<R>& c, const MinorDev<R>& m, const MsScratch<R>& s, cudaStream_t st);
 // RAD_GAS and SOOTA of RAD0 (Rad0.f90:116-132) on the current T, P, DNST
 // and minor species: AKLG and AKLS of every open cell with T >= TG_MN
 template <typename R>
@@ -223,10 +257,14 @@ template <typename R> void launch_qconv(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_scalar_sources_first(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_scalar_assemble(const Ctx<R>& c, int L, bool new_as, cudaStream_t s);
 template <typename R> void launch_scalar_finish(const Ctx<R>& c, int L, cudaStream_t s);
+template <typename R> void launch_scalar_faces_into(const Ctx<R>& c, R* const* as_out, double sgm, cudaStream_t s);
 template <typename R> void launch_props(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_tave(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_extr(const Ctx<R>& c, cudaStream_t s);
 template <typename R> void launch_intp(const Ctx<R>& c, cudaStream_t s);
+template <typename R> void launch_initsvm(const Ctx<R>& c, const MinorDev<R>& m, int restart, cudaStream_t s);
+template <typename R> void launch_extrm(const Ctx<R>& c, const MinorDev<R>& m, cudaStream_t s);
+template <typename R> void launch_intpm(const Ctx<R>& c, const MinorDev<R>& m, cudaStream_t s);
 template <typename R> void launch_rad_emission(const Ctx<R>& c, cudaStream_t s, const double* gas_aklg = nullptr,
                                                const double* gas_akls = nullptr);
 template <typename R> void launch_residual(const Ctx<R>& c, const Sys<R>& sys, int slot, cudaStream_t s);

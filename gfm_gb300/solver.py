@@ -330,6 +330,17 @@ class GpuSolver:
         """The minor species state the band model (and MSFLOW) work on."""
         self._check(self.lib.gfm_gpu_minor_upload(self.h, C.byref(m.to_c())))
 
+    def initsvm(self, restart: bool = False) -> None:
+        """INITSVM: the minor species from the major ones, or (restart) the
+        uploaded state with its inlets reset and exits extrapolated."""
+        self._check(self.lib.gfm_gpu_initsvm(self.h, int(restart)))
+
+    def msflow(self, maxms: int) -> dict:
+        """MSFLOW on the frozen flow; the last iteration's figures."""
+        st = abi.GfmMsflowStats()
+        self._check(self.lib.gfm_gpu_msflow(self.h, maxms, C.byref(st)))
+        return st.as_dict()
+
     def minor_download(self) -> "Minor":
         out = Minor.empty(self.case.mp, self.case.np, self.case.lp)
         c = out.to_c()

@@ -452,13 +452,26 @@ int  gfm_gpu_wall_setup(gfm_handle *h, const gfm_wall_spec *spec);
 int  gfm_gpu_wall_totals(gfm_handle *h, gfm_wall_totals *out);
 int  gfm_gpu_wall_get(gfm_handle *h, const char *name, double *out, int cap);
 /* Minor species and soot on the device (ms=1 of the reference).
- * gfm_gpu_minor_upload / _download move the MSFLOW state.  With
- * params.gas_model = 1 the emission and the volume transfer take their
+ * gfm_gpu_minor_upload / _download move the MSFLOW state.  gfm_gpu_initsvm is
+ * INITSVM (Initsv.f90:329-378): restart = 0 starts from the major species
+ * (GFM 1, 2, 4, 5, 6 from GF, CO, NO and soot zero); restart = 1 keeps the
+ * uploaded state but resets the inlet cells to the major species and
+ * extrapolates the exits (EXTRM); both end with INTPM.  gfm_gpu_msflow runs
+ * MSFLOW (Msflow.f90:10-169) on the frozen flow: up to maxms iterations of
+ * GSLV3M (reaction rates, the seven species and soot, Gslv3m.f90:8-286),
+ * EXTRM and INTPM, stopping when every resid_ms <= BMCON after iteration 10;
+ * `out` (may be NULL) receives the last iteration's figures.
+ * With params.gas_model = 1 the emission and the volume transfer take their
  * absorption coefficients from RAD_GAS and SOOTA on this state
  * (Rad0.f90:116-132, Rad_gas.f90:16-395, Rad_soot.f90:26-69) instead of the
- * gray akl0; they return GFM_E_ARG until a state has been uploaded. */
+ * gray akl0, and gfm_gpu_gflow's first emission update runs INITSVM (a
+ * restart when IRSTYPM = 1 and a state was uploaded) and MSFLOW(300) before
+ * it, as SPHASE does (Sphase.f90:210-224).  Without a minor species state
+ * the band model returns GFM_E_ARG. */
 int  gfm_gpu_minor_upload(gfm_handle *h, const gfm_minor *m);
 int  gfm_gpu_minor_download(gfm_handle *h, gfm_minor *m);
+int  gfm_gpu_initsvm(gfm_handle *h, int restart);
+int  gfm_gpu_msflow(gfm_handle *h, int maxms, gfm_msflow_stats *out);
 /* Device times (CUDA events on the handle's stream) accumulated since the
  * last reset: adi_ms = line-solver batches, gflow_ms = whole GFLOW calls
  * (first to last iteration of each gfm_gpu_gflow), other_ms reserved;

@@ -510,7 +510,7 @@ struct Oracle {
     // minor species and soot (ms=1, Setup.f90:904-929): GFM(MP,NP,LP,7), smf,
     // the soot sources of the last MSFLOW iteration, RRMS(MZ,NZ,LZ,5)
     vec GFMS, SMF, BS_SOOT_PREV, SFP_SOOT_PREV, RRMS, AP1;
-    int itr_ms = 0, imscon = 0, IGS0 = 0, minor_on = 0;
+    int itr_ms = 0, imscon = 0, IGS0 = 0, minor_on = 0, minor_from_host = 0;
     double resid_ms[9] = {0}, resid_ms_pre[9] = {0};
     // state scalars
     int itr_gas, do_rad_qe_only_cnt, i1st_rad_qe_done, NELG;
@@ -2225,6 +2225,404 @@ struct Oracle {
                         }
                 }
     }
+    // ---- minor species and soot (Initsv.f90:329-378, Msflow.f90, Gslv3m.f90,
+    //      Sourcem.f90, Extr.f90:258-300, Intp.f90:348-420, Flx1d.f90:114-160) ----
+    void minor_alloc() {   // allocate_ms (Setup.f90:904-929): zeros
+        if (minor_on) return;
+        GFMS.assign(7 * N, 0.0); SMF.assign(N, 0.0); BS_SOOT_PREV.assign(N, 0.0); SFP_SOOT_PREV.assign(N, 0.0);
+        RRMS.assign(5L * MZ * NZ * LZ, 0.0);
+        for (int l = 0; l <= 8; ++l) { resid_ms[l] = 1.0e-16; resid_ms_pre[l] = 1.0e-16; }
+        minor_on = 1;
+    }
+    // INITSVM: a new start from the major species, or the restart state
+    // (already in place) with the inlets reset and the exits extrapolated
+    void INITSVM(int restart) {
+        minor_alloc();
+        if (!restart) {
+            std::fill(SMF.begin(), SMF.end(), 0.0);
+            std::fill(GFMS.begin(), GFMS.end(), 0.0);
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) {
+                        gfm(I, J, K, 1) = gf(I, J, K, IYF);
+                        gfm(I, J, K, 2) = gf(I, J, K, IYO2);
+                        gfm(I, J, K, 4) = gf(I, J, K, IYH2O);
+                        gfm(I, J, K, 5) = gf(I, J, K, IYCO2);
+                        gfm(I, J, K, 6) = gf(I, J, K, IYN2);
+                    }
+        } else {
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) {
+                        if (ibcell(I, J, K) != 2) continue;
+                        gfm(I, J, K, 1) = gf(I, J, K, IYF);
+                        gfm(I, J, K, 2) = gf(I, J, K, IYO2);
+                        gfm(I, J, K, 4) = gf(I, J, K, IYH2O);
+                        gfm(I, J, K, 5) = gf(I, J, K, IYCO2);
+                        gfm(I, J, K, 6) = gf(I, J, K, IYN2);
+                        gfm(I, J, K, 3) = ZERO;
+                        gfm(I, J, K, 7) = ZERO;
+                    }
+            EXTRM();
+        }
+        IGS0 = 0;
+        INTPM();
+    }
+    void EXTRM() {   // Extr.f90:258-300
+        for (int i = 2; i <= MP; i += 2)
+            for (int j = 2; j <= NP; j += 2)
+                for (int k = 2; k <= LP; k += 2) {
+                    if (ibcell(i, j, k) % 10 != 3) continue;
+                    int i1, j1, k1, i2, j2, k2, ixd;
+                    EXT01(false, i, j, k, i1, j1, k1, i2, j2, k2, ixd);
+                    double f1, f2;
+                    EXTR1(f1, f2, i, j, k, i1, j1, k1, i2, j2, k2, ixd);
+                    for (int L = 1; L <= 7; ++L) {
+                        double g0 = gfm(i1, j1, k1, L) * f1 + gfm(i2, j2, k2, L) * f2;
+                        gfm(i, j, k, L) = fmax2(g0, ZERO);
+                        const int jj = (j + j1) / 2;   // the y-face, whatever the exit's direction
+                        gfm(i, jj, k, L) = gfm(i, j, k, L);
+                    }
+                    a3(SMF, i, j, k) = a3(SMF, i1, j1, k1);
+                }
+        for (int i = 2; i <= MP; i += 2)
+            for (int j = 2; j <= NP; j += 2)
+                for (int k = 2; k <= LP; k += 2) {
+                    if (ibcell(i, j, k) % 10 != 1) continue;
+                    int i1, j1, k1, i2, j2, k2, ixd;
+                    EXT01(true, i, j, k, i1, j1, k1, i2, j2, k2, ixd);
+                    for (int L = 1; L <= 7; ++L) {
+                        gfm(i, j, k, L) = gfm(i1, j1, k1, L);
+                        if (ixd == 1) gfm((i + i1) / 2, j, k, L) = gfm(i, j, k, L);
+                        else if (ixd == 2) gfm(i, (j + j1) / 2, k, L) = gfm(i, j, k, L);
+                        else gfm(i, j, (k + k1) / 2, L) = gfm(i, j, k, L);
+                    }
+                }
+    }
+    // INTP0M (Intp.f90:404-420): F1 is the caller's variable, as in INTP0
+    void INTP0M(double& F1, int I, int J, int K, int I1, int J1, int K1, int I2, int J2, int K2) {
+        if (ibcell(I, J, K) == 3) return;
+        if (ibcell(I, J, K) == 2) {
+            if (ibcell(I1, J1, K1) == 2 && ibcell(I2, J2, K2) == 0) F1 = ONE;
+            else if (ibcell(I1, J1, K1) == 0 && ibcell(I2, J2, K2) == 2) F1 = ZERO;
+        }
+        const double F2 = ONE - F1;
+        for (int L = 1; L <= 7; ++L) gfm(I, J, K, L) = F1 * gfm(I1, J1, K1, L) + F2 * gfm(I2, J2, K2, L);
+    }
+    void INTPM() {   // Intp.f90:348-400
+        for (int I = 2; I <= MP; I += 2) {
+            for (int K = 3; K <= LPM1; K += 2) {
+                double F1 = INTP1(I, 0, K, 3);
+                for (int J = 2; J <= NP; J += 2) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0M(F1, I, J, K, I, J, K + 1, I, J, K - 1);
+                }
+            }
+            for (int J = 3; J <= NPM1; J += 2) {
+                double F1 = INTP1(I, J, 0, 2);
+                for (int K = 2; K <= LP; ++K) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0M(F1, I, J, K, I, J + 1, K, I, J - 1, K);
+                }
+            }
+        }
+        for (int I = 3; I <= MPM1; I += 2) {
+            double F1 = INTP1(I, 0, 0, 1);
+            for (int K = 2; K <= LP; ++K)
+                for (int J = 2; J <= NP; ++J) {
+                    if (ibcell(I, J, K) == 1) continue;
+                    INTP0M(F1, I, J, K, I + 1, J, K, I - 1, J, K);
+                }
+        }
+    }
+    // FLX1DM (Flx1d.f90:114-160): species flow through the x-face plane I
+    // (id 1: positive, 2: negative) or the y-face plane J
+    double flxm(int I, int L, int id) {
+        double s = ZERO;
+        for (int j = 4; j <= NPM2; j += 2)
+            for (int k = LKZ1; k <= LKZ2; k += 2) {
+                if (ibcell(I, j, k) == 1) continue;
+                const double g0 = a3(THETA, I, j, k) * a3(DNST, I, j, k) * ug(I, j, k, 1) * AREA_C(I, j, k, 1) * pr.gmfr;
+                if ((g0 >= ZERO ? 1 : 2) == id) s = s + std::fabs(g0) * gfm(I, j, k, L);
+            }
+        return s;
+    }
+    double flym(int J, int L, int id) {
+        double s = ZERO;
+        for (int i = 4; i <= MPM2; i += 2)
+            for (int k = LKZ1; k <= LKZ2; k += 2) {
+                if (ibcell(i, J, k) == 1) continue;
+                const double g0 = a3(THETA, i, J, k) * a3(DNST, i, J, k) * ug(i, J, k, 2) * AREA_C(i, J, k, 2) * pr.gmfr;
+                if ((g0 >= ZERO ? 1 : 2) == id) s = s + std::fabs(g0) * gfm(i, J, k, L);
+            }
+        return s;
+    }
+    // SPIN (Gslv3m.f90:292-305): inflow of species LSP into the cell (kmol/s)
+    double SPIN(int I, int J, int K, int LSP) {
+        const double G11 = as(I, J, K, 1, 1) * gfm(I - 2, J, K, LSP), G12 = as(I, J, K, 1, 2) * gfm(I + 2, J, K, LSP);
+        const double G21 = as(I, J, K, 2, 1) * gfm(I, J - 2, K, LSP), G22 = as(I, J, K, 2, 2) * gfm(I, J + 2, K, LSP);
+        const double G31 = as(I, J, K, 3, 1) * gfm(I, J, K - 2, LSP), G32 = as(I, J, K, 3, 2) * gfm(I, J, K + 2, LSP);
+        double FXMS = G11 + G12 + G21 + G22 + G31 + G32;
+        return FXMS * pr.gmfr / WMS[LSP - 1];
+    }
+    // RR2 of GSLV3M keeps its value from cell to cell: a cell whose first
+    // reaction is off subtracts the previous cell's last RR2 (its reaction 4
+    // and 5 rate) from its O2 inflow.  It is kept from call to call here
+    // (zero before the first), a local the reference leaves undefined there.
+    double rr2_carry = 0.0;
+    double soot_tot = 0, smf_max = 0, smf_max_noclip = 0, bal_ms = 0;
+    void GSLV3M() {
+        const int MI1 = 4, MI3 = MPM2, NJ1 = NJY1, NJ3 = NJY2, LK1 = LKZ1, LK3 = LKZ2;
+        const double SML1 = 1.0e-25;
+        // CK0_M, BETA, ODR, ERC (Var_mod.f90:231-235)
+        const double CK0M[5] = {1.66e15, 7.94e14, 2.24e14, 7.94e22, 9.33e14};
+        const double BETA5 = -0.5;
+        const double ODR1[5] = {1.46, 1.6904, 1.0, 0.721, 1.0}, ODR2[5] = {0.5217, 1.57, 0.0, 4.0111, 0.5};
+        const double ERC[5] = {20643.0, 11613.0, 62281.0, 44369.0, 68899.0};
+        double RR2 = rr2_carry;
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) > 0) continue;
+                    const int ID2 = I / 2, JD2 = J / 2, KD2 = K / 2;
+                    const double TMP = a3(T, I, J, K) * pr.t0;
+                    const double DNST1 = a3(DNST, I, J, K) * pr.dnst0;
+                    const double VOL = DX[I] * DR[J] * DZ[K] * 1.0;   // *VOL0
+                    double G[8];
+                    for (int L = 1; L <= 7; ++L) G[L] = gfm(I, J, K, L) / WMS[L - 1] * DNST1;
+                    // reaction 1
+                    const double FXMS1 = SPIN(I, J, K, 1);
+                    double FXMS2 = SPIN(I, J, K, 2);
+                    if (G[1] <= SML1 || G[2] <= SML1) {
+                        rrms(ID2, JD2, KD2, 1) = 0;
+                    } else {
+                        const double RR1 = std::pow(G[1], ODR1[0]) * std::pow(G[2], ODR2[0]);
+                        RR2 = CK0M[0] * RR1 * std::exp(-ERC[0] / TMP) * VOL;
+                        if (RR2 > FXMS1) RR2 = FXMS1;
+                        if (FXMS2 / 1.5 < RR2) RR2 = FXMS2 / 1.5;
+                        rrms(ID2, JD2, KD2, 1) = RR2 * 0.3 + rrms(ID2, JD2, KD2, 1) * 0.7;
+                    }
+                    // reaction 2
+                    FXMS2 = FXMS2 - RR2 * 1.5;
+                    if (FXMS2 > small20 && G[3] > small20) {
+                        const double RR1 = std::pow(G[3], ODR1[1]) * std::pow(G[2], ODR2[1]);
+                        RR2 = CK0M[1] * RR1 * std::exp(-ERC[1] / TMP) * VOL;
+                        if (FXMS2 * 2 < RR2) RR2 = FXMS2 * 2;
+                        const double FXMS3 = SPIN(I, J, K, 3);
+                        RR2 = fmin2(RR2, FXMS3);
+                    } else {
+                        RR2 = 0;
+                    }
+                    // reaction 3
+                    double RR3;
+                    if (G[5] > small20) {
+                        const double RR1 = std::pow(G[5], ODR1[2]);
+                        RR3 = CK0M[2] * RR1 * std::exp(-ERC[2] / TMP) * VOL;
+                        const double FXMS5 = SPIN(I, J, K, 5);
+                        RR3 = fmin2(RR3, FXMS5);
+                    } else {
+                        RR3 = 0;
+                    }
+                    double RR1 = RR2 - RR3;
+                    if (RR1 < 0) RR1 = 0;
+                    rrms(ID2, JD2, KD2, 2) = RR1 * 0.3 + rrms(ID2, JD2, KD2, 2) * 0.7;
+                    // reactions 4 and 5
+                    if (G[2] > small20 && G[3] > small20 && G[6] > small20) {
+                        const double R1 = std::pow(G[3], ODR1[3]) * std::pow(G[2], ODR2[3]) * gfm(I, J, K, 6) / 0.725;
+                        RR2 = CK0M[3] * R1 * std::exp(-ERC[3] / TMP) * VOL;
+                    } else {
+                        RR2 = 0;
+                    }
+                    if (G[2] > small20 && G[6] > small20) {
+                        const double R1 = std::pow(G[6], ODR1[4]) * std::pow(G[2], ODR2[4]);
+                        RR3 = CK0M[4] * R1 * std::exp(-ERC[4] / TMP) * std::pow(TMP, BETA5);
+                        RR3 = RR3 * VOL;
+                    } else {
+                        RR3 = 0;
+                    }
+                    RR2 = RR2 + RR3;
+                    rrms(ID2, JD2, KD2, 4) = RR2;
+                }
+        rr2_carry = RR2;
+        // the seven species (Gslv3m.f90:131-192)
+        for (int L = 1; L <= 7; ++L) {
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) a3(FZ, I, J, K) = gfm(I, J, K, L);
+            SOURCEM(L, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            SGM = pr.ssigma;
+            if (IGS0 == 0) {
+                GSLV3G0(MI1, MI3, NJ1, NJ3, LK1, LK3, 0);
+                AP1 = AP;
+                IGS0 = 1;
+            } else {
+                AP = AP1;
+            }
+            const double RFM = pr.rfm, RFMC = ONE - pr.rfm;
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        const double VOL = VOL_C(I, J, K);
+                        a3(AP, I, J, K) = a3(AP, I, J, K) - (a3(SFP, I, J, K) * VOL);
+                        a3(AP, I, J, K) = a3(AP, I, J, K) / RFM;
+                        a3(BS, I, J, K) = a3(BS, I, J, K) + RFMC * a3(FZ, I, J, K) * a3(AP, I, J, K);
+                    }
+            resid_ms_pre[L] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            ADLBL3(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesm);
+            resid_ms[L] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        if (ibcell(I, J, K) >= 1) continue;
+                        double& z = a3(FZ, I, J, K);
+                        if (z > ONE) z = ONE;
+                        if (z < 0) z = 0;
+                        if (L == 3 && z > 0.1) z = 0.1;
+                        if (L == 7 && z > 1.0e-2) z = 1.0e-2;
+                        gfm(I, J, K, L) = RFMC * gfm(I, J, K, L) + RFM * z;
+                        if (gfm(I, J, K, L) < small20) gfm(I, J, K, L) = 0;
+                    }
+        }
+        // mass balance of the species (Gslv3m.f90:196-218)
+        double vol_tot = ZERO;
+        for (int i = 2; i <= MP; i += 2)
+            for (int j = 2; j <= NP; j += 2)
+                for (int k = 2; k <= LP; k += 2)
+                    if (ibcell(i, j, k) == 0) vol_tot = vol_tot + VOL_C(i, j, k) * 1.0;
+        bal_ms = 0;
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    double G0 = ZERO;
+                    for (int L = 1; L <= 7; ++L) G0 = G0 + gfm(I, J, K, L);
+                    bal_ms = bal_ms + std::fabs(ONE - G0) * VOL_C(I, J, K);
+                }
+        bal_ms = bal_ms * 1.0 / vol_tot;
+        // soot (Gslv3m.f90:225-284)
+        if (!pr.react) return;
+        const int L = 8;
+        for (int I = 2; I <= MP; I += 2)
+            for (int J = 2; J <= NP; J += 2)
+                for (int K = 2; K <= LP; K += 2) a3(FZ, I, J, K) = a3(SMF, I, J, K);
+        SOURCEM(11, MI1, MI3, NJ1, NJ3, LK1, LK3);
+        SGM = pr.ssigma;
+        GSLV3G0(MI1, MI3, NJ1, NJ3, LK1, LK3, 1);
+        const double RFM = pr.rfm_soot, RFMC = ONE - pr.rfm_soot;
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    const double VOL = VOL_C(I, J, K);
+                    a3(BS, I, J, K) = a3(BS, I, J, K) * VOL;
+                    a3(AP, I, J, K) = a3(AP, I, J, K) - (a3(SFP, I, J, K) * VOL);
+                    a3(AP, I, J, K) = a3(AP, I, J, K) / RFM;
+                    a3(BS, I, J, K) = a3(BS, I, J, K) + RFMC * a3(FZ, I, J, K) * a3(AP, I, J, K);
+                }
+        resid_ms_pre[L] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+        ADLBL3(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3, pr.ntimesm);
+        resid_ms[L] = calc_residual(FZ, MI1, MI3, NJ1, NJ3, LK1, LK3);
+        soot_tot = 0; smf_max = ZERO; smf_max_noclip = ZERO;
+        for (int I = MI1; I <= MI3; I += 2)
+            for (int J = NJ1; J <= NJ3; J += 2)
+                for (int K = LK1; K <= LK3; K += 2) {
+                    if (ibcell(I, J, K) >= 1) continue;
+                    const double z = a3(FZ, I, J, K);
+                    smf_max_noclip = std::max(smf_max_noclip, z);
+                    double G0;
+                    if (z > pr.soot_cap) G0 = pr.soot_cap;
+                    else if (z > small20) G0 = z;
+                    else G0 = ZERO;
+                    smf_max = std::max(smf_max, G0);
+                    a3(SMF, I, J, K) = RFM * G0 + RFMC * a3(SMF, I, J, K);
+                    const double vol = DX[I] * DR[J] * DZ[K];
+                    soot_tot = soot_tot + a3(SMF, I, J, K) * a3(DNST, I, J, K) * pr.dnst0 * vol;
+                }
+    }
+    // SOURCEM (Sourcem.f90:8-122): NELM 1..7 the species, 11 soot (the
+    // current soot model, ioldsoot = 0)
+    void SOURCEM(int NELM, int MI1, int MI3, int NJ1, int NJ3, int LK1, int LK3) {
+        if (NELM != 11) {
+            for (int I = MI1; I <= MI3; I += 2)
+                for (int J = NJ1; J <= NJ3; J += 2)
+                    for (int K = LK1; K <= LK3; K += 2) {
+                        a3(SFP, I, J, K) = ZERO;
+                        a3(BS, I, J, K) = ZERO;
+                        if (ibcell(I, J, K) > 0) continue;
+                        const int ID2 = I / 2, JD2 = J / 2, KD2 = K / 2;
+                        double G0;
+                        if (NELM == 1) G0 = -rrms(ID2, JD2, KD2, 1);
+                        else if (NELM == 2)
+                            G0 = -rrms(ID2, JD2, KD2, 1) * 1.5 - rrms(ID2, JD2, KD2, 2) * 0.5 - rrms(ID2, JD2, KD2, 4);
+                        else if (NELM == 3) G0 = rrms(ID2, JD2, KD2, 1) - rrms(ID2, JD2, KD2, 2);
+                        else if (NELM == 4) G0 = rrms(ID2, JD2, KD2, 1) * TWO;
+                        else if (NELM == 5) G0 = rrms(ID2, JD2, KD2, 2);
+                        else if (NELM == 6) G0 = -rrms(ID2, JD2, KD2, 4);
+                        else G0 = rrms(ID2, JD2, KD2, 4) * TWO;
+                        a3(BS, I, J, K) = G0 * WMS[NELM - 1] / pr.gmfr;
+                    }
+            return;
+        }
+        const double snorm = pr.r0 / (pr.dnst0 * pr.ug0);
+        const double E0_sf = pr.t0_sf < small20 ? ZERO : std::exp(-pr.esf_r / pr.t0_sf);
+        const double E0_so = pr.t0_so < small20 ? ZERO : std::sqrt(pr.t0_so) * std::exp(-pr.eso_r / pr.t0_so);
+        std::fill(BS.begin(), BS.end(), ZERO);
+        std::fill(SFP.begin(), SFP.end(), ZERO);
+        for (int i = MI1; i <= MI3; i += 2)
+            for (int j = NJ1; j <= NJ3; j += 2)
+                for (int k = LK1; k <= LK3; k += 2) {
+                    const double Tcell = a3(T, i, j, k) * pr.t0;
+                    if (ibcell(i, j, k) > 0 || !pr.react) continue;
+                    if (Tcell > pr.t0_sf) {
+                        a3(BS, i, j, k) = pr.aform * gfm(i, j, k, 1) * (std::exp(-pr.esf_r / Tcell) - E0_sf) * snorm;
+                        if (itr_ms > 1)
+                            a3(BS, i, j, k) = pr.rf_soot_form * a3(BS, i, j, k) + (ONE - pr.rf_soot_form) * a3(BS_SOOT_PREV, i, j, k);
+                    }
+                    if (Tcell > pr.t0_so) {
+                        a3(SFP, i, j, k) = -pr.aoxid * gfm(i, j, k, 2) * (std::sqrt(Tcell) * std::exp(-pr.eso_r / Tcell) - E0_so) * snorm;
+                        if (itr_ms > 1)
+                            a3(SFP, i, j, k) = pr.rf_soot_oxid * a3(SFP, i, j, k) + (ONE - pr.rf_soot_oxid) * a3(SFP_SOOT_PREV, i, j, k);
+                    }
+                }
+        BS_SOOT_PREV = BS;
+        SFP_SOOT_PREV = SFP;
+    }
+    // MSFLOW (Msflow.f90:29-165); returns the iterations done
+    int MSFLOW(int maxms, double* gfm_out, double& svf_r) {
+        IGS0 = 0;
+        int done = 0;
+        for (int L1 = 1; L1 <= maxms; ++L1) {
+            itr_ms = itr_ms + 1;
+            ++done;
+            GSLV3M();
+            for (int L = 1; L <= 7; ++L)
+                gfm_out[L - 1] = flxm(5, L, 2) + flxm(MP - 3, L, 1) + flym(5, L, 2) + flym(NP - 3, L, 1);
+            double G1 = 0;
+            svf_r = 0;
+            for (int I = 2; I <= MP; I += 2)
+                for (int J = 2; J <= NP; J += 2)
+                    for (int K = 2; K <= LP; K += 2) {
+                        if (ibcell(I, J, K) != 3) continue;
+                        double G0 = AREA_C(I, J, K, 3);
+                        if (G0 < small20) G0 = AREA_C(I, J, K, 2);
+                        if (G0 < small20) G0 = AREA_C(I, J, K, 1);
+                        G1 = G1 + G0;
+                        svf_r = svf_r + a3(SMF, I, J, K) * a3(DNST, I, J, K) * pr.dnst0 / DNST_SOOT * G0;
+                    }
+            svf_r = svf_r / G1;
+            imscon = 0;
+            if (itr_ms > 10) {
+                imscon = 1;
+                for (int l = 1; l <= 8; ++l) if (resid_ms[l] > pr.bmcon) imscon = 0;
+            }
+            if (imscon == 1) break;
+            EXTRM();
+            INTPM();
+        }
+        return done;
+    }
+
     void props(double G0) {   // Gflow.f90:302-382
         for (int I = 2; I <= MP; I += 2)
             for (int J = 2; J <= NP; J += 2)
@@ -3196,7 +3594,6 @@ int gfo_gflow_steps(void* vo, int stop_after) {
 int gfo_gflow(void* vo, int n_iter, gfm_iter_stats* out, int* n_done) {
     Oracle* o = static_cast<Oracle*>(vo);
     if (!o || n_iter < 0) return GFM_E_ARG;
-    if (o->pr.rad_emission && o->pr.gas_model && !o->minor_on) return GFM_E_ARG;
     int done = 0, conv = 0;
     for (int it = 0; it < n_iter; ++it) {
         o->itr_gas = o->itr_gas + 1;
@@ -3206,6 +3603,13 @@ int gfo_gflow(void* vo, int n_iter, gfm_iter_stats* out, int* n_done) {
         if (o->pr.rad_emission) {   // Sphase.f90:204-231 (emission only)
             o->do_rad_qe_only_cnt = o->do_rad_qe_only_cnt + 1;
             if (o->do_rad_qe_only_cnt >= o->pr.rad_qe_frequency && o->itr_gas > 50) {
+                if (o->pr.gas_model && o->i1st_rad_qe_done == 0) {
+                    // the first emission update runs INITSVM and MSFLOW(300) before it
+                    double out[7], svf;
+                    o->INITSVM(o->pr.irstypm != 0 && o->minor_from_host);
+                    o->MSFLOW(300, out, svf);
+                }
+                if (o->pr.gas_model && !o->minor_on) return GFM_E_ARG;
                 o->rad_qe_only();
                 o->do_rad_qe_only_cnt = 0;
             }
@@ -3377,7 +3781,35 @@ int gfo_minor_set(void* vo, const gfm_minor* m) {
     copy_in(o->RRMS, m->rrms, 5 * NCA);
     o->itr_ms = m->itr_ms;
     o->imscon = m->imscon;
+    if (!o->minor_on) for (int l = 0; l <= 8; ++l) { o->resid_ms[l] = 1.0e-16; o->resid_ms_pre[l] = 1.0e-16; }
     o->minor_on = 1;
+    o->minor_from_host = 1;
+    return GFM_OK;
+}
+int gfo_initsvm(void* vo, int restart) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || (restart && !o->minor_on)) return GFM_E_ARG;
+    o->INITSVM(restart);
+    return GFM_OK;
+}
+int gfo_msflow(void* vo, int maxms, gfm_msflow_stats* out) {
+    Oracle* o = static_cast<Oracle*>(vo);
+    if (!o || maxms < 0 || !o->minor_on) return GFM_E_ARG;
+    double g[7] = {0}, svf = 0;
+    const int done = o->MSFLOW(maxms, g, svf);
+    if (out) {
+        std::memset(out, 0, sizeof *out);
+        out->itr_ms = o->itr_ms;
+        out->iterations = done;
+        out->converged = o->imscon;
+        for (int l = 0; l < 8; ++l) { out->resid_ms_pre[l] = o->resid_ms_pre[l + 1]; out->resid_ms[l] = o->resid_ms[l + 1]; }
+        out->bal_ms = o->bal_ms;
+        out->soot_tot = o->soot_tot;
+        out->smf_max = o->smf_max;
+        out->smf_max_noclip = o->smf_max_noclip;
+        for (int l = 0; l < 7; ++l) out->gfm_out[l] = g[l];
+        out->svf_r = svf;
+    }
     return GFM_OK;
 }
 int gfo_minor_get(void* vo, gfm_minor* m) {

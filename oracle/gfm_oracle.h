@@ -62,6 +62,12 @@ int   gfo_minor_set(void *o, const gfm_minor *m);
 /* The emission-only source QE from the current state (rad_qe_only,
  * Rad_emis.f90:411-466 with RAD0). */
 int   gfo_rad_emission(void *o);
+/* INITSVM (restart 0: from the major species; 1: the state set by
+ * gfo_minor_set, inlets reset, exits extrapolated) and MSFLOW on the frozen
+ * flow.  With params.gas_model and the emission update on, gfo_gflow's
+ * first emission update runs them first (MSFLOW(300)), as SPHASE does. */
+int   gfo_initsvm(void *o, int restart);
+int   gfo_msflow(void *o, int maxms, gfm_msflow_stats *out);
 int   gfo_minor_get(void *o, gfm_minor *m);
 double gfo_rif3(double x);
 double gfo_zy1(const double *x, const double *y, double x1, int n);

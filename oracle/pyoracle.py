@@ -50,6 +50,8 @@ def load(check_bounds: bool = False) -> C.CDLL:
     lib.gfo_minor_set.argtypes = [C.c_void_p, C.POINTER(abi.GfmMinor)]
     lib.gfo_minor_get.argtypes = [C.c_void_p, C.POINTER(abi.GfmMinor)]
     lib.gfo_rad_emission.argtypes = [C.c_void_p]
+    lib.gfo_initsvm.argtypes = [C.c_void_p, C.c_int]
+    lib.gfo_msflow.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.GfmMsflowStats)]
     for n in ("gfo_da", "gfo_tgamf", "gfo_emf", "gfo_rif3", "gfo_t_to_enth", "gfo_enth_to_t", "gfo_zy1", "gfo_atand"):
         getattr(lib, n).restype = C.c_double
     lib.gfo_da.argtypes = [C.c_double, C.c_double]
@@ -164,6 +166,18 @@ class Oracle:
         rc = self.lib.gfo_rad_emission(self.o)
         if rc != 0:
             raise RuntimeError(f"gfo_rad_emission: {rc}")
+
+    def initsvm(self, restart: bool = False) -> None:
+        rc = self.lib.gfo_initsvm(self.o, int(restart))
+        if rc != 0:
+            raise RuntimeError(f"gfo_initsvm: {rc}")
+
+    def msflow(self, maxms: int) -> dict:
+        st = abi.GfmMsflowStats()
+        rc = self.lib.gfo_msflow(self.o, maxms, C.byref(st))
+        if rc != 0:
+            raise RuntimeError(f"gfo_msflow: {rc}")
+        return st.as_dict()
 
     def minor_set(self, m) -> None:
         """The minor species state (a gfm_gb300.solver.Minor) the band model
