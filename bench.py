@@ -548,6 +548,13 @@ def run_ours(args):
         except Exception as e:   # reported, never required
             wall = {"failed": str(e)}
 
+    minor = None
+    if rank == 0 and not args.no_minor:
+        try:
+            minor = minor_species_leg(args, not args.no_cpu_baseline)
+        except Exception as e:   # reported, never required
+            minor = {"failed": str(e)}
+
     batched = None
     if rank == 0 and not args.no_batched:
         try:
@@ -593,6 +600,7 @@ def run_ours(args):
             "rad_transfer": rad,
             "tc21_case0041": tc21,
             "wall_exchange": wall,
+            "minor_species": minor,
             "clocks": clk.summary(),
             "gpu_launches": int(prof["kernels_per_iter"] * nd),
             "plain_fp64": plain,
@@ -729,6 +737,125 @@ def rad_transfer_leg(with_cpu: bool) -> dict:
     return out
 
 
+def _converged_case0041(d: pathlib.Path, **kw):
+    """TC21 case 0041 read from its files with the end-of-run restarts of its
+    reference run (rg0041c.d, rs0041c.d), and that run's minor species."""
+    import lzma
+    import shutil
+    from gfm_gb300 import Case
+    gold = pathlib.Path(__file__).resolve().parent / "tests" / "golden" / "case0041"
+    for n in ("gd0041c.dat", "sbc0041c.dat", "it0041t.dat", "relaxfactorc.txt"):
+        shutil.copyfile(gold / n, d / n)
+    for k in ("rg", "rs"):
+        (d / f"{k}0041c.d").write_bytes(lzma.decompress((gold / f"{k}0041c.d.xz").read_bytes()))
+    case = Case.from_files(d, "0041", restart=True, gas_model=True, **kw)
+    ref = json.loads((gold / "case0041_reference.json").read_text())["rad_detail_last"]
+    return case, case.read_minor(d / "rs0041c.d"), ref
+
+
+def minor_species_leg(args, with_cpu: bool) -> dict:
+    """The band model and the minor species (gas.cu, minor.cu).  On TC21 case
+    0041 from its reference run's end-of-run restarts (FP64): the volume
+    transfer on the band model (RAD_GAS and SOOTA in RAD0) with its error
+    against that run's own radiation record, and MSFLOW(300) after one gas
+    iteration; next to the oracle on one host core (the transfer, and 30
+    MSFLOW iterations scaled to 300).  On the 192x96x64 furnace (mixed, red-
+    black, from INITSVM's new start after 3 iterations): one MSFLOW iteration
+    and one emission update with the band model against the gray one."""
+    import tempfile
+    import numpy as np
+    from gfm_gb300 import Case, GpuSolver, abi, configs
+    from oracle.pyoracle import Oracle
+    keys = (("tot_qe_h2o_co2", "qe_h2o_co2"), ("tot_qe_soot", "qe_soot"), ("qe_sum_from_open", "qe_from_media"),
+            ("qa_sum_to_melt", "qa_melt"), ("qa_sum_to_wall", "qa_wall"), ("qa_sum_to_open", "qa_media"))
+    out = {}
+    with tempfile.TemporaryDirectory() as dd:
+        case, minor, ref = _converged_case0041(pathlib.Path(dd))
+        g = GpuSolver(case, precision=abi.GFM_PREC_FP64, adi_mode=abi.GFM_ADI_REDBLACK)
+        g.start()
+        g.minor_upload(minor)
+        g.rad_transfer()   # first call: buffers, launch plan
+        ts = []
+        for _ in range(3):
+            g.start()
+            t0 = time.perf_counter()
+            tot = g.rad_transfer()
+            ts.append(time.perf_counter() - t0)
+        err = max(abs(tot[a] / ref[b] - 1.0) for a, b in keys)
+        g.start()
+        g.gflow(1)
+        g.initsvm(restart=True)
+        t0 = time.perf_counter()
+        st = g.msflow(300)
+        t_ms = time.perf_counter() - t0
+        g.close()
+        out["tc21"] = {"workload": f"TC21 case 0041 ({case.ncells:,} open cells, 10 bands) from its reference run's "
+                                   "end-of-run restarts, FP64, red-black order",
+                       "transfer_seconds": sorted(ts)[1],
+                       "transfer_max_rel_error_vs_reference_record": err,
+                       "msflow_300_seconds": t_ms, "msflow_resid": st["resid_ms"],
+                       "timing": "host wall clock around the synchronous calls (transfer: median of 3)"}
+        if with_cpu:
+            o = Oracle(case)
+            o.initsv()
+            o.minor_set(minor)
+            t0 = time.perf_counter()
+            o.rad_transfer()
+            t_o = time.perf_counter() - t0
+            o2 = Oracle(case)
+            o2.initsv()
+            o2.gflow(1)
+            o2.minor_set(minor)
+            o2.initsvm(restart=True)
+            t0 = time.perf_counter()
+            o2.msflow(30)
+            t_o_ms = (time.perf_counter() - t0) * 10.0
+            out["tc21"]["cpu_baseline"] = {"transfer_seconds": t_o, "msflow_300_seconds": t_o_ms, "cores": 1,
+                                           "kind": "port", "sample": "the oracle's transfer; 30 MSFLOW iterations "
+                                                                     "scaled to 300"}
+            out["tc21"]["transfer_speedup"] = t_o / out["tc21"]["transfer_seconds"]
+            out["tc21"]["msflow_speedup"] = t_o_ms / t_ms
+            o.close()
+            o2.close()
+    # the 192x96x64 furnace
+    prec = abi.GFM_PREC_MIXED if args.prec == "mixed" else abi.GFM_PREC_FP64
+    case = Case(configs.large_furnace())
+    case.c.params.gas_model = 1
+    g = GpuSolver(case, precision=prec, adi_mode=abi.GFM_ADI_REDBLACK)
+    g.start()
+    g.gflow(3)
+    g.initsvm(restart=False)
+    g.msflow(3)
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = g.msflow(20)
+    t_it = (time.perf_counter() - t0) / 20
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        g.rad_emission()
+        ts.append(time.perf_counter() - t0)
+    t_band = sorted(ts)[1]
+    g.close()
+    case.c.params.gas_model = 0
+    g = GpuSolver(case, precision=prec, adi_mode=abi.GFM_ADI_REDBLACK)
+    g.start()
+    ts = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        g.rad_emission()
+        ts.append(time.perf_counter() - t0)
+    t_gray = sorted(ts)[1]
+    g.close()
+    case.close()
+    out["furnace_192x96x64"] = {"precision": args.prec, "msflow_ms_per_iteration": 1e3 * t_it,
+                                "emission_band_model_ms": 1e3 * t_band, "emission_gray_ms": 1e3 * t_gray,
+                                "timing": "host wall clock around synchronous calls (MSFLOW: 20 iterations after 3; "
+                                          "emission: median of 3)"}
+    return out
+
+
 def wall_exchange_leg(with_cpu: bool) -> dict:
     """The wall radiosity exchange (wall_q_amb and wallq after the volume
     transfer, Qwall.f90:990-1245) on TC21 case 0041 read from its files, gray
@@ -842,6 +969,7 @@ def main():
     ap.add_argument("--no-rad", action="store_true", help="skip the volume radiation transfer leg")
     ap.add_argument("--no-tc21", action="store_true", help="skip the TC21 case 0041 leg")
     ap.add_argument("--no-wall", action="store_true", help="skip the wall radiosity exchange leg")
+    ap.add_argument("--no-minor", action="store_true", help="skip the band model and minor species leg")
     ap.add_argument("--case", choices=["large", "medium", "xl"], default="large",
                     help="medium: the same furnace at 96x48x32, for kernel captures; xl: 384x160x96 with 10 bands "
                          "(neither is the benchmark workload)")

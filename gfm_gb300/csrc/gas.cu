@@ -131,11 +131,51 @@ __device__ inline double banda(double ALP, double BTA, double A0, double W_R, do
     return A0 * A_S;
 }
 
-struct Cell { double T_RAD, TT0, P_RAD, YCO2, YH2O, OPL; };
+// A cell's state for the band model, with U = HCK*V/T_RAD of the three band
+// centres of each gas and exp(-U), exp(-U/2): CHIWHI's terms
+// exp(-U*NV)/PER(NG-1,NG-1)*PER(...) are formed as products of these powers,
+// and the square roots of its integer factors PER(M,N) come from a table,
+// which leaves one exponential per centre and cell in place of one per term
+// (the same sums to the last bits: the powers carry NV rounding steps)
+struct Cell {
+    double T_RAD, TT0, P_RAD, YCO2, YH2O, OPL;
+    double U[2][3], eU[2][3], eUh[2][3];
+};
+constexpr int kPerRows = 104;   // NV + NG + NDK - 1 <= 99 + 2 + 2 - 1 (NV stops at 100)
+
+__device__ inline void chiwhi_fast(const Cell& c, const double* __restrict__ sqper, int s, double& CHI, double& YNXY) {
+    const int gas = site_gas(s);
+    double UD = 0.0, XD = 0.0, XY = 0.0, YN = 0.0;
+    for (int K = 0; K < 3; ++K) {
+        const int ng = site_ng(gas, K), nd = site_nd(s, K);
+        int NV = nd < 0 ? -nd : 0;
+        const int NDK = nd < 0 ? -nd : nd;
+        double e = 1.0, eh = 1.0;                 // exp(-U*NV), exp(-U*NV/2)
+        for (int q = 0; q < NV; ++q) { e *= c.eU[gas][K]; eh *= c.eUh[gas][K]; }
+        double Y1 = 0.0;
+        for (;;) {
+            // PER(NG-1,NG-1) = 1 for NG = 1, 2
+            const double X1 = e * per(NV + ng + NDK - 1, ng + NDK - 1);
+            const double X2 = e * per(NV + ng - 1, ng - 1);
+            if (X1 < 1.0e-10) break;
+            XY = XY + X1;
+            XD = XD + X2;
+            Y1 = Y1 + eh * __ldg(sqper + (NV + ng + NDK - 1) * 4 + (ng + NDK - 1));
+            NV = NV + 1;
+            if (NV >= 100) break;
+            e *= c.eU[gas][K];
+            eh *= c.eUh[gas][K];
+        }
+        YN = YN + Y1 * Y1;
+        UD = UD - c.U[gas][K] * nd;
+    }
+    CHI = (1.0 - exp(UD)) * XY / XD;
+    YNXY = YN / XY;
+}
 
 // CHIWHI at T0_R and at T_RAD for one site
-__device__ inline void chiwhi_pair(const GasConst& k, int s, const Cell& c, double& CHI0, double& WHI0, double& CHI,
-                                   double& WHI) {
+__device__ inline void chiwhi_pair(const GasConst& k, const double* sqper, int s, const Cell& c, double& CHI0, double& WHI0,
+                                   double& CHI, double& WHI) {
     const double r = sqrt(c.TT0);
     if (s == H1) {   // pure rotational band: ND_R all zero
         CHI0 = 1.0; WHI0 = 1.0 / r; CHI = 1.0; WHI = 1.0 / r;
@@ -144,15 +184,15 @@ __device__ inline void chiwhi_pair(const GasConst& k, int s, const Cell& c, doub
     CHI0 = k.chi0[s];
     WHI0 = k.ynxy0[s] / r;
     double ynxy;
-    chiwhi_sums(s, c.T_RAD, CHI, ynxy);
+    chiwhi_fast(c, sqper, s, CHI, ynxy);
     WHI = ynxy / r;
 }
 
 // A1 (Rad_gas.f90:284-296)
-__device__ inline double a1(const GasConst& k, int s, double B1, double B2, double B3, const Cell& c, double W_R,
-                            double PE, int& err) {
+__device__ inline double a1(const GasConst& k, const double* sqper, int s, double B1, double B2, double B3, const Cell& c,
+                            double W_R, double PE, int& err) {
     double CHI0, WHI0, CHI, WHI;
-    chiwhi_pair(k, s, c, CHI0, WHI0, CHI, WHI);
+    chiwhi_pair(k, sqper, s, c, CHI0, WHI0, CHI, WHI);
     const double C3 = B3 * sqrt(c.T_RAD / kT0R);
     const double C1 = B1 * CHI / CHI0;
     const double C2 = 2.0 * sqrt(C1 * C3 * B2 * WHI / WHI0);
@@ -160,48 +200,48 @@ __device__ inline double a1(const GasConst& k, int s, double B1, double B2, doub
 }
 
 // AH2O (Rad_gas.f90:149-212): band absorptances of H2O (1/m)
-__device__ void ah2o(const GasConst& k, const Cell& c, double* AA, int& err) {
+__device__ void ah2o(const GasConst& k, const double* sqper, const Cell& c, double* AA, int& err) {
     for (int n = 0; n < 5; ++n) AA[n] = 0.0;
     if (c.YH2O <= 0.0 || c.T_RAD <= 3.0e+2) return;
     const double PE = c.P_RAD + c.P_RAD * c.YH2O * (0.86e+1 / c.TT0 - 0.5);
     const double W_R = c.P_RAD * c.YH2O * c.OPL / c.T_RAD / 8.208e-2 * kWh2o;
-    AA[0] = a1(k, H1, 0.52e+4 * exp(-0.176e+2 / c.TT0), 0.14311, 0.284e+2, c, W_R, PE, err);
-    AA[1] = a1(k, H2, 0.412e+2, 0.9427e-1, 0.564e+2, c, W_R, PE, err);
+    AA[0] = a1(k, sqper, H1, 0.52e+4 * exp(-0.176e+2 / c.TT0), 0.14311, 0.284e+2, c, W_R, PE, err);
+    AA[1] = a1(k, sqper, H2, 0.412e+2, 0.9427e-1, 0.564e+2, c, W_R, PE, err);
     double CHI0, WHI0, CHI, WHI;
-    chiwhi_pair(k, H3A, c, CHI0, WHI0, CHI, WHI);
+    chiwhi_pair(k, sqper, H3A, c, CHI0, WHI0, CHI, WHI);
     const double T1 = 0.19 * CHI / CHI0, T4 = 0.13219 * WHI / WHI0;
-    chiwhi_pair(k, H3B, c, CHI0, WHI0, CHI, WHI);
+    chiwhi_pair(k, sqper, H3B, c, CHI0, WHI0, CHI, WHI);
     const double T2 = 0.23e+1 * CHI / CHI0, T5 = 0.13219 * WHI / WHI0;
-    chiwhi_pair(k, H3C, c, CHI0, WHI0, CHI, WHI);
+    chiwhi_pair(k, sqper, H3C, c, CHI0, WHI0, CHI, WHI);
     const double T3 = 0.224e+2 * CHI / CHI0, T6 = 0.13219 * WHI / WHI0;
     const double C1 = T1 + T2 + T3;
     const double C3 = 0.6e+2 * c.TT0;
     const double BTA = 2.0 * sqrt(C3) * (sqrt(T1 * T4) + sqrt(T2 * T5) + sqrt(T3 * T6));
     AA[2] = banda(C1, BTA, C3, W_R, PE, err);
-    AA[3] = a1(k, H4, 3.0, 0.8169e-1, 0.431e2, c, W_R, PE, err);
-    AA[4] = a1(k, H5, 0.25e+1, 0.11628, 0.32e+2, c, W_R, PE, err);
+    AA[3] = a1(k, sqper, H4, 3.0, 0.8169e-1, 0.431e2, c, W_R, PE, err);
+    AA[4] = a1(k, sqper, H5, 0.25e+1, 0.11628, 0.32e+2, c, W_R, PE, err);
     for (int n = 0; n < 5; ++n) AA[n] = AA[n] * 1.0e+2;
 }
 
 // ACO2 (Rad_gas.f90:224-274): band absorptances of CO2 (1/m)
-__device__ void aco2(const GasConst& k, const Cell& c, double* AA, int& err) {
+__device__ void aco2(const GasConst& k, const double* sqper, const Cell& c, double* AA, int& err) {
     const double W_R = c.P_RAD * c.YCO2 * c.OPL / c.T_RAD / 8.208e-2 * kWco2;
     if (W_R <= 0.0) { err |= 4; for (int n = 0; n < 6; ++n) AA[n] = 0.0; return; }
     const double q = c.P_RAD + c.P_RAD * c.YCO2 * 0.3;
     double PE = pow(q, 0.7);
-    AA[0] = a1(k, C1, 0.19e+2, 0.6157e-1, 0.127e2, c, W_R, PE, err);
+    AA[0] = a1(k, sqper, C1, 0.19e+2, 0.6157e-1, 0.127e2, c, W_R, PE, err);
     PE = pow(q, 0.8);
-    AA[1] = a1(k, C23, 0.36, 0.4017e-1, 0.134e+2, c, W_R, PE, err);
-    AA[2] = a1(k, C23, 0.24, 0.11888, 0.101e+2, c, W_R, PE, err);
-    AA[3] = a1(k, C4, 0.11e+3, 0.24723, 0.112e+2, c, W_R, PE, err);
+    AA[1] = a1(k, sqper, C23, 0.36, 0.4017e-1, 0.134e+2, c, W_R, PE, err);
+    AA[2] = a1(k, sqper, C23, 0.24, 0.11888, 0.101e+2, c, W_R, PE, err);
+    AA[3] = a1(k, sqper, C4, 0.11e+3, 0.24723, 0.112e+2, c, W_R, PE, err);
     PE = pow(q, 0.65);
-    AA[4] = a1(k, C5, 4.0, 0.13341, 23.5, c, W_R, PE, err);
-    AA[5] = a1(k, C6, 0.66e-1, 0.39305, 0.345e+2, c, W_R, PE, err);
+    AA[4] = a1(k, sqper, C5, 4.0, 0.13341, 23.5, c, W_R, PE, err);
+    AA[5] = a1(k, sqper, C6, 0.66e-1, 0.39305, 0.345e+2, c, W_R, PE, err);
     for (int n = 0; n < 6; ++n) AA[n] = AA[n] * 1.0e+2;
 }
 
 // RAD_GAS without SOOTA (Rad_gas.f90:23-134): AKLG of every band
-__device__ void rad_gas(const GasConst& k, const Cell& c, double* AKLG, int& err) {
+__device__ void rad_gas(const GasConst& k, const double* sqper, const Cell& c, double* AKLG, int& err) {
     const double EPS1 = 1.0e-4;
     double WH[5][3], WC[6][3], WNG[11][2];
     for (int n = 0; n < 5; ++n) WH[n][0] = WH[n][1] = WH[n][2] = 0.0;
@@ -210,7 +250,7 @@ __device__ void rad_gas(const GasConst& k, const Cell& c, double* AKLG, int& err
     if (c.YH2O > EPS1) {
         WH[1][1] = 1.60e+5; WH[2][1] = 3.76e+5; WH[3][1] = 5.35e+5; WH[4][1] = 7.25e+5;
         double AA[5];
-        ah2o(k, c, AA, err);
+        ah2o(k, sqper, c, AA, err);
         WH[0][1] = AA[0] / 2;
         WH[0][2] = AA[0];
         for (int N = 1; N < 5; ++N) {
@@ -224,7 +264,7 @@ __device__ void rad_gas(const GasConst& k, const Cell& c, double* AKLG, int& err
         WC[0][1] = 6.67e+4; WC[1][1] = 9.60e+4; WC[2][1] = 1.06e+5;
         WC[3][2] = 2.41e+5; WC[4][1] = 3.66e+5; WC[5][1] = 5.20e+5;
         double AA[6];
-        aco2(k, c, AA, err);
+        aco2(k, sqper, c, AA, err);
         for (int N = 0; N < 6; ++N) {
             const double G0 = AA[N] / 2;
             if (N == 0 && G0 > WC[0][1]) {
@@ -291,6 +331,7 @@ struct GasArgs {
     double t0, pg0, dnst0;
     GasConst k;
     double *aklg, *akls, *fvs;   // aklg/akls: cell + l*n (cell = I fastest); fvs by loop order
+    const double* sqper;         // sqrt(PER(M,N)), M < kPerRows, N <= 3, at M*4 + N
     int* setter;                 // by loop order q = ((I/2-1)*NZ + J/2-1)*LZ + K/2-1: q or -1
     int* blockmax;
     int* err;
@@ -330,7 +371,13 @@ __global__ void __launch_bounds__(128) k_gas_band(GasArgs<R> a) {
             if (sa > kSmall16) {
                 cl.OPL = 6.0 * vol / sa;
                 if (cl.OPL > 1.0e-10) {
-                    rad_gas(a.k, cl, aklg, err);
+                    for (int gs = 0; gs < 2; ++gs)
+                        for (int K = 0; K < 3; ++K) {
+                            cl.U[gs][K] = kHckR * site_v(gs, K) / T_RAD;
+                            cl.eU[gs][K] = exp(-cl.U[gs][K]);
+                            cl.eUh[gs][K] = exp(-0.5 * cl.U[gs][K]);
+                        }
+                    rad_gas(a.k, a.sqper, cl, aklg, err);
                     if (fvs >= 1.0e-14) set = q;
                 }
             }
@@ -426,6 +473,12 @@ double soot_g0(double WL0) {
 
 int gas_scan_blocks(int ncell) { return (ncell + kScanBlock - 1) / kScanBlock; }
 
+int gas_sqper_size() { return kPerRows * 4; }
+void gas_sqper_fill(double* t) {
+    for (int m = 0; m < kPerRows; ++m)
+        for (int n = 0; n < 4; ++n) t[m * 4 + n] = n <= m ? std::sqrt(per(m, n)) : 0.0;
+}
+
 void launch_prefix_max(int* a, int n, int* blockmax, cudaStream_t st) {
     const int nb = gas_scan_blocks(n);
     k_gas_scan_block<<<nb, kScanBlock, 0, st>>>(a, n, blockmax);
@@ -450,6 +503,7 @@ int launch_gas_band(const GasBuffers& b, const GeoT<double>& g, const R* T, cons
         chiwhi_sums(s, kT0R, a.k.chi0[s], a.k.ynxy0[s]);
     }
     a.aklg = b.aklg; a.akls = b.akls; a.fvs = b.fvs; a.setter = b.setter; a.blockmax = b.blockmax; a.err = b.err;
+    a.sqper = b.sqper;
     const int n = a.MZ * a.NZ * a.LZ;
     const int gb = (n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096;
     k_gas_band<R><<<gb, 128, 0, st>>>(a);

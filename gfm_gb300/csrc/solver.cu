@@ -1649,9 +1649,20 @@ extern "C" int gfm_gpu_wall_get(gfm_handle* h, const char* name, double* out, in
     const WallArgs& a = h->wall;
     if (cap < a.nb) return GFM_E_ARG;
     const std::string s(name);
+    if (s == "qrs") {
+        // the melt-surface heat flux of the melt patches, qc + q_conv + the
+        // radiation from the boundaries - the radiosity (Qwall.f90:1166), 0 elsewhere
+        std::vector<double> qc(a.nb), qv(a.nb), rad(a.nb), J(a.nb);
+        CK(cudaMemcpy(qc.data(), a.qc, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(qv.data(), a.qconv, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(rad.data(), a.rad, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(J.data(), a.J, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < a.nb; ++i) out[i] = h->wall_typ[i] == 4 ? qc[i] + qv[i] + rad[i] - J[i] : 0.0;
+        return a.nb;
+    }
     const double* src = s == "b_t" ? a.bT : s == "radiosity" ? a.J : s == "q_amb" ? a.qamb : s == "q_conv" ? a.qconv
                       : s == "qc" ? a.qc : s == "qeb" ? a.qeb : s == "emis" ? a.emis : s == "b_face_area" ? a.face_area
-                      : s == "patch_area" ? a.area : nullptr;
+                      : s == "patch_area" ? a.area : s == "rad" ? a.rad : nullptr;
     if (!src) return GFM_E_ARG;
     CK(cudaMemcpy(out, src, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
     return a.nb;
@@ -1747,6 +1758,11 @@ int gas_band(gfm_handle* h) {
             (rc = dalloc(h, &h->gas.fvs, ncl)) || (rc = dalloc(h, &h->gas.setter, ncl)) ||
             (rc = dalloc(h, &h->gas.blockmax, gas_scan_blocks(ncl))) || (rc = dalloc(h, &h->gas.err, 1)))
             return rc;
+        std::vector<double> t((size_t)gas_sqper_size());
+        gas_sqper_fill(t.data());
+        double* d = nullptr;
+        if ((rc = dupload(h, &d, t))) return rc;
+        h->gas.sqper = d;
     }
     if ((rc = ensure_double_coords(h))) return rc;
     const gfm_params& P = h->params;

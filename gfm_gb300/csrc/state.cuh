@@ -195,8 +195,11 @@ struct GasBuffers {
     double* fvs;                 // soot volume fraction, by loop order (K fastest)
     int *setter, *blockmax;      // the cells that set AKLS, and the prefix maxima
     int* err;                    // bit 1: BANDA argument < 0, bit 2: W_R <= 0 with CO2
+    const double* sqper;         // square roots of CHIWHI's integer factors (gas_sqper_fill)
 };
 int gas_scan_blocks(int ncell);
+int gas_sqper_size();
+void gas_sqper_fill(double* table);
 // in-place prefix maximum of a[0..n): a[i] becomes the maximum within its
 // block of 1024 up to i, blockmax[b] the maximum of the blocks before b
 // (gas_scan_blocks(n) entries); the full prefix at i is the larger of the two

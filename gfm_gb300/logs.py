@@ -34,6 +34,13 @@ The run files of the GUI's energy-balance views are written here too:
                      one energy record per iteration ((1x,i5,8e22.14),
                      track_energy, A0main.f90:371-399) and the energy balance
                      at the end of the run (A0main.f90:300-312)
+
+and the combustion side's hand-over to the melt domain:
+
+  it####m.dat        the melt-surface heat flux after a radiation call, with
+                     the mean wall temperature, the largest gas temperature
+                     and the heat into the melt (QRN_PRN, Qrn.f90:363-392);
+                     the melt domain reads it and writes it####t.dat back
 """
 from __future__ import annotations
 
@@ -289,3 +296,67 @@ class RunFiles:
             f.close()
         self.fh = {}
 
+
+
+# ---- it####m.dat: the heat flux into the melt ------------------------------------
+_MELT_LABELS = ("              Distribution indicator", "  Mean Wall Temperature in Combustion Space (K)",
+                "  Max Temperature in Combustion Space (K)", "  Heat Transfer to Melter (W)")
+
+
+def list_real(v: float) -> str:
+    """The reference compiler's list-directed output of a REAL(8) of
+    magnitude 0.1 to 1e15: fifteen significant digits in a 19-column F field
+    and six trailing blanks."""
+    import math
+    a = abs(v)
+    if not (0.1 <= a < 1.0e15):
+        return f"{v:25.15E}"
+    e = int(math.floor(math.log10(a)))
+    for ee in (e, e + 1):
+        t = f"{a:.{max(0, 14 - ee)}f}"
+        if len(t.replace(".", "").lstrip("0")) <= 15 or ee == e + 1:
+            break
+    return (("-" if v < 0 else "") + t).rjust(19) + " " * 6
+
+
+def melt_flux_file(x, r, qrs, avg_wall_T: float, tmax_c: float, q_melt: float, itn: int = 1) -> bytes:
+    """it####m.dat as QRN_PRN writes it (Qrn.f90:363-392).  x and r are the
+    doubled grid's X(1..MP) and R(1..NP) (0-based arrays), qrs[(I, J)] the
+    melt-surface heat flux (W/m2) at the even positions that have one (0
+    elsewhere).  Returns the bytes, CR-LF line ends."""
+    mp, np_ = len(x), len(r)
+    lines = [fortran_i(itn, 12) + " " + _MELT_LABELS[0]]
+    for v, lab in zip((avg_wall_T, tmax_c, q_melt), _MELT_LABELS[1:]):
+        lines.append(list_real(v) + lab)
+    lines += ["", " " * 9 + "Surface Radiation Heat Flux (W/m**2)"]
+    j1 = 2
+    while True:
+        j2 = min(j1 + 20, np_)
+        js = range(j1, j2 + 1, 2)
+        lines += ["", "    X  /  Y" + "".join(f"{r[j - 1]:11.3f}" for j in js)]
+        for i in range(2, mp + 1, 2):
+            lines.append(f"{x[i - 1]:11.3f}" + "".join(fortran_e(float(qrs.get((i, j), 0.0)), 11, 4) for j in js))
+        j1 = j2 + 2
+        if j1 > np_:
+            break
+    return ("\r\n".join(lines) + "\r\n").encode()
+
+
+def read_melt_flux_file(data: bytes, mp: int, np_: int) -> dict:
+    """The numbers of an it####m.dat: itn, avg_wall_T, tmax_c, q_melt and
+    qrs[(I, J)] in the file's column order."""
+    rows = data.decode().split("\r\n")
+    out = {"itn": int(rows[0].split()[0]), "avg_wall_T": float(rows[1].split()[0]),
+           "tmax_c": float(rows[2].split()[0]), "q_melt": float(rows[3].split()[0]), "qrs": {}}
+    k, j1 = 6, 2
+    while j1 <= np_:
+        j2 = min(j1 + 20, np_)
+        js = list(range(j1, j2 + 1, 2))
+        k += 2   # the blank line and the X / Y header
+        for i in range(2, mp + 1, 2):
+            vals = [float(rows[k][11 + 11 * n: 22 + 11 * n]) for n in range(len(js))]
+            for j, v in zip(js, vals):
+                out["qrs"][(i, j)] = v
+            k += 1
+        j1 = j2 + 2
+    return out

@@ -446,7 +446,9 @@ int  gfm_gpu_rad_transfer(gfm_handle *h, gfm_rad_totals *out);
  * patch order; both reach the same fixed point.  Every exit patch must lie in
  * an exhaust of `spec`.  gfm_gpu_wall_totals returns the last exchange's
  * results; gfm_gpu_wall_get copies one per-patch array ("b_t", "radiosity",
- * "q_amb", "q_conv", "qc", "qeb", "emis", "b_face_area", "patch_area") and
+ * "q_amb", "q_conv", "qc", "qeb", "emis", "b_face_area", "patch_area", "rad" the
+ * radiation from the boundaries, "qrs" the melt-surface heat flux of the melt
+ * patches, Qwall.f90:1166) and
  * returns the patch count. */
 int  gfm_gpu_wall_setup(gfm_handle *h, const gfm_wall_spec *spec);
 int  gfm_gpu_wall_totals(gfm_handle *h, gfm_wall_totals *out);

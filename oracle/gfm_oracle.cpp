@@ -3644,6 +3644,13 @@ long gfo_get_array(void* vo, const char* name, double* out, long cap) {
     const vec* patch_arr = s == "b_t" ? &o->b_T : s == "radiosity" ? &o->radiosity : s == "q_amb" ? &o->q_amb
                          : s == "q_conv" ? &o->q_conv : s == "qc" ? &o->qc : s == "qeb" ? &o->qeb : s == "emis" ? &o->emis
                          : s == "b_face_area" ? &o->b_face_area : s == "patch_area" ? &o->patch_area : nullptr;
+    if (s == "qrs") {   // QRS at each melt patch's (b_i, b_j), 0 for the others
+        const long nb = (long)o->b_typ.size();
+        if (cap < nb) return GFM_E_ARG;
+        for (long i = 0; i < nb; ++i)
+            out[i] = o->b_typ[i] == 4 && !o->qrs.empty() ? o->qrs[(size_t)(o->b_i[i] - 1) + (size_t)o->MP * (o->b_j[i] - 1)] : 0.0;
+        return nb;
+    }
     if (patch_arr) {
         const long nb = (long)patch_arr->size();
         if (cap < nb) return GFM_E_ARG;

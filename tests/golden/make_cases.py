@@ -30,7 +30,9 @@ reference's own run of the case printed:
 The first 48 lines of each per-iteration log (convg, gresid, gresid_xtra,
 Tave, Info and, where the run wrote them, the pre-solve gresidp and
 gresid_xtrap) and the first 80 lines of summary####c.txt are copied unchanged
-into logs/, as the byte-level reference of their format.  For case0041 the
+into logs/, as the byte-level reference of their format, and for the cases
+whose restarts are kept the melt hand-over file it####m.dat written by the
+run's last radiation call.  For case0041 the
 converged restart file rg0041c.d and the minor species restart rs0041c.d
 (written after the run's last MSFLOW, read by the RAD_EMIS of that last
 rad_detail record) are stored xz-compressed.
@@ -108,6 +110,7 @@ def main(pkg_root: str) -> None:
                 "qa_inlet", "qa_sum", "q_diff")
         ref["rad_detail_last"] = {"itr_gas": int(rad[-1][0]), **{k: float(v) for k, v in zip(keys, rad[-1][1:])}}
         if keep_rg:
+            shutil.copyfile(case / f"it{num}m.dat", out / "logs" / f"it{num}m.dat")
             for kind in ("rg", "rs"):
                 raw = (case / f"{kind}{num}c.d").read_bytes()
                 (out / f"{kind}{num}c.d.xz").write_bytes(lzma.compress(raw, preset=9))

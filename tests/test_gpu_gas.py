@@ -70,3 +70,32 @@ def test_band_model_without_minor_species_is_refused(tmp_path):
     g.upload(case.initial_fields())
     with pytest.raises(Exception):
         g.rad_transfer()
+
+
+def test_wall_exchange_with_band_model_reproduces_melt_handover(tmp_path):
+    """The GPU's transfer and wall exchange on the band model, from the
+    converged restarts of case 0041: the melt-surface heat flux, the mean
+    wall temperature and the heat into the melt against the oracle and
+    against the hand-over file the reference's run wrote
+    (tests/test_melt_handover.py)."""
+    import pathlib
+    from gfm_gb300 import logs
+    case, minor = converged("0041", tmp_path, wall_sink=True)
+    ref = logs.read_melt_flux_file((pathlib.Path(__file__).resolve().parent / "golden" / "case0041" / "logs" /
+                                    "it0041m.dat").read_bytes(), case.mp, case.np)
+    g = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    g.start()
+    g.minor_upload(minor)
+    g.wall_setup()
+    g.rad_transfer()
+    o = Oracle(case)
+    o.initsv()
+    o.minor_set(minor)
+    o.wall_setup()
+    o.rad_transfer()
+    tg, to = g.wall_totals(), o.wall_totals()
+    for k in ("avg_wall_T", "q_melt"):
+        assert tg[k] == pytest.approx(to[k], rel=1e-7), k
+    assert _rel(g.wall_array("qrs"), o.patch_array("qrs")) < 1e-7
+    assert tg["avg_wall_T"] == pytest.approx(ref["avg_wall_T"], rel=1e-6)
+    assert tg["q_melt"] == pytest.approx(ref["q_melt"], rel=1e-5)
