@@ -463,7 +463,7 @@ __global__ void k_rad_emission(Ctx<R> c, const double* __restrict__ gas_aklg, co
                 double deb[16], eb0 = 0.0;
                 for (int l = 1; l <= c.nwl - 1; ++l) {
                     double x1 = (c.p.hck / c.p.ri / c.wl[l - 1]) / T_rad;
-                    double eb1 = rif3(x1);
+                    double eb1 = rif3_pow(x1);
                     deb[l - 1] = eb1 - eb0;
                     if (deb[l - 1] <= 1.0e-3) deb[l - 1] = 0.0; else eb0 = eb1;
                 }

@@ -23,6 +23,7 @@
 #include "state.cuh"
 
 #include <cmath>
+#include <type_traits>
 
 namespace gfm {
 namespace {
@@ -86,6 +87,13 @@ __host__ __device__ inline double per(int M, int N) {   // PER, Rad_fun.f90:14-3
     for (int I = M - N + 1; I <= M; ++I) p = p * I;
     return p;
 }
+// the same in integers: CHIWHI's factors stay below 103*102*101, exact in int
+__host__ __device__ inline int per_i(int M, int N) {
+    int p = 1;
+    if (M == 0 || N == 0) return p;
+    for (int I = M - N + 1; I <= M; ++I) p = p * I;
+    return p;
+}
 
 // CHIWHI's sums (Rad_gas.f90:314-340) for a site with some ND_R non-zero:
 // CHI and YN/XY at temperature TT
@@ -116,18 +124,22 @@ __host__ __device__ inline void chiwhi_sums(int s, double TT, double& CHI, doubl
     YNXY = YN / XY;
 }
 
+// The band model in the arithmetic of the path: double on the FP64 path,
+// float on the mixed one (T below).  Every constant is converted to T first.
+
 // BANDA (Rad_gas.f90:360-395)
-__device__ inline double banda(double ALP, double BTA, double A0, double W_R, double PE, int& err) {
-    if (A0 <= 0) return 0.0;
-    if (ALP < 0.0 || BTA < 0.0 || A0 < 0.0 || W_R * PE < 0) { err |= 2; return 0.0; }
-    if (W_R * PE == 0) return 0.0;
-    const double ETA = BTA * PE;
-    const double TAU = ALP * W_R / A0;
-    double A_S;
-    if (ETA >= 1.0) A_S = TAU <= 1.0 ? TAU : 1.0 + log(TAU);
+template <typename T>
+__device__ inline T banda(T ALP, T BTA, T A0, T W_R, T PE, int& err) {
+    if (A0 <= T(0)) return T(0);
+    if (ALP < T(0) || BTA < T(0) || A0 < T(0) || W_R * PE < T(0)) { err |= 2; return T(0); }
+    if (W_R * PE == T(0)) return T(0);
+    const T ETA = BTA * PE;
+    const T TAU = ALP * W_R / A0;
+    T A_S;
+    if (ETA >= T(1)) A_S = TAU <= T(1) ? TAU : T(1) + log(TAU);
     else if (TAU <= ETA) A_S = TAU;
-    else if (TAU <= 1 / ETA) A_S = 2.0 * sqrt(ETA * TAU) - ETA;
-    else A_S = log(ETA * TAU) + 2.0 - ETA;
+    else if (TAU <= T(1) / ETA) A_S = T(2) * sqrt(ETA * TAU) - ETA;
+    else A_S = log(ETA * TAU) + T(2) - ETA;
     return A0 * A_S;
 }
 
@@ -137,27 +149,29 @@ __device__ inline double banda(double ALP, double BTA, double A0, double W_R, do
 // and the square roots of its integer factors PER(M,N) come from a table,
 // which leaves one exponential per centre and cell in place of one per term
 // (the same sums to the last bits: the powers carry NV rounding steps)
+template <typename T>
 struct Cell {
-    double T_RAD, TT0, P_RAD, YCO2, YH2O, OPL;
-    double U[2][3], eU[2][3], eUh[2][3];
+    T T_RAD, TT0, P_RAD, YCO2, YH2O, OPL;
+    T U[2][3], eU[2][3], eUh[2][3];
 };
 constexpr int kPerRows = 104;   // NV + NG + NDK - 1 <= 99 + 2 + 2 - 1 (NV stops at 100)
 
-__device__ inline void chiwhi_fast(const Cell& c, const double* __restrict__ sqper, int s, double& CHI, double& YNXY) {
+template <typename T>
+__device__ inline void chiwhi_fast(const Cell<T>& c, const T* __restrict__ sqper, int s, T& CHI, T& YNXY) {
     const int gas = site_gas(s);
-    double UD = 0.0, XD = 0.0, XY = 0.0, YN = 0.0;
+    T UD = T(0), XD = T(0), XY = T(0), YN = T(0);
     for (int K = 0; K < 3; ++K) {
         const int ng = site_ng(gas, K), nd = site_nd(s, K);
         int NV = nd < 0 ? -nd : 0;
         const int NDK = nd < 0 ? -nd : nd;
-        double e = 1.0, eh = 1.0;                 // exp(-U*NV), exp(-U*NV/2)
+        T e = T(1), eh = T(1);                    // exp(-U*NV), exp(-U*NV/2)
         for (int q = 0; q < NV; ++q) { e *= c.eU[gas][K]; eh *= c.eUh[gas][K]; }
-        double Y1 = 0.0;
+        T Y1 = T(0);
         for (;;) {
             // PER(NG-1,NG-1) = 1 for NG = 1, 2
-            const double X1 = e * per(NV + ng + NDK - 1, ng + NDK - 1);
-            const double X2 = e * per(NV + ng - 1, ng - 1);
-            if (X1 < 1.0e-10) break;
+            const T X1 = e * T(per_i(NV + ng + NDK - 1, ng + NDK - 1));
+            const T X2 = e * T(per_i(NV + ng - 1, ng - 1));
+            if (X1 < T(1.0e-10)) break;
             XY = XY + X1;
             XD = XD + X2;
             Y1 = Y1 + eh * __ldg(sqper + (NV + ng + NDK - 1) * 4 + (ng + NDK - 1));
@@ -167,108 +181,112 @@ __device__ inline void chiwhi_fast(const Cell& c, const double* __restrict__ sqp
             eh *= c.eUh[gas][K];
         }
         YN = YN + Y1 * Y1;
-        UD = UD - c.U[gas][K] * nd;
+        UD = UD - c.U[gas][K] * T(nd);
     }
-    CHI = (1.0 - exp(UD)) * XY / XD;
+    CHI = (T(1) - exp(UD)) * XY / XD;
     YNXY = YN / XY;
 }
 
 // CHIWHI at T0_R and at T_RAD for one site
-__device__ inline void chiwhi_pair(const GasConst& k, const double* sqper, int s, const Cell& c, double& CHI0, double& WHI0,
-                                   double& CHI, double& WHI) {
-    const double r = sqrt(c.TT0);
+template <typename T>
+__device__ inline void chiwhi_pair(const GasConst& k, const T* sqper, int s, const Cell<T>& c, T& CHI0, T& WHI0, T& CHI,
+                                   T& WHI) {
+    const T r = sqrt(c.TT0);
     if (s == H1) {   // pure rotational band: ND_R all zero
-        CHI0 = 1.0; WHI0 = 1.0 / r; CHI = 1.0; WHI = 1.0 / r;
+        CHI0 = T(1); WHI0 = T(1) / r; CHI = T(1); WHI = T(1) / r;
         return;
     }
-    CHI0 = k.chi0[s];
-    WHI0 = k.ynxy0[s] / r;
-    double ynxy;
+    CHI0 = T(k.chi0[s]);
+    WHI0 = T(k.ynxy0[s]) / r;
+    T ynxy;
     chiwhi_fast(c, sqper, s, CHI, ynxy);
     WHI = ynxy / r;
 }
 
 // A1 (Rad_gas.f90:284-296)
-__device__ inline double a1(const GasConst& k, const double* sqper, int s, double B1, double B2, double B3, const Cell& c,
-                            double W_R, double PE, int& err) {
-    double CHI0, WHI0, CHI, WHI;
+template <typename T>
+__device__ inline T a1(const GasConst& k, const T* sqper, int s, T B1, T B2, T B3, const Cell<T>& c, T W_R, T PE, int& err) {
+    T CHI0, WHI0, CHI, WHI;
     chiwhi_pair(k, sqper, s, c, CHI0, WHI0, CHI, WHI);
-    const double C3 = B3 * sqrt(c.T_RAD / kT0R);
-    const double C1 = B1 * CHI / CHI0;
-    const double C2 = 2.0 * sqrt(C1 * C3 * B2 * WHI / WHI0);
+    const T C3 = B3 * sqrt(c.T_RAD / T(kT0R));
+    const T C1 = B1 * CHI / CHI0;
+    const T C2 = T(2) * sqrt(C1 * C3 * B2 * WHI / WHI0);
     return banda(C1, C2, C3, W_R, PE, err);
 }
 
 // AH2O (Rad_gas.f90:149-212): band absorptances of H2O (1/m)
-__device__ void ah2o(const GasConst& k, const double* sqper, const Cell& c, double* AA, int& err) {
-    for (int n = 0; n < 5; ++n) AA[n] = 0.0;
-    if (c.YH2O <= 0.0 || c.T_RAD <= 3.0e+2) return;
-    const double PE = c.P_RAD + c.P_RAD * c.YH2O * (0.86e+1 / c.TT0 - 0.5);
-    const double W_R = c.P_RAD * c.YH2O * c.OPL / c.T_RAD / 8.208e-2 * kWh2o;
-    AA[0] = a1(k, sqper, H1, 0.52e+4 * exp(-0.176e+2 / c.TT0), 0.14311, 0.284e+2, c, W_R, PE, err);
-    AA[1] = a1(k, sqper, H2, 0.412e+2, 0.9427e-1, 0.564e+2, c, W_R, PE, err);
-    double CHI0, WHI0, CHI, WHI;
+template <typename T>
+__device__ void ah2o(const GasConst& k, const T* sqper, const Cell<T>& c, T* AA, int& err) {
+    for (int n = 0; n < 5; ++n) AA[n] = T(0);
+    if (c.YH2O <= T(0) || c.T_RAD <= T(3.0e+2)) return;
+    const T PE = c.P_RAD + c.P_RAD * c.YH2O * (T(0.86e+1) / c.TT0 - T(0.5));
+    const T W_R = c.P_RAD * c.YH2O * c.OPL / c.T_RAD / T(8.208e-2) * T(kWh2o);
+    AA[0] = a1(k, sqper, H1, T(0.52e+4) * exp(T(-0.176e+2) / c.TT0), T(0.14311), T(0.284e+2), c, W_R, PE, err);
+    AA[1] = a1(k, sqper, H2, T(0.412e+2), T(0.9427e-1), T(0.564e+2), c, W_R, PE, err);
+    T CHI0, WHI0, CHI, WHI;
     chiwhi_pair(k, sqper, H3A, c, CHI0, WHI0, CHI, WHI);
-    const double T1 = 0.19 * CHI / CHI0, T4 = 0.13219 * WHI / WHI0;
+    const T T1 = T(0.19) * CHI / CHI0, T4 = T(0.13219) * WHI / WHI0;
     chiwhi_pair(k, sqper, H3B, c, CHI0, WHI0, CHI, WHI);
-    const double T2 = 0.23e+1 * CHI / CHI0, T5 = 0.13219 * WHI / WHI0;
+    const T T2 = T(0.23e+1) * CHI / CHI0, T5 = T(0.13219) * WHI / WHI0;
     chiwhi_pair(k, sqper, H3C, c, CHI0, WHI0, CHI, WHI);
-    const double T3 = 0.224e+2 * CHI / CHI0, T6 = 0.13219 * WHI / WHI0;
-    const double C1 = T1 + T2 + T3;
-    const double C3 = 0.6e+2 * c.TT0;
-    const double BTA = 2.0 * sqrt(C3) * (sqrt(T1 * T4) + sqrt(T2 * T5) + sqrt(T3 * T6));
+    const T T3 = T(0.224e+2) * CHI / CHI0, T6 = T(0.13219) * WHI / WHI0;
+    const T C1 = T1 + T2 + T3;
+    const T C3 = T(0.6e+2) * c.TT0;
+    const T BTA = T(2) * sqrt(C3) * (sqrt(T1 * T4) + sqrt(T2 * T5) + sqrt(T3 * T6));
     AA[2] = banda(C1, BTA, C3, W_R, PE, err);
-    AA[3] = a1(k, sqper, H4, 3.0, 0.8169e-1, 0.431e2, c, W_R, PE, err);
-    AA[4] = a1(k, sqper, H5, 0.25e+1, 0.11628, 0.32e+2, c, W_R, PE, err);
-    for (int n = 0; n < 5; ++n) AA[n] = AA[n] * 1.0e+2;
+    AA[3] = a1(k, sqper, H4, T(3.0), T(0.8169e-1), T(0.431e2), c, W_R, PE, err);
+    AA[4] = a1(k, sqper, H5, T(0.25e+1), T(0.11628), T(0.32e+2), c, W_R, PE, err);
+    for (int n = 0; n < 5; ++n) AA[n] = AA[n] * T(1.0e+2);
 }
 
 // ACO2 (Rad_gas.f90:224-274): band absorptances of CO2 (1/m)
-__device__ void aco2(const GasConst& k, const double* sqper, const Cell& c, double* AA, int& err) {
-    const double W_R = c.P_RAD * c.YCO2 * c.OPL / c.T_RAD / 8.208e-2 * kWco2;
-    if (W_R <= 0.0) { err |= 4; for (int n = 0; n < 6; ++n) AA[n] = 0.0; return; }
-    const double q = c.P_RAD + c.P_RAD * c.YCO2 * 0.3;
-    double PE = pow(q, 0.7);
-    AA[0] = a1(k, sqper, C1, 0.19e+2, 0.6157e-1, 0.127e2, c, W_R, PE, err);
-    PE = pow(q, 0.8);
-    AA[1] = a1(k, sqper, C23, 0.36, 0.4017e-1, 0.134e+2, c, W_R, PE, err);
-    AA[2] = a1(k, sqper, C23, 0.24, 0.11888, 0.101e+2, c, W_R, PE, err);
-    AA[3] = a1(k, sqper, C4, 0.11e+3, 0.24723, 0.112e+2, c, W_R, PE, err);
-    PE = pow(q, 0.65);
-    AA[4] = a1(k, sqper, C5, 4.0, 0.13341, 23.5, c, W_R, PE, err);
-    AA[5] = a1(k, sqper, C6, 0.66e-1, 0.39305, 0.345e+2, c, W_R, PE, err);
-    for (int n = 0; n < 6; ++n) AA[n] = AA[n] * 1.0e+2;
+template <typename T>
+__device__ void aco2(const GasConst& k, const T* sqper, const Cell<T>& c, T* AA, int& err) {
+    const T W_R = c.P_RAD * c.YCO2 * c.OPL / c.T_RAD / T(8.208e-2) * T(kWco2);
+    if (W_R <= T(0)) { err |= 4; for (int n = 0; n < 6; ++n) AA[n] = T(0); return; }
+    const T q = c.P_RAD + c.P_RAD * c.YCO2 * T(0.3);
+    T PE = pow(q, T(0.7));
+    AA[0] = a1(k, sqper, C1, T(0.19e+2), T(0.6157e-1), T(0.127e2), c, W_R, PE, err);
+    PE = pow(q, T(0.8));
+    AA[1] = a1(k, sqper, C23, T(0.36), T(0.4017e-1), T(0.134e+2), c, W_R, PE, err);
+    AA[2] = a1(k, sqper, C23, T(0.24), T(0.11888), T(0.101e+2), c, W_R, PE, err);
+    AA[3] = a1(k, sqper, C4, T(0.11e+3), T(0.24723), T(0.112e+2), c, W_R, PE, err);
+    PE = pow(q, T(0.65));
+    AA[4] = a1(k, sqper, C5, T(4.0), T(0.13341), T(23.5), c, W_R, PE, err);
+    AA[5] = a1(k, sqper, C6, T(0.66e-1), T(0.39305), T(0.345e+2), c, W_R, PE, err);
+    for (int n = 0; n < 6; ++n) AA[n] = AA[n] * T(1.0e+2);
 }
 
 // RAD_GAS without SOOTA (Rad_gas.f90:23-134): AKLG of every band
-__device__ void rad_gas(const GasConst& k, const double* sqper, const Cell& c, double* AKLG, int& err) {
-    const double EPS1 = 1.0e-4;
-    double WH[5][3], WC[6][3], WNG[11][2];
-    for (int n = 0; n < 5; ++n) WH[n][0] = WH[n][1] = WH[n][2] = 0.0;
-    for (int n = 0; n < 6; ++n) WC[n][0] = WC[n][1] = WC[n][2] = 0.0;
-    for (int n = 0; n < k.nwl; ++n) AKLG[n] = 0.0;
+template <typename T>
+__device__ void rad_gas(const GasConst& k, const T* sqper, const Cell<T>& c, T* AKLG, int& err) {
+    const T EPS1 = T(1.0e-4);
+    T WH[5][3], WC[6][3], WNG[11][2];
+    for (int n = 0; n < 5; ++n) WH[n][0] = WH[n][1] = WH[n][2] = T(0);
+    for (int n = 0; n < 6; ++n) WC[n][0] = WC[n][1] = WC[n][2] = T(0);
+    for (int n = 0; n < k.nwl; ++n) AKLG[n] = T(0);
     if (c.YH2O > EPS1) {
-        WH[1][1] = 1.60e+5; WH[2][1] = 3.76e+5; WH[3][1] = 5.35e+5; WH[4][1] = 7.25e+5;
-        double AA[5];
+        WH[1][1] = T(1.60e+5); WH[2][1] = T(3.76e+5); WH[3][1] = T(5.35e+5); WH[4][1] = T(7.25e+5);
+        T AA[5];
         ah2o(k, sqper, c, AA, err);
-        WH[0][1] = AA[0] / 2;
+        WH[0][1] = AA[0] / T(2);
         WH[0][2] = AA[0];
         for (int N = 1; N < 5; ++N) {
-            const double G0 = AA[N] / 2;
+            const T G0 = AA[N] / T(2);
             WH[N][0] = WH[N][1] - G0;
             WH[N][2] = WH[N][1] + G0;
             if (WH[N - 1][2] > WH[N][0]) WH[N - 1][2] = WH[N][0];
         }
     }
     if (c.YCO2 > EPS1) {
-        WC[0][1] = 6.67e+4; WC[1][1] = 9.60e+4; WC[2][1] = 1.06e+5;
-        WC[3][2] = 2.41e+5; WC[4][1] = 3.66e+5; WC[5][1] = 5.20e+5;
-        double AA[6];
+        WC[0][1] = T(6.67e+4); WC[1][1] = T(9.60e+4); WC[2][1] = T(1.06e+5);
+        WC[3][2] = T(2.41e+5); WC[4][1] = T(3.66e+5); WC[5][1] = T(5.20e+5);
+        T AA[6];
         aco2(k, sqper, c, AA, err);
         for (int N = 0; N < 6; ++N) {
-            const double G0 = AA[N] / 2;
+            const T G0 = AA[N] / T(2);
             if (N == 0 && G0 > WC[0][1]) {
-                WC[0][0] = 0;
+                WC[0][0] = T(0);
                 WC[0][2] = AA[0];
             } else if (N == 3) {
                 WC[N][1] = WC[N][2] - G0;
@@ -286,18 +304,18 @@ __device__ void rad_gas(const GasConst& k, const double* sqper, const Cell& c, d
     for (int N = 0; N < 10; ++N) {
         for (int N2 = N + 1; N2 < 11; ++N2) {
             if (WNG[N][0] < WNG[N2][0]) continue;
-            double t = WNG[N][0]; WNG[N][0] = WNG[N2][0]; WNG[N2][0] = t;
+            T t = WNG[N][0]; WNG[N][0] = WNG[N2][0]; WNG[N2][0] = t;
             t = WNG[N][1]; WNG[N][1] = WNG[N2][1]; WNG[N2][1] = t;
         }
         if (N == 0) continue;
         if (WNG[N - 1][1] > WNG[N][0]) WNG[N - 1][1] = WNG[N][0];
     }
-    double WL2 = 10 / k.wl[0];
+    T WL2 = T(10) / T(k.wl[0]);
     int N0 = 10;
     for (int N = 0; N < k.nwl; ++N) {
-        const double WL1 = N == k.nwl - 1 ? 0 : 1 / k.wl[N];
+        const T WL1 = N == k.nwl - 1 ? T(0) : T(1) / T(k.wl[N]);
         if (WL2 <= WL1 || WNG[10][1] <= WL1) { WL2 = WL1; continue; }
-        double E0 = 0.0;
+        T E0 = T(0);
         for (int N1 = N0; N1 >= 0; --N1) {
             if (WNG[N1][1] <= WL1) { N0 = N1; break; }
             if (WNG[N1][1] >= WL1 && WNG[N1][1] <= WL2) {
@@ -310,12 +328,12 @@ __device__ void rad_gas(const GasConst& k, const double* sqper, const Cell& c, d
                 E0 = E0 + WNG[N1][1] - WNG[N1][0];
             }
         }
-        if (E0 <= 0 || WL2 <= WL1) {
-            AKLG[N] = 0.0;
+        if (E0 <= T(0) || WL2 <= WL1) {
+            AKLG[N] = T(0);
         } else {
             E0 = E0 / (WL2 - WL1);
-            double G0 = 1 - E0;
-            if (G0 <= 1.0e-20) G0 = 1.0e-20;
+            T G0 = T(1) - E0;
+            if (G0 <= T(1.0e-20)) G0 = T(1.0e-20);
             AKLG[N] = -log(G0) / c.OPL;
         }
         WL2 = WL1;
@@ -331,7 +349,7 @@ struct GasArgs {
     double t0, pg0, dnst0;
     GasConst k;
     double *aklg, *akls, *fvs;   // aklg/akls: cell + l*n (cell = I fastest); fvs by loop order
-    const double* sqper;         // sqrt(PER(M,N)), M < kPerRows, N <= 3, at M*4 + N
+    const R* sqper;              // sqrt(PER(M,N)), M < kPerRows, N <= 3, at M*4 + N, in the path's arithmetic
     int* setter;                 // by loop order q = ((I/2-1)*NZ + J/2-1)*LZ + K/2-1: q or -1
     int* blockmax;
     int* err;
@@ -347,42 +365,43 @@ __global__ void __launch_bounds__(128) k_gas_band(GasArgs<R> a) {
         const int id = c % a.MZ, jd = (c / a.MZ) % a.NZ, kd = c / (a.MZ * a.NZ);
         const int I = 2 * (id + 1), J = 2 * (jd + 1), K = 2 * (kd + 1);
         const int q = (id * a.NZ + jd) * a.LZ + kd;
-        double aklg[kRadMaxBands];
-        for (int l = 0; l < a.k.nwl; ++l) aklg[l] = 0.0;
+        R aklg[kRadMaxBands];
+        for (int l = 0; l < a.k.nwl; ++l) aklg[l] = R(0);
         int set = -1;
         double fvs = 0.0;
         const long long o = pidx(a.g, I, J, K);
         const double T_RAD = (double)a.T[o] * a.t0;
         if (a.g.ib[o] <= 0 && T_RAD >= kTgMnGas) {
-            Cell cl;
-            cl.T_RAD = T_RAD;
-            cl.TT0 = sqrt(T_RAD / kT0R);
-            cl.P_RAD = (1.0 + (double)a.P[o]) * a.pg0 / kP0R;
+            Cell<R> cl;
+            cl.T_RAD = R(T_RAD);
+            cl.TT0 = sqrt(R(T_RAD) / R(kT0R));
+            cl.P_RAD = R((1.0 + (double)a.P[o]) * a.pg0 / kP0R);
             double sum = 0.0;
             for (int m = 0; m < 7; ++m) sum = sum + (double)a.gfm[m][o] / wms(m);
             const double wmix = 1.0 / sum;
-            cl.YCO2 = (double)a.gfm[4][o] * wmix / kWco2;
-            cl.YH2O = (double)a.gfm[3][o] * wmix / kWh2o;
+            cl.YCO2 = R((double)a.gfm[4][o] * wmix / kWco2);
+            cl.YH2O = R((double)a.gfm[3][o] * wmix / kWh2o);
             fvs = (double)a.smf[o] * (double)a.DNST[o] * a.dnst0 / kDnstSoot;
             const double dx = a.g.DX[I], dr = a.g.DR[J], dz = a.g.DZ[K];
             double vol = dx * dr * a.g.RS[J] * dz;
             if (a.g.HALF && a.g.ib[o] <= -1) vol = vol * a.g.BVF[-a.g.ib[o] - 1];
             const double sa = ((dx * dr) + (dr * dz) + (dx * dz)) * 2.0;
             if (sa > kSmall16) {
-                cl.OPL = 6.0 * vol / sa;
-                if (cl.OPL > 1.0e-10) {
+                const double opl = 6.0 * vol / sa;
+                cl.OPL = R(opl);
+                if (opl > 1.0e-10) {
                     for (int gs = 0; gs < 2; ++gs)
-                        for (int K = 0; K < 3; ++K) {
-                            cl.U[gs][K] = kHckR * site_v(gs, K) / T_RAD;
-                            cl.eU[gs][K] = exp(-cl.U[gs][K]);
-                            cl.eUh[gs][K] = exp(-0.5 * cl.U[gs][K]);
+                        for (int K3 = 0; K3 < 3; ++K3) {
+                            cl.U[gs][K3] = R(kHckR * site_v(gs, K3)) / cl.T_RAD;
+                            cl.eU[gs][K3] = exp(-cl.U[gs][K3]);
+                            cl.eUh[gs][K3] = exp(R(-0.5) * cl.U[gs][K3]);
                         }
                     rad_gas(a.k, a.sqper, cl, aklg, err);
                     if (fvs >= 1.0e-14) set = q;
                 }
             }
         }
-        for (int l = 0; l < a.k.nwl; ++l) a.aklg[c + (long long)l * n] = aklg[l];
+        for (int l = 0; l < a.k.nwl; ++l) a.aklg[c + (long long)l * n] = (double)aklg[l];
         a.setter[q] = set;
         a.fvs[q] = fvs;
     }
@@ -503,7 +522,8 @@ int launch_gas_band(const GasBuffers& b, const GeoT<double>& g, const R* T, cons
         chiwhi_sums(s, kT0R, a.k.chi0[s], a.k.ynxy0[s]);
     }
     a.aklg = b.aklg; a.akls = b.akls; a.fvs = b.fvs; a.setter = b.setter; a.blockmax = b.blockmax; a.err = b.err;
-    a.sqper = b.sqper;
+    if constexpr (std::is_same<R, double>::value) a.sqper = b.sqper;
+    else a.sqper = b.sqperf;
     const int n = a.MZ * a.NZ * a.LZ;
     const int gb = (n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096;
     k_gas_band<R><<<gb, 128, 0, st>>>(a);

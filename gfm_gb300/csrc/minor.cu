@@ -394,10 +394,12 @@ __global__ void __launch_bounds__(kMsBlock) k_ms_stats(Ctx<R> c, MinorDev<R> m, 
         const double tot = block_sum(sum, sh);
         if (threadIdx.x == 0) s.stats[l] = tot;
     } else {
+        // the exit cells are EXTR's records of kind 3
         double num = 0.0, den = 0.0;
-        const int hx = g.MP / 2, hy = g.NP / 2, hz = g.LP / 2;
-        for (int t = threadIdx.x; t < hx * hy * hz; t += blockDim.x) {
-            const int I = 2 * (t % hx + 1), J = 2 * ((t / hx) % hy + 1), K = 2 * (t / (hx * hy) + 1);
+        for (int t = threadIdx.x; t < c.n_extr_io; t += blockDim.x) {
+            const ExtrRec& e = c.extr_io[t];
+            if (e.kind != 3) continue;
+            const int I = e.I, J = e.J, K = e.K;
             const long long o = pidx(g, I, J, K);
             if (g.ib[o] != 3) continue;
             double G0 = (double)area_c(g, I, J, K, 3);

@@ -1763,6 +1763,10 @@ int gas_band(gfm_handle* h) {
         double* d = nullptr;
         if ((rc = dupload(h, &d, t))) return rc;
         h->gas.sqper = d;
+        std::vector<float> tf(t.begin(), t.end());
+        float* df = nullptr;
+        if ((rc = dupload(h, &df, tf))) return rc;
+        h->gas.sqperf = df;
     }
     if ((rc = ensure_double_coords(h))) return rc;
     const gfm_params& P = h->params;

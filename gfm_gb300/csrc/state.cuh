@@ -196,6 +196,7 @@ struct GasBuffers {
     int *setter, *blockmax;      // the cells that set AKLS, and the prefix maxima
     int* err;                    // bit 1: BANDA argument < 0, bit 2: W_R <= 0 with CO2
     const double* sqper;         // square roots of CHIWHI's integer factors (gas_sqper_fill)
+    const float* sqperf;         //   the same in FP32, for the mixed path
 };
 int gas_scan_blocks(int ncell);
 int gas_sqper_size();

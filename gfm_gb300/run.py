@@ -6,6 +6,10 @@ in tests/golden), starts it (INITSV), runs `warmup` outer iterations and then
 `iters` more, and prints one JSON line with the device time per iteration,
 the line solver's share and the last iteration's residuals.  It is the
 workload the kernel profiles in profiles/ were taken on.
+
+`--minor N` then runs INITSVM (from the major species) and N MSFLOW
+iterations of the minor species, and one emission update on the band model
+(RAD_GAS and SOOTA), and adds their times.
 """
 from __future__ import annotations
 
@@ -38,8 +42,11 @@ def main(argv=None) -> int:
     ap.add_argument("--adi", choices=["redblack", "march"], default="redblack")
     ap.add_argument("--iters", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--minor", type=int, default=0, help="MSFLOW iterations and a band-model emission update after")
     a = ap.parse_args(argv)
     case = build_case(a.case)
+    if a.minor:
+        case.c.params.gas_model = 1
     s = GpuSolver(case, adi_mode=abi.GFM_ADI_REDBLACK if a.adi == "redblack" else abi.GFM_ADI_MARCH,
                   precision=abi.GFM_PREC_MIXED if a.prec == "mixed" else abi.GFM_PREC_FP64)
     s.start()
@@ -49,10 +56,21 @@ def main(argv=None) -> int:
     st, nd = s.gflow(a.iters)
     kt = s.kernel_times()
     prof = s.iteration_profile()
+    out = {"case": a.case, "cells": case.ncells, "prec": a.prec, "adi": a.adi, "iterations": nd,
+           "ms_per_iteration": kt["gflow_ms"] / max(nd, 1), "line_solver_ms_per_iteration": kt["adi_ms"] / max(nd, 1),
+           "kernels_per_iteration": prof["kernels_per_iter"], "res_mass": st["res_mass"]}
+    if a.minor:
+        import time
+        s.initsvm(restart=False)
+        t0 = time.perf_counter()
+        ms = s.msflow(a.minor)
+        out["msflow_ms_per_iteration"] = 1e3 * (time.perf_counter() - t0) / a.minor
+        out["msflow_resid"] = ms["resid_ms"]
+        t0 = time.perf_counter()
+        s.rad_emission()
+        out["band_model_emission_ms"] = 1e3 * (time.perf_counter() - t0)
     s.close()
-    print(json.dumps({"case": a.case, "cells": case.ncells, "prec": a.prec, "adi": a.adi, "iterations": nd,
-                      "ms_per_iteration": kt["gflow_ms"] / max(nd, 1), "line_solver_ms_per_iteration": kt["adi_ms"] / max(nd, 1),
-                      "kernels_per_iteration": prof["kernels_per_iter"], "res_mass": st["res_mass"]}))
+    print(json.dumps(out))
     return 0
 
 
