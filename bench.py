@@ -224,6 +224,12 @@ CEILING_NOTE = ("not the case's schedule: the pressure (ntimesg 4) and p' (ntime
                 "iterations this run needs are the floor that a learned or otherwise better p' start could reach")
 
 
+CONVERGED_FIELD_NOTE = ("with the pressure solves converged the iteration is no longer chaotic: the mixed and FP64 "
+                        "runs of a seed stop at the same iteration, and field_error_vs_fp64 compares their fields "
+                        "there (at res_mass 1e-3, not a converged state: the residual still oscillates as it "
+                        "decays)")
+
+
 def _median(v):
     v = sorted(v)
     return None if not v else (v[len(v) // 2] if len(v) % 2 else 0.5 * (v[len(v) // 2 - 1] + v[len(v) // 2]))
@@ -235,7 +241,9 @@ def time_to_residual_leg(case, adi, args) -> tuple:
     on seeded variants of the 48x24x16 furnace), on four seeded 192x96x64
     furnaces; each run carries the error of every reported field where it
     stopped against the plain FP64 path's run of the same seed (the FP64
-    oracle's arithmetic, checked against it at 1e-9 per iteration)."""
+    oracle's arithmetic, checked against it at 1e-9 per iteration).  The
+    converged-pressure runs (pressure and p' sweeps raised to CEILING_SWEEPS)
+    do the same for both precisions."""
     from gfm_gb300 import Case, abi, configs
     thr = args.ttr or TTR_THRESHOLD
     lp = None
@@ -280,14 +288,23 @@ def time_to_residual_leg(case, adi, args) -> tuple:
         # solve leaves, the most any better p' start can save.
         v = list(configs.REFERENCE_SWEEPS)
         v[3] = v[4] = CEILING_SWEEPS
-        cr = []
+        cr, cr64 = [], []
         for seed in TTR_SEEDS:
             c = Case(configs.large_furnace(seed=seed, ntimesg=tuple(v)))
-            r = time_to_residual(c, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max)
-            r["seed"] = seed
+            f64, fmix = [], []
+            r64 = time_to_residual(c, adi, abi.GFM_PREC_FP64, thr, args.ttr_max, fields_out=f64)
+            r = time_to_residual(c, adi, abi.GFM_PREC_MIXED, thr, args.ttr_max, fields_out=fmix)
+            if r["iterations"] == r64["iterations"]:
+                r["field_error_vs_fp64"] = field_errors(c, fmix[0], f64[0])
+            r["seed"] = r64["seed"] = seed
             cr.append(r)
-        ttr["converged_pressure"] = {"sweeps_p": CEILING_SWEEPS, "sweeps_pprime": CEILING_SWEEPS,
-                                     "note": CEILING_NOTE, "mixed": summary(cr), "runs": cr}
+            cr64.append(r64)
+        cp = {"sweeps_p": CEILING_SWEEPS, "sweeps_pprime": CEILING_SWEEPS, "note": CEILING_NOTE,
+              "field_note": CONVERGED_FIELD_NOTE, "mixed": summary(cr), "fp64": summary(cr64),
+              "runs": cr, "runs_fp64": cr64}
+        if cp["fp64"]["median_seconds"] and cp["mixed"]["median_seconds"]:
+            cp["mixed_vs_fp64_speedup"] = cp["fp64"]["median_seconds"] / cp["mixed"]["median_seconds"]
+        ttr["converged_pressure"] = cp
     if ttr["fp64"]["median_seconds"] and ttr["mixed"]["median_seconds"]:
         ttr["mixed_vs_fp64_speedup"] = ttr["fp64"]["median_seconds"] / ttr["mixed"]["median_seconds"]
     if learned is not None:
