@@ -231,7 +231,7 @@ class GfmCase(C.Structure):
 
 class GfmCaseFiles(C.Structure):
     _fields_ = [("gd", C.c_char_p), ("sbc", C.c_char_p), ("relax", C.c_char_p), ("it", C.c_char_p),
-                ("rg", C.c_char_p), ("kinetic", C.c_char_p)]
+                ("rg", C.c_char_p), ("kinetic", C.c_char_p), ("rr", C.c_char_p)]
 
 
 class GfmCaseOptions(C.Structure):
@@ -279,6 +279,8 @@ SIGNATURES = [
     ("gfm_gpu_wall_setup", C.c_int, [C.c_void_p, C.POINTER(GfmWallSpec)]),
     ("gfm_gpu_wall_totals", C.c_int, [C.c_void_p, C.POINTER(GfmWallTotals)]),
     ("gfm_gpu_wall_get", C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_int]),
+    ("gfm_gpu_wall_vf", C.c_longlong, [C.c_void_p, _dp, C.c_longlong]),
+    ("gfm_gpu_wall_put", C.c_int, [C.c_void_p, C.c_char_p, _dp, C.c_int]),
     ("gfm_minor_read", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmMinor)]),
     ("gfm_minor_write", C.c_int, [C.c_char_p, C.POINTER(GfmGrid), C.POINTER(GfmMinor)]),
     ("gfm_gpu_minor_upload", C.c_int, [C.c_void_p, C.POINTER(GfmMinor)]),

@@ -414,6 +414,7 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
     const bool restart = in.rg_path != nullptr;
     if (restart) {
         int rc = read_restart(in.rg_path, s, P, F, tail, maxgi);
+        if (rc == GFM_OK && in.rr_path) rc = read_rad_restart(in.rr_path, s, P);
         if (rc != GFM_OK) return fail(rc);
         P.maxgi = maxgi;
         if (in.have_it) melt_surf_t(s, in, P, area_melt_surf, true);

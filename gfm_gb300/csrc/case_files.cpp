@@ -613,6 +613,36 @@ int read_restart(const char* path, CaseStore& s, const gfm_params& P, gfm_fields
     return GFM_OK;
 }
 
+// The radiation restart's first four records: QE, QA, QL (MZ,NZ,LZ) and
+// wall_rad_T (MP,NP,LP), K slowest; the rest (the RAD0/QRNF totals and the
+// boundary patches' state) belongs to the wall exchange and is restored on a
+// handle (gfm_gpu_wall_put).  A wall cell centre with wall_rad_T > 0 takes
+// that temperature and its enthalpy (Rad_emis.f90:91-100).
+int read_rad_restart(const char* path, CaseStore& s, const gfm_params& P) {
+    const int mp = s.mp, np = s.np, lp = s.lp;
+    const size_t ncell = (size_t)(mp / 2) * (np / 2) * (lp / 2), N = (size_t)s.n();
+    std::vector<double> ql(ncell), wt(N);
+    RecReader r;
+    r.fp = std::fopen(path, "rb");
+    if (!r.fp) return GFM_E_IO;
+    s.qe.assign(ncell, 0.0);
+    s.qa.assign(ncell, 0.0);
+    const bool ok = r.rec(s.qe.data(), ncell * sizeof(double)) && r.rec(s.qa.data(), ncell * sizeof(double)) &&
+                    r.rec(ql.data(), ncell * sizeof(double)) && r.rec(wt.data(), N * sizeof(double));
+    std::fclose(r.fp);
+    if (!ok) return GFM_E_IO;
+    for (int k = lp; k >= 2; k -= 2)
+        for (int i = 2; i <= mp; i += 2)
+            for (int j = 2; j <= np; j += 2) {
+                const long a = s.at(i, j, k);
+                if (wt[a] > 0.0) {
+                    s.t[a] = wt[a] / P.t0;
+                    prop_t2h(s, P, a);
+                }
+            }
+    return GFM_OK;
+}
+
 }  // namespace host
 }  // namespace gfm
 
@@ -649,6 +679,7 @@ extern "C" int gfm_case_read(const gfm_case_files* files, const gfm_case_options
         in.gas_model = opt->gas_model;
     }
     in.rg_path = files->rg;
+    in.rr_path = files->rr;
     rc = gfm::host::finish_case(S, in, files->kinetic, out, summary);
     if (rc != GFM_OK) return rc;
     if (summary) {

@@ -66,8 +66,9 @@ struct CaseInputs {
     int itn = 0;
     double surf_t = 0.0;
     std::vector<double> tgs;
-    // restart file, NULL for a fresh start
+    // restart file, NULL for a fresh start; radiation restart, NULL for none
     const char* rg_path = nullptr;
+    const char* rr_path = nullptr;
     int interval_rad = 100, initial_gitr = 100;
     // minor species and soot (Var_mod.f90:215, 465-492; Setup.f90:161-185),
     // relaxfactorc.txt's minor-species lines (Setup.f90:476-511)
@@ -103,6 +104,9 @@ int finish_case(CaseStore* S, const CaseInputs& in, const char* kinetic_path, gf
 // Returns a GFM status; on success fills the restart tail values.
 int read_restart(const char* path, CaseStore& s, const gfm_params& P, gfm_fields& F, gfm_restart_tail& tail,
                  int& maxgi);
+// rad_emis_rr (Rad_emis.f90:17-110) after it: QE and QA, and the wall
+// temperatures of the last exchange into T and H at the closed wall cells.
+int read_rad_restart(const char* path, CaseStore& s, const gfm_params& P);
 
 // Property helpers in the reference's order (Prop.f90), on the store's arrays.
 void prop_dnst(CaseStore& s, const gfm_params& P, long a);   // dnst_calc (Prop.f90:187-198)

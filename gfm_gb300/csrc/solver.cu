@@ -129,7 +129,7 @@ struct gfm_handle {
     bool wall_on = false;
     gfm_wall_spec wspec{};
     WallArgs wall{};
-    std::vector<int> wall_typ;
+    std::vector<int> wall_typ, wall_exh;
     double wall_area_total = 0;
     int wall_first = 1, iterw = 0, wall_frac_exits = 0;
     int* d_frac_exit = nullptr;
@@ -1610,10 +1610,10 @@ extern "C" int gfm_gpu_wall_setup(gfm_handle* h, const gfm_wall_spec* spec) {
     a.o_bc = ip[6]; a.o_b = ip[7]; a.sink = ip[8]; h->d_frac_exit = ip[9];
     a.px = dp[0]; a.py = dp[1]; a.pz = dp[2]; a.emis = dp[3]; a.area = dp[4]; a.face_area = dp[5]; a.bT_exit = dp[6];
     if ((rc = dupload(h, &h->d_frac, frac))) return rc;
-    double* work[9];
-    for (int q = 0; q < 9; ++q) if ((rc = dalloc(h, &work[q], nb))) return rc;
+    double* work[10];
+    for (int q = 0; q < 10; ++q) if ((rc = dalloc(h, &work[q], nb))) return rc;
     a.bT = work[0]; a.J = work[1]; a.Jn = work[2]; a.qc = work[3]; a.qeb = work[4]; a.qconv = work[5];
-    a.qamb = work[6]; a.rad = work[7]; a.rel = work[8];
+    a.qamb = work[6]; a.rad = work[7]; a.rel = work[8]; a.vfsum = work[9];
     if ((rc = dalloc(h, &a.part, (long long)kWallSlots * kWallBlocks))) return rc;
     // the view factors: FP64 on the FP64 path, FP32 on the mixed one
     const size_t vf_bytes = (size_t)nb * nb * (h->prec == GFM_PREC_FP64 ? 8 : 4);
@@ -1634,6 +1634,7 @@ extern "C" int gfm_gpu_wall_setup(gfm_handle* h, const gfm_wall_spec* spec) {
     h->wall = a;
     h->wspec = *spec;
     h->wall_typ = typ;
+    h->wall_exh = exh;
     h->wall_on = true;
     return GFM_OK;
 }
@@ -1660,12 +1661,74 @@ extern "C" int gfm_gpu_wall_get(gfm_handle* h, const char* name, double* out, in
         for (int i = 0; i < a.nb; ++i) out[i] = h->wall_typ[i] == 4 ? qc[i] + qv[i] + rad[i] - J[i] : 0.0;
         return a.nb;
     }
+    // the patch list and the closed cell behind each patch (the face's
+    // neighbour on the side its direction points away from)
+    const std::vector<int16_t>* list = s == "b_typ" ? &h->bp_typ : s == "b_i" ? &h->bp_i : s == "b_j" ? &h->bp_j
+                                     : s == "b_k" ? &h->bp_k : s == "b_orient" ? &h->bp_ori
+                                     : s == "b_direct" ? &h->bp_dir : nullptr;
+    if (list) {
+        for (int n = 0; n < a.nb; ++n) out[n] = (*list)[n];
+        return a.nb;
+    }
+    if (s == "bc_i" || s == "bc_j" || s == "bc_k") {
+        const int axis = s == "bc_i" ? 1 : s == "bc_j" ? 2 : 3;
+        const std::vector<int16_t>& pos = axis == 1 ? h->bp_i : axis == 2 ? h->bp_j : h->bp_k;
+        for (int n = 0; n < a.nb; ++n)
+            out[n] = pos[n] + (h->bp_ori[n] == axis ? (h->bp_dir[n] == 0 ? -1 : 1) : 0);
+        return a.nb;
+    }
+    if (s == "b_exh") {
+        for (int n = 0; n < a.nb; ++n) out[n] = h->wall_exh[n];
+        return a.nb;
+    }
     const double* src = s == "b_t" ? a.bT : s == "radiosity" ? a.J : s == "q_amb" ? a.qamb : s == "q_conv" ? a.qconv
                       : s == "qc" ? a.qc : s == "qeb" ? a.qeb : s == "emis" ? a.emis : s == "b_face_area" ? a.face_area
-                      : s == "patch_area" ? a.area : s == "rad" ? a.rad : nullptr;
+                      : s == "patch_area" ? a.area : s == "rad" ? a.rad : s == "vf_sum" ? a.vfsum : nullptr;
     if (!src) return GFM_E_ARG;
     CK(cudaMemcpy(out, src, (size_t)a.nb * sizeof(double), cudaMemcpyDeviceToHost));
     return a.nb;
+}
+
+extern "C" long long gfm_gpu_wall_vf(gfm_handle* h, double* out, long long cap) {
+    if (!h || !out || !h->wall_on) return GFM_E_ARG;
+    const WallArgs& a = h->wall;
+    const long long nn = (long long)a.nb * a.nb;
+    if (cap < nn) return GFM_E_ARG;
+    if (a.vf64) {
+        CK(cudaMemcpy(out, a.vf64, (size_t)nn * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> row(a.nb);
+        for (int n = 0; n < a.nb; ++n) {
+            CK(cudaMemcpy(row.data(), a.vf32 + (size_t)n * a.nb, (size_t)a.nb * sizeof(float), cudaMemcpyDeviceToHost));
+            for (int m = 0; m < a.nb; ++m) out[(size_t)n * a.nb + m] = row[m];
+        }
+    }
+    return nn;
+}
+
+extern "C" int gfm_gpu_wall_put(gfm_handle* h, const char* name, const double* src, int n) {
+    if (!h || !name || !src || !h->wall_on) return GFM_E_ARG;
+    const WallArgs& a = h->wall;
+    const std::string s(name);
+    if (s == "radiosity" || s == "b_t") {
+        if (n != a.nb) return GFM_E_ARG;
+        for (int q = 0; q < n; ++q) if (!std::isfinite(src[q])) return GFM_E_NAN;
+        CK(cudaMemcpy(s == "b_t" ? a.bT : a.J, src, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+        if (s == "b_t") {
+            // the given wall temperatures stand at the next exchange, and the
+            // gas solve's wall sink reads them too
+            h->wall_first = 0;
+            launch_wall_to_sink(a, h->d_patches, h->stream);
+            CK(cudaStreamSynchronize(h->stream));
+        }
+        return GFM_OK;
+    }
+    if (n != 1 || !std::isfinite(src[0])) return GFM_E_ARG;
+    if (s == "iterw") h->iterw = (int)src[0];
+    else if (s == "q_melt") h->q_melt = src[0];
+    else if (s == "avg_wall_T") h->avg_wall_T = src[0];
+    else return GFM_E_ARG;
+    return GFM_OK;
 }
 
 namespace {

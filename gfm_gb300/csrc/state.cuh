@@ -130,6 +130,7 @@ struct WallArgs {
     const double *px, *py, *pz;    // X(b_i), R(b_j), Z(b_k)
     const double *emis, *area, *face_area, *bT_exit;   // bT_exit: exits' temperature at the first exchange
     double *bT, *J, *Jn, *qc, *qeb, *qconv, *qamb, *rad, *rel;
+    double* vfsum;                 // row sums of the view factors before normalisation
     double* part;                  // kWallSlots x kWallBlocks partial sums
     double sig, radi_min, t0, u_a0, t_a, t_mnk;
 };

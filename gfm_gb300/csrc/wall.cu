@@ -55,7 +55,10 @@ __global__ void __launch_bounds__(256) k_wall_vf(WallArgs a, V* vf) {
         double part = 0.0;
         for (int m = threadIdx.x; m < nb; m += blockDim.x) part += vfac(m);
         const double sum = block_sum(part, sh);
-        if (threadIdx.x == 0) s_sum = sum;
+        if (threadIdx.x == 0) {
+            s_sum = sum;
+            a.vfsum[n] = sum;
+        }
         __syncthreads();
         const double vs = s_sum;
         V* row = vf + (size_t)n * nb;

@@ -129,14 +129,18 @@ class Case:
                    sigma_eps: float = 1.0, wall_sink: bool = False, t_wall_k: float = 1700.0,
                    rad_emission: bool = False, kappa=None, maxgi: int = 0,
                    adi_mode: int = abi.GFM_ADI_MARCH, precision: int = abi.GFM_PREC_FP64,
-                   gas_model: bool = False, lib: C.CDLL | None = None) -> "Case":
+                   gas_model: bool = False, rad_restart=None, lib: C.CDLL | None = None) -> "Case":
         """The start-up the Fortran host does from a case directory: reads
         gd<runum>c.dat, sbc<runum>c.dat, it<runum>t.dat (when present),
         relaxfactorc.txt (``relax``, default: in the case directory) and the
         kinetics table, and with ``restart`` the restart file rg<runum>c.d
         (A0main.f90:158-190).  ``summary`` holds what GRID3/SBC derived.
         ``gas_model`` takes the absorption coefficients from RAD_GAS and
-        SOOTA on the minor species instead of ``kappa``."""
+        SOOTA on the minor species instead of ``kappa``.  ``rad_restart``
+        (with ``restart``): the radiation restart rr<runum>c.d to read after
+        it, True for the one in the case directory or a path (rad_emis_rr,
+        Rad_emis.f90:17-110; the wall state it holds goes to a handle with
+        ``radrestart.restore``)."""
         import pathlib
         d = pathlib.Path(case_dir)
         it = d / f"it{runum}t.dat"
@@ -146,7 +150,12 @@ class Case:
             "it": it if it.exists() else None,
             "rg": d / f"rg{runum}c.d" if restart else None,
             "kinetic": pathlib.Path(kinetic) if kinetic else abi.KINETIC_PATH,
+            "rr": None,
         }
+        if rad_restart is not None and rad_restart is not False:
+            if not restart:
+                raise ValueError("a radiation restart is read after the gas restart (restart=True)")
+            paths["rr"] = d / f"rr{runum}c.d" if rad_restart is True else pathlib.Path(rad_restart)
         self = cls(None, lib)
         self.name = f"case{runum}"
         self._paths = {k: (str(v).encode() if v is not None else None) for k, v in paths.items()}
@@ -371,6 +380,21 @@ class GpuSolver:
         if n != out.size:
             self._check(n if n < 0 else abi.GFM_E_ARG)
         return out
+
+    def wall_vf(self) -> np.ndarray:
+        """The normalised view factors, vf[n, m] from near patch n to far patch m."""
+        nb = self.case.grid.b_cnt
+        out = np.zeros((nb, nb))
+        n = self.lib.gfm_gpu_wall_vf(self.h, abi.dptr(out), out.size)
+        if n != out.size:
+            self._check(n if n < 0 else abi.GFM_E_ARG)
+        return out
+
+    def wall_put(self, name: str, values) -> None:
+        """Restores "radiosity" or "b_t" (per patch), or "iterw", "q_melt",
+        "avg_wall_T" (one value) of the wall exchange."""
+        v = np.ascontiguousarray(np.atleast_1d(values), dtype=np.float64)
+        self._check(self.lib.gfm_gpu_wall_put(self.h, name.encode(), abi.dptr(v), v.size))
 
     def adlbl3(self, xt, ap, as6, bs, ib, ie, jb, je, kb, ke, nim) -> np.ndarray:
         x = np.ascontiguousarray(xt, dtype=np.float64).copy()

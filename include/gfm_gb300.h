@@ -282,6 +282,11 @@ typedef struct gfm_case_files {
     const char *rg;       /* rg####c.d restart (Initsv.f90:225-316); NULL: fresh
                              start by gen_initial_guess (Initsv.f90:97-162)      */
     const char *kinetic;  /* Kinetic.d (Setup.f90:858-888)                       */
+    const char *rr;       /* rr####c.d radiation restart (rad_emis_rr,
+                             Rad_emis.f90:17-110), read after rg: QE, QA and
+                             the wall temperatures of the last exchange
+                             (wall_rad_T into T and H at the closed wall
+                             cells); NULL: QE and QA start from zero         */
 } gfm_case_files;
 
 /* Choices the input files do not carry. */
@@ -448,11 +453,21 @@ int  gfm_gpu_rad_transfer(gfm_handle *h, gfm_rad_totals *out);
  * results; gfm_gpu_wall_get copies one per-patch array ("b_t", "radiosity",
  * "q_amb", "q_conv", "qc", "qeb", "emis", "b_face_area", "patch_area", "rad" the
  * radiation from the boundaries, "qrs" the melt-surface heat flux of the melt
- * patches, Qwall.f90:1166) and
- * returns the patch count. */
+ * patches, Qwall.f90:1166; the patch list "b_typ", "b_i", "b_j", "b_k",
+ * "b_orient", "b_direct", the closed cell "bc_i", "bc_j", "bc_k", the exhaust
+ * "b_exh" and "vf_sum", the view factors' row sums before normalisation,
+ * Qwall.f90:562-666) and returns the patch count.  gfm_gpu_wall_vf copies the
+ * normalised view factors, row n (the near patch) at out[n*b_cnt .. ], and
+ * returns b_cnt*b_cnt (cap: elements of out).
+ * gfm_gpu_wall_put restores the state the radiation restart holds
+ * (rad_emis_rr, Rad_emis.f90:17-88): "radiosity" and "b_t" (n = b_cnt; the
+ * next exchange then keeps the given wall temperatures, as after an earlier
+ * exchange), and the scalars "iterw", "q_melt" and "avg_wall_T" (n = 1). */
 int  gfm_gpu_wall_setup(gfm_handle *h, const gfm_wall_spec *spec);
 int  gfm_gpu_wall_totals(gfm_handle *h, gfm_wall_totals *out);
 int  gfm_gpu_wall_get(gfm_handle *h, const char *name, double *out, int cap);
+long long gfm_gpu_wall_vf(gfm_handle *h, double *out, long long cap);
+int  gfm_gpu_wall_put(gfm_handle *h, const char *name, const double *src, int n);
 /* Minor species and soot on the device (ms=1 of the reference).
  * gfm_gpu_minor_upload / _download move the MSFLOW state.  gfm_gpu_initsvm is
  * INITSVM (Initsv.f90:329-378): restart = 0 starts from the major species

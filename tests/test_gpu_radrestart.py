@@ -1,0 +1,97 @@
+"""A restart through the radiation restart on the GPU: a run of TC21 case
+0041 (band model, wall exchange) writes rg and rr after a radiation call; a
+new handle started from them, with the wall state restored, gives the next
+radiation call the continuing run gives (Initsv.f90:312, Rad_emis.f90:17-110)."""
+import numpy as np
+import pytest
+
+from gfm_gb300 import Case, GpuSolver, abi, radrestart
+
+from .test_oracle_gas import converged, converged_dir
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_restart_from_rr_continues_the_run(tmp_path):
+    case, minor = converged("0041", tmp_path, wall_sink=True)
+    d = converged_dir("0041", tmp_path)
+    a = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    a.start()
+    a.minor_upload(minor)
+    a.wall_setup()
+    rr = radrestart.collect(a, a.rad_transfer(), a.wall_totals())
+    assert rr["b_cnt"] == case.grid.b_cnt and rr["iwall_count"] > 0 and rr["imelt_count"] > 0
+    assert np.allclose(rr["vf"].sum(axis=1)[rr["vf_sum"] > 0], 1.0, atol=1e-12)
+    case.write_restart(d / "rg0041c.d", a.download())
+    radrestart.write(d / "rr0041c.d", rr)
+    back = radrestart.read(d / "rr0041c.d", case.mp, case.np, case.lp)
+    assert np.array_equal(back["radiosity"], rr["radiosity"]) and np.array_equal(back["vf"], rr["vf"])
+    rad2 = a.rad_transfer()
+    wall2 = a.wall_totals()
+
+    c2 = Case.from_files(d, "0041", restart=True, gas_model=True, wall_sink=True, rad_restart=True)
+    f2 = c2.initial_fields()
+    assert np.array_equal(f2.arrays["qa"], rr["qa"]) and np.array_equal(f2.arrays["qe"], rr["qe"])
+    b = GpuSolver(c2, precision=abi.GFM_PREC_FP64)
+    b.start()
+    b.minor_upload(minor)
+    b.wall_setup()
+    radrestart.restore(b, back)
+    assert np.array_equal(b.wall_array("b_t"), rr["b_T"])
+    rad2b = b.rad_transfer()
+    wall2b = b.wall_totals()
+    for k in rad2:
+        assert rad2b[k] == pytest.approx(rad2[k], rel=1e-9, abs=1e-12), k
+    # A restart is not the continuing run to the last bit, in the reference
+    # either: the case read applies melt_surf_T again (relaxed against the
+    # stored T_surf_prev) and INITSV interpolates the faces the wall exchange
+    # had set.  The next exchange agrees to about 3e-7; the wall state itself
+    # is restored exactly (the next test).
+    for k in ("avg_wall_T", "q_melt", "q_wall_loss", "q_incident_total", "qconv_total", "q_rad_inlet",
+              "q_rad_outlet"):
+        assert wall2b[k] == pytest.approx(wall2[k], rel=1e-5), k
+    for n in ("b_t", "radiosity", "qrs"):
+        assert _rel(b.wall_array(n), a.wall_array(n)) < 1e-5, n
+    assert _rel(b.download().arrays["qa"], a.download().arrays["qa"]) < 1e-9
+
+
+def test_restored_wall_state_continues_the_exchange_exactly(tmp_path):
+    """The wall state alone: a handle given the continuing run's fields and
+    the file's wall state makes the continuing run's next exchange."""
+    case, minor = converged("0041", tmp_path, wall_sink=True)
+    a = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    a.start()
+    a.minor_upload(minor)
+    a.wall_setup()
+    rr = radrestart.collect(a, a.rad_transfer(), a.wall_totals())
+    fa = a.download()
+    rad2, wall2 = a.rad_transfer(), a.wall_totals()
+    b = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    b.upload(fa)
+    b.minor_upload(minor)
+    b.wall_setup()
+    radrestart.restore(b, rr)
+    rad2b, wall2b = b.rad_transfer(), b.wall_totals()
+    for k in rad2:
+        assert rad2b[k] == pytest.approx(rad2[k], rel=1e-12, abs=1e-12), k
+    for k in wall2:
+        assert wall2b[k] == pytest.approx(wall2[k], rel=1e-12, abs=1e-12), k
+    for n in ("b_t", "radiosity", "qrs"):
+        assert _rel(b.wall_array(n), a.wall_array(n)) < 1e-12, n
+
+
+def test_restore_refuses_another_patch_list(tmp_path):
+    case, minor = converged("0041", tmp_path, wall_sink=True)
+    a = GpuSolver(case, precision=abi.GFM_PREC_FP64)
+    a.start()
+    a.minor_upload(minor)
+    a.wall_setup()
+    rr = radrestart.collect(a, a.rad_transfer(), a.wall_totals())
+    rr["b_i"] = rr["b_i"].copy()
+    rr["b_i"][0] += 2
+    with pytest.raises(radrestart.RadRestartError):
+        radrestart.restore(a, rr)
