@@ -49,11 +49,14 @@ def test_restart_from_rr_continues_the_run(tmp_path):
     # A restart is not the continuing run to the last bit, in the reference
     # either: the case read applies melt_surf_T again (relaxed against the
     # stored T_surf_prev) and INITSV interpolates the faces the wall exchange
-    # had set.  The next exchange agrees to about 3e-7; the wall state itself
-    # is restored exactly (the next test).
+    # had set.  The next exchange agrees to about 3e-7; the net radiation
+    # through the inlets and exits, a difference of large terms, is held to
+    # 1e-6 of the incident total.  The wall state itself is restored exactly
+    # (the next test).
+    scale = 1e-6 * wall2["q_incident_total"]
     for k in ("avg_wall_T", "q_melt", "q_wall_loss", "q_incident_total", "qconv_total", "q_rad_inlet",
               "q_rad_outlet"):
-        assert wall2b[k] == pytest.approx(wall2[k], rel=1e-5), k
+        assert wall2b[k] == pytest.approx(wall2[k], rel=1e-5, abs=scale), k
     for n in ("b_t", "radiosity", "qrs"):
         assert _rel(b.wall_array(n), a.wall_array(n)) < 1e-5, n
     assert _rel(b.download().arrays["qa"], a.download().arrays["qa"]) < 1e-9
