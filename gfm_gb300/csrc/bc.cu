@@ -438,6 +438,53 @@ __global__ void k_pref(Ctx<R> c, int I1, int J1, int K1, int I2, int J2, int K2,
 // (zero where the cell does not emit), then T=(T*T0)/T0 as the reference's
 // whole-array round trip does.
 // ---------------------------------------------------------------------------
+// 1/n and its powers for the terms of RIF(3,0,X), n = 1..1000, formed once on
+// the host with the products the device formed per term before (the same
+// bits: q = 1/n, then q*q, q2*q, q3*q).  Every thread of
+// a warp reads the same n at once, a broadcast from constant memory, so a
+// term costs no division on the narrow FP64 pipe.
+constexpr int kRifTerms = 1000;
+__constant__ double c_rif_q[4 * kRifTerms];
+
+int prepare_rif_table() {
+    static double tab[4 * kRifTerms];
+    for (int n = 1; n <= kRifTerms; ++n) {
+        const double q = 1.0 / (double)n;
+        const double q2 = q * q, q3 = q2 * q, q4 = q3 * q;
+        double* t = tab + 4 * (n - 1);
+        t[0] = q; t[1] = q2; t[2] = q3; t[3] = q4;
+    }
+    return cudaMemcpyToSymbol(c_rif_q, tab, sizeof tab) == cudaSuccess ? GFM_OK : GFM_E_CUDA;
+}
+
+// RIF(3,0,X) of rif3 (physics.h) with exp(-n*x) formed as the n-th power of
+// exp(-x) and the powers of 1/n from the table: one exponential per call and
+// no division per term in place of one exponential and four divisions per
+// term (the same sum to the last bits).
+__device__ __forceinline__ double rif3_tab(double x) {
+    const double pi = 3.141592653589793;
+    if (x > 1.0e16) return 0.0;
+    if (x == 0.0) return 1.0;
+    const double ex = exp(-x);
+    const double x2 = x * x, x3 = x2 * x;
+    double e = ex;
+    double r = 0.0;
+    for (int n = 1; n <= kRifTerms; ++n) {
+        const double* q = c_rif_q + 4 * (n - 1);
+        double g0 = 0.0;
+        g0 = g0 + x3 * q[0];
+        g0 = g0 + 3.0 * x2 * q[1];
+        g0 = g0 + 6.0 * x * q[2];
+        g0 = g0 + 6.0 * q[3];
+        g0 = g0 * e;
+        r = r + g0;
+        if (fabs(g0) <= 1.0e-16) break;
+        e = e * ex;
+    }
+    r = r * 1.5e1 / (pi * pi * pi * pi);
+    return r > 1.0 ? 1.0 : r;
+}
+
 template <typename R>
 __global__ void k_rad_emission(Ctx<R> c, const double* __restrict__ gas_aklg, const double* __restrict__ gas_akls) {
     const GeoT<R>& g = c.g;
@@ -463,7 +510,7 @@ __global__ void k_rad_emission(Ctx<R> c, const double* __restrict__ gas_aklg, co
                 double deb[16], eb0 = 0.0;
                 for (int l = 1; l <= c.nwl - 1; ++l) {
                     double x1 = (c.p.hck / c.p.ri / c.wl[l - 1]) / T_rad;
-                    double eb1 = rif3_pow(x1);
+                    double eb1 = rif3_tab(x1);
                     deb[l - 1] = eb1 - eb0;
                     if (deb[l - 1] <= 1.0e-3) deb[l - 1] = 0.0; else eb0 = eb1;
                 }

@@ -273,35 +273,6 @@ GFM_HD double rif3(double x) {
     return r > 1.0 ? 1.0 : r;
 }
 
-// RIF(3,0,X) with exp(-n*x) formed as the n-th power of exp(-x) and the
-// powers of 1/n from one division: one exponential per call and one division
-// per term in place of one exponential and four divisions per term (the same
-// sum to the last bits); the emission-only source uses it.
-GFM_HD double rif3_pow(double x) {
-    const double pi = 3.141592653589793;
-    if (x > 1.0e16) return 0.0;
-    if (x == 0.0) return 1.0;
-    const double ex = exp(-x);
-    const double x2 = x * x, x3 = x2 * x;
-    double e = ex;
-    double r = 0.0;
-    for (int n = 1; n <= 1000; ++n) {
-        const double q = 1.0 / (double)n;
-        const double q2 = q * q, q3 = q2 * q, q4 = q3 * q;
-        double g0 = 0.0;
-        g0 = g0 + x3 * q;
-        g0 = g0 + 3.0 * x2 * q2;
-        g0 = g0 + 6.0 * x * q3;
-        g0 = g0 + 6.0 * q4;
-        g0 = g0 * e;
-        r = r + g0;
-        if (fabs(g0) <= 1.0e-16) break;
-        e = e * ex;
-    }
-    r = r * 1.5e1 / (pi * pi * pi * pi);
-    return r > 1.0 ? 1.0 : r;
-}
-
 // Linear table lookup ZY1 (Source.f90:814-831).
 GFM_HD double zy1(const double* x, const double* y, double x1, int n) {
     if (x1 < x[0]) return y[0] * x1 / x[0];

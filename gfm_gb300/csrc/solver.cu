@@ -896,6 +896,7 @@ int create_impl(const gfm_grid* gr, const gfm_params* prm, gfm_handle** out) {
     cudaError_t ce = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { h->err = cudaGetErrorString(ce); return GFM_E_CUDA; }
     if (prepare_line_solver() != GFM_OK) { h->err = "cannot raise the line solver's shared-memory limit"; return GFM_E_CUDA; }
+    if (prepare_rif_table() != GFM_OK) { h->err = "cannot load the emission update's RIF3 table"; return GFM_E_CUDA; }
     {
         const char* tn = std::getenv("GFM_RB_TUNE");
         h->tune = !(tn && tn[0] == '0');

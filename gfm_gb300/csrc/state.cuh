@@ -294,6 +294,7 @@ int prepare_rbp();
 template <typename R> int launch_adlbl3_scr(const GeoT<R>& g, const Sys<R>* sys, const AdiScratch<R>* scr, int nsys,
                                             int mode, cudaStream_t s, int rb_flags);
 int prepare_line_solver();   // once per process, before any stream capture
+int prepare_rif_table();     // the RIF3 term table of the emission update, likewise
 // deterministic finish of block partials: op 0 sum, 1 max, 2 residual
 // (sum/NCELLS floored at 1e-16, NaN -> 1e-16), 3 sum/NCELLS
 struct FinishSpec {
