@@ -136,3 +136,11 @@ def test_case_restart_takes_qe_qa_and_wall_temperatures(tmp_path):
     assert np.array_equal(f2.arrays["gf"][:, mask], f0.arrays["gf"][:, mask])
     with pytest.raises(ValueError):
         Case.from_files(d, "0041", restart=False, rad_restart=True)
+    # a named file that is missing or too short is an error, as rad_emis_rr's
+    # read errors stop the reference ("unable to read radiation restart file")
+    from gfm_gb300.solver import GfmError
+    with pytest.raises(GfmError):
+        Case.from_files(d, "0041", restart=True, rad_restart=d / "rr9999c.d")
+    (d / "short.d").write_bytes((d / "rr0041c.d").read_bytes()[:1000])
+    with pytest.raises(GfmError):
+        Case.from_files(d, "0041", restart=True, rad_restart=d / "short.d")
