@@ -4,6 +4,7 @@
 // sequence (Gflow.f90:6-408) issued on one CUDA stream per handle.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <array>
 #include <map>
 #include <mutex>
@@ -1698,10 +1699,13 @@ extern "C" long long gfm_gpu_wall_vf(gfm_handle* h, double* out, long long cap) 
     if (a.vf64) {
         CK(cudaMemcpy(out, a.vf64, (size_t)nn * sizeof(double), cudaMemcpyDeviceToHost));
     } else {
-        std::vector<float> row(a.nb);
-        for (int n = 0; n < a.nb; ++n) {
-            CK(cudaMemcpy(row.data(), a.vf32 + (size_t)n * a.nb, (size_t)a.nb * sizeof(float), cudaMemcpyDeviceToHost));
-            for (int m = 0; m < a.nb; ++m) out[(size_t)n * a.nb + m] = row[m];
+        // FP32 on the mixed path: whole rows at a time, about 64 MB a copy
+        const size_t rows = std::max<size_t>(1, ((size_t)64 << 20) / ((size_t)a.nb * sizeof(float)));
+        std::vector<float> buf(rows * (size_t)a.nb);
+        for (size_t n0 = 0; n0 < (size_t)a.nb; n0 += rows) {
+            const size_t cnt = std::min(rows, (size_t)a.nb - n0) * (size_t)a.nb;
+            CK(cudaMemcpy(buf.data(), a.vf32 + n0 * a.nb, cnt * sizeof(float), cudaMemcpyDeviceToHost));
+            for (size_t q = 0; q < cnt; ++q) out[n0 * a.nb + q] = buf[q];
         }
     }
     return nn;

@@ -99,3 +99,18 @@ def test_restore_refuses_another_patch_list(tmp_path):
     rr["b_i"][0] += 2
     with pytest.raises(radrestart.RadRestartError):
         radrestart.restore(a, rr)
+
+
+def test_view_factors_of_the_mixed_path(tmp_path):
+    """The mixed path keeps the view factors in FP32; gfm_gpu_wall_vf hands
+    them out as doubles, row by row as the FP64 path does."""
+    case, _ = converged("0041", tmp_path, wall_sink=True)
+    out = {}
+    for prec in (abi.GFM_PREC_FP64, abi.GFM_PREC_MIXED):
+        g = GpuSolver(case, precision=prec)
+        g.start()
+        g.wall_setup()
+        out[prec] = (g.wall_vf(), g.wall_array("vf_sum"))
+    (v64, s64), (v32, s32) = out[abi.GFM_PREC_FP64], out[abi.GFM_PREC_MIXED]
+    assert np.array_equal(s32, s64)
+    assert np.array_equal(v32, v64.astype(np.float32).astype(np.float64))
