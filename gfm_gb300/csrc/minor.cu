@@ -66,7 +66,7 @@ __device__ __forceinline__ double rate45(const double* G, double gfm6, double TM
         RR2 = 0;
     }
     if (G[1] > 1.0e-20 && G[5] > 1.0e-20) {
-        const double R1 = pow(G[5], 1.0) * pow(G[1], 0.5);
+        const double R1 = G[5] * sqrt(G[1]);   // GFM6**ODR(5,1) * GFM2**ODR(5,2), orders 1 and 0.5
         RR3 = 9.33e14 * R1 * exp(-68899.0 / TMP) * pow(TMP, -0.5);
         RR3 = RR3 * VOL;
     } else {
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kMsBlock) k_ms_rates(Ctx<R> c, MinorDev<R> m, 
         // reaction 3: CO2 -> CO + 0.5 O2
         double RR3;
         if (G[4] > 1.0e-20) {
-            const double RR1 = pow(G[4], 1.0);
+            const double RR1 = G[4];   // GFM5**ODR(3,1), order 1
             RR3 = 2.24e14 * RR1 * exp(-62281.0 / TMP) * VOL;
             const double FXMS5 = spin(c, m, as, o, I, J, K, 4);
             RR3 = RR3 < FXMS5 ? RR3 : FXMS5;

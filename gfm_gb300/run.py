@@ -64,7 +64,9 @@ def main(argv=None) -> int:
         s.initsvm(restart=False)
         t0 = time.perf_counter()
         ms = s.msflow(a.minor)
-        out["msflow_ms_per_iteration"] = 1e3 * (time.perf_counter() - t0) / a.minor
+        # MSFLOW stops early once every residual is below BMCON
+        out["msflow_iterations"] = ms["iterations"]
+        out["msflow_ms_per_iteration"] = 1e3 * (time.perf_counter() - t0) / max(ms["iterations"], 1)
         out["msflow_resid"] = ms["resid_ms"]
         t0 = time.perf_counter()
         s.rad_emission()
